@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Benchmark: path samples/s of the plain megakernel on the SDF-fractal scene
+(mandelbulb over a ground plane under a 5800 K sky dome, 1024x1024, 64 spp,
+max depth 6 — the reference-expressible form of the headline config).
+
+One step = one full render of the workload: 1024*1024*64 = 67.1 M camera
+paths (4 hero wavelengths each) in ceil(64/spf) dispatches, inputs resident on
+the device.  `e2e` repeats the step through the reference-facing C ABI
+(pt_render_offscreen) from host buffers: scene packing and upload, the
+dispatches, and the read-back of the 16 MiB accumulator each step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun each rank renders its own replica (distinct sample indices,
+no exchange): weak scaling.  --impl reference times the CPU restatement of
+the reference shader (the reference itself is Vulkan-only) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SCENE = os.path.join(ROOT, "pathtracer_gb300", "scenes", "mandelbulb_plane.json")
+WORKLOAD = "mandelbulb_plane_1024x1024_64spp_depth6"
+METRIC = "path_samples_per_s"
+UNIT = "path samples/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--res", type=int, default=1024)
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--spf", type=int, default=64, help="samples per dispatch")
+    ap.add_argument("--depth", type=int, default=6)
+    ap.add_argument("--cpu-rows", type=int, default=32, help="rows in the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_baseline(args, W, H, spf_total, nthreads):
+    """The CPU restatement (oracle, OpenMP) on a stratified sample of rows."""
+    from oracle import compare
+    from pathtracer_gb300 import Scene, cie_analytic
+
+    scene = Scene.load(SCENE)
+    cie = cie_analytic()
+    ubo = scene.pack_ubo(cie)
+    plugins = compare.plugins_for(scene)
+    push = scene.push_constants(W, H, spf_total, spf_total, spf_total, args.depth)
+    rows = max(1, min(args.cpu_rows, H))
+    stride = H // rows
+    acc = np.zeros((H, W, 4), np.float32)
+    t0 = time.perf_counter()
+    for r in range(rows):
+        y = r * stride + stride // 2
+        compare.run_oracle(ubo, push, plugins, accum=acc, rect=(0, y, W, y + 1), nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    samples = rows * W * spf_total
+    return samples / dt, samples, dt, rows
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from oracle import oracle as _o
+
+    _o.build()
+    W = H = args.res
+    nthreads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, samples, dt, rows = cpu_baseline(args, W, H, args.spp, nthreads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    sample = f"{rows} evenly spaced rows of {W}x{H} at {args.spp} spp ({samples} paths per step)"
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * samples / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "resolution": [W, H], "spp": args.spp, "max_depth": args.depth},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+        return rc
+
+    import torch
+
+    from pathtracer_gb300 import Context, Scene, build, cie_analytic, native, render_offscreen
+
+    build.build()
+    torch.cuda.set_device(local)
+    W = H = args.res
+    spf = min(args.spf, args.spp)
+    ndisp = (args.spp + spf - 1) // spf
+    samples_per_step = W * H * spf * ndisp
+    scene = Scene.load(SCENE)
+    cie = cie_analytic()
+    ctx = Context(local)
+    ctx.bind(scene, cie)
+    ctx.resize_accum(W, H)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+
+    # Distinct sample indices per rank and per step (replicas, no exchange).
+    base = rank * (args.warmup + args.steps + 1) * ndisp * spf
+
+    def one_step(step_idx):
+        frame = base + step_idx * ndisp * spf
+        cur = 0
+        for _ in range(ndisp):
+            frame += spf
+            cur += spf
+            ctx.dispatch(scene.push_constants(W, H, frame, cur, spf, args.depth))
+
+    for i in range(args.warmup):
+        one_step(i)
+    ctx.wait()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    times = []
+    with ClockSampler(local) as clk:
+        t_wall0 = time.perf_counter()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            one_step(args.warmup + i)
+            e1.record(stream)
+            times.append((e0, e1))
+        ctx.wait()
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    ms = [a.elapsed_time(b) for a, b in times]
+    ms_step = sum(ms) / len(ms)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = samples_per_step * world / (ms_step / 1000.0)
+
+    # End to end through the C ABI with host buffers.
+    e2e_secs = []
+    for i in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        acc, _ = render_offscreen(ctx, scene, cie, W, H, args.spp, spf, args.depth,
+                                  frame_offset=base + (args.warmup + args.steps + i) * ndisp * spf)
+        e2e_secs.append(time.perf_counter() - t0)
+    e2e_step = statistics.median(e2e_secs)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t.item())
+    e2e_value = samples_per_step * world / e2e_step
+    h2d = native.UBO_FLOATS * 4
+    d2h = W * H * 16 + 9 * 4 * sum(list(scene.counts().values())[:5])
+
+    peaks, peak_kind = measured_peaks()
+    # HBM roofline of the megakernel: algorithmic bytes = the accumulator
+    # read-modify-write (16 B read + 16 B write per pixel per dispatch).
+    alg_bytes = 32.0 * W * H * ndisp
+    achieved_gbs = alg_bytes / (ms_step / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "resolution": [W, H], "spp": args.spp, "max_depth": args.depth,
+                   "samples_per_dispatch": spf, "dispatches_per_step": ndisp,
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps * ndisp,
+        "wall_s_timed_region": t_wall,
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
+                     "note": f"peak {peak_kind}; the megakernel is FP32/SFU-issue bound, its HBM traffic is the "
+                             "accumulator only"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        nthreads = os.cpu_count() or 1
+        v, samples, dt, rows = cpu_baseline(args, W, H, args.spp, nthreads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                "sample": f"{rows} evenly spaced rows of {W}x{H} at {args.spp} spp "
+                                          f"({samples} paths, {dt:.1f} s)"}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

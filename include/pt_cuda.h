@@ -1,0 +1,189 @@
+/*
+ * pt_cuda.h — C ABI of libpt_cuda, the GB300 (sm_103a) replacement for the
+ * Vulkan compute dispatch of phyastro/PathTracer.
+ *
+ * The reference host packs a scene into a float uniform buffer, pushes 88 bytes
+ * of push constants, dispatches src/shader.comp over ceil(W/16) x ceil(H/16)
+ * workgroups and waits on a fence; the shader read-modify-writes an RGBA32F
+ * texel buffer holding the running mean of CIE XYZ per pixel.  This library
+ * exposes the same contract as plain C calls: the byte layouts of pt_ubo and
+ * pt_push are identical to the reference's UniformBufferObject and
+ * PushConstantValues, and the accumulator has the reference's layout
+ * (float4 XYZ + w=1 at index x + W*y over invocation coordinates).
+ *
+ * Conventions
+ *   - Every call returns a status code (PT_OK == 0); no exception crosses the
+ *     ABI.  pt_last_error() returns a message for the last failing call.
+ *   - The context owns all device memory.  Input structs are copied at call
+ *     time; the caller keeps ownership of its buffers.
+ *   - A context is single-threaded (one stream, like the reference's one
+ *     compute queue); distinct contexts may be used from distinct threads.
+ */
+#ifndef PT_CUDA_H
+#define PT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Sizes of the uniform-buffer arrays (src/pathtracer.cpp:39-43, src/shader.comp:11-15). */
+#define PT_MAX_OBJECTS_SIZE 1024
+#define PT_MAX_SDFS_SIZE 768
+#define PT_MAX_MATERIALS_SIZE 783
+#define PT_MAX_LIGHTS_SIZE 128
+#define PT_MAX_LIGHTIDS_SIZE 64
+#define PT_CIE_TABLE_SIZE 1323 /* 441 wavelengths 360..800 nm, x y z interleaved */
+/* SDF slots that the shader can evaluate: SearchSDF builds a 32-bit set mask
+ * and set2..set4 are never filled (src/shader.comp:732-777). */
+#define PT_MAX_LIVE_SDFS 32
+
+/* Status codes. */
+#define PT_OK 0
+#define PT_ERR_INVALID 1       /* bad argument (null pointer, size, layout) */
+#define PT_ERR_CUDA 2          /* a CUDA runtime call failed */
+#define PT_ERR_TIMEOUT 3       /* pt_wait deadline passed; the work is still queued */
+#define PT_ERR_UNSUPPORTED 4   /* e.g. an SDF plug-in source that is not recognised */
+#define PT_ERR_NO_SCENE 5      /* dispatch before pt_upload_scene / pt_resize_accum */
+#define PT_ERR_OOM 6           /* device allocation failed */
+#define PT_ERR_KERNEL 7        /* a kernel reported an error through its status word */
+
+/* Byte-for-byte the reference's UniformBufferObject (src/pathtracer.cpp:187-195)
+ * and the shader's `ubo` block (src/shader.comp:19-27): 4097 floats = 16388 B.
+ * Object/material/light IDs are stored as floats, 1-based, 0 = none. */
+typedef struct pt_ubo {
+    float numObjects[7]; /* spheres, planes, boxes, lenses, cyclides, sdfs, lights */
+    float objects[PT_MAX_OBJECTS_SIZE];
+    float sdfs[PT_MAX_SDFS_SIZE];
+    float materials[PT_MAX_MATERIALS_SIZE];
+    float lights[PT_MAX_LIGHTS_SIZE];
+    float lightIDs[PT_MAX_LIGHTIDS_SIZE];
+    float CIEXYZ1931[PT_CIE_TABLE_SIZE];
+} pt_ubo;
+
+/* Byte-for-byte the reference's PushConstantValues (src/pathtracer.cpp:197-218)
+ * and the shader's push-constant block (src/shader.comp:31-52): 88 B. */
+typedef struct pt_push {
+    int32_t resolution[2];
+    int32_t frame;          /* samples issued so far, including this dispatch */
+    int32_t currentSamples; /* samples in the running mean after this dispatch */
+    int32_t samplesPerFrame;
+    float FPS;
+    float persistence;
+    int32_t pathLength;
+    float cameraAngle[2]; /* (-angle.y, angle.x) in degrees, as the host pushes it */
+    float cameraPosX;
+    float cameraPosY;
+    float cameraPosZ;
+    int32_t ISO;
+    float cameraSize;
+    float apertureSize;
+    float apertureDist;
+    float lensRadius;
+    float lensFocalLength;
+    float lensThickness;
+    float lensDistance;
+    int32_t tonemap;
+} pt_push;
+
+/* SDF plug-ins.  The reference splices GLSL snippets defining
+ * `float sdf(in vec3 p)` / `float sdfmaterial(in vec3 p)` into the shader
+ * (src/pathtracer.cpp:2004-2054).  The four shipped snippets (sdfs/<name>.glsl)
+ * are CUDA __device__ functions here; `material` carries the constants that
+ * the scene files vary in their copies of sdfmaterial. */
+enum {
+    PT_SDF_NONE = 0,
+    PT_SDF_BLOB = 1,       /* sdfs/blob.glsl: material = lobe IDs (default 4,5,6) */
+    PT_SDF_MANDELBULB = 2, /* sdfs/mandelbulb.glsl: material = mix endpoints (default 4,3) */
+    PT_SDF_MENGER = 3,     /* sdfs/menger.glsl: material[0] constant (default 0) */
+    PT_SDF_TERRAIN = 4     /* sdfs/terrain.glsl: material[0] constant (default 0) */
+};
+enum {
+    PT_SDFMAT_DEFAULT = 0,  /* the snippet's own sdfmaterial form with `material` */
+    PT_SDFMAT_CONSTANT = 1  /* sdfmaterial returns material[0] */
+};
+typedef struct pt_sdf_plugin {
+    int32_t kind;
+    int32_t material_mode;
+    float material[3];
+} pt_sdf_plugin;
+
+typedef struct pt_ctx pt_ctx;
+
+/* Create a context on CUDA device `device` (replaces instance/device/pipeline
+ * creation, src/pathtracer.cpp:1227-2092). */
+int pt_create(pt_ctx** out, int device);
+int pt_destroy(pt_ctx* ctx);
+
+/* Replaces InsertSDF + GLSLToSPIRV + RecompileComputeShaders
+ * (src/pathtracer.cpp:2004-2054, 1811-1868, 3836-3841).  Each source is either
+ * the GLSL text of a scene's `sdf[i].glsl` (recognised by a whitespace-
+ * insensitive fingerprint of the reference's snippets) or a spec
+ * "builtin:<blob|mandelbulb|menger|terrain>[:m0,m1,m2]".  Positions and
+ * bounding boxes come from pt_ubo.sdfs, as in the reference. */
+int pt_set_sdfs(pt_ctx* ctx, const char* const* sources, int n);
+/* Same, from already-decoded descriptors. */
+int pt_set_sdf_plugins(pt_ctx* ctx, const pt_sdf_plugin* plugins, int n);
+/* Decode one source string into a descriptor without a context. */
+int pt_parse_sdf_source(const char* source, pt_sdf_plugin* out);
+/* The whitespace-insensitive FNV-1a-64 fingerprint pt_parse_sdf_source
+ * matches GLSL text by (0 for NULL). */
+uint64_t pt_sdf_source_fingerprint(const char* source);
+
+/* Replaces the UBO upload (src/pathtracer.cpp:3805-3807). */
+int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo);
+
+/* Replaces CreateTexelBuffer (src/pathtracer.cpp:2250-2256): a zeroed
+ * W*H float4 accumulator. */
+int pt_resize_accum(pt_ctx* ctx, int width, int height);
+
+/* Replaces RecordComputeCommandBuffer + vkQueueSubmit
+ * (src/pathtracer.cpp:3586-3608, 3843-3880).  Asynchronous on the context's
+ * stream; resolution must equal the accumulator size. */
+int pt_dispatch(pt_ctx* ctx, const pt_push* push);
+
+/* Replaces vkWaitForFences (src/pathtracer.cpp:3846): waits at most
+ * timeout_ns and returns PT_ERR_TIMEOUT instead of blocking forever. */
+int pt_wait(pt_ctx* ctx, uint64_t timeout_ns);
+
+/* Replaces the mapped read of the texel buffer in SaveRender
+ * (src/pathtracer.cpp:3496-3515).  Synchronous.  bytes >= W*H*16. */
+int pt_read_accum(pt_ctx* ctx, float* host, size_t bytes);
+/* Uploads a host accumulator (resume a progressive render).  Synchronous. */
+int pt_write_accum(pt_ctx* ctx, const float* host, size_t bytes);
+/* Device address of the accumulator (float4 per pixel), or NULL. */
+void* pt_accum_device_ptr(pt_ctx* ctx);
+
+/* The cudaStream_t the context launches on (as void*), and a way to replace
+ * it with a caller-owned stream (NULL restores the context's own stream). */
+void* pt_stream(pt_ctx* ctx);
+int pt_set_stream(pt_ctx* ctx, void* stream);
+
+/* Message of the last failing call on this context (never NULL). */
+const char* pt_last_error(pt_ctx* ctx);
+
+/* ---- verification hooks (not in the reference) --------------------------
+ * Per-path branch trace of the next dispatch: for every invocation (x, y)
+ * and sample k, path index p = (y * W + x) * samplesPerFrame + k; events
+ * [p * depth_cap + i] holds bounce i's event word (PT_EV_* below), nevents[p]
+ * the number of bounces, colors[p*3..] the sample's XYZ before averaging.
+ * Device pointers owned by the caller; pass NULLs to disable. */
+int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_colors, int depth_cap);
+
+/* Event word layout, identical in the CPU restatement used by the tests. */
+#define PT_EV_HIT_MASK 0xFFFu     /* global object index; PT_EV_HIT_SDF, PT_EV_HIT_MISS */
+#define PT_EV_HIT_SDF 0xFFEu
+#define PT_EV_HIT_MISS 0xFFFu
+#define PT_EV_EMITTER (1u << 12)  /* emitter hit, path terminated */
+#define PT_EV_LIGHT_SHIFT 13      /* 7 bits: light pick index (randomLight) */
+#define PT_EV_SHADOW_SHIFT 20     /* 2 bits: 0 none, 1 RR-culled, 2 occluded, 3 visible */
+#define PT_EV_RR_KILL (1u << 22)  /* terminated by Russian roulette */
+#define PT_EV_VALID (1u << 23)
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_CUDA_H */

@@ -1,0 +1,104 @@
+/*
+ * pt_host.h — C ABI of libpt_host, the headless host that drives libpt_cuda.
+ *
+ * It re-states, without GLFW/ImGui/Vulkan, the parts of the reference's
+ * src/pathtracer.cpp that sit above the compute dispatch: the scene JSON
+ * schema (UpdateFromJSON / UpdateToJSON, :2576-2858), the uniform-buffer
+ * packing with its light list (UpdateUniformBuffer, :3642-3811), the push
+ * constants (UpdatePushConstant, :3813-3834), the offscreen progressive loop
+ * (MainLoop with OFFSCREENRENDER, :3965-4093) and the export tonemap + PPM
+ * writer (SaveRender / SavePPM, :3491-3518, :918-933).
+ *
+ * All calls return PT_OK (0) or a PT_ERR_* code from pt_cuda.h and never
+ * throw.  Messages go to the caller's buffer where one is taken.
+ */
+#ifndef PT_HOST_H
+#define PT_HOST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "pt_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pt_scene pt_scene;
+
+/* Parse a scene JSON document (the reference's schema; "sdf[i].builtin" is
+ * accepted in place of "glsl" as "blob" | "mandelbulb" | ... or a full
+ * "builtin:<name>[:m0,m1,m2]" spec).  Missing object arrays are empty, as in
+ * the reference; missing camera or object fields are errors. */
+int pt_scene_parse(const char* json, size_t len, pt_scene** out, char* err, size_t err_cap);
+int pt_scene_load_file(const char* path, pt_scene** out, char* err, size_t err_cap);
+void pt_scene_free(pt_scene* scene);
+
+/* counts[0..8] = spheres, planes, boxes, lenses, cyclides, sdfs, materials,
+ * lights, camera shots. */
+int pt_scene_counts(const pt_scene* scene, int counts[9]);
+
+/* UpdateUniformBuffer: pack objects, SDF boxes, materials, lights and the
+ * light-ID list (with the reference's lens/cyclide light-list quirk), and
+ * copy `cie` (1323 floats) into the table.  Fails with PT_ERR_INVALID when
+ * the scene overflows the fixed arrays (the reference truncates silently). */
+int pt_scene_pack_ubo(const pt_scene* scene, const float* cie, pt_ubo* out);
+
+/* The host's progressive-render state that UpdatePushConstant reads. */
+typedef struct pt_frame_state {
+    int32_t width, height;
+    int32_t frame;           /* samples issued so far including this dispatch */
+    int32_t currentSamples;  /* samples in the running mean after this dispatch */
+    int32_t samplesPerFrame;
+    float FPS;               /* 1 / frameTime */
+    float persistence;       /* reference default 0.0625 */
+    int32_t pathLength;
+    int32_t cameraShotIndex; /* 1-based, reference default 1 */
+    int32_t tonemap;         /* 0 none, 1 Reinhard, 2 ACES, 3 DEUCES (reference default 3) */
+} pt_frame_state;
+
+/* UpdatePushConstant. */
+int pt_scene_push_constants(const pt_scene* scene, const pt_frame_state* st, pt_push* out);
+
+/* Source text of SDF i (its "glsl", or the builtin spec), owned by the scene. */
+const char* pt_scene_sdf_source(const pt_scene* scene, int i);
+
+/* UpdateToJSON + dump(4): writes a NUL-terminated document of at most cap
+ * bytes; *needed receives the full size including the NUL. */
+int pt_scene_to_json(const pt_scene* scene, char* buf, size_t cap, size_t* needed);
+
+/* Pack + pt_set_sdfs + pt_upload_scene on a context (a scene load and the
+ * recompile it triggers in the reference, :3442-3461 and :3836-3841). */
+int pt_scene_bind(pt_ctx* ctx, const pt_scene* scene, const float* cie);
+
+/* The reference's offscreen render (numSamples, samplesPerFrame, path length
+ * and shot index read from stdin there): frame += spf per dispatch until
+ * currentSamples >= numSamples, then the accumulator is read back. */
+typedef struct pt_offscreen_opts {
+    int32_t width, height;
+    int32_t numSamples;
+    int32_t samplesPerFrame;
+    int32_t pathLength;
+    int32_t cameraShotIndex;
+    int32_t tonemap;
+    int32_t frameOffset; /* samples already issued before this render (0 in the reference) */
+} pt_offscreen_opts;
+int pt_render_offscreen(pt_ctx* ctx, const pt_scene* scene, const float* cie, const pt_offscreen_opts* opts,
+                        float* accum_out, size_t accum_bytes, double* seconds_out);
+
+/* SaveRender's per-pixel chain: E->D65 Bradford, XYZ->sRGB, max(0), tonemap,
+ * sRGB companding, 8-bit truncation.  rgb_out holds W*H*3 bytes. */
+int pt_export_rgb8(const float* accum, int width, int height, int tonemap, uint8_t* rgb_out);
+/* SavePPM: binary P6 with "P6\nW\nH\n255\n" header. */
+int pt_save_ppm(const char* path, const uint8_t* rgb, int width, int height);
+
+/* CIE 1931 2-degree colour-matching functions at 1 nm over 360..800 nm from
+ * the multi-lobe Gaussian fit of Wyman, Sloan & Shirley (JCGT 2(2), 2013),
+ * x y z interleaved: a caller-supplied table for pt_ubo.CIEXYZ1931. */
+void pt_cie_analytic_table(float out[PT_CIE_TABLE_SIZE]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PT_HOST_H */

@@ -1,0 +1,99 @@
+"""ctypes wrapper of the CPU restatement of src/shader.comp (oracle/pt_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the tests, the smoke check and the CPU-baseline
+leg of bench.py use it as the checker.  The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libpt_oracle.so")
+
+
+class PtoTrace(ctypes.Structure):
+    _fields_ = [
+        ("depth_cap", ctypes.c_int),
+        ("events", ctypes.c_void_p),
+        ("nevents", ctypes.c_void_p),
+        ("colors", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def build() -> str:
+    src = os.path.join(HERE, "pt_oracle.c")
+    deps = [src, os.path.join(HERE, "pt_oracle.h"), os.path.join(HERE, "..", "include", "pt_cuda.h")]
+    if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
+        os.makedirs(os.path.dirname(LIB), exist_ok=True)
+        subprocess.run([os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-std=c11", "-ffp-contract=off",
+                        "-fno-fast-math", "-fopenmp", "-shared", "-o", LIB, src, "-lm"], check=True)
+    return LIB
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.pto_dispatch.restype = ctypes.c_int
+        L.pto_dispatch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(PtoTrace), ctypes.c_int]
+        L.pto_pcg32.restype = ctypes.c_uint32
+        L.pto_pcg32.argtypes = [ctypes.c_uint32]
+        L.pto_random_float.restype = ctypes.c_float
+        L.pto_random_float.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+        L.pto_generate_seed.restype = ctypes.c_uint32
+        L.pto_generate_seed.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int]
+        L.pto_bk7_index.restype = ctypes.c_float
+        L.pto_bk7_index.argtypes = [ctypes.c_float]
+        L.pto_blackbody.restype = None
+        L.pto_blackbody.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
+        L.pto_blackbody_peak.restype = ctypes.c_float
+        L.pto_blackbody_peak.argtypes = [ctypes.c_float]
+        L.pto_sdf_eval.restype = ctypes.c_float
+        L.pto_sdf_eval.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.pto_sdf_material.restype = ctypes.c_float
+        L.pto_sdf_material.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.pto_wave_to_xyz.restype = None
+        L.pto_wave_to_xyz.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def dispatch(ubo: np.ndarray, push, plugins: list, accum: np.ndarray, rect=None, trace_depth: int = 0,
+             nthreads: int = 0):
+    """Runs the shader over rect=(x0, y0, x1, y1) (default: the whole frame).
+
+    Returns (events, nevents, colors) when trace_depth > 0, else None.
+    accum is updated in place (H x W x 4 float32).
+    """
+    W, H = push.resolution[0], push.resolution[1]
+    x0, y0, x1, y1 = rect if rect is not None else (0, 0, W, H)
+    spf = push.samplesPerFrame
+    npaths = (x1 - x0) * (y1 - y0) * spf
+    tr = None
+    out = None
+    if trace_depth > 0:
+        ev = np.zeros(npaths * trace_depth, np.uint32)
+        nev = np.zeros(npaths, np.uint32)
+        col = np.zeros(npaths * 3, np.float32)
+        tr = PtoTrace(trace_depth, ev.ctypes.data, nev.ctypes.data, col.ctypes.data)
+        out = (ev.reshape(npaths, trace_depth), nev, col.reshape(npaths, 3))
+    from pathtracer_gb300.native import PtSdfPlugin  # struct layout only
+
+    arr = (PtSdfPlugin * max(1, len(plugins)))(*plugins)
+    assert accum.dtype == np.float32 and accum.flags["C_CONTIGUOUS"] and accum.size == W * H * 4
+    rc = lib().pto_dispatch(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins),
+                            accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr) if tr else None, nthreads)
+    if rc != 0:
+        raise RuntimeError(f"pto_dispatch failed: {rc}")
+    return out

@@ -1,0 +1,1289 @@
+/*
+ * pt_oracle.c — scalar CPU restatement of src/shader.comp (phyastro/PathTracer).
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for libpt_cuda.  Each function below
+ * cites the shader lines it restates (SC = src/shader.comp) and evaluates the
+ * GLSL expressions in the same order, in float, without contraction
+ * (compiled with -ffp-contract=off); `fma` is called exactly where the shader
+ * writes fma.  GLSL built-ins follow their specification:
+ *   mix(x,y,a) = x*(1-a) + y*a        mod(x,y) = x - y*floor(x/y)
+ *   normalize(v) = v * (1/sqrt(v.v))  length(v) = sqrt(v.v)
+ *   inversesqrt(x) = 1/sqrt(x)        sign, step, faceforward, refract as specified
+ *   min/max = IEEE minNum/maxNum (fminf/fmaxf)
+ * Transcendentals are the C library's (sinf, cosf, expf, logf, powf, acosf).
+ * Out-of-range reads of the uniform arrays return 0 (robust buffer access).
+ *
+ * Parity unpinned: the reference has no tests or golden vectors and cannot
+ * run here (Vulkan/Windows); primitives are pinned by known-answer values
+ * derived from its formulas (tests/test_oracle_kat.py).
+ */
+#include "pt_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define PI_F 3.141592653589792623810034526344f /* SC:9 */
+#define ONEBYTHREE 0.3333333f                  /* SC:10 */
+#define MAXDIST 1e5f                           /* SC:8 */
+
+/* ------------------------------------------------------------------ */
+/* GLSL value types and built-ins                                      */
+/* ------------------------------------------------------------------ */
+typedef struct { float x, y; } vec2;
+typedef struct { float x, y, z; } vec3;
+typedef struct { float x, y, z, w; } vec4;
+typedef struct { vec3 c0, c1, c2; } mat3; /* columns */
+
+static inline vec2 mk2(float x, float y) { vec2 r = {x, y}; return r; }
+static inline vec3 mk3(float x, float y, float z) { vec3 r = {x, y, z}; return r; }
+static inline vec4 mk4(float x, float y, float z, float w) { vec4 r = {x, y, z, w}; return r; }
+static inline vec4 s4(float s) { return mk4(s, s, s, s); }
+
+static inline vec3 add3(vec3 a, vec3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline vec3 sub3(vec3 a, vec3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline vec3 mul3(vec3 a, vec3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline vec3 div3(vec3 a, vec3 b) { return mk3(a.x / b.x, a.y / b.y, a.z / b.z); }
+static inline vec3 scl3(vec3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+static inline vec3 neg3(vec3 a) { return mk3(-a.x, -a.y, -a.z); }
+static inline vec3 fma3(vec3 a, vec3 b, vec3 c) { return mk3(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z)); }
+static inline vec3 abs3(vec3 a) { return mk3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+static inline vec3 min3(vec3 a, vec3 b) { return mk3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
+static inline vec3 max3(vec3 a, vec3 b) { return mk3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)); }
+static inline float dot3(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline float length3(vec3 a) { return sqrtf(dot3(a, a)); }
+static inline vec3 normalize3(vec3 a) { float inv = 1.0f / sqrtf(dot3(a, a)); return scl3(a, inv); }
+
+static inline vec4 add4(vec4 a, vec4 b) { return mk4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+static inline vec4 mul4(vec4 a, vec4 b) { return mk4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+static inline vec4 scl4(vec4 a, float s) { return mk4(a.x * s, a.y * s, a.z * s, a.w * s); }
+static inline vec4 div4s(vec4 a, float s) { return mk4(a.x / s, a.y / s, a.z / s, a.w / s); }
+
+static inline float signf_glsl(float x) { return (x > 0.0f) ? 1.0f : ((x < 0.0f) ? -1.0f : 0.0f); }
+static inline float stepf_glsl(float edge, float x) { return (x < edge) ? 0.0f : 1.0f; }
+static inline float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+static inline float modf_glsl(float x, float y) { return x - y * floorf(x / y); }
+
+/* mat3 * vec3: sum over columns. */
+static inline vec3 mat_mul_vec(mat3 m, vec3 v) {
+    return mk3(m.c0.x * v.x + m.c1.x * v.y + m.c2.x * v.z,
+               m.c0.y * v.x + m.c1.y * v.y + m.c2.y * v.z,
+               m.c0.z * v.x + m.c1.z * v.y + m.c2.z * v.z);
+}
+/* vec3 * mat3: dot with each column. */
+static inline vec3 vec_mul_mat(vec3 v, mat3 m) { return mk3(dot3(v, m.c0), dot3(v, m.c1), dot3(v, m.c2)); }
+static inline mat3 mat_mul_mat(mat3 a, mat3 b) {
+    mat3 r;
+    r.c0 = mat_mul_vec(a, b.c0);
+    r.c1 = mat_mul_vec(a, b.c1);
+    r.c2 = mat_mul_vec(a, b.c2);
+    return r;
+}
+
+/* refract(I, N, eta) per the GLSL specification. */
+static inline vec3 refract3(vec3 I, vec3 N, float eta) {
+    float d = dot3(N, I);
+    float k = 1.0f - eta * eta * (1.0f - d * d);
+    if (k < 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+    return sub3(scl3(I, eta), scl3(N, eta * d + sqrtf(k)));
+}
+
+/* ------------------------------------------------------------------ */
+/* Per-dispatch state                                                  */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    const pt_ubo* u;
+    const pt_push* pc;
+    const pt_sdf_plugin* plug;
+    int nplug;
+    vec3 cameraPos; /* SC:127 */
+    /* trace bookkeeping (not part of the shader's arithmetic) */
+    int last_hit;      /* object index of the last successful hit in Intersection */
+    int light_pick;
+    int shadow_state;
+} ctx_t;
+
+static inline float OBJ(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_OBJECTS_SIZE) ? c->u->objects[i] : 0.0f; }
+static inline float SDFS(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_SDFS_SIZE) ? c->u->sdfs[i] : 0.0f; }
+static inline float MATS(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_MATERIALS_SIZE) ? c->u->materials[i] : 0.0f; }
+static inline float LIGHTS(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_LIGHTS_SIZE) ? c->u->lights[i] : 0.0f; }
+static inline float LIGHTIDS(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_LIGHTIDS_SIZE) ? c->u->lightIDs[i] : 0.0f; }
+static inline float CIE(const ctx_t* c, int i) { return (i >= 0 && i < PT_CIE_TABLE_SIZE) ? c->u->CIEXYZ1931[i] : 0.0f; }
+
+typedef struct { vec3 origin, dir; } Ray;
+typedef struct { vec3 pos; float radius; int materialID, lightID; } sphere_t;
+typedef struct { vec3 pos; int materialID, lightID; } plane_t;
+typedef struct { vec3 pos, rotation, size; int materialID, lightID; } box_t;
+typedef struct { vec3 pos; float radius, sliceSize; int is1stSlice; vec3 rotation; int materialID, lightID; } slice_t;
+typedef struct { vec3 pos, rotation; float radius, focalLength, thickness; int isConverging; int materialID, lightID; } lens_t;
+typedef struct { vec3 pos, rotation, scale; float a, b, c, d, brad; int materialID, lightID; } cyclide_t;
+typedef struct { vec3 reflection; } material_t;
+typedef struct { float x, y; } light_t;
+
+/* SC:129-140 */
+static vec3 WaveToXYZ(const ctx_t* c, float wave) {
+    vec3 XYZ = mk3(0.0f, 0.0f, 0.0f);
+    if ((wave >= 360.0f) && (wave <= 800.0f)) {
+        int index3 = 3 * (int)(floorf(wave) - 360.0f);
+        vec3 t1 = mk3(CIE(c, index3), CIE(c, index3 + 1), CIE(c, index3 + 2));
+        vec3 t2 = mk3(CIE(c, index3 + 3), CIE(c, index3 + 4), CIE(c, index3 + 5));
+        float a = wave - floorf(wave);
+        XYZ = mk3(mixf(t1.x, t2.x, a), mixf(t1.y, t2.y, a), mixf(t1.z, t2.z, a));
+    }
+    return XYZ;
+}
+
+/* SC:143-152 */
+static mat3 RotationMatrix(vec3 angle) {
+    angle = scl3(angle, 0.0174532925199f);
+    vec3 s = mk3(sinf(angle.x), sinf(angle.y), sinf(angle.z));
+    vec3 co = mk3(cosf(angle.x), cosf(angle.y), cosf(angle.z));
+    mat3 mX = {{1.0f, 0.0f, 0.0f}, {0.0f, co.x, -s.x}, {0.0f, s.x, co.x}};
+    mat3 mY = {{co.y, 0.0f, s.y}, {0.0f, 1.0f, 0.0f}, {-s.y, 0.0f, co.y}};
+    mat3 mZ = {{co.z, -s.z, 0.0f}, {s.z, co.z, 0.0f}, {0.0f, 0.0f, 1.0f}};
+    return mat_mul_mat(mat_mul_mat(mX, mY), mZ);
+}
+
+/* SC:154-235 */
+static sphere_t UnpackSphere(const ctx_t* c, int index) {
+    sphere_t o;
+    index *= 6;
+    o.pos = mk3(OBJ(c, index), OBJ(c, index + 1), OBJ(c, index + 2));
+    o.radius = OBJ(c, index + 3);
+    o.materialID = (int)OBJ(c, index + 4) - 1;
+    o.lightID = (int)OBJ(c, index + 5) - 1;
+    return o;
+}
+static plane_t UnpackPlane(const ctx_t* c, int index, int offset) {
+    plane_t o;
+    index *= 5;
+    o.pos = mk3(OBJ(c, index + offset), OBJ(c, index + 1 + offset), OBJ(c, index + 2 + offset));
+    o.materialID = (int)OBJ(c, index + 3 + offset) - 1;
+    o.lightID = (int)OBJ(c, index + 4 + offset) - 1;
+    return o;
+}
+static box_t UnpackBox(const ctx_t* c, int index, int offset) {
+    box_t o;
+    index *= 11;
+    o.pos = mk3(OBJ(c, index + offset), OBJ(c, index + 1 + offset), OBJ(c, index + 2 + offset));
+    o.rotation = mk3(OBJ(c, index + 3 + offset), OBJ(c, index + 4 + offset), OBJ(c, index + 5 + offset));
+    o.size = mk3(OBJ(c, index + 6 + offset), OBJ(c, index + 7 + offset), OBJ(c, index + 8 + offset));
+    o.materialID = (int)OBJ(c, index + 9 + offset) - 1;
+    o.lightID = (int)OBJ(c, index + 10 + offset) - 1;
+    return o;
+}
+static lens_t UnpackLens(const ctx_t* c, int index, int offset) {
+    lens_t o;
+    index *= 12;
+    o.pos = mk3(OBJ(c, index + offset), OBJ(c, index + 1 + offset), OBJ(c, index + 2 + offset));
+    o.rotation = mk3(OBJ(c, index + 3 + offset), OBJ(c, index + 4 + offset), OBJ(c, index + 5 + offset));
+    o.radius = OBJ(c, index + 6 + offset);
+    o.focalLength = OBJ(c, index + 7 + offset);
+    o.thickness = OBJ(c, index + 8 + offset);
+    o.isConverging = OBJ(c, index + 9 + offset) != 0.0f;
+    o.materialID = (int)OBJ(c, index + 10 + offset) - 1;
+    o.lightID = (int)OBJ(c, index + 11 + offset) - 1;
+    return o;
+}
+static cyclide_t UnpackCyclide(const ctx_t* c, int index, int offset) {
+    cyclide_t o;
+    index *= 16;
+    o.pos = mk3(OBJ(c, index + offset), OBJ(c, index + offset + 1), OBJ(c, index + offset + 2));
+    o.rotation = mk3(OBJ(c, index + 3 + offset), OBJ(c, index + 4 + offset), OBJ(c, index + 5 + offset));
+    o.scale = mk3(OBJ(c, index + 6 + offset), OBJ(c, index + 7 + offset), OBJ(c, index + 8 + offset));
+    o.a = OBJ(c, index + 9 + offset);
+    o.b = OBJ(c, index + 10 + offset);
+    o.c = OBJ(c, index + 11 + offset);
+    o.d = OBJ(c, index + 12 + offset);
+    o.brad = OBJ(c, index + 13 + offset);
+    o.materialID = (int)OBJ(c, index + 14 + offset) - 1;
+    o.lightID = (int)OBJ(c, index + 15 + offset) - 1;
+    return o;
+}
+static material_t UnpackMaterial(const ctx_t* c, int index) {
+    material_t m;
+    index *= 3;
+    m.reflection = mk3(MATS(c, index), MATS(c, index + 1), MATS(c, index + 2));
+    return m;
+}
+static light_t UnpackLight(const ctx_t* c, int index) {
+    light_t l;
+    if (index == -1) {
+        l.x = 5500.0f;
+        l.y = 0.0f;
+        return l;
+    }
+    index *= 2;
+    l.x = LIGHTS(c, index);
+    l.y = LIGHTS(c, index + 1);
+    return l;
+}
+/* SC:237-254 */
+static material_t GetMaterialMix(const ctx_t* c, float materialID) {
+    material_t m1 = UnpackMaterial(c, (int)floorf(materialID));
+    material_t m2 = UnpackMaterial(c, (int)ceilf(materialID));
+    float x = materialID - floorf(materialID);
+    material_t m;
+    m.reflection = mk3(mixf(m1.reflection.x, m2.reflection.x, x), mixf(m1.reflection.y, m2.reflection.y, x),
+                       mixf(m1.reflection.z, m2.reflection.z, x));
+    return m;
+}
+static light_t GetLightMix(const ctx_t* c, float lightID) { return UnpackLight(c, (int)lightID); }
+
+/* SC:263-276 */
+static int BoundingSphere(Ray ray, vec3 pos, float radius2) {
+    vec3 lo = sub3(ray.origin, pos);
+    float b = dot3(ray.dir, lo);
+    float cc = dot3(lo, lo) - radius2;
+    if ((b * b) < cc) return 0;
+    if ((b >= 0.0f) && (cc >= 0.0f)) return 0;
+    return 1;
+}
+
+/* SC:278-287 (SortMinMax SC:256-261) */
+static vec2 RayIntersectAABB(vec3 origin, vec3 invdir, vec3 pos, vec3 size) {
+    vec3 lo = sub3(origin, pos);
+    vec3 tMin = mul3(fma3(size, mk3(-0.5f, -0.5f, -0.5f), neg3(lo)), invdir);
+    vec3 tMax = mul3(fma3(size, mk3(0.5f, 0.5f, 0.5f), neg3(lo)), invdir);
+    vec3 a = min3(tMin, tMax), b = max3(tMin, tMax);
+    float t1 = fmaxf(fmaxf(a.x, a.y), a.z);
+    float t2 = fminf(fminf(b.x, b.y), b.z);
+    return mk2(t1, t2);
+}
+
+typedef struct {
+    float hitdist;
+    vec3 normal;
+    float materialID;
+    float lightID;
+} hit_t;
+
+/* SC:289-317 */
+static int SphereIntersection(Ray ray, sphere_t o, hit_t* h) {
+    vec3 lo = sub3(ray.origin, o.pos);
+    float b = 2.0f * dot3(ray.dir, lo);
+    float cc = dot3(lo, lo) - (o.radius * o.radius);
+    float disc = b * b - 4.0f * cc;
+    if (disc < 0.0f) return 0;
+    float sqrtD = sqrtf(disc);
+    float t1 = (-b - sqrtD) * 0.5f;
+    float t2 = (-b + sqrtD) * 0.5f;
+    float t = (t1 > 0.0f) ? t1 : t2;
+    int isOutside = (t1 > 0.0f) ? 1 : -1;
+    if (t < 1e-4f) return 0;
+    if (t < h->hitdist) {
+        h->hitdist = t;
+        h->normal = normalize3(scl3(fma3(ray.dir, mk3(t, t, t), lo), (float)isOutside));
+        h->materialID = (float)o.materialID;
+        h->lightID = (float)o.lightID;
+        return 1;
+    }
+    return 0;
+}
+
+/* SC:319-335 */
+static int PlaneIntersection(Ray ray, plane_t o, hit_t* h) {
+    vec3 lo = sub3(ray.origin, o.pos);
+    float t = -lo.y / ray.dir.y;
+    if (t < 1e-4f) return 0;
+    if (t < h->hitdist) {
+        h->hitdist = t;
+        /* faceforward(N, I, Nref) = dot(Nref, I) < 0 ? N : -N with N = Nref = (0,1,0) */
+        float d = 0.0f * ray.dir.x + 1.0f * ray.dir.y + 0.0f * ray.dir.z;
+        h->normal = (d < 0.0f) ? mk3(0.0f, 1.0f, 0.0f) : mk3(-0.0f, -1.0f, -0.0f);
+        h->materialID = (float)o.materialID;
+        h->lightID = (float)o.lightID;
+        return 1;
+    }
+    return 0;
+}
+
+/* SC:337-364 */
+static int BoxIntersection(Ray ray, box_t o, hit_t* h) {
+    mat3 m = RotationMatrix(o.rotation);
+    vec3 lo = vec_mul_mat(sub3(ray.origin, o.pos), m);
+    vec3 dir = vec_mul_mat(ray.dir, m);
+    vec3 invdir = mk3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+    vec3 tMin = mul3(fma3(o.size, mk3(-0.5f, -0.5f, -0.5f), neg3(lo)), invdir);
+    vec3 tMax = mul3(fma3(o.size, mk3(0.5f, 0.5f, 0.5f), neg3(lo)), invdir);
+    vec3 a = min3(tMin, tMax), b = max3(tMin, tMax);
+    float t1 = fmaxf(fmaxf(a.x, a.y), a.z);
+    float t2 = fminf(fminf(b.x, b.y), b.z);
+    float t = (t1 < 0.0f) ? t2 : t1;
+    if ((t1 > t2) || (t < 1e-4f)) return 0;
+    if (t < h->hitdist) {
+        h->hitdist = t;
+        vec3 p = abs3(div3(add3(lo, scl3(dir, t)), o.size));
+        float mx = fmaxf(fmaxf(p.x, p.y), p.z);
+        vec3 st = mk3(stepf_glsl(mx, p.x), stepf_glsl(mx, p.y), stepf_glsl(mx, p.z));
+        vec3 sg = mk3(-signf_glsl(dir.x), -signf_glsl(dir.y), -signf_glsl(dir.z));
+        h->normal = mat_mul_vec(m, mul3(st, sg));
+        h->materialID = (float)o.materialID;
+        h->lightID = (float)o.lightID;
+        return 1;
+    }
+    return 0;
+}
+
+/* SC:366-417 */
+static int SphereSliceIntersection(Ray ray, slice_t o, float localSlicePos, int isSideInvert, hit_t* h, int* isOutside) {
+    mat3 m = RotationMatrix(o.rotation);
+    float sliceOffset = o.radius - o.sliceSize;
+    vec3 org = vec_mul_mat(sub3(ray.origin, o.pos), m);
+    if (o.is1stSlice) {
+        org.x += localSlicePos - o.sliceSize - sliceOffset;
+    } else {
+        org.x -= localSlicePos - o.sliceSize - sliceOffset;
+    }
+    vec3 dir = vec_mul_mat(ray.dir, m);
+    float b = 2.0f * dot3(dir, org);
+    float cc = dot3(org, org) - (o.radius * o.radius);
+    float disc = b * b - 4.0f * cc;
+    float t = 1e6f;
+    int isOut = 1;
+    if (disc < 0.0f) return 0;
+    float sqrtD = sqrtf(disc);
+    float t1 = (-b - sqrtD) * 0.5f;
+    float t2 = (-b + sqrtD) * 0.5f;
+    if (o.is1stSlice) {
+        t1 = (fmaf(dir.x, t1, org.x) > -sliceOffset) ? 1e6f : t1;
+        t2 = (fmaf(dir.x, t2, org.x) > -sliceOffset) ? 1e6f : t2;
+    } else {
+        t1 = (fmaf(dir.x, t1, org.x) < sliceOffset) ? 1e6f : t1;
+        t2 = (fmaf(dir.x, t2, org.x) < sliceOffset) ? 1e6f : t2;
+    }
+    t = (t1 > 0.0f) ? t1 : t;
+    if (t2 < t) {
+        t = t2;
+        isOut = -1;
+    }
+    if (t < 1e-4f) return 0;
+    if (t < h->hitdist) {
+        h->hitdist = t;
+        h->normal = mat_mul_vec(m, normalize3(scl3(fma3(dir, mk3(t, t, t), org), (float)isOut)));
+        *isOutside = (!isSideInvert) ? isOut : -isOut;
+        h->materialID = (float)o.materialID;
+        h->lightID = (float)o.lightID;
+        return 1;
+    }
+    return 0;
+}
+
+/* SC:419-448 */
+static int LensIntersection(Ray ray, lens_t o, hit_t* h, int* isOutside) {
+    float lensThicknessHalf = 2.0f * o.focalLength - sqrtf(4.0f * o.focalLength * o.focalLength - o.radius * o.radius);
+    float lensSlicePos = 0.5f * (o.isConverging ? o.thickness : -o.thickness);
+    if (o.isConverging) lensSlicePos += lensThicknessHalf;
+    int isIntersect = 0;
+    for (int i = 0; i < 2; i++) {
+        slice_t s;
+        s.pos = o.pos;
+        s.radius = 2.0f * o.focalLength;
+        s.sliceSize = lensThicknessHalf;
+        s.is1stSlice = (i == 0);
+        s.rotation = o.rotation;
+        s.materialID = o.materialID;
+        s.lightID = o.lightID;
+        if (SphereSliceIntersection(ray, s, lensSlicePos, !o.isConverging, h, isOutside)) isIntersect = 1;
+    }
+    return isIntersect;
+}
+
+/* SC:450-472 */
+static inline float EvalQuadratic(float a, float b, float c, float x) { return x * (x * a + b) + c; }
+static inline float EvalCubic(float a, float b, float c, float d, float x) { return x * (x * (x * a + b) + c) + d; }
+static inline float EvalQuartic(float a, float b, float c, float d, float e, float x) {
+    return x * (x * (x * (x * a + b) + c) + d) + e;
+}
+
+/* SC:474-503; returns the number of leading real roots flagged (1 or 3). */
+static int SolveCubic(float b, float c, float d, vec3* roots) {
+    float bdiv3 = b * ONEBYTHREE;
+    float Q = c * ONEBYTHREE - bdiv3 * bdiv3;
+    float R = 0.5f * bdiv3 * c - bdiv3 * bdiv3 * bdiv3 - 0.5f * d;
+    float D = Q * Q * Q + R * R;
+    if (D > 0.0f) {
+        float u = R + sqrtf(D);
+        float v = R - sqrtf(D);
+        float S = signf_glsl(u) * powf(fabsf(u), ONEBYTHREE);
+        float T = signf_glsl(v) * powf(fabsf(v), ONEBYTHREE);
+        roots->x = S + T - bdiv3;
+        for (int i = 0; i < 2; i++) {
+            roots->x -= EvalCubic(1.0f, b, c, d, roots->x) / EvalQuadratic(3.0f, 2.0f * b, c, roots->x);
+        }
+        return 1;
+    }
+    float sqrtnegQ = sqrtf(-Q);
+    float thetadiv3 = acosf(R / (sqrtnegQ * sqrtnegQ * sqrtnegQ)) * ONEBYTHREE;
+    float TWOPIBYTHREE = fmaf(2.0f, PI_F, ONEBYTHREE);
+    float k = 2.0f * sqrtnegQ;
+    roots->x = k * cosf(thetadiv3) - bdiv3;
+    roots->y = k * cosf(thetadiv3 + TWOPIBYTHREE) - bdiv3;
+    roots->z = k * cosf(fmaf(2.0f, TWOPIBYTHREE, thetadiv3)) - bdiv3;
+    for (int i = 0; i < 2; i++) {
+        roots->x -= EvalCubic(1.0f, b, c, d, roots->x) / EvalQuadratic(3.0f, 2.0f * b, c, roots->x);
+        roots->y -= EvalCubic(1.0f, b, c, d, roots->y) / EvalQuadratic(3.0f, 2.0f * b, c, roots->y);
+        roots->z -= EvalCubic(1.0f, b, c, d, roots->z) / EvalQuadratic(3.0f, 2.0f * b, c, roots->z);
+    }
+    return 3;
+}
+
+/* SC:505-541; real[i] flags which of roots[0..3] are set. */
+static void SolveQuartic(float a, float b, float c, float d, float e, float roots[4], int real[4]) {
+    float inva = 1.0f / a;
+    float inva2 = inva * 0.5f;
+    float inva2a2 = inva2 * inva2;
+    float bb = b * b;
+    float p = -1.5f * bb * inva2a2 + c * inva;
+    float q = bb * b * inva2a2 * inva2 - b * c * inva * inva2 + d * inva;
+    float r = -0.1875f * bb * bb * inva2a2 * inva2a2 + 0.5f * c * bb * inva2a2 * inva2 - b * d * inva2a2 + e * inva;
+    vec3 s = mk3(0.0f, 0.0f, 0.0f);
+    SolveCubic(0.5f * -p, -r, 0.5f * p * r - 0.125f * q * q, &s);
+    real[0] = real[1] = real[2] = real[3] = 0;
+    float s2subp = 2.0f * s.x - p;
+    if (s2subp < 0.0f) return;
+    float invs2subp = -2.0f * s.x - p;
+    float sqrts2subp = sqrtf(s2subp);
+    float q2divsqrt = 2.0f * q / sqrts2subp;
+    float invaddq2div = invs2subp + q2divsqrt;
+    float invsubq2div = invs2subp - q2divsqrt;
+    float bdiv4a = 0.25f * inva * b;
+    if (invaddq2div >= 0.0f) {
+        float sq = sqrtf(invaddq2div);
+        roots[0] = 0.5f * (-sqrts2subp + 1.0f * sq) - bdiv4a;
+        roots[1] = 0.5f * (-sqrts2subp + -1.0f * sq) - bdiv4a;
+        for (int i = 0; i < 2; i++) {
+            roots[i] -= EvalQuartic(a, b, c, d, e, roots[i]) / EvalCubic(4.0f * a, 3.0f * b, 2.0f * c, d, roots[i]);
+        }
+        real[0] = real[1] = 1;
+    }
+    if (invsubq2div >= 0.0f) {
+        float sq = sqrtf(invsubq2div);
+        roots[2] = 0.5f * (sqrts2subp + 1.0f * sq) - bdiv4a;
+        roots[3] = 0.5f * (sqrts2subp + -1.0f * sq) - bdiv4a;
+        for (int i = 2; i < 4; i++) {
+            roots[i] -= EvalQuartic(a, b, c, d, e, roots[i]) / EvalCubic(4.0f * a, 3.0f * b, 2.0f * c, d, roots[i]);
+        }
+        real[2] = real[3] = 1;
+    }
+}
+
+/* Swizzles used by the cyclide. */
+static inline vec3 xzy(vec3 v) { return mk3(v.x, v.z, v.y); }
+static inline vec3 yzx(vec3 v) { return mk3(v.y, v.z, v.x); }
+static inline vec3 zxy(vec3 v) { return mk3(v.z, v.x, v.y); }
+
+/* SC:633-679 */
+static int DupinCyclide(Ray ray, cyclide_t ob, hit_t* h) {
+    mat3 m = RotationMatrix(ob.rotation);
+    vec3 o = xzy(div3(vec_mul_mat(sub3(ray.origin, ob.pos), m), ob.scale));
+    vec3 d = xzy(div3(vec_mul_mat(ray.dir, m), ob.scale));
+    float A = ob.a, B = ob.b, C = ob.c, Dd = ob.d;
+    vec3 dd = mul3(d, d), oo = mul3(o, o), od = mul3(o, d);
+    vec3 dyzx = yzx(d), dzxy = zxy(d), oyzx = yzx(o), ozxy = zxy(o);
+    float a4 = dot3(dd, dd) + 2.0f * dot3(dd, mul3(dyzx, dyzx));
+    float a3 = 4.0f * (dot3(o, mul3(dd, d)) + dot3(od, mul3(dyzx, dyzx)) + dot3(od, mul3(dzxy, dzxy)));
+    float a2 = 6.0f * dot3(oo, dd) + 8.0f * dot3(od, mul3(oyzx, dyzx)) +
+               2.0f * (dot3(oo, mul3(dyzx, dyzx)) + dot3(oo, mul3(dzxy, dzxy))) +
+               2.0f * (B * B - Dd * Dd) * dot3(d, d) - 4.0f * (A * A * d.x * d.x + B * B * d.y * d.y);
+    float a1 = 4.0f * (dot3(mul3(oo, o), d) + dot3(oo, mul3(oyzx, dyzx)) + dot3(oo, mul3(ozxy, dzxy)) +
+                       2.0f * A * C * Dd * d.x + (B * B - Dd * Dd) * dot3(o, d) -
+                       2.0f * (A * A * o.x * d.x + B * B * o.y * d.y));
+    float a0 = dot3(oo, oo) + 2.0f * dot3(oo, mul3(oyzx, oyzx)) + B * B * B * B + Dd * Dd * Dd * Dd -
+               2.0f * B * B * Dd * Dd - 4.0f * C * C * Dd * Dd + 8.0f * A * C * Dd * o.x +
+               2.0f * (B * B - Dd * Dd) * dot3(o, o) - 4.0f * (A * A * o.x * o.x + B * B * o.y * o.y);
+    float roots[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    int real[4];
+    SolveQuartic(a4, a3, a2, a1, a0, roots, real);
+    float t = 1e6f;
+    for (int i = 0; i < 4; i++) {
+        if (real[i]) {
+            if ((roots[i] < t) && (roots[i] > 0.0f)) t = roots[i];
+        }
+    }
+    if (t < h->hitdist) {
+        h->hitdist = t;
+        float x = o.x + d.x * t;
+        float y = o.y + d.y * t;
+        float z = o.z + d.z * t;
+        float term1 = x * x + y * y + z * z + B * B - Dd * Dd;
+        vec3 n;
+        n.x = 4.0f * (x * term1 - 2.0f * A * (A * x - C * Dd));
+        n.y = 4.0f * z * term1;
+        n.z = 4.0f * y * (term1 - 2.0f * B * B);
+        h->normal = normalize3(n);
+        h->materialID = (float)ob.materialID;
+        h->lightID = (float)ob.lightID;
+        return 1;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* SDF plug-ins (sdfs/<name>.glsl) and the spliced SDF()/SDFMATERIAL()  */
+/* ------------------------------------------------------------------ */
+/* SC:686-702 */
+static inline float smin1(float x, float y) {
+    float k = 0.02f;
+    k *= 6.0f;
+    float h = fmaxf(k - fabsf(x - y), 0.0f) / k;
+    float m = h * h * h * 0.5f;
+    float s = m * k * ONEBYTHREE;
+    return fminf(x, y) - s;
+}
+static inline vec2 smin2(vec2 x, vec2 y) {
+    float k = 0.02f;
+    k *= 6.0f;
+    float h = fmaxf(k - fabsf(x.x - y.x), 0.0f) / k;
+    float m = h * h * h * 0.5f;
+    float s = m * k * ONEBYTHREE;
+    return (x.x < y.x) ? mk2(x.x - s, x.y + (y.y - x.y) * m) : mk2(y.x - s, x.y + (y.y - x.y) * (1.0f - m));
+}
+
+/* sdfs/blob.glsl:1-8 */
+static float blob_sdf(vec3 p) {
+    float s1 = length3(p) - 1.0f;
+    float s2 = length3(mk3(p.x, p.y - 1.0f, p.z)) - 0.7f;
+    float s3 = length3(mk3(p.x - 0.25f, p.y - 1.25f, p.z - 0.5f)) - 0.25f;
+    float s4 = length3(mk3(p.x + 0.25f, p.y - 1.25f, p.z - 0.5f)) - 0.25f;
+    return smin1(smin1(smin1(s1, s2), s3), s4);
+}
+/* sdfs/blob.glsl:10-17 (lobe material IDs parameterised) */
+static float blob_material(vec3 p, const float* m) {
+    vec2 s1 = mk2(length3(p) - 1.0f, m[0]);
+    vec2 s2 = mk2(length3(mk3(p.x, p.y - 1.0f, p.z)) - 0.7f, m[1]);
+    vec2 s3 = mk2(length3(mk3(p.x - 0.25f, p.y - 1.25f, p.z - 0.5f)) - 0.25f, m[2]);
+    vec2 s4 = mk2(length3(mk3(p.x + 0.25f, p.y - 1.25f, p.z - 0.5f)) - 0.25f, m[2]);
+    return smin2(smin2(smin2(s1, s2), s3), s4).y;
+}
+
+/* sdfs/mandelbulb.glsl:3-52 */
+static float mandelbulb_sdf(vec3 p) {
+    vec3 z = p;
+    float r = length3(z);
+    float dr = 1.0f;
+    for (int i = 0; i < 4; i++) {
+        dr = 8.0f * powf(r, 7.0f) * dr + 1.0f;
+        float invr = 1.0f / r;
+        float invl = 1.0f / sqrtf(z.x * z.x + z.z * z.z);
+        r *= r;
+        r *= r;
+        r *= r;
+        float cost = z.z * invl;
+        float cosp = z.y * invr;
+        float sint = z.x * invl;
+        float sinp = invr / invl;
+        float cost2 = cost * cost;
+        float cosp2 = cosp * cosp;
+        float cost8 = fmaf(fmaf(fmaf(fmaf(128.0f, cost2, -256.0f), cost2, 160.0f), cost2, -32.0f), cost2, 1.0f);
+        float cosp8 = fmaf(fmaf(fmaf(fmaf(128.0f, cosp2, -256.0f), cosp2, 160.0f), cosp2, -32.0f), cosp2, 1.0f);
+        float sint8 = fmaf(fmaf(fmaf(128.0f, cost2, -192.0f), cost2, 80.0f), cost2, -8.0f) * sint * cost;
+        float sinp8 = fmaf(fmaf(fmaf(128.0f, cosp2, -192.0f), cosp2, 80.0f), cosp2, -8.0f) * sinp * cosp;
+        z = scl3(mk3(sint8 * sinp8, cosp8, cost8 * sinp8), r);
+        z = add3(z, p);
+        r = length3(z);
+        if (r > 16.0f) break;
+    }
+    return 0.5f * logf(r) * r / dr;
+}
+/* sdfs/mandelbulb.glsl:54-58 (mix endpoints parameterised) */
+static float mandelbulb_material(vec3 p, const float* m) {
+    float factor = dot3(p, p);
+    return mixf(m[0], m[1], factor / (0.8f + factor));
+}
+
+/* sdfs/menger.glsl:2-23 */
+static float menger_sdf(vec3 p) {
+    vec3 q = sub3(abs3(p), mk3(1.0f, 1.0f, 1.0f));
+    float d = length3(max3(q, mk3(0.0f, 0.0f, 0.0f))) + fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.0f);
+    float s = 1.0f;
+    for (int m = 0; m < 5; m++) {
+        vec3 ps = scl3(p, s);
+        vec3 a = mk3(modf_glsl(ps.x, 2.0f) - 1.0f, modf_glsl(ps.y, 2.0f) - 1.0f, modf_glsl(ps.z, 2.0f) - 1.0f);
+        s *= 3.0f;
+        vec3 r = mk3(fabsf(1.0f - 3.0f * fabsf(a.x)), fabsf(1.0f - 3.0f * fabsf(a.y)), fabsf(1.0f - 3.0f * fabsf(a.z)));
+        float da = fmaxf(r.x, r.y);
+        float db = fmaxf(r.y, r.z);
+        float dc = fmaxf(r.z, r.x);
+        float c = (fminf(da, fminf(db, dc)) - 1.0f) / s;
+        d = fmaxf(d, c);
+    }
+    return d;
+}
+
+/* sdfs/terrain.glsl:1-8 */
+static float terrain_height(float x) {
+    return sinf(0.0625f * x) + sinf(0.125f * (x + 10.0f)) + 0.25f * sinf(0.25f * x) + 0.125f * sinf(0.5f * x) +
+           0.25f * sinf(x) + 0.25f * sinf(2.0f * x + 1.0f) + 0.125f * sinf(4.0f * x + 2.0f) +
+           0.0625f * sinf(8.0f * x + 1.0f) + 0.03125f * sinf(16.0f * x + 5.0f) + 0.015625f * sinf(32.0f * x) +
+           0.0078125f * sinf(64.0f * x);
+}
+static float terrain_sdf(vec3 p) { return p.y - (terrain_height(p.x) + terrain_height(p.z)); }
+
+static float plugin_sdf(const pt_sdf_plugin* pl, vec3 p) {
+    switch (pl->kind) {
+        case PT_SDF_BLOB: return blob_sdf(p);
+        case PT_SDF_MANDELBULB: return mandelbulb_sdf(p);
+        case PT_SDF_MENGER: return menger_sdf(p);
+        case PT_SDF_TERRAIN: return terrain_sdf(p);
+        default: return MAXDIST;
+    }
+}
+static float plugin_material(const pt_sdf_plugin* pl, vec3 p) {
+    if (pl->material_mode == PT_SDFMAT_CONSTANT) return pl->material[0];
+    switch (pl->kind) {
+        case PT_SDF_BLOB: return blob_material(p, pl->material);
+        case PT_SDF_MANDELBULB: return mandelbulb_material(p, pl->material);
+        default: return pl->material[0];
+    }
+}
+
+static inline vec3 sdf_pos(const ctx_t* c, int i) { return mk3(SDFS(c, 6 * i), SDFS(c, 6 * i + 1), SDFS(c, 6 * i + 2)); }
+
+/* SC:706-711 with the code InsertSDF splices in (src/pathtracer.cpp:2004-2054):
+ * for each SDF i in scene order, if bit i of set1 is set: sdf = min(sdf, SDFi(p - pos_i)). */
+static float SDF(const ctx_t* c, vec3 p, uint32_t set1) {
+    float sdf = MAXDIST;
+    int n = c->nplug < PT_MAX_LIVE_SDFS ? c->nplug : PT_MAX_LIVE_SDFS;
+    for (int i = 0; i < n; i++) {
+        uint32_t code = 1u << i;
+        if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
+            sdf = fminf(sdf, plugin_sdf(&c->plug[i], sub3(p, sdf_pos(c, i))));
+        }
+    }
+    return sdf;
+}
+/* SC:713-719 with the spliced lines: material = minMaterial(sdf, SDFi, material, SDFiMATERIAL);
+ * sdf = min(sdf, SDFi) — minMaterial(x,y,m1,m2) = x < y ? m1 : m2 (SC:681-683). */
+static float SDFMATERIAL(const ctx_t* c, vec3 p, uint32_t set1) {
+    float sdf = MAXDIST;
+    float mat = 0.0f;
+    int n = c->nplug < PT_MAX_LIVE_SDFS ? c->nplug : PT_MAX_LIVE_SDFS;
+    for (int i = 0; i < n; i++) {
+        uint32_t code = 1u << i;
+        if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
+            vec3 q = sub3(p, sdf_pos(c, i));
+            float di = plugin_sdf(&c->plug[i], q);
+            mat = (sdf < di) ? mat : plugin_material(&c->plug[i], q);
+            sdf = fminf(sdf, di);
+        }
+    }
+    return mat;
+}
+
+/* SC:721-730 */
+static vec3 CalculateNumericalSDFNormals(const ctx_t* c, vec3 p, uint32_t set1) {
+    float e = 1e-4f;
+    vec3 n = mk3(SDF(c, mk3(p.x + e, p.y + 0.0f, p.z + 0.0f), set1) - SDF(c, mk3(p.x - e, p.y - 0.0f, p.z - 0.0f), set1),
+                 SDF(c, mk3(p.x + 0.0f, p.y + e, p.z + 0.0f), set1) - SDF(c, mk3(p.x - 0.0f, p.y - e, p.z - 0.0f), set1),
+                 SDF(c, mk3(p.x + 0.0f, p.y + 0.0f, p.z + e), set1) - SDF(c, mk3(p.x - 0.0f, p.y - 0.0f, p.z - e), set1));
+    return normalize3(n);
+}
+
+/* SC:732-777 */
+static int SearchSDF(const ctx_t* c, vec3 p, vec3 invdir, vec2* tMinMax, uint32_t* set1) {
+    int found = 0;
+    *set1 = 0;
+    for (int i = 0; (float)i < c->u->numObjects[5]; i++) {
+        vec3 pos = sdf_pos(c, i);
+        vec3 size = mk3(SDFS(c, 6 * i + 3), SDFS(c, 6 * i + 4), SDFS(c, 6 * i + 5));
+        vec2 bm = RayIntersectAABB(p, invdir, pos, size);
+        uint32_t bit = (i < 32) ? (1u << i) : 0u;
+        if ((bm.x > bm.y) || (bm.y < 0.0f)) continue;
+        if (bm.x < tMinMax->x) {
+            found = 1;
+            if (bm.y < tMinMax->x) {
+                *tMinMax = bm;
+                *set1 = bit;
+            } else {
+                if (bm.y < tMinMax->y) {
+                    tMinMax->x = bm.x;
+                    *set1 += bit;
+                } else {
+                    *tMinMax = bm;
+                    *set1 += bit;
+                }
+            }
+        } else {
+            if (bm.x < tMinMax->y) {
+                found = 1;
+                if (bm.y > tMinMax->y) {
+                    tMinMax->y = bm.y;
+                    *set1 += bit;
+                } else {
+                    *set1 += bit;
+                }
+            }
+        }
+    }
+    return found;
+}
+
+/* SC:779-860 */
+static int SphereTracing(const ctx_t* c, Ray ray, hit_t* h) {
+    float t = 1e-3f;
+    float insT = 0.0f;
+    const float omegaMax = 1.70f;
+    const float omegaSpeed = 0.20f;
+    float omega = omegaMax;
+    float omegaSpeedFactor = 0.0f;
+    float previousRadius = 0.0f;
+    vec3 p = ray.origin;
+    vec3 invdir = mk3(1.0f / ray.dir.x, 1.0f / ray.dir.y, 1.0f / ray.dir.z);
+    int points = 0;
+    vec2 tMinMax = mk2(MAXDIST, MAXDIST);
+    uint32_t set1 = 0;
+    if (SearchSDF(c, p, invdir, &tMinMax, &set1)) {
+        t = fmaxf(tMinMax.x, t);
+        p = fma3(ray.dir, mk3(t, t, t), ray.origin);
+    } else {
+        return 0;
+    }
+    float k = signf_glsl(SDF(c, ray.origin, set1));
+    for (int i = 0; i < 512; i++) {
+        float radius = SDF(c, p, set1);
+        if (insT > (fabsf(previousRadius) + fabsf(radius))) {
+            t -= insT;
+            omega = 1.0f;
+            insT = previousRadius * omega * k;
+            t += insT;
+            p = fma3(ray.dir, mk3(t, t, t), ray.origin);
+            continue;
+        }
+        if (fabsf(radius) < 1e-4f) break;
+        if (t > tMinMax.y) {
+            points += 1;
+        } else {
+            points = 0;
+        }
+        if (points >= 2) {
+            t = tMinMax.y + 1e-3f;
+            tMinMax = mk2(MAXDIST, MAXDIST);
+            if (SearchSDF(c, fma3(ray.dir, mk3(t, t, t), ray.origin), invdir, &tMinMax, &set1)) {
+                tMinMax.x += t;
+                tMinMax.y += t;
+                t = fmaxf(tMinMax.x, t);
+                p = fma3(ray.dir, mk3(t, t, t), ray.origin);
+                continue;
+            } else {
+                return 0;
+            }
+        }
+        insT = radius * omega * k;
+        t += insT;
+        p = fma3(ray.dir, mk3(t, t, t), ray.origin);
+        omegaSpeedFactor = fminf(radius / previousRadius, 0.99f);
+        omega += omegaSpeed * (fminf(1.0f / (1.0f - omegaSpeedFactor), omegaMax) - omega);
+        previousRadius = radius;
+    }
+    if (t < h->hitdist) {
+        h->hitdist = t - 1e-3f;
+        p = fma3(ray.dir, mk3(t, t, t), ray.origin);
+        h->normal = CalculateNumericalSDFNormals(c, p, set1);
+        h->materialID = SDFMATERIAL(c, p, set1);
+        h->lightID = -1.0f;
+        return 1;
+    }
+    return 0;
+}
+
+static inline int NUM(const ctx_t* c, int k) { return (int)c->u->numObjects[k]; }
+
+static float lens_bounding_radius(lens_t o) {
+    float br;
+    if (o.isConverging) {
+        br = (o.radius * o.radius) + (0.25f * o.thickness * o.thickness);
+    } else {
+        br = 0.5f * o.thickness + 2.0f * o.focalLength - sqrtf(4.0f * o.focalLength * o.focalLength - o.radius * o.radius);
+        br = br * br + o.radius * o.radius;
+    }
+    return br;
+}
+
+/* SC:862-934 (Intersection) and SC:1121-1223 (LightSourceVisibilityCheck) share
+ * this loop; *objectID receives the index of the last object whose test hit
+ * (-1 for an SDF hit or no hit), as LightSourceVisibilityCheck computes it. */
+static void IntersectAll(const ctx_t* c, Ray ray, hit_t* h, int* objectID) {
+    int offset = 0, objectOffset = 0;
+    int id = -1;
+    for (int i = 0; (float)i < c->u->numObjects[0]; i++) {
+        sphere_t o = UnpackSphere(c, i);
+        if (SphereIntersection(ray, o, h)) id = i;
+    }
+    offset += 6 * NUM(c, 0);
+    objectOffset += NUM(c, 0);
+    for (int i = 0; (float)i < c->u->numObjects[1]; i++) {
+        plane_t o = UnpackPlane(c, i, offset);
+        if (PlaneIntersection(ray, o, h)) id = i + objectOffset;
+    }
+    offset += 5 * NUM(c, 1);
+    objectOffset += NUM(c, 1);
+    for (int i = 0; (float)i < c->u->numObjects[2]; i++) {
+        box_t o = UnpackBox(c, i, offset);
+        if (!BoundingSphere(ray, o.pos, 0.25f * dot3(o.size, o.size))) continue;
+        if (BoxIntersection(ray, o, h)) id = i + objectOffset;
+    }
+    offset += 11 * NUM(c, 2);
+    objectOffset += NUM(c, 2);
+    for (int i = 0; (float)i < c->u->numObjects[3]; i++) {
+        lens_t o = UnpackLens(c, i, offset);
+        int isOutside = 1;
+        if (!BoundingSphere(ray, o.pos, lens_bounding_radius(o))) continue;
+        if (LensIntersection(ray, o, h, &isOutside)) id = i + objectOffset;
+    }
+    offset += 12 * NUM(c, 3);
+    objectOffset += NUM(c, 3);
+    for (int i = 0; (float)i < c->u->numObjects[4]; i++) {
+        cyclide_t o = UnpackCyclide(c, i, offset);
+        if (!BoundingSphere(ray, o.pos, o.brad)) continue;
+        if (DupinCyclide(ray, o, h)) id = i + objectOffset;
+    }
+    if (SphereTracing(c, ray, h)) id = -2; /* SDF */
+    *objectID = id;
+}
+
+/* SC:937-958 */
+uint32_t pto_pcg32(uint32_t seed) {
+    uint32_t state = seed * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+static inline float RandomFloatPCG32(uint32_t* seed) {
+    *seed = pto_pcg32(*seed);
+    return (float)(*seed) / 4294967296.0f; /* float(seed) / float(0xFFFFFFFFu) */
+}
+float pto_random_float(uint32_t* seed) { return RandomFloatPCG32(seed); }
+
+/* SC:976-1028 */
+static vec2 SampleUniformUnitDisk(uint32_t* seed) {
+    float rx = RandomFloatPCG32(seed);
+    float ry = RandomFloatPCG32(seed);
+    float phi = 2.0f * PI_F * ry;
+    float d = sqrtf(rx);
+    return mk2(d * cosf(phi), d * sinf(phi));
+}
+static vec3 SampleUniformUnitSphere(uint32_t* seed) {
+    float rx = RandomFloatPCG32(seed);
+    float ry = RandomFloatPCG32(seed);
+    float phi = 2.0f * PI_F * ry;
+    float sinTheta = 2.0f * rx - 1.0f;
+    float cosTheta = sqrtf(fmaf(-sinTheta, sinTheta, 1.0f));
+    return mk3(cosf(phi) * cosTheta, sinf(phi) * cosTheta, sinTheta);
+}
+static vec3 SampleCosineUnitCone(uint32_t* seed, float cosThetaMax) {
+    float rx = RandomFloatPCG32(seed);
+    float ry = RandomFloatPCG32(seed);
+    float cosAlphaMax = 2.0f * cosThetaMax * cosThetaMax - 1.0f;
+    float phi = 2.0f * PI_F * ry;
+    float cosTheta = (1.0f - cosAlphaMax) * rx + cosAlphaMax;
+    float sinTheta = sqrtf(fmaf(-cosTheta, cosTheta, 1.0f));
+    return normalize3(mk3(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta + 1.0f));
+}
+
+/* SC:1030-1055 */
+static vec4 SpectralPowerDistribution(vec4 l, float l_peak, float d, int invert) {
+    float den = 2.0f * d * d;
+    vec4 x = mk4((l.x - l_peak) / den, (l.y - l_peak) / den, (l.z - l_peak) / den, (l.w - l_peak) / den);
+    vec4 r = mk4(expf(-x.x * x.x), expf(-x.y * x.y), expf(-x.z * x.z), expf(-x.w * x.w));
+    float a = (float)invert;
+    return mk4(mixf(r.x, 1.0f - r.x, a), mixf(r.y, 1.0f - r.y, a), mixf(r.z, 1.0f - r.z, a), mixf(r.w, 1.0f - r.w, a));
+}
+static inline float bb1(float l, float T) {
+    return (1.1910429724e-16f * powf(l, -5.0f)) / (expf(0.014387768775f / (l * T)) - 1.0f);
+}
+static inline float BlackBodyRadiationPeak(float T) { return 4.0956746759e-6f * powf(T, 5.0f); }
+static vec4 Emit(vec4 l, light_t lt) {
+    float temperature = fmaxf(lt.x, 0.0f);
+    vec4 lm = scl4(l, 1e-9f);
+    float peak = BlackBodyRadiationPeak(temperature);
+    vec4 e = mk4(bb1(lm.x, temperature) / peak, bb1(lm.y, temperature) / peak, bb1(lm.z, temperature) / peak,
+                 bb1(lm.w, temperature) / peak);
+    return scl4(e, fmaxf(lt.y, 0.0f));
+}
+void pto_blackbody(const float* l_m, float T, float* out4) {
+    for (int i = 0; i < 4; i++) out4[i] = bb1(l_m[i], T);
+}
+float pto_blackbody_peak(float T) { return BlackBodyRadiationPeak(T); }
+
+/* SC:1064-1073 */
+static float RefractiveIndexBK7Glass(float l) {
+    l *= 1e-3f;
+    float l2 = l * l;
+    float n2 = 1.0f;
+    n2 += (1.03961212f * l2) / (l2 - 6.00069867e-3f);
+    n2 += (0.231792344f * l2) / (l2 - 2.00179144e-2f);
+    n2 += (1.01046945f * l2) / (l2 - 1.03560653e2f);
+    return sqrtf(n2);
+}
+float pto_bk7_index(float l) { return RefractiveIndexBK7Glass(l); }
+
+/* SC:1075-1080 */
+static vec4 EvaluateBRDF(vec4 l, material_t mat) {
+    vec4 s = SpectralPowerDistribution(l, mat.reflection.x, mat.reflection.y, (int)mat.reflection.z);
+    return div4s(s, PI_F);
+}
+
+/* SC:1093-1119 */
+static vec3 ToWorld(vec3 v, vec3 n) {
+    vec3 b1 = mk3(0.0f, -1.0f, 0.0f);
+    vec3 b2 = mk3(-1.0f, 0.0f, 0.0f);
+    if (n.z >= -0.9999999f) {
+        float a = 1.0f / (1.0f + n.z);
+        float b = -n.x * n.y * a;
+        b1 = mk3(1.0f - (n.x * n.x * a), b, -n.x);
+        b2 = mk3(b, 1.0f - (n.y * n.y * a), -n.y);
+    }
+    return add3(add3(scl3(b1, v.x), scl3(b2, v.y)), scl3(n, v.z));
+}
+
+/* SC:1225-1285 */
+static int SampleRandomLightSource(ctx_t* c, uint32_t* seed, float* boundingRadius, vec3* pos, float* lightID) {
+    int randomLight = (int)floorf(RandomFloatPCG32(seed) * c->u->numObjects[6]);
+    c->light_pick = randomLight;
+    int randomLightID = (int)LIGHTIDS(c, randomLight);
+    int offset = 0;
+    if (randomLightID < NUM(c, 0)) {
+        sphere_t o = UnpackSphere(c, randomLightID);
+        *boundingRadius = o.radius;
+        *pos = o.pos;
+        *lightID = (float)o.lightID;
+        return (int)LIGHTIDS(c, randomLight);
+    }
+    randomLightID -= NUM(c, 0);
+    offset += 6 * NUM(c, 0);
+    if (randomLightID < NUM(c, 1)) {
+        plane_t o = UnpackPlane(c, randomLightID, offset);
+        *boundingRadius = 1e5f;
+        *pos = o.pos;
+        *lightID = (float)o.lightID;
+        return (int)LIGHTIDS(c, randomLight);
+    }
+    randomLightID -= NUM(c, 1);
+    offset += 5 * NUM(c, 1);
+    if (randomLightID < NUM(c, 2)) {
+        box_t o = UnpackBox(c, randomLightID, offset);
+        *boundingRadius = 0.5f * length3(o.size);
+        *pos = o.pos;
+        *lightID = (float)o.lightID;
+        return (int)LIGHTIDS(c, randomLight);
+    }
+    randomLightID -= NUM(c, 2);
+    offset += 11 * NUM(c, 2);
+    if (randomLightID < NUM(c, 2)) { /* SC:1264 compares with numObjects[2] */
+        lens_t o = UnpackLens(c, randomLightID, offset);
+        *boundingRadius = sqrtf((o.radius * o.radius) + (0.25f * o.thickness * o.thickness));
+        *pos = o.pos;
+        *lightID = (float)o.lightID;
+        return (int)LIGHTIDS(c, randomLight);
+    }
+    randomLightID -= NUM(c, 3);
+    offset += 12 * NUM(c, 3);
+    if (randomLightID < NUM(c, 3)) { /* SC:1275 compares with numObjects[3] */
+        cyclide_t o = UnpackCyclide(c, randomLightID, offset);
+        *boundingRadius = sqrtf(o.brad);
+        *pos = o.pos;
+        *lightID = (float)o.lightID;
+        return (int)LIGHTIDS(c, randomLight);
+    }
+    return 0;
+}
+
+/* SC:1121-1223 */
+static int LightSourceVisibilityCheck(const ctx_t* c, Ray ray, int lightObjectID) {
+    hit_t h;
+    h.hitdist = MAXDIST;
+    h.normal = mk3(0.0f, 0.0f, 0.0f);
+    h.materialID = 0.0f;
+    h.lightID = -1.0f;
+    int objectID = -1;
+    IntersectAll(c, ray, &h, &objectID);
+    if (objectID == -2) objectID = -1;
+    return objectID == lightObjectID;
+}
+
+static inline float MISPowerHeuristicsBeta2(float pdf1, float pdf2) { return pdf1 * pdf1 / (pdf1 * pdf1 + pdf2 * pdf2); }
+
+/* SC:1298-1343 */
+static vec4 SampleLightSource(ctx_t* c, vec4 l, vec4 rayradiance, vec3 outOrigin, vec3 normal, material_t mat,
+                              uint32_t* seed, float BRDFpdf, float* MISBRDFWeight) {
+    float boundingRadius = 0.0f;
+    vec3 lightPos = mk3(0.0f, 0.0f, 0.0f);
+    float lightIDOut = -1.0f;
+    int lightObjectID = 0;
+    float lightpdf = 0.0f;
+    c->shadow_state = 0;
+    c->light_pick = 0;
+    if (c->u->numObjects[6] > 0.0f) {
+        lightObjectID = SampleRandomLightSource(c, seed, &boundingRadius, &lightPos, &lightIDOut);
+        vec3 toL = sub3(lightPos, outOrigin);
+        float invLightDistance = 1.0f / length3(toL);
+        vec3 lightDir = scl3(sub3(lightPos, outOrigin), invLightDistance);
+        float sinthetaMax = fminf(boundingRadius * invLightDistance, 1.0f);
+        float costhetaMax = sqrtf(1.0f - sinthetaMax * sinthetaMax);
+        Ray outRay;
+        outRay.origin = outOrigin;
+        outRay.dir = ToWorld(SampleCosineUnitCone(seed, costhetaMax), lightDir);
+        lightpdf = 1.0f / c->u->numObjects[6];
+        lightpdf *= dot3(outRay.dir, lightDir) / (PI_F * (1.0f - costhetaMax * costhetaMax));
+        *MISBRDFWeight = MISPowerHeuristicsBeta2(BRDFpdf, lightpdf);
+        float costheta = dot3(outRay.dir, normal);
+        float deathProbability = 1.25f * fmaxf(*MISBRDFWeight - 0.2f, 0.0f);
+        if (costheta >= 0.0f) {
+            if (RandomFloatPCG32(seed) > deathProbability) {
+                int vis = LightSourceVisibilityCheck(c, outRay, lightObjectID);
+                c->shadow_state = vis ? 3 : 2;
+                if (vis) {
+                    light_t lt = GetLightMix(c, lightIDOut);
+                    vec4 brdf = EvaluateBRDF(l, mat);
+                    vec4 f = div4s(scl4(brdf, costheta), lightpdf);
+                    rayradiance = mul4(rayradiance, f);
+                    return scl4(mul4(Emit(l, lt), rayradiance), 1.0f - *MISBRDFWeight);
+                }
+            } else {
+                *MISBRDFWeight = 1.0f;
+                c->shadow_state = 1;
+            }
+        }
+        return s4(0.0f);
+    }
+    *MISBRDFWeight = MISPowerHeuristicsBeta2(BRDFpdf, lightpdf);
+    return s4(0.0f);
+}
+
+/* SC:1345-1391; *event receives the trace word of this bounce. */
+static vec4 TraceRay(ctx_t* c, vec4 l, vec4* rayradiance, Ray* inRay, uint32_t* seed, float* MISBRDFWeight,
+                     int* isTerminate, uint32_t* event) {
+    vec4 radiance = s4(0.0f);
+    hit_t h;
+    h.hitdist = MAXDIST;
+    h.normal = mk3(0.0f, 0.0f, 0.0f);
+    h.materialID = 0.0f;
+    h.lightID = -1.0f;
+    int objectID = -1;
+    IntersectAll(c, *inRay, &h, &objectID);
+    float hitdist = h.hitdist;
+    material_t mat = GetMaterialMix(c, h.materialID);
+    light_t lt = GetLightMix(c, h.lightID);
+    uint32_t ev = PT_EV_VALID;
+    if (hitdist < MAXDIST) {
+        ev |= (objectID == -2) ? PT_EV_HIT_SDF : (uint32_t)(objectID & 0xFFF);
+        if (lt.y > 0.0f) {
+            radiance = scl4(mul4(Emit(l, lt), *rayradiance), *MISBRDFWeight);
+            *isTerminate = 1;
+            *event = ev | PT_EV_EMITTER;
+            return radiance;
+        }
+        Ray outRay;
+        outRay.origin = fma3(inRay->dir, mk3(hitdist, hitdist, hitdist), inRay->origin);
+        outRay.dir = normalize3(add3(h.normal, SampleUniformUnitSphere(seed)));
+        float BRDFpdf = dot3(outRay.dir, h.normal) / PI_F;
+        radiance = SampleLightSource(c, l, *rayradiance, outRay.origin, h.normal, mat, seed, BRDFpdf, MISBRDFWeight);
+        ev |= ((uint32_t)(c->light_pick & 0x7F) << PT_EV_LIGHT_SHIFT) | ((uint32_t)c->shadow_state << PT_EV_SHADOW_SHIFT);
+        float costheta = dot3(outRay.dir, h.normal);
+        vec4 brdf = EvaluateBRDF(l, mat);
+        vec4 f = div4s(scl4(brdf, costheta), BRDFpdf);
+        *rayradiance = mul4(*rayradiance, f);
+        vec4 rr = *rayradiance;
+        float rp = fminf(fmaxf(fmaxf(rr.x, fmaxf(rr.y, fmaxf(rr.z, rr.w))), 0.0f), 0.99f);
+        if (RandomFloatPCG32(seed) > rp) {
+            *isTerminate = 1;
+            *event = ev | PT_EV_RR_KILL;
+            return radiance;
+        }
+        *rayradiance = scl4(*rayradiance, 1.0f / rp);
+        *inRay = outRay;
+    } else {
+        ev |= PT_EV_HIT_MISS;
+        *isTerminate = 1;
+    }
+    *event = ev;
+    return radiance;
+}
+
+/* SC:1393-1407 */
+static vec4 TracePath(ctx_t* c, vec4 l, Ray ray, uint32_t* seed, uint32_t* events, int depth_cap, uint32_t* nev) {
+    vec4 radiance = s4(0.0f);
+    vec4 rayradiance = s4(1.0f);
+    float MISBRDFWeight = 1.0f;
+    int isTerminate = 0;
+    int n = 0;
+    for (int i = 0; i < c->pc->pathLength; i++) {
+        uint32_t ev = 0;
+        radiance = add4(radiance, TraceRay(c, l, &rayradiance, &ray, seed, &MISBRDFWeight, &isTerminate, &ev));
+        if (events && n < depth_cap) events[n] = ev;
+        n++;
+        if (isTerminate) break;
+    }
+    if (nev) *nev = (uint32_t)n;
+    return radiance;
+}
+
+/* SC:1409-1444 */
+static void TracePathLens(const ctx_t* c, float l, Ray* ray, vec3 forwardDir) {
+    const pt_push* pc = c->pc;
+    lens_t o;
+    o.radius = pc->lensRadius;
+    o.focalLength = pc->lensFocalLength;
+    o.thickness = pc->lensThickness;
+    o.isConverging = 1;
+    o.pos = add3(c->cameraPos, scl3(forwardDir, pc->lensDistance));
+    o.rotation = mk3(0.0f, 90.0f - pc->cameraAngle[1], pc->cameraAngle[0]);
+    o.materialID = 0;
+    o.lightID = 0;
+    for (int i = 0; i < 2; i++) {
+        hit_t h;
+        h.hitdist = 1e6f;
+        h.normal = mk3(0.0f, 0.0f, 0.0f);
+        h.materialID = 0.0f;
+        h.lightID = -1.0f;
+        int isOutside = 1;
+        LensIntersection(*ray, o, &h, &isOutside);
+        float n1, n2;
+        if (isOutside == 1) {
+            n1 = 1.0f;
+            n2 = RefractiveIndexBK7Glass(l);
+        } else {
+            n1 = RefractiveIndexBK7Glass(l);
+            n2 = 1.0f;
+        }
+        float n12 = n1 / n2;
+        l = l * n12;
+        ray->origin = fma3(ray->dir, mk3(h.hitdist, h.hitdist, h.hitdist), ray->origin);
+        ray->dir = refract3(ray->dir, h.normal, n12);
+    }
+}
+
+/* SC:1446-1490 */
+static vec3 Scene(ctx_t* c, uint32_t xx, uint32_t xy_y, vec2 uv, int k, uint32_t* events, int depth_cap, uint32_t* nev) {
+    const pt_push* pc = c->pc;
+    uint32_t seed = pto_generate_seed(xx, xy_y, pc->frame, pc->samplesPerFrame, k, pc->resolution[0]);
+    float jx = 2.0f * RandomFloatPCG32(&seed) - 0.5f;
+    float jy = 2.0f * RandomFloatPCG32(&seed) - 0.5f;
+    uv.x += jx / (float)pc->resolution[0];
+    uv.y += jy / (float)pc->resolution[1];
+    mat3 m = RotationMatrix(mk3(pc->cameraAngle[0], pc->cameraAngle[1], 0.0f));
+    float sc = -pc->cameraSize * 0.5f;
+    uv.x *= sc;
+    uv.y *= sc;
+    Ray ray;
+    ray.origin = add3(c->cameraPos, vec_mul_mat(mk3(uv.x, uv.y, 0.0f), m));
+    vec2 disk = SampleUniformUnitDisk(&seed);
+    float ha = 0.5f * pc->apertureSize;
+    vec3 pointOnAperture = add3(c->cameraPos, vec_mul_mat(mk3(ha * disk.x, ha * disk.y, pc->apertureDist), m));
+    ray.dir = normalize3(sub3(pointOnAperture, ray.origin));
+    vec3 forwardDir = mk3(m.c0.z, m.c1.z, m.c2.z);
+    float rh = RandomFloatPCG32(&seed);
+    float l_h = mixf(360.0f, 800.0f, rh);
+    TracePathLens(c, l_h, &ray, forwardDir);
+    /* SampleWavelengths SC:971-974 */
+    float base = l_h - 390.0f;
+    vec4 l = mk4(390.0f + modf_glsl(base + 82.5f, 330.0f), 390.0f + modf_glsl(base + 165.0f, 330.0f),
+                 390.0f + modf_glsl(base + 247.5f, 330.0f), 390.0f + modf_glsl(base + 330.0f, 330.0f));
+    vec4 radiance = TracePath(c, l, ray, &seed, events, depth_cap, nev);
+    vec3 wx = WaveToXYZ(c, l.x), wy = WaveToXYZ(c, l.y), wz = WaveToXYZ(c, l.z), ww = WaveToXYZ(c, l.w);
+    vec3 sum = add3(add3(add3(scl3(wx, radiance.x), scl3(wy, radiance.y)), scl3(wz, radiance.z)), scl3(ww, radiance.w));
+    vec3 color = scl3(scl3(sum, 720.0f - 390.0f), 0.25f);
+    if (color.x != color.x) return mk3(0.0f, 0.0f, 0.0f);
+    if (color.y != color.y) return mk3(0.0f, 0.0f, 0.0f);
+    if (color.z != color.z) return mk3(0.0f, 0.0f, 0.0f);
+    return color;
+}
+
+uint32_t pto_generate_seed(uint32_t x, uint32_t y, int frame, int spf, int k, int width) {
+    uint32_t seed = (uint32_t)(frame - spf + k);
+    seed = pto_pcg32(seed);
+    seed += x + (uint32_t)width * y;
+    return seed;
+}
+
+void pto_wave_to_xyz(const float* cie, float wave, float* out3) {
+    pt_ubo* u = (pt_ubo*)calloc(1, sizeof(pt_ubo));
+    memcpy(u->CIEXYZ1931, cie, sizeof(u->CIEXYZ1931));
+    ctx_t c;
+    memset(&c, 0, sizeof(c));
+    c.u = u;
+    vec3 r = WaveToXYZ(&c, wave);
+    out3[0] = r.x;
+    out3[1] = r.y;
+    out3[2] = r.z;
+    free(u);
+}
+
+float pto_sdf_eval(const pt_sdf_plugin* pl, const float* p) { return plugin_sdf(pl, mk3(p[0], p[1], p[2])); }
+float pto_sdf_material(const pt_sdf_plugin* pl, const float* p) { return plugin_material(pl, mk3(p[0], p[1], p[2])); }
+
+/* SC:1492-1533 */
+int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plugins, int nplugins, float* accum,
+                 int x0, int y0, int x1, int y1, const pto_trace* trace, int nthreads) {
+    if (!ubo || !pc || !accum) return PT_ERR_INVALID;
+    const int W = pc->resolution[0], H = pc->resolution[1];
+    if (W <= 0 || H <= 0 || pc->samplesPerFrame <= 0) return PT_ERR_INVALID;
+    if (x0 < 0 || y0 < 0 || x1 > W || y1 > H || x0 > x1 || y0 > y1) return PT_ERR_INVALID;
+    if (nplugins < 0 || (nplugins > 0 && !plugins)) return PT_ERR_INVALID;
+    const int spf = pc->samplesPerFrame;
+    const int rw = x1 - x0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = y0; y < y1; y++) {
+        ctx_t c;
+        memset(&c, 0, sizeof(c));
+        c.u = ubo;
+        c.pc = pc;
+        c.plug = plugins;
+        c.nplug = nplugins;
+        c.cameraPos = mk3(pc->cameraPosX, pc->cameraPosY, pc->cameraPosZ);
+        for (int x = x0; x < x1; x++) {
+            size_t coords = (size_t)x + (size_t)W * (size_t)y;
+            float* px = accum + 4 * coords;
+            vec3 inColor = mk3(px[0], px[1], px[2]);
+            /* Rendering SC:1509-1523 */
+            uint32_t xx = (uint32_t)x;
+            uint32_t yy = (uint32_t)H - (uint32_t)y;
+            vec2 uv = mk2((2.0f * (float)xx - (float)W) / (float)H, (2.0f * (float)yy - (float)H) / (float)H);
+            vec3 outColor = mk3(0.0f, 0.0f, 0.0f);
+            for (int i = 0; i < spf; i++) {
+                size_t pidx = ((size_t)(y - y0) * (size_t)rw + (size_t)(x - x0)) * (size_t)spf + (size_t)i;
+                uint32_t* ev = NULL;
+                uint32_t* nev = NULL;
+                int cap = 0;
+                if (trace && trace->events) {
+                    ev = trace->events + pidx * (size_t)trace->depth_cap;
+                    cap = trace->depth_cap;
+                }
+                if (trace && trace->nevents) nev = trace->nevents + pidx;
+                vec3 col = Scene(&c, xx, yy, uv, i, ev, cap, nev);
+                if (trace && trace->colors) {
+                    trace->colors[pidx * 3 + 0] = col.x;
+                    trace->colors[pidx * 3 + 1] = col.y;
+                    trace->colors[pidx * 3 + 2] = col.z;
+                }
+                outColor = add3(outColor, col);
+            }
+            float fs = (float)spf;
+            outColor = mk3(outColor.x / fs, outColor.y / fs, outColor.z / fs);
+            outColor = scl3(outColor, pc->apertureSize * pc->apertureSize * (float)pc->ISO);
+            /* Accumulate SC:1492-1507 */
+            if ((pc->currentSamples == pc->samplesPerFrame) && (pc->frame > pc->samplesPerFrame)) {
+                float weight = powf(2.0f, -8.0f / (pc->FPS * pc->persistence));
+                outColor = add3(scl3(outColor, 1.0f - weight), scl3(inColor, weight));
+            } else {
+                int unitSamples = pc->currentSamples / pc->samplesPerFrame;
+                float us = (float)unitSamples;
+                vec3 t = add3(scl3(inColor, (float)(unitSamples - 1)), outColor);
+                outColor = mk3(t.x / us, t.y / us, t.z / us);
+            }
+            px[0] = outColor.x;
+            px[1] = outColor.y;
+            px[2] = outColor.z;
+            px[3] = 1.0f;
+        }
+    }
+    return PT_OK;
+}

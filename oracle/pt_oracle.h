@@ -1,0 +1,57 @@
+/*
+ * pt_oracle.h — CPU restatement of the reference's per-pixel spectral
+ * path-tracing kernel (src/shader.comp) for checking libpt_cuda.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this
+ * library; only the tests, the smoke check and the CPU-baseline leg of the
+ * benchmark load it, as the checker.
+ *
+ * Parity status: the reference has no tests, golden vectors or images, and
+ * it cannot run on these machines (Vulkan + Windows), so this restatement is
+ * "parity unpinned" against the reference itself.  Its primitives are pinned
+ * by known-answer values derived from the reference's formulas (PCG32 hash,
+ * seeds, BK7 index, blackbody peak); see tests/test_oracle_kat.py.
+ */
+#ifndef PT_ORACLE_H
+#define PT_ORACLE_H
+
+#include <stdint.h>
+#include "../include/pt_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pto_trace {
+    int depth_cap;      /* event words stored per path */
+    uint32_t* events;   /* [npaths * depth_cap] */
+    uint32_t* nevents;  /* [npaths] */
+    float* colors;      /* [npaths * 3] */
+} pto_trace;
+
+/*
+ * Runs the shader's main() (src/shader.comp:1525-1533) for every invocation
+ * (x, y) in [x0, x1) x [y0, y1), reading and writing `accum` (W*H float4,
+ * index x + W*y).  Path index for the trace is
+ * ((y - y0) * (x1 - x0) + (x - x0)) * samplesPerFrame + k.
+ * nthreads <= 0 uses all OpenMP threads.  Returns 0 or an error code.
+ */
+int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plugins, int nplugins,
+                 float* accum, int x0, int y0, int x1, int y1, const pto_trace* trace, int nthreads);
+
+/* Primitives exposed for known-answer tests. */
+uint32_t pto_pcg32(uint32_t seed);
+float pto_random_float(uint32_t* seed);
+uint32_t pto_generate_seed(uint32_t x, uint32_t y, int frame, int spf, int k, int width);
+float pto_bk7_index(float wavelength_nm);
+void pto_blackbody(const float* l_m, float T, float* out4);
+float pto_blackbody_peak(float T);
+float pto_sdf_eval(const pt_sdf_plugin* plugin, const float* p3);
+float pto_sdf_material(const pt_sdf_plugin* plugin, const float* p3);
+void pto_wave_to_xyz(const float* cie, float wave, float* out3);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,112 @@
+"""Builds the native libraries in-tree: libpt_cuda.so (nvcc, sm_103a) and
+libpt_host.so (g++), into pathtracer_gb300/lib/.
+
+No cmake: each library is one compiler invocation, and the independent ones
+run in parallel.  Kernels are compiled with -fmad=false (every a*b+c stays
+two roundings, as the shader's expressions are written; fma only where the
+shader says fma) and IEEE division and square root (nvcc's defaults).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(PKG, "lib")
+
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-shared"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", "-Wextra"]
+
+CUDA_SOURCES = [
+    "kernel/pt_megakernel.cu",
+    "pt_api.cu",
+    "pt_sdf_source.cpp",
+]
+HOST_SOURCES = [
+    "host/pt_json.cpp",
+    "host/pt_scene.cpp",
+    "host/pt_offscreen.cpp",
+]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: libpt_cuda needs the CUDA toolkit")
+
+
+def _cuda_home(nvcc: str) -> str:
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+
+
+def _run(cmd: list[str]) -> None:
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"build failed ({proc.returncode}): {' '.join(cmd)}\n{proc.stdout}")
+
+
+def _stale(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    deps = list(sources)
+    for d in (os.path.join(CSRC, "kernel"), os.path.join(CSRC, "host"), os.path.join(ROOT, "include")):
+        deps += [os.path.join(d, f) for f in os.listdir(d)]
+    return any(os.path.getmtime(s) > t for s in deps if os.path.isfile(s))
+
+
+def build(force: bool = False, verbose: bool = False) -> dict[str, str]:
+    """Compiles both libraries (if stale) and returns their paths."""
+    os.makedirs(LIB, exist_ok=True)
+    nvcc = _nvcc()
+    cuda_inc = os.path.join(_cuda_home(nvcc), "include")
+    cuda_so = os.path.join(LIB, "libpt_cuda.so")
+    host_so = os.path.join(LIB, "libpt_host.so")
+    cuda_src = [os.path.join(CSRC, s) for s in CUDA_SOURCES]
+    host_src = [os.path.join(CSRC, s) for s in HOST_SOURCES]
+
+    cuda_cmd = [nvcc, *NVCC_FLAGS, "-o", cuda_so, *cuda_src]
+    host_cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, f"-I{cuda_inc}", "-o", host_so, *host_src,
+                f"-L{LIB}", "-lpt_cuda", "-Wl,-rpath,$ORIGIN"]
+
+    if force or _stale(cuda_so, cuda_src):
+        if verbose:
+            print(" ".join(cuda_cmd), file=sys.stderr)
+        _run(cuda_cmd)
+    if force or _stale(host_so, host_src) or os.path.getmtime(cuda_so) > os.path.getmtime(host_so):
+        if verbose:
+            print(" ".join(host_cmd), file=sys.stderr)
+        _run(host_cmd)
+    return {"cuda": cuda_so, "host": host_so}
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compiles the CPU restatement used by the tests (oracle/, the checker)."""
+    out = os.path.join(ROOT, "oracle", "_build", "libpt_oracle.so")
+    src = os.path.join(ROOT, "oracle", "pt_oracle.c")
+    hdrs = [os.path.join(ROOT, "oracle", "pt_oracle.h"), os.path.join(ROOT, "include", "pt_cuda.h")]
+    if force or not os.path.exists(out) or any(os.path.getmtime(s) > os.path.getmtime(out) for s in [src, *hdrs]):
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        _run([os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fno-fast-math",
+              "-fopenmp", "-shared", "-o", out, src, "-lm"])
+    return out
+
+
+def build_all(force: bool = False) -> dict[str, str]:
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        fo = ex.submit(build_oracle, force)
+        fl = ex.submit(build, force)
+        paths = fl.result()
+        paths["oracle"] = fo.result()
+    return paths
+
+
+if __name__ == "__main__":
+    print(build_all(force="--force" in sys.argv))

@@ -1,0 +1,18 @@
+// pt_megakernel.h — host entry points of the megakernel translation unit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pt_scene.cuh"
+
+// Block shape of the plain megakernel: 16 x 8 pixels, one warp = 16 x 2 pixels.
+#define PT_MK_BLOCK_X 16
+#define PT_MK_BLOCK_Y 8
+#define PT_MK_THREADS (PT_MK_BLOCK_X * PT_MK_BLOCK_Y)
+
+// Writes 9 floats per object (column-major RotationMatrix of its rotation;
+// identity for spheres and planes) to d_out[9 * total_objects].
+cudaError_t ptk_rotation_setup(const KScene* scene, float* d_out, cudaStream_t stream);
+
+// One dispatch of the plain megakernel over params->pc.resolution.
+cudaError_t ptk_launch_megakernel(const KParams* params, bool trace, cudaStream_t stream);

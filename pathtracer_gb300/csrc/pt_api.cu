@@ -1,0 +1,292 @@
+// pt_api.cu — the C ABI of libpt_cuda (include/pt_cuda.h).
+//
+// A context stands in for the reference's Vulkan device, compute pipeline,
+// uniform buffer, texel buffer and fence (src/pathtracer.cpp:1227-2423,
+// 3586-3608, 3843-3880).  It owns its device memory and one stream; nothing
+// here is process-global, so contexts may coexist on one device.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+
+#include "../../include/pt_cuda.h"
+#include "kernel/pt_megakernel.h"
+
+struct pt_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    KParams* params = nullptr;  // host image of the launch parameters
+    bool has_scene = false;
+    float* d_cie = nullptr;
+    float* d_rot = nullptr;
+    float4* d_accum = nullptr;
+    int width = 0, height = 0;
+    pt_sdf_plugin plug[PT_MAX_LIVE_SDFS];
+    int nplug = 0;
+    KTrace trace{nullptr, nullptr, nullptr, 0};
+    std::string err;
+};
+
+namespace {
+
+int fail(pt_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_fail(pt_ctx* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(ctx, e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA, m);
+}
+
+#define PT_CUDA_TRY(ctx, call)                                   \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+bool integral_count(float v, int max, int* out) {
+    if (!(v >= 0.0f) || v > (float)max || std::floor(v) != v) return false;
+    *out = (int)v;
+    return true;
+}
+
+void refresh_plugins(pt_ctx* ctx) {
+    std::memset(ctx->params->s.plug, 0, sizeof(ctx->params->s.plug));
+    std::memcpy(ctx->params->s.plug, ctx->plug, sizeof(pt_sdf_plugin) * (size_t)ctx->nplug);
+    ctx->params->s.meta.nplug = ctx->nplug;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_create(pt_ctx** out, int device) {
+    if (!out) return PT_ERR_INVALID;
+    *out = nullptr;
+    pt_ctx* ctx = new (std::nothrow) pt_ctx();
+    if (!ctx) return PT_ERR_OOM;
+    ctx->params = new (std::nothrow) KParams();
+    if (!ctx->params) {
+        delete ctx;
+        return PT_ERR_OOM;
+    }
+    std::memset(ctx->params, 0, sizeof(KParams));
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_cie, sizeof(float) * PT_CIE_TABLE_SIZE);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rot, sizeof(float) * 9 * PT_MAX_SCENE_OBJECTS);
+    if (e != cudaSuccess) {
+        pt_destroy(ctx);
+        return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return PT_OK;
+}
+
+int pt_destroy(pt_ctx* ctx) {
+    if (!ctx) return PT_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_accum) cudaFree(ctx->d_accum);
+    if (ctx->d_cie) cudaFree(ctx->d_cie);
+    if (ctx->d_rot) cudaFree(ctx->d_rot);
+    if (ctx->done) cudaEventDestroy(ctx->done);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx->params;
+    delete ctx;
+    return PT_OK;
+}
+
+int pt_set_sdf_plugins(pt_ctx* ctx, const pt_sdf_plugin* plugins, int n) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (n < 0 || (n > 0 && !plugins)) return fail(ctx, PT_ERR_INVALID, "pt_set_sdf_plugins: bad plug-in array");
+    if (n > PT_MAX_LIVE_SDFS)
+        return fail(ctx, PT_ERR_UNSUPPORTED, "pt_set_sdf_plugins: at most 32 SDFs can be evaluated (32-bit set mask)");
+    for (int i = 0; i < n; i++) {
+        if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_TERRAIN)
+            return fail(ctx, PT_ERR_INVALID, "pt_set_sdf_plugins: unknown plug-in kind");
+    }
+    if (n > 0) std::memcpy(ctx->plug, plugins, sizeof(pt_sdf_plugin) * (size_t)n);
+    ctx->nplug = n;
+    refresh_plugins(ctx);
+    return PT_OK;
+}
+
+int pt_set_sdfs(pt_ctx* ctx, const char* const* sources, int n) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (n < 0 || (n > 0 && !sources)) return fail(ctx, PT_ERR_INVALID, "pt_set_sdfs: bad source array");
+    if (n > PT_MAX_LIVE_SDFS)
+        return fail(ctx, PT_ERR_UNSUPPORTED, "pt_set_sdfs: at most 32 SDFs can be evaluated (32-bit set mask)");
+    pt_sdf_plugin tmp[PT_MAX_LIVE_SDFS];
+    for (int i = 0; i < n; i++) {
+        const int rc = pt_parse_sdf_source(sources[i], &tmp[i]);
+        if (rc != PT_OK) {
+            char buf[160];
+            std::snprintf(buf, sizeof buf,
+                          "pt_set_sdfs: SDF %d is neither a recognised plug-in snippet nor a builtin: spec", i);
+            return fail(ctx, rc, buf);
+        }
+    }
+    return pt_set_sdf_plugins(ctx, tmp, n);
+}
+
+int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!ubo) return fail(ctx, PT_ERR_INVALID, "pt_upload_scene: null ubo");
+    int n[7];
+    const int caps[7] = {PT_MAX_OBJECTS_SIZE / 6, PT_MAX_OBJECTS_SIZE / 5, PT_MAX_OBJECTS_SIZE / 11,
+                         PT_MAX_OBJECTS_SIZE / 12, PT_MAX_OBJECTS_SIZE / 16, PT_MAX_SDFS_SIZE / 6,
+                         PT_MAX_LIGHTIDS_SIZE};
+    for (int i = 0; i < 7; i++) {
+        if (!integral_count(ubo->numObjects[i], caps[i], &n[i]))
+            return fail(ctx, PT_ERR_INVALID, "pt_upload_scene: numObjects[" + std::to_string(i) + "] is not a valid count");
+    }
+    const int floats = 6 * n[0] + 5 * n[1] + 11 * n[2] + 12 * n[3] + 16 * n[4];
+    if (floats > PT_MAX_OBJECTS_SIZE)
+        return fail(ctx, PT_ERR_INVALID, "pt_upload_scene: objects overflow the 1024-float object array");
+    if (n[5] > PT_MAX_LIVE_SDFS)
+        return fail(ctx, PT_ERR_UNSUPPORTED, "pt_upload_scene: at most 32 SDFs can be evaluated (32-bit set mask)");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+
+    KScene& S = ctx->params->s;
+    std::memcpy(S.numObjects, ubo->numObjects, sizeof(S.numObjects));
+    std::memcpy(S.objects, ubo->objects, sizeof(S.objects));
+    std::memcpy(S.sdfs, ubo->sdfs, sizeof(S.sdfs));
+    std::memcpy(S.materials, ubo->materials, sizeof(S.materials));
+    std::memcpy(S.lights, ubo->lights, sizeof(S.lights));
+    std::memcpy(S.lightIDs, ubo->lightIDs, sizeof(S.lightIDs));
+    for (int i = 0; i < 7; i++) S.meta.n[i] = n[i];
+    S.meta.offset[0] = 0;
+    S.meta.offset[1] = 6 * n[0];
+    S.meta.offset[2] = S.meta.offset[1] + 5 * n[1];
+    S.meta.offset[3] = S.meta.offset[2] + 11 * n[2];
+    S.meta.offset[4] = S.meta.offset[3] + 12 * n[3];
+    S.meta.total_objects = n[0] + n[1] + n[2] + n[3] + n[4];
+    refresh_plugins(ctx);
+
+    PT_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_cie, ubo->CIEXYZ1931, sizeof(float) * PT_CIE_TABLE_SIZE,
+                                     cudaMemcpyHostToDevice, ctx->stream));
+    // Derive the rotation matrices on the device (the kernel's own sin/cos),
+    // then carry them in the launch parameters.
+    std::memset(S.rot, 0, sizeof(S.rot));
+    if (S.meta.total_objects > 0) {
+        PT_CUDA_TRY(ctx, ptk_rotation_setup(&S, ctx->d_rot, ctx->stream));
+        PT_CUDA_TRY(ctx, cudaMemcpyAsync(S.rot, ctx->d_rot, sizeof(float) * 9 * (size_t)S.meta.total_objects,
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->has_scene = true;
+    return PT_OK;
+}
+
+int pt_resize_accum(pt_ctx* ctx, int width, int height) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (width <= 0 || height <= 0 || (long long)width * (long long)height > (1ll << 31))
+        return fail(ctx, PT_ERR_INVALID, "pt_resize_accum: bad size");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->d_accum) {
+        cudaFree(ctx->d_accum);
+        ctx->d_accum = nullptr;
+        ctx->width = ctx->height = 0;
+    }
+    const size_t bytes = (size_t)width * (size_t)height * sizeof(float4);
+    PT_CUDA_TRY(ctx, cudaMalloc(&ctx->d_accum, bytes));
+    PT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_accum, 0, bytes, ctx->stream));
+    ctx->width = width;
+    ctx->height = height;
+    return PT_OK;
+}
+
+int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_colors, int depth_cap) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (depth_cap < 0 || (d_events && depth_cap == 0)) return fail(ctx, PT_ERR_INVALID, "pt_set_trace: bad depth_cap");
+    ctx->trace = KTrace{d_events, d_nevents, d_colors, depth_cap};
+    return PT_OK;
+}
+
+int pt_dispatch(pt_ctx* ctx, const pt_push* push) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!push) return fail(ctx, PT_ERR_INVALID, "pt_dispatch: null push constants");
+    if (!ctx->has_scene) return fail(ctx, PT_ERR_NO_SCENE, "pt_dispatch: no scene uploaded");
+    if (!ctx->d_accum) return fail(ctx, PT_ERR_NO_SCENE, "pt_dispatch: no accumulator (pt_resize_accum)");
+    if (push->resolution[0] != ctx->width || push->resolution[1] != ctx->height)
+        return fail(ctx, PT_ERR_INVALID, "pt_dispatch: resolution differs from the accumulator size");
+    if (push->samplesPerFrame <= 0) return fail(ctx, PT_ERR_INVALID, "pt_dispatch: samplesPerFrame must be positive");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    KParams& P = *ctx->params;
+    P.pc = *push;
+    P.accum = ctx->d_accum;
+    P.cie = ctx->d_cie;
+    P.trace = ctx->trace;
+    const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
+    PT_CUDA_TRY(ctx, ptk_launch_megakernel(&P, trace, ctx->stream));
+    PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
+    return PT_OK;
+}
+
+int pt_wait(pt_ctx* ctx, uint64_t timeout_ns) {
+    if (!ctx) return PT_ERR_INVALID;
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const auto start = std::chrono::steady_clock::now();
+    auto sleep = std::chrono::microseconds(20);
+    for (;;) {
+        const cudaError_t e = cudaStreamQuery(ctx->stream);
+        if (e == cudaSuccess) return PT_OK;
+        if (e != cudaErrorNotReady) return cuda_fail(ctx, e, "pt_wait");
+        const auto waited = std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - start);
+        if ((uint64_t)waited.count() >= timeout_ns) return fail(ctx, PT_ERR_TIMEOUT, "pt_wait: deadline passed");
+        std::this_thread::sleep_for(sleep);
+        if (sleep < std::chrono::microseconds(2000)) sleep *= 2;
+    }
+}
+
+int pt_read_accum(pt_ctx* ctx, float* host, size_t bytes) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!ctx->d_accum) return fail(ctx, PT_ERR_NO_SCENE, "pt_read_accum: no accumulator");
+    const size_t need = (size_t)ctx->width * (size_t)ctx->height * sizeof(float4);
+    if (!host || bytes < need) return fail(ctx, PT_ERR_INVALID, "pt_read_accum: buffer too small");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    PT_CUDA_TRY(ctx, cudaMemcpyAsync(host, ctx->d_accum, need, cudaMemcpyDeviceToHost, ctx->stream));
+    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_write_accum(pt_ctx* ctx, const float* host, size_t bytes) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!ctx->d_accum) return fail(ctx, PT_ERR_NO_SCENE, "pt_write_accum: no accumulator");
+    const size_t need = (size_t)ctx->width * (size_t)ctx->height * sizeof(float4);
+    if (!host || bytes < need) return fail(ctx, PT_ERR_INVALID, "pt_write_accum: buffer too small");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    PT_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_accum, host, need, cudaMemcpyHostToDevice, ctx->stream));
+    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+void* pt_accum_device_ptr(pt_ctx* ctx) { return ctx ? (void*)ctx->d_accum : nullptr; }
+
+void* pt_stream(pt_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int pt_set_stream(pt_ctx* ctx, void* stream) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return PT_OK;
+}
+
+const char* pt_last_error(pt_ctx* ctx) {
+    if (!ctx) return "null context";
+    return ctx->err.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,204 @@
+"""ctypes bindings of libpt_cuda (include/pt_cuda.h) and libpt_host
+(include/pt_host.h).
+
+This module only declares signatures and loads the in-tree libraries; it
+never substitutes another implementation.  If a library is missing, loading
+raises NativeLibraryError (call pathtracer_gb300.build.build() first).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib")
+
+PT_OK = 0
+PT_ERR_INVALID = 1
+PT_ERR_CUDA = 2
+PT_ERR_TIMEOUT = 3
+PT_ERR_UNSUPPORTED = 4
+PT_ERR_NO_SCENE = 5
+PT_ERR_OOM = 6
+PT_ERR_KERNEL = 7
+
+UBO_FLOATS = 4097  # 7 + 1024 + 768 + 783 + 128 + 64 + 1323
+UBO_OFFSETS = {
+    "numObjects": (0, 7),
+    "objects": (7, 1024),
+    "sdfs": (1031, 768),
+    "materials": (1799, 783),
+    "lights": (2582, 128),
+    "lightIDs": (2710, 64),
+    "CIEXYZ1931": (2774, 1323),
+}
+
+PT_SDF_NONE, PT_SDF_BLOB, PT_SDF_MANDELBULB, PT_SDF_MENGER, PT_SDF_TERRAIN = range(5)
+PT_SDFMAT_DEFAULT, PT_SDFMAT_CONSTANT = 0, 1
+
+PT_EV_HIT_MASK = 0xFFF
+PT_EV_HIT_SDF = 0xFFE
+PT_EV_HIT_MISS = 0xFFF
+PT_EV_EMITTER = 1 << 12
+PT_EV_LIGHT_SHIFT = 13
+PT_EV_SHADOW_SHIFT = 20
+PT_EV_RR_KILL = 1 << 22
+PT_EV_VALID = 1 << 23
+
+
+class NativeLibraryError(RuntimeError):
+    pass
+
+
+class PtPush(ctypes.Structure):
+    """pt_push: byte-for-byte the reference's PushConstantValues (88 B)."""
+
+    _fields_ = [
+        ("resolution", ctypes.c_int32 * 2),
+        ("frame", ctypes.c_int32),
+        ("currentSamples", ctypes.c_int32),
+        ("samplesPerFrame", ctypes.c_int32),
+        ("FPS", ctypes.c_float),
+        ("persistence", ctypes.c_float),
+        ("pathLength", ctypes.c_int32),
+        ("cameraAngle", ctypes.c_float * 2),
+        ("cameraPosX", ctypes.c_float),
+        ("cameraPosY", ctypes.c_float),
+        ("cameraPosZ", ctypes.c_float),
+        ("ISO", ctypes.c_int32),
+        ("cameraSize", ctypes.c_float),
+        ("apertureSize", ctypes.c_float),
+        ("apertureDist", ctypes.c_float),
+        ("lensRadius", ctypes.c_float),
+        ("lensFocalLength", ctypes.c_float),
+        ("lensThickness", ctypes.c_float),
+        ("lensDistance", ctypes.c_float),
+        ("tonemap", ctypes.c_int32),
+    ]
+
+
+class PtSdfPlugin(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("material_mode", ctypes.c_int32),
+        ("material", ctypes.c_float * 3),
+    ]
+
+
+class PtFrameState(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32),
+        ("height", ctypes.c_int32),
+        ("frame", ctypes.c_int32),
+        ("currentSamples", ctypes.c_int32),
+        ("samplesPerFrame", ctypes.c_int32),
+        ("FPS", ctypes.c_float),
+        ("persistence", ctypes.c_float),
+        ("pathLength", ctypes.c_int32),
+        ("cameraShotIndex", ctypes.c_int32),
+        ("tonemap", ctypes.c_int32),
+    ]
+
+
+class PtOffscreenOpts(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32),
+        ("height", ctypes.c_int32),
+        ("numSamples", ctypes.c_int32),
+        ("samplesPerFrame", ctypes.c_int32),
+        ("pathLength", ctypes.c_int32),
+        ("cameraShotIndex", ctypes.c_int32),
+        ("tonemap", ctypes.c_int32),
+        ("frameOffset", ctypes.c_int32),
+    ]
+
+
+assert ctypes.sizeof(PtPush) == 88
+assert ctypes.sizeof(PtSdfPlugin) == 20
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_sz = ctypes.c_size_t
+
+# (name, restype, argtypes) for every symbol include/pt_cuda.h declares.
+CUDA_API = [
+    ("pt_create", _i, [ctypes.POINTER(_vp), _i]),
+    ("pt_destroy", _i, [_vp]),
+    ("pt_set_sdfs", _i, [_vp, ctypes.POINTER(ctypes.c_char_p), _i]),
+    ("pt_set_sdf_plugins", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i]),
+    ("pt_parse_sdf_source", _i, [ctypes.c_char_p, ctypes.POINTER(PtSdfPlugin)]),
+    ("pt_upload_scene", _i, [_vp, _vp]),
+    ("pt_resize_accum", _i, [_vp, _i, _i]),
+    ("pt_dispatch", _i, [_vp, ctypes.POINTER(PtPush)]),
+    ("pt_wait", _i, [_vp, ctypes.c_uint64]),
+    ("pt_read_accum", _i, [_vp, _vp, _sz]),
+    ("pt_write_accum", _i, [_vp, _vp, _sz]),
+    ("pt_accum_device_ptr", _vp, [_vp]),
+    ("pt_stream", _vp, [_vp]),
+    ("pt_set_stream", _i, [_vp, _vp]),
+    ("pt_last_error", ctypes.c_char_p, [_vp]),
+    ("pt_set_trace", _i, [_vp, _vp, _vp, _vp, _i]),
+    ("pt_sdf_source_fingerprint", ctypes.c_uint64, [ctypes.c_char_p]),
+]
+
+# Every symbol include/pt_host.h declares.
+HOST_API = [
+    ("pt_scene_parse", _i, [ctypes.c_char_p, _sz, ctypes.POINTER(_vp), ctypes.c_char_p, _sz]),
+    ("pt_scene_load_file", _i, [ctypes.c_char_p, ctypes.POINTER(_vp), ctypes.c_char_p, _sz]),
+    ("pt_scene_free", None, [_vp]),
+    ("pt_scene_counts", _i, [_vp, ctypes.POINTER(_i)]),
+    ("pt_scene_pack_ubo", _i, [_vp, _vp, _vp]),
+    ("pt_scene_push_constants", _i, [_vp, ctypes.POINTER(PtFrameState), ctypes.POINTER(PtPush)]),
+    ("pt_scene_sdf_source", ctypes.c_char_p, [_vp, _i]),
+    ("pt_scene_to_json", _i, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(_sz)]),
+    ("pt_scene_bind", _i, [_vp, _vp, _vp]),
+    ("pt_render_offscreen", _i, [_vp, _vp, _vp, ctypes.POINTER(PtOffscreenOpts), _vp, _sz,
+                                 ctypes.POINTER(ctypes.c_double)]),
+    ("pt_export_rgb8", _i, [_vp, _i, _i, _i, _vp]),
+    ("pt_save_ppm", _i, [ctypes.c_char_p, _vp, _i, _i]),
+    ("pt_cie_analytic_table", None, [_vp]),
+]
+
+_cache: dict[str, ctypes.CDLL] = {}
+
+
+def _load(name: str, api) -> ctypes.CDLL:
+    if name in _cache:
+        return _cache[name]
+    path = os.path.join(LIB_DIR, name)
+    if not os.path.exists(path):
+        raise NativeLibraryError(f"{path} is missing: build it with pathtracer_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for sym, res, args in api:
+        fn = getattr(lib, sym)
+        fn.restype = res
+        fn.argtypes = args
+    _cache[name] = lib
+    return lib
+
+
+def cuda() -> ctypes.CDLL:
+    """libpt_cuda.so (loads libcudart; no GPU needed until a context is made)."""
+    return _load("libpt_cuda.so", CUDA_API)
+
+
+def host() -> ctypes.CDLL:
+    """libpt_host.so (links libpt_cuda.so)."""
+    cuda()
+    return _load("libpt_host.so", HOST_API)
+
+
+def ptr(a: np.ndarray) -> int:
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data
+
+
+def plugin(kind: int, mode: int = PT_SDFMAT_DEFAULT, material=(0.0, 0.0, 0.0)) -> PtSdfPlugin:
+    p = PtSdfPlugin()
+    p.kind = kind
+    p.material_mode = mode
+    for i, v in enumerate(material):
+        p.material[i] = float(v)
+    return p

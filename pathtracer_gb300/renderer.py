@@ -1,0 +1,212 @@
+"""Python mirror of the drop-in boundary: a Context over libpt_cuda and a
+Scene over libpt_host, with the reference host's calls by name.
+
+    scene = Scene.load("pathtracer_gb300/scenes/mandelbulb_plane.json")
+    with Context(device=0) as ctx:
+        accum, secs = render_offscreen(ctx, scene, cie_analytic(), 1024, 1024, num_samples=64, spf=64, path_length=6)
+
+Every call goes through the C ABI; a failing status raises PathTracerError
+with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native
+from .native import PtFrameState, PtOffscreenOpts, PtPush
+
+
+class PathTracerError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def cie_analytic() -> np.ndarray:
+    """CIE 1931 table (1323 floats, 360..800 nm) from the Wyman-Sloan-Shirley fit."""
+    out = np.zeros(1323, np.float32)
+    native.host().pt_cie_analytic_table(native.ptr(out))
+    return out
+
+
+class Scene:
+    """A parsed scene JSON (the reference's schema)."""
+
+    def __init__(self, handle: int):
+        self._h = ctypes.c_void_p(handle)
+        self._lib = native.host()
+
+    @classmethod
+    def parse(cls, text: str | bytes) -> "Scene":
+        data = text.encode() if isinstance(text, str) else text
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        rc = native.host().pt_scene_parse(data, len(data), ctypes.byref(h), err, 512)
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, err.value.decode())
+        return cls(h.value)
+
+    @classmethod
+    def load(cls, path: str) -> "Scene":
+        with open(path, "rb") as f:
+            return cls.parse(f.read())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.pt_scene_free(h)
+            self._h = None
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def counts(self) -> dict[str, int]:
+        c = (ctypes.c_int * 9)()
+        self._lib.pt_scene_counts(self._h, c)
+        keys = ["spheres", "planes", "boxes", "lenses", "cyclides", "sdfs", "materials", "lights", "shots"]
+        return dict(zip(keys, list(c)))
+
+    def pack_ubo(self, cie: np.ndarray | None) -> np.ndarray:
+        ubo = np.zeros(native.UBO_FLOATS, np.float32)
+        cie_p = None if cie is None else native.ptr(np.ascontiguousarray(cie, np.float32))
+        rc = self._lib.pt_scene_pack_ubo(self._h, cie_p, native.ptr(ubo))
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, "scene overflows the uniform buffer arrays")
+        return ubo
+
+    def push_constants(self, width: int, height: int, frame: int, current_samples: int, spf: int,
+                       path_length: int, shot: int = 1, fps: float = 1.0 / 0.0166, persistence: float = 0.0625,
+                       tonemap: int = 3) -> PtPush:
+        st = PtFrameState(width, height, frame, current_samples, spf, fps, persistence, path_length, shot, tonemap)
+        out = PtPush()
+        rc = self._lib.pt_scene_push_constants(self._h, ctypes.byref(st), ctypes.byref(out))
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, "bad frame state or camera shot index")
+        return out
+
+    def sdf_sources(self) -> list[str]:
+        n = self.counts()["sdfs"]
+        return [self._lib.pt_scene_sdf_source(self._h, i).decode() for i in range(n)]
+
+    def to_json(self) -> str:
+        need = ctypes.c_size_t()
+        self._lib.pt_scene_to_json(self._h, None, 0, ctypes.byref(need))
+        buf = ctypes.create_string_buffer(need.value)
+        rc = self._lib.pt_scene_to_json(self._h, buf, need, ctypes.byref(need))
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, "to_json failed")
+        return buf.value.decode()
+
+
+class Context:
+    """pt_ctx: one device, one stream, owns the accumulator."""
+
+    def __init__(self, device: int = 0):
+        self._lib = native.cuda()
+        h = ctypes.c_void_p()
+        rc = self._lib.pt_create(ctypes.byref(h), device)
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, f"pt_create(device={device}) failed")
+        self._h = h
+        self.width = self.height = 0
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.pt_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def _check(self, rc: int):
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, self._lib.pt_last_error(self._h).decode())
+
+    def set_sdfs(self, sources: list[str]):
+        arr = (ctypes.c_char_p * max(1, len(sources)))(*[s.encode() for s in sources])
+        self._check(self._lib.pt_set_sdfs(self._h, arr, len(sources)))
+
+    def set_sdf_plugins(self, plugins: list):
+        arr = (native.PtSdfPlugin * max(1, len(plugins)))(*plugins)
+        self._check(self._lib.pt_set_sdf_plugins(self._h, arr, len(plugins)))
+
+    def upload_scene(self, ubo: np.ndarray):
+        ubo = np.ascontiguousarray(ubo, np.float32)
+        assert ubo.size == native.UBO_FLOATS
+        self._check(self._lib.pt_upload_scene(self._h, native.ptr(ubo)))
+
+    def bind(self, scene: Scene, cie: np.ndarray):
+        cie = np.ascontiguousarray(cie, np.float32)
+        self._check(native.host().pt_scene_bind(self._h, scene.handle, native.ptr(cie)))
+
+    def resize_accum(self, width: int, height: int):
+        self._check(self._lib.pt_resize_accum(self._h, width, height))
+        self.width, self.height = width, height
+
+    def dispatch(self, push: PtPush):
+        self._check(self._lib.pt_dispatch(self._h, ctypes.byref(push)))
+
+    def wait(self, timeout_ns: int = 2**64 - 1):
+        self._check(self._lib.pt_wait(self._h, ctypes.c_uint64(timeout_ns)))
+
+    def read_accum(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width, 4), np.float32)
+        self._check(self._lib.pt_read_accum(self._h, native.ptr(out), out.nbytes))
+        return out
+
+    def write_accum(self, data: np.ndarray):
+        data = np.ascontiguousarray(data, np.float32)
+        self._check(self._lib.pt_write_accum(self._h, native.ptr(data), data.nbytes))
+
+    def accum_device_ptr(self) -> int:
+        return self._lib.pt_accum_device_ptr(self._h) or 0
+
+    def stream(self) -> int:
+        return self._lib.pt_stream(self._h) or 0
+
+    def set_stream(self, stream: int | None):
+        self._check(self._lib.pt_set_stream(self._h, stream))
+
+    def set_trace(self, events_ptr: int, nevents_ptr: int, colors_ptr: int, depth_cap: int):
+        self._check(self._lib.pt_set_trace(self._h, events_ptr or None, nevents_ptr or None, colors_ptr or None,
+                                           depth_cap))
+
+
+def render_offscreen(ctx: Context, scene: Scene, cie: np.ndarray, width: int, height: int, num_samples: int,
+                     spf: int, path_length: int, shot: int = 1, tonemap: int = 3, frame_offset: int = 0):
+    """The reference's offscreen render; returns (accumulator HxWx4, seconds)."""
+    cie = np.ascontiguousarray(cie, np.float32)
+    opts = PtOffscreenOpts(width, height, num_samples, spf, path_length, shot, tonemap, frame_offset)
+    out = np.empty((height, width, 4), np.float32)
+    secs = ctypes.c_double()
+    rc = native.host().pt_render_offscreen(ctx.handle, scene.handle, native.ptr(cie), ctypes.byref(opts),
+                                           native.ptr(out), out.nbytes, ctypes.byref(secs))
+    if rc != native.PT_OK:
+        raise PathTracerError(rc, native.cuda().pt_last_error(ctx.handle).decode())
+    ctx.width, ctx.height = width, height
+    return out, secs.value
+
+
+def export_rgb8(accum: np.ndarray, tonemap: int = 3) -> np.ndarray:
+    """SaveRender's tonemap chain on the host: HxWx4 float -> HxWx3 uint8."""
+    accum = np.ascontiguousarray(accum, np.float32)
+    h, w = accum.shape[:2]
+    rgb = np.empty((h, w, 3), np.uint8)
+    rc = native.host().pt_export_rgb8(native.ptr(accum), w, h, tonemap, native.ptr(rgb))
+    if rc != native.PT_OK:
+        raise PathTracerError(rc, "export failed")
+    return rgb

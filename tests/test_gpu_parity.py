@@ -1,0 +1,175 @@
+"""Parity of the sm_103a megakernel with the CPU restatement of the shader.
+
+Every test calls the library through its C ABI (ctypes), on the same scene,
+UBO and push constants the oracle gets.  Criteria (oracle/compare.py):
+>= 99.9% of paths follow the identical branch sequence; matching paths agree
+in per-sample XYZ within 1e-4 relative; pixels whose paths all match agree in
+the accumulated XYZ within 1e-4 relative; w == 1 everywhere.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import SCENES
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rt(built):
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("no CUDA device: -m gpu tests need a GPU")
+    from pathtracer_gb300 import Context, Scene, cie_analytic
+
+    return {"Context": Context, "Scene": Scene, "cie": cie_analytic()}
+
+
+def _setup(rt, name, W, H):
+    from oracle import compare
+
+    scene = rt["Scene"].load(os.path.join(SCENES, name + ".json"))
+    ctx = rt["Context"](0)
+    ctx.bind(scene, rt["cie"])
+    ctx.resize_accum(W, H)
+    ubo = scene.pack_ubo(rt["cie"])
+    return scene, ctx, ubo, compare.plugins_for(scene)
+
+
+def _check(report):
+    from oracle import compare
+
+    assert compare.passes(report), report
+
+
+@pytest.mark.parametrize(
+    "name,W,H,spf,depth",
+    [
+        ("cornell_box", 64, 64, 4, 8),
+        ("mandelbulb_plane", 64, 48, 4, 6),
+        ("feature_mix", 64, 48, 4, 6),
+        ("menger_terrain", 48, 40, 4, 12),
+    ],
+)
+def test_single_dispatch_matches_oracle(rt, name, W, H, spf, depth):
+    from oracle import compare
+
+    scene, ctx, ubo, plugins = _setup(rt, name, W, H)
+    push = scene.push_constants(W, H, spf, spf, spf, depth)
+    acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=depth)
+    acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
+    rep = compare.compare(acc_o, tr_o, acc_g, tr_g, spf)
+    print(name, rep)
+    _check(rep)
+    ctx.close()
+
+
+def test_ragged_resolution_and_short_paths(rt):
+    """W, H not multiples of the 16x8 block; pathLength 1 and 0."""
+    from oracle import compare
+
+    W, H = 37, 23
+    scene, ctx, ubo, plugins = _setup(rt, "feature_mix", W, H)
+    for depth in (1, 0):
+        ctx.resize_accum(W, H)
+        push = scene.push_constants(W, H, 3, 3, 3, depth)
+        acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=max(depth, 1))
+        acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=max(depth, 1))
+        _check(compare.compare(acc_o, tr_o, acc_g, tr_g, 3))
+    ctx.close()
+
+
+def test_progressive_running_mean_and_ema(rt):
+    """Several dispatches: running mean (SC:1504-1506), then a reset frame with
+    frame > spf that takes the EMA branch (SC:1500-1502)."""
+    from oracle import compare
+
+    W, H, spf, depth = 40, 32, 2, 5
+    scene, ctx, ubo, plugins = _setup(rt, "cornell_box", W, H)
+    acc_o = np.zeros((H, W, 4), np.float32)
+    frame = cur = 0
+    for it in range(4):
+        frame += spf
+        cur = spf if it == 3 else cur + spf  # the 4th dispatch is a reset with frame > spf
+        push = scene.push_constants(W, H, frame, cur, spf, depth)
+        acc_o, tr_o = compare.run_oracle(ubo, push, plugins, accum=acc_o, trace_depth=depth)
+        acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
+        _check(compare.compare(acc_o.copy(), tr_o, acc_g, tr_g, spf))
+        ctx.write_accum(acc_o)  # continue both from the same state
+    ctx.close()
+
+
+def test_offscreen_loop_matches_oracle_loop(rt):
+    """pt_render_offscreen (MainLoop offscreen) against the oracle driven the
+    same way: frame and currentSamples += spf until numSamples."""
+    from oracle import compare
+    from pathtracer_gb300 import render_offscreen
+
+    W, H, spf, n, depth = 48, 32, 3, 8, 6
+    scene = rt["Scene"].load(os.path.join(SCENES, "mandelbulb_plane.json"))
+    ubo = scene.pack_ubo(rt["cie"])
+    plugins = compare.plugins_for(scene)
+    with rt["Context"](0) as ctx:
+        acc_g, secs = render_offscreen(ctx, scene, rt["cie"], W, H, n, spf, depth)
+    acc_o = np.zeros((H, W, 4), np.float32)
+    frame = cur = 0
+    while True:
+        frame += spf
+        cur += spf
+        compare.run_oracle(ubo, scene.push_constants(W, H, frame, cur, spf, depth), plugins, accum=acc_o)
+        if cur >= n:
+            break
+    rel = np.abs(acc_o - acc_g) / np.maximum(np.maximum(np.abs(acc_o), np.abs(acc_g)), 1e-6)
+    # No trace here: count pixels outside tolerance; path flips are rare.
+    frac_bad = float(np.mean(rel[..., :3].max(axis=-1) > 1e-4))
+    assert frac_bad < 0.02, frac_bad
+    assert secs > 0
+
+
+def test_error_paths(rt):
+    from pathtracer_gb300 import PathTracerError, native
+
+    ctx = rt["Context"](0)
+    scene = rt["Scene"].load(os.path.join(SCENES, "cornell_box.json"))
+    push = scene.push_constants(16, 16, 1, 1, 1, 4)
+    with pytest.raises(PathTracerError) as e:
+        ctx.dispatch(push)
+    assert e.value.code == native.PT_ERR_NO_SCENE
+    ctx.bind(scene, rt["cie"])
+    ctx.resize_accum(8, 8)
+    with pytest.raises(PathTracerError) as e:
+        ctx.dispatch(push)  # resolution differs from the accumulator
+    assert e.value.code == native.PT_ERR_INVALID
+    bad = scene.pack_ubo(rt["cie"])
+    bad[5] = 33.0  # 33 SDFs cannot be evaluated with a 32-bit set mask
+    with pytest.raises(PathTracerError) as e:
+        ctx.upload_scene(bad)
+    assert e.value.code == native.PT_ERR_UNSUPPORTED
+    with pytest.raises(PathTracerError):
+        ctx.set_sdfs(["float sdf(in vec3 p) { return 1.0; }"])
+    ctx.close()
+
+
+def test_wait_deadline(rt):
+    """pt_wait returns PT_ERR_TIMEOUT at its deadline instead of blocking, and
+    the same context keeps working afterwards."""
+    from pathtracer_gb300 import PathTracerError, native
+
+    W = H = 512
+    scene = rt["Scene"].load(os.path.join(SCENES, "mandelbulb_plane.json"))
+    with rt["Context"](0) as ctx:
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        ctx.dispatch(scene.push_constants(W, H, 64, 64, 64, 6))
+        try:
+            ctx.wait(timeout_ns=1000)
+            timed_out = False
+        except PathTracerError as e:
+            assert e.code == native.PT_ERR_TIMEOUT
+            timed_out = True
+        ctx.wait()
+        acc = ctx.read_accum()
+        assert np.isfinite(acc).all()
+        assert timed_out
