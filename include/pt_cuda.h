@@ -172,6 +172,11 @@ const char* pt_last_error(pt_ctx* ctx);
  * Device pointers owned by the caller; pass NULLs to disable. */
 int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_colors, int depth_cap);
 
+/* Evaluates one include/pt_mathf.h function on the device over device
+ * arrays (fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos), so tests can
+ * compare its bits with the same function on the CPU.  Synchronous. */
+int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float* d_out, int n);
+
 /* Event word layout, identical in the CPU restatement used by the tests. */
 #define PT_EV_HIT_MASK 0xFFFu     /* global object index; PT_EV_HIT_SDF, PT_EV_HIT_MISS */
 #define PT_EV_HIT_SDF 0xFFEu

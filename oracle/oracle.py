@@ -65,6 +65,8 @@ def lib() -> ctypes.CDLL:
         L.pto_sdf_material.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.pto_wave_to_xyz.restype = None
         L.pto_wave_to_xyz.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
+        L.pto_mathf_eval.restype = ctypes.c_int
+        L.pto_mathf_eval.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -96,4 +98,18 @@ def dispatch(ubo: np.ndarray, push, plugins: list, accum: np.ndarray, rect=None,
                             accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr) if tr else None, nthreads)
     if rc != 0:
         raise RuntimeError(f"pto_dispatch failed: {rc}")
+    return out
+
+
+MATHF = {"sin": 0, "cos": 1, "exp": 2, "log": 3, "pow": 4, "acos": 5}
+
+
+def mathf(fn: str, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
+    """pt_mathf function `fn` on the CPU over float32 arrays."""
+    x = np.ascontiguousarray(x, np.float32)
+    yy = np.ascontiguousarray(y if y is not None else x, np.float32)
+    out = np.empty_like(x)
+    rc = lib().pto_mathf_eval(MATHF[fn], x.ctypes.data, yy.ctypes.data, out.ctypes.data, x.size)
+    if rc != 0:
+        raise ValueError(fn)
     return out

@@ -10,7 +10,8 @@
  *   normalize(v) = v * (1/sqrt(v.v))  length(v) = sqrt(v.v)
  *   inversesqrt(x) = 1/sqrt(x)        sign, step, faceforward, refract as specified
  *   min/max = IEEE minNum/maxNum (fminf/fmaxf)
- * Transcendentals are the C library's (sinf, cosf, expf, logf, powf, acosf).
+ * Transcendentals are the pt_mathf functions (include/pt_mathf.h), the same
+ * float algorithms the GPU kernels run, so both sides compute identical bits.
  * Out-of-range reads of the uniform arrays return 0 (robust buffer access).
  *
  * Parity unpinned: the reference has no tests or golden vectors and cannot
@@ -18,6 +19,7 @@
  * derived from its formulas (tests/test_oracle_kat.py).
  */
 #include "pt_oracle.h"
+#include "../include/pt_mathf.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -139,8 +141,8 @@ static vec3 WaveToXYZ(const ctx_t* c, float wave) {
 /* SC:143-152 */
 static mat3 RotationMatrix(vec3 angle) {
     angle = scl3(angle, 0.0174532925199f);
-    vec3 s = mk3(sinf(angle.x), sinf(angle.y), sinf(angle.z));
-    vec3 co = mk3(cosf(angle.x), cosf(angle.y), cosf(angle.z));
+    vec3 s = mk3(ptm_sinf(angle.x), ptm_sinf(angle.y), ptm_sinf(angle.z));
+    vec3 co = mk3(ptm_cosf(angle.x), ptm_cosf(angle.y), ptm_cosf(angle.z));
     mat3 mX = {{1.0f, 0.0f, 0.0f}, {0.0f, co.x, -s.x}, {0.0f, s.x, co.x}};
     mat3 mY = {{co.y, 0.0f, s.y}, {0.0f, 1.0f, 0.0f}, {-s.y, 0.0f, co.y}};
     mat3 mZ = {{co.z, -s.z, 0.0f}, {s.z, co.z, 0.0f}, {0.0f, 0.0f, 1.0f}};
@@ -408,8 +410,8 @@ static int SolveCubic(float b, float c, float d, vec3* roots) {
     if (D > 0.0f) {
         float u = R + sqrtf(D);
         float v = R - sqrtf(D);
-        float S = signf_glsl(u) * powf(fabsf(u), ONEBYTHREE);
-        float T = signf_glsl(v) * powf(fabsf(v), ONEBYTHREE);
+        float S = signf_glsl(u) * ptm_powf(fabsf(u), ONEBYTHREE);
+        float T = signf_glsl(v) * ptm_powf(fabsf(v), ONEBYTHREE);
         roots->x = S + T - bdiv3;
         for (int i = 0; i < 2; i++) {
             roots->x -= EvalCubic(1.0f, b, c, d, roots->x) / EvalQuadratic(3.0f, 2.0f * b, c, roots->x);
@@ -417,12 +419,12 @@ static int SolveCubic(float b, float c, float d, vec3* roots) {
         return 1;
     }
     float sqrtnegQ = sqrtf(-Q);
-    float thetadiv3 = acosf(R / (sqrtnegQ * sqrtnegQ * sqrtnegQ)) * ONEBYTHREE;
+    float thetadiv3 = ptm_acosf(R / (sqrtnegQ * sqrtnegQ * sqrtnegQ)) * ONEBYTHREE;
     float TWOPIBYTHREE = fmaf(2.0f, PI_F, ONEBYTHREE);
     float k = 2.0f * sqrtnegQ;
-    roots->x = k * cosf(thetadiv3) - bdiv3;
-    roots->y = k * cosf(thetadiv3 + TWOPIBYTHREE) - bdiv3;
-    roots->z = k * cosf(fmaf(2.0f, TWOPIBYTHREE, thetadiv3)) - bdiv3;
+    roots->x = k * ptm_cosf(thetadiv3) - bdiv3;
+    roots->y = k * ptm_cosf(thetadiv3 + TWOPIBYTHREE) - bdiv3;
+    roots->z = k * ptm_cosf(fmaf(2.0f, TWOPIBYTHREE, thetadiv3)) - bdiv3;
     for (int i = 0; i < 2; i++) {
         roots->x -= EvalCubic(1.0f, b, c, d, roots->x) / EvalQuadratic(3.0f, 2.0f * b, c, roots->x);
         roots->y -= EvalCubic(1.0f, b, c, d, roots->y) / EvalQuadratic(3.0f, 2.0f * b, c, roots->y);
@@ -566,7 +568,7 @@ static float mandelbulb_sdf(vec3 p) {
     float r = length3(z);
     float dr = 1.0f;
     for (int i = 0; i < 4; i++) {
-        dr = 8.0f * powf(r, 7.0f) * dr + 1.0f;
+        dr = 8.0f * ptm_powf(r, 7.0f) * dr + 1.0f;
         float invr = 1.0f / r;
         float invl = 1.0f / sqrtf(z.x * z.x + z.z * z.z);
         r *= r;
@@ -587,7 +589,7 @@ static float mandelbulb_sdf(vec3 p) {
         r = length3(z);
         if (r > 16.0f) break;
     }
-    return 0.5f * logf(r) * r / dr;
+    return 0.5f * ptm_logf(r) * r / dr;
 }
 /* sdfs/mandelbulb.glsl:54-58 (mix endpoints parameterised) */
 static float mandelbulb_material(vec3 p, const float* m) {
@@ -616,10 +618,10 @@ static float menger_sdf(vec3 p) {
 
 /* sdfs/terrain.glsl:1-8 */
 static float terrain_height(float x) {
-    return sinf(0.0625f * x) + sinf(0.125f * (x + 10.0f)) + 0.25f * sinf(0.25f * x) + 0.125f * sinf(0.5f * x) +
-           0.25f * sinf(x) + 0.25f * sinf(2.0f * x + 1.0f) + 0.125f * sinf(4.0f * x + 2.0f) +
-           0.0625f * sinf(8.0f * x + 1.0f) + 0.03125f * sinf(16.0f * x + 5.0f) + 0.015625f * sinf(32.0f * x) +
-           0.0078125f * sinf(64.0f * x);
+    return ptm_sinf(0.0625f * x) + ptm_sinf(0.125f * (x + 10.0f)) + 0.25f * ptm_sinf(0.25f * x) + 0.125f * ptm_sinf(0.5f * x) +
+           0.25f * ptm_sinf(x) + 0.25f * ptm_sinf(2.0f * x + 1.0f) + 0.125f * ptm_sinf(4.0f * x + 2.0f) +
+           0.0625f * ptm_sinf(8.0f * x + 1.0f) + 0.03125f * ptm_sinf(16.0f * x + 5.0f) + 0.015625f * ptm_sinf(32.0f * x) +
+           0.0078125f * ptm_sinf(64.0f * x);
 }
 static float terrain_sdf(vec3 p) { return p.y - (terrain_height(p.x) + terrain_height(p.z)); }
 
@@ -863,7 +865,7 @@ static vec2 SampleUniformUnitDisk(uint32_t* seed) {
     float ry = RandomFloatPCG32(seed);
     float phi = 2.0f * PI_F * ry;
     float d = sqrtf(rx);
-    return mk2(d * cosf(phi), d * sinf(phi));
+    return mk2(d * ptm_cosf(phi), d * ptm_sinf(phi));
 }
 static vec3 SampleUniformUnitSphere(uint32_t* seed) {
     float rx = RandomFloatPCG32(seed);
@@ -871,7 +873,7 @@ static vec3 SampleUniformUnitSphere(uint32_t* seed) {
     float phi = 2.0f * PI_F * ry;
     float sinTheta = 2.0f * rx - 1.0f;
     float cosTheta = sqrtf(fmaf(-sinTheta, sinTheta, 1.0f));
-    return mk3(cosf(phi) * cosTheta, sinf(phi) * cosTheta, sinTheta);
+    return mk3(ptm_cosf(phi) * cosTheta, ptm_sinf(phi) * cosTheta, sinTheta);
 }
 static vec3 SampleCosineUnitCone(uint32_t* seed, float cosThetaMax) {
     float rx = RandomFloatPCG32(seed);
@@ -880,21 +882,21 @@ static vec3 SampleCosineUnitCone(uint32_t* seed, float cosThetaMax) {
     float phi = 2.0f * PI_F * ry;
     float cosTheta = (1.0f - cosAlphaMax) * rx + cosAlphaMax;
     float sinTheta = sqrtf(fmaf(-cosTheta, cosTheta, 1.0f));
-    return normalize3(mk3(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta + 1.0f));
+    return normalize3(mk3(ptm_cosf(phi) * sinTheta, ptm_sinf(phi) * sinTheta, cosTheta + 1.0f));
 }
 
 /* SC:1030-1055 */
 static vec4 SpectralPowerDistribution(vec4 l, float l_peak, float d, int invert) {
     float den = 2.0f * d * d;
     vec4 x = mk4((l.x - l_peak) / den, (l.y - l_peak) / den, (l.z - l_peak) / den, (l.w - l_peak) / den);
-    vec4 r = mk4(expf(-x.x * x.x), expf(-x.y * x.y), expf(-x.z * x.z), expf(-x.w * x.w));
+    vec4 r = mk4(ptm_expf(-x.x * x.x), ptm_expf(-x.y * x.y), ptm_expf(-x.z * x.z), ptm_expf(-x.w * x.w));
     float a = (float)invert;
     return mk4(mixf(r.x, 1.0f - r.x, a), mixf(r.y, 1.0f - r.y, a), mixf(r.z, 1.0f - r.z, a), mixf(r.w, 1.0f - r.w, a));
 }
 static inline float bb1(float l, float T) {
-    return (1.1910429724e-16f * powf(l, -5.0f)) / (expf(0.014387768775f / (l * T)) - 1.0f);
+    return (1.1910429724e-16f * ptm_powf(l, -5.0f)) / (ptm_expf(0.014387768775f / (l * T)) - 1.0f);
 }
-static inline float BlackBodyRadiationPeak(float T) { return 4.0956746759e-6f * powf(T, 5.0f); }
+static inline float BlackBodyRadiationPeak(float T) { return 4.0956746759e-6f * ptm_powf(T, 5.0f); }
 static vec4 Emit(vec4 l, light_t lt) {
     float temperature = fmaxf(lt.x, 0.0f);
     vec4 lm = scl4(l, 1e-9f);
@@ -1271,7 +1273,7 @@ int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plug
             outColor = scl3(outColor, pc->apertureSize * pc->apertureSize * (float)pc->ISO);
             /* Accumulate SC:1492-1507 */
             if ((pc->currentSamples == pc->samplesPerFrame) && (pc->frame > pc->samplesPerFrame)) {
-                float weight = powf(2.0f, -8.0f / (pc->FPS * pc->persistence));
+                float weight = ptm_powf(2.0f, -8.0f / (pc->FPS * pc->persistence));
                 outColor = add3(scl3(outColor, 1.0f - weight), scl3(inColor, weight));
             } else {
                 int unitSamples = pc->currentSamples / pc->samplesPerFrame;
@@ -1283,6 +1285,23 @@ int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plug
             px[1] = outColor.y;
             px[2] = outColor.z;
             px[3] = 1.0f;
+        }
+    }
+    return PT_OK;
+}
+
+/* Evaluates one pt_mathf function over arrays (for accuracy tests):
+ * fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos. */
+int pto_mathf_eval(int fn, const float* x, const float* y, float* out, int n) {
+    for (int i = 0; i < n; i++) {
+        switch (fn) {
+            case 0: out[i] = ptm_sinf(x[i]); break;
+            case 1: out[i] = ptm_cosf(x[i]); break;
+            case 2: out[i] = ptm_expf(x[i]); break;
+            case 3: out[i] = ptm_logf(x[i]); break;
+            case 4: out[i] = ptm_powf(x[i], y[i]); break;
+            case 5: out[i] = ptm_acosf(x[i]); break;
+            default: return PT_ERR_INVALID;
         }
     }
     return PT_OK;

@@ -49,6 +49,7 @@ float pto_blackbody_peak(float T);
 float pto_sdf_eval(const pt_sdf_plugin* plugin, const float* p3);
 float pto_sdf_material(const pt_sdf_plugin* plugin, const float* p3);
 void pto_wave_to_xyz(const float* cie, float wave, float* out3);
+int pto_mathf_eval(int fn, const float* x, const float* y, float* out, int n);
 
 #ifdef __cplusplus
 }

@@ -194,13 +194,13 @@ PT_DI float solve_cubic_first(float b, float c, float d) {
     if (D > 0.0f) {
         const float u = R + sqrtf(D);
         const float v = R - sqrtf(D);
-        const float S = sign_glsl(u) * powf(fabsf(u), PT_ONEBYTHREE);
-        const float T = sign_glsl(v) * powf(fabsf(v), PT_ONEBYTHREE);
+        const float S = sign_glsl(u) * ptm_powf(fabsf(u), PT_ONEBYTHREE);
+        const float T = sign_glsl(v) * ptm_powf(fabsf(v), PT_ONEBYTHREE);
         x = S + T - bdiv3;
     } else {
         const float sqrtnegQ = sqrtf(-Q);
-        const float thetadiv3 = acosf(R / (sqrtnegQ * sqrtnegQ * sqrtnegQ)) * PT_ONEBYTHREE;
-        x = 2.0f * sqrtnegQ * cosf(thetadiv3) - bdiv3;
+        const float thetadiv3 = ptm_acosf(R / (sqrtnegQ * sqrtnegQ * sqrtnegQ)) * PT_ONEBYTHREE;
+        x = 2.0f * sqrtnegQ * ptm_cosf(thetadiv3) - bdiv3;
     }
 #pragma unroll
     for (int i = 0; i < 2; i++) x -= eval_cubic(1.0f, b, c, d, x) / eval_quadratic(3.0f, 2.0f * b, c, x);
@@ -343,7 +343,7 @@ PT_DI float sdf(float3 p) {
     float dr = 1.0f;
 #pragma unroll 1
     for (int i = 0; i < 4; i++) {
-        dr = 8.0f * powf(r, 7.0f) * dr + 1.0f;
+        dr = 8.0f * ptm_powf(r, 7.0f) * dr + 1.0f;
         const float invr = 1.0f / r;
         const float invl = 1.0f / sqrtf(z.x * z.x + z.z * z.z);
         r *= r;
@@ -366,7 +366,7 @@ PT_DI float sdf(float3 p) {
         r = length3(z);
         if (r > 16.0f) break;
     }
-    return 0.5f * logf(r) * r / dr;
+    return 0.5f * ptm_logf(r) * r / dr;
 }
 PT_DI float sdfmaterial(float3 p, const float* m) {
     const float factor = dot3(p, p);
@@ -398,10 +398,10 @@ PT_DI float sdf(float3 p) {
 
 namespace sdf_terrain {  // sdfs/terrain.glsl
 PT_DI float height(float x) {
-    return sinf(0.0625f * x) + sinf(0.125f * (x + 10.0f)) + 0.25f * sinf(0.25f * x) + 0.125f * sinf(0.5f * x) +
-           0.25f * sinf(x) + 0.25f * sinf(2.0f * x + 1.0f) + 0.125f * sinf(4.0f * x + 2.0f) +
-           0.0625f * sinf(8.0f * x + 1.0f) + 0.03125f * sinf(16.0f * x + 5.0f) + 0.015625f * sinf(32.0f * x) +
-           0.0078125f * sinf(64.0f * x);
+    return ptm_sinf(0.0625f * x) + ptm_sinf(0.125f * (x + 10.0f)) + 0.25f * ptm_sinf(0.25f * x) + 0.125f * ptm_sinf(0.5f * x) +
+           0.25f * ptm_sinf(x) + 0.25f * ptm_sinf(2.0f * x + 1.0f) + 0.125f * ptm_sinf(4.0f * x + 2.0f) +
+           0.0625f * ptm_sinf(8.0f * x + 1.0f) + 0.03125f * ptm_sinf(16.0f * x + 5.0f) + 0.015625f * ptm_sinf(32.0f * x) +
+           0.0078125f * ptm_sinf(64.0f * x);
 }
 PT_DI float sdf(float3 p) { return p.y - (height(p.x) + height(p.z)); }
 }  // namespace sdf_terrain

@@ -47,7 +47,7 @@ PT_DI float3 wave_to_xyz(const float* __restrict__ cie, float wave) {
 PT_DI float4 evaluate_brdf(float4 l, float peak, float sigma, float invertf) {
     const float den = 2.0f * sigma * sigma;
     const float4 x = f4((l.x - peak) / den, (l.y - peak) / den, (l.z - peak) / den, (l.w - peak) / den);
-    const float4 r = f4(expf(-x.x * x.x), expf(-x.y * x.y), expf(-x.z * x.z), expf(-x.w * x.w));
+    const float4 r = f4(ptm_expf(-x.x * x.x), ptm_expf(-x.y * x.y), ptm_expf(-x.z * x.z), ptm_expf(-x.w * x.w));
     const float a = (float)(int)invertf;
     const float4 s = f4(mix_glsl(r.x, 1.0f - r.x, a), mix_glsl(r.y, 1.0f - r.y, a), mix_glsl(r.z, 1.0f - r.z, a),
                         mix_glsl(r.w, 1.0f - r.w, a));
@@ -56,12 +56,12 @@ PT_DI float4 evaluate_brdf(float4 l, float peak, float sigma, float invertf) {
 
 // BlackBodyRadiation / Emit, SC:1040-1055.
 PT_DI float blackbody(float l, float T) {
-    return (1.1910429724e-16f * powf(l, -5.0f)) / (expf(0.014387768775f / (l * T)) - 1.0f);
+    return (1.1910429724e-16f * ptm_powf(l, -5.0f)) / (ptm_expf(0.014387768775f / (l * T)) - 1.0f);
 }
 PT_DI float4 emit(float4 l, float temperature_in, float luminosity) {
     const float T = fmaxf(temperature_in, 0.0f);
     const float4 lm = l * 1e-9f;
-    const float peak = 4.0956746759e-6f * powf(T, 5.0f);
+    const float peak = 4.0956746759e-6f * ptm_powf(T, 5.0f);
     const float4 e = f4(blackbody(lm.x, T) / peak, blackbody(lm.y, T) / peak, blackbody(lm.z, T) / peak,
                         blackbody(lm.w, T) / peak);
     return e * fmaxf(luminosity, 0.0f);
@@ -254,8 +254,9 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
             const float phi = 2.0f * PT_PI * ry;
             const float dd = sqrtf(rx);
             const float ha = 0.5f * pc.apertureSize;
-            const float3 poa =
-                camPos + mul_vm(f3(ha * (dd * cosf(phi)), ha * (dd * sinf(phi)), pc.apertureDist), camS.cam);
+            float sp, cp;
+            ptm_sincosf(phi, &sp, &cp);
+            const float3 poa = camPos + mul_vm(f3(ha * (dd * cp), ha * (dd * sp), pc.apertureDist), camS.cam);
             dir = normalize3(poa - org);
             // SampleHeroWavelength SC:960-963, TracePathLens SC:1409-1444.
             const float lh = mix_glsl(360.0f, 800.0f, rnd(seed));
@@ -336,7 +337,9 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
                         const float phi = 2.0f * PT_PI * ry;
                         const float sinTheta = 2.0f * rx - 1.0f;
                         const float cosTheta = sqrtf(__fmaf_rn(-sinTheta, sinTheta, 1.0f));
-                        dir = normalize3(nrm + f3(cosf(phi) * cosTheta, sinf(phi) * cosTheta, sinTheta));
+                        float sp, cp;
+                        ptm_sincosf(phi, &sp, &cp);
+                        dir = normalize3(nrm + f3(cp * cosTheta, sp * cosTheta, sinTheta));
                     }
                     brdfPdf = dot3(dir, nrm) / PT_PI;
                     // SampleLightSource, SC:1298-1343.
@@ -358,8 +361,9 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
                             const float phi = 2.0f * PT_PI * ry;
                             const float cosTheta = (1.0f - cosAlphaMax) * rx + cosAlphaMax;
                             const float sinTheta = sqrtf(__fmaf_rn(-cosTheta, cosTheta, 1.0f));
-                            shDir = to_world(normalize3(f3(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta + 1.0f)),
-                                             lightDir);
+                            float sp, cp;
+                            ptm_sincosf(phi, &sp, &cp);
+                            shDir = to_world(normalize3(f3(cp * sinTheta, sp * sinTheta, cosTheta + 1.0f)), lightDir);
                         }
                         lightPdf = 1.0f / numLights;
                         lightPdf *= dot3(shDir, lightDir) / (PT_PI * (1.0f - costhetaMax * costhetaMax));
@@ -435,7 +439,7 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
     const float4 old = P.accum[pix];
     const float3 in = f3(old.x, old.y, old.z);
     if ((pc.currentSamples == pc.samplesPerFrame) && (pc.frame > pc.samplesPerFrame)) {
-        const float w = powf(2.0f, -8.0f / (pc.FPS * pc.persistence));
+        const float w = ptm_powf(2.0f, -8.0f / (pc.FPS * pc.persistence));
         out = out * (1.0f - w) + in * w;
     } else {
         const int unitSamples = pc.currentSamples / pc.samplesPerFrame;
@@ -475,6 +479,30 @@ __global__ void rotation_setup_kernel(const __grid_constant__ KScene S, float* _
 }
 
 }  // namespace
+
+namespace {
+__global__ void mathf_eval_kernel(int fn, const float* __restrict__ x, const float* __restrict__ y,
+                                  float* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float r;
+    switch (fn) {
+        case 0: r = ptm_sinf(x[i]); break;
+        case 1: r = ptm_cosf(x[i]); break;
+        case 2: r = ptm_expf(x[i]); break;
+        case 3: r = ptm_logf(x[i]); break;
+        case 4: r = ptm_powf(x[i], y[i]); break;
+        default: r = ptm_acosf(x[i]); break;
+    }
+    out[i] = r;
+}
+}  // namespace
+
+cudaError_t ptk_mathf_eval(int fn, const float* x, const float* y, float* out, int n, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    mathf_eval_kernel<<<(n + 255) / 256, 256, 0, stream>>>(fn, x, y, out, n);
+    return cudaGetLastError();
+}
 
 cudaError_t ptk_rotation_setup(const KScene* scene, float* d_out, cudaStream_t stream) {
     const int n = scene->meta.total_objects;

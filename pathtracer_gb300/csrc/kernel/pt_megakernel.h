@@ -16,3 +16,7 @@ cudaError_t ptk_rotation_setup(const KScene* scene, float* d_out, cudaStream_t s
 
 // One dispatch of the plain megakernel over params->pc.resolution.
 cudaError_t ptk_launch_megakernel(const KParams* params, bool trace, cudaStream_t stream);
+
+// Evaluates a pt_mathf function over device arrays (verification hook):
+// fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos.
+cudaError_t ptk_mathf_eval(int fn, const float* x, const float* y, float* out, int n, cudaStream_t stream);

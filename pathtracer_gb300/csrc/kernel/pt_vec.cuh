@@ -6,10 +6,14 @@
 // specification: mix(x,y,a) = x*(1-a) + y*a, mod(x,y) = x - y*floor(x/y),
 // normalize(v) = v * (1/sqrt(v.v)), inversesqrt(x) = 1/sqrt(x) (IEEE sqrt and
 // division, never the approximate rsqrt), min/max = IEEE minNum/maxNum.
+// sin, cos, exp, log, pow and acos are the pt_mathf functions, which compute
+// the same bits on the GPU and on a CPU.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "../../../include/pt_mathf.h"
 
 #define PT_DI __device__ __forceinline__
 
@@ -75,8 +79,10 @@ PT_DI float3 refract3(float3 I, float3 N, float eta) {
 // RotationMatrix (src/shader.comp:143-152): mX * mY * mZ from degrees.
 PT_DI m3 rotation_matrix(float3 angle) {
     angle = angle * 0.0174532925199f;
-    const float sx = sinf(angle.x), sy = sinf(angle.y), sz = sinf(angle.z);
-    const float cx = cosf(angle.x), cy = cosf(angle.y), cz = cosf(angle.z);
+    float sx, sy, sz, cx, cy, cz;
+    ptm_sincosf(angle.x, &sx, &cx);
+    ptm_sincosf(angle.y, &sy, &cy);
+    ptm_sincosf(angle.z, &sz, &cz);
     const m3 mX{f3(1.0f, 0.0f, 0.0f), f3(0.0f, cx, -sx), f3(0.0f, sx, cx)};
     const m3 mY{f3(cy, 0.0f, sy), f3(0.0f, 1.0f, 0.0f), f3(-sy, 0.0f, cy)};
     const m3 mZ{f3(cz, -sz, 0.0f), f3(sz, cz, 0.0f), f3(0.0f, 0.0f, 1.0f)};

@@ -140,6 +140,7 @@ CUDA_API = [
     ("pt_last_error", ctypes.c_char_p, [_vp]),
     ("pt_set_trace", _i, [_vp, _vp, _vp, _vp, _i]),
     ("pt_sdf_source_fingerprint", ctypes.c_uint64, [ctypes.c_char_p]),
+    ("pt_mathf_eval", _i, [_vp, _i, _vp, _vp, _vp, _i]),
 ]
 
 # Every symbol include/pt_host.h declares.
