@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--spf", type=int, default=64, help="samples per dispatch")
     ap.add_argument("--depth", type=int, default=6)
     ap.add_argument("--cpu-rows", type=int, default=32, help="rows in the CPU baseline sample")
+    ap.add_argument("--engine", default="wavefront", choices=["wavefront", "megakernel"])
+    ap.add_argument("--compare-engines", type=int, default=1, help="also time the other engine (1 step)")
     return ap.parse_args()
 
 
@@ -205,13 +207,15 @@ def main():
     scene = Scene.load(SCENE)
     cie = cie_analytic()
     ctx = Context(local)
+    engine_id = native.PT_ENGINE_WAVEFRONT if args.engine == "wavefront" else native.PT_ENGINE_MEGAKERNEL
+    ctx.set_engine(engine_id)
     ctx.bind(scene, cie)
     ctx.resize_accum(W, H)
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
 
     # Distinct sample indices per rank and per step (replicas, no exchange).
-    base = rank * (args.warmup + args.steps + 1) * ndisp * spf
+    base = rank * (args.warmup + args.steps + 8) * ndisp * spf
 
     def one_step(step_idx):
         frame = base + step_idx * ndisp * spf
@@ -247,6 +251,28 @@ def main():
         t_wall = time.perf_counter() - t_wall0
     ms = [a.elapsed_time(b) for a, b in times]
     ms_step = sum(ms) / len(ms)
+    iters = ctx.last_iterations()
+
+    # The other engine on the same workload (one warm-up, one timed step).
+    other = {}
+    if args.compare_engines:
+        ctx.set_engine(1 - engine_id)
+        one_step(args.warmup + args.steps)
+        ctx.wait()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            o0 = torch.cuda.Event(enable_timing=True)
+            o1 = torch.cuda.Event(enable_timing=True)
+            o0.record(stream)
+        one_step(args.warmup + args.steps + 1)
+        o1.record(stream)
+        ctx.wait()
+        torch.cuda.synchronize()
+        oms = o0.elapsed_time(o1)
+        other = {("megakernel" if engine_id == native.PT_ENGINE_WAVEFRONT else "wavefront"):
+                 {"value": samples_per_step / (oms / 1000.0), "ms_per_step": oms}}
+        ctx.set_engine(engine_id)
     if world > 1:
         import torch.distributed as dist
 
@@ -260,7 +286,7 @@ def main():
     for i in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
         acc, _ = render_offscreen(ctx, scene, cie, W, H, args.spp, spf, args.depth,
-                                  frame_offset=base + (args.warmup + args.steps + i) * ndisp * spf)
+                                  frame_offset=base + (args.warmup + args.steps + 2 + i) * ndisp * spf)
         e2e_secs.append(time.perf_counter() - t0)
     e2e_step = statistics.median(e2e_secs)
     if world > 1:
@@ -286,7 +312,10 @@ def main():
                    "samples_per_dispatch": spf, "dispatches_per_step": ndisp,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps * ndisp,
+        "engine": args.engine,
+        "engines": {args.engine: {"value": value / world, "ms_per_step": ms_step}, **other},
+        "wavefront_iterations_per_dispatch": iters if args.engine == "wavefront" else None,
+        "gpu_launches": args.steps * ndisp * ((5 * iters + 2) if args.engine == "wavefront" else 1),
         "wall_s_timed_region": t_wall,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,

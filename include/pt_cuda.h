@@ -144,6 +144,24 @@ int pt_resize_accum(pt_ctx* ctx, int width, int height);
  * stream; resolution must equal the accumulator size. */
 int pt_dispatch(pt_ctx* ctx, const pt_push* push);
 
+/* Engines behind pt_dispatch; both compute the reference's per-sample
+ * arithmetic bit for bit and differ only in scheduling.
+ *   PT_ENGINE_MEGAKERNEL: one thread per pixel, samples in order (the plain
+ *     method).  Asynchronous.
+ *   PT_ENGINE_WAVEFRONT (default): every sample is a work item in a pool of
+ *     path slots in device memory; compacted ray queues per stage and a
+ *     persistent SDF-march kernel; per-sample XYZ summed per pixel in sample
+ *     order at the end.  Allocates its scratch on first use; pt_dispatch
+ *     returns once the dispatch is resolved on the stream. */
+#define PT_ENGINE_MEGAKERNEL 0
+#define PT_ENGINE_WAVEFRONT 1
+int pt_set_engine(pt_ctx* ctx, int engine);
+int pt_get_engine(pt_ctx* ctx);
+/* Path slots of the wavefront pool (default 2^21; 208 B each). */
+int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots);
+/* Wavefront iterations the last dispatch needed (diagnostics). */
+uint32_t pt_last_iterations(pt_ctx* ctx);
+
 /* Replaces vkWaitForFences (src/pathtracer.cpp:3846): waits at most
  * timeout_ns and returns PT_ERR_TIMEOUT instead of blocking forever. */
 int pt_wait(pt_ctx* ctx, uint64_t timeout_ns);

@@ -29,7 +29,8 @@ _lib = None
 
 def build() -> str:
     src = os.path.join(HERE, "pt_oracle.c")
-    deps = [src, os.path.join(HERE, "pt_oracle.h"), os.path.join(HERE, "..", "include", "pt_cuda.h")]
+    deps = [src, os.path.join(HERE, "pt_oracle.h"), os.path.join(HERE, "..", "include", "pt_cuda.h"),
+            os.path.join(HERE, "..", "include", "pt_mathf.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         subprocess.run([os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-std=c11", "-ffp-contract=off",

@@ -25,6 +25,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wal
 
 CUDA_SOURCES = [
     "kernel/pt_megakernel.cu",
+    "kernel/pt_wavefront.cu",
     "pt_api.cu",
     "pt_sdf_source.cpp",
 ]
@@ -91,7 +92,8 @@ def build_oracle(force: bool = False) -> str:
     """Compiles the CPU restatement used by the tests (oracle/, the checker)."""
     out = os.path.join(ROOT, "oracle", "_build", "libpt_oracle.so")
     src = os.path.join(ROOT, "oracle", "pt_oracle.c")
-    hdrs = [os.path.join(ROOT, "oracle", "pt_oracle.h"), os.path.join(ROOT, "include", "pt_cuda.h")]
+    hdrs = [os.path.join(ROOT, "oracle", "pt_oracle.h"), os.path.join(ROOT, "include", "pt_cuda.h"),
+            os.path.join(ROOT, "include", "pt_mathf.h")]
     if force or not os.path.exists(out) or any(os.path.getmtime(s) > os.path.getmtime(out) for s in [src, *hdrs]):
         os.makedirs(os.path.dirname(out), exist_ok=True)
         _run([os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fno-fast-math",

@@ -440,10 +440,10 @@ PT_DI float scene_sdf(const KScene& S, float3 p, uint32_t set1) {
     return sdf;
 }
 // Out-of-line copy for the cold call sites (sign at the origin, normals).
-__device__ __noinline__ float scene_sdf_cold(const KScene& S, float3 p, uint32_t set1) { return scene_sdf(S, p, set1); }
+static __device__ __noinline__ float scene_sdf_cold(const KScene& S, float3 p, uint32_t set1) { return scene_sdf(S, p, set1); }
 
 // SDFMATERIAL() with the spliced minMaterial lines (SC:681-683, SC:713-719).
-__device__ __noinline__ float scene_sdf_material(const KScene& S, float3 p, uint32_t set1) {
+static __device__ __noinline__ float scene_sdf_material(const KScene& S, float3 p, uint32_t set1) {
     float sdf = PT_MAXDIST;
     float mat = 0.0f;
     uint32_t bits = set1 & ((S.meta.nplug >= 32) ? 0xFFFFFFFFu : ((1u << S.meta.nplug) - 1u));
@@ -577,10 +577,10 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
     return false;
 }
 
-// Intersection (SC:862-934) and the object loop of LightSourceVisibilityCheck
-// (SC:1121-1223): objectID = index of the last object whose test hit, -2 for
-// an SDF hit, -1 for none.
-PT_DI void intersect_all(const KScene& S, float3 org, float3 dir, Hit& h, int& objectID) {
+// The analytic part of Intersection (SC:862-923) and of the object loop of
+// LightSourceVisibilityCheck (SC:1121-1201): objectID = index of the last
+// object whose test hit, -1 for none.
+PT_DI void intersect_analytic(const KScene& S, float3 org, float3 dir, Hit& h, int& objectID) {
     int id = -1;
     const int n0 = S.meta.n[0], n1 = S.meta.n[1], n2 = S.meta.n[2], n3 = S.meta.n[3], n4 = S.meta.n[4];
     int gi = 0;
@@ -634,8 +634,14 @@ PT_DI void intersect_all(const KScene& S, float3 org, float3 dir, Hit& h, int& o
         if (!bounding_sphere(org, dir, pos, S.objects[b + 13])) continue;
         if (cyclide_intersect(S, org, dir, b, s_rotation(S, gi), h)) id = gi;
     }
-    if (S.meta.n[5] > 0) {
-        if (sphere_trace(S, org, dir, h)) id = -2;
-    }
     objectID = id;
+}
+
+// Intersection (SC:862-934) / LightSourceVisibilityCheck's loop: the analytic
+// objects, then sphere tracing of the SDFs (objectID -2 for an SDF hit).
+PT_DI void intersect_all(const KScene& S, float3 org, float3 dir, Hit& h, int& objectID) {
+    intersect_analytic(S, org, dir, h, objectID);
+    if (S.meta.n[5] > 0) {
+        if (sphere_trace(S, org, dir, h)) objectID = -2;
+    }
 }

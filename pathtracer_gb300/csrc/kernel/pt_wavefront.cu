@@ -1,0 +1,479 @@
+// pt_wavefront.cu — the wavefront renderer: path state in HBM, compacted
+// ray queues, a persistent SDF-march kernel with per-lane ray refill.
+//
+// The plain megakernel keeps one pixel per thread, so lanes wait for the
+// slowest neighbour's SDF march and for pixels with more work (measured:
+// 5.3 of 32 lanes active per warp instruction).  Here every path sample of a
+// dispatch is an independent work item in a pool of P slots; each iteration
+// runs four stage kernels over compacted queues:
+//   isect  analytic primitives + SDF bounding boxes for every pending ray
+//          (primary or shadow) -> rays that need sphere tracing go to MARCH,
+//          the rest to SHADE;
+//   march  persistent: each lane holds one ray and does exactly one SDF
+//          evaluation per loop iteration (sign probe, march step, normal
+//          probes), refilling from the queue the moment its ray is done, so
+//          all lanes execute the same SDF code;
+//   shade  emitter / miss / BRDF sample / light sample / shadow result /
+//          Russian roulette (the shared pt_path.cuh functions) -> next ray to
+//          the next ISECT queue, finished samples write their XYZ and free
+//          their slot;
+//   gen    start new samples in free slots.
+// A one-thread bookkeeping kernel advances the counters.  Queues are filled
+// with warp-aggregated atomics (ballot + popc + one atomicAdd per warp).
+// After the last sample, `resolve` sums each pixel's samples in sample order
+// and applies Rendering/Accumulate — the same float operations, in the same
+// order, as the megakernel and the shader, so results are bit-identical.
+#include <cuda_runtime.h>
+
+#include "pt_path.cuh"
+#include "pt_wavefront.h"
+
+namespace {
+
+constexpr uint32_t kShadowFlag = 1u << 30;
+constexpr int kStageThreads = 256;
+
+// Warp-aggregated append of `value` to queue[count++] for lanes with pred.
+// Must be called by all 32 lanes of the warp.
+PT_DI void q_push(uint32_t* __restrict__ queue, uint32_t* count, uint32_t value, bool pred) {
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) queue[base + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = value;
+}
+
+struct PoolView {
+    float4 *s0, *s1, *s2, *s3, *s4, *s5, *s6, *s7;  // see WfPool
+    uint4* s8;
+    float4 *s9, *h0, *h1;
+};
+
+PT_DI PoolView view(const WfArgs& A) {
+    const WfPool& p = A.pool;
+    return PoolView{p.s0, p.s1, p.s2, p.s3, p.s4, p.s5, p.s6, p.s7, p.s8, p.s9, p.h0, p.h1};
+}
+
+PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t& flags, uint32_t& sample) {
+    const float4 a = v.s0[slot], b = v.s1[slot], c = v.s2[slot], d = v.s3[slot];
+    ps.org = f3(a.x, a.y, a.z);
+    ps.mis = a.w;
+    ps.dir = f3(b.x, b.y, b.z);
+    ps.brdfPdf = b.w;
+    ps.shDir = f3(c.x, c.y, c.z);
+    ps.cosL = c.w;
+    ps.nrm = f3(d.x, d.y, d.z);
+    ps.lightPdf = d.w;
+    ps.brdf = v.s4[slot];
+    ps.rr = v.s5[slot];
+    ps.radiance = v.s6[slot];
+    ps.l = v.s7[slot];
+    const uint4 m = v.s8[slot];
+    ps.seed = m.x;
+    flags = m.y;
+    ps.bounce = (int)(m.y & 0x3fffffffu);
+    sample = m.z;
+    ps.shObj = (int)m.w;
+    const float4 e = v.s9[slot];
+    ps.shLightID = e.x;
+    ps.ev = __float_as_uint(e.y);
+}
+
+PT_DI void store_state(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t flags, uint32_t sample) {
+    v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
+    v.s1[slot] = make_float4(ps.dir.x, ps.dir.y, ps.dir.z, ps.brdfPdf);
+    v.s2[slot] = make_float4(ps.shDir.x, ps.shDir.y, ps.shDir.z, ps.cosL);
+    v.s3[slot] = make_float4(ps.nrm.x, ps.nrm.y, ps.nrm.z, ps.lightPdf);
+    v.s4[slot] = ps.brdf;
+    v.s5[slot] = ps.rr;
+    v.s6[slot] = ps.radiance;
+    v.s7[slot] = ps.l;
+    v.s8[slot] = make_uint4(ps.seed, flags | ((uint32_t)ps.bounce & 0x3fffffffu), sample, (uint32_t)ps.shObj);
+    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
+}
+
+// Sample id s of a dispatch: k = s / (W*H), pixel = s % (W*H).  The colour
+// buffer is [k][pixel], so `resolve` reads it coalesced; traces use the
+// megakernel's path index pixel * spf + k.
+PT_DI size_t trace_index(const pt_push& pc, uint32_t s) {
+    const uint32_t npix = (uint32_t)pc.resolution[0] * (uint32_t)pc.resolution[1];
+    return (size_t)(s % npix) * (size_t)pc.samplesPerFrame + (size_t)(s / npix);
+}
+
+template <bool TRACE>
+__global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ WfArgs A) {
+    __shared__ CamInfo camS;
+    if (threadIdx.x == 0) camS = make_camera(A.pc);
+    __syncthreads();
+    WfCounters& C = *A.counters;
+    const uint32_t remaining = C.total - C.next_sample;
+    const uint32_t n = min(C.n_free, remaining);
+    const uint32_t nfree = C.n_free;
+    const uint32_t first = C.next_sample;
+    const uint32_t nxt = C.cur ^ 1u;
+    const PoolView v = view(A);
+    const pt_push& pc = A.pc;
+    const int W = pc.resolution[0], H = pc.resolution[1];
+    const uint32_t npix = (uint32_t)W * (uint32_t)H;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t slot = 0;
+        if (valid) {
+            slot = A.q_free[nfree - n + i];
+            const uint32_t s = first + i;
+            const uint32_t k = s / npix, pix = s % npix;
+            const int x = (int)(pix % (uint32_t)W), y = (int)(pix / (uint32_t)W);
+            const uint32_t xx = (uint32_t)x, yy = (uint32_t)H - (uint32_t)y;
+            const float uvx = (2.0f * (float)xx - (float)W) / (float)H;
+            const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
+            PathState ps;
+            start_sample(ps, pc, camS, xx, yy, uvx, uvy, (int)k);
+            ps.nrm = f3(0.0f, 0.0f, 0.0f);
+            ps.shDir = f3(0.0f, 0.0f, 1.0f);
+            ps.brdf = f4s(0.0f);
+            ps.brdfPdf = ps.lightPdf = ps.cosL = 0.0f;
+            ps.shLightID = -1.0f;
+            ps.shObj = 0;
+            ps.ev = 0;
+            store_state(v, slot, ps, 0u, s);
+        }
+        q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, valid);
+    }
+}
+
+__global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant__ WfArgs A) {
+    const KScene& S = *A.scene;
+    WfCounters& C = *A.counters;
+    const uint32_t cur = C.cur;
+    const uint32_t n = C.n_isect[cur];
+    const uint32_t* __restrict__ q = A.q_isect[cur];
+    const PoolView v = view(A);
+    const bool has_sdf = S.meta.n[5] > 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        bool march = false;
+        uint32_t slot = 0;
+        if (valid) {
+            slot = q[i];
+            const float4 o = v.s0[slot];
+            const uint32_t flags = v.s8[slot].y;
+            const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
+            const float3 org = f3(o.x, o.y, o.z), dir = f3(d.x, d.y, d.z);
+            Hit h;
+            h.hitdist = PT_MAXDIST;
+            h.normal = f3(0.0f, 0.0f, 0.0f);
+            h.materialID = 0.0f;
+            h.lightID = -1.0f;
+            int objectID = -1;
+            intersect_analytic(S, org, dir, h, objectID);
+            if (has_sdf) {
+                const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+                float2 tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
+                uint32_t set1 = 0;
+                march = search_sdf(S, org, invdir, tmm, set1);
+            }
+            v.h0[slot] = make_float4(h.hitdist, h.materialID, h.lightID, __int_as_float(objectID));
+            v.h1[slot] = make_float4(h.normal.x, h.normal.y, h.normal.z, 0.0f);
+        }
+        q_push(A.q_march, &C.n_march, slot, valid && march);
+        q_push(A.q_shade, &C.n_shade, slot, valid && !march);
+    }
+}
+
+// SphereTracing (SC:779-860) with one SDF evaluation per loop iteration per lane.
+enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NORMAL5 = 8, MP_NO_BOX = 9 };
+
+__global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant__ WfArgs A) {
+    const KScene& S = *A.scene;
+    WfCounters& C = *A.counters;
+    const uint32_t n = C.n_march;
+    const PoolView v = view(A);
+    const int lane = threadIdx.x & 31;
+
+    uint32_t slot = 0;
+    int phase = MP_EMPTY;
+    bool exhausted = false;
+    float3 org = f3(0.0f, 0.0f, 0.0f), dir = f3(0.0f, 0.0f, 1.0f), invdir = f3(0.0f, 0.0f, 0.0f), p = org;
+    float t = 0.0f, insT = 0.0f, omega = 0.0f, prevR = 0.0f, hitdist = 0.0f, k = 0.0f, nplus = 0.0f;
+    float3 nv = f3(0.0f, 0.0f, 0.0f);
+    float2 tmm = make_float2(0.0f, 0.0f);
+    uint32_t set1 = 0;
+    int points = 0, iter = 0;
+    const float omegaMax = 1.70f, omegaSpeed = 0.20f, e = 1e-4f;
+
+    for (;;) {
+        // Refill lanes that have no ray (warp-aggregated fetch).
+        const bool need = (phase == MP_EMPTY) && !exhausted;
+        const unsigned mneed = __ballot_sync(0xffffffffu, need);
+        if (mneed) {
+            const int leader = __ffs(mneed) - 1;
+            uint32_t b = 0;
+            if (lane == leader) b = atomicAdd(&C.march_cursor, (uint32_t)__popc(mneed));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (need) {
+                const uint32_t idx = b + (uint32_t)__popc(mneed & ((1u << lane) - 1u));
+                if (idx < n) {
+                    slot = A.q_march[idx];
+                    const float4 o = v.s0[slot];
+                    const uint32_t flags = v.s8[slot].y;
+                    const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
+                    org = f3(o.x, o.y, o.z);
+                    dir = f3(d.x, d.y, d.z);
+                    hitdist = v.h0[slot].x;
+                    invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+                    t = 1e-3f;
+                    insT = 0.0f;
+                    omega = omegaMax;
+                    prevR = 0.0f;
+                    points = 0;
+                    iter = 0;
+                    tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
+                    set1 = 0;
+                    if (search_sdf(S, org, invdir, tmm, set1)) {
+                        t = fmaxf(tmm.x, t);
+                        p = fma3s(dir, t, org);
+                        phase = MP_SIGN;
+                    } else {
+                        phase = MP_NO_BOX;  // (isect found a box with the same test) keep the analytic hit
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, phase != MP_EMPTY) == 0) break;
+
+        // One SDF evaluation.
+        const bool evalLane = (phase >= MP_SIGN && phase <= MP_NORMAL5);
+        float3 q = p;
+        if (phase == MP_SIGN) q = org;
+        if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
+            // CalculateNumericalSDFNormals (SC:721-730): p +- h.xyy, h.yxy, h.yyx
+            const int j = phase - MP_NORMAL0;
+            const float ex = (j == 0) ? e : 0.0f, ey = (j == 2) ? e : 0.0f, ez = (j == 4) ? e : 0.0f;
+            const float mx = (j == 1) ? e : 0.0f, my = (j == 3) ? e : 0.0f, mz = (j == 5) ? e : 0.0f;
+            q = (j & 1) ? f3(p.x - mx, p.y - my, p.z - mz) : f3(p.x + ex, p.y + ey, p.z + ez);
+        }
+        float val = 0.0f;
+        if (evalLane) val = scene_sdf(S, q, set1);
+
+        bool finished = false, hit = false;
+        if (phase == MP_SIGN) {
+            k = sign_glsl(val);
+            phase = MP_STEP;
+        } else if (phase == MP_STEP) {
+            const float radius = val;
+            bool exitLoop = false;
+            if (insT > (fabsf(prevR) + fabsf(radius))) {
+                t -= insT;
+                omega = 1.0f;
+                insT = prevR * omega * k;
+                t += insT;
+                p = fma3s(dir, t, org);
+            } else if (fabsf(radius) < 1e-4f) {
+                exitLoop = true;
+            } else {
+                if (t > tmm.y) {
+                    points += 1;
+                } else {
+                    points = 0;
+                }
+                bool researched = false;
+                if (points >= 2) {
+                    t = tmm.y + 1e-3f;
+                    tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
+                    if (search_sdf(S, fma3s(dir, t, org), invdir, tmm, set1)) {
+                        tmm.x += t;
+                        tmm.y += t;
+                        t = fmaxf(tmm.x, t);
+                        p = fma3s(dir, t, org);
+                        researched = true;
+                    } else {
+                        finished = true;  // left every SDF box: no SDF hit
+                    }
+                }
+                if (!finished && !researched) {
+                    insT = radius * omega * k;
+                    t += insT;
+                    p = fma3s(dir, t, org);
+                    const float omegaSpeedFactor = fminf(radius / prevR, 0.99f);
+                    omega += omegaSpeed * (fminf(1.0f / (1.0f - omegaSpeedFactor), omegaMax) - omega);
+                    prevR = radius;
+                }
+            }
+            if (!finished && !exitLoop) {
+                iter++;
+                if (iter >= 512) exitLoop = true;
+            }
+            if (exitLoop) {
+                if (t < hitdist) {
+                    p = fma3s(dir, t, org);
+                    phase = MP_NORMAL0;
+                } else {
+                    finished = true;
+                }
+            }
+        } else if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
+            const int j = phase - MP_NORMAL0;
+            if ((j & 1) == 0) {
+                nplus = val;
+            } else {
+                const float dv = nplus - val;
+                if (j == 1) nv.x = dv;
+                else if (j == 3) nv.y = dv;
+                else nv.z = dv;
+            }
+            phase++;
+            if (phase > MP_NORMAL5) {
+                hit = true;
+                finished = true;
+            }
+        } else if (phase == MP_NO_BOX) {
+            finished = true;
+        }
+
+        if (finished && hit) {
+            const float3 nrm = normalize3(nv);
+            const float mat = scene_sdf_material(S, p, set1);
+            v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
+            v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        }
+        q_push(A.q_shade, &C.n_shade, slot, finished);
+        if (finished) phase = MP_EMPTY;
+    }
+}
+
+template <bool TRACE>
+__global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant__ WfArgs A) {
+    const KScene& S = *A.scene;
+    WfCounters& C = *A.counters;
+    const uint32_t n = C.n_shade;
+    const uint32_t nxt = C.cur ^ 1u;
+    const PoolView v = view(A);
+    const pt_push& pc = A.pc;
+    const int depth = pc.pathLength;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t slot = 0;
+        bool again = false, freed = false;
+        if (valid) {
+            slot = A.q_shade[i];
+            PathState ps;
+            uint32_t flags, sample;
+            load_state(v, slot, ps, flags, sample);
+            const float4 h0 = v.h0[slot], h1 = v.h1[slot];
+            Hit h;
+            h.hitdist = h0.x;
+            h.materialID = h0.y;
+            h.lightID = h0.z;
+            h.normal = f3(h1.x, h1.y, h1.z);
+            const int objectID = __float_as_int(h0.w);
+            const StepResult r = (flags & kShadowFlag) ? shade_shadow<TRACE>(ps, S, objectID, depth)
+                                                       : shade_primary<TRACE>(ps, S, h, objectID, depth);
+            if (TRACE && r != STEP_SHADOW && A.trace.events) {
+                const size_t p = trace_index(pc, sample);
+                const int b = ps.bounce - 1;
+                if (b < A.trace.cap) A.trace.events[p * (size_t)A.trace.cap + b] = ps.ev;
+            }
+            if (r == STEP_TERMINATED) {
+                const float3 col = sample_color(ps, A.cie);
+                A.colors[sample] = make_float4(col.x, col.y, col.z, 0.0f);
+                if (TRACE) {
+                    const size_t p = trace_index(pc, sample);
+                    if (A.trace.nevents) A.trace.nevents[p] = (uint32_t)ps.bounce;
+                    if (A.trace.colors) {
+                        A.trace.colors[3 * p] = col.x;
+                        A.trace.colors[3 * p + 1] = col.y;
+                        A.trace.colors[3 * p + 2] = col.z;
+                    }
+                }
+                freed = true;
+            } else {
+                store_state(v, slot, ps, (r == STEP_SHADOW) ? kShadowFlag : 0u, sample);
+                again = true;
+            }
+        }
+        q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, again);
+        q_push(A.q_free, &C.n_free, slot, freed);
+    }
+}
+
+__global__ void wf_book(WfCounters* __restrict__ Cp, uint32_t pool) {
+    WfCounters& C = *Cp;
+    const uint32_t n = min(C.n_free, C.total - C.next_sample);
+    C.next_sample += n;
+    C.n_free -= n;
+    C.n_isect[C.cur] = 0;
+    C.cur ^= 1u;
+    C.n_march = 0;
+    C.march_cursor = 0;
+    C.n_shade = 0;
+    C.iterations += 1;
+    C.done = (C.next_sample == C.total && C.n_free == pool) ? 1u : 0u;
+}
+
+__global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_free, uint32_t pool, uint32_t total) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < pool) q_free[i] = i;
+    if (i == 0) {
+        WfCounters& C = *Cp;
+        C.n_isect[0] = C.n_isect[1] = 0;
+        C.cur = 0;
+        C.n_march = C.march_cursor = C.n_shade = 0;
+        C.n_free = pool;
+        C.next_sample = 0;
+        C.total = total;
+        C.iterations = 0;
+        C.done = (total == 0) ? 1u : 0u;
+    }
+}
+
+// Rendering + Accumulate over the ordered sample colours, one thread per pixel.
+__global__ void __launch_bounds__(kStageThreads) wf_resolve(const __grid_constant__ WfArgs A) {
+    const pt_push& pc = A.pc;
+    const uint32_t npix = (uint32_t)pc.resolution[0] * (uint32_t)pc.resolution[1];
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    float3 sum = f3(0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < pc.samplesPerFrame; k++) {
+        const float4 c = A.colors[(size_t)k * npix + pix];
+        sum = sum + f3(c.x, c.y, c.z);
+    }
+    A.accum[pix] = accumulate(pc, sum, A.accum[pix]);
+}
+
+}  // namespace
+
+cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream) {
+    wf_init<<<(a->pool_size + 255) / 256, 256, 0, stream>>>(a->counters, a->q_free, a->pool_size, a->total);
+    return cudaGetLastError();
+}
+
+cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream) {
+    wf_isect<<<grid, kStageThreads, 0, stream>>>(*a);
+    wf_march<<<grid, kStageThreads, 0, stream>>>(*a);
+    if (trace) {
+        wf_shade<true><<<grid, kStageThreads, 0, stream>>>(*a);
+        wf_gen<true><<<grid, kStageThreads, 0, stream>>>(*a);
+    } else {
+        wf_shade<false><<<grid, kStageThreads, 0, stream>>>(*a);
+        wf_gen<false><<<grid, kStageThreads, 0, stream>>>(*a);
+    }
+    wf_book<<<1, 1, 0, stream>>>(a->counters, a->pool_size);
+    return cudaGetLastError();
+}
+
+cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, cudaStream_t stream) {
+    const uint32_t npix = (uint32_t)a->pc.resolution[0] * (uint32_t)a->pc.resolution[1];
+    wf_resolve<<<(npix + kStageThreads - 1) / kStageThreads, kStageThreads, 0, stream>>>(*a);
+    return cudaGetLastError();
+}

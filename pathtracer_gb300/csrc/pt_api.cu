@@ -16,6 +16,7 @@
 
 #include "../../include/pt_cuda.h"
 #include "kernel/pt_megakernel.h"
+#include "kernel/pt_wavefront.h"
 
 struct pt_ctx {
     int device = 0;
@@ -31,6 +32,13 @@ struct pt_ctx {
     pt_sdf_plugin plug[PT_MAX_LIVE_SDFS];
     int nplug = 0;
     KTrace trace{nullptr, nullptr, nullptr, 0};
+    int engine = PT_ENGINE_WAVEFRONT;
+    uint32_t pool_cap = 1u << 21;  // wavefront path slots
+    KScene* d_scene = nullptr;     // device copy for the wavefront kernels
+    void* d_wf = nullptr;          // wavefront scratch (pool, queues, colours, counters)
+    size_t wf_bytes = 0;
+    WfCounters* h_counters = nullptr;  // pinned
+    uint32_t last_iterations = 0;
     std::string err;
 };
 
@@ -64,7 +72,50 @@ void refresh_plugins(pt_ctx* ctx) {
     ctx->params->s.meta.nplug = ctx->nplug;
 }
 
+// Keeps the device copy of the scene (read by the wavefront kernels) in step
+// with the launch-parameter copy (read by the megakernel).
+cudaError_t sync_device_scene(pt_ctx* ctx) {
+    if (!ctx->has_scene) return cudaSuccess;
+    return cudaMemcpyAsync(ctx->d_scene, &ctx->params->s, sizeof(KScene), cudaMemcpyHostToDevice, ctx->stream);
+}
+
+template <typename T>
+T* carve(char*& p, size_t count) {
+    T* r = reinterpret_cast<T*>(p);
+    p += ((count * sizeof(T) + 255) / 256) * 256;
+    return r;
+}
+
+// Lays the wavefront's buffers out in one scratch allocation.
+size_t wavefront_layout(char* base, uint32_t pool, uint32_t total, WfArgs* a) {
+    char* p = base;
+    WfPool& P = a->pool;
+    P.s0 = carve<float4>(p, pool);
+    P.s1 = carve<float4>(p, pool);
+    P.s2 = carve<float4>(p, pool);
+    P.s3 = carve<float4>(p, pool);
+    P.s4 = carve<float4>(p, pool);
+    P.s5 = carve<float4>(p, pool);
+    P.s6 = carve<float4>(p, pool);
+    P.s7 = carve<float4>(p, pool);
+    P.s8 = carve<uint4>(p, pool);
+    P.s9 = carve<float4>(p, pool);
+    P.h0 = carve<float4>(p, pool);
+    P.h1 = carve<float4>(p, pool);
+    a->q_isect[0] = carve<uint32_t>(p, pool);
+    a->q_isect[1] = carve<uint32_t>(p, pool);
+    a->q_march = carve<uint32_t>(p, pool);
+    a->q_shade = carve<uint32_t>(p, pool);
+    a->q_free = carve<uint32_t>(p, pool);
+    a->colors = carve<float4>(p, total);
+    a->counters = carve<WfCounters>(p, 1);
+    return (size_t)(p - base);
+}
+
+
 }  // namespace
+
+static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push);
 
 extern "C" {
 
@@ -85,6 +136,8 @@ int pt_create(pt_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_cie, sizeof(float) * PT_CIE_TABLE_SIZE);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rot, sizeof(float) * 9 * PT_MAX_SCENE_OBJECTS);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_scene, sizeof(KScene));
+    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, sizeof(WfCounters));
     if (e != cudaSuccess) {
         pt_destroy(ctx);
         return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
@@ -101,6 +154,9 @@ int pt_destroy(pt_ctx* ctx) {
     if (ctx->d_accum) cudaFree(ctx->d_accum);
     if (ctx->d_cie) cudaFree(ctx->d_cie);
     if (ctx->d_rot) cudaFree(ctx->d_rot);
+    if (ctx->d_scene) cudaFree(ctx->d_scene);
+    if (ctx->d_wf) cudaFree(ctx->d_wf);
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     if (ctx->done) cudaEventDestroy(ctx->done);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx->params;
@@ -120,6 +176,8 @@ int pt_set_sdf_plugins(pt_ctx* ctx, const pt_sdf_plugin* plugins, int n) {
     if (n > 0) std::memcpy(ctx->plug, plugins, sizeof(pt_sdf_plugin) * (size_t)n);
     ctx->nplug = n;
     refresh_plugins(ctx);
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    PT_CUDA_TRY(ctx, sync_device_scene(ctx));
     return PT_OK;
 }
 
@@ -187,6 +245,7 @@ int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo) {
     }
     PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->has_scene = true;
+    PT_CUDA_TRY(ctx, sync_device_scene(ctx));
     return PT_OK;
 }
 
@@ -230,11 +289,31 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push) {
     P.accum = ctx->d_accum;
     P.cie = ctx->d_cie;
     P.trace = ctx->trace;
+    if (ctx->engine == PT_ENGINE_WAVEFRONT && push->pathLength > 0) return dispatch_wavefront(ctx, push);
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
     PT_CUDA_TRY(ctx, ptk_launch_megakernel(&P, trace, ctx->stream));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
 }
+
+int pt_set_engine(pt_ctx* ctx, int engine) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (engine != PT_ENGINE_MEGAKERNEL && engine != PT_ENGINE_WAVEFRONT)
+        return fail(ctx, PT_ERR_INVALID, "pt_set_engine: unknown engine");
+    ctx->engine = engine;
+    return PT_OK;
+}
+
+int pt_get_engine(pt_ctx* ctx) { return ctx ? ctx->engine : -1; }
+
+int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (slots < 1024 || slots > (1u << 28)) return fail(ctx, PT_ERR_INVALID, "pt_set_wavefront_pool: 1024..2^28 slots");
+    ctx->pool_cap = slots;
+    return PT_OK;
+}
+
+uint32_t pt_last_iterations(pt_ctx* ctx) { return ctx ? ctx->last_iterations : 0; }
 
 int pt_wait(pt_ctx* ctx, uint64_t timeout_ns) {
     if (!ctx) return PT_ERR_INVALID;
@@ -300,3 +379,55 @@ const char* pt_last_error(pt_ctx* ctx) {
 }
 
 }  // extern "C"
+
+// The wavefront dispatch: iterations are launched in chunks; between chunks
+// the counters are read back to stop once every sample has finished.
+static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
+    const uint64_t total64 = (uint64_t)push->resolution[0] * (uint64_t)push->resolution[1] *
+                             (uint64_t)push->samplesPerFrame;
+    if (total64 >= (1ull << 31)) return fail(ctx, PT_ERR_INVALID, "pt_dispatch: more than 2^31 samples in one dispatch");
+    const uint32_t total = (uint32_t)total64;
+    const uint32_t pool = total < ctx->pool_cap ? (total < 1024u ? 1024u : total) : ctx->pool_cap;
+    WfArgs a;
+    std::memset(&a, 0, sizeof a);
+    const size_t need = wavefront_layout(reinterpret_cast<char*>(0), pool, total, &a) + 256;
+    if (need > ctx->wf_bytes) {
+        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->d_wf) cudaFree(ctx->d_wf);
+        ctx->d_wf = nullptr;
+        ctx->wf_bytes = 0;
+        PT_CUDA_TRY(ctx, cudaMalloc(&ctx->d_wf, need));
+        ctx->wf_bytes = need;
+    }
+    wavefront_layout(static_cast<char*>(ctx->d_wf), pool, total, &a);
+    a.scene = ctx->d_scene;
+    a.pc = *push;
+    a.accum = ctx->d_accum;
+    a.cie = ctx->d_cie;
+    a.trace = ctx->trace;
+    a.pool_size = pool;
+    a.total = total;
+    const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
+    int dev_sms = 0;
+    PT_CUDA_TRY(ctx, cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int grid = dev_sms * 4;  // 4 blocks of 256 threads per SM (64 registers)
+    PT_CUDA_TRY(ctx, ptk_wavefront_launch_init(&a, ctx->stream));
+    const int depth = push->pathLength;
+    const uint64_t max_iter = ((uint64_t)total / pool + 2) * (2ull * (uint64_t)depth + 3) + 16;
+    uint64_t iter = 0;
+    int chunk = 8;
+    for (;;) {
+        for (int c = 0; c < chunk; c++) PT_CUDA_TRY(ctx, ptk_wavefront_launch_iteration(&a, trace, grid, ctx->stream));
+        iter += (uint64_t)chunk;
+        PT_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_counters, a.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->h_counters->done) break;
+        if (iter > max_iter) return fail(ctx, PT_ERR_KERNEL, "pt_dispatch: wavefront did not drain");
+        if (chunk < 64) chunk *= 2;
+    }
+    ctx->last_iterations = ctx->h_counters->iterations;
+    PT_CUDA_TRY(ctx, ptk_wavefront_launch_resolve(&a, ctx->stream));
+    PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
+    return PT_OK;
+}

@@ -23,6 +23,9 @@ PT_ERR_NO_SCENE = 5
 PT_ERR_OOM = 6
 PT_ERR_KERNEL = 7
 
+PT_ENGINE_MEGAKERNEL = 0
+PT_ENGINE_WAVEFRONT = 1
+
 UBO_FLOATS = 4097  # 7 + 1024 + 768 + 783 + 128 + 64 + 1323
 UBO_OFFSETS = {
     "numObjects": (0, 7),
@@ -141,6 +144,10 @@ CUDA_API = [
     ("pt_set_trace", _i, [_vp, _vp, _vp, _vp, _i]),
     ("pt_sdf_source_fingerprint", ctypes.c_uint64, [ctypes.c_char_p]),
     ("pt_mathf_eval", _i, [_vp, _i, _vp, _vp, _vp, _i]),
+    ("pt_set_engine", _i, [_vp, _i]),
+    ("pt_get_engine", _i, [_vp]),
+    ("pt_set_wavefront_pool", _i, [_vp, ctypes.c_uint32]),
+    ("pt_last_iterations", ctypes.c_uint32, [_vp]),
 ]
 
 # Every symbol include/pt_host.h declares.

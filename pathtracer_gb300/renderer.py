@@ -181,6 +181,18 @@ class Context:
     def set_stream(self, stream: int | None):
         self._check(self._lib.pt_set_stream(self._h, stream))
 
+    def set_engine(self, engine: int):
+        self._check(self._lib.pt_set_engine(self._h, engine))
+
+    def engine(self) -> int:
+        return self._lib.pt_get_engine(self._h)
+
+    def set_wavefront_pool(self, slots: int):
+        self._check(self._lib.pt_set_wavefront_pool(self._h, slots))
+
+    def last_iterations(self) -> int:
+        return self._lib.pt_last_iterations(self._h)
+
     def set_trace(self, events_ptr: int, nevents_ptr: int, colors_ptr: int, depth_cap: int):
         self._check(self._lib.pt_set_trace(self._h, events_ptr or None, nevents_ptr or None, colors_ptr or None,
                                            depth_cap))

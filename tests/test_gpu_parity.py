@@ -1,4 +1,5 @@
-"""Parity of the sm_103a megakernel with the CPU restatement of the shader.
+"""Parity of both sm_103a engines (megakernel, wavefront) with the CPU
+restatement of the shader.
 
 Every test calls the library through its C ABI (ctypes), on the same scene,
 UBO and push constants the oracle gets.  Criteria (oracle/compare.py):
@@ -27,11 +28,15 @@ def rt(built):
     return {"Context": Context, "Scene": Scene, "cie": cie_analytic()}
 
 
-def _setup(rt, name, W, H):
+ENGINES = [0, 1]  # PT_ENGINE_MEGAKERNEL, PT_ENGINE_WAVEFRONT
+
+
+def _setup(rt, name, W, H, engine=1):
     from oracle import compare
 
     scene = rt["Scene"].load(os.path.join(SCENES, name + ".json"))
     ctx = rt["Context"](0)
+    ctx.set_engine(engine)
     ctx.bind(scene, rt["cie"])
     ctx.resize_accum(W, H)
     ubo = scene.pack_ubo(rt["cie"])
@@ -44,6 +49,7 @@ def _check(report):
     assert compare.passes(report), report
 
 
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize(
     "name,W,H,spf,depth",
     [
@@ -53,10 +59,10 @@ def _check(report):
         ("menger_terrain", 48, 40, 4, 12),
     ],
 )
-def test_single_dispatch_matches_oracle(rt, name, W, H, spf, depth):
+def test_single_dispatch_matches_oracle(rt, name, W, H, spf, depth, engine):
     from oracle import compare
 
-    scene, ctx, ubo, plugins = _setup(rt, name, W, H)
+    scene, ctx, ubo, plugins = _setup(rt, name, W, H, engine)
     push = scene.push_constants(W, H, spf, spf, spf, depth)
     acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=depth)
     acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
@@ -66,12 +72,13 @@ def test_single_dispatch_matches_oracle(rt, name, W, H, spf, depth):
     ctx.close()
 
 
-def test_ragged_resolution_and_short_paths(rt):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_ragged_resolution_and_short_paths(rt, engine):
     """W, H not multiples of the 16x8 block; pathLength 1 and 0."""
     from oracle import compare
 
     W, H = 37, 23
-    scene, ctx, ubo, plugins = _setup(rt, "feature_mix", W, H)
+    scene, ctx, ubo, plugins = _setup(rt, "feature_mix", W, H, engine)
     for depth in (1, 0):
         ctx.resize_accum(W, H)
         push = scene.push_constants(W, H, 3, 3, 3, depth)
@@ -81,13 +88,14 @@ def test_ragged_resolution_and_short_paths(rt):
     ctx.close()
 
 
-def test_progressive_running_mean_and_ema(rt):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_progressive_running_mean_and_ema(rt, engine):
     """Several dispatches: running mean (SC:1504-1506), then a reset frame with
     frame > spf that takes the EMA branch (SC:1500-1502)."""
     from oracle import compare
 
     W, H, spf, depth = 40, 32, 2, 5
-    scene, ctx, ubo, plugins = _setup(rt, "cornell_box", W, H)
+    scene, ctx, ubo, plugins = _setup(rt, "cornell_box", W, H, engine)
     acc_o = np.zeros((H, W, 4), np.float32)
     frame = cur = 0
     for it in range(4):
@@ -160,6 +168,7 @@ def test_wait_deadline(rt):
     W = H = 512
     scene = rt["Scene"].load(os.path.join(SCENES, "mandelbulb_plane.json"))
     with rt["Context"](0) as ctx:
+        ctx.set_engine(0)  # the megakernel's dispatch returns before the work is done
         ctx.bind(scene, rt["cie"])
         ctx.resize_accum(W, H)
         ctx.dispatch(scene.push_constants(W, H, 64, 64, 64, 6))
@@ -173,3 +182,38 @@ def test_wait_deadline(rt):
         acc = ctx.read_accum()
         assert np.isfinite(acc).all()
         assert timed_out
+
+
+@pytest.mark.parametrize("name,W,H,spf,depth", [("mandelbulb_plane", 256, 256, 16, 6), ("feature_mix", 200, 150, 8, 8),
+                                                ("menger_terrain", 160, 120, 8, 12)])
+def test_wavefront_equals_megakernel_bitwise(rt, name, W, H, spf, depth):
+    """The two engines schedule the same per-sample arithmetic differently;
+    their accumulators are identical bit for bit."""
+    scene = rt["Scene"].load(os.path.join(SCENES, name + ".json"))
+    out = []
+    for engine in ENGINES:
+        with rt["Context"](0) as ctx:
+            ctx.set_engine(engine)
+            ctx.bind(scene, rt["cie"])
+            ctx.resize_accum(W, H)
+            for it in range(2):
+                ctx.dispatch(scene.push_constants(W, H, spf * (it + 1), spf * (it + 1), spf, depth))
+            ctx.wait()
+            out.append(ctx.read_accum())
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
+def test_wavefront_small_pool_recycles_slots(rt):
+    """A pool far smaller than the sample count: slots are freed and reused
+    many times; results stay identical to the oracle."""
+    from oracle import compare
+
+    W, H, spf, depth = 48, 40, 4, 6
+    scene, ctx, ubo, plugins = _setup(rt, "feature_mix", W, H, 1)
+    ctx.set_wavefront_pool(1024)
+    push = scene.push_constants(W, H, spf, spf, spf, depth)
+    acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=depth)
+    acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
+    _check(compare.compare(acc_o, tr_o, acc_g, tr_g, spf))
+    assert ctx.last_iterations() > 10
+    ctx.close()
