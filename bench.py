@@ -50,6 +50,8 @@ def parse_args():
     ap.add_argument("--cpu-rows", type=int, default=32, help="rows in the CPU baseline sample")
     ap.add_argument("--engine", default="wavefront", choices=["wavefront", "megakernel"])
     ap.add_argument("--compare-engines", type=int, default=1, help="also time the other engine (1 step)")
+    ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0: library default)")
+    ap.add_argument("--budget", type=int, default=0, help="wavefront march steps per launch (0: default)")
     return ap.parse_args()
 
 
@@ -209,6 +211,10 @@ def main():
     ctx = Context(local)
     engine_id = native.PT_ENGINE_WAVEFRONT if args.engine == "wavefront" else native.PT_ENGINE_MEGAKERNEL
     ctx.set_engine(engine_id)
+    if args.pool:
+        ctx.set_wavefront_pool(args.pool)
+    if args.budget:
+        ctx.set_march_budget(args.budget)
     ctx.bind(scene, cie)
     ctx.resize_accum(W, H)
     stream = torch.cuda.ExternalStream(ctx.stream())
@@ -310,7 +316,8 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "resolution": [W, H], "spp": args.spp, "max_depth": args.depth,
                    "samples_per_dispatch": spf, "dispatches_per_step": ndisp,
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
+                   "wavefront_pool": args.pool or None, "march_budget": args.budget or None},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "engine": args.engine,
         "engines": {args.engine: {"value": value / world, "ms_per_step": ms_step}, **other},

@@ -21,6 +21,7 @@ class PtoTrace(ctypes.Structure):
         ("events", ctypes.c_void_p),
         ("nevents", ctypes.c_void_p),
         ("colors", ctypes.c_void_p),
+        ("counters", ctypes.c_void_p),
     ]
 
 
@@ -89,7 +90,7 @@ def dispatch(ubo: np.ndarray, push, plugins: list, accum: np.ndarray, rect=None,
         ev = np.zeros(npaths * trace_depth, np.uint32)
         nev = np.zeros(npaths, np.uint32)
         col = np.zeros(npaths * 3, np.float32)
-        tr = PtoTrace(trace_depth, ev.ctypes.data, nev.ctypes.data, col.ctypes.data)
+        tr = PtoTrace(trace_depth, ev.ctypes.data, nev.ctypes.data, col.ctypes.data, None)
         out = (ev.reshape(npaths, trace_depth), nev, col.reshape(npaths, 3))
     from pathtracer_gb300.native import PtSdfPlugin  # struct layout only
 
@@ -114,3 +115,25 @@ def mathf(fn: str, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
     if rc != 0:
         raise ValueError(fn)
     return out
+
+
+COUNTERS = ["samples", "path_rays", "shadow_rays", "sphere", "plane", "bounding_sphere", "box", "lens_slice",
+            "cyclide", "aabb", "march_steps", "sdf_blob", "sdf_mandelbulb", "mandelbulb_iters", "sdf_menger",
+            "sdf_terrain", "sdf_material", "emit", "brdf", "surface_hits"]
+
+
+def count_work(ubo: np.ndarray, push, plugins: list, rect=None, nthreads: int = 0) -> dict:
+    """Runs the shader over rect with the work counters on; returns them by name."""
+    W, H = push.resolution[0], push.resolution[1]
+    x0, y0, x1, y1 = rect if rect is not None else (0, 0, W, H)
+    cnt = np.zeros(len(COUNTERS), np.uint64)
+    tr = PtoTrace(0, None, None, None, cnt.ctypes.data)
+    from pathtracer_gb300.native import PtSdfPlugin  # struct layout only
+
+    arr = (PtSdfPlugin * max(1, len(plugins)))(*plugins)
+    accum = np.zeros((H, W, 4), np.float32)
+    rc = lib().pto_dispatch(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins),
+                            accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr), nthreads)
+    if rc != 0:
+        raise RuntimeError(f"pto_dispatch failed: {rc}")
+    return {k: int(v) for k, v in zip(COUNTERS, cnt)}

@@ -31,6 +31,7 @@
 #define PI_F 3.141592653589792623810034526344f /* SC:9 */
 #define ONEBYTHREE 0.3333333f                  /* SC:10 */
 #define MAXDIST 1e5f                           /* SC:8 */
+#define COUNT(c, k) do { if ((c)->cnt) (c)->cnt[k]++; } while (0)
 
 /* ------------------------------------------------------------------ */
 /* GLSL value types and built-ins                                      */
@@ -106,6 +107,7 @@ typedef struct {
     int last_hit;      /* object index of the last successful hit in Intersection */
     int light_pick;
     int shadow_state;
+    uint64_t* cnt;     /* work counters of this thread (PTO_C_*) or NULL */
 } ctx_t;
 
 static inline float OBJ(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_OBJECTS_SIZE) ? c->u->objects[i] : 0.0f; }
@@ -562,12 +564,15 @@ static float blob_material(vec3 p, const float* m) {
     return smin2(smin2(smin2(s1, s2), s3), s4).y;
 }
 
+static _Thread_local uint64_t* tl_cnt; /* work counters of the calling thread (for the plug-ins) */
+
 /* sdfs/mandelbulb.glsl:3-52 */
 static float mandelbulb_sdf(vec3 p) {
     vec3 z = p;
     float r = length3(z);
     float dr = 1.0f;
     for (int i = 0; i < 4; i++) {
+        if (tl_cnt) tl_cnt[PTO_C_MANDELBULB_ITERS]++;
         dr = 8.0f * ptm_powf(r, 7.0f) * dr + 1.0f;
         float invr = 1.0f / r;
         float invl = 1.0f / sqrtf(z.x * z.x + z.z * z.z);
@@ -653,6 +658,7 @@ static float SDF(const ctx_t* c, vec3 p, uint32_t set1) {
     for (int i = 0; i < n; i++) {
         uint32_t code = 1u << i;
         if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
+            if (c->cnt) c->cnt[PTO_C_SDF_BLOB + (c->plug[i].kind == PT_SDF_BLOB ? 0 : c->plug[i].kind == PT_SDF_MANDELBULB ? 1 : c->plug[i].kind == PT_SDF_MENGER ? 3 : 4)]++;
             sdf = fminf(sdf, plugin_sdf(&c->plug[i], sub3(p, sdf_pos(c, i))));
         }
     }
@@ -668,7 +674,9 @@ static float SDFMATERIAL(const ctx_t* c, vec3 p, uint32_t set1) {
         uint32_t code = 1u << i;
         if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
             vec3 q = sub3(p, sdf_pos(c, i));
+            if (c->cnt) c->cnt[PTO_C_SDF_BLOB + (c->plug[i].kind == PT_SDF_BLOB ? 0 : c->plug[i].kind == PT_SDF_MANDELBULB ? 1 : c->plug[i].kind == PT_SDF_MENGER ? 3 : 4)]++;
             float di = plugin_sdf(&c->plug[i], q);
+            if (!(sdf < di)) COUNT(c, PTO_C_SDF_MATERIAL);
             mat = (sdf < di) ? mat : plugin_material(&c->plug[i], q);
             sdf = fminf(sdf, di);
         }
@@ -692,6 +700,7 @@ static int SearchSDF(const ctx_t* c, vec3 p, vec3 invdir, vec2* tMinMax, uint32_
     for (int i = 0; (float)i < c->u->numObjects[5]; i++) {
         vec3 pos = sdf_pos(c, i);
         vec3 size = mk3(SDFS(c, 6 * i + 3), SDFS(c, 6 * i + 4), SDFS(c, 6 * i + 5));
+        COUNT(c, PTO_C_AABB);
         vec2 bm = RayIntersectAABB(p, invdir, pos, size);
         uint32_t bit = (i < 32) ? (1u << i) : 0u;
         if ((bm.x > bm.y) || (bm.y < 0.0f)) continue;
@@ -746,6 +755,7 @@ static int SphereTracing(const ctx_t* c, Ray ray, hit_t* h) {
     }
     float k = signf_glsl(SDF(c, ray.origin, set1));
     for (int i = 0; i < 512; i++) {
+        COUNT(c, PTO_C_MARCH_STEPS);
         float radius = SDF(c, p, set1);
         if (insT > (fabsf(previousRadius) + fabsf(radius))) {
             t -= insT;
@@ -813,19 +823,23 @@ static void IntersectAll(const ctx_t* c, Ray ray, hit_t* h, int* objectID) {
     int id = -1;
     for (int i = 0; (float)i < c->u->numObjects[0]; i++) {
         sphere_t o = UnpackSphere(c, i);
+        COUNT(c, PTO_C_SPHERE);
         if (SphereIntersection(ray, o, h)) id = i;
     }
     offset += 6 * NUM(c, 0);
     objectOffset += NUM(c, 0);
     for (int i = 0; (float)i < c->u->numObjects[1]; i++) {
         plane_t o = UnpackPlane(c, i, offset);
+        COUNT(c, PTO_C_PLANE);
         if (PlaneIntersection(ray, o, h)) id = i + objectOffset;
     }
     offset += 5 * NUM(c, 1);
     objectOffset += NUM(c, 1);
     for (int i = 0; (float)i < c->u->numObjects[2]; i++) {
         box_t o = UnpackBox(c, i, offset);
+        COUNT(c, PTO_C_BOUNDING_SPHERE);
         if (!BoundingSphere(ray, o.pos, 0.25f * dot3(o.size, o.size))) continue;
+        COUNT(c, PTO_C_BOX);
         if (BoxIntersection(ray, o, h)) id = i + objectOffset;
     }
     offset += 11 * NUM(c, 2);
@@ -833,14 +847,18 @@ static void IntersectAll(const ctx_t* c, Ray ray, hit_t* h, int* objectID) {
     for (int i = 0; (float)i < c->u->numObjects[3]; i++) {
         lens_t o = UnpackLens(c, i, offset);
         int isOutside = 1;
+        COUNT(c, PTO_C_BOUNDING_SPHERE);
         if (!BoundingSphere(ray, o.pos, lens_bounding_radius(o))) continue;
+        if (c->cnt) c->cnt[PTO_C_LENS_SLICE] += 2;
         if (LensIntersection(ray, o, h, &isOutside)) id = i + objectOffset;
     }
     offset += 12 * NUM(c, 3);
     objectOffset += NUM(c, 3);
     for (int i = 0; (float)i < c->u->numObjects[4]; i++) {
         cyclide_t o = UnpackCyclide(c, i, offset);
+        COUNT(c, PTO_C_BOUNDING_SPHERE);
         if (!BoundingSphere(ray, o.pos, o.brad)) continue;
+        COUNT(c, PTO_C_CYCLIDE);
         if (DupinCyclide(ray, o, h)) id = i + objectOffset;
     }
     if (SphereTracing(c, ray, h)) id = -2; /* SDF */
@@ -995,6 +1013,7 @@ static int SampleRandomLightSource(ctx_t* c, uint32_t* seed, float* boundingRadi
 
 /* SC:1121-1223 */
 static int LightSourceVisibilityCheck(const ctx_t* c, Ray ray, int lightObjectID) {
+    COUNT(c, PTO_C_SHADOW_RAYS);
     hit_t h;
     h.hitdist = MAXDIST;
     h.normal = mk3(0.0f, 0.0f, 0.0f);
@@ -1038,6 +1057,8 @@ static vec4 SampleLightSource(ctx_t* c, vec4 l, vec4 rayradiance, vec3 outOrigin
                 int vis = LightSourceVisibilityCheck(c, outRay, lightObjectID);
                 c->shadow_state = vis ? 3 : 2;
                 if (vis) {
+                    COUNT(c, PTO_C_EMIT);
+                    COUNT(c, PTO_C_BRDF);
                     light_t lt = GetLightMix(c, lightIDOut);
                     vec4 brdf = EvaluateBRDF(l, mat);
                     vec4 f = div4s(scl4(brdf, costheta), lightpdf);
@@ -1065,6 +1086,7 @@ static vec4 TraceRay(ctx_t* c, vec4 l, vec4* rayradiance, Ray* inRay, uint32_t* 
     h.materialID = 0.0f;
     h.lightID = -1.0f;
     int objectID = -1;
+    COUNT(c, PTO_C_PATH_RAYS);
     IntersectAll(c, *inRay, &h, &objectID);
     float hitdist = h.hitdist;
     material_t mat = GetMaterialMix(c, h.materialID);
@@ -1073,11 +1095,14 @@ static vec4 TraceRay(ctx_t* c, vec4 l, vec4* rayradiance, Ray* inRay, uint32_t* 
     if (hitdist < MAXDIST) {
         ev |= (objectID == -2) ? PT_EV_HIT_SDF : (uint32_t)(objectID & 0xFFF);
         if (lt.y > 0.0f) {
+            COUNT(c, PTO_C_EMIT);
             radiance = scl4(mul4(Emit(l, lt), *rayradiance), *MISBRDFWeight);
             *isTerminate = 1;
             *event = ev | PT_EV_EMITTER;
             return radiance;
         }
+        COUNT(c, PTO_C_SURFACE_HITS);
+        COUNT(c, PTO_C_BRDF);
         Ray outRay;
         outRay.origin = fma3(inRay->dir, mk3(hitdist, hitdist, hitdist), inRay->origin);
         outRay.dir = normalize3(add3(h.normal, SampleUniformUnitSphere(seed)));
@@ -1161,6 +1186,8 @@ static void TracePathLens(const ctx_t* c, float l, Ray* ray, vec3 forwardDir) {
 /* SC:1446-1490 */
 static vec3 Scene(ctx_t* c, uint32_t xx, uint32_t xy_y, vec2 uv, int k, uint32_t* events, int depth_cap, uint32_t* nev) {
     const pt_push* pc = c->pc;
+    COUNT(c, PTO_C_SAMPLES);
+    if (c->cnt) c->cnt[PTO_C_LENS_SLICE] += 4; /* the camera lens: 2 intersections x 2 slices */
     uint32_t seed = pto_generate_seed(xx, xy_y, pc->frame, pc->samplesPerFrame, k, pc->resolution[0]);
     float jx = 2.0f * RandomFloatPCG32(&seed) - 0.5f;
     float jy = 2.0f * RandomFloatPCG32(&seed) - 0.5f;
@@ -1235,12 +1262,16 @@ int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plug
 #pragma omp parallel for schedule(dynamic, 1)
     for (int y = y0; y < y1; y++) {
         ctx_t c;
+        uint64_t cnt[PTO_C_COUNT];
         memset(&c, 0, sizeof(c));
+        memset(cnt, 0, sizeof(cnt));
         c.u = ubo;
         c.pc = pc;
         c.plug = plugins;
         c.nplug = nplugins;
         c.cameraPos = mk3(pc->cameraPosX, pc->cameraPosY, pc->cameraPosZ);
+        c.cnt = (trace && trace->counters) ? cnt : NULL;
+        tl_cnt = c.cnt;
         for (int x = x0; x < x1; x++) {
             size_t coords = (size_t)x + (size_t)W * (size_t)y;
             float* px = accum + 4 * coords;
@@ -1286,6 +1317,13 @@ int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plug
             px[2] = outColor.z;
             px[3] = 1.0f;
         }
+        if (c.cnt) {
+            for (int k = 0; k < PTO_C_COUNT; k++) {
+#pragma omp atomic
+                trace->counters[k] += cnt[k];
+            }
+        }
+        tl_cnt = NULL;
     }
     return PT_OK;
 }

@@ -27,7 +27,35 @@ typedef struct pto_trace {
     uint32_t* events;   /* [npaths * depth_cap] */
     uint32_t* nevents;  /* [npaths] */
     float* colors;      /* [npaths * 3] */
+    uint64_t* counters; /* [PTO_C_COUNT] work counters, summed over the dispatch (or NULL) */
 } pto_trace;
+
+/* Work counters: how often each unit of the shader's work runs.  Multiplied
+ * by the floating-point operations each unit performs, they give the
+ * algorithmic FP32 work of a render (the roofline numerator). */
+enum {
+    PTO_C_SAMPLES = 0,       /* Scene() calls: camera paths */
+    PTO_C_PATH_RAYS,         /* TraceRay: Intersection of a path ray */
+    PTO_C_SHADOW_RAYS,       /* LightSourceVisibilityCheck */
+    PTO_C_SPHERE,            /* SphereIntersection */
+    PTO_C_PLANE,             /* PlaneIntersection */
+    PTO_C_BOUNDING_SPHERE,   /* BoundingSphere (boxes, lenses, cyclides) */
+    PTO_C_BOX,               /* BoxIntersection */
+    PTO_C_LENS_SLICE,        /* SphereSliceIntersection (scene lenses and the camera lens) */
+    PTO_C_CYCLIDE,           /* DupinCyclide */
+    PTO_C_AABB,              /* RayIntersectAABB (SearchSDF) */
+    PTO_C_MARCH_STEPS,       /* SphereTracing loop iterations */
+    PTO_C_SDF_BLOB,          /* plug-in evaluations by kind */
+    PTO_C_SDF_MANDELBULB,
+    PTO_C_MANDELBULB_ITERS,  /* iterations inside the mandelbulb loop */
+    PTO_C_SDF_MENGER,
+    PTO_C_SDF_TERRAIN,
+    PTO_C_SDF_MATERIAL,      /* sdfmaterial evaluations */
+    PTO_C_EMIT,              /* Emit (4 wavelengths) */
+    PTO_C_BRDF,              /* EvaluateBRDF (4 wavelengths) */
+    PTO_C_SURFACE_HITS,      /* non-emissive hits: BRDF sampling + light sampling */
+    PTO_C_COUNT
+};
 
 /*
  * Runs the shader's main() (src/shader.comp:1525-1533) for every invocation

@@ -181,8 +181,9 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
             }
             v.h0[slot] = make_float4(h.hitdist, h.materialID, h.lightID, __int_as_float(objectID));
             v.h1[slot] = make_float4(h.normal.x, h.normal.y, h.normal.z, 0.0f);
+            if (march) A.pool.m2[slot] = 0u;
         }
-        q_push(A.q_march, &C.n_march, slot, valid && march);
+        q_push(A.q_march[cur], &C.n_march[cur], slot, valid && march);
         q_push(A.q_shade, &C.n_shade, slot, valid && !march);
     }
 }
@@ -193,9 +194,14 @@ enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NOR
 __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant__ WfArgs A) {
     const KScene& S = *A.scene;
     WfCounters& C = *A.counters;
-    const uint32_t n = C.n_march;
+    const uint32_t cur = C.cur;
+    const uint32_t n = C.n_march[cur];
+    const uint32_t* __restrict__ qin = A.q_march[cur];
     const PoolView v = view(A);
+    const WfPool& M = A.pool;
     const int lane = threadIdx.x & 31;
+    const int budget = A.march_budget;
+    int steps = 0;
 
     uint32_t slot = 0;
     int phase = MP_EMPTY;
@@ -220,7 +226,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
             if (need) {
                 const uint32_t idx = b + (uint32_t)__popc(mneed & ((1u << lane) - 1u));
                 if (idx < n) {
-                    slot = A.q_march[idx];
+                    slot = qin[idx];
                     const float4 o = v.s0[slot];
                     const uint32_t flags = v.s8[slot].y;
                     const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
@@ -228,6 +234,23 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                     dir = f3(d.x, d.y, d.z);
                     hitdist = v.h0[slot].x;
                     invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+                    steps = 0;
+                    const uint32_t saved = M.m2[slot];
+                  if (saved & 0x80000000u) {
+                    // continue a march suspended by the previous launch
+                    const float4 a0 = M.m0[slot], a1 = M.m1[slot];
+                    t = a0.x;
+                    insT = a0.y;
+                    omega = a0.z;
+                    prevR = a0.w;
+                    tmm = make_float2(a1.x, a1.y);
+                    k = a1.z;
+                    set1 = __float_as_uint(a1.w);
+                    iter = (int)(saved & 1023u);
+                    points = (int)((saved >> 10) & 0xffffu);
+                    p = fma3s(dir, t, org);
+                    phase = MP_STEP;
+                  } else {
                     t = 1e-3f;
                     insT = 0.0f;
                     omega = omegaMax;
@@ -243,6 +266,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                     } else {
                         phase = MP_NO_BOX;  // (isect found a box with the same test) keep the analytic hit
                     }
+                  }
                 } else {
                     exhausted = true;
                 }
@@ -264,7 +288,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
         float val = 0.0f;
         if (evalLane) val = scene_sdf(S, q, set1);
 
-        bool finished = false, hit = false;
+        bool finished = false, hit = false, suspend = false;
         if (phase == MP_SIGN) {
             k = sign_glsl(val);
             phase = MP_STEP;
@@ -319,6 +343,12 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                 } else {
                     finished = true;
                 }
+            } else if (!finished && ++steps >= budget) {
+                // out of budget for this launch: save the state, continue next iteration
+                M.m0[slot] = make_float4(t, insT, omega, prevR);
+                M.m1[slot] = make_float4(tmm.x, tmm.y, k, __uint_as_float(set1));
+                M.m2[slot] = 0x80000000u | ((uint32_t)min(points, 0xffff) << 10) | (uint32_t)iter;
+                suspend = true;
             }
         } else if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
             const int j = phase - MP_NORMAL0;
@@ -346,7 +376,8 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
             v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
         }
         q_push(A.q_shade, &C.n_shade, slot, finished);
-        if (finished) phase = MP_EMPTY;
+        q_push(A.q_march[cur ^ 1u], &C.n_march[cur ^ 1u], slot, suspend);
+        if (finished || suspend) phase = MP_EMPTY;
     }
 }
 
@@ -413,8 +444,8 @@ __global__ void wf_book(WfCounters* __restrict__ Cp, uint32_t pool) {
     C.next_sample += n;
     C.n_free -= n;
     C.n_isect[C.cur] = 0;
+    C.n_march[C.cur] = 0;
     C.cur ^= 1u;
-    C.n_march = 0;
     C.march_cursor = 0;
     C.n_shade = 0;
     C.iterations += 1;
@@ -428,7 +459,7 @@ __global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_fr
         WfCounters& C = *Cp;
         C.n_isect[0] = C.n_isect[1] = 0;
         C.cur = 0;
-        C.n_march = C.march_cursor = C.n_shade = 0;
+        C.n_march[0] = C.n_march[1] = C.march_cursor = C.n_shade = 0;
         C.n_free = pool;
         C.next_sample = 0;
         C.total = total;

@@ -33,7 +33,8 @@ struct pt_ctx {
     int nplug = 0;
     KTrace trace{nullptr, nullptr, nullptr, 0};
     int engine = PT_ENGINE_WAVEFRONT;
-    uint32_t pool_cap = 1u << 21;  // wavefront path slots
+    uint32_t pool_cap = 1u << 23;  // wavefront path slots
+    int march_budget = 64;
     KScene* d_scene = nullptr;     // device copy for the wavefront kernels
     void* d_wf = nullptr;          // wavefront scratch (pool, queues, colours, counters)
     size_t wf_bytes = 0;
@@ -102,9 +103,13 @@ size_t wavefront_layout(char* base, uint32_t pool, uint32_t total, WfArgs* a) {
     P.s9 = carve<float4>(p, pool);
     P.h0 = carve<float4>(p, pool);
     P.h1 = carve<float4>(p, pool);
+    P.m0 = carve<float4>(p, pool);
+    P.m1 = carve<float4>(p, pool);
+    P.m2 = carve<uint32_t>(p, pool);
     a->q_isect[0] = carve<uint32_t>(p, pool);
     a->q_isect[1] = carve<uint32_t>(p, pool);
-    a->q_march = carve<uint32_t>(p, pool);
+    a->q_march[0] = carve<uint32_t>(p, pool);
+    a->q_march[1] = carve<uint32_t>(p, pool);
     a->q_shade = carve<uint32_t>(p, pool);
     a->q_free = carve<uint32_t>(p, pool);
     a->colors = carve<float4>(p, total);
@@ -315,6 +320,13 @@ int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots) {
 
 uint32_t pt_last_iterations(pt_ctx* ctx) { return ctx ? ctx->last_iterations : 0; }
 
+int pt_set_march_budget(pt_ctx* ctx, int steps) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (steps < 1 || steps > 512) return fail(ctx, PT_ERR_INVALID, "pt_set_march_budget: 1..512 steps");
+    ctx->march_budget = steps;
+    return PT_OK;
+}
+
 int pt_wait(pt_ctx* ctx, uint64_t timeout_ns) {
     if (!ctx) return PT_ERR_INVALID;
     PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
@@ -407,13 +419,17 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     a.trace = ctx->trace;
     a.pool_size = pool;
     a.total = total;
+    a.march_budget = ctx->march_budget;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
     int dev_sms = 0;
     PT_CUDA_TRY(ctx, cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
     const int grid = dev_sms * 4;  // 4 blocks of 256 threads per SM (64 registers)
     PT_CUDA_TRY(ctx, ptk_wavefront_launch_init(&a, ctx->stream));
     const int depth = push->pathLength;
-    const uint64_t max_iter = ((uint64_t)total / pool + 2) * (2ull * (uint64_t)depth + 3) + 16;
+    // Every iteration moves every live path by one ray; a ray's march spans at
+    // most ceil(512 / budget) + 1 iterations.
+    const uint64_t march_iters = 512ull / (uint64_t)ctx->march_budget + 2;
+    const uint64_t max_iter = ((uint64_t)total / pool + 2) * (2ull * (uint64_t)depth + 3) * march_iters + 16;
     uint64_t iter = 0;
     int chunk = 8;
     for (;;) {

@@ -148,6 +148,7 @@ CUDA_API = [
     ("pt_get_engine", _i, [_vp]),
     ("pt_set_wavefront_pool", _i, [_vp, ctypes.c_uint32]),
     ("pt_last_iterations", ctypes.c_uint32, [_vp]),
+    ("pt_set_march_budget", _i, [_vp, _i]),
 ]
 
 # Every symbol include/pt_host.h declares.

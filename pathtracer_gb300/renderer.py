@@ -190,6 +190,9 @@ class Context:
     def set_wavefront_pool(self, slots: int):
         self._check(self._lib.pt_set_wavefront_pool(self._h, slots))
 
+    def set_march_budget(self, steps: int):
+        self._check(self._lib.pt_set_march_budget(self._h, steps))
+
     def last_iterations(self) -> int:
         return self._lib.pt_last_iterations(self._h)
 

@@ -204,13 +204,15 @@ def test_wavefront_equals_megakernel_bitwise(rt, name, W, H, spf, depth):
 
 
 def test_wavefront_small_pool_recycles_slots(rt):
-    """A pool far smaller than the sample count: slots are freed and reused
-    many times; results stay identical to the oracle."""
+    """A pool far smaller than the sample count and a 3-step march budget:
+    slots are freed and reused many times and marches are suspended and
+    resumed across iterations; results stay identical to the oracle."""
     from oracle import compare
 
     W, H, spf, depth = 48, 40, 4, 6
     scene, ctx, ubo, plugins = _setup(rt, "feature_mix", W, H, 1)
     ctx.set_wavefront_pool(1024)
+    ctx.set_march_budget(3)  # most marches are suspended and resumed several times
     push = scene.push_constants(W, H, spf, spf, spf, depth)
     acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=depth)
     acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
