@@ -49,6 +49,7 @@ extern "C" {
 #define PT_ERR_NO_SCENE 5      /* dispatch before pt_upload_scene / pt_resize_accum */
 #define PT_ERR_OOM 6           /* device allocation failed */
 #define PT_ERR_KERNEL 7        /* a kernel reported an error through its status word */
+#define PT_ERR_TOO_LARGE 8     /* the request exceeds pt_dispatch_noalloc's fixed scratch */
 
 /* Byte-for-byte the reference's UniformBufferObject (src/pathtracer.cpp:187-195)
  * and the shader's `ubo` block (src/shader.comp:19-27): 4097 floats = 16388 B.
@@ -198,6 +199,32 @@ int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_
  * arrays (fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos), so tests can
  * compare its bits with the same function on the CPU.  Synchronous. */
 int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float* d_out, int n);
+
+/* ---- dispatch without allocating (not in the reference) -----------------
+ * No counterpart in the reference.  One wavefront dispatch (the engine
+ * PT_ENGINE_WAVEFRONT runs, bit-identical results) for callers that cannot
+ * allocate device memory while they render: a plug-in whose host application
+ * owns the GPU memory budget and forbids allocations after start-up, a
+ * real-time loop that cannot pay an allocator's latency or fragmentation,
+ * or code recorded into a stream capture, where cudaMalloc is not allowed.
+ * It allocates nothing: the caller passes the scene and push constants in
+ * host memory and the accumulator (W*H float4, read and written as by
+ * pt_dispatch) in its own device memory; all working memory of the call
+ * lives in one fixed array of PT_NOALLOC_SCRATCH_BYTES (32 MiB) in the
+ * library's device image, which every GPU that loads the library holds
+ * until the process exits.  Limits: W*H*samplesPerFrame <=
+ * PT_NOALLOC_MAX_SAMPLES per call (else PT_ERR_TOO_LARGE), and
+ * PT_NOALLOC_POOL_SLOTS path slots.  The first call on each device looks up
+ * the array's device address (make it before any stream capture).  All calls
+ * share the array, so calls that overlap on the GPU (on two streams at once)
+ * race; the counters are reset at the start of every call.  Runs on
+ * `stream` (NULL: the default stream) and returns when the dispatch is
+ * complete.  No per-path trace. */
+#define PT_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define PT_NOALLOC_MAX_SAMPLES (1u << 20)
+#define PT_NOALLOC_POOL_SLOTS (1u << 16)
+int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins, const pt_push* push,
+                        float* d_accum, void* stream);
 
 /* Event word layout, identical in the CPU restatement used by the tests. */
 #define PT_EV_HIT_MASK 0xFFFu     /* global object index; PT_EV_HIT_SDF, PT_EV_HIT_MISS */

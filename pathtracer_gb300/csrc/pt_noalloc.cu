@@ -1,0 +1,221 @@
+// pt_noalloc.cu — pt_dispatch_noalloc: one wavefront dispatch that allocates
+// nothing.
+//
+// Some callers cannot allocate device memory when they render: a plug-in
+// inside a host application that owns the GPU's memory budget and forbids
+// allocations after start-up, a real-time loop that cannot afford an
+// allocator's latency or fragmentation, or code recorded into a stream
+// capture where cudaMalloc is not allowed.  This entry point takes the scene
+// and push constants by host pointer and the accumulator as caller-owned
+// device memory, and keeps all of its own working memory — the device copy
+// of the scene, the CIE table, the path pool, the ray queues, the per-sample
+// colours and the counters — in one file-scope __device__ array of fixed size
+// (PT_NOALLOC_SCRATCH_BYTES, about 32.5 MB), which every GPU that loads the
+// library holds until the process exits.
+//
+// In host code the array's name is only a host-side stand-in, so the first
+// call on each device looks up its device address with cudaGetSymbolAddress
+// (with that device current) and caches it; make that first call before any
+// stream capture.  Every call shares the array and overwrites what it needs
+// (the counters are reset, the colours and path slots are rewritten), so
+// calls that overlap on the GPU — on two streams at once — race.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/pt_cuda.h"
+#include "kernel/pt_megakernel.h"
+#include "kernel/pt_wavefront.h"
+
+namespace {
+
+constexpr size_t r256(size_t x) { return (x + 255) / 256 * 256; }
+
+constexpr uint32_t kPool = PT_NOALLOC_POOL_SLOTS;
+constexpr uint32_t kMaxSamples = PT_NOALLOC_MAX_SAMPLES;
+constexpr size_t kSceneOff = 0;
+constexpr size_t kCieOff = kSceneOff + r256(sizeof(KScene));
+constexpr size_t kPoolOff = kCieOff + r256(sizeof(float) * PT_CIE_TABLE_SIZE);
+constexpr size_t kVec4Arrays = 14;  // s0..s9, h0, h1, m0, m1 (16 B per slot each)
+constexpr size_t kU32Arrays = 7;    // m2, two ISECT queues, two MARCH queues, SHADE, FREE
+constexpr size_t kColorsOff = kPoolOff + kVec4Arrays * r256((size_t)kPool * 16) + kU32Arrays * r256((size_t)kPool * 4);
+constexpr size_t kCountersOff = kColorsOff + r256((size_t)kMaxSamples * 16);
+constexpr size_t kScratchBytes = kCountersOff + r256(sizeof(WfCounters));
+static_assert(kScratchBytes <= PT_NOALLOC_SCRATCH_BYTES, "PT_NOALLOC_SCRATCH_BYTES is too small");
+
+}  // namespace
+
+// The fixed working memory of pt_dispatch_noalloc (see the file comment).
+static __device__ __align__(256) unsigned char pt_noalloc_scratch[PT_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+std::mutex g_mutex;
+void* g_scratch[64] = {};  // device address of pt_noalloc_scratch per device
+
+int scratch_address(int device, unsigned char** out) {
+    if (device < 0 || device >= 64) return PT_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_scratch[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, pt_noalloc_scratch);
+        if (e != cudaSuccess || !p) return PT_ERR_CUDA;
+        g_scratch[device] = p;
+    }
+    *out = static_cast<unsigned char*>(g_scratch[device]);
+    return PT_OK;
+}
+
+bool valid_count(float v, int max, int* out) {
+    if (!(v >= 0.0f) || v > (float)max || std::floor(v) != v) return false;
+    *out = (int)v;
+    return true;
+}
+
+// The launch-parameter image of the scene (as pt_upload_scene builds it),
+// without rotation matrices (a kernel writes those into the device copy).
+int build_scene(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplug, KScene* S) {
+    int n[7];
+    const int caps[7] = {PT_MAX_OBJECTS_SIZE / 6, PT_MAX_OBJECTS_SIZE / 5, PT_MAX_OBJECTS_SIZE / 11,
+                         PT_MAX_OBJECTS_SIZE / 12, PT_MAX_OBJECTS_SIZE / 16, PT_MAX_SDFS_SIZE / 6,
+                         PT_MAX_LIGHTIDS_SIZE};
+    for (int i = 0; i < 7; i++)
+        if (!valid_count(ubo->numObjects[i], caps[i], &n[i])) return PT_ERR_INVALID;
+    if (6 * n[0] + 5 * n[1] + 11 * n[2] + 12 * n[3] + 16 * n[4] > PT_MAX_OBJECTS_SIZE) return PT_ERR_INVALID;
+    if (n[5] > PT_MAX_LIVE_SDFS || nplug > PT_MAX_LIVE_SDFS) return PT_ERR_UNSUPPORTED;
+    for (int i = 0; i < nplug; i++)
+        if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_TERRAIN) return PT_ERR_INVALID;
+    std::memset(S, 0, sizeof(KScene));
+    std::memcpy(S->numObjects, ubo->numObjects, sizeof(S->numObjects));
+    std::memcpy(S->objects, ubo->objects, sizeof(S->objects));
+    std::memcpy(S->sdfs, ubo->sdfs, sizeof(S->sdfs));
+    std::memcpy(S->materials, ubo->materials, sizeof(S->materials));
+    std::memcpy(S->lights, ubo->lights, sizeof(S->lights));
+    std::memcpy(S->lightIDs, ubo->lightIDs, sizeof(S->lightIDs));
+    for (int i = 0; i < 7; i++) S->meta.n[i] = n[i];
+    S->meta.offset[0] = 0;
+    S->meta.offset[1] = 6 * n[0];
+    S->meta.offset[2] = S->meta.offset[1] + 5 * n[1];
+    S->meta.offset[3] = S->meta.offset[2] + 11 * n[2];
+    S->meta.offset[4] = S->meta.offset[3] + 12 * n[3];
+    S->meta.total_objects = n[0] + n[1] + n[2] + n[3] + n[4];
+    if (nplug > 0) std::memcpy(S->plug, plugins, sizeof(pt_sdf_plugin) * (size_t)nplug);
+    S->meta.nplug = nplug;
+    return PT_OK;
+}
+
+template <typename T>
+T* take(unsigned char*& p, size_t count) {
+    T* r = reinterpret_cast<T*>(p);
+    p += r256(count * sizeof(T));
+    return r;
+}
+
+#define PT_NA_TRY(call)                                 \
+    do {                                                \
+        if ((call) != cudaSuccess) return PT_ERR_CUDA; \
+    } while (0)
+
+}  // namespace
+
+extern "C" int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins,
+                                   const pt_push* push, float* d_accum, void* stream_ptr) {
+    if (!ubo || !push || !d_accum || nplugins < 0 || (nplugins > 0 && !plugins)) return PT_ERR_INVALID;
+    if (push->resolution[0] <= 0 || push->resolution[1] <= 0 || push->samplesPerFrame <= 0) return PT_ERR_INVALID;
+    const uint64_t total64 = (uint64_t)push->resolution[0] * (uint64_t)push->resolution[1] *
+                             (uint64_t)push->samplesPerFrame;
+    if (total64 > kMaxSamples) return PT_ERR_TOO_LARGE;
+    const uint32_t total = (uint32_t)total64;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+
+    // The scene image is built on the stack (about 19 KB): no heap use.
+    KParams host_params;
+    KScene& S = host_params.s;
+    const int rc = build_scene(ubo, plugins, nplugins, &S);
+    if (rc != PT_OK) return rc;
+
+    int device = 0;
+    PT_NA_TRY(cudaGetDevice(&device));
+    unsigned char* base = nullptr;
+    const int rs = scratch_address(device, &base);
+    if (rs != PT_OK) return rs;
+    KScene* d_scene = reinterpret_cast<KScene*>(base + kSceneOff);
+    float* d_cie = reinterpret_cast<float*>(base + kCieOff);
+
+    PT_NA_TRY(cudaMemcpyAsync(d_scene, &S, sizeof(KScene), cudaMemcpyHostToDevice, stream));
+    PT_NA_TRY(cudaMemcpyAsync(d_cie, ubo->CIEXYZ1931, sizeof(float) * PT_CIE_TABLE_SIZE, cudaMemcpyHostToDevice,
+                              stream));
+    if (S.meta.total_objects > 0) PT_NA_TRY(ptk_rotation_setup(&S, &d_scene->rot[0][0], stream));
+
+    if (push->pathLength <= 0) {
+        // No bounce is traced: the megakernel needs no scratch beyond the CIE table.
+        host_params.pc = *push;
+        host_params.accum = reinterpret_cast<float4*>(d_accum);
+        host_params.cie = d_cie;
+        host_params.trace = KTrace{nullptr, nullptr, nullptr, 0};
+        PT_NA_TRY(ptk_launch_megakernel(&host_params, false, stream));
+        PT_NA_TRY(cudaStreamSynchronize(stream));
+        return PT_OK;
+    }
+
+    WfArgs a;
+    std::memset(&a, 0, sizeof a);
+    unsigned char* p = base + kPoolOff;
+    WfPool& P = a.pool;
+    P.s0 = take<float4>(p, kPool);
+    P.s1 = take<float4>(p, kPool);
+    P.s2 = take<float4>(p, kPool);
+    P.s3 = take<float4>(p, kPool);
+    P.s4 = take<float4>(p, kPool);
+    P.s5 = take<float4>(p, kPool);
+    P.s6 = take<float4>(p, kPool);
+    P.s7 = take<float4>(p, kPool);
+    P.s8 = take<uint4>(p, kPool);
+    P.s9 = take<float4>(p, kPool);
+    P.h0 = take<float4>(p, kPool);
+    P.h1 = take<float4>(p, kPool);
+    P.m0 = take<float4>(p, kPool);
+    P.m1 = take<float4>(p, kPool);
+    P.m2 = take<uint32_t>(p, kPool);
+    a.q_isect[0] = take<uint32_t>(p, kPool);
+    a.q_isect[1] = take<uint32_t>(p, kPool);
+    a.q_march[0] = take<uint32_t>(p, kPool);
+    a.q_march[1] = take<uint32_t>(p, kPool);
+    a.q_shade = take<uint32_t>(p, kPool);
+    a.q_free = take<uint32_t>(p, kPool);
+    a.colors = reinterpret_cast<float4*>(base + kColorsOff);
+    a.counters = reinterpret_cast<WfCounters*>(base + kCountersOff);
+    a.scene = d_scene;
+    a.pc = *push;
+    a.accum = reinterpret_cast<float4*>(d_accum);
+    a.cie = d_cie;
+    a.trace = KTrace{nullptr, nullptr, nullptr, 0};
+    a.pool_size = total < kPool ? (total < 1024u ? 1024u : total) : kPool;
+    a.total = total;
+    a.march_budget = 64;
+
+    int sms = 0;
+    PT_NA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const int grid = sms * 4;
+    PT_NA_TRY(ptk_wavefront_launch_init(&a, stream));  // resets the counters left by the previous call
+    const uint64_t march_iters = 512ull / 64ull + 2;
+    const uint64_t max_iter =
+        ((uint64_t)total / a.pool_size + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
+    uint64_t iter = 0;
+    int chunk = 8;
+    WfCounters hc;
+    for (;;) {
+        for (int c = 0; c < chunk; c++) PT_NA_TRY(ptk_wavefront_launch_iteration(&a, false, grid, stream));
+        iter += (uint64_t)chunk;
+        PT_NA_TRY(cudaMemcpyAsync(&hc, a.counters, sizeof hc, cudaMemcpyDeviceToHost, stream));
+        PT_NA_TRY(cudaStreamSynchronize(stream));
+        if (hc.done) break;
+        if (iter > max_iter) return PT_ERR_KERNEL;
+        if (chunk < 64) chunk *= 2;
+    }
+    PT_NA_TRY(ptk_wavefront_launch_resolve(&a, stream));
+    PT_NA_TRY(cudaStreamSynchronize(stream));
+    return PT_OK;
+}

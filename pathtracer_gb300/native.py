@@ -22,6 +22,8 @@ PT_ERR_UNSUPPORTED = 4
 PT_ERR_NO_SCENE = 5
 PT_ERR_OOM = 6
 PT_ERR_KERNEL = 7
+PT_ERR_TOO_LARGE = 8
+PT_NOALLOC_MAX_SAMPLES = 1 << 20
 
 PT_ENGINE_MEGAKERNEL = 0
 PT_ENGINE_WAVEFRONT = 1
@@ -149,6 +151,7 @@ CUDA_API = [
     ("pt_set_wavefront_pool", _i, [_vp, ctypes.c_uint32]),
     ("pt_last_iterations", ctypes.c_uint32, [_vp]),
     ("pt_set_march_budget", _i, [_vp, _i]),
+    ("pt_dispatch_noalloc", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(PtPush), _vp, _vp]),
 ]
 
 # Every symbol include/pt_host.h declares.
