@@ -158,7 +158,7 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push);
 #define PT_ENGINE_WAVEFRONT 1
 int pt_set_engine(pt_ctx* ctx, int engine);
 int pt_get_engine(pt_ctx* ctx);
-/* Path slots of the wavefront pool (default 2^23; 252 B each, plus 16 B per
+/* Path slots of the wavefront pool (default 2^21; 252 B each, plus 16 B per
  * sample of the dispatch for the sample colours). */
 int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots);
 /* Sphere-tracing iterations a ray may take per march launch before it is

@@ -27,6 +27,7 @@ CUDA_SOURCES = [
     "kernel/pt_megakernel.cu",
     "kernel/pt_wavefront.cu",
     "pt_api.cu",
+    "pt_engine.cu",
     "pt_noalloc.cu",
     "pt_sdf_source.cpp",
 ]

@@ -156,13 +156,6 @@ PT_DI int sample_random_light(const KScene& S, uint32_t& seed, float& boundingRa
     return 0;
 }
 
-// Camera quantities that depend only on the push constants (SC:1456,
-// SC:1409-1418): derived once per block (megakernel) or per launch.
-struct CamInfo {
-    m3 cam;
-    m3 lensRot;
-    float3 lensPos;
-};
 
 PT_DI CamInfo make_camera(const pt_push& pc) {
     CamInfo c;

@@ -38,6 +38,14 @@ struct KScene {
     float rot[PT_MAX_SCENE_OBJECTS][9];
 };
 
+// Camera quantities that depend only on the push constants (SC:1456,
+// SC:1409-1418): derived once per block (megakernel) or per job (wavefront).
+struct CamInfo {
+    m3 cam;
+    m3 lensRot;
+    float3 lensPos;
+};
+
 struct KTrace {
     uint32_t* events;
     uint32_t* nevents;

@@ -57,7 +57,8 @@ PT_DI PoolView view(const WfArgs& A) {
     return PoolView{p.s0, p.s1, p.s2, p.s3, p.s4, p.s5, p.s6, p.s7, p.s8, p.s9, p.h0, p.h1};
 }
 
-PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t& flags, uint32_t& sample) {
+PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t& flags, uint32_t& sample,
+                      uint32_t& job) {
     const float4 a = v.s0[slot], b = v.s1[slot], c = v.s2[slot], d = v.s3[slot];
     ps.org = f3(a.x, a.y, a.z);
     ps.mis = a.w;
@@ -80,9 +81,11 @@ PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t&
     const float4 e = v.s9[slot];
     ps.shLightID = e.x;
     ps.ev = __float_as_uint(e.y);
+    job = __float_as_uint(e.z);
 }
 
-PT_DI void store_state(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t flags, uint32_t sample) {
+PT_DI void store_state(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t flags, uint32_t sample,
+                       uint32_t job) {
     v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
     v.s1[slot] = make_float4(ps.dir.x, ps.dir.y, ps.dir.z, ps.brdfPdf);
     v.s2[slot] = make_float4(ps.shDir.x, ps.shDir.y, ps.shDir.z, ps.cosL);
@@ -92,7 +95,24 @@ PT_DI void store_state(const PoolView& v, uint32_t slot, const PathState& ps, ui
     v.s6[slot] = ps.radiance;
     v.s7[slot] = ps.l;
     v.s8[slot] = make_uint4(ps.seed, flags | ((uint32_t)ps.bounce & 0x3fffffffu), sample, (uint32_t)ps.shObj);
-    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
+    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
+}
+
+PT_DI uint32_t slot_job(const PoolView& v, uint32_t slot) { return __float_as_uint(v.s9[slot].z); }
+
+// The job whose pass holds global sample s: the last job with first <= s
+// (passes are appended in increasing order of first).
+PT_DI uint32_t find_job(const WfJob* __restrict__ jobs, uint32_t njobs, uint64_t s) {
+    uint32_t lo = 0, hi = njobs;  // invariant: jobs[lo].first <= s < jobs[hi].first
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].first <= s) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    return lo;
 }
 
 // Sample id s of a dispatch: k = s / (W*H), pixel = s % (W*H).  The colour
@@ -103,21 +123,21 @@ PT_DI size_t trace_index(const pt_push& pc, uint32_t s) {
     return (size_t)(s % npix) * (size_t)pc.samplesPerFrame + (size_t)(s / npix);
 }
 
-template <bool TRACE>
+// Samples of every pass in the table (passes are appended in order of first).
+PT_DI uint64_t jobs_total(const WfArgs& A) {
+    if (A.njobs == 0) return 0;
+    const WfJob& L = A.jobs[A.njobs - 1];
+    return L.first + (uint64_t)L.count;
+}
+
 __global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ WfArgs A) {
-    __shared__ CamInfo camS;
-    if (threadIdx.x == 0) camS = make_camera(A.pc);
-    __syncthreads();
     WfCounters& C = *A.counters;
-    const uint32_t remaining = C.total - C.next_sample;
-    const uint32_t n = min(C.n_free, remaining);
+    const uint64_t remaining = jobs_total(A) - C.next_sample;
+    const uint32_t n = (uint32_t)min((uint64_t)C.n_free, remaining);
     const uint32_t nfree = C.n_free;
-    const uint32_t first = C.next_sample;
+    const uint64_t first = C.next_sample;
     const uint32_t nxt = C.cur ^ 1u;
     const PoolView v = view(A);
-    const pt_push& pc = A.pc;
-    const int W = pc.resolution[0], H = pc.resolution[1];
-    const uint32_t npix = (uint32_t)W * (uint32_t)H;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -125,14 +145,21 @@ __global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ 
         uint32_t slot = 0;
         if (valid) {
             slot = A.q_free[nfree - n + i];
-            const uint32_t s = first + i;
-            const uint32_t k = s / npix, pix = s % npix;
+            const uint64_t s = first + i;
+            const uint32_t job = find_job(A.jobs, A.njobs, s);
+            const WfJob& J = A.jobs[job];
+            const uint32_t local = (uint32_t)(s - J.first);
+            const pt_push& pc = J.pc;
+            const int W = pc.resolution[0], H = pc.resolution[1];
+            const uint32_t npix = (uint32_t)W * (uint32_t)H;
+            const uint32_t k = local / npix, pix = local % npix;
             const int x = (int)(pix % (uint32_t)W), y = (int)(pix / (uint32_t)W);
             const uint32_t xx = (uint32_t)x, yy = (uint32_t)H - (uint32_t)y;
             const float uvx = (2.0f * (float)xx - (float)W) / (float)H;
             const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
+            const CamInfo cam = J.cam;
             PathState ps;
-            start_sample(ps, pc, camS, xx, yy, uvx, uvy, (int)k);
+            start_sample(ps, pc, cam, xx, yy, uvx, uvy, (int)k);
             ps.nrm = f3(0.0f, 0.0f, 0.0f);
             ps.shDir = f3(0.0f, 0.0f, 1.0f);
             ps.brdf = f4s(0.0f);
@@ -140,20 +167,24 @@ __global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ 
             ps.shLightID = -1.0f;
             ps.shObj = 0;
             ps.ev = 0;
-            store_state(v, slot, ps, 0u, s);
+            store_state(v, slot, ps, 0u, local, job);
         }
         q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, valid);
     }
 }
 
+__global__ void wf_job_setup(const __grid_constant__ WfArgs A, uint32_t j0, uint32_t j1) {
+    const uint32_t j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= j1) return;
+    A.jobs[j].cam = make_camera(A.jobs[j].pc);
+}
+
 __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant__ WfArgs A) {
-    const KScene& S = *A.scene;
     WfCounters& C = *A.counters;
     const uint32_t cur = C.cur;
     const uint32_t n = C.n_isect[cur];
     const uint32_t* __restrict__ q = A.q_isect[cur];
     const PoolView v = view(A);
-    const bool has_sdf = S.meta.n[5] > 0;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -162,6 +193,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
         uint32_t slot = 0;
         if (valid) {
             slot = q[i];
+            const KScene& S = *A.jobs[slot_job(v, slot)].scene;
             const float4 o = v.s0[slot];
             const uint32_t flags = v.s8[slot].y;
             const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
@@ -173,7 +205,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
             h.lightID = -1.0f;
             int objectID = -1;
             intersect_analytic(S, org, dir, h, objectID);
-            if (has_sdf) {
+            if (S.meta.n[5] > 0) {
                 const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
                 float2 tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
                 uint32_t set1 = 0;
@@ -192,7 +224,6 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
 enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NORMAL5 = 8, MP_NO_BOX = 9 };
 
 __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant__ WfArgs A) {
-    const KScene& S = *A.scene;
     WfCounters& C = *A.counters;
     const uint32_t cur = C.cur;
     const uint32_t n = C.n_march[cur];
@@ -204,6 +235,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     int steps = 0;
 
     uint32_t slot = 0;
+    const KScene* Sp = nullptr;
     int phase = MP_EMPTY;
     bool exhausted = false;
     float3 org = f3(0.0f, 0.0f, 0.0f), dir = f3(0.0f, 0.0f, 1.0f), invdir = f3(0.0f, 0.0f, 0.0f), p = org;
@@ -227,6 +259,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                 const uint32_t idx = b + (uint32_t)__popc(mneed & ((1u << lane) - 1u));
                 if (idx < n) {
                     slot = qin[idx];
+                    Sp = A.jobs[slot_job(v, slot)].scene;
                     const float4 o = v.s0[slot];
                     const uint32_t flags = v.s8[slot].y;
                     const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
@@ -259,7 +292,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                     iter = 0;
                     tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
                     set1 = 0;
-                    if (search_sdf(S, org, invdir, tmm, set1)) {
+                    if (search_sdf(*Sp, org, invdir, tmm, set1)) {
                         t = fmaxf(tmm.x, t);
                         p = fma3s(dir, t, org);
                         phase = MP_SIGN;
@@ -286,7 +319,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
             q = (j & 1) ? f3(p.x - mx, p.y - my, p.z - mz) : f3(p.x + ex, p.y + ey, p.z + ez);
         }
         float val = 0.0f;
-        if (evalLane) val = scene_sdf(S, q, set1);
+        if (evalLane) val = scene_sdf(*Sp, q, set1);
 
         bool finished = false, hit = false, suspend = false;
         if (phase == MP_SIGN) {
@@ -313,7 +346,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                 if (points >= 2) {
                     t = tmm.y + 1e-3f;
                     tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
-                    if (search_sdf(S, fma3s(dir, t, org), invdir, tmm, set1)) {
+                    if (search_sdf(*Sp, fma3s(dir, t, org), invdir, tmm, set1)) {
                         tmm.x += t;
                         tmm.y += t;
                         t = fmaxf(tmm.x, t);
@@ -371,7 +404,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
 
         if (finished && hit) {
             const float3 nrm = normalize3(nv);
-            const float mat = scene_sdf_material(S, p, set1);
+            const float mat = scene_sdf_material(*Sp, p, set1);
             v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
             v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
         }
@@ -381,26 +414,37 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     }
 }
 
+// Adds 1 to jobs[job].finished for every lane with pred, one atomic per
+// distinct job in the warp.  Called by all 32 lanes.
+PT_DI void count_finished(WfJob* __restrict__ jobs, uint32_t job, bool pred) {
+    const unsigned active = __ballot_sync(0xffffffffu, pred);
+    if (!active) return;
+    const unsigned same = __match_any_sync(0xffffffffu, pred ? job : 0xffffffffu);
+    if (pred && (__ffs(same & active) - 1) == (int)(threadIdx.x & 31))
+        atomicAdd(&jobs[job].finished, (uint32_t)__popc(same & active));
+}
+
 template <bool TRACE>
 __global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant__ WfArgs A) {
-    const KScene& S = *A.scene;
     WfCounters& C = *A.counters;
     const uint32_t n = C.n_shade;
     const uint32_t nxt = C.cur ^ 1u;
     const PoolView v = view(A);
-    const pt_push& pc = A.pc;
-    const int depth = pc.pathLength;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool valid = i < n;
-        uint32_t slot = 0;
+        uint32_t slot = 0, job = 0;
         bool again = false, freed = false;
         if (valid) {
             slot = A.q_shade[i];
             PathState ps;
             uint32_t flags, sample;
-            load_state(v, slot, ps, flags, sample);
+            load_state(v, slot, ps, flags, sample, job);
+            const WfJob& J = A.jobs[job];
+            const KScene& S = *J.scene;
+            const pt_push& pc = J.pc;
+            const int depth = pc.pathLength;
             const float4 h0 = v.h0[slot], h1 = v.h1[slot];
             Hit h;
             h.hitdist = h0.x;
@@ -416,8 +460,8 @@ __global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant_
                 if (b < A.trace.cap) A.trace.events[p * (size_t)A.trace.cap + b] = ps.ev;
             }
             if (r == STEP_TERMINATED) {
-                const float3 col = sample_color(ps, A.cie);
-                A.colors[sample] = make_float4(col.x, col.y, col.z, 0.0f);
+                const float3 col = sample_color(ps, J.cie);
+                J.colors[sample] = make_float4(col.x, col.y, col.z, 0.0f);
                 if (TRACE) {
                     const size_t p = trace_index(pc, sample);
                     if (A.trace.nevents) A.trace.nevents[p] = (uint32_t)ps.bounce;
@@ -429,18 +473,22 @@ __global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant_
                 }
                 freed = true;
             } else {
-                store_state(v, slot, ps, (r == STEP_SHADOW) ? kShadowFlag : 0u, sample);
+                store_state(v, slot, ps, (r == STEP_SHADOW) ? kShadowFlag : 0u, sample, job);
                 again = true;
             }
         }
         q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, again);
         q_push(A.q_free, &C.n_free, slot, freed);
+        count_finished(A.jobs, job, freed);
     }
 }
 
-__global__ void wf_book(WfCounters* __restrict__ Cp, uint32_t pool) {
-    WfCounters& C = *Cp;
-    const uint32_t n = min(C.n_free, C.total - C.next_sample);
+__global__ void wf_book(const __grid_constant__ WfArgs A) {
+    WfCounters& C = *A.counters;
+    const uint32_t pool = A.pool_size;
+    const uint64_t total = jobs_total(A);
+    const uint32_t n = (uint32_t)min((uint64_t)C.n_free, total - C.next_sample);
+    C.total = total;
     C.next_sample += n;
     C.n_free -= n;
     C.n_isect[C.cur] = 0;
@@ -449,43 +497,50 @@ __global__ void wf_book(WfCounters* __restrict__ Cp, uint32_t pool) {
     C.march_cursor = 0;
     C.n_shade = 0;
     C.iterations += 1;
-    C.done = (C.next_sample == C.total && C.n_free == pool) ? 1u : 0u;
+    C.live = pool - C.n_free;
 }
 
-__global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_free, uint32_t pool, uint32_t total) {
+__global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_free, uint32_t pool) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < pool) q_free[i] = i;
     if (i == 0) {
         WfCounters& C = *Cp;
         C.n_isect[0] = C.n_isect[1] = 0;
+        C.n_march[0] = C.n_march[1] = 0;
         C.cur = 0;
-        C.n_march[0] = C.n_march[1] = C.march_cursor = C.n_shade = 0;
+        C.march_cursor = C.n_shade = 0;
         C.n_free = pool;
         C.next_sample = 0;
-        C.total = total;
+        C.total = 0;
         C.iterations = 0;
-        C.done = (total == 0) ? 1u : 0u;
+        C.live = 0;
     }
 }
 
-// Rendering + Accumulate over the ordered sample colours, one thread per pixel.
-__global__ void __launch_bounds__(kStageThreads) wf_resolve(const __grid_constant__ WfArgs A) {
-    const pt_push& pc = A.pc;
+// Rendering + Accumulate over one pass's ordered sample colours, one thread per pixel.
+__global__ void __launch_bounds__(kStageThreads) wf_resolve(const pt_push pc, float4* __restrict__ accum,
+                                                           const float4* __restrict__ colors) {
     const uint32_t npix = (uint32_t)pc.resolution[0] * (uint32_t)pc.resolution[1];
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= npix) return;
     float3 sum = f3(0.0f, 0.0f, 0.0f);
     for (int k = 0; k < pc.samplesPerFrame; k++) {
-        const float4 c = A.colors[(size_t)k * npix + pix];
+        const float4 c = colors[(size_t)k * npix + pix];
         sum = sum + f3(c.x, c.y, c.z);
     }
-    A.accum[pix] = accumulate(pc, sum, A.accum[pix]);
+    accum[pix] = accumulate(pc, sum, accum[pix]);
 }
 
 }  // namespace
 
 cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream) {
-    wf_init<<<(a->pool_size + 255) / 256, 256, 0, stream>>>(a->counters, a->q_free, a->pool_size, a->total);
+    wf_init<<<(a->pool_size + 255) / 256, 256, 0, stream>>>(a->counters, a->q_free, a->pool_size);
+    return cudaGetLastError();
+}
+
+cudaError_t ptk_wavefront_launch_job_setup(const WfArgs* a, uint32_t j0, uint32_t j1, cudaStream_t stream) {
+    if (j1 <= j0) return cudaSuccess;
+    wf_job_setup<<<(j1 - j0 + 63) / 64, 64, 0, stream>>>(*a, j0, j1);
     return cudaGetLastError();
 }
 
@@ -494,17 +549,19 @@ cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid
     wf_march<<<grid, kStageThreads, 0, stream>>>(*a);
     if (trace) {
         wf_shade<true><<<grid, kStageThreads, 0, stream>>>(*a);
-        wf_gen<true><<<grid, kStageThreads, 0, stream>>>(*a);
     } else {
         wf_shade<false><<<grid, kStageThreads, 0, stream>>>(*a);
-        wf_gen<false><<<grid, kStageThreads, 0, stream>>>(*a);
     }
-    wf_book<<<1, 1, 0, stream>>>(a->counters, a->pool_size);
+    wf_gen<<<grid, kStageThreads, 0, stream>>>(*a);
+    wf_book<<<1, 1, 0, stream>>>(*a);
     return cudaGetLastError();
 }
 
-cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, cudaStream_t stream) {
-    const uint32_t npix = (uint32_t)a->pc.resolution[0] * (uint32_t)a->pc.resolution[1];
-    wf_resolve<<<(npix + kStageThreads - 1) / kStageThreads, kStageThreads, 0, stream>>>(*a);
+cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,
+                                         const float4* colors, cudaStream_t stream) {
+    (void)a;
+    (void)job;
+    const uint32_t npix = (uint32_t)pc->resolution[0] * (uint32_t)pc->resolution[1];
+    wf_resolve<<<(npix + kStageThreads - 1) / kStageThreads, kStageThreads, 0, stream>>>(*pc, accum, colors);
     return cudaGetLastError();
 }

@@ -1,4 +1,5 @@
-// pt_wavefront.h — data of the wavefront renderer (pt_wavefront.cu).
+// pt_wavefront.h — data of the wavefront renderer (pt_wavefront.cu) and the
+// host-side engine that drives it (pt_engine.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -6,11 +7,11 @@
 
 #include "pt_scene.cuh"
 
-// Path state, structure of arrays, one entry per pool slot (192 B per slot):
+// Path state, structure of arrays, one entry per pool slot:
 //   s0 org.xyz, mis       s1 dir.xyz, brdfPdf    s2 shDir.xyz, cosL
 //   s3 nrm.xyz, lightPdf  s4 brdf                s5 throughput
-//   s6 radiance           s7 wavelengths         s8 seed, flags|bounce, sample id, shObj
-//   s9 shLightID, trace event word               h0 hitdist, materialID, lightID, objectID
+//   s6 radiance           s7 wavelengths         s8 seed, flags|bounce, sample (in its pass), shObj
+//   s9 shLightID, trace event word, job          h0 hitdist, materialID, lightID, objectID
 //   h1 hit normal
 // and the sphere-tracing state of a ray whose march continues in the next
 // iteration: m0 t, insT, omega, prevRadius; m1 tMinMax.xy, k, set1 bits;
@@ -23,44 +24,55 @@ struct WfPool {
     uint32_t* m2;
 };
 
+// One render pass of one job: samplesPerFrame samples of every pixel.
+struct WfJob {
+    const KScene* scene;  // device copy of the job's scene
+    const float* cie;     // device CIE table
+    float4* accum;        // W*H float4 accumulator (read and written by resolve)
+    float4* colors;       // W*H*spf sample XYZ, [k][pixel]
+    uint64_t first;       // global index of the pass's first sample
+    uint32_t count;       // W*H*spf
+    uint32_t finished;    // samples finished (atomic)
+    CamInfo cam;          // camera derived on the device (wf_job_setup)
+    pt_push pc;
+};
+
 struct WfCounters {
     uint32_t n_isect[2];  // the two ISECT queues (current, next)
-    uint32_t cur;
     uint32_t n_march[2];  // the two MARCH queues (current, next)
+    uint32_t cur;
     uint32_t march_cursor;
     uint32_t n_shade;
     uint32_t n_free;
-    uint32_t next_sample;  // samples started so far
-    uint32_t total;        // samples in the dispatch
+    uint64_t next_sample;  // global samples started so far
+    uint64_t total;        // global samples of every pass in the table (written by the bookkeeping kernel)
     uint32_t iterations;
-    uint32_t done;         // all samples started and finished
+    uint32_t live;         // slots holding a path (pool - n_free)
     uint32_t pad[4];
 };
 
 struct WfArgs {
-    const KScene* scene;  // device copy of the scene
-    pt_push pc;
+    WfJob* jobs;   // device job table
+    uint32_t njobs;
     WfPool pool;
     uint32_t* q_isect[2];
     uint32_t* q_march[2];
     uint32_t* q_shade;
     uint32_t* q_free;
     WfCounters* counters;
-    float4* colors;  // [k][pixel] sample XYZ
-    float4* accum;
-    const float* cie;
-    KTrace trace;
+    KTrace trace;  // single-job dispatches only
     uint32_t pool_size;
-    uint32_t total;
     int march_budget;  // sphere-tracing iterations per ray per march launch
 };
 
-// Bytes of device scratch for a pool of `pool` slots and `total` samples.
-inline size_t ptk_wavefront_scratch_bytes(uint32_t pool, uint32_t total) {
-    return (size_t)pool * (14 * 16 + 7 * 4) + (size_t)total * 16 + 256;
-}
+// Bytes of the engine's device buffers for a pool of `pool` slots.
+inline size_t ptk_wavefront_pool_bytes(uint32_t pool) { return (size_t)pool * (14 * 16 + 7 * 4) + 32 * 256; }
 
 cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream);
+// Derives the camera of jobs [j0, j1) on the device.
+cudaError_t ptk_wavefront_launch_job_setup(const WfArgs* a, uint32_t j0, uint32_t j1, cudaStream_t stream);
 // One iteration: isect, march, shade, gen, bookkeeping (grid = blocks per stage kernel).
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream);
-cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, cudaStream_t stream);
+// Rendering/Accumulate of one job pass from its ordered sample colours.
+cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,
+                                         const float4* colors, cudaStream_t stream);

@@ -17,6 +17,7 @@
 #include "../../include/pt_cuda.h"
 #include "kernel/pt_megakernel.h"
 #include "kernel/pt_wavefront.h"
+#include "pt_engine.h"
 
 struct pt_ctx {
     int device = 0;
@@ -33,12 +34,12 @@ struct pt_ctx {
     int nplug = 0;
     KTrace trace{nullptr, nullptr, nullptr, 0};
     int engine = PT_ENGINE_WAVEFRONT;
-    uint32_t pool_cap = 1u << 23;  // wavefront path slots
+    uint32_t pool_cap = 1u << 21;  // wavefront path slots
     int march_budget = 64;
     KScene* d_scene = nullptr;     // device copy for the wavefront kernels
-    void* d_wf = nullptr;          // wavefront scratch (pool, queues, colours, counters)
-    size_t wf_bytes = 0;
-    WfCounters* h_counters = nullptr;  // pinned
+    WfEngine* wf = nullptr;        // wavefront driver (created on first use, grows with the dispatch)
+    float4* d_colors = nullptr;    // per-sample colours of the current dispatch
+    size_t colors_bytes = 0;
     uint32_t last_iterations = 0;
     std::string err;
 };
@@ -80,44 +81,6 @@ cudaError_t sync_device_scene(pt_ctx* ctx) {
     return cudaMemcpyAsync(ctx->d_scene, &ctx->params->s, sizeof(KScene), cudaMemcpyHostToDevice, ctx->stream);
 }
 
-template <typename T>
-T* carve(char*& p, size_t count) {
-    T* r = reinterpret_cast<T*>(p);
-    p += ((count * sizeof(T) + 255) / 256) * 256;
-    return r;
-}
-
-// Lays the wavefront's buffers out in one scratch allocation.
-size_t wavefront_layout(char* base, uint32_t pool, uint32_t total, WfArgs* a) {
-    char* p = base;
-    WfPool& P = a->pool;
-    P.s0 = carve<float4>(p, pool);
-    P.s1 = carve<float4>(p, pool);
-    P.s2 = carve<float4>(p, pool);
-    P.s3 = carve<float4>(p, pool);
-    P.s4 = carve<float4>(p, pool);
-    P.s5 = carve<float4>(p, pool);
-    P.s6 = carve<float4>(p, pool);
-    P.s7 = carve<float4>(p, pool);
-    P.s8 = carve<uint4>(p, pool);
-    P.s9 = carve<float4>(p, pool);
-    P.h0 = carve<float4>(p, pool);
-    P.h1 = carve<float4>(p, pool);
-    P.m0 = carve<float4>(p, pool);
-    P.m1 = carve<float4>(p, pool);
-    P.m2 = carve<uint32_t>(p, pool);
-    a->q_isect[0] = carve<uint32_t>(p, pool);
-    a->q_isect[1] = carve<uint32_t>(p, pool);
-    a->q_march[0] = carve<uint32_t>(p, pool);
-    a->q_march[1] = carve<uint32_t>(p, pool);
-    a->q_shade = carve<uint32_t>(p, pool);
-    a->q_free = carve<uint32_t>(p, pool);
-    a->colors = carve<float4>(p, total);
-    a->counters = carve<WfCounters>(p, 1);
-    return (size_t)(p - base);
-}
-
-
 }  // namespace
 
 static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push);
@@ -142,7 +105,6 @@ int pt_create(pt_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_cie, sizeof(float) * PT_CIE_TABLE_SIZE);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rot, sizeof(float) * 9 * PT_MAX_SCENE_OBJECTS);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_scene, sizeof(KScene));
-    if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, sizeof(WfCounters));
     if (e != cudaSuccess) {
         pt_destroy(ctx);
         return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
@@ -160,8 +122,11 @@ int pt_destroy(pt_ctx* ctx) {
     if (ctx->d_cie) cudaFree(ctx->d_cie);
     if (ctx->d_rot) cudaFree(ctx->d_rot);
     if (ctx->d_scene) cudaFree(ctx->d_scene);
-    if (ctx->d_wf) cudaFree(ctx->d_wf);
-    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->wf) {
+        ctx->wf->destroy();
+        delete ctx->wf;
+    }
+    if (ctx->d_colors) cudaFree(ctx->d_colors);
     if (ctx->done) cudaEventDestroy(ctx->done);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx->params;
@@ -392,58 +357,56 @@ const char* pt_last_error(pt_ctx* ctx) {
 
 }  // extern "C"
 
-// The wavefront dispatch: iterations are launched in chunks; between chunks
-// the counters are read back to stop once every sample has finished.
+// The wavefront dispatch: one pass of one job on the context's engine,
+// drained, then resolved into the accumulator.
 static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     const uint64_t total64 = (uint64_t)push->resolution[0] * (uint64_t)push->resolution[1] *
                              (uint64_t)push->samplesPerFrame;
-    if (total64 >= (1ull << 31)) return fail(ctx, PT_ERR_INVALID, "pt_dispatch: more than 2^31 samples in one dispatch");
+    if (total64 >= (1ull << 32)) return fail(ctx, PT_ERR_INVALID, "pt_dispatch: more than 2^32 samples in one dispatch");
     const uint32_t total = (uint32_t)total64;
-    const uint32_t pool = total < ctx->pool_cap ? (total < 1024u ? 1024u : total) : ctx->pool_cap;
-    WfArgs a;
-    std::memset(&a, 0, sizeof a);
-    const size_t need = wavefront_layout(reinterpret_cast<char*>(0), pool, total, &a) + 256;
-    if (need > ctx->wf_bytes) {
+    uint32_t pool = total < ctx->pool_cap ? total : ctx->pool_cap;
+    if (pool < 1024u) pool = 1024u;
+    if (!ctx->wf || ctx->wf->pool < pool) {
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        if (ctx->d_wf) cudaFree(ctx->d_wf);
-        ctx->d_wf = nullptr;
-        ctx->wf_bytes = 0;
-        PT_CUDA_TRY(ctx, cudaMalloc(&ctx->d_wf, need));
-        ctx->wf_bytes = need;
+        if (!ctx->wf) ctx->wf = new (std::nothrow) WfEngine();
+        if (!ctx->wf) return fail(ctx, PT_ERR_OOM, "pt_dispatch: out of host memory");
+        PT_CUDA_TRY(ctx, ctx->wf->create(ctx->device, ctx->stream, pool, 4096, ctx->march_budget));
     }
-    wavefront_layout(static_cast<char*>(ctx->d_wf), pool, total, &a);
-    a.scene = ctx->d_scene;
-    a.pc = *push;
-    a.accum = ctx->d_accum;
-    a.cie = ctx->d_cie;
-    a.trace = ctx->trace;
-    a.pool_size = pool;
-    a.total = total;
-    a.march_budget = ctx->march_budget;
+    const size_t cbytes = (size_t)total * sizeof(float4);
+    if (cbytes > ctx->colors_bytes) {
+        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->d_colors) cudaFree(ctx->d_colors);
+        ctx->d_colors = nullptr;
+        ctx->colors_bytes = 0;
+        PT_CUDA_TRY(ctx, cudaMalloc(&ctx->d_colors, cbytes));
+        ctx->colors_bytes = cbytes;
+    }
+    WfEngine& E = *ctx->wf;
+    E.stream = ctx->stream;
+    E.args.march_budget = ctx->march_budget;
+    E.args.trace = ctx->trace;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
-    int dev_sms = 0;
-    PT_CUDA_TRY(ctx, cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    const int grid = dev_sms * 4;  // 4 blocks of 256 threads per SM (64 registers)
-    PT_CUDA_TRY(ctx, ptk_wavefront_launch_init(&a, ctx->stream));
-    const int depth = push->pathLength;
+    PT_CUDA_TRY(ctx, E.reset());
+    WfJob j;
+    std::memset(&j, 0, sizeof j);
+    j.scene = ctx->d_scene;
+    j.cie = ctx->d_cie;
+    j.accum = ctx->d_accum;
+    j.colors = ctx->d_colors;
+    j.pc = *push;
+    uint32_t idx = 0;
+    PT_CUDA_TRY(ctx, E.add_pass(j, &idx));
     // Every iteration moves every live path by one ray; a ray's march spans at
     // most ceil(512 / budget) + 1 iterations.
     const uint64_t march_iters = 512ull / (uint64_t)ctx->march_budget + 2;
-    const uint64_t max_iter = ((uint64_t)total / pool + 2) * (2ull * (uint64_t)depth + 3) * march_iters + 16;
-    uint64_t iter = 0;
-    int chunk = 8;
-    for (;;) {
-        for (int c = 0; c < chunk; c++) PT_CUDA_TRY(ctx, ptk_wavefront_launch_iteration(&a, trace, grid, ctx->stream));
-        iter += (uint64_t)chunk;
-        PT_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_counters, a.counters, sizeof(WfCounters), cudaMemcpyDeviceToHost,
-                                         ctx->stream));
-        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        if (ctx->h_counters->done) break;
-        if (iter > max_iter) return fail(ctx, PT_ERR_KERNEL, "pt_dispatch: wavefront did not drain");
-        if (chunk < 64) chunk *= 2;
-    }
-    ctx->last_iterations = ctx->h_counters->iterations;
-    PT_CUDA_TRY(ctx, ptk_wavefront_launch_resolve(&a, ctx->stream));
+    const uint64_t max_iter =
+        ((uint64_t)total / E.pool + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
+    const cudaError_t e = E.drain(trace, max_iter);
+    if (e == cudaErrorTimeout) return fail(ctx, PT_ERR_KERNEL, "pt_dispatch: wavefront did not drain");
+    PT_CUDA_TRY(ctx, e);
+    ctx->last_iterations = E.host_counters->iterations;
+    E.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
+    PT_CUDA_TRY(ctx, E.resolve(idx));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
 }

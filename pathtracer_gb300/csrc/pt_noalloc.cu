@@ -28,6 +28,7 @@
 #include "../../include/pt_cuda.h"
 #include "kernel/pt_megakernel.h"
 #include "kernel/pt_wavefront.h"
+#include "pt_engine.h"
 
 namespace {
 
@@ -35,14 +36,14 @@ constexpr size_t r256(size_t x) { return (x + 255) / 256 * 256; }
 
 constexpr uint32_t kPool = PT_NOALLOC_POOL_SLOTS;
 constexpr uint32_t kMaxSamples = PT_NOALLOC_MAX_SAMPLES;
+// The engine's arrays for kPool slots and one pass (WfEngine::bytes_for).
+constexpr size_t kEngineBytes =
+    14 * r256((size_t)kPool * 16) + 7 * r256((size_t)kPool * 4) + r256(sizeof(WfCounters)) + r256(sizeof(WfJob));
 constexpr size_t kSceneOff = 0;
 constexpr size_t kCieOff = kSceneOff + r256(sizeof(KScene));
-constexpr size_t kPoolOff = kCieOff + r256(sizeof(float) * PT_CIE_TABLE_SIZE);
-constexpr size_t kVec4Arrays = 14;  // s0..s9, h0, h1, m0, m1 (16 B per slot each)
-constexpr size_t kU32Arrays = 7;    // m2, two ISECT queues, two MARCH queues, SHADE, FREE
-constexpr size_t kColorsOff = kPoolOff + kVec4Arrays * r256((size_t)kPool * 16) + kU32Arrays * r256((size_t)kPool * 4);
-constexpr size_t kCountersOff = kColorsOff + r256((size_t)kMaxSamples * 16);
-constexpr size_t kScratchBytes = kCountersOff + r256(sizeof(WfCounters));
+constexpr size_t kEngineOff = kCieOff + r256(sizeof(float) * PT_CIE_TABLE_SIZE);
+constexpr size_t kColorsOff = kEngineOff + kEngineBytes;
+constexpr size_t kScratchBytes = kColorsOff + r256((size_t)kMaxSamples * 16);
 static_assert(kScratchBytes <= PT_NOALLOC_SCRATCH_BYTES, "PT_NOALLOC_SCRATCH_BYTES is too small");
 
 }  // namespace
@@ -106,13 +107,6 @@ int build_scene(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplug, KSce
     return PT_OK;
 }
 
-template <typename T>
-T* take(unsigned char*& p, size_t count) {
-    T* r = reinterpret_cast<T*>(p);
-    p += r256(count * sizeof(T));
-    return r;
-}
-
 #define PT_NA_TRY(call)                                 \
     do {                                                \
         if ((call) != cudaSuccess) return PT_ERR_CUDA; \
@@ -160,62 +154,30 @@ extern "C" int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugi
         return PT_OK;
     }
 
-    WfArgs a;
-    std::memset(&a, 0, sizeof a);
-    unsigned char* p = base + kPoolOff;
-    WfPool& P = a.pool;
-    P.s0 = take<float4>(p, kPool);
-    P.s1 = take<float4>(p, kPool);
-    P.s2 = take<float4>(p, kPool);
-    P.s3 = take<float4>(p, kPool);
-    P.s4 = take<float4>(p, kPool);
-    P.s5 = take<float4>(p, kPool);
-    P.s6 = take<float4>(p, kPool);
-    P.s7 = take<float4>(p, kPool);
-    P.s8 = take<uint4>(p, kPool);
-    P.s9 = take<float4>(p, kPool);
-    P.h0 = take<float4>(p, kPool);
-    P.h1 = take<float4>(p, kPool);
-    P.m0 = take<float4>(p, kPool);
-    P.m1 = take<float4>(p, kPool);
-    P.m2 = take<uint32_t>(p, kPool);
-    a.q_isect[0] = take<uint32_t>(p, kPool);
-    a.q_isect[1] = take<uint32_t>(p, kPool);
-    a.q_march[0] = take<uint32_t>(p, kPool);
-    a.q_march[1] = take<uint32_t>(p, kPool);
-    a.q_shade = take<uint32_t>(p, kPool);
-    a.q_free = take<uint32_t>(p, kPool);
-    a.colors = reinterpret_cast<float4*>(base + kColorsOff);
-    a.counters = reinterpret_cast<WfCounters*>(base + kCountersOff);
-    a.scene = d_scene;
-    a.pc = *push;
-    a.accum = reinterpret_cast<float4*>(d_accum);
-    a.cie = d_cie;
-    a.trace = KTrace{nullptr, nullptr, nullptr, 0};
-    a.pool_size = total < kPool ? (total < 1024u ? 1024u : total) : kPool;
-    a.total = total;
-    a.march_budget = 64;
-
-    int sms = 0;
-    PT_NA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    const int grid = sms * 4;
-    PT_NA_TRY(ptk_wavefront_launch_init(&a, stream));  // resets the counters left by the previous call
+    // The wavefront engine on the fixed array, with host read-back storage on
+    // the stack.
+    if (WfEngine::bytes_for(kPool, 1) != kEngineBytes) return PT_ERR_INVALID;
+    WfEngine engine;
+    WfCounters counters;
+    WfJob job_table[1];
+    PT_NA_TRY(engine.attach(device, stream, total < kPool ? (total < 1024u ? 1024u : total) : kPool, 1, 64,
+                            base + kEngineOff, kEngineBytes, &counters, job_table));
+    WfJob j;
+    std::memset(&j, 0, sizeof j);
+    j.scene = d_scene;
+    j.cie = d_cie;
+    j.accum = reinterpret_cast<float4*>(d_accum);
+    j.colors = reinterpret_cast<float4*>(base + kColorsOff);
+    j.pc = *push;
+    uint32_t idx = 0;
+    PT_NA_TRY(engine.add_pass(j, &idx));
     const uint64_t march_iters = 512ull / 64ull + 2;
     const uint64_t max_iter =
-        ((uint64_t)total / a.pool_size + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
-    uint64_t iter = 0;
-    int chunk = 8;
-    WfCounters hc;
-    for (;;) {
-        for (int c = 0; c < chunk; c++) PT_NA_TRY(ptk_wavefront_launch_iteration(&a, false, grid, stream));
-        iter += (uint64_t)chunk;
-        PT_NA_TRY(cudaMemcpyAsync(&hc, a.counters, sizeof hc, cudaMemcpyDeviceToHost, stream));
-        PT_NA_TRY(cudaStreamSynchronize(stream));
-        if (hc.done) break;
-        if (iter > max_iter) return PT_ERR_KERNEL;
-        if (chunk < 64) chunk *= 2;
-    }
-    PT_NA_TRY(ptk_wavefront_launch_resolve(&a, stream));
+        ((uint64_t)total / engine.pool + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
+    const cudaError_t e = engine.drain(false, max_iter);
+    if (e == cudaErrorTimeout) return PT_ERR_KERNEL;
+    PT_NA_TRY(e);
+    PT_NA_TRY(engine.resolve(idx));
     PT_NA_TRY(cudaStreamSynchronize(stream));
     return PT_OK;
 }
