@@ -10,6 +10,14 @@ the device.  `e2e` repeats the step through the reference-facing C ABI
 dispatches, and the read-back of the 16 MiB accumulator each step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py --workload batch64 [--steps K] [--warmup W]
+
+--workload batch64 is the mixed-job batch: 64 seeded sphere-scene jobs
+(pt_scene_generate, seeds 0-63: 128^2-1024^2, 4-256 spp, depth 8; 1.80 G
+path samples) rendered as one batch through pt_batch (one pass per job, all
+in one wavefront pool), against the same 64 jobs dispatched one after
+another through the plain megakernel on one stream.  Both render the same
+samples, so the images are bit-identical (checked) and the RMSE is equal.
 
 Under torchrun each rank renders its own replica (distinct sample indices,
 no exchange): weak scaling.  --impl reference times the CPU restatement of
@@ -18,6 +26,7 @@ the reference shader (the reference itself is Vulkan-only) on the host cores.
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import statistics
@@ -52,6 +61,10 @@ def parse_args():
     ap.add_argument("--compare-engines", type=int, default=1, help="also time the other engine (1 step)")
     ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0: library default)")
     ap.add_argument("--budget", type=int, default=0, help="wavefront march steps per launch (0: default)")
+    ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64"])
+    ap.add_argument("--jobs", type=int, default=64, help="batch64: jobs per batch")
+    ap.add_argument("--route", default="auto", choices=["auto", "staged", "persistent"],
+                    help="batch64: engine route of the passes")
     return ap.parse_args()
 
 
@@ -175,8 +188,214 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
     return 0
 
+BATCH_WORKLOAD = "batch64_spheres_seeds0-63_res128-1024_spp4-256_depth8"
+
+
+def make_jobs(n, first_seed, kind=None):
+    """n seeded jobs: (scene, spec, packed ubo, plug-ins)."""
+    from pathtracer_gb300 import Scene, cie_analytic, native
+
+    cie = cie_analytic()
+    out = []
+    for seed in range(first_seed, first_seed + n):
+        scene, spec = Scene.generate(native.PT_GEN_SPHERES if kind is None else kind, seed)
+        out.append((scene, spec, scene.pack_ubo(cie), scene.sdf_plugins()))
+    return out, cie
+
+
+def pctl(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = min(len(xs) - 1, max(0, int(np.ceil(q / 100.0 * len(xs))) - 1))
+    return xs[k]
+
+
+def batch_cpu_baseline(jobs, nthreads, rows_per_job=2, njobs=16):
+    """The CPU restatement (oracle, OpenMP) on rows of the first jobs."""
+    from oracle import compare
+
+    samples = 0
+    t0 = time.perf_counter()
+    for scene, spec, ubo, plugins in jobs[:njobs]:
+        W, H = spec.width, spec.height
+        push = scene.push_constants(W, H, spec.spp, spec.spp, spec.spp, spec.pathLength)
+        acc = np.zeros((H, W, 4), np.float32)
+        for r in range(rows_per_job):
+            y = (2 * r + 1) * H // (2 * rows_per_job)
+            compare.run_oracle(ubo, push, compare.plugins_for(scene), accum=acc, rect=(0, y, W, y + 1),
+                               nthreads=nthreads)
+            samples += W * spec.spp
+    dt = time.perf_counter() - t0
+    return samples / dt, samples, dt
+
+
+def run_batch(args, rank, world):
+    """The mixed-job batch: batched wavefront vs the plain megakernel, serial."""
+    import torch
+
+    from pathtracer_gb300 import Batch, Context, build, native
+
+    build.build()
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
+    local = torch.cuda.current_device()
+    jobs, cie = make_jobs(args.jobs, rank * args.jobs)
+    pushes = [sc.push_constants(sp.width, sp.height, sp.spp, sp.spp, sp.spp, sp.pathLength) for sc, sp, _, _ in jobs]
+    samples = sum(sp.width * sp.height * sp.spp for _, sp, _, _ in jobs)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    b = Batch(local, pool_slots=args.pool or (1 << 21), max_passes=4096)
+    b.set_route({"auto": native.PT_BATCH_ROUTE_AUTO, "staged": native.PT_BATCH_ROUTE_STAGED,
+                 "persistent": native.PT_BATCH_ROUTE_PERSISTENT}[args.route])
+    if args.budget:
+        b.set_march_budget(args.budget)
+    sids = [b.add_scene(ubo, plugins) for _, _, ubo, plugins in jobs]
+    tids = [b.add_target(sp.width, sp.height) for _, sp, _, _ in jobs]
+    bstream = torch.cuda.ExternalStream(b.stream())
+
+    def batched_step():
+        with torch.cuda.stream(bstream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(bstream)
+        it0 = b.stats()["iterations"]
+        for sid, tid, push in zip(sids, tids, pushes):
+            b.add_pass(sid, tid, push)
+        lat = {}
+        chunk = 16
+        while b.pending():
+            for pid in b.step(chunk):
+                lat[pid] = time.perf_counter() - t0
+        e1.record(bstream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1000.0, list(lat.values()), b.stats()["iterations"] - it0
+
+    for _ in range(args.warmup):
+        batched_step()
+    bt, blat, biters = [], [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            secs, lat, iters = batched_step()
+            bt.append(secs)
+            blat += lat
+            biters.append(iters)
+    b_secs = statistics.mean(bt)
+    batched_images = [b.read_target(t) for t in tids[:8]]
+
+    # The plain megakernel: one context per job (scene bound, accumulator
+    # resident), every dispatch on one stream, one after another.
+    ctxs = []
+    for scene, spec, _, _ in jobs:
+        c = Context(local)
+        c.set_engine(native.PT_ENGINE_MEGAKERNEL)
+        c.bind(scene, cie)
+        c.resize_accum(spec.width, spec.height)
+        ctxs.append(c)
+    shared = ctxs[0].stream()
+    for c in ctxs:
+        c.set_stream(shared)
+    pstream = torch.cuda.ExternalStream(shared)
+
+    def plain_step():
+        with torch.cuda.stream(pstream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e0.record(pstream)
+        evs = []
+        for c, push in zip(ctxs, pushes):
+            c.dispatch(push)
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(pstream)
+            evs.append(ev)
+        evs[-1].synchronize()
+        return e0.elapsed_time(evs[-1]) / 1000.0, [e0.elapsed_time(ev) / 1000.0 for ev in evs]
+
+    plain_steps = max(1, min(args.steps, 2))
+    plain_step()
+    pt_, plat = [], []
+    for _ in range(plain_steps):
+        secs, lat = plain_step()
+        pt_.append(secs)
+        plat += lat
+    p_secs = statistics.mean(pt_)
+    identical = all(np.array_equal(img.view(np.uint32), c.read_accum().view(np.uint32))
+                    for img, c in zip(batched_images, ctxs))
+    # The shared stream belongs to ctxs[0]: hand every context its own stream
+    # back before any is destroyed.
+    for c in ctxs:
+        c.set_stream(None)
+    for c in ctxs:
+        c.close()
+
+    # End to end through the C ABI from host buffers: scene upload, targets,
+    # passes, run, read-back of every image, release.
+    e2e = []
+    h2d = d2h = 0
+    for _ in range(max(1, min(args.steps, 2))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = [b.add_scene(ubo, plugins) for _, _, ubo, plugins in jobs]
+        t2 = [b.add_target(sp.width, sp.height) for _, sp, _, _ in jobs]
+        for sid, tid, push in zip(s2, t2, pushes):
+            b.add_pass(sid, tid, push)
+        b.run()
+        imgs = [b.read_target(t) for t in t2]
+        e2e.append(time.perf_counter() - t0)
+        h2d = native.UBO_FLOATS * 4 * len(jobs)
+        d2h = sum(im.nbytes for im in imgs)
+        for sid, tid in zip(s2, t2):
+            b.release_target(tid)
+            b.release_scene(sid)
+    e2e_secs = statistics.median(e2e)
+    st = b.stats()
+    b.close()
+
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([b_secs, e2e_secs], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        b_secs, e2e_secs = (float(x) for x in t.tolist())
+    value = samples * world / b_secs
+    peaks, peak_kind = measured_peaks()
+    iters = statistics.mean(biters)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * b_secs, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+        "config": {"workload": BATCH_WORKLOAD, "jobs": len(jobs), "samples_per_step": samples,
+                   "passes_per_job": 1, "route": args.route, "passes_staged": st["passes_staged"],
+                   "passes_persistent": st["passes_persistent"], "l2": "flushed between timed steps (256 MiB write)",
+                   "parallelism": f"replicas x{world}", "wavefront_pool": st["pool_slots"],
+                   "march_budget": args.budget or None},
+        "e2e": {"value": samples * world / e2e_secs, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "batched": {"value": samples / b_secs, "ms_per_step": 1000.0 * b_secs,
+                    "job_latency_s": {"p50": pctl(blat, 50), "p99": pctl(blat, 99)},
+                    "iterations_per_step": iters},
+        "plain_megakernel_serial": {"value": samples / p_secs, "ms_per_step": 1000.0 * p_secs,
+                                    "job_latency_s": {"p50": pctl(plat, 50), "p99": pctl(plat, 99)}},
+        "speedup_vs_plain": p_secs / b_secs,
+        "results_identical_to_plain": identical,
+        "gpu_launches": int(args.steps * (5 * iters + 2 * len(jobs))),
+        "roofline": {"bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": None,
+                     "traffic": None, "note": f"peak {peak_kind}; see the mandelbulb workload for the kernel roofline"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        nthreads = os.cpu_count() or 1
+        v, n, dt = batch_cpu_baseline(jobs, nthreads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                "sample": f"2 rows of each of the first 16 jobs at their spp ({n} paths, {dt:.1f} s)"}
+        print(json.dumps(line), flush=True)
+    return 0
+
 
 def main():
+    faulthandler.enable()
     args = parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -188,6 +407,13 @@ def main():
 
             torch.cuda.set_device(local)
         dist.init_process_group(backend=backend)
+    if args.workload == "batch64":
+        rc = run_batch(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+        return rc
     if args.impl == "reference":
         rc = run_reference(args, rank, world)
         if world > 1:

@@ -50,6 +50,7 @@ extern "C" {
 #define PT_ERR_OOM 6           /* device allocation failed */
 #define PT_ERR_KERNEL 7        /* a kernel reported an error through its status word */
 #define PT_ERR_TOO_LARGE 8     /* the request exceeds pt_dispatch_noalloc's fixed scratch */
+#define PT_ERR_BUSY 9          /* the resource is still in use by passes in flight */
 
 /* Byte-for-byte the reference's UniformBufferObject (src/pathtracer.cpp:187-195)
  * and the shader's `ubo` block (src/shader.comp:19-27): 4097 floats = 16388 B.
@@ -180,7 +181,10 @@ int pt_write_accum(pt_ctx* ctx, const float* host, size_t bytes);
 void* pt_accum_device_ptr(pt_ctx* ctx);
 
 /* The cudaStream_t the context launches on (as void*), and a way to replace
- * it with a caller-owned stream (NULL restores the context's own stream). */
+ * it with a caller-owned stream (NULL restores the context's own stream).
+ * A replaced stream must outlive every later call on the context, pt_destroy
+ * included (it synchronises the stream): restore NULL before the stream's
+ * owner — possibly another context — destroys it. */
 void* pt_stream(pt_ctx* ctx);
 int pt_set_stream(pt_ctx* ctx, void* stream);
 
@@ -225,6 +229,91 @@ int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float
 #define PT_NOALLOC_POOL_SLOTS (1u << 16)
 int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins, const pt_push* push,
                         float* d_accum, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Batched rendering.  No counterpart in the reference, which renders one
+ * scene per compute dispatch (src/pathtracer.cpp:3586-3608): these calls keep
+ * many scenes and accumulators resident on one device and run render passes
+ * of all of them through one shared wavefront path pool, so a pass of a small
+ * job fills the lanes a large job leaves idle.
+ *
+ *   scene   a packed pt_ubo plus its SDF plug-ins (as pt_upload_scene +
+ *           pt_set_sdf_plugins), copied at call time;
+ *   target  an accumulator of W x H pixels: PT_TARGET_FLOAT is the
+ *           reference's float4 XYZ buffer (Rendering/Accumulate,
+ *           src/shader.comp:1492-1523); PT_TARGET_FP64 sums every sample's
+ *           exposed XYZ in double precision (reference images: FP32 paths,
+ *           FP64 accumulation; read back as the mean);
+ *   pass    one dispatch's worth of samples (a pt_push) of one scene into one
+ *           target.  A pass into a float target ends with exactly the value
+ *           pt_dispatch would leave for the same push constants, bit for bit.
+ *
+ * Two engines run the passes, each on its own stream: the staged wavefront
+ * kernels (compacted ray queues; best where SDF marching makes lanes
+ * diverge) and a persistent path kernel (paths stay in registers, lanes
+ * refill from a shared sample counter; best for analytic scenes).  The
+ * default route sends passes of scenes with SDFs to the first and the rest
+ * to the second; both give results bit-identical to pt_dispatch.
+ *
+ * Passes are resolved in the order they were added per target; passes of
+ * different targets complete independently.  A batch is single-threaded like
+ * a context.  pt_batch_step returns the passes that completed (resolved) since
+ * the last call; pt_batch_run steps until none is pending.
+ * ------------------------------------------------------------------------- */
+typedef struct pt_batch pt_batch;
+
+#define PT_TARGET_FLOAT 0
+#define PT_TARGET_FP64 1
+
+#define PT_BATCH_ROUTE_AUTO 0       /* SDF scenes staged, analytic scenes persistent */
+#define PT_BATCH_ROUTE_STAGED 1     /* every pass through the staged wavefront kernels */
+#define PT_BATCH_ROUTE_PERSISTENT 2 /* every pass through the persistent path kernel */
+
+typedef struct pt_batch_info {
+    uint64_t samples_done;  /* samples of resolved passes */
+    uint64_t samples_added; /* samples of every pass added */
+    uint64_t iterations;    /* wavefront iterations launched */
+    uint32_t passes_added;
+    uint32_t passes_pending;
+    uint32_t pool_slots;
+    uint32_t pass_slots;    /* passes of one engine that can be in flight at once */
+    uint32_t passes_staged; /* passes routed to each engine so far */
+    uint32_t passes_persistent;
+} pt_batch_info;
+
+/* pool_slots >= 1024 paths in flight in the staged engine; max_passes passes
+ * of each engine in flight at once. */
+int pt_batch_create(pt_batch** out, int device, uint32_t pool_slots, uint32_t max_passes);
+int pt_batch_destroy(pt_batch* batch);
+const char* pt_batch_last_error(pt_batch* batch);
+void* pt_batch_stream(pt_batch* batch);
+int pt_batch_set_march_budget(pt_batch* batch, int steps);
+/* Engine choice for passes added from now on (PT_BATCH_ROUTE_*). */
+int pt_batch_set_route(pt_batch* batch, int route);
+int pt_batch_add_scene(pt_batch* batch, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins,
+                       int* scene_id);
+int pt_batch_add_target(pt_batch* batch, int width, int height, int kind, int* target_id);
+/* Device pointer of a target: float4 per pixel (FLOAT) or 4 doubles per pixel
+ * (FP64: x, y, z sums and the sample count). */
+void* pt_batch_target_device_ptr(pt_batch* batch, int target_id);
+/* Queues a pass; push->resolution must be the target's.  PT_ERR_BUSY when
+ * max_passes passes are in flight. */
+int pt_batch_add_pass(pt_batch* batch, int scene_id, int target_id, const pt_push* push, int* pass_id);
+int pt_batch_step(pt_batch* batch, int iterations, int* completed, int capacity, int* ncompleted);
+int pt_batch_pending(pt_batch* batch);
+int pt_batch_run(pt_batch* batch, uint64_t max_iterations);
+int pt_batch_stats(pt_batch* batch, pt_batch_info* out);
+/* Samples per pixel resolved into a target so far. */
+int pt_batch_target_samples(pt_batch* batch, int target_id, uint64_t* samples);
+/* W*H float4 (FP64 targets: their mean, rounded to float). */
+int pt_batch_read_target(pt_batch* batch, int target_id, float* host, size_t bytes);
+/* sqrt(sum |a - r|^2 / sum |r|^2) over the XYZ channels of a float target a
+ * against a reference target r of the same size, reduced on the device in
+ * double precision. */
+int pt_batch_rmse(pt_batch* batch, int target_id, int reference_id, double* rel_rmse);
+/* PT_ERR_BUSY while passes of the target / scene are in flight. */
+int pt_batch_release_target(pt_batch* batch, int target_id);
+int pt_batch_release_scene(pt_batch* batch, int scene_id);
 
 /* Event word layout, identical in the CPU restatement used by the tests. */
 #define PT_EV_HIT_MASK 0xFFFu     /* global object index; PT_EV_HIT_SDF, PT_EV_HIT_MISS */

@@ -71,6 +71,36 @@ int pt_scene_to_json(const pt_scene* scene, char* buf, size_t cap, size_t* neede
  * recompile it triggers in the reference, :3442-3461 and :3836-3841). */
 int pt_scene_bind(pt_ctx* ctx, const pt_scene* scene, const float* cie);
 
+/* The scene's SDF plug-ins (each SDF's source through pt_parse_sdf_source),
+ * for pt_batch_add_scene: writes min(count, cap) entries, *count = SDFs. */
+int pt_scene_sdf_plugins(const pt_scene* scene, pt_sdf_plugin* out, int cap, int* count);
+
+/* Seeded synthetic render jobs.  No counterpart in the reference: stand-ins
+ * for a stream of user scenes, deterministic per seed on every platform
+ * (std::mt19937_64 plus libm-free transforms), expressed in the reference's
+ * scene schema and method.
+ *   PT_GEN_SPHERES  4-64 spheres, centres U[-2,2]^3, radii lognormal(-1.5,
+ *                   0.5), three material classes, on a ground plane, one
+ *                   blackbody sphere light at 3000-9000 K; W = H uniform over
+ *                   {128, 256, 512, 1024}; spp log-uniform over [4, 256];
+ *                   path length 8.
+ *   PT_GEN_SDF      a mandelbulb, menger or blob plug-in over a ground plane
+ *                   under a sky and a sun; W = H uniform over {256, 512,
+ *                   1024}; spp 0 (open); path length 8. */
+#define PT_GEN_SPHERES 0
+#define PT_GEN_SDF 1
+typedef struct pt_job_spec {
+    int32_t kind;
+    int32_t width, height;
+    int32_t spp;
+    int32_t pathLength;
+    int32_t sdf_kind; /* PT_SDF_* of an SDF job, PT_SDF_NONE otherwise */
+    int32_t objects;  /* spheres of a sphere job (light excluded), 1 for an SDF job */
+    int32_t pad;
+    uint64_t seed;
+} pt_job_spec;
+int pt_scene_generate(int kind, uint64_t seed, pt_scene** out, pt_job_spec* spec);
+
 /* The reference's offscreen render (numSamples, samplesPerFrame, path length
  * and shot index read from stdin there): frame += spf per dispatch until
  * currentSamples >= numSamples, then the accumulator is read back. */

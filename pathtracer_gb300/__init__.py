@@ -6,6 +6,6 @@ and libpt_host.so (headless scene/packing/offscreen host, include/pt_host.h).
 This package builds them in-tree (``build.build()``) and binds them with
 ctypes (``native``, ``renderer``).
 """
-from .renderer import Context, PathTracerError, Scene, cie_analytic, export_rgb8, render_offscreen  # noqa: F401
+from .renderer import Batch, Context, PathTracerError, Scene, cie_analytic, export_rgb8, render_offscreen  # noqa: F401
 
 SCENES_DIR = __import__("os").path.join(__import__("os").path.dirname(__file__), "scenes")

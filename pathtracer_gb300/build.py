@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "lib")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-shared"]
+NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", "-Wextra"]
 
 CUDA_SOURCES = [
@@ -29,12 +29,14 @@ CUDA_SOURCES = [
     "pt_api.cu",
     "pt_engine.cu",
     "pt_noalloc.cu",
+    "pt_batch.cu",
     "pt_sdf_source.cpp",
 ]
 HOST_SOURCES = [
     "host/pt_json.cpp",
     "host/pt_scene.cpp",
     "host/pt_offscreen.cpp",
+    "host/pt_generate.cpp",
 ]
 
 
@@ -75,14 +77,24 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, str]:
     cuda_src = [os.path.join(CSRC, s) for s in CUDA_SOURCES]
     host_src = [os.path.join(CSRC, s) for s in HOST_SOURCES]
 
-    cuda_cmd = [nvcc, *NVCC_FLAGS, "-o", cuda_so, *cuda_src]
     host_cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, f"-I{cuda_inc}", "-o", host_so, *host_src,
                 f"-L{LIB}", "-lpt_cuda", "-Wl,-rpath,$ORIGIN"]
 
     if force or _stale(cuda_so, cuda_src):
+        # One object per translation unit, compiled in parallel, then linked.
+        objdir = os.path.join(LIB, "obj")
+        os.makedirs(objdir, exist_ok=True)
+        objs = [os.path.join(objdir, os.path.basename(s) + ".o") for s in cuda_src]
+        cmds = [[nvcc, *NVCC_FLAGS, "-c", "-o", o, s] for s, o in zip(cuda_src, objs)]
         if verbose:
-            print(" ".join(cuda_cmd), file=sys.stderr)
-        _run(cuda_cmd)
+            for c in cmds:
+                print(" ".join(c), file=sys.stderr)
+        with ThreadPoolExecutor(max_workers=min(len(cmds), os.cpu_count() or 1)) as ex:
+            list(ex.map(_run, cmds))
+        link = [nvcc, ARCH, "-shared", "-o", cuda_so, *objs]
+        if verbose:
+            print(" ".join(link), file=sys.stderr)
+        _run(link)
     if force or _stale(host_so, host_src) or os.path.getmtime(cuda_so) > os.path.getmtime(host_so):
         if verbose:
             print(" ".join(host_cmd), file=sys.stderr)

@@ -350,6 +350,17 @@ const char* pt_scene_sdf_source(const pt_scene* s, int i) {
     return s->sdfs[(size_t)i].source.c_str();
 }
 
+int pt_scene_sdf_plugins(const pt_scene* s, pt_sdf_plugin* out, int cap, int* count) {
+    if (!s || !count || cap < 0 || (cap > 0 && !out)) return PT_ERR_INVALID;
+    const int n = (int)s->sdfs.size();
+    *count = n;
+    for (int i = 0; i < n && i < cap; i++) {
+        const int rc = pt_parse_sdf_source(s->sdfs[(size_t)i].source.c_str(), &out[i]);
+        if (rc != PT_OK) return rc;
+    }
+    return PT_OK;
+}
+
 // UpdateToJSON, PT:2724-2858, then dump(4).
 int pt_scene_to_json(const pt_scene* s, char* buf, size_t cap, size_t* needed) {
     if (!s) return PT_ERR_INVALID;

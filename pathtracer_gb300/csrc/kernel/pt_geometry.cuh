@@ -6,6 +6,7 @@
 // from the launch's constant bank instead of being unpacked into structs.
 #pragma once
 
+#include "pt_features.h"
 #include "pt_scene.cuh"
 
 #define PT_PI 3.141592653589792623810034526344f  // SC:9
@@ -580,6 +581,7 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
 // The analytic part of Intersection (SC:862-923) and of the object loop of
 // LightSourceVisibilityCheck (SC:1121-1201): objectID = index of the last
 // object whose test hit, -1 for none.
+template <int FEAT = PT_FEAT_ALL>
 PT_DI void intersect_analytic(const KScene& S, float3 org, float3 dir, Hit& h, int& objectID) {
     int id = -1;
     const int n0 = S.meta.n[0], n1 = S.meta.n[1], n2 = S.meta.n[2], n3 = S.meta.n[3], n4 = S.meta.n[4];
@@ -600,48 +602,57 @@ PT_DI void intersect_analytic(const KScene& S, float3 org, float3 dir, Hit& h, i
                             h))
             id = gi;
     }
+    if constexpr ((FEAT & PT_FEAT_BOX) != 0) {
 #pragma unroll 1
-    for (int i = 0; i < n2; i++, gi++) {
-        const int b = S.meta.offset[2] + 11 * i;
-        const float3 pos = f3(S.objects[b], S.objects[b + 1], S.objects[b + 2]);
-        const float3 size = f3(S.objects[b + 6], S.objects[b + 7], S.objects[b + 8]);
-        if (!bounding_sphere(org, dir, pos, 0.25f * dot3(size, size))) continue;
-        if (box_intersect(org, dir, pos, size, s_rotation(S, gi), (float)((int)S.objects[b + 9] - 1),
-                          (float)((int)S.objects[b + 10] - 1), h))
-            id = gi;
+        for (int i = 0; i < n2; i++, gi++) {
+            const int b = S.meta.offset[2] + 11 * i;
+            const float3 pos = f3(S.objects[b], S.objects[b + 1], S.objects[b + 2]);
+            const float3 size = f3(S.objects[b + 6], S.objects[b + 7], S.objects[b + 8]);
+            if (!bounding_sphere(org, dir, pos, 0.25f * dot3(size, size))) continue;
+            if (box_intersect(org, dir, pos, size, s_rotation(S, gi), (float)((int)S.objects[b + 9] - 1),
+                              (float)((int)S.objects[b + 10] - 1), h))
+                id = gi;
+        }
     }
+    if constexpr ((FEAT & PT_FEAT_LENS) != 0) {
 #pragma unroll 1
-    for (int i = 0; i < n3; i++, gi++) {
-        const int b = S.meta.offset[3] + 12 * i;
-        LensGeom L;
-        L.pos = f3(S.objects[b], S.objects[b + 1], S.objects[b + 2]);
-        L.radius = S.objects[b + 6];
-        L.focal = S.objects[b + 7];
-        L.thickness = S.objects[b + 8];
-        L.converging = S.objects[b + 9] != 0.0f;
-        if (!bounding_sphere(org, dir, L.pos, lens_bounding_radius2(L.radius, L.focal, L.thickness, L.converging)))
-            continue;
-        L.rot = s_rotation(S, gi);
-        int isOutside = 1;
-        if (lens_intersect(org, dir, L, (float)((int)S.objects[b + 10] - 1), (float)((int)S.objects[b + 11] - 1),
-                           h, isOutside))
-            id = gi;
+        for (int i = 0; i < n3; i++, gi++) {
+            const int b = S.meta.offset[3] + 12 * i;
+            LensGeom L;
+            L.pos = f3(S.objects[b], S.objects[b + 1], S.objects[b + 2]);
+            L.radius = S.objects[b + 6];
+            L.focal = S.objects[b + 7];
+            L.thickness = S.objects[b + 8];
+            L.converging = S.objects[b + 9] != 0.0f;
+            if (!bounding_sphere(org, dir, L.pos, lens_bounding_radius2(L.radius, L.focal, L.thickness, L.converging)))
+                continue;
+            L.rot = s_rotation(S, gi);
+            int isOutside = 1;
+            if (lens_intersect(org, dir, L, (float)((int)S.objects[b + 10] - 1), (float)((int)S.objects[b + 11] - 1),
+                               h, isOutside))
+                id = gi;
+        }
     }
+    if constexpr ((FEAT & PT_FEAT_CYCLIDE) != 0) {
 #pragma unroll 1
-    for (int i = 0; i < n4; i++, gi++) {
-        const int b = S.meta.offset[4] + 16 * i;
-        const float3 pos = f3(S.objects[b], S.objects[b + 1], S.objects[b + 2]);
-        if (!bounding_sphere(org, dir, pos, S.objects[b + 13])) continue;
-        if (cyclide_intersect(S, org, dir, b, s_rotation(S, gi), h)) id = gi;
+        for (int i = 0; i < n4; i++, gi++) {
+            const int b = S.meta.offset[4] + 16 * i;
+            const float3 pos = f3(S.objects[b], S.objects[b + 1], S.objects[b + 2]);
+            if (!bounding_sphere(org, dir, pos, S.objects[b + 13])) continue;
+            if (cyclide_intersect(S, org, dir, b, s_rotation(S, gi), h)) id = gi;
+        }
     }
     objectID = id;
 }
 
 // Intersection (SC:862-934) / LightSourceVisibilityCheck's loop: the analytic
 // objects, then sphere tracing of the SDFs (objectID -2 for an SDF hit).
+template <int FEAT = PT_FEAT_ALL>
 PT_DI void intersect_all(const KScene& S, float3 org, float3 dir, Hit& h, int& objectID) {
-    intersect_analytic(S, org, dir, h, objectID);
-    if (S.meta.n[5] > 0) {
-        if (sphere_trace(S, org, dir, h)) objectID = -2;
+    intersect_analytic<FEAT>(S, org, dir, h, objectID);
+    if constexpr ((FEAT & PT_FEAT_SDF) != 0) {
+        if (S.meta.n[5] > 0) {
+            if (sphere_trace(S, org, dir, h)) objectID = -2;
+        }
     }
 }

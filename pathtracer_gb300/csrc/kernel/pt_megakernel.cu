@@ -16,7 +16,7 @@
 
 namespace {
 
-template <bool TRACE>
+template <bool TRACE, int FEAT>
 __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constant__ KParams P) {
     const KScene& S = P.s;
     const pt_push& pc = P.pc;
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
         h.materialID = 0.0f;
         h.lightID = -1.0f;
         int objectID = -1;
-        intersect_all(S, ps.org, shadow ? ps.shDir : ps.dir, h, objectID);
+        intersect_all<FEAT>(S, ps.org, shadow ? ps.shDir : ps.dir, h, objectID);
         const StepResult r =
             shadow ? shade_shadow<TRACE>(ps, S, objectID, depth) : shade_primary<TRACE>(ps, S, h, objectID, depth);
         shadow = (r == STEP_SHADOW);
@@ -151,9 +151,15 @@ cudaError_t ptk_launch_megakernel(const KParams* params, bool trace, cudaStream_
     const dim3 block(PT_MK_BLOCK_X, PT_MK_BLOCK_Y);
     const dim3 grid((W + PT_MK_BLOCK_X - 1) / PT_MK_BLOCK_X, (H + PT_MK_BLOCK_Y - 1) / PT_MK_BLOCK_Y);
     if (trace) {
-        megakernel<true><<<grid, block, 0, stream>>>(*params);
-    } else {
-        megakernel<false><<<grid, block, 0, stream>>>(*params);
+        megakernel<true, PT_FEAT_ALL><<<grid, block, 0, stream>>>(*params);
+        return cudaGetLastError();
+    }
+    // The smallest variant that covers the scene's primitive classes.
+    switch (pt_feature_variant(params->s.meta.n)) {
+        case 0: megakernel<false, 0><<<grid, block, 0, stream>>>(*params); break;
+        case PT_FEAT_BOX: megakernel<false, PT_FEAT_BOX><<<grid, block, 0, stream>>>(*params); break;
+        case PT_FEAT_ANALYTIC: megakernel<false, PT_FEAT_ANALYTIC><<<grid, block, 0, stream>>>(*params); break;
+        default: megakernel<false, PT_FEAT_ALL><<<grid, block, 0, stream>>>(*params); break;
     }
     return cudaGetLastError();
 }

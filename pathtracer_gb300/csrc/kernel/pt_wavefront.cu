@@ -100,19 +100,19 @@ PT_DI void store_state(const PoolView& v, uint32_t slot, const PathState& ps, ui
 
 PT_DI uint32_t slot_job(const PoolView& v, uint32_t slot) { return __float_as_uint(v.s9[slot].z); }
 
-// The job whose pass holds global sample s: the last job with first <= s
-// (passes are appended in increasing order of first).
-PT_DI uint32_t find_job(const WfJob* __restrict__ jobs, uint32_t njobs, uint64_t s) {
-    uint32_t lo = 0, hi = njobs;  // invariant: jobs[lo].first <= s < jobs[hi].first
+// The ring entry of the pass that holds global sample s: the last pass in
+// [lo, hi) with first <= s (passes are appended in increasing order of first).
+PT_DI uint32_t find_job(const WfJob* __restrict__ jobs, uint32_t cap, uint32_t lo, uint32_t hi, uint64_t s) {
+    // invariant: jobs[lo % cap].first <= s < jobs[hi % cap].first (or hi is the end)
     while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (jobs[mid].first <= s) {
+        const uint32_t mid = lo + ((hi - lo) >> 1);
+        if (jobs[mid % cap].first <= s) {
             lo = mid;
         } else {
             hi = mid;
         }
     }
-    return lo;
+    return lo % cap;
 }
 
 // Sample id s of a dispatch: k = s / (W*H), pixel = s % (W*H).  The colour
@@ -123,16 +123,17 @@ PT_DI size_t trace_index(const pt_push& pc, uint32_t s) {
     return (size_t)(s % npix) * (size_t)pc.samplesPerFrame + (size_t)(s / npix);
 }
 
-// Samples of every pass in the table (passes are appended in order of first).
-PT_DI uint64_t jobs_total(const WfArgs& A) {
-    if (A.njobs == 0) return 0;
-    const WfJob& L = A.jobs[A.njobs - 1];
+// Samples of every pass added so far: the end of the last pass.
+PT_DI uint64_t jobs_total(const WfArgs& A, uint32_t hi) {
+    if (hi == 0) return 0;
+    const WfJob& L = A.jobs[(hi - 1) % A.job_cap];
     return L.first + (uint64_t)L.count;
 }
 
 __global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
-    const uint64_t remaining = jobs_total(A) - C.next_sample;
+    const uint32_t job_lo = C.job_lo, job_hi = C.job_hi;
+    const uint64_t remaining = jobs_total(A, job_hi) - C.next_sample;
     const uint32_t n = (uint32_t)min((uint64_t)C.n_free, remaining);
     const uint32_t nfree = C.n_free;
     const uint64_t first = C.next_sample;
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ 
         if (valid) {
             slot = A.q_free[nfree - n + i];
             const uint64_t s = first + i;
-            const uint32_t job = find_job(A.jobs, A.njobs, s);
+            const uint32_t job = find_job(A.jobs, A.job_cap, job_lo, job_hi, s);
             const WfJob& J = A.jobs[job];
             const uint32_t local = (uint32_t)(s - J.first);
             const pt_push& pc = J.pc;
@@ -173,10 +174,14 @@ __global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ 
     }
 }
 
-__global__ void wf_job_setup(const __grid_constant__ WfArgs A, uint32_t j0, uint32_t j1) {
-    const uint32_t j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= j1) return;
-    A.jobs[j].cam = make_camera(A.jobs[j].pc);
+__global__ void wf_job_add(const __grid_constant__ WfArgs A, const WfJob job, uint32_t index, uint32_t lo) {
+    WfJob& J = A.jobs[index % A.job_cap];
+    J = job;
+    J.finished = 0;
+    J.cam = make_camera(job.pc);
+    WfCounters& C = *A.counters;
+    C.job_hi = index + 1;
+    C.job_lo = lo;
 }
 
 __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant__ WfArgs A) {
@@ -483,10 +488,112 @@ __global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant_
     }
 }
 
+
+// Persistent mode: the megakernel's per-thread path loop (one intersect_all
+// call site per iteration for primary and shadow rays alike) over the samples
+// of every pass in the ring.  A lane whose path ends takes the next sample
+// at once, from a chunk its warp claimed with one atomic, so lanes stay busy
+// across pixels, samples and passes; no path state leaves registers.  Each
+// sample's colour goes to its pass's colour buffer, which `resolve` sums in
+// sample order, so results equal the megakernel's bit for bit.  Suited to
+// scenes without SDFs, where lanes of a warp do similar work per ray; SDF
+// marching diverges per lane and belongs to the staged kernels above.
+constexpr uint32_t kPersistChunk = 256;
+
+__global__ void wf_persist_setup(const __grid_constant__ WfArgs A, uint64_t budget) {
+    WfCounters& C = *A.counters;
+    const uint64_t total = jobs_total(A, C.job_hi);
+    const uint64_t begin = C.pk_end;  // warps of the last launch may have claimed past it
+    const uint64_t end = (total - begin > budget) ? begin + budget : total;
+    C.next_sample = begin;
+    C.pk_end = end;
+    C.total = total;
+    C.iterations += 1;
+}
+
+template <int FEAT>
+__global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_constant__ WfArgs A) {
+    WfCounters& C = *A.counters;
+    const uint64_t end = C.pk_end;
+    const uint32_t job_lo = C.job_lo, job_hi = C.job_hi;
+    const int lane = (int)(threadIdx.x & 31);
+    const unsigned lt = (1u << lane) - 1u;
+    uint64_t cbase = 0;   // warp-uniform: unassigned samples of the warp's chunk
+    uint32_t cleft = 0;
+    bool exhausted = false;  // warp-uniform: no sample left below `end`
+    bool active = false, shadow = false;
+    uint32_t job = 0, local = 0;
+    PathState ps;
+    for (;;) {
+        // Refill idle lanes from the warp's chunk, claiming chunks as needed.
+        unsigned need = __ballot_sync(0xffffffffu, !active) ;
+        while (need && !exhausted) {
+            if (cleft == 0) {
+                unsigned long long b = 0;
+                if (lane == 0) b = atomicAdd(reinterpret_cast<unsigned long long*>(&C.next_sample), kPersistChunk);
+                b = __shfl_sync(0xffffffffu, b, 0);
+                if (b >= end) {
+                    exhausted = true;
+                    break;
+                }
+                cbase = b;
+                cleft = (end - b < kPersistChunk) ? (uint32_t)(end - b) : kPersistChunk;
+            }
+            const uint32_t n = min((uint32_t)__popc(need), cleft);
+            const uint32_t rank = (uint32_t)__popc(need & lt);
+            const bool mine = ((need >> lane) & 1u) && rank < n;
+            if (mine) {
+                const uint64_t s = cbase + rank;
+                job = find_job(A.jobs, A.job_cap, job_lo, job_hi, s);
+                const WfJob& J = A.jobs[job];
+                local = (uint32_t)(s - J.first);
+                const pt_push& pc = J.pc;
+                const int W = pc.resolution[0], H = pc.resolution[1];
+                const uint32_t npix = (uint32_t)W * (uint32_t)H;
+                const uint32_t k = local / npix, pix = local % npix;
+                const uint32_t xx = pix % (uint32_t)W, yy = (uint32_t)H - pix / (uint32_t)W;
+                const float uvx = (2.0f * (float)xx - (float)W) / (float)H;
+                const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
+                const CamInfo cam = J.cam;
+                start_sample(ps, pc, cam, xx, yy, uvx, uvy, (int)k);
+                shadow = false;
+                active = true;
+            }
+            cbase += n;
+            cleft -= n;
+            need = __ballot_sync(0xffffffffu, !active);
+        }
+        if (exhausted && __ballot_sync(0xffffffffu, active) == 0) break;
+        bool finished = false;
+        if (active) {
+            const WfJob& J = A.jobs[job];
+            const KScene& S = *J.scene;
+            const int depth = J.pc.pathLength;
+            Hit h;
+            h.hitdist = PT_MAXDIST;
+            h.normal = f3(0.0f, 0.0f, 0.0f);
+            h.materialID = 0.0f;
+            h.lightID = -1.0f;
+            int objectID = -1;
+            intersect_all<FEAT>(S, ps.org, shadow ? ps.shDir : ps.dir, h, objectID);
+            const StepResult r = shadow ? shade_shadow<false>(ps, S, objectID, depth)
+                                        : shade_primary<false>(ps, S, h, objectID, depth);
+            shadow = (r == STEP_SHADOW);
+            if (r == STEP_TERMINATED) {
+                const float3 col = sample_color(ps, J.cie);
+                J.colors[local] = make_float4(col.x, col.y, col.z, 0.0f);
+                finished = true;
+                active = false;
+            }
+        }
+        count_finished(A.jobs, job, finished);
+    }
+}
+
 __global__ void wf_book(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
     const uint32_t pool = A.pool_size;
-    const uint64_t total = jobs_total(A);
+    const uint64_t total = jobs_total(A, C.job_hi);
     const uint32_t n = (uint32_t)min((uint64_t)C.n_free, total - C.next_sample);
     C.total = total;
     C.next_sample += n;
@@ -514,6 +621,8 @@ __global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_fr
         C.total = 0;
         C.iterations = 0;
         C.live = 0;
+        C.job_lo = C.job_hi = 0;
+        C.pk_end = 0;
     }
 }
 
@@ -538,9 +647,9 @@ cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-cudaError_t ptk_wavefront_launch_job_setup(const WfArgs* a, uint32_t j0, uint32_t j1, cudaStream_t stream) {
-    if (j1 <= j0) return cudaSuccess;
-    wf_job_setup<<<(j1 - j0 + 63) / 64, 64, 0, stream>>>(*a, j0, j1);
+cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint32_t index, uint32_t lo,
+                                         cudaStream_t stream) {
+    wf_job_add<<<1, 1, 0, stream>>>(*a, *job, index, lo);
     return cudaGetLastError();
 }
 
@@ -555,6 +664,47 @@ cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid
     wf_gen<<<grid, kStageThreads, 0, stream>>>(*a);
     wf_book<<<1, 1, 0, stream>>>(*a);
     return cudaGetLastError();
+}
+
+cudaError_t ptk_persist_launch(const WfArgs* a, int variant, int sms, uint64_t budget, cudaStream_t stream) {
+    wf_persist_setup<<<1, 1, 0, stream>>>(*a, budget);
+    switch (variant) {
+        case 0: wf_persist<0><<<sms * ptk_persist_blocks_per_sm(0), kPersistThreads, 0, stream>>>(*a); break;
+        case PT_FEAT_BOX:
+            wf_persist<PT_FEAT_BOX><<<sms * ptk_persist_blocks_per_sm(PT_FEAT_BOX), kPersistThreads, 0, stream>>>(*a);
+            break;
+        case PT_FEAT_ANALYTIC:
+            wf_persist<PT_FEAT_ANALYTIC>
+                <<<sms * ptk_persist_blocks_per_sm(PT_FEAT_ANALYTIC), kPersistThreads, 0, stream>>>(*a);
+            break;
+        default:
+            wf_persist<PT_FEAT_ALL><<<sms * ptk_persist_blocks_per_sm(PT_FEAT_ALL), kPersistThreads, 0, stream>>>(*a);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+int ptk_persist_blocks_per_sm(int variant) {
+    static int cache[16] = {0};
+    const int v = variant & 15;
+    if (cache[v]) return cache[v];
+    int n = 0;
+    cudaError_t e;
+    switch (v) {
+        case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<0>, kPersistThreads, 0); break;
+        case PT_FEAT_BOX:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<PT_FEAT_BOX>, kPersistThreads, 0);
+            break;
+        case PT_FEAT_ANALYTIC:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<PT_FEAT_ANALYTIC>, kPersistThreads, 0);
+            break;
+        default:
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<PT_FEAT_ALL>, kPersistThreads, 0);
+            break;
+    }
+    if (e != cudaSuccess || n < 1) n = 1;
+    cache[v] = n;
+    return n;
 }
 
 cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,

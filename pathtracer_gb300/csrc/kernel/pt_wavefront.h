@@ -25,6 +25,9 @@ struct WfPool {
 };
 
 // One render pass of one job: samplesPerFrame samples of every pixel.
+// The table is a ring of job_cap entries: pass number j (counting every pass
+// added since the last reset) lives at jobs[j % job_cap].  Passes [job_lo,
+// job_hi) are live; an entry is reused only after its pass was resolved.
 struct WfJob {
     const KScene* scene;  // device copy of the job's scene
     const float* cie;     // device CIE table
@@ -33,6 +36,7 @@ struct WfJob {
     uint64_t first;       // global index of the pass's first sample
     uint32_t count;       // W*H*spf
     uint32_t finished;    // samples finished (atomic)
+    int32_t variant;      // primitive classes of the scene (PT_FEAT_*), for the persistent kernel
     CamInfo cam;          // camera derived on the device (wf_job_setup)
     pt_push pc;
 };
@@ -48,12 +52,16 @@ struct WfCounters {
     uint64_t total;        // global samples of every pass in the table (written by the bookkeeping kernel)
     uint32_t iterations;
     uint32_t live;         // slots holding a path (pool - n_free)
-    uint32_t pad[4];
+    uint32_t job_lo;       // oldest pass that may still hold unfinished samples
+    uint32_t job_hi;       // passes added so far
+    uint64_t pk_end;       // persistent mode: end of the sample range of the current launch
 };
 
+// Everything here is fixed between resets, so a captured chain of iterations
+// stays valid while passes are added and retired.
 struct WfArgs {
-    WfJob* jobs;   // device job table
-    uint32_t njobs;
+    WfJob* jobs;   // device job table (ring)
+    uint32_t job_cap;
     WfPool pool;
     uint32_t* q_isect[2];
     uint32_t* q_march[2];
@@ -69,10 +77,20 @@ struct WfArgs {
 inline size_t ptk_wavefront_pool_bytes(uint32_t pool) { return (size_t)pool * (14 * 16 + 7 * 4) + 32 * 256; }
 
 cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream);
-// Derives the camera of jobs [j0, j1) on the device.
-cudaError_t ptk_wavefront_launch_job_setup(const WfArgs* a, uint32_t j0, uint32_t j1, cudaStream_t stream);
+// Writes pass number `index` (camera derived on the device) and publishes
+// job_hi = index + 1, job_lo = lo.
+cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint32_t index, uint32_t lo,
+                                         cudaStream_t stream);
 // One iteration: isect, march, shade, gen, bookkeeping (grid = blocks per stage kernel).
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream);
+// Persistent mode: one launch of the persistent path kernel over the next
+// `budget` samples of the job ring, compiled for primitive classes `variant`
+// (PT_FEAT_*: 0, BOX, ANALYTIC or ALL), with every block resident at once
+// on `sms` multiprocessors.
+cudaError_t ptk_persist_launch(const WfArgs* a, int variant, int sms, uint64_t budget, cudaStream_t stream);
+// Blocks of the persistent kernel variant that fit on one SM at once.
+int ptk_persist_blocks_per_sm(int variant);
+constexpr int kPersistThreads = 128;
 // Rendering/Accumulate of one job pass from its ordered sample colours.
 cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,
                                          const float4* colors, cudaStream_t stream);

@@ -17,6 +17,7 @@
 #include "../../include/pt_cuda.h"
 #include "kernel/pt_megakernel.h"
 #include "kernel/pt_wavefront.h"
+#include "kernel/pt_features.h"
 #include "pt_engine.h"
 
 struct pt_ctx {
@@ -382,8 +383,8 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
         ctx->colors_bytes = cbytes;
     }
     WfEngine& E = *ctx->wf;
-    E.stream = ctx->stream;
-    E.args.march_budget = ctx->march_budget;
+    E.set_stream(ctx->stream);
+    E.set_march_budget(ctx->march_budget);
     E.args.trace = ctx->trace;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
     PT_CUDA_TRY(ctx, E.reset());
@@ -394,6 +395,7 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     j.accum = ctx->d_accum;
     j.colors = ctx->d_colors;
     j.pc = *push;
+    j.variant = PT_FEAT_ALL;
     uint32_t idx = 0;
     PT_CUDA_TRY(ctx, E.add_pass(j, &idx));
     // Every iteration moves every live path by one ray; a ray's march spans at

@@ -1,7 +1,10 @@
 // pt_engine.cu — host driver of the wavefront renderer (see pt_engine.h).
 #include "pt_engine.h"
 
+#include "kernel/pt_features.h"
+
 #include <cstring>
+#include <new>
 
 namespace {
 
@@ -66,12 +69,14 @@ static cudaError_t common_setup(WfEngine& e, int device, cudaStream_t stream, ui
     e.max_jobs = max_jobs;
     std::memset(&e.args, 0, sizeof e.args);
     layout(reinterpret_cast<uintptr_t>(e.buffer), pool, max_jobs, &e.args);
+    e.args.job_cap = max_jobs;
     e.args.pool_size = pool;
     e.args.march_budget = march_budget;
     e.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
     int sms = 0;
     EN_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     e.grid = sms * 4;  // 4 blocks of 256 threads per SM (64 registers per thread)
+    e.sms = sms;
     return e.reset();
 }
 
@@ -82,9 +87,10 @@ cudaError_t WfEngine::create(int dev, cudaStream_t s, uint32_t pool_slots, uint3
     owns_buffer = true;
     EN_TRY(cudaMallocHost(&host_counters, sizeof(WfCounters)));
     owns_host_counters = true;
-    // Pinned: each entry is written once and copied to the device asynchronously.
-    EN_TRY(cudaMallocHost(&jobs, sizeof(WfJob) * max_job_count));
+    jobs = new (std::nothrow) WfJob[max_job_count];
+    if (!jobs) return cudaErrorMemoryAllocation;
     owns_jobs = true;
+    use_graph = true;
     return common_setup(*this, dev, s, pool_slots, max_job_count, march_budget);
 }
 
@@ -100,49 +106,103 @@ cudaError_t WfEngine::attach(int dev, cudaStream_t s, uint32_t pool_slots, uint3
     owns_buffer = false;
     host_counters = host_counters_storage;
     owns_host_counters = false;
+    use_graph = false;
     return common_setup(*this, dev, s, pool_slots, max_job_count, march_budget);
 }
 
+void WfEngine::drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+}
+
 void WfEngine::destroy() {
+    drop_graph();
     if (owns_buffer && buffer) cudaFree(buffer);
     if (owns_host_counters && host_counters) cudaFreeHost(host_counters);
-    if (owns_jobs && jobs) cudaFreeHost(jobs);
+    if (owns_jobs && jobs) delete[] jobs;
     buffer = nullptr;
     host_counters = nullptr;
     jobs = nullptr;
     owns_buffer = owns_host_counters = owns_jobs = false;
-    njobs = 0;
+    use_graph = false;
+    njobs = lo = 0;
     total = 0;
 }
 
+void WfEngine::set_march_budget(int budget) {
+    if (budget != args.march_budget) drop_graph();
+    args.march_budget = budget;
+}
+
+void WfEngine::set_stream(cudaStream_t s) { stream = s; }
+
+void WfEngine::set_persistent(bool on) { persistent = on; }
+
 cudaError_t WfEngine::reset() {
-    njobs = 0;
+    njobs = lo = 0;
     total = 0;
-    args.njobs = 0;
+    persist_issued = 0;
     return ptk_wavefront_launch_init(&args, stream);
 }
 
 cudaError_t WfEngine::add_pass(const WfJob& job, uint32_t* index) {
-    if (njobs >= max_jobs) return cudaErrorInvalidValue;
+    if (njobs - lo >= max_jobs) return cudaErrorInvalidValue;
     WfJob j = job;
     j.first = total;
     j.count = (uint32_t)((uint64_t)j.pc.resolution[0] * (uint64_t)j.pc.resolution[1] *
                          (uint64_t)j.pc.samplesPerFrame);
     j.finished = 0;
     std::memset(&j.cam, 0, sizeof j.cam);
-    const uint32_t idx = njobs++;
-    jobs[idx] = j;
+    const uint32_t idx = njobs;
+    // Stream-ordered: kernels launched from now on see job_hi = idx + 1 and
+    // derive the sample total from this entry.
+    EN_TRY(ptk_wavefront_launch_job_add(&args, &j, idx, lo, stream));
+    jobs[idx % max_jobs] = j;
+    njobs = idx + 1;
     total += j.count;
-    // Stream-ordered: the table entry, then its camera.  Kernels launched from
-    // now on see njobs = idx + 1 and derive the sample total from this entry.
-    EN_TRY(cudaMemcpyAsync(args.jobs + idx, &jobs[idx], sizeof(WfJob), cudaMemcpyHostToDevice, stream));
-    args.njobs = idx + 1;
-    EN_TRY(ptk_wavefront_launch_job_setup(&args, idx, idx + 1, stream));
     if (index) *index = idx;
     return cudaSuccess;
 }
 
+void WfEngine::retire(uint32_t new_lo) {
+    if (new_lo > lo && new_lo <= njobs) lo = new_lo;
+}
+
+cudaError_t WfEngine::build_graph() {
+    drop_graph();
+    cudaStream_t cs = nullptr;
+    EN_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    WfArgs a = args;
+    a.trace = KTrace{nullptr, nullptr, nullptr, 0};
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int i = 0; i < graph_chunk && e == cudaSuccess; i++) e = ptk_wavefront_launch_iteration(&a, false, grid, cs);
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) graph = nullptr;
+    return e;
+}
+
 cudaError_t WfEngine::run(int n, bool trace) {
+    if (persistent) {
+        // One kernel variant covering every pass still in the ring.
+        int variant = 0;
+        for (uint32_t j = lo; j < njobs; j++) variant = pt_variant_union(variant, jobs[j % max_jobs].variant);
+        for (int i = 0; i < n && persist_issued < total; i++) {
+            EN_TRY(ptk_persist_launch(&args, variant, sms, persist_budget, stream));
+            persist_issued = (total - persist_issued > persist_budget) ? persist_issued + persist_budget : total;
+        }
+        return cudaSuccess;
+    }
+    if (use_graph && !trace && n >= graph_chunk) {
+        if (!graph) EN_TRY(build_graph());
+        for (; n >= graph_chunk; n -= graph_chunk) EN_TRY(cudaGraphLaunch(graph, stream));
+    }
     for (int i = 0; i < n; i++) EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream));
     return cudaSuccess;
 }
@@ -155,19 +215,34 @@ cudaError_t WfEngine::read_counters(WfCounters* out) {
 }
 
 cudaError_t WfEngine::read_finished(uint32_t j0, uint32_t j1, uint32_t* out) {
-    for (uint32_t j = j0; j < j1; j++)
-        EN_TRY(cudaMemcpyAsync(out + (j - j0), &args.jobs[j].finished, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                               stream));
+    if (j1 < j0 || j1 - j0 > max_jobs) return cudaErrorInvalidValue;
+    // The `finished` fields of a run of ring entries: one strided copy, two
+    // where the run wraps.
+    uint32_t j = j0;
+    while (j < j1) {
+        const uint32_t r = j % max_jobs;
+        const uint32_t n = (j1 - j < max_jobs - r) ? (j1 - j) : (max_jobs - r);
+        EN_TRY(cudaMemcpy2DAsync(out + (j - j0), sizeof(uint32_t), &args.jobs[r].finished, sizeof(WfJob),
+                                 sizeof(uint32_t), n, cudaMemcpyDeviceToHost, stream));
+        j += n;
+    }
     return cudaStreamSynchronize(stream);
 }
 
-cudaError_t WfEngine::resolve(uint32_t j) {
-    if (j >= njobs) return cudaErrorInvalidValue;
-    const WfJob& J = jobs[j];
-    return ptk_wavefront_launch_resolve(&args, j, &J.pc, J.accum, J.colors, stream);
+cudaError_t WfEngine::resolve(uint32_t j, cudaStream_t on) {
+    if (j >= njobs || j < lo) return cudaErrorInvalidValue;
+    const WfJob& J = job(j);
+    return ptk_wavefront_launch_resolve(&args, j % max_jobs, &J.pc, J.accum, J.colors, on ? on : stream);
 }
 
 cudaError_t WfEngine::drain(bool trace, uint64_t max_iterations) {
+    if (persistent) {
+        // Every launch finishes the samples it covers.
+        const uint64_t launches = (total - persist_issued + persist_budget - 1) / persist_budget;
+        if (launches > max_iterations) return cudaErrorTimeout;
+        EN_TRY(run((int)launches, false));
+        return read_counters(host_counters);
+    }
     uint64_t iter = 0;
     int chunk = 8;
     WfCounters c;

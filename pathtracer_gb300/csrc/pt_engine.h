@@ -1,12 +1,16 @@
 // pt_engine.h — host driver of the wavefront renderer.
 //
-// One engine owns a pool of path slots, its ray queues and a table of render
+// One engine owns a pool of path slots, its ray queues and a ring of render
 // passes ("jobs": one scene, one accumulator, samplesPerFrame samples of every
 // pixel).  Passes can be added while others are in flight; every sample of
 // every pass is an independent work item of the same pool, so passes of
 // different scenes, resolutions and sample counts share each launch.  The
-// caller drives iterations and resolves each pass once all of its samples
-// have finished.
+// caller drives iterations, resolves each pass once all of its samples have
+// finished, and retires resolved passes so their ring entries can be reused.
+//
+// The kernels' arguments do not change between resets (pass bounds live in
+// device counters), so a chain of iterations is captured once as a CUDA graph
+// and replayed: one launch per chunk instead of five per iteration.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -19,11 +23,12 @@ struct WfEngine {
     int device = 0;
     cudaStream_t stream = nullptr;
     uint32_t pool = 0;
-    uint32_t max_jobs = 0;
+    uint32_t max_jobs = 0;    // ring entries
     int grid = 0;
     WfArgs args{};
-    WfJob* jobs = nullptr;    // host mirror of the job table (max_jobs entries)
-    uint32_t njobs = 0;
+    WfJob* jobs = nullptr;    // host mirror of the ring (max_jobs entries)
+    uint32_t njobs = 0;       // passes added since the last reset (job_hi)
+    uint32_t lo = 0;          // passes below this were resolved and retired
     bool owns_jobs = false;
     uint64_t total = 0;       // samples of all passes added
     void* buffer = nullptr;   // device memory of pool, queues, counters and job table
@@ -31,30 +36,62 @@ struct WfEngine {
     size_t buffer_bytes = 0;
     WfCounters* host_counters = nullptr;  // read-back target (pinned when the engine allocated it)
     bool owns_host_counters = false;
+    // Graph replay of `graph_chunk` iterations (engines that allocate only).
+    bool use_graph = false;
+    int graph_chunk = 8;
+    cudaGraphExec_t graph = nullptr;
+    // Persistent mode: each iteration is one launch of the persistent path
+    // kernel over the next `persist_budget` samples instead of one pass of
+    // the staged kernels; the pool is not used.
+    bool persistent = false;
+    int sms = 0;
+    uint64_t persist_budget = 1ull << 23;
+    uint64_t persist_issued = 0;  // samples covered by launches so far
 
-    // Bytes of device memory for `pool` slots and `max_jobs` passes.
+    // Bytes of device memory for `pool` slots and `max_jobs` ring entries.
     static size_t bytes_for(uint32_t pool, uint32_t max_jobs);
     // Allocates its own memory.
     cudaError_t create(int device, cudaStream_t stream, uint32_t pool, uint32_t max_jobs, int march_budget);
     // Uses caller-provided device memory (bytes_for) and host storage for the
-    // counters and the job table (max_jobs entries); allocates nothing.
+    // counters and the job ring (max_jobs entries); allocates nothing and
+    // launches kernels one by one.
     cudaError_t attach(int device, cudaStream_t stream, uint32_t pool, uint32_t max_jobs, int march_budget,
                        void* device_buffer, size_t bytes, WfCounters* host_counters_storage, WfJob* host_jobs);
     void destroy();
 
-    // Empties the pool and the job table (asynchronous, stream-ordered).
+    // Empties the pool and the job ring (asynchronous, stream-ordered).
     cudaError_t reset();
-    // Appends a pass; `job` is filled by the caller except first/count/finished/cam.
+    // Sphere-tracing iterations per ray per march launch.
+    void set_march_budget(int budget);
+    // Staged kernels (false) or the persistent path kernel (true).
+    void set_persistent(bool on);
+    // Persistent mode: every sample added so far is covered by a launch.
+    bool persistent_idle() const { return persist_issued >= total; }
+    // Stream the kernels are launched on.
+    void set_stream(cudaStream_t s);
+    // Appends a pass; `job` is filled by the caller except first/count/finished/cam
+    // (job.variant: the scene's primitive classes, PT_FEAT_ALL when unknown).
+    // Fails with cudaErrorInvalidValue while the ring is full.
     cudaError_t add_pass(const WfJob& job, uint32_t* index);
+    // Passes [lo, new_lo) were resolved: their ring entries may be reused.
+    void retire(uint32_t new_lo);
     // Launches `n` iterations.
     cudaError_t run(int n, bool trace);
     // Reads the counters (synchronises the stream).
     cudaError_t read_counters(WfCounters* out);
-    // Reads the finished-sample counts of passes [j0, j1) (synchronises the stream).
+    // Reads the finished-sample counts of passes [j0, j1) (at most max_jobs;
+    // synchronises the stream).
     cudaError_t read_finished(uint32_t j0, uint32_t j1, uint32_t* out);
-    // Rendering/Accumulate of pass `j` into its accumulator.
-    cudaError_t resolve(uint32_t j);
+    // Rendering/Accumulate of pass `j` into its accumulator (on `on`, or the
+    // engine's stream).
+    cudaError_t resolve(uint32_t j, cudaStream_t on = nullptr);
+    // Host copy of pass j (valid until its ring entry is reused).
+    const WfJob& job(uint32_t j) const { return jobs[j % max_jobs]; }
     // Runs until every pass added so far has finished (polling between chunks of
     // iterations), or `max_iterations` have run (returns cudaErrorTimeout then).
     cudaError_t drain(bool trace, uint64_t max_iterations);
+
+   private:
+    void drop_graph();
+    cudaError_t build_graph();
 };

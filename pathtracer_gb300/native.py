@@ -23,10 +23,21 @@ PT_ERR_NO_SCENE = 5
 PT_ERR_OOM = 6
 PT_ERR_KERNEL = 7
 PT_ERR_TOO_LARGE = 8
+PT_ERR_BUSY = 9
 PT_NOALLOC_MAX_SAMPLES = 1 << 20
 
 PT_ENGINE_MEGAKERNEL = 0
 PT_ENGINE_WAVEFRONT = 1
+
+PT_TARGET_FLOAT = 0
+PT_TARGET_FP64 = 1
+
+PT_BATCH_ROUTE_AUTO = 0
+PT_BATCH_ROUTE_STAGED = 1
+PT_BATCH_ROUTE_PERSISTENT = 2
+
+PT_GEN_SPHERES = 0
+PT_GEN_SDF = 1
 
 UBO_FLOATS = 4097  # 7 + 1024 + 768 + 783 + 128 + 64 + 1323
 UBO_OFFSETS = {
@@ -119,6 +130,34 @@ class PtOffscreenOpts(ctypes.Structure):
     ]
 
 
+class PtBatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("samples_done", ctypes.c_uint64),
+        ("samples_added", ctypes.c_uint64),
+        ("iterations", ctypes.c_uint64),
+        ("passes_added", ctypes.c_uint32),
+        ("passes_pending", ctypes.c_uint32),
+        ("pool_slots", ctypes.c_uint32),
+        ("pass_slots", ctypes.c_uint32),
+        ("passes_staged", ctypes.c_uint32),
+        ("passes_persistent", ctypes.c_uint32),
+    ]
+
+
+class PtJobSpec(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("width", ctypes.c_int32),
+        ("height", ctypes.c_int32),
+        ("spp", ctypes.c_int32),
+        ("pathLength", ctypes.c_int32),
+        ("sdf_kind", ctypes.c_int32),
+        ("objects", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
 assert ctypes.sizeof(PtPush) == 88
 assert ctypes.sizeof(PtSdfPlugin) == 20
 
@@ -152,6 +191,25 @@ CUDA_API = [
     ("pt_last_iterations", ctypes.c_uint32, [_vp]),
     ("pt_set_march_budget", _i, [_vp, _i]),
     ("pt_dispatch_noalloc", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(PtPush), _vp, _vp]),
+    ("pt_batch_create", _i, [ctypes.POINTER(_vp), _i, ctypes.c_uint32, ctypes.c_uint32]),
+    ("pt_batch_destroy", _i, [_vp]),
+    ("pt_batch_last_error", ctypes.c_char_p, [_vp]),
+    ("pt_batch_stream", _vp, [_vp]),
+    ("pt_batch_set_march_budget", _i, [_vp, _i]),
+    ("pt_batch_set_route", _i, [_vp, _i]),
+    ("pt_batch_add_scene", _i, [_vp, _vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
+    ("pt_batch_add_target", _i, [_vp, _i, _i, _i, ctypes.POINTER(_i)]),
+    ("pt_batch_target_device_ptr", _vp, [_vp, _i]),
+    ("pt_batch_add_pass", _i, [_vp, _i, _i, ctypes.POINTER(PtPush), ctypes.POINTER(_i)]),
+    ("pt_batch_step", _i, [_vp, _i, ctypes.POINTER(_i), _i, ctypes.POINTER(_i)]),
+    ("pt_batch_pending", _i, [_vp]),
+    ("pt_batch_run", _i, [_vp, ctypes.c_uint64]),
+    ("pt_batch_stats", _i, [_vp, ctypes.POINTER(PtBatchInfo)]),
+    ("pt_batch_target_samples", _i, [_vp, _i, ctypes.POINTER(ctypes.c_uint64)]),
+    ("pt_batch_read_target", _i, [_vp, _i, _vp, _sz]),
+    ("pt_batch_rmse", _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_double)]),
+    ("pt_batch_release_target", _i, [_vp, _i]),
+    ("pt_batch_release_scene", _i, [_vp, _i]),
 ]
 
 # Every symbol include/pt_host.h declares.
@@ -170,6 +228,8 @@ HOST_API = [
     ("pt_export_rgb8", _i, [_vp, _i, _i, _i, _vp]),
     ("pt_save_ppm", _i, [ctypes.c_char_p, _vp, _i, _i]),
     ("pt_cie_analytic_table", None, [_vp]),
+    ("pt_scene_sdf_plugins", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
+    ("pt_scene_generate", _i, [_i, ctypes.c_uint64, ctypes.POINTER(_vp), ctypes.POINTER(PtJobSpec)]),
 ]
 
 _cache: dict[str, ctypes.CDLL] = {}

@@ -53,6 +53,16 @@ class Scene:
         with open(path, "rb") as f:
             return cls.parse(f.read())
 
+    @classmethod
+    def generate(cls, kind: int, seed: int) -> tuple["Scene", native.PtJobSpec]:
+        """A seeded synthetic job (pt_scene_generate): the scene and its spec."""
+        h = ctypes.c_void_p()
+        spec = native.PtJobSpec()
+        rc = native.host().pt_scene_generate(kind, ctypes.c_uint64(seed), ctypes.byref(h), ctypes.byref(spec))
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, "pt_scene_generate failed")
+        return cls(h.value), spec
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:
@@ -90,6 +100,15 @@ class Scene:
     def sdf_sources(self) -> list[str]:
         n = self.counts()["sdfs"]
         return [self._lib.pt_scene_sdf_source(self._h, i).decode() for i in range(n)]
+
+    def sdf_plugins(self) -> list:
+        n = self.counts()["sdfs"]
+        arr = (native.PtSdfPlugin * max(1, n))()
+        cnt = ctypes.c_int()
+        rc = self._lib.pt_scene_sdf_plugins(self._h, arr, n, ctypes.byref(cnt))
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, "an SDF source is not a recognised plug-in")
+        return list(arr[:n])
 
     def to_json(self) -> str:
         need = ctypes.c_size_t()
@@ -199,6 +218,111 @@ class Context:
     def set_trace(self, events_ptr: int, nevents_ptr: int, colors_ptr: int, depth_cap: int):
         self._check(self._lib.pt_set_trace(self._h, events_ptr or None, nevents_ptr or None, colors_ptr or None,
                                            depth_cap))
+
+
+class Batch:
+    """pt_batch: many scenes, targets and passes in one wavefront pool."""
+
+    def __init__(self, device: int = 0, pool_slots: int = 1 << 21, max_passes: int = 4096):
+        self._lib = native.cuda()
+        h = ctypes.c_void_p()
+        rc = self._lib.pt_batch_create(ctypes.byref(h), device, pool_slots, max_passes)
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, f"pt_batch_create(device={device}) failed")
+        self._h = h
+        self._sizes: dict[int, tuple[int, int]] = {}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.pt_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def _check(self, rc: int):
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, self._lib.pt_batch_last_error(self._h).decode())
+
+    def stream(self) -> int:
+        return self._lib.pt_batch_stream(self._h) or 0
+
+    def set_march_budget(self, steps: int):
+        self._check(self._lib.pt_batch_set_march_budget(self._h, steps))
+
+    def set_route(self, route: int):
+        self._check(self._lib.pt_batch_set_route(self._h, route))
+
+    def add_scene(self, ubo: np.ndarray, plugins: list) -> int:
+        ubo = np.ascontiguousarray(ubo, np.float32)
+        assert ubo.size == native.UBO_FLOATS
+        arr = (native.PtSdfPlugin * max(1, len(plugins)))(*plugins)
+        out = ctypes.c_int()
+        self._check(self._lib.pt_batch_add_scene(self._h, native.ptr(ubo), arr, len(plugins), ctypes.byref(out)))
+        return out.value
+
+    def add_target(self, width: int, height: int, kind: int = native.PT_TARGET_FLOAT) -> int:
+        out = ctypes.c_int()
+        self._check(self._lib.pt_batch_add_target(self._h, width, height, kind, ctypes.byref(out)))
+        self._sizes[out.value] = (width, height)
+        return out.value
+
+    def add_pass(self, scene: int, target: int, push: PtPush) -> int:
+        out = ctypes.c_int()
+        self._check(self._lib.pt_batch_add_pass(self._h, scene, target, ctypes.byref(push), ctypes.byref(out)))
+        return out.value
+
+    def step(self, iterations: int, capacity: int = 4096) -> list[int]:
+        ids = (ctypes.c_int * max(1, capacity))()
+        n = ctypes.c_int()
+        self._check(self._lib.pt_batch_step(self._h, iterations, ids, capacity, ctypes.byref(n)))
+        return list(ids[: n.value])
+
+    def pending(self) -> int:
+        return self._lib.pt_batch_pending(self._h)
+
+    def run(self, max_iterations: int = 1 << 40):
+        self._check(self._lib.pt_batch_run(self._h, ctypes.c_uint64(max_iterations)))
+
+    def stats(self) -> dict:
+        info = native.PtBatchInfo()
+        self._check(self._lib.pt_batch_stats(self._h, ctypes.byref(info)))
+        return {k: getattr(info, k) for k, _ in native.PtBatchInfo._fields_}
+
+    def target_samples(self, target: int) -> int:
+        out = ctypes.c_uint64()
+        self._check(self._lib.pt_batch_target_samples(self._h, target, ctypes.byref(out)))
+        return out.value
+
+    def read_target(self, target: int) -> np.ndarray:
+        w, h = self._sizes[target]
+        out = np.empty((h, w, 4), np.float32)
+        self._check(self._lib.pt_batch_read_target(self._h, target, native.ptr(out), out.nbytes))
+        return out
+
+    def target_device_ptr(self, target: int) -> int:
+        return self._lib.pt_batch_target_device_ptr(self._h, target) or 0
+
+    def rmse(self, target: int, reference: int) -> float:
+        out = ctypes.c_double()
+        self._check(self._lib.pt_batch_rmse(self._h, target, reference, ctypes.byref(out)))
+        return out.value
+
+    def release_target(self, target: int):
+        self._check(self._lib.pt_batch_release_target(self._h, target))
+
+    def release_scene(self, scene: int):
+        self._check(self._lib.pt_batch_release_scene(self._h, scene))
 
 
 def render_offscreen(ctx: Context, scene: Scene, cie: np.ndarray, width: int, height: int, num_samples: int,

@@ -219,3 +219,34 @@ def test_wavefront_small_pool_recycles_slots(rt):
     _check(compare.compare(acc_o, tr_o, acc_g, tr_g, spf))
     assert ctx.last_iterations() > 10
     ctx.close()
+
+
+@pytest.mark.parametrize("kind,seed", [(0, 4), (0, 9), (1, 2)])
+def test_untraced_variants_match_oracle(rt, kind, seed):
+    """Generated scenes through the specialised (untraced) kernel variants —
+    the megakernel and the batch's persistent kernel — against the oracle:
+    per-pixel XYZ identical."""
+    from oracle import compare
+    from pathtracer_gb300 import Batch, native
+
+    scene, spec = rt["Scene"].generate(kind, seed)
+    W, H, spf = 40, 32, 3
+    push = scene.push_constants(W, H, spf, spf, spf, spec.pathLength)
+    ubo = scene.pack_ubo(rt["cie"])
+    acc_o, _ = compare.run_oracle(ubo, push, compare.plugins_for(scene))
+    with rt["Context"](0) as ctx:
+        ctx.set_engine(native.PT_ENGINE_MEGAKERNEL)
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        ctx.dispatch(push)
+        ctx.wait()
+        acc_m = ctx.read_accum()
+    with Batch(0, pool_slots=1 << 12, max_passes=4) as b:
+        b.set_route(native.PT_BATCH_ROUTE_PERSISTENT)
+        sid = b.add_scene(ubo, scene.sdf_plugins())
+        tid = b.add_target(W, H)
+        b.add_pass(sid, tid, push)
+        b.run()
+        acc_p = b.read_target(tid)
+    np.testing.assert_array_equal(acc_m[..., :3], acc_o[..., :3])
+    np.testing.assert_array_equal(acc_p[..., :3], acc_o[..., :3])
