@@ -11,6 +11,7 @@ dispatches, and the read-back of the 16 MiB accumulator each step.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
   python bench.py --workload batch64 [--steps K] [--warmup W]
+  python bench.py --workload serve [--rate R] [--duration T]
 
 --workload batch64 is the mixed-job batch: 64 seeded sphere-scene jobs
 (pt_scene_generate, seeds 0-63: 128^2-1024^2, 4-256 spp, depth 8; 1.80 G
@@ -18,6 +19,14 @@ path samples) rendered as one batch through pt_batch (one pass per job, all
 in one wavefront pool), against the same 64 jobs dispatched one after
 another through the plain megakernel on one stream.  Both render the same
 samples, so the images are bit-identical (checked) and the RMSE is equal.
+
+--workload serve replays a Poisson request stream (70% sphere jobs, 30% SDF
+jobs, from a pool of resident scenes with FP64 references) through
+pt_server: each job is refined in 8-spp passes until its relative RMSE is at
+most the target (or the sample cap), batched (continuous batching under an
+HBM budget) and then plain (one job at a time through the megakernel), on
+the same trace.  Both arms render the same passes of every job, so each
+job's error is identical between them.
 
 Under torchrun each rank renders its own replica (distinct sample indices,
 no exchange): weak scaling.  --impl reference times the CPU restatement of
@@ -61,7 +70,15 @@ def parse_args():
     ap.add_argument("--compare-engines", type=int, default=1, help="also time the other engine (1 step)")
     ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0: library default)")
     ap.add_argument("--budget", type=int, default=0, help="wavefront march steps per launch (0: default)")
-    ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64"])
+    ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64", "serve"])
+    ap.add_argument("--rate", type=float, default=2.0, help="serve: Poisson arrivals per second")
+    ap.add_argument("--duration", type=float, default=30.0, help="serve: seconds of arrivals")
+    ap.add_argument("--target-rmse", type=float, default=0.02, help="serve: relative RMSE target per job")
+    ap.add_argument("--max-spp", type=int, default=512, help="serve: sample cap per job")
+    ap.add_argument("--ref-spp", type=int, default=1024, help="serve: FP64 reference samples per pixel")
+    ap.add_argument("--pool-scenes", type=int, default=16, help="serve: scenes in the request pool")
+    ap.add_argument("--burst", type=int, default=0,
+                    help="serve: N requests all arriving at t=0 instead of the Poisson stream (saturates both arms)")
     ap.add_argument("--jobs", type=int, default=64, help="batch64: jobs per batch")
     ap.add_argument("--route", default="auto", choices=["auto", "staged", "persistent"],
                     help="batch64: engine route of the passes")
@@ -394,6 +411,107 @@ def run_batch(args, rank, world):
     return 0
 
 
+SERVE_WORKLOAD = "serve_poisson_70pct_spheres_30pct_sdf_rmse2pct_8spp_passes"
+
+
+def run_serve(args, rank, world):
+    """Poisson request stream through pt_server, batched vs plain."""
+    import torch
+
+    from pathtracer_gb300 import Scene, Server, build, cie_analytic, native
+
+    build.build()
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
+    local = torch.cuda.current_device()
+    cie = cie_analytic()
+    n_sdf = max(1, round(0.3 * args.pool_scenes))
+    n_sph = args.pool_scenes - n_sdf
+    pool = []
+    for k in range(args.pool_scenes):
+        kind, seed = (native.PT_GEN_SPHERES, 1000 + k) if k < n_sph else (native.PT_GEN_SDF, 2000 + k)
+        sc, spec = Scene.generate(kind, seed + 100000 * rank)
+        push = sc.push_constants(spec.width, spec.height, 1, 1, 1, spec.pathLength)
+        pool.append((kind, sc, spec, push))
+    srv = Server(local, mode=native.PT_SERVE_BATCHED, spp_per_pass=8, hbm_budget=64 << 30,
+                 pool_slots=args.pool or (1 << 21), iterations_per_poll=4)
+    t0 = time.perf_counter()
+    for key, (kind, sc, spec, push) in enumerate(pool):
+        srv.add_scene(key, sc.pack_ubo(cie), sc.sdf_plugins())
+        srv.render_reference(key, push, args.ref_spp, 32)
+    ref_secs = time.perf_counter() - t0
+
+    rng = np.random.default_rng(7 + rank)
+    arrivals, reqs = [], []
+    t = 0.0 if args.burst else rng.exponential(1.0 / args.rate)
+    while (len(reqs) < args.burst) if args.burst else (t < args.duration):
+        key = int(rng.integers(0, n_sph)) if rng.random() < 0.7 else n_sph + int(rng.integers(0, n_sdf))
+        reqs.append(Server.job(key, pool[key][3], args.max_spp, args.target_rmse))
+        arrivals.append(float(t))
+        if not args.burst:
+            t += rng.exponential(1.0 / args.rate)
+
+    def arm(mode):
+        srv.set_mode(mode)
+        with ClockSampler(local) as clk:
+            res = srv.run_trace(reqs, arrivals)
+        lat = [r.t_done - r.t_submit for r in res]
+        samples = sum(r.samples for r in res)
+        makespan = max(r.t_done for r in res) - min(arrivals)
+        return res, {"jobs": len(res), "samples": samples, "makespan_s": makespan,
+                     "path_samples_per_s": samples / makespan,
+                     "time_to_target_s": {"p50": pctl(lat, 50), "p99": pctl(lat, 99), "mean": statistics.mean(lat)},
+                     "queue_wait_s": {"p50": pctl([r.t_admit - r.t_submit for r in res], 50),
+                                      "p99": pctl([r.t_admit - r.t_submit for r in res], 99)},
+                     "clocks": clk.summary()}
+
+    res_b, batched = arm(native.PT_SERVE_BATCHED)
+    st = srv.stats()
+    res_p, plain = arm(native.PT_SERVE_PLAIN)
+    identical = all((a.spp, a.rmse) == (b.spp, b.rmse) for a, b in zip(res_b, res_p))
+    reached = sum(1 for r in res_b if r.rmse <= args.target_rmse) / max(1, len(res_b))
+    per_job = [r.samples for r in res_b]
+    srv.close()
+
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([batched["makespan_s"]], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    value = batched["path_samples_per_s"] * world
+    span = args.duration if not args.burst else None
+    offered = sum(per_job) / span if span else None
+    mean_job = sum(per_job) / max(1, len(per_job))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
+        "ms_per_step": 1000.0 * batched["makespan_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, Poisson arrivals)",
+        "config": {"workload": SERVE_WORKLOAD + ("_burst" if args.burst else ""),
+                   "rate_jobs_per_s": None if args.burst else args.rate,
+                   "duration_s": None if args.burst else args.duration, "burst_jobs": args.burst or None,
+                   "target_rmse": args.target_rmse, "max_spp": args.max_spp, "spp_per_pass": 8,
+                   "reference_spp": args.ref_spp, "pool_scenes": args.pool_scenes,
+                   "parallelism": f"replicas x{world}", "hbm_budget_gib": 64},
+        "serve": {"batched": batched, "plain_megakernel_serial": plain,
+                  "throughput_speedup_vs_plain": batched["path_samples_per_s"] / plain["path_samples_per_s"],
+                  "p50_speedup_vs_plain": plain["time_to_target_s"]["p50"] / batched["time_to_target_s"]["p50"],
+                  "p99_speedup_vs_plain": plain["time_to_target_s"]["p99"] / batched["time_to_target_s"]["p99"],
+                  "rmse_identical_per_job": identical, "reached_target_fraction": reached,
+                  "offered_samples_per_s": offered, "mean_samples_per_job": mean_job,
+                  "offered_at_200_jobs_per_s": mean_job * 200.0,
+                  "saturates_at_200_jobs_per_s": mean_job * 200.0 > batched["path_samples_per_s"],
+                  "reference_render_s": ref_secs, "hbm_peak_bytes": st["bytes_peak"],
+                  "resident_bytes": st["resident_bytes"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "requests carry no host buffers; scenes are resident"},
+        "gpu_launches": None,
+        "roofline": None,
+        "clocks": batched["clocks"],
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     faulthandler.enable()
     args = parse_args()
@@ -407,8 +525,8 @@ def main():
 
             torch.cuda.set_device(local)
         dist.init_process_group(backend=backend)
-    if args.workload == "batch64":
-        rc = run_batch(args, rank, world)
+    if args.workload in ("batch64", "serve"):
+        rc = run_batch(args, rank, world) if args.workload == "batch64" else run_serve(args, rank, world)
         if world > 1:
             import torch.distributed as dist
 

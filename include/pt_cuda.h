@@ -311,6 +311,12 @@ int pt_batch_read_target(pt_batch* batch, int target_id, float* host, size_t byt
  * against a reference target r of the same size, reduced on the device in
  * double precision. */
 int pt_batch_rmse(pt_batch* batch, int target_id, int reference_id, double* rel_rmse);
+/* The same for n (target, reference) pairs in one launch and one copy back. */
+int pt_batch_rmse_many(pt_batch* batch, const int* target_ids, const int* reference_ids, int n, double* rel_rmse);
+/* The same for a caller's device image (W*H float4, e.g. a context's
+ * accumulator, complete before the call) against a reference target. */
+int pt_batch_rmse_image(pt_batch* batch, const void* d_image, int width, int height, int reference_id,
+                        double* rel_rmse);
 /* PT_ERR_BUSY while passes of the target / scene are in flight. */
 int pt_batch_release_target(pt_batch* batch, int target_id);
 int pt_batch_release_scene(pt_batch* batch, int scene_id);

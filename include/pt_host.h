@@ -127,6 +127,95 @@ int pt_save_ppm(const char* path, const uint8_t* rgb, int width, int height);
  * x y z interleaved: a caller-supplied table for pt_ubo.CIEXYZ1931. */
 void pt_cie_analytic_table(float out[PT_CIE_TABLE_SIZE]);
 
+/* ---------------------------------------------------------------------------
+ * Render serving.  No counterpart in the reference, whose host renders one
+ * scene at a time: requests name a resident scene and a target error; each
+ * admitted job is refined with progressive passes of spp_per_pass samples
+ * (pass k: frame = currentSamples = k * spp_per_pass, the reference's
+ * offscreen loop) until its relative RMSE (pt_batch_rmse) against the scene's
+ * FP64 reference is at most target_rmse, or max_spp is reached.
+ *   PT_SERVE_BATCHED  continuous batching on a pt_batch: requests are
+ *                     admitted in arrival order while their accumulator and
+ *                     in-flight sample colours fit hbm_budget; the passes of
+ *                     all admitted jobs share every launch.
+ *   PT_SERVE_PLAIN    one job at a time through pt_dispatch on the plain
+ *                     megakernel (the drop-in path), for comparison.
+ * A job's image after k passes is the same bits in both modes, alone or in
+ * any mix.  Times are seconds on the server's monotonic clock.
+ * ------------------------------------------------------------------------- */
+typedef struct pt_server pt_server;
+
+#define PT_SERVE_BATCHED 0
+#define PT_SERVE_PLAIN 1
+
+typedef struct pt_server_opts {
+    int32_t mode;                /* PT_SERVE_* */
+    int32_t spp_per_pass;        /* default 8 */
+    uint64_t hbm_budget;         /* bytes for admitted jobs (default 64 GiB) */
+    uint32_t pool_slots;         /* staged-engine path slots (default 2^21) */
+    uint32_t max_passes;         /* passes in flight per engine (default 4096) */
+    int32_t iterations_per_poll; /* engine iterations per pt_server_poll (default 4) */
+    int32_t passes_in_flight;    /* per job (default 1) */
+    int32_t keep_images;         /* keep finished images until pt_server_release */
+    int32_t pad;
+} pt_server_opts;
+
+typedef struct pt_server_job {
+    int32_t scene_key;
+    int32_t max_spp;     /* sample cap per pixel */
+    double target_rmse;  /* stop at this relative RMSE vs the reference (0: run to max_spp) */
+    pt_push push;        /* resolution, camera, pathLength; frame/currentSamples/samplesPerFrame set per pass */
+} pt_server_job;
+
+typedef struct pt_server_result {
+    uint64_t job_id;
+    int32_t status;
+    int32_t spp;       /* samples per pixel rendered */
+    double rmse;       /* at completion; -1 without a reference */
+    double t_submit;   /* arrival */
+    double t_admit;
+    double t_done;     /* time to target = t_done - t_submit */
+    uint64_t samples;  /* path samples rendered for the job */
+} pt_server_result;
+
+typedef struct pt_server_stats {
+    uint64_t submitted, admitted, completed;
+    uint64_t samples;
+    uint64_t bytes_in_use, bytes_peak; /* admitted jobs, against hbm_budget */
+    uint64_t resident_bytes;           /* FP64 references and scene copies */
+    uint32_t queued, active;
+} pt_server_stats;
+
+int pt_server_create(pt_server** out, int device, const pt_server_opts* opts);
+int pt_server_destroy(pt_server* server);
+const char* pt_server_last_error(pt_server* server);
+double pt_server_now(pt_server* server);
+/* Switches between PT_SERVE_BATCHED and PT_SERVE_PLAIN while no job is
+ * queued or running; scenes and references stay resident. */
+int pt_server_set_mode(pt_server* server, int mode);
+/* The batch the server renders with (scenes, references, statistics). */
+pt_batch* pt_server_batch(pt_server* server);
+/* Makes a scene resident under `key`. */
+int pt_server_add_scene(pt_server* server, int key, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins);
+/* Renders scene `key`'s FP64 reference for a view (push: resolution, camera,
+ * path length) with spp samples per pixel from sample indices no request
+ * uses; blocks until done. */
+int pt_server_render_reference(pt_server* server, int key, const pt_push* push, int spp, int spp_per_pass);
+int pt_server_submit(pt_server* server, const pt_server_job* job, uint64_t* job_id);
+/* Admits, feeds and advances the work once; returns jobs finished since the
+ * last call (up to capacity; the rest on later calls). */
+int pt_server_poll(pt_server* server, pt_server_result* done, int capacity, int* ndone);
+/* Jobs queued, active or finished but not yet returned by pt_server_poll. */
+int pt_server_pending(pt_server* server);
+int pt_server_read_image(pt_server* server, uint64_t job_id, float* host, size_t bytes);
+int pt_server_release(pt_server* server, uint64_t job_id);
+int pt_server_get_stats(pt_server* server, pt_server_stats* out);
+/* Replays an arrival trace: request i is submitted `arrivals[i]` seconds
+ * (non-decreasing) after the call and results[i] receives its outcome, with
+ * times relative to the call.  Returns when every request has finished. */
+int pt_server_run_trace(pt_server* server, const pt_server_job* jobs, const double* arrivals, int n,
+                        pt_server_result* results);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,6 +6,7 @@ and libpt_host.so (headless scene/packing/offscreen host, include/pt_host.h).
 This package builds them in-tree (``build.build()``) and binds them with
 ctypes (``native``, ``renderer``).
 """
-from .renderer import Batch, Context, PathTracerError, Scene, cie_analytic, export_rgb8, render_offscreen  # noqa: F401
+from .renderer import (  # noqa: F401
+    Batch, Context, PathTracerError, Scene, Server, cie_analytic, export_rgb8, render_offscreen)
 
 SCENES_DIR = __import__("os").path.join(__import__("os").path.dirname(__file__), "scenes")

@@ -20,7 +20,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "lib")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC"]
+NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-Wall"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", "-Wextra"]
 
 CUDA_SOURCES = [
@@ -37,6 +37,7 @@ HOST_SOURCES = [
     "host/pt_scene.cpp",
     "host/pt_offscreen.cpp",
     "host/pt_generate.cpp",
+    "host/pt_server.cpp",
 ]
 
 

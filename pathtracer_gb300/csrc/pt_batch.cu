@@ -55,6 +55,14 @@ struct BatchTarget {
     uint64_t samples = 0;  // resolved samples per pixel
 };
 
+struct RmseItem {
+    const float4* a;         // image
+    const float4* ref;       // float reference, or
+    const double* ref_sum;   // FP64 sums (x, y, z, samples) per pixel
+    uint32_t n;              // pixels
+    uint32_t pad;
+};
+
 struct BatchPass {
     int scene = -1, target = -1;
     int engine = 0;     // kStaged or kPersistent
@@ -91,8 +99,13 @@ struct pt_batch {
     uint64_t samples_done = 0;
     uint64_t iterations = 0;
     uint32_t* h_finished = nullptr;  // pinned, max_passes entries
-    double* d_rmse = nullptr;        // sum of squared differences, sum of squares
-    double* h_rmse = nullptr;        // pinned
+    // RMSE reductions: per item, sum of squared differences and sum of squares.
+    int rmse_cap = 0;
+    struct RmseItem* h_items = nullptr;  // pinned
+    struct RmseItem* d_items = nullptr;
+    double2* d_partial = nullptr;  // kRmseBlocks per item
+    double2* d_rmse = nullptr;
+    double2* h_rmse = nullptr;     // pinned
     std::vector<char> blocked;       // per target, scratch of pt_batch_step
     std::string err;
 };
@@ -173,23 +186,28 @@ __global__ void fp64_to_float_kernel(const double* __restrict__ sum, uint32_t np
     out[pix] = make_float4((float)(s[0] * inv), (float)(s[1] * inv), (float)(s[2] * inv), 1.0f);
 }
 
-// Sums of squared differences and squared reference values over the XYZ
-// channels of an image against a reference given as floats (ref) or as FP64
-// sums (ref_sum, divided by their sample count).
-__global__ void rmse_kernel(const float4* __restrict__ a, const float4* __restrict__ ref,
-                            const double* __restrict__ ref_sum, uint32_t n, double* __restrict__ out) {
+// Per item (blockIdx.y): sums of squared differences and squared reference
+// values over the XYZ channels of an image against a reference given as
+// floats or as FP64 sums (divided by their sample count).  Each block writes
+// its partial sums; rmse_final adds them in a fixed order, so the result is
+// the same bits on every run.
+constexpr int kRmseBlocks = 64, kRmseThreads = 256;
+
+__global__ void __launch_bounds__(kRmseThreads) rmse_partial(const RmseItem* __restrict__ items,
+                                                             double2* __restrict__ partial) {
+    const RmseItem it = items[blockIdx.y];
     double d2 = 0.0, r2 = 0.0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 x = a[i];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < it.n; i += gridDim.x * blockDim.x) {
+        const float4 x = it.a[i];
         double rx, ry, rz;
-        if (ref_sum) {
-            const double* s = ref_sum + 4 * (size_t)i;
+        if (it.ref_sum) {
+            const double* s = it.ref_sum + 4 * (size_t)i;
             const double inv = s[3] > 0.0 ? 1.0 / s[3] : 0.0;
             rx = s[0] * inv;
             ry = s[1] * inv;
             rz = s[2] * inv;
         } else {
-            const float4 r = ref[i];
+            const float4 r = it.ref[i];
             rx = r.x;
             ry = r.y;
             rz = r.z;
@@ -202,15 +220,85 @@ __global__ void rmse_kernel(const float4* __restrict__ a, const float4* __restri
         d2 += __shfl_down_sync(0xffffffffu, d2, o);
         r2 += __shfl_down_sync(0xffffffffu, r2, o);
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&out[0], d2);
-        atomicAdd(&out[1], r2);
+    __shared__ double2 warp_sums[kRmseThreads / 32];
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = make_double2(d2, r2);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 t = warp_sums[0];
+        for (int w = 1; w < kRmseThreads / 32; w++) {
+            t.x += warp_sums[w].x;
+            t.y += warp_sums[w].y;
+        }
+        partial[blockIdx.y * kRmseBlocks + blockIdx.x] = t;
     }
+}
+
+// One warp per item: the block partials in a fixed order.
+__global__ void rmse_final(const double2* __restrict__ partial, double2* __restrict__ out) {
+    const int lane = (int)threadIdx.x;
+    double d2 = 0.0, r2 = 0.0;
+    for (int k = lane; k < kRmseBlocks; k += 32) {
+        d2 += partial[blockIdx.x * kRmseBlocks + k].x;
+        r2 += partial[blockIdx.x * kRmseBlocks + k].y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d2 += __shfl_down_sync(0xffffffffu, d2, o);
+        r2 += __shfl_down_sync(0xffffffffu, r2, o);
+    }
+    if (lane == 0) out[blockIdx.x] = make_double2(d2, r2);
 }
 
 int check_target(pt_batch* b, int target_id, const char* what) {
     if (target_id < 0 || target_id >= (int)b->targets.size() || !b->targets[(size_t)target_id].live)
         return bfail(b, PT_ERR_INVALID, std::string(what) + ": unknown or released target");
+    return PT_OK;
+}
+
+void free_rmse(pt_batch* b) {
+    if (b->h_items) cudaFreeHost(b->h_items);
+    if (b->d_items) cudaFree(b->d_items);
+    if (b->d_partial) cudaFree(b->d_partial);
+    if (b->d_rmse) cudaFree(b->d_rmse);
+    if (b->h_rmse) cudaFreeHost(b->h_rmse);
+    b->h_items = b->d_items = nullptr;
+    b->d_partial = b->d_rmse = b->h_rmse = nullptr;
+    b->rmse_cap = 0;
+}
+
+cudaError_t reserve_rmse(pt_batch* b, int n) {
+    if (n <= b->rmse_cap) return cudaSuccess;
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return e;
+    free_rmse(b);
+    int cap = 64;
+    while (cap < n) cap *= 2;
+    e = cudaMallocHost(&b->h_items, sizeof(RmseItem) * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_items, sizeof(RmseItem) * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_partial, sizeof(double2) * kRmseBlocks * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_rmse, sizeof(double2) * (size_t)cap);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_rmse, sizeof(double2) * (size_t)cap);
+    if (e != cudaSuccess) {
+        free_rmse(b);
+        return e;
+    }
+    b->rmse_cap = cap;
+    return cudaSuccess;
+}
+
+// Relative RMSE of items [0, n) of b->h_items: one launch, one copy back.
+int run_rmse(pt_batch* b, int n, double* out) {
+    if (n == 0) return PT_OK;
+    PT_B_TRY(b, cudaMemcpyAsync(b->d_items, b->h_items, sizeof(RmseItem) * (size_t)n, cudaMemcpyHostToDevice,
+                                b->stream));
+    rmse_partial<<<dim3(kRmseBlocks, (unsigned)n), kRmseThreads, 0, b->stream>>>(b->d_items, b->d_partial);
+    PT_B_TRY(b, cudaGetLastError());
+    rmse_final<<<(unsigned)n, 32, 0, b->stream>>>(b->d_partial, b->d_rmse);
+    PT_B_TRY(b, cudaGetLastError());
+    PT_B_TRY(b, cudaMemcpyAsync(b->h_rmse, b->d_rmse, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost,
+                                b->stream));
+    PT_B_TRY(b, cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < n; i++)
+        out[i] = (b->h_rmse[i].y > 0.0) ? std::sqrt(b->h_rmse[i].x / b->h_rmse[i].y) : 0.0;
     return PT_OK;
 }
 
@@ -244,8 +332,6 @@ int pt_batch_create(pt_batch** out, int device, uint32_t pool_slots, uint32_t ma
         }
     }
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_finished, sizeof(uint32_t) * max_passes);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_rmse, 2 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMallocHost(&b->h_rmse, 2 * sizeof(double));
     if (e != cudaSuccess) {
         pt_batch_destroy(b);
         return e == cudaErrorMemoryAllocation ? PT_ERR_OOM : PT_ERR_CUDA;
@@ -278,8 +364,7 @@ int pt_batch_destroy(pt_batch* b) {
     if (b->ev) cudaEventDestroy(b->ev);
     if (b->mempool) cudaMemPoolDestroy(b->mempool);
     if (b->h_finished) cudaFreeHost(b->h_finished);
-    if (b->d_rmse) cudaFree(b->d_rmse);
-    if (b->h_rmse) cudaFreeHost(b->h_rmse);
+    free_rmse(b);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return PT_OK;
@@ -603,24 +688,45 @@ int pt_batch_read_target(pt_batch* b, int target_id, float* host, size_t bytes) 
     return PT_OK;
 }
 
-int pt_batch_rmse(pt_batch* b, int target_id, int reference_id, double* rel_rmse) {
+int pt_batch_rmse_many(pt_batch* b, const int* target_ids, const int* reference_ids, int n, double* rel_rmse) {
     if (!b) return PT_ERR_INVALID;
-    if (!rel_rmse) return bfail(b, PT_ERR_INVALID, "pt_batch_rmse: null result");
-    if (check_target(b, target_id, "pt_batch_rmse") != PT_OK) return PT_ERR_INVALID;
-    if (check_target(b, reference_id, "pt_batch_rmse") != PT_OK) return PT_ERR_INVALID;
-    const BatchTarget& t = b->targets[(size_t)target_id];
-    const BatchTarget& r = b->targets[(size_t)reference_id];
-    if (t.kind != PT_TARGET_FLOAT || t.width != r.width || t.height != r.height)
-        return bfail(b, PT_ERR_INVALID, "pt_batch_rmse: target must be a float image of the reference's size");
+    if (n < 0 || (n > 0 && (!target_ids || !reference_ids || !rel_rmse)))
+        return bfail(b, PT_ERR_INVALID, "pt_batch_rmse_many: bad arguments");
+    for (int i = 0; i < n; i++) {
+        if (check_target(b, target_ids[i], "pt_batch_rmse") != PT_OK) return PT_ERR_INVALID;
+        if (check_target(b, reference_ids[i], "pt_batch_rmse") != PT_OK) return PT_ERR_INVALID;
+        const BatchTarget& t = b->targets[(size_t)target_ids[i]];
+        const BatchTarget& r = b->targets[(size_t)reference_ids[i]];
+        if (t.kind != PT_TARGET_FLOAT || t.width != r.width || t.height != r.height)
+            return bfail(b, PT_ERR_INVALID, "pt_batch_rmse: target must be a float image of the reference's size");
+    }
     PT_B_TRY(b, cudaSetDevice(b->device));
-    PT_B_TRY(b, cudaMemsetAsync(b->d_rmse, 0, 2 * sizeof(double), b->stream));
-    const uint32_t n = (uint32_t)t.width * (uint32_t)t.height;
-    rmse_kernel<<<152, 256, 0, b->stream>>>(t.d_accum, r.d_accum, r.d_sum, n, b->d_rmse);
-    PT_B_TRY(b, cudaGetLastError());
-    PT_B_TRY(b, cudaMemcpyAsync(b->h_rmse, b->d_rmse, 2 * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
-    PT_B_TRY(b, cudaStreamSynchronize(b->stream));
-    *rel_rmse = (b->h_rmse[1] > 0.0) ? std::sqrt(b->h_rmse[0] / b->h_rmse[1]) : 0.0;
-    return PT_OK;
+    PT_B_TRY(b, reserve_rmse(b, n));
+    for (int i = 0; i < n; i++) {
+        const BatchTarget& t = b->targets[(size_t)target_ids[i]];
+        const BatchTarget& r = b->targets[(size_t)reference_ids[i]];
+        b->h_items[i] = RmseItem{t.d_accum, r.d_accum, r.d_sum, (uint32_t)t.width * (uint32_t)t.height, 0};
+    }
+    return run_rmse(b, n, rel_rmse);
+}
+
+int pt_batch_rmse(pt_batch* b, int target_id, int reference_id, double* rel_rmse) {
+    return pt_batch_rmse_many(b, &target_id, &reference_id, 1, rel_rmse);
+}
+
+int pt_batch_rmse_image(pt_batch* b, const void* d_image, int width, int height, int reference_id,
+                        double* rel_rmse) {
+    if (!b) return PT_ERR_INVALID;
+    if (!d_image || !rel_rmse) return bfail(b, PT_ERR_INVALID, "pt_batch_rmse_image: bad arguments");
+    if (check_target(b, reference_id, "pt_batch_rmse_image") != PT_OK) return PT_ERR_INVALID;
+    const BatchTarget& r = b->targets[(size_t)reference_id];
+    if (width != r.width || height != r.height)
+        return bfail(b, PT_ERR_INVALID, "pt_batch_rmse_image: size differs from the reference's");
+    PT_B_TRY(b, cudaSetDevice(b->device));
+    PT_B_TRY(b, reserve_rmse(b, 1));
+    b->h_items[0] = RmseItem{static_cast<const float4*>(d_image), r.d_accum, r.d_sum,
+                             (uint32_t)width * (uint32_t)height, 0};
+    return run_rmse(b, 1, rel_rmse);
 }
 
 int pt_batch_release_target(pt_batch* b, int target_id) {

@@ -39,6 +39,9 @@ PT_BATCH_ROUTE_PERSISTENT = 2
 PT_GEN_SPHERES = 0
 PT_GEN_SDF = 1
 
+PT_SERVE_BATCHED = 0
+PT_SERVE_PLAIN = 1
+
 UBO_FLOATS = 4097  # 7 + 1024 + 768 + 783 + 128 + 64 + 1323
 UBO_OFFSETS = {
     "numObjects": (0, 7),
@@ -158,6 +161,56 @@ class PtJobSpec(ctypes.Structure):
     ]
 
 
+class PtServerOpts(ctypes.Structure):
+    _fields_ = [
+        ("mode", ctypes.c_int32),
+        ("spp_per_pass", ctypes.c_int32),
+        ("hbm_budget", ctypes.c_uint64),
+        ("pool_slots", ctypes.c_uint32),
+        ("max_passes", ctypes.c_uint32),
+        ("iterations_per_poll", ctypes.c_int32),
+        ("passes_in_flight", ctypes.c_int32),
+        ("keep_images", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
+class PtServerJob(ctypes.Structure):
+    _fields_ = [
+        ("scene_key", ctypes.c_int32),
+        ("max_spp", ctypes.c_int32),
+        ("target_rmse", ctypes.c_double),
+        ("push", PtPush),
+    ]
+
+
+class PtServerResult(ctypes.Structure):
+    _fields_ = [
+        ("job_id", ctypes.c_uint64),
+        ("status", ctypes.c_int32),
+        ("spp", ctypes.c_int32),
+        ("rmse", ctypes.c_double),
+        ("t_submit", ctypes.c_double),
+        ("t_admit", ctypes.c_double),
+        ("t_done", ctypes.c_double),
+        ("samples", ctypes.c_uint64),
+    ]
+
+
+class PtServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_uint64),
+        ("admitted", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("samples", ctypes.c_uint64),
+        ("bytes_in_use", ctypes.c_uint64),
+        ("bytes_peak", ctypes.c_uint64),
+        ("resident_bytes", ctypes.c_uint64),
+        ("queued", ctypes.c_uint32),
+        ("active", ctypes.c_uint32),
+    ]
+
+
 assert ctypes.sizeof(PtPush) == 88
 assert ctypes.sizeof(PtSdfPlugin) == 20
 
@@ -208,6 +261,8 @@ CUDA_API = [
     ("pt_batch_target_samples", _i, [_vp, _i, ctypes.POINTER(ctypes.c_uint64)]),
     ("pt_batch_read_target", _i, [_vp, _i, _vp, _sz]),
     ("pt_batch_rmse", _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_double)]),
+    ("pt_batch_rmse_many", _i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), _i, ctypes.POINTER(ctypes.c_double)]),
+    ("pt_batch_rmse_image", _i, [_vp, _vp, _i, _i, _i, ctypes.POINTER(ctypes.c_double)]),
     ("pt_batch_release_target", _i, [_vp, _i]),
     ("pt_batch_release_scene", _i, [_vp, _i]),
 ]
@@ -230,6 +285,22 @@ HOST_API = [
     ("pt_cie_analytic_table", None, [_vp]),
     ("pt_scene_sdf_plugins", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
     ("pt_scene_generate", _i, [_i, ctypes.c_uint64, ctypes.POINTER(_vp), ctypes.POINTER(PtJobSpec)]),
+    ("pt_server_create", _i, [ctypes.POINTER(_vp), _i, ctypes.POINTER(PtServerOpts)]),
+    ("pt_server_destroy", _i, [_vp]),
+    ("pt_server_last_error", ctypes.c_char_p, [_vp]),
+    ("pt_server_now", ctypes.c_double, [_vp]),
+    ("pt_server_set_mode", _i, [_vp, _i]),
+    ("pt_server_batch", _vp, [_vp]),
+    ("pt_server_add_scene", _i, [_vp, _i, _vp, ctypes.POINTER(PtSdfPlugin), _i]),
+    ("pt_server_render_reference", _i, [_vp, _i, ctypes.POINTER(PtPush), _i, _i]),
+    ("pt_server_submit", _i, [_vp, ctypes.POINTER(PtServerJob), ctypes.POINTER(ctypes.c_uint64)]),
+    ("pt_server_poll", _i, [_vp, ctypes.POINTER(PtServerResult), _i, ctypes.POINTER(_i)]),
+    ("pt_server_pending", _i, [_vp]),
+    ("pt_server_read_image", _i, [_vp, ctypes.c_uint64, _vp, _sz]),
+    ("pt_server_release", _i, [_vp, ctypes.c_uint64]),
+    ("pt_server_get_stats", _i, [_vp, ctypes.POINTER(PtServerStats)]),
+    ("pt_server_run_trace", _i, [_vp, ctypes.POINTER(PtServerJob), ctypes.POINTER(ctypes.c_double), _i,
+                                 ctypes.POINTER(PtServerResult)]),
 ]
 
 _cache: dict[str, ctypes.CDLL] = {}

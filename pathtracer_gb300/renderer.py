@@ -318,11 +318,120 @@ class Batch:
         self._check(self._lib.pt_batch_rmse(self._h, target, reference, ctypes.byref(out)))
         return out.value
 
+    def rmse_many(self, targets: list[int], references: list[int]) -> list[float]:
+        n = len(targets)
+        t = (ctypes.c_int * max(1, n))(*targets)
+        r = (ctypes.c_int * max(1, n))(*references)
+        out = (ctypes.c_double * max(1, n))()
+        self._check(self._lib.pt_batch_rmse_many(self._h, t, r, n, out))
+        return list(out[:n])
+
+    def rmse_image(self, d_image: int, width: int, height: int, reference: int) -> float:
+        out = ctypes.c_double()
+        self._check(self._lib.pt_batch_rmse_image(self._h, d_image, width, height, reference, ctypes.byref(out)))
+        return out.value
+
     def release_target(self, target: int):
         self._check(self._lib.pt_batch_release_target(self._h, target))
 
     def release_scene(self, scene: int):
         self._check(self._lib.pt_batch_release_scene(self._h, scene))
+
+
+class Server:
+    """pt_server: progressive render serving with error targets (libpt_host)."""
+
+    def __init__(self, device: int = 0, mode: int = native.PT_SERVE_BATCHED, spp_per_pass: int = 8,
+                 hbm_budget: int = 64 << 30, pool_slots: int = 1 << 21, max_passes: int = 4096,
+                 iterations_per_poll: int = 4, passes_in_flight: int = 1, keep_images: bool = False):
+        self._lib = native.host()
+        opts = native.PtServerOpts(mode, spp_per_pass, hbm_budget, pool_slots, max_passes, iterations_per_poll,
+                                   passes_in_flight, int(keep_images), 0)
+        h = ctypes.c_void_p()
+        rc = self._lib.pt_server_create(ctypes.byref(h), device, ctypes.byref(opts))
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, "pt_server_create failed")
+        self._h = h
+        self._sizes: dict[int, tuple[int, int]] = {}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.pt_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, self._lib.pt_server_last_error(self._h).decode())
+
+    def now(self) -> float:
+        return self._lib.pt_server_now(self._h)
+
+    def set_mode(self, mode: int):
+        self._check(self._lib.pt_server_set_mode(self._h, mode))
+
+    def add_scene(self, key: int, ubo: np.ndarray, plugins: list):
+        ubo = np.ascontiguousarray(ubo, np.float32)
+        arr = (native.PtSdfPlugin * max(1, len(plugins)))(*plugins)
+        self._check(self._lib.pt_server_add_scene(self._h, key, native.ptr(ubo), arr, len(plugins)))
+
+    def render_reference(self, key: int, push: PtPush, spp: int, spp_per_pass: int = 32):
+        self._check(self._lib.pt_server_render_reference(self._h, key, ctypes.byref(push), spp, spp_per_pass))
+
+    @staticmethod
+    def job(scene_key: int, push: PtPush, max_spp: int, target_rmse: float = 0.0) -> native.PtServerJob:
+        return native.PtServerJob(scene_key, max_spp, target_rmse, push)
+
+    def submit(self, job: native.PtServerJob) -> int:
+        out = ctypes.c_uint64()
+        self._check(self._lib.pt_server_submit(self._h, ctypes.byref(job), ctypes.byref(out)))
+        self._sizes[out.value] = (job.push.resolution[0], job.push.resolution[1])
+        return out.value
+
+    def poll(self, capacity: int = 256) -> list[native.PtServerResult]:
+        buf = (native.PtServerResult * capacity)()
+        n = ctypes.c_int()
+        self._check(self._lib.pt_server_poll(self._h, buf, capacity, ctypes.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def pending(self) -> int:
+        return self._lib.pt_server_pending(self._h)
+
+    def drain(self) -> list[native.PtServerResult]:
+        out = []
+        while self.pending() > 0:
+            out += self.poll()
+        return out
+
+    def read_image(self, job_id: int) -> np.ndarray:
+        w, h = self._sizes[job_id]
+        out = np.empty((h, w, 4), np.float32)
+        self._check(self._lib.pt_server_read_image(self._h, ctypes.c_uint64(job_id), native.ptr(out), out.nbytes))
+        return out
+
+    def release(self, job_id: int):
+        self._check(self._lib.pt_server_release(self._h, ctypes.c_uint64(job_id)))
+
+    def stats(self) -> dict:
+        st = native.PtServerStats()
+        self._check(self._lib.pt_server_get_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in native.PtServerStats._fields_}
+
+    def run_trace(self, jobs: list, arrivals: list[float]) -> list[native.PtServerResult]:
+        n = len(jobs)
+        arr_j = (native.PtServerJob * max(1, n))(*jobs)
+        arr_t = (ctypes.c_double * max(1, n))(*arrivals)
+        res = (native.PtServerResult * max(1, n))()
+        self._check(self._lib.pt_server_run_trace(self._h, arr_j, arr_t, n, res))
+        return [res[i] for i in range(n)]
 
 
 def render_offscreen(ctx: Context, scene: Scene, cie: np.ndarray, width: int, height: int, num_samples: int,
