@@ -70,6 +70,11 @@ def parse_args():
     ap.add_argument("--compare-engines", type=int, default=1, help="also time the other engine (1 step)")
     ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0: library default)")
     ap.add_argument("--budget", type=int, default=0, help="wavefront march steps per launch (0: default)")
+    ap.add_argument("--refill", type=int, default=0, help="wavefront march refill threshold (0: default)")
+    ap.add_argument("--drain", type=int, default=-1, help="wavefront march drain lanes (-1: default)")
+    ap.add_argument("--blocks", type=int, default=0, help="wavefront stage blocks per SM (0: default)")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
     ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64", "serve"])
     ap.add_argument("--rate", type=float, default=2.0, help="serve: Poisson arrivals per second")
     ap.add_argument("--duration", type=float, default=30.0, help="serve: seconds of arrivals")
@@ -261,7 +266,7 @@ def run_batch(args, rank, world):
     samples = sum(sp.width * sp.height * sp.spp for _, sp, _, _ in jobs)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    b = Batch(local, pool_slots=args.pool or (1 << 21), max_passes=4096)
+    b = Batch(local, pool_slots=args.pool or (1 << 19), max_passes=4096)
     b.set_route({"auto": native.PT_BATCH_ROUTE_AUTO, "staged": native.PT_BATCH_ROUTE_STAGED,
                  "persistent": native.PT_BATCH_ROUTE_PERSISTENT}[args.route])
     if args.budget:
@@ -433,7 +438,7 @@ def run_serve(args, rank, world):
         push = sc.push_constants(spec.width, spec.height, 1, 1, 1, spec.pathLength)
         pool.append((kind, sc, spec, push))
     srv = Server(local, mode=native.PT_SERVE_BATCHED, spp_per_pass=8, hbm_budget=64 << 30,
-                 pool_slots=args.pool or (1 << 21), iterations_per_poll=4)
+                 pool_slots=args.pool or (1 << 19), iterations_per_poll=4)
     t0 = time.perf_counter()
     for key, (kind, sc, spec, push) in enumerate(pool):
         srv.add_scene(key, sc.pack_ubo(cie), sc.sdf_plugins())
@@ -559,8 +564,18 @@ def main():
         ctx.set_wavefront_pool(args.pool)
     if args.budget:
         ctx.set_march_budget(args.budget)
+    knobs = {k: v for k, v in (("refill_min", args.refill), ("blocks_per_sm", args.blocks)) if v}
+    if args.drain >= 0:
+        knobs["drain_lanes"] = args.drain
+    if knobs:
+        ctx.set_tuning(**knobs)
     ctx.bind(scene, cie)
     ctx.resize_accum(W, H)
+    tuned, tune_secs = None, 0.0
+    if args.autotune and args.engine == "wavefront":
+        t0 = time.perf_counter()
+        tuned, _ = ctx.autotune(scene.push_constants(W, H, 8, 8, 8, args.depth), rounds=args.autotune)
+        tune_secs = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
 
@@ -661,7 +676,8 @@ def main():
         "config": {"workload": WORKLOAD, "resolution": [W, H], "spp": args.spp, "max_depth": args.depth,
                    "samples_per_dispatch": spf, "dispatches_per_step": ndisp,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                   "wavefront_pool": args.pool or None, "march_budget": args.budget or None},
+                   "wavefront_tuning": ctx.tuning() if args.engine == "wavefront" else None,
+                   "autotuned": bool(tuned), "autotune_s": tune_secs},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "engine": args.engine,
         "engines": {args.engine: {"value": value / world, "ms_per_step": ms_step}, **other},

@@ -159,7 +159,7 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push);
 #define PT_ENGINE_WAVEFRONT 1
 int pt_set_engine(pt_ctx* ctx, int engine);
 int pt_get_engine(pt_ctx* ctx);
-/* Path slots of the wavefront pool (default 2^21; 252 B each, plus 16 B per
+/* Path slots of the wavefront pool (default 2^19, whose state fits in L2; 252 B each, plus 16 B per
  * sample of the dispatch for the sample colours). */
 int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots);
 /* Sphere-tracing iterations a ray may take per march launch before it is
@@ -229,6 +229,25 @@ int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float
 #define PT_NOALLOC_POOL_SLOTS (1u << 16)
 int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins, const pt_push* push,
                         float* d_accum, void* stream);
+
+/* Knobs of the wavefront engine (no counterpart in the reference).  The
+ * defaults suit the SDF scenes measured on GB300; pt_autotune_wavefront
+ * picks them for a given scene and dispatch shape. */
+typedef struct pt_wavefront_tuning {
+    uint32_t pool_slots;   /* path slots (1024..2^28; default 2^19) */
+    int32_t march_budget;  /* SDF steps per ray per march launch (1..512; default 64) */
+    int32_t refill_min;    /* idle lanes a march warp gathers before refilling them together (1..32) */
+    int32_t drain_lanes;   /* a march warp left with fewer rays after its queue drained suspends them (0..32) */
+    int32_t blocks_per_sm; /* stage-kernel blocks of 256 threads per SM (1..8) */
+} pt_wavefront_tuning;
+int pt_get_wavefront_tuning(pt_ctx* ctx, pt_wavefront_tuning* out);
+int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* tuning);
+/* The autotuner: coordinate descent over the knobs above, `rounds` passes,
+ * timing wavefront dispatches of `push` (its resolution must be the
+ * accumulator's) on the bound scene.  Installs and returns the fastest
+ * setting and its seconds per dispatch; the accumulator is left as it was. */
+int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavefront_tuning* best,
+                          double* best_seconds);
 
 /* ---------------------------------------------------------------------------
  * Batched rendering.  No counterpart in the reference, which renders one

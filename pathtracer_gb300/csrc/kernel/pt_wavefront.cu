@@ -32,6 +32,12 @@ namespace {
 
 constexpr uint32_t kShadowFlag = 1u << 30;
 constexpr int kStageThreads = 256;
+// wf_march: after a large queue is drained, a warp with fewer rays than
+// WfArgs::drain_lanes suspends those that have marched kDrainMinSteps steps
+// in this launch, for the next iteration.
+constexpr int kDrainMinSteps = 8;
+// SphereTracing's over-relaxation start (SC:781).
+constexpr float kOmegaMax = 1.70f;
 
 // Warp-aggregated append of `value` to queue[count++] for lanes with pred.
 // Must be called by all 32 lanes of the warp.
@@ -215,10 +221,16 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
                 float2 tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
                 uint32_t set1 = 0;
                 march = search_sdf(S, org, invdir, tmm, set1);
+                if (march) {
+                    // SphereTracing's start (SC:779-790): the march kernel
+                    // picks the ray up like one it suspended.
+                    A.pool.m0[slot] = make_float4(fmaxf(tmm.x, 1e-3f), 0.0f, kOmegaMax, 0.0f);
+                    A.pool.m1[slot] = make_float4(tmm.x, tmm.y, 0.0f, __uint_as_float(set1));
+                    A.pool.m2[slot] = 0u;
+                }
             }
             v.h0[slot] = make_float4(h.hitdist, h.materialID, h.lightID, __int_as_float(objectID));
             v.h1[slot] = make_float4(h.normal.x, h.normal.y, h.normal.z, 0.0f);
-            if (march) A.pool.m2[slot] = 0u;
         }
         q_push(A.q_march[cur], &C.n_march[cur], slot, valid && march);
         q_push(A.q_shade, &C.n_shade, slot, valid && !march);
@@ -226,7 +238,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
 }
 
 // SphereTracing (SC:779-860) with one SDF evaluation per loop iteration per lane.
-enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NORMAL5 = 8, MP_NO_BOX = 9 };
+enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NORMAL5 = 8 };
 
 __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
@@ -237,25 +249,29 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     const WfPool& M = A.pool;
     const int lane = threadIdx.x & 31;
     const int budget = A.march_budget;
+    const int refill_min = A.refill_min;
     int steps = 0;
+    // Draining only pays while the queue holds more rays than the grid has lanes.
+    const bool many = n >= 2u * gridDim.x * blockDim.x;
 
     uint32_t slot = 0;
     const KScene* Sp = nullptr;
     int phase = MP_EMPTY;
     bool exhausted = false;
-    float3 org = f3(0.0f, 0.0f, 0.0f), dir = f3(0.0f, 0.0f, 1.0f), invdir = f3(0.0f, 0.0f, 0.0f), p = org;
+    float3 org = f3(0.0f, 0.0f, 0.0f), dir = f3(0.0f, 0.0f, 1.0f), p = org;
     float t = 0.0f, insT = 0.0f, omega = 0.0f, prevR = 0.0f, hitdist = 0.0f, k = 0.0f, nplus = 0.0f;
     float3 nv = f3(0.0f, 0.0f, 0.0f);
     float2 tmm = make_float2(0.0f, 0.0f);
     uint32_t set1 = 0;
     int points = 0, iter = 0;
-    const float omegaMax = 1.70f, omegaSpeed = 0.20f, e = 1e-4f;
+    const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
 
     for (;;) {
-        // Refill lanes that have no ray (warp-aggregated fetch).
+        // Refill lanes that have no ray (warp-aggregated fetch), once at
+        // least refill_min of them are idle or the warp has none left.
         const bool need = (phase == MP_EMPTY) && !exhausted;
         const unsigned mneed = __ballot_sync(0xffffffffu, need);
-        if (mneed) {
+        if (mneed && (__popc(mneed) >= refill_min || __ballot_sync(0xffffffffu, phase != MP_EMPTY) == 0)) {
             const int leader = __ffs(mneed) - 1;
             uint32_t b = 0;
             if (lane == leader) b = atomicAdd(&C.march_cursor, (uint32_t)__popc(mneed));
@@ -271,11 +287,10 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                     org = f3(o.x, o.y, o.z);
                     dir = f3(d.x, d.y, d.z);
                     hitdist = v.h0[slot].x;
-                    invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
                     steps = 0;
+                    // A ray from isect (flag bit clear: start with the sign
+                    // probe) or one suspended by an earlier launch.
                     const uint32_t saved = M.m2[slot];
-                  if (saved & 0x80000000u) {
-                    // continue a march suspended by the previous launch
                     const float4 a0 = M.m0[slot], a1 = M.m1[slot];
                     t = a0.x;
                     insT = a0.y;
@@ -287,30 +302,18 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                     iter = (int)(saved & 1023u);
                     points = (int)((saved >> 10) & 0xffffu);
                     p = fma3s(dir, t, org);
-                    phase = MP_STEP;
-                  } else {
-                    t = 1e-3f;
-                    insT = 0.0f;
-                    omega = omegaMax;
-                    prevR = 0.0f;
-                    points = 0;
-                    iter = 0;
-                    tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
-                    set1 = 0;
-                    if (search_sdf(*Sp, org, invdir, tmm, set1)) {
-                        t = fmaxf(tmm.x, t);
-                        p = fma3s(dir, t, org);
-                        phase = MP_SIGN;
-                    } else {
-                        phase = MP_NO_BOX;  // (isect found a box with the same test) keep the analytic hit
-                    }
-                  }
+                    phase = (saved & 0x80000000u) ? MP_STEP : MP_SIGN;
                 } else {
                     exhausted = true;
                 }
             }
         }
-        if (__ballot_sync(0xffffffffu, phase != MP_EMPTY) == 0) break;
+        const unsigned live = __ballot_sync(0xffffffffu, phase != MP_EMPTY);
+        if (live == 0) break;
+        // Once the queue is drained, a warp with few rays left would run on
+        // with most lanes idle: its marching rays save their state and
+        // continue in full warps next iteration instead.
+        const bool drain = many && __ballot_sync(0xffffffffu, exhausted) != 0 && __popc(live) < A.drain_lanes;
 
         // One SDF evaluation.
         const bool evalLane = (phase >= MP_SIGN && phase <= MP_NORMAL5);
@@ -351,6 +354,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                 if (points >= 2) {
                     t = tmm.y + 1e-3f;
                     tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
+                    const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
                     if (search_sdf(*Sp, fma3s(dir, t, org), invdir, tmm, set1)) {
                         tmm.x += t;
                         tmm.y += t;
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                 } else {
                     finished = true;
                 }
-            } else if (!finished && ++steps >= budget) {
+            } else if (!finished && (++steps >= budget || (drain && steps >= kDrainMinSteps))) {
                 // out of budget for this launch: save the state, continue next iteration
                 M.m0[slot] = make_float4(t, insT, omega, prevR);
                 M.m1[slot] = make_float4(tmm.x, tmm.y, k, __uint_as_float(set1));
@@ -403,8 +407,6 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                 hit = true;
                 finished = true;
             }
-        } else if (phase == MP_NO_BOX) {
-            finished = true;
         }
 
         if (finished && hit) {

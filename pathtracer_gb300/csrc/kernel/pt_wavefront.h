@@ -71,6 +71,8 @@ struct WfArgs {
     KTrace trace;  // single-job dispatches only
     uint32_t pool_size;
     int march_budget;  // sphere-tracing iterations per ray per march launch
+    int refill_min;    // idle lanes a march warp gathers before it refills them at once
+    int drain_lanes;   // a drained march warp with fewer rays suspends them (0: never)
 };
 
 // Bytes of the engine's device buffers for a pool of `pool` slots.

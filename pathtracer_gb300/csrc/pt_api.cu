@@ -6,6 +6,7 @@
 // here is process-global, so contexts may coexist on one device.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -35,8 +36,11 @@ struct pt_ctx {
     int nplug = 0;
     KTrace trace{nullptr, nullptr, nullptr, 0};
     int engine = PT_ENGINE_WAVEFRONT;
-    uint32_t pool_cap = 1u << 21;  // wavefront path slots
+    uint32_t pool_cap = 1u << 19;  // wavefront path slots (the state of 2^19 paths fits in L2)
     int march_budget = 64;
+    int refill_min = 2;    // measured best on GB300 (mandelbulb 1024x1024)
+    int drain_lanes = 24;
+    int blocks_per_sm = 4;
     KScene* d_scene = nullptr;     // device copy for the wavefront kernels
     WfEngine* wf = nullptr;        // wavefront driver (created on first use, grows with the dispatch)
     float4* d_colors = nullptr;    // per-sample colours of the current dispatch
@@ -293,6 +297,105 @@ int pt_set_march_budget(pt_ctx* ctx, int steps) {
     return PT_OK;
 }
 
+int pt_get_wavefront_tuning(pt_ctx* ctx, pt_wavefront_tuning* out) {
+    if (!ctx || !out) return PT_ERR_INVALID;
+    out->pool_slots = ctx->pool_cap;
+    out->march_budget = ctx->march_budget;
+    out->refill_min = ctx->refill_min;
+    out->drain_lanes = ctx->drain_lanes;
+    out->blocks_per_sm = ctx->blocks_per_sm;
+    return PT_OK;
+}
+
+int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* t) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!t || t->pool_slots < 1024 || t->pool_slots > (1u << 28) || t->march_budget < 1 || t->march_budget > 512 ||
+        t->refill_min < 1 || t->refill_min > 32 || t->drain_lanes < 0 || t->drain_lanes > 32 || t->blocks_per_sm < 1 ||
+        t->blocks_per_sm > 8)
+        return fail(ctx, PT_ERR_INVALID, "pt_set_wavefront_tuning: a value is out of range");
+    ctx->pool_cap = t->pool_slots;
+    ctx->march_budget = t->march_budget;
+    ctx->refill_min = t->refill_min;
+    ctx->drain_lanes = t->drain_lanes;
+    ctx->blocks_per_sm = t->blocks_per_sm;
+    return PT_OK;
+}
+
+// Coordinate descent over the wavefront knobs, timing real dispatches of
+// `push` (host wall clock around dispatch + wait, best of two after a
+// warm-up).  The accumulator is restored afterwards.
+int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavefront_tuning* best,
+                          double* best_seconds) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!push || rounds < 1 || !best) return fail(ctx, PT_ERR_INVALID, "pt_autotune_wavefront: bad arguments");
+    if (!ctx->has_scene || !ctx->d_accum) return fail(ctx, PT_ERR_NO_SCENE, "pt_autotune_wavefront: no scene");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)ctx->width * (size_t)ctx->height * sizeof(float4);
+    float4* saved = nullptr;
+    PT_CUDA_TRY(ctx, cudaMalloc(&saved, bytes));
+    cudaError_t ce = cudaMemcpyAsync(saved, ctx->d_accum, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (ce != cudaSuccess) {
+        cudaFree(saved);
+        return cuda_fail(ctx, ce, "pt_autotune_wavefront");
+    }
+    const int engine = ctx->engine;
+    ctx->engine = PT_ENGINE_WAVEFRONT;
+    auto time_one = [&](const pt_wavefront_tuning& t, double* secs) -> int {
+        int rc = pt_set_wavefront_tuning(ctx, &t);
+        double b = 1e30;
+        for (int i = 0; i < 3 && rc == PT_OK; i++) {
+            const auto t0 = std::chrono::steady_clock::now();
+            rc = pt_dispatch(ctx, push);
+            if (rc == PT_OK) rc = pt_wait(ctx, UINT64_MAX);
+            const double d = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (i > 0) b = std::min(b, d);
+        }
+        *secs = b;
+        return rc;
+    };
+    static const uint32_t kPools[] = {1u << 18, 3u << 17, 1u << 19, 3u << 18, 1u << 20};
+    static const int kBudgets[] = {32, 64, 128};
+    static const int kRefill[] = {1, 2, 4, 8};
+    static const int kDrain[] = {0, 8, 16, 24};
+    static const int kBlocks[] = {2, 3, 4};
+    pt_wavefront_tuning cur;
+    pt_get_wavefront_tuning(ctx, &cur);
+    double cur_t = 0.0;
+    int rc = time_one(cur, &cur_t);
+    for (int r = 0; r < rounds && rc == PT_OK; r++) {
+        for (int knob = 0; knob < 5 && rc == PT_OK; knob++) {
+            const int nvals = knob == 0 ? 5 : knob == 1 ? 3 : knob == 2 ? 4 : knob == 3 ? 4 : 3;
+            for (int i = 0; i < nvals && rc == PT_OK; i++) {
+                pt_wavefront_tuning c = cur;
+                switch (knob) {
+                    case 0: c.pool_slots = kPools[i]; break;
+                    case 1: c.march_budget = kBudgets[i]; break;
+                    case 2: c.refill_min = kRefill[i]; break;
+                    case 3: c.drain_lanes = kDrain[i]; break;
+                    default: c.blocks_per_sm = kBlocks[i]; break;
+                }
+                if (std::memcmp(&c, &cur, sizeof c) == 0) continue;
+                double t = 0.0;
+                rc = time_one(c, &t);
+                if (rc == PT_OK && t < 0.99 * cur_t) {
+                    cur = c;
+                    cur_t = t;
+                }
+            }
+        }
+    }
+    ctx->engine = engine;
+    if (rc == PT_OK) rc = pt_set_wavefront_tuning(ctx, &cur);
+    ce = cudaMemcpyAsync(ctx->d_accum, saved, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+    cudaFree(saved);
+    if (rc != PT_OK) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "pt_autotune_wavefront");
+    *best = cur;
+    if (best_seconds) *best_seconds = cur_t;
+    return PT_OK;
+}
+
 int pt_wait(pt_ctx* ctx, uint64_t timeout_ns) {
     if (!ctx) return PT_ERR_INVALID;
     PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
@@ -367,7 +470,7 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     const uint32_t total = (uint32_t)total64;
     uint32_t pool = total < ctx->pool_cap ? total : ctx->pool_cap;
     if (pool < 1024u) pool = 1024u;
-    if (!ctx->wf || ctx->wf->pool < pool) {
+    if (!ctx->wf || ctx->wf->pool < pool || ctx->wf->pool > ctx->pool_cap) {
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
         if (!ctx->wf) ctx->wf = new (std::nothrow) WfEngine();
         if (!ctx->wf) return fail(ctx, PT_ERR_OOM, "pt_dispatch: out of host memory");
@@ -385,6 +488,7 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     WfEngine& E = *ctx->wf;
     E.set_stream(ctx->stream);
     E.set_march_budget(ctx->march_budget);
+    E.set_tuning(ctx->refill_min, ctx->drain_lanes, ctx->blocks_per_sm);
     E.args.trace = ctx->trace;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
     PT_CUDA_TRY(ctx, E.reset());

@@ -72,11 +72,13 @@ static cudaError_t common_setup(WfEngine& e, int device, cudaStream_t stream, ui
     e.args.job_cap = max_jobs;
     e.args.pool_size = pool;
     e.args.march_budget = march_budget;
+    e.args.refill_min = 2;
+    e.args.drain_lanes = 24;
     e.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
     int sms = 0;
     EN_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    e.grid = sms * 4;  // 4 blocks of 256 threads per SM (64 registers per thread)
-    e.sms = sms;
+    e.sms = e.sms_count = sms;
+    e.grid = sms * e.blocks_per_sm;  // blocks of 256 threads (64 registers per thread: 4 fit on an SM)
     return e.reset();
 }
 
@@ -135,6 +137,14 @@ void WfEngine::set_march_budget(int budget) {
 }
 
 void WfEngine::set_stream(cudaStream_t s) { stream = s; }
+
+void WfEngine::set_tuning(int refill, int drain, int bps) {
+    if (refill != args.refill_min || drain != args.drain_lanes || bps != blocks_per_sm) drop_graph();
+    args.refill_min = refill;
+    args.drain_lanes = drain;
+    blocks_per_sm = bps;
+    grid = sms_count * bps;
+}
 
 void WfEngine::set_persistent(bool on) { persistent = on; }
 

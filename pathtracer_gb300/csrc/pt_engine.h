@@ -26,6 +26,8 @@ struct WfEngine {
     uint32_t max_jobs = 0;    // ring entries
     int grid = 0;
     WfArgs args{};
+    int sms_count = 0;
+    int blocks_per_sm = 4;
     WfJob* jobs = nullptr;    // host mirror of the ring (max_jobs entries)
     uint32_t njobs = 0;       // passes added since the last reset (job_hi)
     uint32_t lo = 0;          // passes below this were resolved and retired
@@ -63,6 +65,8 @@ struct WfEngine {
     cudaError_t reset();
     // Sphere-tracing iterations per ray per march launch.
     void set_march_budget(int budget);
+    // March refill threshold, drain threshold and stage-kernel blocks per SM.
+    void set_tuning(int refill_min, int drain_lanes, int blocks_per_sm);
     // Staged kernels (false) or the persistent path kernel (true).
     void set_persistent(bool on);
     // Persistent mode: every sample added so far is covered by a launch.

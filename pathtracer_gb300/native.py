@@ -133,6 +133,16 @@ class PtOffscreenOpts(ctypes.Structure):
     ]
 
 
+class PtWavefrontTuning(ctypes.Structure):
+    _fields_ = [
+        ("pool_slots", ctypes.c_uint32),
+        ("march_budget", ctypes.c_int32),
+        ("refill_min", ctypes.c_int32),
+        ("drain_lanes", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+    ]
+
+
 class PtBatchInfo(ctypes.Structure):
     _fields_ = [
         ("samples_done", ctypes.c_uint64),
@@ -243,6 +253,10 @@ CUDA_API = [
     ("pt_set_wavefront_pool", _i, [_vp, ctypes.c_uint32]),
     ("pt_last_iterations", ctypes.c_uint32, [_vp]),
     ("pt_set_march_budget", _i, [_vp, _i]),
+    ("pt_get_wavefront_tuning", _i, [_vp, ctypes.POINTER(PtWavefrontTuning)]),
+    ("pt_set_wavefront_tuning", _i, [_vp, ctypes.POINTER(PtWavefrontTuning)]),
+    ("pt_autotune_wavefront", _i, [_vp, ctypes.POINTER(PtPush), _i, ctypes.POINTER(PtWavefrontTuning),
+                                   ctypes.POINTER(ctypes.c_double)]),
     ("pt_dispatch_noalloc", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(PtPush), _vp, _vp]),
     ("pt_batch_create", _i, [ctypes.POINTER(_vp), _i, ctypes.c_uint32, ctypes.c_uint32]),
     ("pt_batch_destroy", _i, [_vp]),

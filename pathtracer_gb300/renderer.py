@@ -212,6 +212,25 @@ class Context:
     def set_march_budget(self, steps: int):
         self._check(self._lib.pt_set_march_budget(self._h, steps))
 
+    def tuning(self) -> dict:
+        t = native.PtWavefrontTuning()
+        self._check(self._lib.pt_get_wavefront_tuning(self._h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in native.PtWavefrontTuning._fields_}
+
+    def set_tuning(self, **kw):
+        cur = self.tuning()
+        cur.update(kw)
+        t = native.PtWavefrontTuning(**cur)
+        self._check(self._lib.pt_set_wavefront_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, push: PtPush, rounds: int = 1) -> tuple[dict, float]:
+        """pt_autotune_wavefront: installs and returns the fastest knobs."""
+        t = native.PtWavefrontTuning()
+        secs = ctypes.c_double()
+        self._check(self._lib.pt_autotune_wavefront(self._h, ctypes.byref(push), rounds, ctypes.byref(t),
+                                                    ctypes.byref(secs)))
+        return {k: getattr(t, k) for k, _ in native.PtWavefrontTuning._fields_}, secs.value
+
     def last_iterations(self) -> int:
         return self._lib.pt_last_iterations(self._h)
 
@@ -223,7 +242,7 @@ class Context:
 class Batch:
     """pt_batch: many scenes, targets and passes in one wavefront pool."""
 
-    def __init__(self, device: int = 0, pool_slots: int = 1 << 21, max_passes: int = 4096):
+    def __init__(self, device: int = 0, pool_slots: int = 1 << 19, max_passes: int = 4096):
         self._lib = native.cuda()
         h = ctypes.c_void_p()
         rc = self._lib.pt_batch_create(ctypes.byref(h), device, pool_slots, max_passes)
@@ -342,7 +361,7 @@ class Server:
     """pt_server: progressive render serving with error targets (libpt_host)."""
 
     def __init__(self, device: int = 0, mode: int = native.PT_SERVE_BATCHED, spp_per_pass: int = 8,
-                 hbm_budget: int = 64 << 30, pool_slots: int = 1 << 21, max_passes: int = 4096,
+                 hbm_budget: int = 64 << 30, pool_slots: int = 1 << 19, max_passes: int = 4096,
                  iterations_per_poll: int = 4, passes_in_flight: int = 1, keep_images: bool = False):
         self._lib = native.host()
         opts = native.PtServerOpts(mode, spp_per_pass, hbm_budget, pool_slots, max_passes, iterations_per_poll,
