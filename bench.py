@@ -154,6 +154,47 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def fp32_peak_tflops(peaks):
+    """Nominal FP32 FMA rate at the measured maximum SM clock: SMs x 128 lanes x 2."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    return sms * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+
+
+def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind):
+    """One extra step with per-stage CUDA events: each stage kernel's device
+    time and, from the committed work model, its achieved FP32 rate; the
+    roofline object is the march kernel's (the dominant one)."""
+    from pathtracer_gb300 import workmodel
+
+    ctx.set_stage_timing(True)
+    run_step()
+    ctx.wait()
+    ms, iters = ctx.stage_times()
+    ctx.set_stage_timing(False)
+    ops = workmodel.fp32_ops_per_sample(workmodel.load(workload)["per_sample"])
+    total_ms = sum(ms.values())
+    peak = fp32_peak_tflops(peaks)
+    stages = {}
+    for st in ("isect", "march", "shade", "gen", "book"):
+        secs = ms[st] / 1000.0
+        work = ops.get(st, 0.0) * samples
+        stages[st] = {"ms": ms[st], "share": ms[st] / total_ms if total_ms else None,
+                      "ms_per_launch": ms[st] / iters if iters else None,
+                      "fp32_tflops": (work / secs / 1e12) if secs and work else None}
+    march = stages["march"]
+    roof = {"bound": "fp32", "kernel": "wf_march", "achieved": march["fp32_tflops"], "peak": peak,
+            "unit": "TFLOP/s", "frac": (march["fp32_tflops"] or 0.0) / peak, "traffic": None,
+            "work_per_sample": ops["march"], "launches": iters,
+            "note": f"peak: nominal FP32 FMA rate (SMs x 128 x 2) at the measured max SM clock ({peak_kind} peaks "
+                    "hold no FP32 figure); achieved: hand-counted FP32 operations of the march stage's events "
+                    "(pathtracer_gb300/workmodel.py, counts per sample from tests/golden/work_*.json) over the "
+                    "summed device time of its launches in one step timed with per-stage CUDA events; DRAM "
+                    "traffic per launch is in profiles/"}
+    return roof, stages, ops
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -250,6 +291,20 @@ def batch_cpu_baseline(jobs, nthreads, rows_per_job=2, njobs=16):
             samples += W * spec.spp
     dt = time.perf_counter() - t0
     return samples / dt, samples, dt
+
+
+def batch_roofline(samples, secs, peaks, peak_kind):
+    """FP32 roofline of the persistent path kernel over a batched step (it is
+    nearly all of the step's device time)."""
+    from pathtracer_gb300 import workmodel
+
+    ops = workmodel.fp32_ops_per_sample(workmodel.load("batch64_spheres")["per_sample"])
+    peak = fp32_peak_tflops(peaks)
+    ach = ops["total"] * samples / secs / 1e12
+    return {"bound": "fp32", "kernel": "wf_persist", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": ach / peak, "traffic": None, "work_per_sample": ops["total"],
+            "note": f"peak: nominal FP32 FMA rate at the measured max SM clock ({peak_kind}); achieved: work-model "
+                    "FP32 operations of the whole step over the step's device time"}
 
 
 def run_batch(args, rank, world):
@@ -403,8 +458,7 @@ def run_batch(args, rank, world):
         "speedup_vs_plain": p_secs / b_secs,
         "results_identical_to_plain": identical,
         "gpu_launches": int(args.steps * (5 * iters + 2 * len(jobs))),
-        "roofline": {"bound": "hbm", "achieved": None, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": None,
-                     "traffic": None, "note": f"peak {peak_kind}; see the mandelbulb workload for the kernel roofline"},
+        "roofline": batch_roofline(samples, b_secs, peaks, peak_kind),
         "clocks": clk.summary(),
     }
     if rank == 0:
@@ -665,10 +719,18 @@ def main():
     d2h = W * H * 16 + 9 * 4 * sum(list(scene.counts().values())[:5])
 
     peaks, peak_kind = measured_peaks()
-    # HBM roofline of the megakernel: algorithmic bytes = the accumulator
-    # read-modify-write (16 B read + 16 B write per pixel per dispatch).
-    alg_bytes = 32.0 * W * H * ndisp
-    achieved_gbs = alg_bytes / (ms_step / 1000.0) / 1e9
+    if args.engine == "wavefront":
+        roofline, stages, ops = stage_roofline(ctx, lambda: one_step(args.warmup + args.steps + 5), samples_per_step,
+                                               WORKLOAD, peaks, peak_kind)
+    else:
+        from pathtracer_gb300 import workmodel
+
+        ops = workmodel.fp32_ops_per_sample(workmodel.load(WORKLOAD)["per_sample"])
+        peak = fp32_peak_tflops(peaks)
+        ach = ops["total"] * samples_per_step / (ms_step / 1000.0) / 1e12
+        roofline = {"bound": "fp32", "kernel": "megakernel", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                    "frac": ach / peak, "traffic": None, "work_per_sample": ops["total"]}
+        stages = None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -684,10 +746,9 @@ def main():
         "wavefront_iterations_per_dispatch": iters if args.engine == "wavefront" else None,
         "gpu_launches": args.steps * ndisp * ((5 * iters + 2) if args.engine == "wavefront" else 1),
         "wall_s_timed_region": t_wall,
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": None,
-                     "note": f"peak {peak_kind}; the megakernel is FP32/SFU-issue bound, its HBM traffic is the "
-                             "accumulator only"},
+        "roofline": roofline,
+        "stages": stages,
+        "fp32_ops_per_sample": ops,
         "clocks": clk.summary(),
     }
     if rank == 0:

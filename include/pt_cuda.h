@@ -249,6 +249,14 @@ int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* tuning);
 int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavefront_tuning* best,
                           double* best_seconds);
 
+/* Stage timing of the wavefront engine: when on, iterations are launched one
+ * kernel at a time with CUDA events around each of the five stage kernels
+ * (isect, march, shade, gen, bookkeeping), and pt_get_stage_times returns the
+ * device milliseconds summed per stage since timing was switched on, and the
+ * iterations timed.  Off by default (it disables graph replay). */
+int pt_set_stage_timing(pt_ctx* ctx, int on);
+int pt_get_stage_times(pt_ctx* ctx, double ms[5], uint64_t* iterations);
+
 /* ---------------------------------------------------------------------------
  * Batched rendering.  No counterpart in the reference, which renders one
  * scene per compute dispatch (src/pathtracer.cpp:3586-3608): these calls keep

@@ -655,16 +655,25 @@ cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint
     return cudaGetLastError();
 }
 
-cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream) {
+cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
+                                           cudaEvent_t* stage_events) {
+    // stage_events (optional): 6 events recorded before isect, march, shade,
+    // gen, bookkeeping and after it, for per-stage device times.
+    if (stage_events) cudaEventRecord(stage_events[0], stream);
     wf_isect<<<grid, kStageThreads, 0, stream>>>(*a);
+    if (stage_events) cudaEventRecord(stage_events[1], stream);
     wf_march<<<grid, kStageThreads, 0, stream>>>(*a);
+    if (stage_events) cudaEventRecord(stage_events[2], stream);
     if (trace) {
         wf_shade<true><<<grid, kStageThreads, 0, stream>>>(*a);
     } else {
         wf_shade<false><<<grid, kStageThreads, 0, stream>>>(*a);
     }
+    if (stage_events) cudaEventRecord(stage_events[3], stream);
     wf_gen<<<grid, kStageThreads, 0, stream>>>(*a);
+    if (stage_events) cudaEventRecord(stage_events[4], stream);
     wf_book<<<1, 1, 0, stream>>>(*a);
+    if (stage_events) cudaEventRecord(stage_events[5], stream);
     return cudaGetLastError();
 }
 

@@ -83,8 +83,12 @@ cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream);
 // job_hi = index + 1, job_lo = lo.
 cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint32_t index, uint32_t lo,
                                          cudaStream_t stream);
-// One iteration: isect, march, shade, gen, bookkeeping (grid = blocks per stage kernel).
-cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream);
+// One iteration: isect, march, shade, gen, bookkeeping (grid = blocks per
+// stage kernel); with stage_events, 6 events bracket the 5 kernels.
+cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
+                                           cudaEvent_t* stage_events = nullptr);
+// Stages timed by the engine's stage-timing mode.
+enum { PT_STAGE_ISECT = 0, PT_STAGE_MARCH, PT_STAGE_SHADE, PT_STAGE_GEN, PT_STAGE_BOOK, PT_STAGE_COUNT };
 // Persistent mode: one launch of the persistent path kernel over the next
 // `budget` samples of the job ring, compiled for primitive classes `variant`
 // (PT_FEAT_*: 0, BOX, ANALYTIC or ALL), with every block resident at once

@@ -38,6 +38,7 @@ struct pt_ctx {
     int engine = PT_ENGINE_WAVEFRONT;
     uint32_t pool_cap = 1u << 19;  // wavefront path slots (the state of 2^19 paths fits in L2)
     int march_budget = 64;
+    bool stage_timing = false;
     int refill_min = 2;    // measured best on GB300 (mandelbulb 1024x1024)
     int drain_lanes = 24;
     int blocks_per_sm = 4;
@@ -297,6 +298,20 @@ int pt_set_march_budget(pt_ctx* ctx, int steps) {
     return PT_OK;
 }
 
+int pt_set_stage_timing(pt_ctx* ctx, int on) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->stage_timing = on != 0;
+    if (ctx->wf) PT_CUDA_TRY(ctx, ctx->wf->set_stage_timing(ctx->stage_timing));
+    return PT_OK;
+}
+
+int pt_get_stage_times(pt_ctx* ctx, double ms[5], uint64_t* iterations) {
+    if (!ctx || !ms) return PT_ERR_INVALID;
+    for (int k = 0; k < PT_STAGE_COUNT; k++) ms[k] = ctx->wf ? ctx->wf->stage_ms[k] : 0.0;
+    if (iterations) *iterations = ctx->wf ? ctx->wf->stage_launches : 0;
+    return PT_OK;
+}
+
 int pt_get_wavefront_tuning(pt_ctx* ctx, pt_wavefront_tuning* out) {
     if (!ctx || !out) return PT_ERR_INVALID;
     out->pool_slots = ctx->pool_cap;
@@ -489,6 +504,7 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     E.set_stream(ctx->stream);
     E.set_march_budget(ctx->march_budget);
     E.set_tuning(ctx->refill_min, ctx->drain_lanes, ctx->blocks_per_sm);
+    if (E.stage_timing != ctx->stage_timing) PT_CUDA_TRY(ctx, E.set_stage_timing(ctx->stage_timing));
     E.args.trace = ctx->trace;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
     PT_CUDA_TRY(ctx, E.reset());

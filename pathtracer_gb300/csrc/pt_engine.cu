@@ -119,6 +119,7 @@ void WfEngine::drop_graph() {
 
 void WfEngine::destroy() {
     drop_graph();
+    set_stage_timing(false);
     if (owns_buffer && buffer) cudaFree(buffer);
     if (owns_host_counters && host_counters) cudaFreeHost(host_counters);
     if (owns_jobs && jobs) delete[] jobs;
@@ -198,7 +199,52 @@ cudaError_t WfEngine::build_graph() {
     return e;
 }
 
+namespace {
+constexpr int kStageEvRounds = 64;
+}
+
+cudaError_t WfEngine::set_stage_timing(bool on) {
+    if (stage_ev) {
+        for (int i = 0; i < kStageEvRounds * 6; i++) cudaEventDestroy(stage_ev[i]);
+        delete[] stage_ev;
+        stage_ev = nullptr;
+    }
+    stage_ev_used = 0;
+    stage_timing = on;
+    for (double& v : stage_ms) v = 0.0;
+    stage_launches = 0;
+    if (!on) return cudaSuccess;
+    stage_ev = new (std::nothrow) cudaEvent_t[kStageEvRounds * 6];
+    if (!stage_ev) return cudaErrorMemoryAllocation;
+    for (int i = 0; i < kStageEvRounds * 6; i++) EN_TRY(cudaEventCreate(&stage_ev[i]));
+    return cudaSuccess;
+}
+
+// Adds the recorded rounds to stage_ms (synchronises on the last event).
+cudaError_t WfEngine::flush_stage_events() {
+    if (!stage_ev_used) return cudaSuccess;
+    EN_TRY(cudaEventSynchronize(stage_ev[stage_ev_used * 6 - 1]));
+    for (int r = 0; r < stage_ev_used; r++) {
+        for (int k = 0; k < PT_STAGE_COUNT; k++) {
+            float ms = 0.0f;
+            EN_TRY(cudaEventElapsedTime(&ms, stage_ev[r * 6 + k], stage_ev[r * 6 + k + 1]));
+            stage_ms[k] += ms;
+        }
+    }
+    stage_launches += (uint64_t)stage_ev_used;
+    stage_ev_used = 0;
+    return cudaSuccess;
+}
+
 cudaError_t WfEngine::run(int n, bool trace) {
+    if (stage_timing && !persistent) {
+        for (int i = 0; i < n; i++) {
+            if (stage_ev_used == kStageEvRounds) EN_TRY(flush_stage_events());
+            EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, &stage_ev[stage_ev_used * 6]));
+            stage_ev_used++;
+        }
+        return flush_stage_events();
+    }
     if (persistent) {
         // One kernel variant covering every pass still in the ring.
         int variant = 0;

@@ -49,6 +49,11 @@ struct WfEngine {
     int sms = 0;
     uint64_t persist_budget = 1ull << 23;
     uint64_t persist_issued = 0;  // samples covered by launches so far
+    // Stage timing (off by default): every iteration is launched without the
+    // graph, bracketed by events; stage_ms accumulates device milliseconds.
+    bool stage_timing = false;
+    double stage_ms[PT_STAGE_COUNT] = {0, 0, 0, 0, 0};
+    uint64_t stage_launches = 0;
 
     // Bytes of device memory for `pool` slots and `max_jobs` ring entries.
     static size_t bytes_for(uint32_t pool, uint32_t max_jobs);
@@ -81,6 +86,8 @@ struct WfEngine {
     void retire(uint32_t new_lo);
     // Launches `n` iterations.
     cudaError_t run(int n, bool trace);
+    // Stage timing on or off (clears the totals).
+    cudaError_t set_stage_timing(bool on);
     // Reads the counters (synchronises the stream).
     cudaError_t read_counters(WfCounters* out);
     // Reads the finished-sample counts of passes [j0, j1) (at most max_jobs;
@@ -98,4 +105,7 @@ struct WfEngine {
    private:
     void drop_graph();
     cudaError_t build_graph();
+    cudaEvent_t* stage_ev = nullptr;  // [64][6] events, reused in rounds of 64 iterations
+    int stage_ev_used = 0;
+    cudaError_t flush_stage_events();
 };

@@ -212,6 +212,18 @@ class Context:
     def set_march_budget(self, steps: int):
         self._check(self._lib.pt_set_march_budget(self._h, steps))
 
+    STAGES = ("isect", "march", "shade", "gen", "book")
+
+    def set_stage_timing(self, on: bool):
+        self._check(self._lib.pt_set_stage_timing(self._h, int(on)))
+
+    def stage_times(self) -> tuple[dict, int]:
+        """Device ms per wavefront stage since stage timing was switched on, and the iterations timed."""
+        ms = (ctypes.c_double * 5)()
+        it = ctypes.c_uint64()
+        self._check(self._lib.pt_get_stage_times(self._h, ms, ctypes.byref(it)))
+        return dict(zip(self.STAGES, list(ms))), it.value
+
     def tuning(self) -> dict:
         t = native.PtWavefrontTuning()
         self._check(self._lib.pt_get_wavefront_tuning(self._h, ctypes.byref(t)))
