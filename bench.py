@@ -82,6 +82,8 @@ def parse_args():
     ap.add_argument("--max-spp", type=int, default=512, help="serve: sample cap per job")
     ap.add_argument("--ref-spp", type=int, default=1024, help="serve: FP64 reference samples per pixel")
     ap.add_argument("--pool-scenes", type=int, default=16, help="serve: scenes in the request pool")
+    ap.add_argument("--iters-per-poll", type=int, default=4, help="serve: engine iterations per server poll")
+    ap.add_argument("--passes-in-flight", type=int, default=1, help="serve: passes in flight per job")
     ap.add_argument("--burst", type=int, default=0,
                     help="serve: N requests all arriving at t=0 instead of the Poisson stream (saturates both arms)")
     ap.add_argument("--jobs", type=int, default=64, help="batch64: jobs per batch")
@@ -492,7 +494,8 @@ def run_serve(args, rank, world):
         push = sc.push_constants(spec.width, spec.height, 1, 1, 1, spec.pathLength)
         pool.append((kind, sc, spec, push))
     srv = Server(local, mode=native.PT_SERVE_BATCHED, spp_per_pass=8, hbm_budget=64 << 30,
-                 pool_slots=args.pool or (1 << 19), iterations_per_poll=4)
+                 pool_slots=args.pool or (1 << 19), iterations_per_poll=args.iters_per_poll,
+                 passes_in_flight=args.passes_in_flight)
     t0 = time.perf_counter()
     for key, (kind, sc, spec, push) in enumerate(pool):
         srv.add_scene(key, sc.pack_ubo(cie), sc.sdf_plugins())
@@ -549,7 +552,8 @@ def run_serve(args, rank, world):
                    "duration_s": None if args.burst else args.duration, "burst_jobs": args.burst or None,
                    "target_rmse": args.target_rmse, "max_spp": args.max_spp, "spp_per_pass": 8,
                    "reference_spp": args.ref_spp, "pool_scenes": args.pool_scenes,
-                   "parallelism": f"replicas x{world}", "hbm_budget_gib": 64},
+                   "parallelism": f"replicas x{world}", "hbm_budget_gib": 64,
+                   "iterations_per_poll": args.iters_per_poll, "passes_in_flight": args.passes_in_flight},
         "serve": {"batched": batched, "plain_megakernel_serial": plain,
                   "throughput_speedup_vs_plain": batched["path_samples_per_s"] / plain["path_samples_per_s"],
                   "p50_speedup_vs_plain": plain["time_to_target_s"]["p50"] / batched["time_to_target_s"]["p50"],

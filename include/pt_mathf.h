@@ -31,8 +31,17 @@
 
 #include <stdint.h>
 
+/* PTM_FN: inlined everywhere.  PTM_CALL: the larger functions; a GPU
+ * translation unit that defines PTM_OUTLINE before including this header
+ * calls them instead of inlining them at every call site (smaller hot loops,
+ * fewer instruction-cache misses).  The arithmetic is the same either way. */
 #if defined(__CUDACC__)
 #define PTM_FN static __device__ __forceinline__
+#if defined(PTM_OUTLINE)
+#define PTM_CALL static __device__ __noinline__
+#else
+#define PTM_CALL static __device__ __forceinline__
+#endif
 #define PTM_FMA(a, b, c) __fmaf_rn((a), (b), (c))
 PTM_FN uint32_t ptm_bits(float f) { return __float_as_uint(f); }
 PTM_FN float ptm_from_bits(uint32_t u) { return __uint_as_float(u); }
@@ -40,6 +49,7 @@ PTM_FN float ptm_from_bits(uint32_t u) { return __uint_as_float(u); }
 #include <math.h>
 #include <string.h>
 #define PTM_FN static inline
+#define PTM_CALL static inline
 #define PTM_FMA(a, b, c) fmaf((a), (b), (c))
 PTM_FN uint32_t ptm_bits(float f) {
     uint32_t u;
@@ -94,12 +104,17 @@ PTM_FN float ptm_from_bits(uint32_t u) {
 #define PTM_A5 7.509485353e-03f
 #define PTM_A6 3.464631364e-02f
 
+typedef struct ptm_sc {
+    float s, c;
+} ptm_sc;
+
 /* sin and cos of x together. */
-PTM_FN void ptm_sincosf(float x, float* s_out, float* c_out) {
+PTM_FN ptm_sc ptm_sincos_inline(float x) {
+    ptm_sc out;
     if (!(x - x == 0.0f)) { /* inf or NaN */
-        *s_out = PTM_NAN;
-        *c_out = PTM_NAN;
-        return;
+        out.s = PTM_NAN;
+        out.c = PTM_NAN;
+        return out;
     }
     const float k = rintf(x * PTM_2_OVER_PI);
     float r = PTM_FMA(-k, PTM_PIO2_1, x);
@@ -126,8 +141,19 @@ PTM_FN void ptm_sincosf(float x, float* s_out, float* c_out) {
         s = -cr;
         c = sr;
     }
-    *s_out = s;
-    *c_out = c;
+    out.s = s;
+    out.c = c;
+    return out;
+}
+
+PTM_CALL ptm_sc ptm_sincos_v(float x) { return ptm_sincos_inline(x); }
+
+PTM_FN float ptm_sinf_inline(float x) { return ptm_sincos_inline(x).s; }
+
+PTM_FN void ptm_sincosf(float x, float* s_out, float* c_out) {
+    const ptm_sc r = ptm_sincos_v(x);
+    *s_out = r.s;
+    *c_out = r.c;
 }
 
 PTM_FN float ptm_sinf(float x) {
@@ -156,7 +182,7 @@ PTM_FN float ptm_scale2(float y, int k) {
     return y * ptm_from_bits((uint32_t)(k + 127) << 23);
 }
 
-PTM_FN float ptm_expf(float x) {
+PTM_CALL float ptm_expf(float x) {
     if (x != x) return x;
     if (x > 88.72283936f) return PTM_INF;
     if (x < -103.9720840f) return 0.0f;
@@ -197,7 +223,7 @@ PTM_FN float ptm_frexp_sqrt2(float x, int* e_out) {
     return m;
 }
 
-PTM_FN float ptm_logf(float x) {
+PTM_FN float ptm_logf_inline(float x) {
     if (x != x) return x;
     if (x < 0.0f) return PTM_NAN;
     if (x == 0.0f) return -PTM_INF;
@@ -207,6 +233,17 @@ PTM_FN float ptm_logf(float x) {
     const float l1p = ptm_log1p_reduced(m - 1.0f);
     const float ef = (float)e;
     return PTM_FMA(ef, PTM_LN2_1, PTM_FMA(ef, PTM_LN2_2, l1p));
+}
+
+PTM_CALL float ptm_logf(float x) { return ptm_logf_inline(x); }
+
+/* |x|^y through exp(y*log|x|), the product's rounding error fed back. */
+PTM_CALL float ptm_pow_exp_log(float ax, float y) {
+    const float L = ptm_logf(ax);
+    const float p = y * L;
+    const float perr = PTM_FMA(y, L, -p);
+    const float e = ptm_expf(p);
+    return PTM_FMA(e, perr, e);
 }
 
 PTM_FN float ptm_powf(float x, float y) {
@@ -238,11 +275,7 @@ PTM_FN float ptm_powf(float x, float y) {
         }
         if (y < 0.0f) r = 1.0f / r;
     } else {
-        const float L = ptm_logf(ax);
-        const float p = y * L;
-        const float perr = PTM_FMA(y, L, -p);
-        const float e = ptm_expf(p);
-        r = PTM_FMA(e, perr, e);
+        r = ptm_pow_exp_log(ax, y);
     }
     return neg ? -r : r;
 }
@@ -254,7 +287,7 @@ PTM_FN float ptm_asin_poly(float x, float z) {
     return PTM_FMA(x * z, A, x);
 }
 
-PTM_FN float ptm_acosf(float x) {
+PTM_CALL float ptm_acosf(float x) {
     if (x != x) return x;
     const float ax = fabsf(x);
     if (ax > 1.0f) return PTM_NAN;

@@ -367,7 +367,7 @@ PT_DI float sdf(float3 p) {
         r = length3(z);
         if (r > 16.0f) break;
     }
-    return 0.5f * ptm_logf(r) * r / dr;
+    return 0.5f * ptm_logf_inline(r) * r / dr;  // inlined: the march loop's hottest call
 }
 PT_DI float sdfmaterial(float3 p, const float* m) {
     const float factor = dot3(p, p);
@@ -399,10 +399,10 @@ PT_DI float sdf(float3 p) {
 
 namespace sdf_terrain {  // sdfs/terrain.glsl
 PT_DI float height(float x) {
-    return ptm_sinf(0.0625f * x) + ptm_sinf(0.125f * (x + 10.0f)) + 0.25f * ptm_sinf(0.25f * x) + 0.125f * ptm_sinf(0.5f * x) +
-           0.25f * ptm_sinf(x) + 0.25f * ptm_sinf(2.0f * x + 1.0f) + 0.125f * ptm_sinf(4.0f * x + 2.0f) +
-           0.0625f * ptm_sinf(8.0f * x + 1.0f) + 0.03125f * ptm_sinf(16.0f * x + 5.0f) + 0.015625f * ptm_sinf(32.0f * x) +
-           0.0078125f * ptm_sinf(64.0f * x);
+    return ptm_sinf_inline(0.0625f * x) + ptm_sinf_inline(0.125f * (x + 10.0f)) + 0.25f * ptm_sinf_inline(0.25f * x) + 0.125f * ptm_sinf_inline(0.5f * x) +
+           0.25f * ptm_sinf_inline(x) + 0.25f * ptm_sinf_inline(2.0f * x + 1.0f) + 0.125f * ptm_sinf_inline(4.0f * x + 2.0f) +
+           0.0625f * ptm_sinf_inline(8.0f * x + 1.0f) + 0.03125f * ptm_sinf_inline(16.0f * x + 5.0f) + 0.015625f * ptm_sinf_inline(32.0f * x) +
+           0.0078125f * ptm_sinf_inline(64.0f * x);
 }
 PT_DI float sdf(float3 p) { return p.y - (height(p.x) + height(p.z)); }
 }  // namespace sdf_terrain

@@ -1,89 +1,13 @@
-// pt_megakernel.cu — the plain per-pixel spectral path tracer for sm_103a.
-//
-// One thread owns one pixel and traces its samplesPerFrame camera paths in
-// order, like main()/Rendering() in src/shader.comp (SC:1509-1533), so the
-// per-pixel sum and the running mean are formed in the reference's order.
-// Inside the thread the path is a small state machine with ONE call site of
-// intersect_all(): a primary ray, then (when next-event estimation needs it)
-// the shadow ray of the same bounce, then the next bounce or the next sample.
-// Lanes of a warp that are at different bounces, samples or ray kinds still
-// execute the scene intersection and SDF march together, instead of
-// splitting into a primary-ray pass and a shadow-ray pass.
+// pt_megakernel.cu — the plain per-pixel spectral path tracer for sm_103a
+// (pt_megakernel_body.cuh): its variants for SDF scenes and traced
+// dispatches, with all math inlined, plus the per-upload rotation setup and
+// the math verification kernel.  The analytic-scene variants live in
+// pt_megakernel_analytic.cu.
 #include <cuda_runtime.h>
 
-#include "pt_megakernel.h"
-#include "pt_path.cuh"
+#include "pt_megakernel_body.cuh"
 
 namespace {
-
-template <bool TRACE, int FEAT>
-__global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constant__ KParams P) {
-    const KScene& S = P.s;
-    const pt_push& pc = P.pc;
-    __shared__ CamInfo camS;
-    if (threadIdx.x == 0 && threadIdx.y == 0) camS = make_camera(pc);
-    __syncthreads();
-
-    const int W = pc.resolution[0], H = pc.resolution[1];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;  // SC:1526 uses '>'; the extra row/column would write out of bounds
-
-    const uint32_t xx = (uint32_t)x;
-    const uint32_t yy = (uint32_t)H - (uint32_t)y;  // SC:1510
-    const float uvx = (2.0f * (float)xx - (float)W) / (float)H;
-    const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
-    const int spf = pc.samplesPerFrame;
-    const int depth = pc.pathLength;
-    const size_t pix = (size_t)y * (size_t)W + (size_t)x;
-
-    float3 sum = f3(0.0f, 0.0f, 0.0f);
-    int k = 0;
-    PathState ps;
-    bool active = false, shadow = false;
-    for (;;) {
-        if (!active) {
-            // Finish sample k-1 (SC:1477-1489, SC:1514-1516) and start sample k.
-            if (k > 0) {
-                const float3 color = sample_color(ps, P.cie);
-                if (TRACE) {
-                    const size_t p = pix * (size_t)spf + (size_t)(k - 1);
-                    if (P.trace.nevents) P.trace.nevents[p] = (uint32_t)ps.bounce;
-                    if (P.trace.colors) {
-                        P.trace.colors[3 * p] = color.x;
-                        P.trace.colors[3 * p + 1] = color.y;
-                        P.trace.colors[3 * p + 2] = color.z;
-                    }
-                }
-                sum = sum + color;
-            }
-            if (k >= spf) break;
-            start_sample(ps, pc, camS, xx, yy, uvx, uvy, k);
-            k++;
-            shadow = false;
-            active = depth > 0;
-            continue;
-        }
-        // ---- the single scene intersection of the loop ----
-        Hit h;
-        h.hitdist = PT_MAXDIST;
-        h.normal = f3(0.0f, 0.0f, 0.0f);
-        h.materialID = 0.0f;
-        h.lightID = -1.0f;
-        int objectID = -1;
-        intersect_all<FEAT>(S, ps.org, shadow ? ps.shDir : ps.dir, h, objectID);
-        const StepResult r =
-            shadow ? shade_shadow<TRACE>(ps, S, objectID, depth) : shade_primary<TRACE>(ps, S, h, objectID, depth);
-        shadow = (r == STEP_SHADOW);
-        if (TRACE && r != STEP_SHADOW) {
-            const size_t p = pix * (size_t)spf + (size_t)(k - 1);
-            const int b = ps.bounce - 1;
-            if (P.trace.events && b < P.trace.cap) P.trace.events[p * (size_t)P.trace.cap + b] = ps.ev;
-        }
-        if (r == STEP_TERMINATED) active = false;
-    }
-    P.accum[pix] = accumulate(pc, sum, P.accum[pix]);
-}
 
 // Per-upload derivation of the rotation matrices of boxes, lenses and cyclides.
 __global__ void rotation_setup_kernel(const __grid_constant__ KScene S, float* __restrict__ out) {
@@ -155,11 +79,8 @@ cudaError_t ptk_launch_megakernel(const KParams* params, bool trace, cudaStream_
         return cudaGetLastError();
     }
     // The smallest variant that covers the scene's primitive classes.
-    switch (pt_feature_variant(params->s.meta.n)) {
-        case 0: megakernel<false, 0><<<grid, block, 0, stream>>>(*params); break;
-        case PT_FEAT_BOX: megakernel<false, PT_FEAT_BOX><<<grid, block, 0, stream>>>(*params); break;
-        case PT_FEAT_ANALYTIC: megakernel<false, PT_FEAT_ANALYTIC><<<grid, block, 0, stream>>>(*params); break;
-        default: megakernel<false, PT_FEAT_ALL><<<grid, block, 0, stream>>>(*params); break;
-    }
+    const int variant = pt_feature_variant(params->s.meta.n);
+    if (variant != PT_FEAT_ALL) return ptk_launch_megakernel_analytic(params, variant, grid, block, stream);
+    megakernel<false, PT_FEAT_ALL><<<grid, block, 0, stream>>>(*params);
     return cudaGetLastError();
 }

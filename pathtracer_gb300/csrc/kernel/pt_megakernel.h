@@ -16,6 +16,10 @@ cudaError_t ptk_rotation_setup(const KScene* scene, float* d_out, cudaStream_t s
 
 // One dispatch of the plain megakernel over params->pc.resolution.
 cudaError_t ptk_launch_megakernel(const KParams* params, bool trace, cudaStream_t stream);
+// The analytic-scene variants (PT_FEAT_* 0, BOX, ANALYTIC), from their own
+// translation unit.
+cudaError_t ptk_launch_megakernel_analytic(const KParams* params, int variant, dim3 grid, dim3 block,
+                                           cudaStream_t stream);
 
 // Evaluates a pt_mathf function over device arrays (verification hook):
 // fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos.

@@ -23,6 +23,9 @@
 // After the last sample, `resolve` sums each pixel's samples in sample order
 // and applies Rendering/Accumulate — the same float operations, in the same
 // order, as the megakernel and the shader, so results are bit-identical.
+// The larger pt_mathf functions are called out of line here (smaller stage
+// and persistent kernels); the SDF plug-ins use inlined math regardless.
+#define PTM_OUTLINE
 #include <cuda_runtime.h>
 
 #include "pt_path.cuh"
