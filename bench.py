@@ -318,7 +318,9 @@ def run_batch(args, rank, world):
     build.build()
     torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
     local = torch.cuda.current_device()
-    jobs, cie = make_jobs(args.jobs, rank * args.jobs)
+    from pathtracer_gb300 import replicas
+
+    jobs, cie = make_jobs(args.jobs, replicas.job_seeds(rank, args.jobs).start)
     pushes = [sc.push_constants(sp.width, sp.height, sp.spp, sp.spp, sp.spp, sp.pathLength) for sc, sp, _, _ in jobs]
     samples = sum(sp.width * sp.height * sp.spp for _, sp, _, _ in jobs)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -432,12 +434,7 @@ def run_batch(args, rank, world):
     st = b.stats()
     b.close()
 
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([b_secs, e2e_secs], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        b_secs, e2e_secs = (float(x) for x in t.tolist())
+    b_secs, e2e_secs = replicas.max_over_ranks([b_secs, e2e_secs])
     value = samples * world / b_secs
     peaks, peak_kind = measured_peaks()
     iters = statistics.mean(biters)
@@ -534,18 +531,16 @@ def run_serve(args, rank, world):
     per_job = [r.samples for r in res_b]
     srv.close()
 
-    if world > 1:
-        import torch.distributed as dist
+    from pathtracer_gb300 import replicas
 
-        tt = torch.tensor([batched["makespan_s"]], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    value = batched["path_samples_per_s"] * world
+    makespan = replicas.max_over_ranks([batched["makespan_s"]])[0]
+    value = replicas.whole_job_rate(batched["samples"], world, makespan)
     span = args.duration if not args.burst else None
     offered = sum(per_job) / span if span else None
     mean_job = sum(per_job) / max(1, len(per_job))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
-        "ms_per_step": 1000.0 * batched["makespan_s"], "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1000.0 * makespan, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, Poisson arrivals)",
         "config": {"workload": SERVE_WORKLOAD + ("_burst" if args.burst else ""),
                    "rate_jobs_per_s": None if args.burst else args.rate,
@@ -638,7 +633,9 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
 
     # Distinct sample indices per rank and per step (replicas, no exchange).
-    base = rank * (args.warmup + args.steps + 8) * ndisp * spf
+    from pathtracer_gb300 import replicas
+
+    base = replicas.frame_base(rank, args.warmup + args.steps, ndisp, spf)
 
     def one_step(step_idx):
         frame = base + step_idx * ndisp * spf
@@ -696,13 +693,8 @@ def main():
         other = {("megakernel" if engine_id == native.PT_ENGINE_WAVEFRONT else "wavefront"):
                  {"value": samples_per_step / (oms / 1000.0), "ms_per_step": oms}}
         ctx.set_engine(engine_id)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = samples_per_step * world / (ms_step / 1000.0)
+    ms_step = replicas.max_over_ranks([ms_step])[0]
+    value = replicas.whole_job_rate(samples_per_step, world, ms_step / 1000.0)
 
     # End to end through the C ABI with host buffers.
     e2e_secs = []
@@ -712,13 +704,8 @@ def main():
                                   frame_offset=base + (args.warmup + args.steps + 2 + i) * ndisp * spf)
         e2e_secs.append(time.perf_counter() - t0)
     e2e_step = statistics.median(e2e_secs)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
-    e2e_value = samples_per_step * world / e2e_step
+    e2e_step = replicas.max_over_ranks([e2e_step])[0]
+    e2e_value = replicas.whole_job_rate(samples_per_step, world, e2e_step)
     h2d = native.UBO_FLOATS * 4
     d2h = W * H * 16 + 9 * 4 * sum(list(scene.counts().values())[:5])
 
