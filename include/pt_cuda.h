@@ -177,6 +177,17 @@ int pt_wait(pt_ctx* ctx, uint64_t timeout_ns);
 int pt_read_accum(pt_ctx* ctx, float* host, size_t bytes);
 /* Uploads a host accumulator (resume a progressive render).  Synchronous. */
 int pt_write_accum(pt_ctx* ctx, const float* host, size_t bytes);
+/* SaveRender's tonemap chain (src/pathtracer.cpp:3491-3518: E->D65,
+ * XYZ->sRGB, max(0), tonemap 0-3, sRGB companding, byte truncation) on the
+ * device.  No reference counterpart as a device call; the same bytes as
+ * pt_export_rgb8 in libpt_host.
+ *   pt_export_rgb8_device: caller's W*H float4 -> W*H*3 bytes, asynchronous
+ *     on `stream` (a cudaStream_t, NULL for the default stream);
+ *   pt_read_rgb8: the context's accumulator into a host buffer of W*H*3
+ *     bytes (3 bytes per pixel cross the bus instead of 16). */
+int pt_export_rgb8_device(const void* d_accum, int width, int height, int tonemap, void* d_rgb, void* stream);
+int pt_read_rgb8(pt_ctx* ctx, int tonemap, uint8_t* host_rgb, size_t bytes);
+
 /* Device address of the accumulator (float4 per pixel), or NULL. */
 void* pt_accum_device_ptr(pt_ctx* ctx);
 

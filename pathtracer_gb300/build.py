@@ -31,6 +31,7 @@ CUDA_SOURCES = [
     "pt_engine.cu",
     "pt_noalloc.cu",
     "pt_batch.cu",
+    "pt_export.cu",
     "pt_sdf_source.cpp",
 ]
 HOST_SOURCES = [

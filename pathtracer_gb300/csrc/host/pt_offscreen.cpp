@@ -9,46 +9,10 @@
 #include <new>
 
 #include "../../../include/pt_host.h"
+#include "../pt_export.cuh"
 #include "pt_scene_model.h"
 
 namespace {
-
-struct v3 {
-    float x, y, z;
-};
-
-// glm: vec3 * mat3 with mat3 given column-major = dot with each column.
-v3 row_times(v3 c, const float m[9]) {
-    return v3{c.x * m[0] + c.y * m[1] + c.z * m[2], c.x * m[3] + c.y * m[4] + c.z * m[5],
-              c.x * m[6] + c.y * m[7] + c.z * m[8]};
-}
-
-// IlluminantEToD65 (Bradford), PT:971-978, and XYZToRGB, PT:980-987.
-const float kEToD65[9] = {0.9531874f, -0.0265906f, 0.0238731f, -0.0382467f, 1.0288406f,
-                          0.0094060f, 0.0026068f,  -0.0030332f, 1.0892565f};
-const float kXYZToRGB[9] = {3.2404542f, -1.5371385f, -0.4985314f, -0.9692660f, 1.8760108f,
-                            0.0415560f, 0.0556434f,  -0.2040259f, 1.0572252f};
-
-float tonemap1(float x, int tonemap) {
-    if (tonemap == 1) x = x / (1.0f + x);  // Reinhard, PT:989-997
-    if (tonemap == 2) {                    // ACES filmic fit, PT:999-1021
-        const float a = 2.51f, b = 0.03f, c = 2.43f, d = 0.59f, e = 0.14f;
-        x = x * (a * x + b) / (x * (c * x + d) + e);
-    }
-    if (tonemap == 3) x = std::exp(-0.25f / x);  // DEUCES, PT:1023-1033
-    return x;
-}
-
-// sRGBCompanding, PT:1061-1071.
-float srgb_companding(float x) {
-    x = (x < 0.0f) ? 0.0f : ((1.0f < x) ? 1.0f : x);  // std::clamp
-    if (x <= 0.0031308f) {
-        x = 12.92f * x;
-    } else {
-        x = 1.055f * std::pow(x, 1.0f / 2.4f) - 0.055f;
-    }
-    return x;
-}
 
 // g(x; mu, s1, s2) of the multi-lobe fit: a Gaussian with a different width
 // on each side of its peak.
@@ -65,17 +29,7 @@ extern "C" {
 int pt_export_rgb8(const float* accum, int width, int height, int tonemap, uint8_t* rgb) {
     if (!accum || !rgb || width <= 0 || height <= 0) return PT_ERR_INVALID;
     const size_t n = (size_t)width * (size_t)height;
-    for (size_t i = 0; i < n; i++) {
-        v3 c{accum[4 * i], accum[4 * i + 1], accum[4 * i + 2]};
-        c = row_times(c, kEToD65);
-        c = row_times(c, kXYZToRGB);
-        c = v3{(c.x < 0.0f) ? 0.0f : c.x, (c.y < 0.0f) ? 0.0f : c.y, (c.z < 0.0f) ? 0.0f : c.z};  // glm::max
-        c = v3{tonemap1(c.x, tonemap), tonemap1(c.y, tonemap), tonemap1(c.z, tonemap)};
-        c = v3{srgb_companding(c.x), srgb_companding(c.y), srgb_companding(c.z)};
-        rgb[3 * i] = (uint8_t)(int)((double)c.x * 255.0);
-        rgb[3 * i + 1] = (uint8_t)(int)((double)c.y * 255.0);
-        rgb[3 * i + 2] = (uint8_t)(int)((double)c.z * 255.0);
-    }
+    for (size_t i = 0; i < n; i++) ptx_pixel(accum[4 * i], accum[4 * i + 1], accum[4 * i + 2], tonemap, rgb + 3 * i);
     return PT_OK;
 }
 

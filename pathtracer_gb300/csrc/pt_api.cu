@@ -45,6 +45,8 @@ struct pt_ctx {
     KScene* d_scene = nullptr;     // device copy for the wavefront kernels
     WfEngine* wf = nullptr;        // wavefront driver (created on first use, grows with the dispatch)
     float4* d_colors = nullptr;    // per-sample colours of the current dispatch
+    uint8_t* d_rgb = nullptr;      // pt_read_rgb8 staging (W*H*3 bytes)
+    size_t rgb_bytes = 0;
     size_t colors_bytes = 0;
     uint32_t last_iterations = 0;
     std::string err;
@@ -90,6 +92,7 @@ cudaError_t sync_device_scene(pt_ctx* ctx) {
 }  // namespace
 
 static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push);
+cudaError_t ptk_export_rgb8(const void* d_accum, int width, int height, int tonemap, void* d_rgb, cudaStream_t stream);
 
 extern "C" {
 
@@ -133,6 +136,7 @@ int pt_destroy(pt_ctx* ctx) {
         delete ctx->wf;
     }
     if (ctx->d_colors) cudaFree(ctx->d_colors);
+    if (ctx->d_rgb) cudaFree(ctx->d_rgb);
     if (ctx->done) cudaEventDestroy(ctx->done);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx->params;
@@ -445,6 +449,27 @@ int pt_write_accum(pt_ctx* ctx, const float* host, size_t bytes) {
     if (!host || bytes < need) return fail(ctx, PT_ERR_INVALID, "pt_write_accum: buffer too small");
     PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     PT_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_accum, host, need, cudaMemcpyHostToDevice, ctx->stream));
+    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
+int pt_read_rgb8(pt_ctx* ctx, int tonemap, uint8_t* host, size_t bytes) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!ctx->d_accum) return fail(ctx, PT_ERR_NO_SCENE, "pt_read_rgb8: no accumulator");
+    const size_t need = (size_t)ctx->width * (size_t)ctx->height * 3;
+    if (!host || bytes < need || tonemap < 0 || tonemap > 3)
+        return fail(ctx, PT_ERR_INVALID, "pt_read_rgb8: bad tonemap or buffer too small");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    if (ctx->rgb_bytes < need) {
+        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->d_rgb) cudaFree(ctx->d_rgb);
+        ctx->d_rgb = nullptr;
+        ctx->rgb_bytes = 0;
+        PT_CUDA_TRY(ctx, cudaMalloc(&ctx->d_rgb, need));
+        ctx->rgb_bytes = need;
+    }
+    PT_CUDA_TRY(ctx, ptk_export_rgb8(ctx->d_accum, ctx->width, ctx->height, tonemap, ctx->d_rgb, ctx->stream));
+    PT_CUDA_TRY(ctx, cudaMemcpyAsync(host, ctx->d_rgb, need, cudaMemcpyDeviceToHost, ctx->stream));
     PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return PT_OK;
 }

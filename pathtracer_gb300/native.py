@@ -242,6 +242,8 @@ CUDA_API = [
     ("pt_read_accum", _i, [_vp, _vp, _sz]),
     ("pt_write_accum", _i, [_vp, _vp, _sz]),
     ("pt_accum_device_ptr", _vp, [_vp]),
+    ("pt_export_rgb8_device", _i, [_vp, _i, _i, _i, _vp, _vp]),
+    ("pt_read_rgb8", _i, [_vp, _i, _vp, _sz]),
     ("pt_stream", _vp, [_vp]),
     ("pt_set_stream", _i, [_vp, _vp]),
     ("pt_last_error", ctypes.c_char_p, [_vp]),

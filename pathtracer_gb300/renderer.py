@@ -187,6 +187,12 @@ class Context:
         self._check(self._lib.pt_read_accum(self._h, native.ptr(out), out.nbytes))
         return out
 
+    def read_rgb8(self, tonemap: int = 3) -> np.ndarray:
+        """The accumulator through SaveRender's tonemap chain on the device."""
+        out = np.empty((self.height, self.width, 3), np.uint8)
+        self._check(self._lib.pt_read_rgb8(self._h, tonemap, native.ptr(out), out.nbytes))
+        return out
+
     def write_accum(self, data: np.ndarray):
         data = np.ascontiguousarray(data, np.float32)
         self._check(self._lib.pt_write_accum(self._h, native.ptr(data), data.nbytes))
