@@ -463,6 +463,22 @@ static __device__ __noinline__ float scene_sdf_material(const KScene& S, float3 
 }
 
 // RayIntersectAABB, SC:278-287.
+// SDFMATERIAL at the end of a march.  When the march converged
+// (|SDF(p)| < 1e-4 over the set) and the set holds one live plug-in, that
+// plug-in is the closest one (its distance is the set's, far below
+// PT_MAXDIST), so the reference's selection (SC:704-719) reduces to its
+// sdfmaterial at p without evaluating the distance again.  Otherwise the
+// full selection runs.
+PT_DI float scene_sdf_material_hit(const KScene& S, float3 p, uint32_t set1, bool converged) {
+    const uint32_t bits = set1 & ((S.meta.nplug >= 32) ? 0xFFFFFFFFu : ((1u << S.meta.nplug) - 1u));
+    if (converged && bits != 0u && (bits & (bits - 1u)) == 0u) {
+        const int i = __ffs(bits) - 1;
+        const pt_sdf_plugin pl = S.plug[i];
+        if (pl.kind != PT_SDF_NONE) return plugin_material(pl, p - sdf_pos(S, i));
+    }
+    return scene_sdf_material(S, p, set1);
+}
+
 PT_DI float2 ray_aabb(float3 origin, float3 invdir, float3 pos, float3 size) {
     const float3 lo = origin - pos;
     const float3 tMin0 = fma3(size, f3(-0.5f, -0.5f, -0.5f), -lo) * invdir;
@@ -523,6 +539,7 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
         return false;
     }
     const float k = sign_glsl(scene_sdf_cold(S, org, set1));
+    bool converged = false;
 #pragma unroll 1
     for (int i = 0; i < 512; i++) {
         const float radius = scene_sdf(S, p, set1);
@@ -534,7 +551,10 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
             p = fma3s(dir, t, org);
             continue;
         }
-        if (fabsf(radius) < 1e-4f) break;
+        if (fabsf(radius) < 1e-4f) {
+            converged = true;
+            break;
+        }
         if (t > tMinMax.y) {
             points += 1;
         } else {
@@ -571,7 +591,7 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
         const float nz = scene_sdf_cold(S, f3(p.x + 0.0f, p.y + 0.0f, p.z + e), set1) -
                          scene_sdf_cold(S, f3(p.x - 0.0f, p.y - 0.0f, p.z - e), set1);
         h.normal = normalize3(f3(nx, ny, nz));
-        h.materialID = scene_sdf_material(S, p, set1);
+        h.materialID = scene_sdf_material_hit(S, p, set1, converged);
         h.lightID = -1.0f;
         return true;
     }

@@ -256,6 +256,14 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     int steps = 0;
     // Draining only pays while the queue holds more rays than the grid has lanes.
     const bool many = n >= 2u * gridDim.x * blockDim.x;
+    // Queue entries per claim: up to 32 while the queue is long, 1 near its end.
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    const uint32_t chunk = max(1u, min(32u, n / (4u * nwarps)));
+    uint32_t cbase = 0, cleft = 0;  // warp-uniform: unused entries of the warp's claim
+    // Finished rays are staged per warp and appended to the shade queue 32 at a time.
+    __shared__ uint32_t staged[kStageThreads / 32][64];
+    uint32_t nstaged = 0;  // warp-uniform
+    const int wib = (int)(threadIdx.x >> 5);
 
     uint32_t slot = 0;
     const KScene* Sp = nullptr;
@@ -267,20 +275,35 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     float2 tmm = make_float2(0.0f, 0.0f);
     uint32_t set1 = 0;
     int points = 0, iter = 0;
+    bool converged = false;  // the march of this lane's ray ended on |SDF| < 1e-4
     const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
 
     for (;;) {
         // Refill lanes that have no ray (warp-aggregated fetch), once at
         // least refill_min of them are idle or the warp has none left.
+        // Queue entries come from a chunk the warp claimed with one atomic
+        // (cbase, cleft: warp-uniform); a refill that needs more than the
+        // chunk holds claims the next chunk.
         const bool need = (phase == MP_EMPTY) && !exhausted;
         const unsigned mneed = __ballot_sync(0xffffffffu, need);
         if (mneed && (__popc(mneed) >= refill_min || __ballot_sync(0xffffffffu, phase != MP_EMPTY) == 0)) {
-            const int leader = __ffs(mneed) - 1;
-            uint32_t b = 0;
-            if (lane == leader) b = atomicAdd(&C.march_cursor, (uint32_t)__popc(mneed));
-            b = __shfl_sync(0xffffffffu, b, leader);
+            const uint32_t want = (uint32_t)__popc(mneed);
+            const uint32_t from_old = min(want, cleft);  // entries left in the current chunk
+            const uint32_t old_base = cbase;
+            uint32_t nb = 0;
+            if (want > from_old) {
+                const uint32_t ncount = max(chunk, want - from_old);
+                if (lane == 0) nb = atomicAdd(&C.march_cursor, ncount);
+                nb = __shfl_sync(0xffffffffu, nb, 0);
+                cbase = nb + (want - from_old);
+                cleft = ncount - (want - from_old);
+            } else {
+                cbase += want;
+                cleft -= want;
+            }
             if (need) {
-                const uint32_t idx = b + (uint32_t)__popc(mneed & ((1u << lane) - 1u));
+                const uint32_t rank = (uint32_t)__popc(mneed & ((1u << lane) - 1u));
+                const uint32_t idx = (rank < from_old) ? old_base + rank : nb + (rank - from_old);
                 if (idx < n) {
                     slot = qin[idx];
                     Sp = A.jobs[slot_job(v, slot)].scene;
@@ -291,6 +314,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                     dir = f3(d.x, d.y, d.z);
                     hitdist = v.h0[slot].x;
                     steps = 0;
+                    converged = false;
                     // A ray from isect (flag bit clear: start with the sign
                     // probe) or one suspended by an earlier launch.
                     const uint32_t saved = M.m2[slot];
@@ -347,6 +371,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                 p = fma3s(dir, t, org);
             } else if (fabsf(radius) < 1e-4f) {
                 exitLoop = true;
+                converged = true;
             } else {
                 if (t > tmm.y) {
                     points += 1;
@@ -414,13 +439,38 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
 
         if (finished && hit) {
             const float3 nrm = normalize3(nv);
-            const float mat = scene_sdf_material(*Sp, p, set1);
+            const float mat = scene_sdf_material_hit(*Sp, p, set1, converged);
             v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
             v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
         }
-        q_push(A.q_shade, &C.n_shade, slot, finished);
+        const unsigned mfin = __ballot_sync(0xffffffffu, finished);
+        if (mfin) {
+            if (finished) staged[wib][nstaged + (uint32_t)__popc(mfin & ((1u << lane) - 1u))] = slot;
+            nstaged += (uint32_t)__popc(mfin);  // < 64: it was < 32 before
+            if (nstaged >= 32) {
+                __syncwarp();
+                uint32_t b = 0;
+                if (lane == 0) b = atomicAdd(&C.n_shade, 32u);
+                b = __shfl_sync(0xffffffffu, b, 0);
+                A.q_shade[b + (uint32_t)lane] = staged[wib][lane];
+                const uint32_t rest = nstaged - 32;
+                const uint32_t moved = ((uint32_t)lane < rest) ? staged[wib][32 + lane] : 0u;
+                __syncwarp();
+                if ((uint32_t)lane < rest) staged[wib][lane] = moved;
+                __syncwarp();
+                nstaged = rest;
+            }
+        }
         q_push(A.q_march[cur ^ 1u], &C.n_march[cur ^ 1u], slot, suspend);
         if (finished || suspend) phase = MP_EMPTY;
+    }
+    // The staged remainder.
+    __syncwarp();
+    if (nstaged) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(&C.n_shade, nstaged);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if ((uint32_t)lane < nstaged) A.q_shade[b + (uint32_t)lane] = staged[wib][lane];
     }
 }
 
