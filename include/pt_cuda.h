@@ -237,7 +237,7 @@ int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float
  * complete.  No per-path trace. */
 #define PT_NOALLOC_SCRATCH_BYTES (32u << 20)
 #define PT_NOALLOC_MAX_SAMPLES (1u << 20)
-#define PT_NOALLOC_POOL_SLOTS (1u << 16)
+#define PT_NOALLOC_POOL_SLOTS (15u << 12) /* 61,440 */
 int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins, const pt_push* push,
                         float* d_accum, void* stream);
 

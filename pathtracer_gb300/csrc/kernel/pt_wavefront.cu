@@ -203,13 +203,14 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool valid = i < n;
-        bool march = false;
+        bool march = false, shadow_ray = false;
         uint32_t slot = 0;
         if (valid) {
             slot = q[i];
             const KScene& S = *A.jobs[slot_job(v, slot)].scene;
             const float4 o = v.s0[slot];
             const uint32_t flags = v.s8[slot].y;
+            shadow_ray = (flags & kShadowFlag) != 0;
             const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
             const float3 org = f3(o.x, o.y, o.z), dir = f3(d.x, d.y, d.z);
             Hit h;
@@ -236,12 +237,46 @@ __global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant_
             v.h1[slot] = make_float4(h.normal.x, h.normal.y, h.normal.z, 0.0f);
         }
         q_push(A.q_march[cur], &C.n_march[cur], slot, valid && march);
-        q_push(A.q_shade, &C.n_shade, slot, valid && !march);
+        q_push(A.q_shade, &C.n_shade, slot, valid && !march && !shadow_ray);
+        q_push(A.q_shadow, &C.n_shadow, slot, valid && !march && shadow_ray);
     }
 }
 
 // SphereTracing (SC:779-860) with one SDF evaluation per loop iteration per lane.
 enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NORMAL5 = 8 };
+
+// Warp-staged queue appends: lanes with pred add `value` to a per-warp
+// buffer of 64 in shared memory (count warp-uniform); every 32 entries go to
+// the queue with one atomic and one coalesced store.  Called by all 32 lanes.
+PT_DI void stage_push(uint32_t* buf, uint32_t& count, bool pred, uint32_t value, uint32_t* queue, uint32_t* qcount,
+                      int lane) {
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return;
+    if (pred) buf[count + (uint32_t)__popc(m & ((1u << lane) - 1u))] = value;
+    count += (uint32_t)__popc(m);  // < 64: it was < 32 before
+    if (count < 32) return;
+    __syncwarp();
+    uint32_t b = 0;
+    if (lane == 0) b = atomicAdd(qcount, 32u);
+    b = __shfl_sync(0xffffffffu, b, 0);
+    queue[b + (uint32_t)lane] = buf[lane];
+    const uint32_t rest = count - 32;
+    const uint32_t moved = ((uint32_t)lane < rest) ? buf[32 + lane] : 0u;
+    __syncwarp();
+    if ((uint32_t)lane < rest) buf[lane] = moved;
+    __syncwarp();
+    count = rest;
+}
+
+// Appends what stage_push still holds.  Called by all 32 lanes.
+PT_DI void stage_flush(uint32_t* buf, uint32_t count, uint32_t* queue, uint32_t* qcount, int lane) {
+    __syncwarp();
+    if (!count) return;
+    uint32_t b = 0;
+    if (lane == 0) b = atomicAdd(qcount, count);
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if ((uint32_t)lane < count) queue[b + (uint32_t)lane] = buf[lane];
+}
 
 __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
@@ -260,9 +295,10 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const uint32_t chunk = max(1u, min(32u, n / (4u * nwarps)));
     uint32_t cbase = 0, cleft = 0;  // warp-uniform: unused entries of the warp's claim
-    // Finished rays are staged per warp and appended to the shade queue 32 at a time.
-    __shared__ uint32_t staged[kStageThreads / 32][64];
-    uint32_t nstaged = 0;  // warp-uniform
+    // Finished rays are staged per warp and kind and appended to the shade
+    // queues 32 at a time.
+    __shared__ uint32_t staged[kStageThreads / 32][2][64];
+    uint32_t nstaged[2] = {0u, 0u};  // warp-uniform: primary hits, shadow results
     const int wib = (int)(threadIdx.x >> 5);
 
     uint32_t slot = 0;
@@ -276,6 +312,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     uint32_t set1 = 0;
     int points = 0, iter = 0;
     bool converged = false;  // the march of this lane's ray ended on |SDF| < 1e-4
+    bool shadow_ray = false;
     const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
 
     for (;;) {
@@ -309,7 +346,8 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
                     Sp = A.jobs[slot_job(v, slot)].scene;
                     const float4 o = v.s0[slot];
                     const uint32_t flags = v.s8[slot].y;
-                    const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
+                    shadow_ray = (flags & kShadowFlag) != 0;
+                    const float4 d = shadow_ray ? v.s2[slot] : v.s1[slot];
                     org = f3(o.x, o.y, o.z);
                     dir = f3(d.x, d.y, d.z);
                     hitdist = v.h0[slot].x;
@@ -443,35 +481,14 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
             v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
             v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
         }
-        const unsigned mfin = __ballot_sync(0xffffffffu, finished);
-        if (mfin) {
-            if (finished) staged[wib][nstaged + (uint32_t)__popc(mfin & ((1u << lane) - 1u))] = slot;
-            nstaged += (uint32_t)__popc(mfin);  // < 64: it was < 32 before
-            if (nstaged >= 32) {
-                __syncwarp();
-                uint32_t b = 0;
-                if (lane == 0) b = atomicAdd(&C.n_shade, 32u);
-                b = __shfl_sync(0xffffffffu, b, 0);
-                A.q_shade[b + (uint32_t)lane] = staged[wib][lane];
-                const uint32_t rest = nstaged - 32;
-                const uint32_t moved = ((uint32_t)lane < rest) ? staged[wib][32 + lane] : 0u;
-                __syncwarp();
-                if ((uint32_t)lane < rest) staged[wib][lane] = moved;
-                __syncwarp();
-                nstaged = rest;
-            }
-        }
+        stage_push(staged[wib][0], nstaged[0], finished && !shadow_ray, slot, A.q_shade, &C.n_shade, lane);
+        stage_push(staged[wib][1], nstaged[1], finished && shadow_ray, slot, A.q_shadow, &C.n_shadow, lane);
         q_push(A.q_march[cur ^ 1u], &C.n_march[cur ^ 1u], slot, suspend);
         if (finished || suspend) phase = MP_EMPTY;
     }
-    // The staged remainder.
-    __syncwarp();
-    if (nstaged) {
-        uint32_t b = 0;
-        if (lane == 0) b = atomicAdd(&C.n_shade, nstaged);
-        b = __shfl_sync(0xffffffffu, b, 0);
-        if ((uint32_t)lane < nstaged) A.q_shade[b + (uint32_t)lane] = staged[wib][lane];
-    }
+    // The staged remainders.
+    stage_flush(staged[wib][0], nstaged[0], A.q_shade, &C.n_shade, lane);
+    stage_flush(staged[wib][1], nstaged[1], A.q_shadow, &C.n_shadow, lane);
 }
 
 // Adds 1 to jobs[job].finished for every lane with pred, one atomic per
@@ -484,27 +501,118 @@ PT_DI void count_finished(WfJob* __restrict__ jobs, uint32_t job, bool pred) {
         atomicAdd(&jobs[job].finished, (uint32_t)__popc(same & active));
 }
 
+// A primary hit reads neither the shadow-ray fields (s2, s3) nor the BRDF
+// (s4): it writes them.
+PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uint32_t& flags, uint32_t& sample,
+                            uint32_t& job) {
+    const float4 a = v.s0[slot], b = v.s1[slot];
+    ps.org = f3(a.x, a.y, a.z);
+    ps.mis = a.w;
+    ps.dir = f3(b.x, b.y, b.z);
+    ps.brdfPdf = b.w;
+    ps.shDir = f3(0.0f, 0.0f, 0.0f);
+    ps.cosL = 0.0f;
+    ps.nrm = f3(0.0f, 0.0f, 0.0f);
+    ps.lightPdf = 0.0f;
+    ps.brdf = f4s(0.0f);
+    ps.rr = v.s5[slot];
+    ps.radiance = v.s6[slot];
+    ps.l = v.s7[slot];
+    const uint4 m = v.s8[slot];
+    ps.seed = m.x;
+    flags = m.y;
+    ps.bounce = (int)(m.y & 0x3fffffffu);
+    sample = m.z;
+    ps.shObj = (int)m.w;
+    const float4 e = v.s9[slot];
+    ps.shLightID = e.x;
+    ps.ev = __float_as_uint(e.y);
+    job = __float_as_uint(e.z);
+}
+
+// After a shadow-ray result only the throughput, the radiance, the RNG and
+// bounce word and (traced) the event word change.
+PT_DI void store_after_shadow(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t sample, uint32_t job,
+                              bool trace) {
+    v.s5[slot] = ps.rr;
+    v.s6[slot] = ps.radiance;
+    v.s8[slot] = make_uint4(ps.seed, (uint32_t)ps.bounce & 0x3fffffffu, sample, (uint32_t)ps.shObj);
+    if (trace) v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
+}
+
+// The end of a shaded step: trace records, the sample's colour when the
+// path ended, the queues.
+template <bool TRACE>
+PT_DI void finish_shade(const WfArgs& A, const WfJob& J, const PathState& ps, StepResult r, uint32_t sample,
+                        bool& freed) {
+    const pt_push& pc = J.pc;
+    if (TRACE && r != STEP_SHADOW && A.trace.events) {
+        const size_t p = trace_index(pc, sample);
+        const int b = ps.bounce - 1;
+        if (b < A.trace.cap) A.trace.events[p * (size_t)A.trace.cap + b] = ps.ev;
+    }
+    if (r == STEP_TERMINATED) {
+        const float3 col = sample_color(ps, J.cie);
+        J.colors[sample] = make_float4(col.x, col.y, col.z, 0.0f);
+        if (TRACE) {
+            const size_t p = trace_index(pc, sample);
+            if (A.trace.nevents) A.trace.nevents[p] = (uint32_t)ps.bounce;
+            if (A.trace.colors) {
+                A.trace.colors[3 * p] = col.x;
+                A.trace.colors[3 * p + 1] = col.y;
+                A.trace.colors[3 * p + 2] = col.z;
+            }
+        }
+        freed = true;
+    }
+}
+
+// Shading in two passes over two queues, so each warp runs one kind of step
+// and moves only the state that kind reads and writes: shadow-ray results
+// (the light sample's contribution, then the bounce's end), then primary
+// hits (emission or BRDF and light sampling).
 template <bool TRACE>
 __global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
-    const uint32_t n = C.n_shade;
     const uint32_t nxt = C.cur ^ 1u;
     const PoolView v = view(A);
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t ns = C.n_shadow;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < ns; base += stride) {
         const uint32_t i = base + threadIdx.x;
-        const bool valid = i < n;
+        const bool valid = i < ns;
+        uint32_t slot = 0, job = 0;
+        bool again = false, freed = false;
+        if (valid) {
+            slot = A.q_shadow[i];
+            PathState ps;
+            uint32_t flags, sample;
+            load_state(v, slot, ps, flags, sample, job);
+            const WfJob& J = A.jobs[job];
+            const int objectID = __float_as_int(v.h0[slot].w);
+            const StepResult r = shade_shadow<TRACE>(ps, *J.scene, objectID, J.pc.pathLength);
+            finish_shade<TRACE>(A, J, ps, r, sample, freed);
+            if (!freed) {
+                store_after_shadow(v, slot, ps, sample, job, TRACE);
+                again = true;
+            }
+        }
+        q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, again);
+        q_push(A.q_free, &C.n_free, slot, freed);
+        count_finished(A.jobs, job, freed);
+    }
+    const uint32_t np = C.n_shade;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < np;
         uint32_t slot = 0, job = 0;
         bool again = false, freed = false;
         if (valid) {
             slot = A.q_shade[i];
             PathState ps;
             uint32_t flags, sample;
-            load_state(v, slot, ps, flags, sample, job);
+            load_for_primary(v, slot, ps, flags, sample, job);
             const WfJob& J = A.jobs[job];
-            const KScene& S = *J.scene;
-            const pt_push& pc = J.pc;
-            const int depth = pc.pathLength;
             const float4 h0 = v.h0[slot], h1 = v.h1[slot];
             Hit h;
             h.hitdist = h0.x;
@@ -512,28 +620,21 @@ __global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant_
             h.lightID = h0.z;
             h.normal = f3(h1.x, h1.y, h1.z);
             const int objectID = __float_as_int(h0.w);
-            const StepResult r = (flags & kShadowFlag) ? shade_shadow<TRACE>(ps, S, objectID, depth)
-                                                       : shade_primary<TRACE>(ps, S, h, objectID, depth);
-            if (TRACE && r != STEP_SHADOW && A.trace.events) {
-                const size_t p = trace_index(pc, sample);
-                const int b = ps.bounce - 1;
-                if (b < A.trace.cap) A.trace.events[p * (size_t)A.trace.cap + b] = ps.ev;
-            }
-            if (r == STEP_TERMINATED) {
-                const float3 col = sample_color(ps, J.cie);
-                J.colors[sample] = make_float4(col.x, col.y, col.z, 0.0f);
-                if (TRACE) {
-                    const size_t p = trace_index(pc, sample);
-                    if (A.trace.nevents) A.trace.nevents[p] = (uint32_t)ps.bounce;
-                    if (A.trace.colors) {
-                        A.trace.colors[3 * p] = col.x;
-                        A.trace.colors[3 * p + 1] = col.y;
-                        A.trace.colors[3 * p + 2] = col.z;
-                    }
-                }
-                freed = true;
-            } else {
-                store_state(v, slot, ps, (r == STEP_SHADOW) ? kShadowFlag : 0u, sample, job);
+            const StepResult r = shade_primary<TRACE>(ps, *J.scene, h, objectID, J.pc.pathLength);
+            finish_shade<TRACE>(A, J, ps, r, sample, freed);
+            if (!freed) {
+                // everything but the wavelengths (s7), which a bounce never changes
+                v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
+                v.s1[slot] = make_float4(ps.dir.x, ps.dir.y, ps.dir.z, ps.brdfPdf);
+                v.s2[slot] = make_float4(ps.shDir.x, ps.shDir.y, ps.shDir.z, ps.cosL);
+                v.s3[slot] = make_float4(ps.nrm.x, ps.nrm.y, ps.nrm.z, ps.lightPdf);
+                v.s4[slot] = ps.brdf;
+                v.s5[slot] = ps.rr;
+                v.s6[slot] = ps.radiance;
+                v.s8[slot] = make_uint4(ps.seed, ((r == STEP_SHADOW) ? kShadowFlag : 0u) |
+                                                     ((uint32_t)ps.bounce & 0x3fffffffu),
+                                        sample, (uint32_t)ps.shObj);
+                v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
                 again = true;
             }
         }
@@ -542,7 +643,6 @@ __global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant_
         count_finished(A.jobs, job, freed);
     }
 }
-
 
 // Persistent mode: the megakernel's per-thread path loop (one intersect_all
 // call site per iteration for primary and shadow rays alike) over the samples
@@ -658,6 +758,7 @@ __global__ void wf_book(const __grid_constant__ WfArgs A) {
     C.cur ^= 1u;
     C.march_cursor = 0;
     C.n_shade = 0;
+    C.n_shadow = 0;
     C.iterations += 1;
     C.live = pool - C.n_free;
 }
@@ -670,7 +771,7 @@ __global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_fr
         C.n_isect[0] = C.n_isect[1] = 0;
         C.n_march[0] = C.n_march[1] = 0;
         C.cur = 0;
-        C.march_cursor = C.n_shade = 0;
+        C.march_cursor = C.n_shade = C.n_shadow = 0;
         C.n_free = pool;
         C.next_sample = 0;
         C.total = 0;

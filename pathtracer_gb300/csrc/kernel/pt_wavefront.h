@@ -46,7 +46,7 @@ struct WfCounters {
     uint32_t n_march[2];  // the two MARCH queues (current, next)
     uint32_t cur;
     uint32_t march_cursor;
-    uint32_t n_shade;
+    uint32_t n_shade;      // primary-ray hits to shade
     uint32_t n_free;
     uint64_t next_sample;  // global samples started so far
     uint64_t total;        // global samples of every pass in the table (written by the bookkeeping kernel)
@@ -55,6 +55,8 @@ struct WfCounters {
     uint32_t job_lo;       // oldest pass that may still hold unfinished samples
     uint32_t job_hi;       // passes added so far
     uint64_t pk_end;       // persistent mode: end of the sample range of the current launch
+    uint32_t n_shadow;     // shadow-ray results to shade
+    uint32_t pad;
 };
 
 // Everything here is fixed between resets, so a captured chain of iterations
@@ -65,7 +67,8 @@ struct WfArgs {
     WfPool pool;
     uint32_t* q_isect[2];
     uint32_t* q_march[2];
-    uint32_t* q_shade;
+    uint32_t* q_shade;   // primary-ray hits
+    uint32_t* q_shadow;  // shadow-ray results
     uint32_t* q_free;
     WfCounters* counters;
     KTrace trace;  // single-job dispatches only
@@ -76,7 +79,7 @@ struct WfArgs {
 };
 
 // Bytes of the engine's device buffers for a pool of `pool` slots.
-inline size_t ptk_wavefront_pool_bytes(uint32_t pool) { return (size_t)pool * (14 * 16 + 7 * 4) + 32 * 256; }
+inline size_t ptk_wavefront_pool_bytes(uint32_t pool) { return (size_t)pool * (14 * 16 + 8 * 4) + 32 * 256; }
 
 cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream);
 // Writes pass number `index` (camera derived on the device) and publishes

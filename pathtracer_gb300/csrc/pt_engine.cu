@@ -41,6 +41,7 @@ size_t layout(uintptr_t base, uint32_t pool, uint32_t max_jobs, WfArgs* a) {
     a->q_march[0] = take<uint32_t>(p, pool);
     a->q_march[1] = take<uint32_t>(p, pool);
     a->q_shade = take<uint32_t>(p, pool);
+    a->q_shadow = take<uint32_t>(p, pool);
     a->q_free = take<uint32_t>(p, pool);
     a->counters = take<WfCounters>(p, 1);
     a->jobs = take<WfJob>(p, max_jobs);
