@@ -12,6 +12,7 @@ dispatches, and the read-back of the 16 MiB accumulator each step.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
   python bench.py --workload batch64 [--steps K] [--warmup W]
   python bench.py --workload serve [--rate R] [--duration T]
+  python bench.py --workload progressive [--spp N] [--ref-spp M]
 
 --workload batch64 is the mixed-job batch: 64 seeded sphere-scene jobs
 (pt_scene_generate, seeds 0-63: 128^2-1024^2, 4-256 spp, depth 8; 1.80 G
@@ -27,6 +28,13 @@ most the target (or the sample cap), batched (continuous batching under an
 HBM budget) and then plain (one job at a time through the megakernel), on
 the same trace.  Both arms render the same passes of every job, so each
 job's error is identical between them.
+
+--workload progressive is the mixed-SDF config in its reference-expressible
+form: menger sponge + sine terrain + a sphere under a sphere light
+(pathtracer_gb300/scenes/menger_terrain.json), 1920x1080, rendered in 16-spp
+passes to --spp samples per pixel at depth 12, by the staged wavefront engine
+and by the plain megakernel, with each pass's relative RMSE against an FP64
+reference (--ref-spp samples per pixel, FP32 paths, FP64 sums).
 
 Under torchrun each rank renders its own replica (distinct sample indices,
 no exchange): weak scaling.  --impl reference times the CPU restatement of
@@ -75,7 +83,8 @@ def parse_args():
     ap.add_argument("--blocks", type=int, default=0, help="wavefront stage blocks per SM (0: default)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
-    ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64", "serve"])
+    ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64", "serve", "progressive"])
+    ap.add_argument("--pass-spp", type=int, default=16, help="progressive: samples per pixel per pass")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: Poisson arrivals per second")
     ap.add_argument("--duration", type=float, default=30.0, help="serve: seconds of arrivals")
     ap.add_argument("--target-rmse", type=float, default=0.02, help="serve: relative RMSE target per job")
@@ -570,6 +579,102 @@ def run_serve(args, rank, world):
     return 0
 
 
+PROGRESSIVE_WORKLOAD = "menger_terrain_1920x1080_16spp_passes_depth12"
+
+
+def run_progressive(args, rank, world):
+    """Progressive rendering in 16-spp passes, wavefront vs plain, error per pass."""
+    import torch
+
+    from pathtracer_gb300 import Batch, Context, Scene, build, cie_analytic, native, replicas
+
+    build.build()
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
+    local = torch.cuda.current_device()
+    W, H, depth, spf = 1920, 1080, 12, args.pass_spp
+    npass = max(1, args.spp // spf)
+    scene = Scene.load(os.path.join(ROOT, "pathtracer_gb300", "scenes", "menger_terrain.json"))
+    cie = cie_analytic()
+    ubo, plugins = scene.pack_ubo(cie), scene.sdf_plugins()
+    base = replicas.frame_base(rank, 1, 1, args.spp)  # distinct samples per replica
+
+    b = Batch(local, pool_slots=args.pool or (1 << 19), max_passes=4096)
+    b.set_route(native.PT_BATCH_ROUTE_STAGED)
+    sid = b.add_scene(ubo, plugins)
+    ref = b.add_target(W, H, native.PT_TARGET_FP64)
+    t0 = time.perf_counter()
+    for k in range(max(1, args.ref_spp // 64)):
+        b.add_pass(sid, ref, scene.push_constants(W, H, (1 << 30) + (k + 1) * 64, 64, 64, depth))
+        if b.pending() >= 64:
+            b.run()
+    b.run()
+    ref_secs = time.perf_counter() - t0
+
+    def push_k(k):
+        # frame = currentSamples = k*spf: the reference's offscreen loop
+        return scene.push_constants(W, H, k * spf, k * spf, spf, depth)
+
+    # Wavefront: every pass through the batch, error checked after each.
+    stream = torch.cuda.ExternalStream(b.stream())
+    tgt = b.add_target(W, H)
+    wf_err, wf_secs = [], 0.0
+    with ClockSampler(local) as clk:
+        for k in range(1, npass + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.add_pass(sid, tgt, push_k(k))
+            b.run()
+            e1.record(stream)
+            e1.synchronize()
+            wf_secs += e0.elapsed_time(e1) / 1000.0
+            wf_err.append(b.rmse(tgt, ref))
+    wf_img = b.read_target(tgt)
+
+    # Plain megakernel: the same passes through pt_dispatch.
+    ctx = Context(local)
+    ctx.set_engine(native.PT_ENGINE_MEGAKERNEL)
+    ctx.bind(scene, cie)
+    ctx.resize_accum(W, H)
+    cstream = torch.cuda.ExternalStream(ctx.stream())
+    pl_err, pl_secs = [], 0.0
+    for k in range(1, npass + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(cstream)
+        ctx.dispatch(push_k(k))
+        e1.record(cstream)
+        e1.synchronize()
+        pl_secs += e0.elapsed_time(e1) / 1000.0
+        pl_err.append(b.rmse_image(ctx.accum_device_ptr(), W, H, ref))
+    identical = bool(np.array_equal(ctx.read_accum().view(np.uint32), wf_img.view(np.uint32)))
+    ctx.close()
+    b.close()
+
+    samples = W * H * spf * npass
+    wf_secs, pl_secs = replicas.max_over_ranks([wf_secs, pl_secs])
+    value = replicas.whole_job_rate(samples, world, wf_secs)
+    peaks, peak_kind = measured_peaks()
+    every = max(1, npass // 8)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": npass, "warmup": 0,
+        "ms_per_step": 1000.0 * wf_secs / npass, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": PROGRESSIVE_WORKLOAD, "resolution": [W, H], "spp": spf * npass, "pass_spp": spf,
+                   "max_depth": depth, "reference_spp": args.ref_spp, "parallelism": f"replicas x{world}"},
+        "progressive": {"wavefront": {"value": samples / wf_secs, "seconds": wf_secs},
+                        "plain_megakernel": {"value": samples / pl_secs, "seconds": pl_secs},
+                        "speedup_vs_plain": pl_secs / wf_secs, "results_identical": identical,
+                        "rmse_per_pass": {str((k + 1) * spf): wf_err[k] for k in range(every - 1, npass, every)},
+                        "rmse_identical_per_pass": wf_err == pl_err, "final_rmse": wf_err[-1],
+                        "reference_render_s": ref_secs},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "passes on a resident scene; each pass's error is reduced on the device"},
+        "gpu_launches": None, "roofline": None, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     faulthandler.enable()
     args = parse_args()
@@ -583,8 +688,8 @@ def main():
 
             torch.cuda.set_device(local)
         dist.init_process_group(backend=backend)
-    if args.workload in ("batch64", "serve"):
-        rc = run_batch(args, rank, world) if args.workload == "batch64" else run_serve(args, rank, world)
+    if args.workload in ("batch64", "serve", "progressive"):
+        rc = {"batch64": run_batch, "serve": run_serve, "progressive": run_progressive}[args.workload](args, rank, world)
         if world > 1:
             import torch.distributed as dist
 
