@@ -326,6 +326,10 @@ int pt_batch_destroy(pt_batch* batch);
 const char* pt_batch_last_error(pt_batch* batch);
 void* pt_batch_stream(pt_batch* batch);
 int pt_batch_set_march_budget(pt_batch* batch, int steps);
+/* Idle lanes a warp of the persistent kernel gathers before it starts new
+ * samples together (1..32, default 16: starting samples one lane at a time
+ * runs the camera and lens code with few lanes active). */
+int pt_batch_set_persist_refill(pt_batch* batch, int lanes);
 /* Engine choice for passes added from now on (PT_BATCH_ROUTE_*). */
 int pt_batch_set_route(pt_batch* batch, int route);
 int pt_batch_add_scene(pt_batch* batch, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins,

@@ -675,13 +675,18 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
     const unsigned lt = (1u << lane) - 1u;
     uint64_t cbase = 0;   // warp-uniform: unassigned samples of the warp's chunk
     uint32_t cleft = 0;
+    uint32_t cjob = 0;      // warp-uniform: pass of the chunk's first sample,
+    uint64_t cjob_end = 0;  // and the end of its sample range
     bool exhausted = false;  // warp-uniform: no sample left below `end`
     bool active = false, shadow = false;
     uint32_t job = 0, local = 0;
     PathState ps;
     for (;;) {
-        // Refill idle lanes from the warp's chunk, claiming chunks as needed.
-        unsigned need = __ballot_sync(0xffffffffu, !active) ;
+        // Refill idle lanes from the warp's chunk, claiming chunks as needed,
+        // once persist_refill lanes are idle (or none is busy): new samples
+        // start together instead of one lane at a time.
+        unsigned need = __ballot_sync(0xffffffffu, !active);
+        if (__popc(need) < A.persist_refill && need != 0xffffffffu) need = 0u;
         while (need && !exhausted) {
             if (cleft == 0) {
                 unsigned long long b = 0;
@@ -693,13 +698,19 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
                 }
                 cbase = b;
                 cleft = (end - b < kPersistChunk) ? (uint32_t)(end - b) : kPersistChunk;
+                // The pass of the chunk's first sample, looked up once for the warp.
+                uint32_t cj = 0;
+                if (lane == 0) cj = find_job(A.jobs, A.job_cap, job_lo, job_hi, b);
+                cjob = __shfl_sync(0xffffffffu, cj, 0);
+                const WfJob& CJ = A.jobs[cjob];
+                cjob_end = CJ.first + (uint64_t)CJ.count;
             }
             const uint32_t n = min((uint32_t)__popc(need), cleft);
             const uint32_t rank = (uint32_t)__popc(need & lt);
             const bool mine = ((need >> lane) & 1u) && rank < n;
             if (mine) {
                 const uint64_t s = cbase + rank;
-                job = find_job(A.jobs, A.job_cap, job_lo, job_hi, s);
+                job = (s < cjob_end) ? cjob : find_job(A.jobs, A.job_cap, job_lo, job_hi, s);
                 const WfJob& J = A.jobs[job];
                 local = (uint32_t)(s - J.first);
                 const pt_push& pc = J.pc;

@@ -90,6 +90,7 @@ struct pt_batch {
     uint32_t pool_slots = 0, max_passes = 0;
     int route = PT_BATCH_ROUTE_AUTO;
     int march_budget = 64;
+    int persist_refill = 16;
     std::vector<BatchScene> scenes;
     std::vector<BatchTarget> targets;
     std::deque<BatchPass> passes;  // indexed by pass id - pass_base
@@ -154,6 +155,7 @@ cudaError_t ensure_engine(pt_batch* b, int e) {
         return r;
     }
     b->engine[e].set_persistent(e == kPersistent);
+    b->engine[e].args.persist_refill = b->persist_refill;
     b->engine_live[e] = true;
     return cudaSuccess;
 }
@@ -379,6 +381,14 @@ int pt_batch_set_march_budget(pt_batch* b, int steps) {
     if (steps < 1 || steps > 512) return bfail(b, PT_ERR_INVALID, "pt_batch_set_march_budget: 1..512 steps");
     b->march_budget = steps;
     for (int e = 0; e < 2; e++) b->engine[e].set_march_budget(steps);
+    return PT_OK;
+}
+
+int pt_batch_set_persist_refill(pt_batch* b, int lanes) {
+    if (!b) return PT_ERR_INVALID;
+    if (lanes < 1 || lanes > 32) return bfail(b, PT_ERR_INVALID, "pt_batch_set_persist_refill: 1..32 lanes");
+    b->persist_refill = lanes;
+    for (int e = 0; e < 2; e++) b->engine[e].args.persist_refill = lanes;
     return PT_OK;
 }
 

@@ -10,6 +10,7 @@ namespace {
 
 constexpr size_t r256(size_t x) { return (x + 255) / 256 * 256; }
 
+
 template <typename T>
 T* take(uintptr_t& p, size_t count) {
     T* r = reinterpret_cast<T*>(p);
@@ -75,6 +76,7 @@ static cudaError_t common_setup(WfEngine& e, int device, cudaStream_t stream, ui
     e.args.march_budget = march_budget;
     e.args.refill_min = 2;
     e.args.drain_lanes = 24;
+    e.args.persist_refill = 16;  // measured best on GB300 (batch of 64 sphere jobs)
     e.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
     int sms = 0;
     EN_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));

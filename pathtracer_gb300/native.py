@@ -268,6 +268,7 @@ CUDA_API = [
     ("pt_batch_stream", _vp, [_vp]),
     ("pt_batch_set_march_budget", _i, [_vp, _i]),
     ("pt_batch_set_route", _i, [_vp, _i]),
+    ("pt_batch_set_persist_refill", _i, [_vp, _i]),
     ("pt_batch_add_scene", _i, [_vp, _vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
     ("pt_batch_add_target", _i, [_vp, _i, _i, _i, ctypes.POINTER(_i)]),
     ("pt_batch_target_device_ptr", _vp, [_vp, _i]),

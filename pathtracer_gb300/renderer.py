@@ -297,6 +297,9 @@ class Batch:
     def set_march_budget(self, steps: int):
         self._check(self._lib.pt_batch_set_march_budget(self._h, steps))
 
+    def set_persist_refill(self, lanes: int):
+        self._check(self._lib.pt_batch_set_persist_refill(self._h, lanes))
+
     def set_route(self, route: int):
         self._check(self._lib.pt_batch_set_route(self._h, route))
 
