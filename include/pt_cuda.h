@@ -22,8 +22,10 @@
 #ifndef PT_CUDA_H
 #define PT_CUDA_H
 
+#if !defined(__CUDACC_RTC__)
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -100,7 +102,8 @@ enum {
     PT_SDF_BLOB = 1,       /* sdfs/blob.glsl: material = lobe IDs (default 4,5,6) */
     PT_SDF_MANDELBULB = 2, /* sdfs/mandelbulb.glsl: material = mix endpoints (default 4,3) */
     PT_SDF_MENGER = 3,     /* sdfs/menger.glsl: material[0] constant (default 0) */
-    PT_SDF_TERRAIN = 4     /* sdfs/terrain.glsl: material[0] constant (default 0) */
+    PT_SDF_TERRAIN = 4,    /* sdfs/terrain.glsl: material[0] constant (default 0) */
+    PT_SDF_CUSTOM = 5      /* other GLSL text: compiled at run time (pt_set_sdfs only) */
 };
 enum {
     PT_SDFMAT_DEFAULT = 0,  /* the snippet's own sdfmaterial form with `material` */
@@ -120,11 +123,15 @@ int pt_create(pt_ctx** out, int device);
 int pt_destroy(pt_ctx* ctx);
 
 /* Replaces InsertSDF + GLSLToSPIRV + RecompileComputeShaders
- * (src/pathtracer.cpp:2004-2054, 1811-1868, 3836-3841).  Each source is either
- * the GLSL text of a scene's `sdf[i].glsl` (recognised by a whitespace-
- * insensitive fingerprint of the reference's snippets) or a spec
- * "builtin:<blob|mandelbulb|menger|terrain>[:m0,m1,m2]".  Positions and
- * bounding boxes come from pt_ubo.sdfs, as in the reference. */
+ * (src/pathtracer.cpp:2004-2054, 1811-1868, 3836-3841).  Each source is the
+ * GLSL text of a scene's `sdf[i].glsl` or a spec
+ * "builtin:<blob|mandelbulb|menger|terrain>[:m0,m1,m2]".  The reference's
+ * four snippets (recognised by a whitespace-insensitive fingerprint) map to
+ * precompiled plug-ins; any other text is translated (pt_glsl_translate) and
+ * compiled at run time into the megakernel on the first dispatch (seconds,
+ * then cached), and scenes holding such text always render with the
+ * megakernel.  Positions and bounding boxes come from pt_ubo.sdfs, as in the
+ * reference. */
 int pt_set_sdfs(pt_ctx* ctx, const char* const* sources, int n);
 /* Same, from already-decoded descriptors. */
 int pt_set_sdf_plugins(pt_ctx* ctx, const pt_sdf_plugin* plugins, int n);
@@ -133,6 +140,18 @@ int pt_parse_sdf_source(const char* source, pt_sdf_plugin* out);
 /* The whitespace-insensitive FNV-1a-64 fingerprint pt_parse_sdf_source
  * matches GLSL text by (0 for NULL). */
 uint64_t pt_sdf_source_fingerprint(const char* source);
+
+/* GLSL SDF snippet (a scene's `sdf[i].glsl`: `float sdf(in vec3 p)` and
+ * `float sdfmaterial(in vec3 p)` plus helpers) to C++ over the GLSL shim the
+ * run-time compiled kernels include, every function renamed <prefix><name>.
+ * Writes a NUL-terminated text of at most cap bytes (*needed: its size);
+ * PT_ERR_UNSUPPORTED with a reason in err for what the shim does not cover. */
+int pt_glsl_translate(const char* glsl, const char* prefix, char* out, size_t cap, size_t* needed, char* err,
+                      size_t err_cap);
+/* Compiles (without loading) the run-time megakernel for n snippets for
+ * compute capability sm (e.g. 103): a check that needs no GPU.  The log
+ * receives the compiler's messages. */
+int pt_jit_check(const char* const* sources, int n, int sm, char* log, size_t log_cap);
 
 /* Replaces the UBO upload (src/pathtracer.cpp:3805-3807). */
 int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo);

@@ -29,7 +29,9 @@
 #ifndef PT_MATHF_H
 #define PT_MATHF_H
 
+#if !defined(__CUDACC_RTC__)
 #include <stdint.h>
+#endif
 
 /* PTM_FN: inlined everywhere.  PTM_CALL: the larger functions; a GPU
  * translation unit that defines PTM_OUTLINE before including this header

@@ -26,13 +26,20 @@ REL_TOL = 1e-4
 PATH_MATCH_MIN = 0.999
 
 
-def plugins_for(scene) -> list:
+def plugins_for(scene, custom: dict | None = None) -> list:
+    """The oracle's plug-in per SDF of the scene.  Text that is not one of the
+    shipped snippets needs an entry in `custom` (source text -> the names of
+    its C restatement's sdf and material functions in user_sdfs.c), which is
+    registered for that slot as PT_SDF_CUSTOM."""
     out = []
-    for src in scene.sdf_sources():
+    for slot, src in enumerate(scene.sdf_sources()):
         p = native.PtSdfPlugin()
         rc = native.cuda().pt_parse_sdf_source(src.encode(), ctypes.byref(p))
         if rc != native.PT_OK:
-            raise ValueError(f"unsupported SDF source: {src[:60]!r}")
+            if not custom or src not in custom:
+                raise ValueError(f"unsupported SDF source: {src[:60]!r}")
+            oracle.set_user_sdf(slot, *custom[src])
+            p = native.plugin(native.PT_SDF_CUSTOM)
         out.append(p)
     return out
 

@@ -39,6 +39,40 @@ def build() -> str:
     return LIB
 
 
+USER_LIB = os.path.join(HERE, "_build", "libpt_user_sdfs.so")
+_user = None
+
+
+def user_sdfs() -> ctypes.CDLL:
+    """The C restatements of the test snippets (oracle/user_sdfs.c)."""
+    global _user
+    if _user is None:
+        src = os.path.join(HERE, "user_sdfs.c")
+        deps = [src, os.path.join(HERE, "..", "include", "pt_mathf.h")]
+        if not os.path.exists(USER_LIB) or any(os.path.getmtime(d) > os.path.getmtime(USER_LIB) for d in deps):
+            os.makedirs(os.path.dirname(USER_LIB), exist_ok=True)
+            subprocess.run([os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-std=c11", "-ffp-contract=off",
+                            "-fno-fast-math", "-shared", "-o", USER_LIB, src, "-lm"], check=True)
+        _user = ctypes.CDLL(USER_LIB)
+    return _user
+
+
+def user_fn(name: str):
+    """A float(float, float, float) function of user_sdfs.c."""
+    f = getattr(user_sdfs(), name)
+    f.restype = ctypes.c_float
+    f.argtypes = [ctypes.c_float] * 3
+    return f
+
+
+def set_user_sdf(slot: int, sdf_name: str | None, material_name: str | None = None) -> None:
+    """Registers user_sdfs.c functions for a PT_SDF_CUSTOM slot (None clears it)."""
+    fs = ctypes.cast(getattr(user_sdfs(), sdf_name), ctypes.c_void_p) if sdf_name else None
+    fm = ctypes.cast(getattr(user_sdfs(), material_name), ctypes.c_void_p) if material_name else None
+    if lib().pto_set_user_sdf(slot, fs, fm) != 0:
+        raise ValueError(f"bad SDF slot {slot}")
+
+
 def lib() -> ctypes.CDLL:
     global _lib
     if _lib is None:
@@ -61,6 +95,8 @@ def lib() -> ctypes.CDLL:
         L.pto_blackbody.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
         L.pto_blackbody_peak.restype = ctypes.c_float
         L.pto_blackbody_peak.argtypes = [ctypes.c_float]
+        L.pto_set_user_sdf.restype = ctypes.c_int
+        L.pto_set_user_sdf.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         L.pto_sdf_eval.restype = ctypes.c_float
         L.pto_sdf_eval.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.pto_sdf_material.restype = ctypes.c_float

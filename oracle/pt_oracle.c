@@ -630,20 +630,38 @@ static float terrain_height(float x) {
 }
 static float terrain_sdf(vec3 p) { return p.y - (terrain_height(p.x) + terrain_height(p.z)); }
 
-static float plugin_sdf(const pt_sdf_plugin* pl, vec3 p) {
+/* SDF slots holding other GLSL text (PT_SDF_CUSTOM): the tests register a C
+ * restatement of each such snippet (oracle/user_sdfs.c) per slot. */
+typedef float (*pto_user_fn)(float x, float y, float z);
+static pto_user_fn g_user_sdf[PT_MAX_LIVE_SDFS];
+static pto_user_fn g_user_mat[PT_MAX_LIVE_SDFS];
+
+int pto_set_user_sdf(int slot, pto_user_fn sdf, pto_user_fn material) {
+    if (slot < 0 || slot >= PT_MAX_LIVE_SDFS) return 1;
+    g_user_sdf[slot] = sdf;
+    g_user_mat[slot] = material;
+    return 0;
+}
+
+static float plugin_sdf(const pt_sdf_plugin* pl, int slot, vec3 p) {
     switch (pl->kind) {
         case PT_SDF_BLOB: return blob_sdf(p);
         case PT_SDF_MANDELBULB: return mandelbulb_sdf(p);
         case PT_SDF_MENGER: return menger_sdf(p);
         case PT_SDF_TERRAIN: return terrain_sdf(p);
+        case PT_SDF_CUSTOM:
+            return (slot >= 0 && slot < PT_MAX_LIVE_SDFS && g_user_sdf[slot]) ? g_user_sdf[slot](p.x, p.y, p.z) : MAXDIST;
         default: return MAXDIST;
     }
 }
-static float plugin_material(const pt_sdf_plugin* pl, vec3 p) {
+static float plugin_material(const pt_sdf_plugin* pl, int slot, vec3 p) {
     if (pl->material_mode == PT_SDFMAT_CONSTANT) return pl->material[0];
     switch (pl->kind) {
         case PT_SDF_BLOB: return blob_material(p, pl->material);
         case PT_SDF_MANDELBULB: return mandelbulb_material(p, pl->material);
+        case PT_SDF_CUSTOM:
+            return (slot >= 0 && slot < PT_MAX_LIVE_SDFS && g_user_mat[slot]) ? g_user_mat[slot](p.x, p.y, p.z)
+                                                                                : pl->material[0];
         default: return pl->material[0];
     }
 }
@@ -659,7 +677,7 @@ static float SDF(const ctx_t* c, vec3 p, uint32_t set1) {
         uint32_t code = 1u << i;
         if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
             if (c->cnt) c->cnt[PTO_C_SDF_BLOB + (c->plug[i].kind == PT_SDF_BLOB ? 0 : c->plug[i].kind == PT_SDF_MANDELBULB ? 1 : c->plug[i].kind == PT_SDF_MENGER ? 3 : 4)]++;
-            sdf = fminf(sdf, plugin_sdf(&c->plug[i], sub3(p, sdf_pos(c, i))));
+            sdf = fminf(sdf, plugin_sdf(&c->plug[i], i, sub3(p, sdf_pos(c, i))));
         }
     }
     return sdf;
@@ -675,9 +693,9 @@ static float SDFMATERIAL(const ctx_t* c, vec3 p, uint32_t set1) {
         if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
             vec3 q = sub3(p, sdf_pos(c, i));
             if (c->cnt) c->cnt[PTO_C_SDF_BLOB + (c->plug[i].kind == PT_SDF_BLOB ? 0 : c->plug[i].kind == PT_SDF_MANDELBULB ? 1 : c->plug[i].kind == PT_SDF_MENGER ? 3 : 4)]++;
-            float di = plugin_sdf(&c->plug[i], q);
+            float di = plugin_sdf(&c->plug[i], i, q);
             if (!(sdf < di)) COUNT(c, PTO_C_SDF_MATERIAL);
-            mat = (sdf < di) ? mat : plugin_material(&c->plug[i], q);
+            mat = (sdf < di) ? mat : plugin_material(&c->plug[i], i, q);
             sdf = fminf(sdf, di);
         }
     }
@@ -1241,8 +1259,8 @@ void pto_wave_to_xyz(const float* cie, float wave, float* out3) {
     free(u);
 }
 
-float pto_sdf_eval(const pt_sdf_plugin* pl, const float* p) { return plugin_sdf(pl, mk3(p[0], p[1], p[2])); }
-float pto_sdf_material(const pt_sdf_plugin* pl, const float* p) { return plugin_material(pl, mk3(p[0], p[1], p[2])); }
+float pto_sdf_eval(const pt_sdf_plugin* pl, const float* p) { return plugin_sdf(pl, 0, mk3(p[0], p[1], p[2])); }
+float pto_sdf_material(const pt_sdf_plugin* pl, const float* p) { return plugin_material(pl, 0, mk3(p[0], p[1], p[2])); }
 
 /* SC:1492-1533 */
 int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plugins, int nplugins, float* accum,

@@ -78,6 +78,8 @@ float pto_sdf_eval(const pt_sdf_plugin* plugin, const float* p3);
 float pto_sdf_material(const pt_sdf_plugin* plugin, const float* p3);
 void pto_wave_to_xyz(const float* cie, float wave, float* out3);
 int pto_mathf_eval(int fn, const float* x, const float* y, float* out, int n);
+/* CPU functions of a PT_SDF_CUSTOM slot (the compiled translation of its GLSL). */
+int pto_set_user_sdf(int slot, float (*sdf)(float, float, float), float (*material)(float, float, float));
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,59 @@
+/* user_sdfs.c — TEST INFRASTRUCTURE ONLY: hand restatements, in C, of the
+ * GLSL SDF snippets the tests use for scenes beyond the reference's four
+ * shipped ones (their GLSL text is in tests/user_snippets.py).  The product
+ * compiles such text at run time (pt_glsl_translate + NVRTC); the oracle
+ * renders the same scene with these functions registered per SDF slot
+ * (pto_set_user_sdf), so a parity failure points at the translation or the
+ * run-time compile, not at a shared helper.
+ *
+ * Arithmetic follows GLSL's meaning of each expression in source order, with
+ * the shader's conventions: single precision, no contraction (built with
+ * -ffp-contract=off), mod(a, b) = a - b * floor(a / b), length = sqrt(dot),
+ * and sin through the shared pt_mathf routines. */
+#include <math.h>
+
+#include "../include/pt_mathf.h"
+
+/* ---- "twisted torus": torus (R 0.8, r 0.25) with a sin ripple ---------- */
+static float torus(float px, float py, float pz, float tx, float ty, float* ring) {
+    const float qx = sqrtf(px * px + pz * pz) - tx;
+    const float qy = py;
+    *ring = qx;
+    return sqrtf(qx * qx + qy * qy) - ty;
+}
+
+float user_torus_sdf(float x, float y, float z) {
+    float ring;
+    const float d = torus(x, y, z, 0.8f, 0.25f, &ring);
+    return d + 0.02f * ptm_sinf(8.0f * x) * ptm_sinf(8.0f * z);
+}
+
+float user_torus_material(float x, float y, float z) {
+    float ring;
+    (void)torus(x, y, z, 0.8f, 0.25f, &ring);
+    return ring > 0.0f ? 2.0f : 3.0f;
+}
+
+/* ---- "lattice": rounded cubes repeated every 0.6, clipped to a box ----- */
+static float box(float px, float py, float pz, float bx, float by, float bz) {
+    const float qx = fabsf(px) - bx, qy = fabsf(py) - by, qz = fabsf(pz) - bz;
+    const float mx = fmaxf(qx, 0.0f), my = fmaxf(qy, 0.0f), mz = fmaxf(qz, 0.0f);
+    return sqrtf(mx * mx + my * my + mz * mz) + fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f);
+}
+
+static float glsl_mod(float a, float b) { return a - b * floorf(a / b); }
+
+float user_lattice_sdf(float x, float y, float z) {
+    const float c = 0.6f;
+    const float h = 0.5f * c;
+    const float rx = glsl_mod(x + h, c) - h;
+    const float ry = glsl_mod(y + h, c) - h;
+    const float rz = glsl_mod(z + h, c) - h;
+    return fmaxf(box(rx, ry, rz, 0.18f, 0.18f, 0.18f) - 0.04f, box(x, y, z, 0.9f, 0.9f, 0.9f));
+}
+
+float user_lattice_material(float x, float y, float z) {
+    (void)x;
+    (void)z;
+    return floorf(fminf(fmaxf(y + 1.0f, 0.0f), 1.5f)) + 1.0f;
+}

@@ -7,6 +7,7 @@ This package builds them in-tree (``build.build()``) and binds them with
 ctypes (``native``, ``renderer``).
 """
 from .renderer import (  # noqa: F401
-    Batch, Context, PathTracerError, Scene, Server, cie_analytic, export_rgb8, render_offscreen)
+    Batch, Context, PathTracerError, Scene, Server, cie_analytic, export_rgb8, glsl_translate, jit_check,
+    render_offscreen)
 
 SCENES_DIR = __import__("os").path.join(__import__("os").path.dirname(__file__), "scenes")

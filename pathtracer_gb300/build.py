@@ -33,7 +33,24 @@ CUDA_SOURCES = [
     "pt_batch.cu",
     "pt_export.cu",
     "pt_sdf_source.cpp",
+    "pt_glsl.cpp",
+    "pt_jit.cu",
 ]
+# Headers the run-time compiled megakernel (pt_jit.cu) includes, under the
+# names their #include lines use; embedded into libpt_cuda as strings.
+JIT_HEADERS = [
+    ("../../../include/pt_cuda.h", "include/pt_cuda.h"),
+    ("../../../include/pt_mathf.h", "include/pt_mathf.h"),
+    ("pt_vec.cuh", "pathtracer_gb300/csrc/kernel/pt_vec.cuh"),
+    ("pt_scene.cuh", "pathtracer_gb300/csrc/kernel/pt_scene.cuh"),
+    ("pt_features.h", "pathtracer_gb300/csrc/kernel/pt_features.h"),
+    ("pt_geometry.cuh", "pathtracer_gb300/csrc/kernel/pt_geometry.cuh"),
+    ("pt_path.cuh", "pathtracer_gb300/csrc/kernel/pt_path.cuh"),
+    ("pt_megakernel.h", "pathtracer_gb300/csrc/kernel/pt_megakernel.h"),
+    ("pt_megakernel_body.cuh", "pathtracer_gb300/csrc/kernel/pt_megakernel_body.cuh"),
+    ("pt_glsl_shim.h", "pathtracer_gb300/csrc/kernel/pt_glsl_shim.h"),
+]
+GEN = os.path.join(LIB, "gen")
 HOST_SOURCES = [
     "host/pt_json.cpp",
     "host/pt_scene.cpp",
@@ -70,6 +87,27 @@ def _stale(target: str, sources: list[str]) -> bool:
     return any(os.path.getmtime(s) > t for s in deps if os.path.isfile(s))
 
 
+def _write_jit_sources() -> None:
+    """pt_jit_sources.inc: the JIT_HEADERS texts as C++ raw string literals."""
+    os.makedirs(GEN, exist_ok=True)
+    names, texts = [], []
+    for name, rel in JIT_HEADERS:
+        with open(os.path.join(ROOT, rel)) as f:
+            text = f.read()
+        if ")PTSRC\"" in text:
+            raise RuntimeError(f"{rel} contains the raw-string delimiter")
+        names.append(f'"{name}"')
+        texts.append('R"PTSRC(' + text + ')PTSRC"')
+    body = ("// Generated by pathtracer_gb300/build.py from the kernel headers.\n"
+            f"static const int kJitHeaderCount = {len(names)};\n"
+            "static const char* const kJitHeaderNames[] = {" + ", ".join(names) + "};\n"
+            "static const char* const kJitHeaderTexts[] = {\n" + ",\n".join(texts) + "};\n")
+    out = os.path.join(GEN, "pt_jit_sources.inc")
+    if not os.path.exists(out) or open(out).read() != body:
+        with open(out, "w") as f:
+            f.write(body)
+
+
 def build(force: bool = False, verbose: bool = False) -> dict[str, str]:
     """Compiles both libraries (if stale) and returns their paths."""
     os.makedirs(LIB, exist_ok=True)
@@ -83,18 +121,19 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, str]:
     host_cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, f"-I{cuda_inc}", "-o", host_so, *host_src,
                 f"-L{LIB}", "-lpt_cuda", "-Wl,-rpath,$ORIGIN"]
 
-    if force or _stale(cuda_so, cuda_src):
+    _write_jit_sources()
+    if force or _stale(cuda_so, cuda_src + [os.path.join(GEN, "pt_jit_sources.inc")]):
         # One object per translation unit, compiled in parallel, then linked.
         objdir = os.path.join(LIB, "obj")
         os.makedirs(objdir, exist_ok=True)
         objs = [os.path.join(objdir, os.path.basename(s) + ".o") for s in cuda_src]
-        cmds = [[nvcc, *NVCC_FLAGS, "-c", "-o", o, s] for s, o in zip(cuda_src, objs)]
+        cmds = [[nvcc, *NVCC_FLAGS, f"-I{GEN}", "-c", "-o", o, s] for s, o in zip(cuda_src, objs)]
         if verbose:
             for c in cmds:
                 print(" ".join(c), file=sys.stderr)
         with ThreadPoolExecutor(max_workers=min(len(cmds), os.cpu_count() or 1)) as ex:
             list(ex.map(_run, cmds))
-        link = [nvcc, ARCH, "-shared", "-o", cuda_so, *objs]
+        link = [nvcc, ARCH, "-shared", "-o", cuda_so, *objs, "-lnvrtc"]
         if verbose:
             print(" ".join(link), file=sys.stderr)
         _run(link)

@@ -407,24 +407,33 @@ PT_DI float height(float x) {
 PT_DI float sdf(float3 p) { return p.y - (height(p.x) + height(p.z)); }
 }  // namespace sdf_terrain
 
-PT_DI float plugin_sdf(int kind, float3 p) {
+// A scene's SDF slot `slot` with plug-in `kind`.  PT_SDF_CUSTOM slots hold
+// GLSL compiled at run time: the module built for them (pt_jit.cu) defines
+// pt_user_sdf / pt_user_material before including these headers; the
+// precompiled kernels never see that kind.
+PT_DI float plugin_sdf(int kind, int slot, float3 p) {
     switch (kind) {
         case PT_SDF_MANDELBULB: return sdf_mandelbulb::sdf(p);
         case PT_SDF_MENGER: return sdf_menger::sdf(p);
         case PT_SDF_BLOB: return sdf_blob::sdf(p);
         case PT_SDF_TERRAIN: return sdf_terrain::sdf(p);
+#if defined(PT_JIT_USER_SDF)
+        case PT_SDF_CUSTOM: return pt_user_sdf(slot, p);
+#endif
         default: return PT_MAXDIST;
     }
 }
-PT_DI float plugin_material(const pt_sdf_plugin& pl, float3 p) {
+PT_DI float plugin_material(const pt_sdf_plugin& pl, int slot, float3 p) {
     if (pl.material_mode == PT_SDFMAT_CONSTANT) return pl.material[0];
     switch (pl.kind) {
         case PT_SDF_BLOB: return sdf_blob::sdfmaterial(p, pl.material);
         case PT_SDF_MANDELBULB: return sdf_mandelbulb::sdfmaterial(p, pl.material);
+#if defined(PT_JIT_USER_SDF)
+        case PT_SDF_CUSTOM: return pt_user_material(slot, p);
+#endif
         default: return pl.material[0];
     }
 }
-
 PT_DI float3 sdf_pos(const KScene& S, int i) { return f3(S.sdfs[6 * i], S.sdfs[6 * i + 1], S.sdfs[6 * i + 2]); }
 
 // SDF() with the lines InsertSDF splices in (src/pathtracer.cpp:2004-2054):
@@ -436,7 +445,7 @@ PT_DI float scene_sdf(const KScene& S, float3 p, uint32_t set1) {
         const int i = __ffs(bits) - 1;
         bits &= bits - 1u;
         const int kind = S.plug[i].kind;
-        if (kind != PT_SDF_NONE) sdf = fminf(sdf, plugin_sdf(kind, p - sdf_pos(S, i)));
+        if (kind != PT_SDF_NONE) sdf = fminf(sdf, plugin_sdf(kind, i, p - sdf_pos(S, i)));
     }
     return sdf;
 }
@@ -454,8 +463,8 @@ static __device__ __noinline__ float scene_sdf_material(const KScene& S, float3 
         const pt_sdf_plugin pl = S.plug[i];
         if (pl.kind != PT_SDF_NONE) {
             const float3 q = p - sdf_pos(S, i);
-            const float di = plugin_sdf(pl.kind, q);
-            mat = (sdf < di) ? mat : plugin_material(pl, q);
+            const float di = plugin_sdf(pl.kind, i, q);
+            mat = (sdf < di) ? mat : plugin_material(pl, i, q);
             sdf = fminf(sdf, di);
         }
     }
@@ -474,7 +483,7 @@ PT_DI float scene_sdf_material_hit(const KScene& S, float3 p, uint32_t set1, boo
     if (converged && bits != 0u && (bits & (bits - 1u)) == 0u) {
         const int i = __ffs(bits) - 1;
         const pt_sdf_plugin pl = S.plug[i];
-        if (pl.kind != PT_SDF_NONE) return plugin_material(pl, p - sdf_pos(S, i));
+        if (pl.kind != PT_SDF_NONE) return plugin_material(pl, i, p - sdf_pos(S, i));
     }
     return scene_sdf_material(S, p, set1);
 }

@@ -1,0 +1,231 @@
+// pt_glsl_shim.h — the part of GLSL that scene SDF snippets use, as C++ for
+// the runtime-compiled kernels (NVRTC) and for the host (g++), with the same
+// float arithmetic on both: IEEE +, -, *, / and sqrt, fma written out, and
+// pt_mathf for the transcendentals.  Snippets reach it through
+// pt_glsl_translate (pt_glsl.cpp), which rewrites float literals, swizzles and
+// parameter qualifiers into this vocabulary.
+//
+// Covered: float/int/bool, vec2/vec3/vec4 (constructors, component access,
+// read swizzles as member calls, arithmetic with vectors and scalars),
+// mat2/mat3 (constructors from columns, matrix * vector), and the built-ins
+// abs sign floor ceil fract mod min max clamp mix step smoothstep sqrt
+// inversesqrt pow exp log sin cos acos length distance dot cross normalize
+// reflect fma radians degrees, plus the shader's smin for floats and vec2.
+#pragma once
+
+#if defined(__CUDACC__)
+#define PTG_FN static __device__ __forceinline__
+#define PTG_M __device__ __forceinline__
+#else
+#define PTG_FN static inline
+#define PTG_M inline
+#endif
+
+#include "../../../include/pt_mathf.h"
+
+namespace ptg {
+
+struct vec2;
+struct vec3;
+struct vec4;
+
+struct vec2 {
+    float x, y;
+    PTG_M vec2() : x(0.0f), y(0.0f) {}
+    PTG_M explicit vec2(float s) : x(s), y(s) {}
+    PTG_M vec2(float a, float b) : x(a), y(b) {}
+    PTG_M vec2 xx() const { return vec2(x, x); }
+    PTG_M vec2 xy() const { return vec2(x, y); }
+    PTG_M vec2 yx() const { return vec2(y, x); }
+    PTG_M vec2 yy() const { return vec2(y, y); }
+};
+
+struct vec3 {
+    float x, y, z;
+    PTG_M vec3() : x(0.0f), y(0.0f), z(0.0f) {}
+    PTG_M explicit vec3(float s) : x(s), y(s), z(s) {}
+    PTG_M vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    PTG_M vec3(vec2 a, float c) : x(a.x), y(a.y), z(c) {}
+    PTG_M vec3(float a, vec2 b) : x(a), y(b.x), z(b.y) {}
+#define PTG_S2(A, B) \
+    PTG_M vec2 A##B() const { return vec2(A, B); }
+    PTG_S2(x, x) PTG_S2(x, y) PTG_S2(x, z) PTG_S2(y, x) PTG_S2(y, y) PTG_S2(y, z) PTG_S2(z, x) PTG_S2(z, y)
+    PTG_S2(z, z)
+#define PTG_S3(A, B, C) \
+    PTG_M vec3 A##B##C() const { return vec3(A, B, C); }
+#define PTG_S3B(A, B) PTG_S3(A, B, x) PTG_S3(A, B, y) PTG_S3(A, B, z)
+#define PTG_S3A(A) PTG_S3B(A, x) PTG_S3B(A, y) PTG_S3B(A, z)
+    PTG_S3A(x) PTG_S3A(y) PTG_S3A(z)
+};
+
+struct vec4 {
+    float x, y, z, w;
+    PTG_M vec4() : x(0.0f), y(0.0f), z(0.0f), w(0.0f) {}
+    PTG_M explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
+    PTG_M vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
+    PTG_M vec4(vec3 a, float d) : x(a.x), y(a.y), z(a.z), w(d) {}
+    PTG_M vec4(vec2 a, vec2 b) : x(a.x), y(a.y), z(b.x), w(b.y) {}
+    PTG_M vec3 xyz() const { return vec3(x, y, z); }
+    PTG_M vec2 xy() const { return vec2(x, y); }
+    PTG_M vec2 zw() const { return vec2(z, w); }
+};
+
+// Component-wise arithmetic.
+#define PTG_OPS(V, EXPAND)                                                                     \
+    PTG_FN V operator+(V a, V b) { return EXPAND(a, +, b); }                                   \
+    PTG_FN V operator-(V a, V b) { return EXPAND(a, -, b); }                                   \
+    PTG_FN V operator*(V a, V b) { return EXPAND(a, *, b); }                                   \
+    PTG_FN V operator/(V a, V b) { return EXPAND(a, /, b); }                                   \
+    PTG_FN V operator+(V a, float s) { return a + V(s); }                                      \
+    PTG_FN V operator-(V a, float s) { return a - V(s); }                                      \
+    PTG_FN V operator*(V a, float s) { return a * V(s); }                                      \
+    PTG_FN V operator/(V a, float s) { return a / V(s); }                                      \
+    PTG_FN V operator+(float s, V a) { return V(s) + a; }                                      \
+    PTG_FN V operator-(float s, V a) { return V(s) - a; }                                      \
+    PTG_FN V operator*(float s, V a) { return V(s) * a; }                                      \
+    PTG_FN V operator/(float s, V a) { return V(s) / a; }                                      \
+    PTG_FN V& operator+=(V& a, V b) { return a = a + b; }                                      \
+    PTG_FN V& operator-=(V& a, V b) { return a = a - b; }                                      \
+    PTG_FN V& operator*=(V& a, V b) { return a = a * b; }                                      \
+    PTG_FN V& operator/=(V& a, V b) { return a = a / b; }                                      \
+    PTG_FN V& operator+=(V& a, float s) { return a = a + s; }                                  \
+    PTG_FN V& operator-=(V& a, float s) { return a = a - s; }                                  \
+    PTG_FN V& operator*=(V& a, float s) { return a = a * s; }                                  \
+    PTG_FN V& operator/=(V& a, float s) { return a = a / s; }
+#define PTG_E2(a, op, b) vec2(a.x op b.x, a.y op b.y)
+#define PTG_E3(a, op, b) vec3(a.x op b.x, a.y op b.y, a.z op b.z)
+#define PTG_E4(a, op, b) vec4(a.x op b.x, a.y op b.y, a.z op b.z, a.w op b.w)
+PTG_OPS(vec2, PTG_E2)
+PTG_OPS(vec3, PTG_E3)
+PTG_OPS(vec4, PTG_E4)
+
+// Negation flips signs (-(+0) is -0, unlike 0 - a).
+PTG_FN vec2 operator-(vec2 a) { return vec2(-a.x, -a.y); }
+PTG_FN vec3 operator-(vec3 a) { return vec3(-a.x, -a.y, -a.z); }
+PTG_FN vec4 operator-(vec4 a) { return vec4(-a.x, -a.y, -a.z, -a.w); }
+
+// Apply a float function component-wise.
+#define PTG_MAP1(NAME, F)                                                                       \
+    PTG_FN float NAME(float a) { return F(a); }                                                 \
+    PTG_FN vec2 NAME(vec2 a) { return vec2(F(a.x), F(a.y)); }                                   \
+    PTG_FN vec3 NAME(vec3 a) { return vec3(F(a.x), F(a.y), F(a.z)); }                           \
+    PTG_FN vec4 NAME(vec4 a) { return vec4(F(a.x), F(a.y), F(a.z), F(a.w)); }
+#define PTG_MAP2(NAME, F)                                                                       \
+    PTG_FN float NAME(float a, float b) { return F(a, b); }                                     \
+    PTG_FN vec2 NAME(vec2 a, vec2 b) { return vec2(F(a.x, b.x), F(a.y, b.y)); }                 \
+    PTG_FN vec3 NAME(vec3 a, vec3 b) { return vec3(F(a.x, b.x), F(a.y, b.y), F(a.z, b.z)); }    \
+    PTG_FN vec4 NAME(vec4 a, vec4 b) { return vec4(F(a.x, b.x), F(a.y, b.y), F(a.z, b.z), F(a.w, b.w)); } \
+    PTG_FN vec2 NAME(vec2 a, float b) { return NAME(a, vec2(b)); }                              \
+    PTG_FN vec3 NAME(vec3 a, float b) { return NAME(a, vec3(b)); }                              \
+    PTG_FN vec4 NAME(vec4 a, float b) { return NAME(a, vec4(b)); }
+
+PTG_FN float f_abs(float a) { return fabsf(a); }
+PTG_FN float f_sign(float a) { return (a > 0.0f) ? 1.0f : ((a < 0.0f) ? -1.0f : 0.0f); }
+PTG_FN float f_floor(float a) { return floorf(a); }
+PTG_FN float f_ceil(float a) { return ceilf(a); }
+PTG_FN float f_fract(float a) { return a - floorf(a); }
+PTG_FN float f_sqrt(float a) { return sqrtf(a); }
+PTG_FN float f_isqrt(float a) { return 1.0f / sqrtf(a); }
+PTG_FN float f_exp(float a) { return ptm_expf(a); }
+PTG_FN float f_log(float a) { return ptm_logf(a); }
+PTG_FN float f_sin(float a) { return ptm_sinf(a); }
+PTG_FN float f_cos(float a) { return ptm_cosf(a); }
+PTG_FN float f_acos(float a) { return ptm_acosf(a); }
+PTG_FN float f_radians(float a) { return a * 0.01745329252f; }
+PTG_FN float f_degrees(float a) { return a * 57.29577951f; }
+PTG_FN float f_mod(float a, float b) { return a - b * floorf(a / b); }
+PTG_FN float f_min(float a, float b) { return fminf(a, b); }
+PTG_FN float f_max(float a, float b) { return fmaxf(a, b); }
+PTG_FN float f_pow(float a, float b) { return ptm_powf(a, b); }
+PTG_FN float f_step(float edge, float a) { return (a < edge) ? 0.0f : 1.0f; }
+
+PTG_MAP1(abs, f_abs)
+PTG_MAP1(sign, f_sign)
+PTG_MAP1(floor, f_floor)
+PTG_MAP1(ceil, f_ceil)
+PTG_MAP1(fract, f_fract)
+PTG_MAP1(sqrt, f_sqrt)
+PTG_MAP1(inversesqrt, f_isqrt)
+PTG_MAP1(exp, f_exp)
+PTG_MAP1(log, f_log)
+PTG_MAP1(sin, f_sin)
+PTG_MAP1(cos, f_cos)
+PTG_MAP1(acos, f_acos)
+PTG_MAP1(radians, f_radians)
+PTG_MAP1(degrees, f_degrees)
+PTG_MAP2(mod, f_mod)
+PTG_MAP2(min, f_min)
+PTG_MAP2(max, f_max)
+PTG_MAP2(pow, f_pow)
+PTG_MAP2(step, f_step)
+PTG_FN vec2 step(float e, vec2 a) { return step(vec2(e), a); }
+PTG_FN vec3 step(float e, vec3 a) { return step(vec3(e), a); }
+
+PTG_FN float fma(float a, float b, float c) { return PTM_FMA(a, b, c); }
+PTG_FN vec2 fma(vec2 a, vec2 b, vec2 c) { return vec2(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y)); }
+PTG_FN vec3 fma(vec3 a, vec3 b, vec3 c) {
+    return vec3(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y), PTM_FMA(a.z, b.z, c.z));
+}
+
+template <typename V> PTG_FN V clamp(V a, V lo, V hi) { return min(max(a, lo), hi); }
+PTG_FN vec2 clamp(vec2 a, float lo, float hi) { return min(max(a, lo), hi); }
+PTG_FN vec3 clamp(vec3 a, float lo, float hi) { return min(max(a, lo), hi); }
+PTG_FN float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+PTG_FN vec2 mix(vec2 a, vec2 b, float t) { return a * (1.0f - t) + b * t; }
+PTG_FN vec3 mix(vec3 a, vec3 b, float t) { return a * (1.0f - t) + b * t; }
+PTG_FN vec3 mix(vec3 a, vec3 b, vec3 t) { return a * (1.0f - t) + b * t; }
+PTG_FN float smoothstep(float e0, float e1, float x) {
+    const float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+
+PTG_FN float dot(float a, float b) { return a * b; }
+PTG_FN float dot(vec2 a, vec2 b) { return a.x * b.x + a.y * b.y; }
+PTG_FN float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+PTG_FN float dot(vec4 a, vec4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+template <typename V> PTG_FN float length(V a) { return sqrtf(dot(a, a)); }
+PTG_FN float length(float a) { return fabsf(a); }
+template <typename V> PTG_FN float distance(V a, V b) { return length(a - b); }
+template <typename V> PTG_FN V normalize(V a) { return a * (1.0f / sqrtf(dot(a, a))); }
+PTG_FN vec3 cross(vec3 a, vec3 b) {
+    return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+template <typename V> PTG_FN V reflect(V i, V n) { return i - 2.0f * dot(n, i) * n; }
+
+struct mat2 {
+    vec2 c0, c1;
+    PTG_M mat2(vec2 a, vec2 b) : c0(a), c1(b) {}
+    PTG_M mat2(float a, float b, float c, float d) : c0(a, b), c1(c, d) {}
+};
+PTG_FN vec2 operator*(mat2 m, vec2 v) { return vec2(m.c0.x * v.x + m.c1.x * v.y, m.c0.y * v.x + m.c1.y * v.y); }
+PTG_FN vec2 operator*(vec2 v, mat2 m) { return vec2(dot(v, m.c0), dot(v, m.c1)); }
+struct mat3 {
+    vec3 c0, c1, c2;
+    PTG_M mat3(vec3 a, vec3 b, vec3 c) : c0(a), c1(b), c2(c) {}
+};
+PTG_FN vec3 operator*(mat3 m, vec3 v) {
+    return vec3(m.c0.x * v.x + m.c1.x * v.y + m.c2.x * v.z, m.c0.y * v.x + m.c1.y * v.y + m.c2.y * v.z,
+                m.c0.z * v.x + m.c1.z * v.y + m.c2.z * v.z);
+}
+PTG_FN vec3 operator*(vec3 v, mat3 m) { return vec3(dot(v, m.c0), dot(v, m.c1), dot(v, m.c2)); }
+
+// The shader's polynomial smooth minimum (src/shader.comp:686-702), k = 0.02 * 6,
+// with its ONEBYTHREE constant (src/shader.comp:10).
+PTG_FN float smin(float x, float y) {
+    float k = 0.02f;
+    k *= 6.0f;
+    const float h = fmaxf(k - fabsf(x - y), 0.0f) / k;
+    const float m = h * h * h * 0.5f;
+    const float s = m * k * 0.3333333f;
+    return fminf(x, y) - s;
+}
+PTG_FN vec2 smin(vec2 x, vec2 y) {
+    float k = 0.02f;
+    k *= 6.0f;
+    const float h = fmaxf(k - fabsf(x.x - y.x), 0.0f) / k;
+    const float m = h * h * h * 0.5f;
+    const float s = m * k * 0.3333333f;
+    return (x.x < y.x) ? vec2(x.x - s, x.y + (y.y - x.y) * m) : vec2(y.x - s, x.y + (y.y - x.y) * (1.0f - m));
+}
+
+}  // namespace ptg

@@ -1,7 +1,9 @@
 // pt_megakernel.h — host entry points of the megakernel translation unit.
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
+#endif
 
 #include "pt_scene.cuh"
 
@@ -10,6 +12,7 @@
 #define PT_MK_BLOCK_Y 8
 #define PT_MK_THREADS (PT_MK_BLOCK_X * PT_MK_BLOCK_Y)
 
+#if !defined(__CUDACC_RTC__)
 // Writes 9 floats per object (column-major RotationMatrix of its rotation;
 // identity for spheres and planes) to d_out[9 * total_objects].
 cudaError_t ptk_rotation_setup(const KScene* scene, float* d_out, cudaStream_t stream);
@@ -24,3 +27,4 @@ cudaError_t ptk_launch_megakernel_analytic(const KParams* params, int variant, d
 // Evaluates a pt_mathf function over device arrays (verification hook):
 // fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos.
 cudaError_t ptk_mathf_eval(int fn, const float* x, const float* y, float* out, int n, cudaStream_t stream);
+#endif

@@ -17,7 +17,12 @@
 #include "pt_megakernel.h"
 #include "pt_path.cuh"
 
+// The run-time compiled module (pt_jit.cu) names its kernels ptjit::...
+#if defined(PT_JIT_USER_SDF)
+namespace ptjit {
+#else
 namespace {
+#endif
 
 template <bool TRACE, int FEAT>
 __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constant__ KParams P) {

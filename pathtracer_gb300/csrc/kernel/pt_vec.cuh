@@ -10,8 +10,10 @@
 // the same bits on the GPU and on a CPU.
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 #include "../../../include/pt_mathf.h"
 

@@ -14,12 +14,14 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <vector>
 
 #include "../../include/pt_cuda.h"
 #include "kernel/pt_megakernel.h"
 #include "kernel/pt_wavefront.h"
 #include "kernel/pt_features.h"
 #include "pt_engine.h"
+#include "pt_jit.h"
 
 struct pt_ctx {
     int device = 0;
@@ -49,6 +51,10 @@ struct pt_ctx {
     size_t rgb_bytes = 0;
     size_t colors_bytes = 0;
     uint32_t last_iterations = 0;
+    // GLSL snippets other than the shipped four (PT_SDF_CUSTOM slots), as
+    // translated by pt_glsl_translate, and the module compiled for them.
+    std::vector<JitSlot> custom;
+    JitModule jit;
     std::string err;
 };
 
@@ -92,6 +98,7 @@ cudaError_t sync_device_scene(pt_ctx* ctx) {
 }  // namespace
 
 static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push);
+static int dispatch_jit(pt_ctx* ctx, bool trace);
 cudaError_t ptk_export_rgb8(const void* d_accum, int width, int height, int tonemap, void* d_rgb, cudaStream_t stream);
 
 extern "C" {
@@ -137,6 +144,7 @@ int pt_destroy(pt_ctx* ctx) {
     }
     if (ctx->d_colors) cudaFree(ctx->d_colors);
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
+    pt_jit_unload(ctx->jit);
     if (ctx->done) cudaEventDestroy(ctx->done);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx->params;
@@ -151,8 +159,10 @@ int pt_set_sdf_plugins(pt_ctx* ctx, const pt_sdf_plugin* plugins, int n) {
         return fail(ctx, PT_ERR_UNSUPPORTED, "pt_set_sdf_plugins: at most 32 SDFs can be evaluated (32-bit set mask)");
     for (int i = 0; i < n; i++) {
         if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_TERRAIN)
-            return fail(ctx, PT_ERR_INVALID, "pt_set_sdf_plugins: unknown plug-in kind");
+            return fail(ctx, PT_ERR_INVALID,
+                        "pt_set_sdf_plugins: unknown plug-in kind (GLSL text goes through pt_set_sdfs)");
     }
+    ctx->custom.clear();
     if (n > 0) std::memcpy(ctx->plug, plugins, sizeof(pt_sdf_plugin) * (size_t)n);
     ctx->nplug = n;
     refresh_plugins(ctx);
@@ -167,16 +177,25 @@ int pt_set_sdfs(pt_ctx* ctx, const char* const* sources, int n) {
     if (n > PT_MAX_LIVE_SDFS)
         return fail(ctx, PT_ERR_UNSUPPORTED, "pt_set_sdfs: at most 32 SDFs can be evaluated (32-bit set mask)");
     pt_sdf_plugin tmp[PT_MAX_LIVE_SDFS];
+    std::vector<JitSlot> custom;
     for (int i = 0; i < n; i++) {
-        const int rc = pt_parse_sdf_source(sources[i], &tmp[i]);
-        if (rc != PT_OK) {
-            char buf[160];
-            std::snprintf(buf, sizeof buf,
-                          "pt_set_sdfs: SDF %d is neither a recognised plug-in snippet nor a builtin: spec", i);
-            return fail(ctx, rc, buf);
-        }
+        if (!sources[i]) return fail(ctx, PT_ERR_INVALID, "pt_set_sdfs: null source");
+        if (pt_parse_sdf_source(sources[i], &tmp[i]) == PT_OK) continue;
+        // Other GLSL: compiled at run time with the megakernel.
+        JitSlot j;
+        std::string why;
+        const int rc = pt_jit_translate_slot(sources[i], i, j, why);
+        if (rc != PT_OK) return fail(ctx, rc, "pt_set_sdfs: SDF " + std::to_string(i) + ": " + why);
+        tmp[i] = pt_sdf_plugin{PT_SDF_CUSTOM, PT_SDFMAT_DEFAULT, {0.0f, 0.0f, 0.0f}};
+        custom.push_back(j);
     }
-    return pt_set_sdf_plugins(ctx, tmp, n);
+    if (n > 0) std::memcpy(ctx->plug, tmp, sizeof(pt_sdf_plugin) * (size_t)n);
+    ctx->nplug = n;
+    ctx->custom = custom;
+    refresh_plugins(ctx);
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    PT_CUDA_TRY(ctx, sync_device_scene(ctx));
+    return PT_OK;
 }
 
 int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo) {
@@ -269,8 +288,9 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push) {
     P.accum = ctx->d_accum;
     P.cie = ctx->d_cie;
     P.trace = ctx->trace;
-    if (ctx->engine == PT_ENGINE_WAVEFRONT && push->pathLength > 0) return dispatch_wavefront(ctx, push);
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
+    if (!ctx->custom.empty()) return dispatch_jit(ctx, trace);
+    if (ctx->engine == PT_ENGINE_WAVEFRONT && push->pathLength > 0) return dispatch_wavefront(ctx, push);
     PT_CUDA_TRY(ctx, ptk_launch_megakernel(&P, trace, ctx->stream));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
@@ -554,6 +574,28 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     ctx->last_iterations = E.host_counters->iterations;
     E.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
     PT_CUDA_TRY(ctx, E.resolve(idx));
+    PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
+    return PT_OK;
+}
+
+// Scenes with GLSL snippets beyond the shipped four: the megakernel compiled
+// at run time with their translation (pt_jit.cu), rebuilt when the set of
+// snippets changes.  The wavefront engine has no run-time compiled form, so
+// these scenes always take the plain megakernel.
+static int dispatch_jit(pt_ctx* ctx, bool trace) {
+    const std::string program = pt_jit_program(ctx->custom);
+    if (ctx->jit.key != program) {
+        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        pt_jit_unload(ctx->jit);
+        std::vector<char> cubin;
+        std::string lowered[2], log;
+        int rc = pt_jit_compile(ctx->device, program, cubin, lowered, log);
+        if (rc != PT_OK) return fail(ctx, rc, "compiling the scene's SDF snippets: " + log);
+        rc = pt_jit_load(cubin, lowered, ctx->jit, log);
+        if (rc != PT_OK) return fail(ctx, rc, log);
+        ctx->jit.key = program;
+    }
+    PT_CUDA_TRY(ctx, pt_jit_launch(ctx->jit, ctx->params, trace, ctx->stream));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
 }

@@ -416,9 +416,13 @@ int pt_batch_add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plug
         return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: objects overflow the 1024-float object array");
     if (n[5] > PT_MAX_LIVE_SDFS || nplugins > PT_MAX_LIVE_SDFS)
         return bfail(b, PT_ERR_UNSUPPORTED, "pt_batch_add_scene: at most 32 SDFs can be evaluated (32-bit set mask)");
-    for (int i = 0; i < nplugins; i++)
+    for (int i = 0; i < nplugins; i++) {
+        if (plugins[i].kind == PT_SDF_CUSTOM)
+            return bfail(b, PT_ERR_UNSUPPORTED,
+                         "pt_batch_add_scene: run-time compiled SDFs render through pt_dispatch only");
         if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_TERRAIN)
             return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: unknown plug-in kind");
+    }
     PT_B_TRY(b, cudaSetDevice(b->device));
     KScene* S = new (std::nothrow) KScene;
     if (!S) return bfail(b, PT_ERR_OOM, "pt_batch_add_scene: out of host memory");

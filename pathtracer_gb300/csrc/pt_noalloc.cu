@@ -86,8 +86,10 @@ int build_scene(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplug, KSce
         if (!valid_count(ubo->numObjects[i], caps[i], &n[i])) return PT_ERR_INVALID;
     if (6 * n[0] + 5 * n[1] + 11 * n[2] + 12 * n[3] + 16 * n[4] > PT_MAX_OBJECTS_SIZE) return PT_ERR_INVALID;
     if (n[5] > PT_MAX_LIVE_SDFS || nplug > PT_MAX_LIVE_SDFS) return PT_ERR_UNSUPPORTED;
-    for (int i = 0; i < nplug; i++)
+    for (int i = 0; i < nplug; i++) {
+        if (plugins[i].kind == PT_SDF_CUSTOM) return PT_ERR_UNSUPPORTED;  // run-time compiled: pt_dispatch only
         if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_TERRAIN) return PT_ERR_INVALID;
+    }
     std::memset(S, 0, sizeof(KScene));
     std::memcpy(S->numObjects, ubo->numObjects, sizeof(S->numObjects));
     std::memcpy(S->objects, ubo->objects, sizeof(S->objects));

@@ -53,7 +53,7 @@ UBO_OFFSETS = {
     "CIEXYZ1931": (2774, 1323),
 }
 
-PT_SDF_NONE, PT_SDF_BLOB, PT_SDF_MANDELBULB, PT_SDF_MENGER, PT_SDF_TERRAIN = range(5)
+PT_SDF_NONE, PT_SDF_BLOB, PT_SDF_MANDELBULB, PT_SDF_MENGER, PT_SDF_TERRAIN, PT_SDF_CUSTOM = range(6)
 PT_SDFMAT_DEFAULT, PT_SDFMAT_CONSTANT = 0, 1
 
 PT_EV_HIT_MASK = 0xFFF
@@ -236,6 +236,9 @@ CUDA_API = [
     ("pt_set_sdf_plugins", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i]),
     ("pt_parse_sdf_source", _i, [ctypes.c_char_p, ctypes.POINTER(PtSdfPlugin)]),
     ("pt_upload_scene", _i, [_vp, _vp]),
+    ("pt_jit_check", _i, [ctypes.POINTER(ctypes.c_char_p), _i, _i, ctypes.c_char_p, _sz]),
+    ("pt_glsl_translate", _i, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _sz, ctypes.POINTER(_sz),
+                               ctypes.c_char_p, _sz]),
     ("pt_resize_accum", _i, [_vp, _i, _i]),
     ("pt_dispatch", _i, [_vp, ctypes.POINTER(PtPush)]),
     ("pt_wait", _i, [_vp, ctypes.c_uint64]),

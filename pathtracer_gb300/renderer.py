@@ -498,3 +498,30 @@ def export_rgb8(accum: np.ndarray, tonemap: int = 3) -> np.ndarray:
     if rc != native.PT_OK:
         raise PathTracerError(rc, "export failed")
     return rgb
+
+
+def glsl_translate(glsl: str, prefix: str = "u0_") -> str:
+    """An SDF snippet's GLSL as the C++ the run-time compiled megakernel
+    includes (functions renamed <prefix><name>); raises on unsupported text."""
+    lib = native.cuda()
+    need = ctypes.c_size_t()
+    err = ctypes.create_string_buffer(256)
+    rc = lib.pt_glsl_translate(glsl.encode(), prefix.encode(), None, 0, ctypes.byref(need), err, len(err))
+    if rc != native.PT_OK:
+        raise PathTracerError(rc, err.value.decode())
+    out = ctypes.create_string_buffer(need.value)
+    rc = lib.pt_glsl_translate(glsl.encode(), prefix.encode(), out, need.value, ctypes.byref(need), err, len(err))
+    if rc != native.PT_OK:
+        raise PathTracerError(rc, err.value.decode())
+    return out.value.decode()
+
+
+def jit_check(sources: list[str], sm: int = 103) -> str:
+    """Compiles the run-time megakernel for these snippets without a GPU;
+    returns the compiler log, raises with it on failure."""
+    arr = (ctypes.c_char_p * max(1, len(sources)))(*[s.encode() for s in sources])
+    log = ctypes.create_string_buffer(1 << 16)
+    rc = native.cuda().pt_jit_check(arr, len(sources), sm, log, len(log))
+    if rc != native.PT_OK:
+        raise PathTracerError(rc, log.value.decode())
+    return log.value.decode()

@@ -1,0 +1,152 @@
+"""The GLSL SDF snippet path without a GPU: pt_glsl_translate's rewrite, its
+rejections, the translation's CPU build against the oracle (bit-exact), and
+pt_jit_check (NVRTC compiles the run-time megakernel for sm_103a)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import REFERENCE, ROOT, reference_available
+from user_snippets import LATTICE, SNIPPETS, TORUS
+
+KERNEL_DIR = os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel")
+BUILD_DIR = os.path.join(ROOT, "oracle", "_build")
+
+
+@pytest.fixture(scope="module")
+def pt(built):
+    import pathtracer_gb300 as pt
+
+    return pt
+
+
+def _cpu_build(pt, name: str, snippets: dict) -> ctypes.CDLL:
+    """The translations of `snippets` (name -> GLSL) compiled with g++ over the
+    shim, each exported as c_<name>_sdf / c_<name>_mat(float, float, float)."""
+    code = '#include "pt_glsl_shim.h"\n'
+    for n, glsl in snippets.items():
+        code += pt.glsl_translate(glsl, n + "_")
+        code += f'extern "C" float c_{n}_sdf(float x, float y, float z) {{ return ptg::{n}_sdf(ptg::vec3(x, y, z)); }}\n'
+        code += (f'extern "C" float c_{n}_mat(float x, float y, float z) '
+                 f'{{ return ptg::{n}_sdfmaterial(ptg::vec3(x, y, z)); }}\n')
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    src = os.path.join(BUILD_DIR, f"glsl_{name}.cpp")
+    lib = os.path.join(BUILD_DIR, f"glsl_{name}.so")
+    with open(src, "w") as f:
+        f.write(code)
+    subprocess.run([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+                    "-I", KERNEL_DIR, "-o", lib, src], check=True)
+    return ctypes.CDLL(lib)
+
+
+def _fn(lib, name):
+    f = getattr(lib, name)
+    f.restype = ctypes.c_float
+    f.argtypes = [ctypes.c_float] * 3
+    return f
+
+
+def _points(n=20000, scale=1.5, seed=1):
+    return (np.random.default_rng(seed).standard_normal((n, 3)) * scale).astype(np.float32)
+
+
+def _bits(x: float) -> int:
+    return int(np.float32(x).view(np.uint32))
+
+
+def test_translation_rewrites_glsl(pt):
+    out = pt.glsl_translate(TORUS, "u3_")
+    assert out.startswith("namespace ptg {")
+    out = " ".join(out.split())  # whitespace is kept as written; compare without it
+    assert "constexpr float R = 0.8f;" in out
+    assert "PTG_FN float u3_sdTorus( vec3 p, vec2 t, float& ring)" in out
+    assert "length(p.xz())" in out
+    assert "vec2(R, 0.25f)" in out and "sin(8.0f * p.z)" in out
+    assert "u3_sdTorus(p, vec2(R, 0.25f), ring);" in out
+    assert "PTG_FN float u3_sdf(vec3 p)" in out and "PTG_FN float u3_sdfmaterial(vec3 p)" in out
+    assert "//" not in out.replace("} // namespace ptg", "")
+    lat = pt.glsl_translate(LATTICE, "u0_")
+    assert "max(q.x, max(q.y, q.z))" in lat  # .g .b name fields
+    assert "/*" not in lat
+    assert "1e-3f" in pt.glsl_translate("float sdf(vec3 p){return 1e-3;} float sdfmaterial(vec3 p){return 2.;}", "a_")
+
+
+@pytest.mark.parametrize("text,why", [
+    ("struct S { float a; }; float sdf(vec3 p){return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "struct"),
+    ("uniform float t; float sdf(vec3 p){return t;} float sdfmaterial(vec3 p){return 0.0;}", "uniform"),
+    ("#define K 2.0\nfloat sdf(vec3 p){return K;} float sdfmaterial(vec3 p){return 0.0;}", "preprocessor"),
+    ("float sdf(vec3 p){p.xy = vec2(0.0); return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "swizzle"),
+    ("float sdf(vec3 p){return length(p) - 1.0;}", "must define"),
+    ("float sdf(vec3 p){return 0.0;} float sdfmaterial(vec3 p){return 0.0;", "unbalanced"),
+    ("float sdf(vec3 p){return 0.0; /* open", "unterminated"),
+    ("const vec3 C = vec3(1.0); float sdf(vec3 p){return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "constants"),
+])
+def test_translation_rejects_what_the_shim_lacks(pt, text, why):
+    from pathtracer_gb300 import native
+
+    with pytest.raises(pt.PathTracerError) as e:
+        pt.glsl_translate(text)
+    assert e.value.code == native.PT_ERR_UNSUPPORTED
+    assert why in str(e.value)
+
+
+def test_user_snippets_match_their_c_restatement(pt):
+    """The translation of each test snippet, built for the CPU, agrees bit for
+    bit with the hand restatement the oracle renders with."""
+    from oracle import oracle
+
+    lib = _cpu_build(pt, "user", {n: g for n, (g, _, _) in SNIPPETS.items()})
+    pts = _points()
+    for n, (_, sdf_name, mat_name) in SNIPPETS.items():
+        fs, fm = _fn(lib, f"c_{n}_sdf"), _fn(lib, f"c_{n}_mat")
+        rs, rm = oracle.user_fn(sdf_name), oracle.user_fn(mat_name)
+        bad_s = sum(_bits(fs(*map(float, p))) != _bits(rs(*map(float, p))) for p in pts)
+        bad_m = sum(_bits(fm(*map(float, p))) != _bits(rm(*map(float, p))) for p in pts)
+        assert bad_s == 0 and bad_m == 0, (n, bad_s, bad_m)
+
+
+@pytest.mark.skipif(not reference_available(), reason="needs the reference's sdfs/*.glsl")
+def test_shipped_snippets_translate_to_the_builtins(pt):
+    """The reference's four snippets, run through the translator and built for
+    the CPU, give the oracle's built-in plug-ins bit for bit (distance and
+    material) — the translator and shim carry the shader's arithmetic."""
+    from oracle import oracle
+    from pathtracer_gb300 import native
+
+    kinds = {"blob": native.PT_SDF_BLOB, "mandelbulb": native.PT_SDF_MANDELBULB,
+             "menger": native.PT_SDF_MENGER, "terrain": native.PT_SDF_TERRAIN}
+    texts = {n: open(os.path.join(REFERENCE, "sdfs", n + ".glsl")).read() for n in kinds}
+    lib = _cpu_build(pt, "shipped", texts)
+    olib = oracle.lib()
+    pts = _points()
+    for n, kind in kinds.items():
+        fs, fm = _fn(lib, f"c_{n}_sdf"), _fn(lib, f"c_{n}_mat")
+        pl = native.PtSdfPlugin()
+        assert native.cuda().pt_parse_sdf_source(texts[n].encode(), ctypes.byref(pl)) == native.PT_OK
+        bad_s = bad_m = 0
+        for p in pts:
+            a = fs(*map(float, p))
+            b = olib.pto_sdf_eval(ctypes.byref(pl), p.ctypes.data)
+            bad_s += _bits(a) != _bits(b)
+            if kind in (native.PT_SDF_BLOB, native.PT_SDF_MANDELBULB):
+                bad_m += _bits(fm(*map(float, p))) != _bits(olib.pto_sdf_material(ctypes.byref(pl), p.ctypes.data))
+        assert bad_s == 0 and bad_m == 0, (n, bad_s, bad_m)
+
+
+def test_jit_check_compiles_the_megakernel(pt):
+    """NVRTC builds the run-time megakernel (both trace variants) for sm_103a
+    with two user snippets in slots 0 and 1."""
+    log = pt.jit_check([TORUS, LATTICE], sm=103)
+    assert "error" not in log.lower()
+
+
+def test_jit_check_reports_compiler_errors(pt):
+    from pathtracer_gb300 import native
+
+    bad = "float sdf(vec3 p){ return wobble(p); } float sdfmaterial(vec3 p){ return 0.0; }"
+    with pytest.raises(pt.PathTracerError) as e:
+        pt.jit_check([bad], sm=103)
+    assert e.value.code == native.PT_ERR_UNSUPPORTED
+    assert "wobble" in str(e.value)

@@ -1,0 +1,143 @@
+"""Scenes whose SDF text is not one of the reference's four snippets: the
+text is translated (pt_glsl_translate), compiled into the megakernel with
+NVRTC on the first dispatch and cached.  Parity is against the oracle with a
+hand restatement of each snippet in C (oracle/user_sdfs.c) registered for its
+slot; criteria as in test_gpu_parity (oracle/compare.py)."""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+from conftest import SCENES
+from user_snippets import LATTICE, SNIPPETS, TORUS
+
+pytestmark = pytest.mark.gpu
+
+CUSTOM = {g: (s, m) for g, s, m in SNIPPETS.values()}
+
+
+@pytest.fixture(scope="module")
+def rt(built):
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("no CUDA device: -m gpu tests need a GPU")
+    from pathtracer_gb300 import Context, Scene, cie_analytic
+
+    return {"Context": Context, "Scene": Scene, "cie": cie_analytic()}
+
+
+def _scene(rt, sdfs):
+    with open(os.path.join(SCENES, "mandelbulb_plane.json")) as f:
+        data = json.load(f)
+    data["sdf"] = sdfs
+    return rt["Scene"].parse(json.dumps(data))
+
+
+TORUS_SDF = {"position": [-1.3, 0.6, 0.0], "boundingSize": [2.4, 2.4, 2.4], "glsl": TORUS}
+LATTICE_SDF = {"position": [1.3, 1.0, 0.0], "boundingSize": [2.0, 2.0, 2.0], "glsl": LATTICE}
+BULB_SDF = {"position": [0.0, 1.15, -2.0], "boundingSize": [2.5, 2.5, 2.5], "builtin": "mandelbulb"}
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+def test_user_snippets_match_oracle(rt, engine):
+    """Two user snippets and a shipped one in one scene, traced per path.
+    The wavefront engine setting routes such scenes to the compiled
+    megakernel as well."""
+    from oracle import compare
+
+    W, H, spf, depth = 64, 48, 4, 6
+    scene = _scene(rt, [TORUS_SDF, LATTICE_SDF, BULB_SDF])
+    ubo = scene.pack_ubo(rt["cie"])
+    plugins = compare.plugins_for(scene, custom=CUSTOM)
+    with rt["Context"](0) as ctx:
+        ctx.set_engine(engine)
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        push = scene.push_constants(W, H, spf, spf, spf, depth)
+        acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=depth)
+        acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
+        rep = compare.compare(acc_o, tr_o, acc_g, tr_g, spf)
+        print(rep)
+        assert compare.passes(rep), rep
+        # the sdf hits are there: some paths end on each user snippet's materials
+        assert np.isfinite(acc_g).all() and acc_g[..., :3].max() > 0
+
+
+def test_untraced_progressive_matches_oracle(rt):
+    """The untraced kernel of the compiled module over three progressive
+    dispatches (running mean), with the snippets in other slots."""
+    from oracle import compare
+
+    W, H, spf, depth = 48, 40, 2, 8
+    scene = _scene(rt, [BULB_SDF, LATTICE_SDF, TORUS_SDF])
+    ubo = scene.pack_ubo(rt["cie"])
+    plugins = compare.plugins_for(scene, custom=CUSTOM)
+    acc_o = np.zeros((H, W, 4), np.float32)
+    with rt["Context"](0) as ctx:
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        for it in range(3):
+            push = scene.push_constants(W, H, spf * (it + 1), spf * (it + 1), spf, depth)
+            compare.run_oracle(ubo, push, plugins, accum=acc_o)
+            ctx.dispatch(push)
+        ctx.wait()
+        acc_g = ctx.read_accum()
+    rel = np.abs(acc_o - acc_g) / np.maximum(np.maximum(np.abs(acc_o), np.abs(acc_g)), 1e-6)
+    frac_bad = float(np.mean(rel[..., :3].max(axis=-1) > 1e-4))
+    assert frac_bad < 0.02, frac_bad
+
+
+def test_module_is_cached_across_scene_changes(rt):
+    """The first dispatch compiles; later ones, also after a scene with only
+    shipped snippets was bound in between, reuse the module."""
+    W, H = 32, 32
+    custom = _scene(rt, [TORUS_SDF])
+    plain = rt["Scene"].load(os.path.join(SCENES, "mandelbulb_plane.json"))
+    with rt["Context"](0) as ctx:
+        ctx.resize_accum(W, H)
+        times = []
+        for scene in (custom, plain, custom):
+            ctx.bind(scene, rt["cie"])
+            t0 = time.perf_counter()
+            ctx.dispatch(scene.push_constants(W, H, 1, 1, 1, 4))
+            ctx.wait()
+            times.append(time.perf_counter() - t0)
+        print("dispatch seconds (compile, shipped, cached):", times)
+        assert times[2] < 0.5 * times[0]
+        assert np.isfinite(ctx.read_accum()).all()
+
+
+def test_compile_error_is_reported_and_context_recovers(rt):
+    from pathtracer_gb300 import PathTracerError, native
+
+    W, H = 16, 16
+    bad = dict(TORUS_SDF, glsl="float sdf(vec3 p){ return wobble(p); }\nfloat sdfmaterial(vec3 p){ return 1.0; }")
+    with rt["Context"](0) as ctx:
+        ctx.resize_accum(W, H)
+        scene = _scene(rt, [bad])
+        ctx.bind(scene, rt["cie"])
+        with pytest.raises(PathTracerError) as e:
+            ctx.dispatch(scene.push_constants(W, H, 1, 1, 1, 4))
+        assert e.value.code == native.PT_ERR_UNSUPPORTED and "wobble" in str(e.value)
+        good = rt["Scene"].load(os.path.join(SCENES, "cornell_box.json"))
+        ctx.bind(good, rt["cie"])
+        ctx.dispatch(good.push_constants(W, H, 1, 1, 1, 4))
+        ctx.wait()
+        assert np.isfinite(ctx.read_accum()).all()
+
+
+def test_batch_rejects_run_time_snippets(rt):
+    from pathtracer_gb300 import Batch, PathTracerError, native
+
+    scene = _scene(rt, [TORUS_SDF])
+    with Batch(0) as b:
+        with pytest.raises(PathTracerError) as e:
+            b.add_scene(scene.pack_ubo(rt["cie"]), [native.plugin(native.PT_SDF_CUSTOM)])
+        assert e.value.code == native.PT_ERR_UNSUPPORTED
+    with rt["Context"](0) as ctx:
+        with pytest.raises(PathTracerError) as e:
+            ctx.set_sdf_plugins([native.plugin(native.PT_SDF_CUSTOM)])
+        assert e.value.code == native.PT_ERR_INVALID
