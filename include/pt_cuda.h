@@ -53,6 +53,7 @@ extern "C" {
 #define PT_ERR_KERNEL 7        /* a kernel reported an error through its status word */
 #define PT_ERR_TOO_LARGE 8     /* the request exceeds pt_dispatch_noalloc's fixed scratch */
 #define PT_ERR_BUSY 9          /* the resource is still in use by passes in flight */
+#define PT_ERR_CANCELLED 10    /* a served job was cancelled (pt_server_cancel) */
 
 /* Byte-for-byte the reference's UniformBufferObject (src/pathtracer.cpp:187-195)
  * and the shader's `ubo` block (src/shader.comp:19-27): 4097 floats = 16388 B.

@@ -207,6 +207,11 @@ int pt_server_submit(pt_server* server, const pt_server_job* job, uint64_t* job_
 int pt_server_poll(pt_server* server, pt_server_result* done, int capacity, int* ndone);
 /* Jobs queued, active or finished but not yet returned by pt_server_poll. */
 int pt_server_pending(pt_server* server);
+/* Cancels a job that has not finished: a queued job is dropped at once; an
+ * admitted one gets no further passes and finishes when its passes in flight
+ * have resolved.  pt_server_poll then returns it with status
+ * PT_ERR_CANCELLED and the samples it rendered. */
+int pt_server_cancel(pt_server* server, uint64_t job_id);
 int pt_server_read_image(pt_server* server, uint64_t job_id, float* host, size_t bytes);
 int pt_server_release(pt_server* server, uint64_t job_id);
 int pt_server_get_stats(pt_server* server, pt_server_stats* out);

@@ -118,6 +118,7 @@ uint64_t job_bytes(const pt_server* s, const Job& j) {
 }
 
 bool done_with(const Job& j) {
+    if (j.status == PT_ERR_CANCELLED) return true;
     const int spp = j.passes_done * j.spf;
     if (j.req.target_rmse > 0.0 && j.rmse >= 0.0 && j.rmse <= j.req.target_rmse) return true;
     return spp >= j.req.max_spp;
@@ -168,7 +169,7 @@ int admit_batched(pt_server* s, double t) {
 int feed_batched(pt_server* s) {
     for (uint64_t id : s->active) {
         Job& j = s->jobs[id];
-        while (!j.finished && j.passes_in_flight < s->opts.passes_in_flight &&
+        while (!j.finished && j.status == PT_OK && j.passes_in_flight < s->opts.passes_in_flight &&
                (j.passes_done + j.passes_in_flight) * j.spf < j.req.max_spp) {
             const SceneEntry& sc = s->scenes[j.req.scene_key];
             const pt_push p = pass_push(j, j.passes_done + j.passes_in_flight + 1);
@@ -445,6 +446,24 @@ int pt_server_poll(pt_server* s, pt_server_result* done, int capacity, int* ndon
 int pt_server_pending(pt_server* s) {
     if (!s) return -1;
     return (int)(s->queue.size() + s->active.size() + s->ready.size());
+}
+
+int pt_server_cancel(pt_server* s, uint64_t job_id) {
+    if (!s) return PT_ERR_INVALID;
+    auto it = s->jobs.find(job_id);
+    if (it == s->jobs.end() || it->second.finished)
+        return sfail(s, PT_ERR_INVALID, "pt_server_cancel: unknown or finished job");
+    Job& j = it->second;
+    j.status = PT_ERR_CANCELLED;
+    auto q = std::find(s->queue.begin(), s->queue.end(), job_id);
+    if (q != s->queue.end()) {
+        s->queue.erase(q);
+        finish(s, j, now_s(s));
+    } else if (j.passes_in_flight == 0) {  // admitted, between passes (always so on the plain path)
+        finish(s, j, now_s(s));
+        s->active.erase(std::remove(s->active.begin(), s->active.end(), job_id), s->active.end());
+    }  // else it finishes when its passes in flight resolve (poll_batched)
+    return PT_OK;
 }
 
 int pt_server_read_image(pt_server* s, uint64_t job_id, float* host, size_t bytes) {

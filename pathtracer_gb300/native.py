@@ -24,6 +24,7 @@ PT_ERR_OOM = 6
 PT_ERR_KERNEL = 7
 PT_ERR_TOO_LARGE = 8
 PT_ERR_BUSY = 9
+PT_ERR_CANCELLED = 10
 PT_NOALLOC_MAX_SAMPLES = 1 << 20
 
 PT_ENGINE_MEGAKERNEL = 0
@@ -320,6 +321,7 @@ HOST_API = [
     ("pt_server_pending", _i, [_vp]),
     ("pt_server_read_image", _i, [_vp, ctypes.c_uint64, _vp, _sz]),
     ("pt_server_release", _i, [_vp, ctypes.c_uint64]),
+    ("pt_server_cancel", _i, [_vp, ctypes.c_uint64]),
     ("pt_server_get_stats", _i, [_vp, ctypes.POINTER(PtServerStats)]),
     ("pt_server_run_trace", _i, [_vp, ctypes.POINTER(PtServerJob), ctypes.POINTER(ctypes.c_double), _i,
                                  ctypes.POINTER(PtServerResult)]),

@@ -460,6 +460,9 @@ class Server:
     def release(self, job_id: int):
         self._check(self._lib.pt_server_release(self._h, ctypes.c_uint64(job_id)))
 
+    def cancel(self, job_id: int):
+        self._check(self._lib.pt_server_cancel(self._h, ctypes.c_uint64(job_id)))
+
     def stats(self) -> dict:
         st = native.PtServerStats()
         self._check(self._lib.pt_server_get_stats(self._h, ctypes.byref(st)))

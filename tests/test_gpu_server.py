@@ -1,7 +1,8 @@
 """Render serving (pt_server_*) on the GPU: a job's result is the same bits
 alone, in a mix of concurrent jobs, and through the plain serial megakernel;
 admission keeps admitted jobs within the memory budget; arrival traces
-replay with every job finishing after it arrived."""
+replay with every job finishing after it arrived; cancelled jobs stop at a
+pass boundary."""
 import numpy as np
 import pytest
 
@@ -110,3 +111,35 @@ def test_server_errors(env):
         with pytest.raises(renderer.PathTracerError) as e:
             s.submit(huge)
         assert e.value.code == native.PT_ERR_TOO_LARGE
+
+
+def test_cancel_queued_admitted_and_plain(env):
+    """A queued job is dropped at once; an admitted one stops after its pass
+    in flight; the plain path stops between passes.  Cancelled jobs come back
+    with PT_ERR_CANCELLED and the samples they rendered; the others finish."""
+    native, renderer, scenes = env
+    per_job = W * H * 16 * (1 + 8)
+    with _server(renderer, native, scenes, native.PT_SERVE_BATCHED, hbm_budget=per_job + 100) as s:
+        ids = [s.submit(renderer.Server.job(k, scenes[k][3], 512 if k == 0 else 24)) for k in range(3)]
+        s.cancel(ids[2])  # still queued
+        first = s.poll()  # admits job 0 (budget: one job), queues its first pass, returns the cancelled one
+        assert [r.job_id for r in first] == [ids[2]]
+        assert first[0].status == native.PT_ERR_CANCELLED and first[0].spp == 0 and first[0].t_admit < 0
+        assert s.stats()["active"] == 1
+        s.cancel(ids[0])  # admitted, pass in flight
+        done = {r.job_id: r for r in s.drain()}
+        assert set(done) == {ids[0], ids[1]}
+        assert done[ids[0]].status == native.PT_ERR_CANCELLED and 8 <= done[ids[0]].spp < 512
+        assert done[ids[1]].status == native.PT_OK and done[ids[1]].spp == 24
+        assert s.stats()["bytes_in_use"] == 0
+        with pytest.raises(renderer.PathTracerError) as e:
+            s.cancel(ids[1])  # finished
+        assert e.value.code == native.PT_ERR_INVALID
+    with _server(renderer, native, scenes, native.PT_SERVE_PLAIN) as s:
+        a = s.submit(renderer.Server.job(0, scenes[0][3], 512))
+        b = s.submit(renderer.Server.job(1, scenes[1][3], 16))
+        assert s.poll() == []  # one pass of job a
+        s.cancel(a)
+        done = {r.job_id: r for r in s.drain()}
+        assert done[a].status == native.PT_ERR_CANCELLED and done[a].spp == 8
+        assert done[b].status == native.PT_OK and done[b].spp == 16
