@@ -81,6 +81,7 @@ def parse_args():
     ap.add_argument("--refill", type=int, default=0, help="wavefront march refill threshold (0: default)")
     ap.add_argument("--drain", type=int, default=-1, help="wavefront march drain lanes (-1: default)")
     ap.add_argument("--blocks", type=int, default=0, help="wavefront stage blocks per SM (0: default)")
+    ap.add_argument("--inner", type=int, default=0, help="wavefront SDF evaluations per march lane between refills (0: default)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
     ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64", "serve", "progressive"])
@@ -722,7 +723,8 @@ def main():
         ctx.set_wavefront_pool(args.pool)
     if args.budget:
         ctx.set_march_budget(args.budget)
-    knobs = {k: v for k, v in (("refill_min", args.refill), ("blocks_per_sm", args.blocks)) if v}
+    knobs = {k: v for k, v in (("refill_min", args.refill), ("blocks_per_sm", args.blocks),
+                               ("march_inner", args.inner)) if v}
     if args.drain >= 0:
         knobs["drain_lanes"] = args.drain
     if knobs:

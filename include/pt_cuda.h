@@ -270,6 +270,7 @@ typedef struct pt_wavefront_tuning {
     int32_t refill_min;    /* idle lanes a march warp gathers before refilling them together (1..32) */
     int32_t drain_lanes;   /* a march warp left with fewer rays after its queue drained suspends them (0..32) */
     int32_t blocks_per_sm; /* stage-kernel blocks of 256 threads per SM (1..8) */
+    int32_t march_inner;   /* SDF evaluations per march lane between the warp's refills (1..16; default 6) */
 } pt_wavefront_tuning;
 int pt_get_wavefront_tuning(pt_ctx* ctx, pt_wavefront_tuning* out);
 int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* tuning);

@@ -35,10 +35,49 @@ namespace {
 
 constexpr uint32_t kShadowFlag = 1u << 30;
 constexpr int kStageThreads = 256;
+// Launch bounds of the queue stages: resident blocks of kStageThreads per SM
+// asked of the compiler (registers capped at 65536 / (256 x blocks)), so that
+// the default grid of 4 blocks per SM is resident at once.  Measured on
+// GB300: march, shade and isect at 4 blocks (64 registers) are 2-3 % faster
+// end to end than with the compiler's own choice (70-74 registers, 3 blocks).
+// PT_WF_<STAGE>_BLOCKS overrides the count; 0 leaves only the block size.
+#ifndef PT_WF_ISECT_BLOCKS
+#define PT_WF_ISECT_BLOCKS 4
+#endif
+#ifndef PT_WF_SHADE_BLOCKS
+#define PT_WF_SHADE_BLOCKS 4
+#endif
+#ifndef PT_WF_MARCH_BLOCKS
+#define PT_WF_MARCH_BLOCKS 4
+#endif
+#ifndef PT_WF_GEN_BLOCKS
+#define PT_WF_GEN_BLOCKS 0
+#endif
+#if PT_WF_ISECT_BLOCKS > 0
+#define PT_ISECT_BOUNDS __launch_bounds__(kStageThreads, PT_WF_ISECT_BLOCKS)
+#else
+#define PT_ISECT_BOUNDS __launch_bounds__(kStageThreads)
+#endif
+#if PT_WF_SHADE_BLOCKS > 0
+#define PT_SHADE_BOUNDS __launch_bounds__(kStageThreads, PT_WF_SHADE_BLOCKS)
+#else
+#define PT_SHADE_BOUNDS __launch_bounds__(kStageThreads)
+#endif
+#if PT_WF_MARCH_BLOCKS > 0
+#define PT_MARCH_BOUNDS __launch_bounds__(kStageThreads, PT_WF_MARCH_BLOCKS)
+#else
+#define PT_MARCH_BOUNDS __launch_bounds__(kStageThreads)
+#endif
+#if PT_WF_GEN_BLOCKS > 0
+#define PT_GEN_BOUNDS __launch_bounds__(kStageThreads, PT_WF_GEN_BLOCKS)
+#else
+#define PT_GEN_BOUNDS __launch_bounds__(kStageThreads)
+#endif
 // wf_march: after a large queue is drained, a warp with fewer rays than
 // WfArgs::drain_lanes suspends those that have marched kDrainMinSteps steps
 // in this launch, for the next iteration.
 constexpr int kDrainMinSteps = 8;
+
 // SphereTracing's over-relaxation start (SC:781).
 constexpr float kOmegaMax = 1.70f;
 
@@ -139,7 +178,7 @@ PT_DI uint64_t jobs_total(const WfArgs& A, uint32_t hi) {
     return L.first + (uint64_t)L.count;
 }
 
-__global__ void __launch_bounds__(kStageThreads) wf_gen(const __grid_constant__ WfArgs A) {
+__global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
     const uint32_t job_lo = C.job_lo, job_hi = C.job_hi;
     const uint64_t remaining = jobs_total(A, job_hi) - C.next_sample;
@@ -193,7 +232,7 @@ __global__ void wf_job_add(const __grid_constant__ WfArgs A, const WfJob job, ui
     C.job_lo = lo;
 }
 
-__global__ void __launch_bounds__(kStageThreads) wf_isect(const __grid_constant__ WfArgs A) {
+__global__ void PT_ISECT_BOUNDS wf_isect(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
     const uint32_t cur = C.cur;
     const uint32_t n = C.n_isect[cur];
@@ -278,7 +317,7 @@ PT_DI void stage_flush(uint32_t* buf, uint32_t count, uint32_t* queue, uint32_t*
     if ((uint32_t)lane < count) queue[b + (uint32_t)lane] = buf[lane];
 }
 
-__global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant__ WfArgs A) {
+__global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
     const uint32_t cur = C.cur;
     const uint32_t n = C.n_march[cur];
@@ -288,6 +327,7 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
     const int lane = threadIdx.x & 31;
     const int budget = A.march_budget;
     const int refill_min = A.refill_min;
+    const int inner = A.march_inner;
     int steps = 0;
     // Draining only pays while the queue holds more rays than the grid has lanes.
     const bool many = n >= 2u * gridDim.x * blockDim.x;
@@ -380,98 +420,106 @@ __global__ void __launch_bounds__(kStageThreads) wf_march(const __grid_constant_
         // continue in full warps next iteration instead.
         const bool drain = many && __ballot_sync(0xffffffffu, exhausted) != 0 && __popc(live) < A.drain_lanes;
 
-        // One SDF evaluation.
-        const bool evalLane = (phase >= MP_SIGN && phase <= MP_NORMAL5);
-        float3 q = p;
-        if (phase == MP_SIGN) q = org;
-        if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
-            // CalculateNumericalSDFNormals (SC:721-730): p +- h.xyy, h.yxy, h.yyx
-            const int j = phase - MP_NORMAL0;
-            const float ex = (j == 0) ? e : 0.0f, ey = (j == 2) ? e : 0.0f, ez = (j == 4) ? e : 0.0f;
-            const float mx = (j == 1) ? e : 0.0f, my = (j == 3) ? e : 0.0f, mz = (j == 5) ? e : 0.0f;
-            q = (j & 1) ? f3(p.x - mx, p.y - my, p.z - mz) : f3(p.x + ex, p.y + ey, p.z + ez);
-        }
-        float val = 0.0f;
-        if (evalLane) val = scene_sdf(*Sp, q, set1);
-
+        // A.march_inner SDF evaluations per lane before the warp refills,
+        // shades finished hits and appends to the queues again: the warp
+        // pays for those once per several evaluations, and a lane whose ray
+        // finishes or is suspended on the way idles until then.
         bool finished = false, hit = false, suspend = false;
-        if (phase == MP_SIGN) {
-            k = sign_glsl(val);
-            phase = MP_STEP;
-        } else if (phase == MP_STEP) {
-            const float radius = val;
-            bool exitLoop = false;
-            if (insT > (fabsf(prevR) + fabsf(radius))) {
-                t -= insT;
-                omega = 1.0f;
-                insT = prevR * omega * k;
-                t += insT;
-                p = fma3s(dir, t, org);
-            } else if (fabsf(radius) < 1e-4f) {
-                exitLoop = true;
-                converged = true;
-            } else {
-                if (t > tmm.y) {
-                    points += 1;
-                } else {
-                    points = 0;
-                }
-                bool researched = false;
-                if (points >= 2) {
-                    t = tmm.y + 1e-3f;
-                    tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
-                    const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-                    if (search_sdf(*Sp, fma3s(dir, t, org), invdir, tmm, set1)) {
-                        tmm.x += t;
-                        tmm.y += t;
-                        t = fmaxf(tmm.x, t);
-                        p = fma3s(dir, t, org);
-                        researched = true;
-                    } else {
-                        finished = true;  // left every SDF box: no SDF hit
-                    }
-                }
-                if (!finished && !researched) {
-                    insT = radius * omega * k;
+#pragma unroll 1
+        for (int sub = 0; sub < inner; sub++) {
+            // One SDF evaluation.
+            const bool evalLane = (phase >= MP_SIGN && phase <= MP_NORMAL5) && !finished && !suspend;
+            if (sub > 0 && __ballot_sync(0xffffffffu, evalLane) == 0) break;
+            float3 q = p;
+            if (phase == MP_SIGN) q = org;
+            if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
+                // CalculateNumericalSDFNormals (SC:721-730): p +- h.xyy, h.yxy, h.yyx
+                const int j = phase - MP_NORMAL0;
+                const float ex = (j == 0) ? e : 0.0f, ey = (j == 2) ? e : 0.0f, ez = (j == 4) ? e : 0.0f;
+                const float mx = (j == 1) ? e : 0.0f, my = (j == 3) ? e : 0.0f, mz = (j == 5) ? e : 0.0f;
+                q = (j & 1) ? f3(p.x - mx, p.y - my, p.z - mz) : f3(p.x + ex, p.y + ey, p.z + ez);
+            }
+            float val = 0.0f;
+            if (evalLane) val = scene_sdf(*Sp, q, set1);
+            if (!evalLane) continue;
+            if (phase == MP_SIGN) {
+                k = sign_glsl(val);
+                phase = MP_STEP;
+            } else if (phase == MP_STEP) {
+                const float radius = val;
+                bool exitLoop = false;
+                if (insT > (fabsf(prevR) + fabsf(radius))) {
+                    t -= insT;
+                    omega = 1.0f;
+                    insT = prevR * omega * k;
                     t += insT;
                     p = fma3s(dir, t, org);
-                    const float omegaSpeedFactor = fminf(radius / prevR, 0.99f);
-                    omega += omegaSpeed * (fminf(1.0f / (1.0f - omegaSpeedFactor), omegaMax) - omega);
-                    prevR = radius;
-                }
-            }
-            if (!finished && !exitLoop) {
-                iter++;
-                if (iter >= 512) exitLoop = true;
-            }
-            if (exitLoop) {
-                if (t < hitdist) {
-                    p = fma3s(dir, t, org);
-                    phase = MP_NORMAL0;
+                } else if (fabsf(radius) < 1e-4f) {
+                    exitLoop = true;
+                    converged = true;
                 } else {
+                    if (t > tmm.y) {
+                        points += 1;
+                    } else {
+                        points = 0;
+                    }
+                    bool researched = false;
+                    if (points >= 2) {
+                        t = tmm.y + 1e-3f;
+                        tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
+                        const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+                        if (search_sdf(*Sp, fma3s(dir, t, org), invdir, tmm, set1)) {
+                            tmm.x += t;
+                            tmm.y += t;
+                            t = fmaxf(tmm.x, t);
+                            p = fma3s(dir, t, org);
+                            researched = true;
+                        } else {
+                            finished = true;  // left every SDF box: no SDF hit
+                        }
+                    }
+                    if (!finished && !researched) {
+                        insT = radius * omega * k;
+                        t += insT;
+                        p = fma3s(dir, t, org);
+                        const float omegaSpeedFactor = fminf(radius / prevR, 0.99f);
+                        omega += omegaSpeed * (fminf(1.0f / (1.0f - omegaSpeedFactor), omegaMax) - omega);
+                        prevR = radius;
+                    }
+                }
+                if (!finished && !exitLoop) {
+                    iter++;
+                    if (iter >= 512) exitLoop = true;
+                }
+                if (exitLoop) {
+                    if (t < hitdist) {
+                        p = fma3s(dir, t, org);
+                        phase = MP_NORMAL0;
+                    } else {
+                        finished = true;
+                    }
+                } else if (!finished && (++steps >= budget || (drain && steps >= kDrainMinSteps))) {
+                    // out of budget for this launch: save the state, continue next iteration
+                    M.m0[slot] = make_float4(t, insT, omega, prevR);
+                    M.m1[slot] = make_float4(tmm.x, tmm.y, k, __uint_as_float(set1));
+                    M.m2[slot] = 0x80000000u | ((uint32_t)min(points, 0xffff) << 10) | (uint32_t)iter;
+                    suspend = true;
+                }
+            } else if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
+                const int j = phase - MP_NORMAL0;
+                if ((j & 1) == 0) {
+                    nplus = val;
+                } else {
+                    const float dv = nplus - val;
+                    if (j == 1) nv.x = dv;
+                    else if (j == 3) nv.y = dv;
+                    else nv.z = dv;
+                }
+                phase++;
+                if (phase > MP_NORMAL5) {
+                    hit = true;
                     finished = true;
                 }
-            } else if (!finished && (++steps >= budget || (drain && steps >= kDrainMinSteps))) {
-                // out of budget for this launch: save the state, continue next iteration
-                M.m0[slot] = make_float4(t, insT, omega, prevR);
-                M.m1[slot] = make_float4(tmm.x, tmm.y, k, __uint_as_float(set1));
-                M.m2[slot] = 0x80000000u | ((uint32_t)min(points, 0xffff) << 10) | (uint32_t)iter;
-                suspend = true;
-            }
-        } else if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
-            const int j = phase - MP_NORMAL0;
-            if ((j & 1) == 0) {
-                nplus = val;
-            } else {
-                const float dv = nplus - val;
-                if (j == 1) nv.x = dv;
-                else if (j == 3) nv.y = dv;
-                else nv.z = dv;
-            }
-            phase++;
-            if (phase > MP_NORMAL5) {
-                hit = true;
-                finished = true;
             }
         }
 
@@ -572,7 +620,7 @@ PT_DI void finish_shade(const WfArgs& A, const WfJob& J, const PathState& ps, St
 // (the light sample's contribution, then the bounce's end), then primary
 // hits (emission or BRDF and light sampling).
 template <bool TRACE>
-__global__ void __launch_bounds__(kStageThreads) wf_shade(const __grid_constant__ WfArgs A) {
+__global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
     const uint32_t nxt = C.cur ^ 1u;
     const PoolView v = view(A);

@@ -76,6 +76,7 @@ struct WfArgs {
     int march_budget;  // sphere-tracing iterations per ray per march launch
     int refill_min;    // idle lanes a march warp gathers before it refills them at once
     int drain_lanes;   // a drained march warp with fewer rays suspends them (0: never)
+    int march_inner;   // SDF evaluations per lane between a march warp's refills and queue appends
     int persist_refill;  // idle lanes a persistent warp gathers before starting new samples together
 };
 

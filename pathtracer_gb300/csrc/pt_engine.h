@@ -71,7 +71,7 @@ struct WfEngine {
     // Sphere-tracing iterations per ray per march launch.
     void set_march_budget(int budget);
     // March refill threshold, drain threshold and stage-kernel blocks per SM.
-    void set_tuning(int refill_min, int drain_lanes, int blocks_per_sm);
+    void set_tuning(int refill_min, int drain_lanes, int blocks_per_sm, int march_inner);
     // Staged kernels (false) or the persistent path kernel (true).
     void set_persistent(bool on);
     // Persistent mode: every sample added so far is covered by a launch.

@@ -141,6 +141,7 @@ class PtWavefrontTuning(ctypes.Structure):
         ("refill_min", ctypes.c_int32),
         ("drain_lanes", ctypes.c_int32),
         ("blocks_per_sm", ctypes.c_int32),
+        ("march_inner", ctypes.c_int32),
     ]
 
 

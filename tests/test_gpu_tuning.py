@@ -24,9 +24,11 @@ def env(built):
 
 SETTINGS = [
     {},
-    {"refill_min": 8, "drain_lanes": 0, "blocks_per_sm": 2},
-    {"pool_slots": 4096, "march_budget": 3, "refill_min": 32, "drain_lanes": 32, "blocks_per_sm": 1},
-    {"pool_slots": 1 << 16, "march_budget": 512, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 8},
+    {"refill_min": 8, "drain_lanes": 0, "blocks_per_sm": 2, "march_inner": 1},
+    {"pool_slots": 4096, "march_budget": 3, "refill_min": 32, "drain_lanes": 32, "blocks_per_sm": 1,
+     "march_inner": 16},
+    {"pool_slots": 1 << 16, "march_budget": 512, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 8,
+     "march_inner": 3},
 ]
 
 
@@ -63,7 +65,9 @@ def test_autotune_keeps_the_accumulator_and_installs_a_setting(env):
         assert np.array_equal(ctx.read_accum(), before)
         assert ctx.tuning() == best and secs > 0.0
         assert 1024 <= best["pool_slots"] and 1 <= best["refill_min"] <= 32 and 1 <= best["blocks_per_sm"] <= 8
-        with pytest.raises(PathTracerError) as e:
-            ctx.set_tuning(refill_min=0)
-        assert e.value.code == native.PT_ERR_INVALID
+        assert 1 <= best["march_inner"] <= 16
+        for bad in ({"refill_min": 0}, {"march_inner": 0}, {"march_inner": 17}):
+            with pytest.raises(PathTracerError) as e:
+                ctx.set_tuning(**bad)
+            assert e.value.code == native.PT_ERR_INVALID
         assert ctx.tuning() == best
