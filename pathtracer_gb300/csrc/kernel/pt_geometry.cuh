@@ -449,6 +449,25 @@ PT_DI float scene_sdf(const KScene& S, float3 p, uint32_t set1) {
     }
     return sdf;
 }
+// scene_sdf that also reports the SDF whose material SDFMATERIAL() picks at
+// p (SC:713-719: the last i with !(running minimum < d_i); -1 for none), so
+// a march that converged at p needs only that SDF's material function there.
+PT_DI float scene_sdf_sel(const KScene& S, float3 p, uint32_t set1, int& sel) {
+    float sdf = PT_MAXDIST;
+    sel = -1;
+    uint32_t bits = set1 & ((S.meta.nplug >= 32) ? 0xFFFFFFFFu : ((1u << S.meta.nplug) - 1u));
+    while (bits) {
+        const int i = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        const int kind = S.plug[i].kind;
+        if (kind != PT_SDF_NONE) {
+            const float di = plugin_sdf(kind, i, p - sdf_pos(S, i));
+            if (!(sdf < di)) sel = i;
+            sdf = fminf(sdf, di);
+        }
+    }
+    return sdf;
+}
 // Out-of-line copy for the cold call sites (sign at the origin, normals).
 static __device__ __noinline__ float scene_sdf_cold(const KScene& S, float3 p, uint32_t set1) { return scene_sdf(S, p, set1); }
 
@@ -471,23 +490,19 @@ static __device__ __noinline__ float scene_sdf_material(const KScene& S, float3 
     return mat;
 }
 
-// RayIntersectAABB, SC:278-287.
-// SDFMATERIAL at the end of a march.  When the march converged
-// (|SDF(p)| < 1e-4 over the set) and the set holds one live plug-in, that
-// plug-in is the closest one (its distance is the set's, far below
-// PT_MAXDIST), so the reference's selection (SC:704-719) reduces to its
-// sdfmaterial at p without evaluating the distance again.  Otherwise the
-// full selection runs.
-PT_DI float scene_sdf_material_hit(const KScene& S, float3 p, uint32_t set1, bool converged) {
-    const uint32_t bits = set1 & ((S.meta.nplug >= 32) ? 0xFFFFFFFFu : ((1u << S.meta.nplug) - 1u));
-    if (converged && bits != 0u && (bits & (bits - 1u)) == 0u) {
-        const int i = __ffs(bits) - 1;
-        const pt_sdf_plugin pl = S.plug[i];
-        if (pl.kind != PT_SDF_NONE) return plugin_material(pl, i, p - sdf_pos(S, i));
-    }
+// SDFMATERIAL (SC:704-719) at a sphere-tracing hit p.  hit_sel >= -1: the
+// march converged on an evaluation at p itself, and hit_sel is what
+// scene_sdf_sel reported there (the same distances in the same order), so the
+// reference's selection reduces to that SDF's sdfmaterial at p, or 0 for
+// none, without evaluating the distances again; otherwise (-2: the march ran
+// out of steps) the full selection runs.
+PT_DI float scene_sdf_material_hit(const KScene& S, float3 p, uint32_t set1, int hit_sel) {
+    if (hit_sel >= 0) return plugin_material(S.plug[hit_sel], hit_sel, p - sdf_pos(S, hit_sel));
+    if (hit_sel == -1) return 0.0f;
     return scene_sdf_material(S, p, set1);
 }
 
+// RayIntersectAABB, SC:278-287.
 PT_DI float2 ray_aabb(float3 origin, float3 invdir, float3 pos, float3 size) {
     const float3 lo = origin - pos;
     const float3 tMin0 = fma3(size, f3(-0.5f, -0.5f, -0.5f), -lo) * invdir;
@@ -548,10 +563,11 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
         return false;
     }
     const float k = sign_glsl(scene_sdf_cold(S, org, set1));
-    bool converged = false;
+    int hit_sel = -2;  // >= -1 once the march converged (scene_sdf_material_hit)
 #pragma unroll 1
     for (int i = 0; i < 512; i++) {
-        const float radius = scene_sdf(S, p, set1);
+        int sel;
+        const float radius = scene_sdf_sel(S, p, set1, sel);
         if (insT > (fabsf(previousRadius) + fabsf(radius))) {
             t -= insT;
             omega = 1.0f;
@@ -561,7 +577,7 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
             continue;
         }
         if (fabsf(radius) < 1e-4f) {
-            converged = true;
+            hit_sel = sel;
             break;
         }
         if (t > tMinMax.y) {
@@ -600,7 +616,7 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
         const float nz = scene_sdf_cold(S, f3(p.x + 0.0f, p.y + 0.0f, p.z + e), set1) -
                          scene_sdf_cold(S, f3(p.x - 0.0f, p.y - 0.0f, p.z - e), set1);
         h.normal = normalize3(f3(nx, ny, nz));
-        h.materialID = scene_sdf_material_hit(S, p, set1, converged);
+        h.materialID = scene_sdf_material_hit(S, p, set1, hit_sel);
         h.lightID = -1.0f;
         return true;
     }

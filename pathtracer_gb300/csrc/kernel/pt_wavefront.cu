@@ -351,7 +351,7 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
     float2 tmm = make_float2(0.0f, 0.0f);
     uint32_t set1 = 0;
     int points = 0, iter = 0;
-    bool converged = false;  // the march of this lane's ray ended on |SDF| < 1e-4
+    int hit_sel = -2;  // >= -1 once the lane's march converged (scene_sdf_material_hit)
     bool shadow_ray = false;
     const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
 
@@ -392,7 +392,7 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
                     dir = f3(d.x, d.y, d.z);
                     hitdist = v.h0[slot].x;
                     steps = 0;
-                    converged = false;
+                    hit_sel = -2;
                     // A ray from isect (flag bit clear: start with the sign
                     // probe) or one suspended by an earlier launch.
                     const uint32_t saved = M.m2[slot];
@@ -440,7 +440,8 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
                 q = (j & 1) ? f3(p.x - mx, p.y - my, p.z - mz) : f3(p.x + ex, p.y + ey, p.z + ez);
             }
             float val = 0.0f;
-            if (evalLane) val = scene_sdf(*Sp, q, set1);
+            int esel = -1;
+            if (evalLane) val = scene_sdf_sel(*Sp, q, set1, esel);
             if (!evalLane) continue;
             if (phase == MP_SIGN) {
                 k = sign_glsl(val);
@@ -456,7 +457,7 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
                     p = fma3s(dir, t, org);
                 } else if (fabsf(radius) < 1e-4f) {
                     exitLoop = true;
-                    converged = true;
+                    hit_sel = esel;
                 } else {
                     if (t > tmm.y) {
                         points += 1;
@@ -525,7 +526,7 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
 
         if (finished && hit) {
             const float3 nrm = normalize3(nv);
-            const float mat = scene_sdf_material_hit(*Sp, p, set1, converged);
+            const float mat = scene_sdf_material_hit(*Sp, p, set1, hit_sel);
             v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
             v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
         }
