@@ -129,10 +129,9 @@ int pt_destroy(pt_ctx* ctx);
  * "builtin:<blob|mandelbulb|menger|terrain>[:m0,m1,m2]".  The reference's
  * four snippets (recognised by a whitespace-insensitive fingerprint) map to
  * precompiled plug-ins; any other text is translated (pt_glsl_translate) and
- * compiled at run time into the megakernel on the first dispatch (seconds,
- * then cached), and scenes holding such text always render with the
- * megakernel.  Positions and bounding boxes come from pt_ubo.sdfs, as in the
- * reference. */
+ * compiled at run time, on the first dispatch of each engine (seconds, then
+ * cached), into the megakernel or the wavefront engine's march kernel.
+ * Positions and bounding boxes come from pt_ubo.sdfs, as in the reference. */
 int pt_set_sdfs(pt_ctx* ctx, const char* const* sources, int n);
 /* Same, from already-decoded descriptors. */
 int pt_set_sdf_plugins(pt_ctx* ctx, const pt_sdf_plugin* plugins, int n);

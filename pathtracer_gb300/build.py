@@ -48,6 +48,8 @@ JIT_HEADERS = [
     ("pt_path.cuh", "pathtracer_gb300/csrc/kernel/pt_path.cuh"),
     ("pt_megakernel.h", "pathtracer_gb300/csrc/kernel/pt_megakernel.h"),
     ("pt_megakernel_body.cuh", "pathtracer_gb300/csrc/kernel/pt_megakernel_body.cuh"),
+    ("pt_wavefront.h", "pathtracer_gb300/csrc/kernel/pt_wavefront.h"),
+    ("pt_march.cuh", "pathtracer_gb300/csrc/kernel/pt_march.cuh"),
     ("pt_glsl_shim.h", "pathtracer_gb300/csrc/kernel/pt_glsl_shim.h"),
 ]
 GEN = os.path.join(LIB, "gen")

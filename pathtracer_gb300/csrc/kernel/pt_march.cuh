@@ -1,0 +1,350 @@
+// pt_march.cuh — the wavefront engine's SDF march kernel (wf_march) and the
+// helpers every stage kernel shares.  Included by pt_wavefront.cu and, for
+// scenes whose SDF text is compiled at run time, by the NVRTC program of
+// pt_jit.cu (with PT_JIT_USER_SDF, in namespace ptjit), so both builds run
+// the same source.
+#pragma once
+
+#include "pt_path.cuh"
+#include "pt_wavefront.h"
+
+#if defined(PT_JIT_USER_SDF)
+namespace ptjit {
+#else
+namespace {
+#endif
+
+constexpr uint32_t kShadowFlag = 1u << 30;
+constexpr int kStageThreads = 256;
+// Launch bounds of the queue stages: resident blocks of kStageThreads per SM
+// asked of the compiler (registers capped at 65536 / (256 x blocks)), so that
+// the default grid of 4 blocks per SM is resident at once.  Measured on
+// GB300: march, shade and isect at 4 blocks (64 registers) are 2-3 % faster
+// end to end than with the compiler's own choice (70-74 registers, 3 blocks).
+// PT_WF_<STAGE>_BLOCKS overrides the count; 0 leaves only the block size.
+#ifndef PT_WF_ISECT_BLOCKS
+#define PT_WF_ISECT_BLOCKS 4
+#endif
+#ifndef PT_WF_SHADE_BLOCKS
+#define PT_WF_SHADE_BLOCKS 4
+#endif
+#ifndef PT_WF_MARCH_BLOCKS
+#define PT_WF_MARCH_BLOCKS 4
+#endif
+#ifndef PT_WF_GEN_BLOCKS
+#define PT_WF_GEN_BLOCKS 0
+#endif
+#if PT_WF_ISECT_BLOCKS > 0
+#define PT_ISECT_BOUNDS __launch_bounds__(kStageThreads, PT_WF_ISECT_BLOCKS)
+#else
+#define PT_ISECT_BOUNDS __launch_bounds__(kStageThreads)
+#endif
+#if PT_WF_SHADE_BLOCKS > 0
+#define PT_SHADE_BOUNDS __launch_bounds__(kStageThreads, PT_WF_SHADE_BLOCKS)
+#else
+#define PT_SHADE_BOUNDS __launch_bounds__(kStageThreads)
+#endif
+#if PT_WF_MARCH_BLOCKS > 0
+#define PT_MARCH_BOUNDS __launch_bounds__(kStageThreads, PT_WF_MARCH_BLOCKS)
+#else
+#define PT_MARCH_BOUNDS __launch_bounds__(kStageThreads)
+#endif
+#if PT_WF_GEN_BLOCKS > 0
+#define PT_GEN_BOUNDS __launch_bounds__(kStageThreads, PT_WF_GEN_BLOCKS)
+#else
+#define PT_GEN_BOUNDS __launch_bounds__(kStageThreads)
+#endif
+// wf_march: after a large queue is drained, a warp with fewer rays than
+// WfArgs::drain_lanes suspends those that have marched kDrainMinSteps steps
+// in this launch, for the next iteration.
+constexpr int kDrainMinSteps = 8;
+
+// SphereTracing's over-relaxation start (SC:781).
+constexpr float kOmegaMax = 1.70f;
+
+// Warp-aggregated append of `value` to queue[count++] for lanes with pred.
+// Must be called by all 32 lanes of the warp.
+PT_DI void q_push(uint32_t* __restrict__ queue, uint32_t* count, uint32_t value, bool pred) {
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) queue[base + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = value;
+}
+
+struct PoolView {
+    float4 *s0, *s1, *s2, *s3, *s4, *s5, *s6, *s7;  // see WfPool
+    uint4* s8;
+    float4 *s9, *h0, *h1;
+};
+
+PT_DI PoolView view(const WfArgs& A) {
+    const WfPool& p = A.pool;
+    return PoolView{p.s0, p.s1, p.s2, p.s3, p.s4, p.s5, p.s6, p.s7, p.s8, p.s9, p.h0, p.h1};
+}
+
+PT_DI uint32_t slot_job(const PoolView& v, uint32_t slot) { return __float_as_uint(v.s9[slot].z); }
+
+// SphereTracing (SC:779-860) with one SDF evaluation per loop iteration per lane.
+enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NORMAL5 = 8 };
+
+// Warp-staged queue appends: lanes with pred add `value` to a per-warp
+// buffer of 64 in shared memory (count warp-uniform); every 32 entries go to
+// the queue with one atomic and one coalesced store.  Called by all 32 lanes.
+PT_DI void stage_push(uint32_t* buf, uint32_t& count, bool pred, uint32_t value, uint32_t* queue, uint32_t* qcount,
+                      int lane) {
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return;
+    if (pred) buf[count + (uint32_t)__popc(m & ((1u << lane) - 1u))] = value;
+    count += (uint32_t)__popc(m);  // < 64: it was < 32 before
+    if (count < 32) return;
+    __syncwarp();
+    uint32_t b = 0;
+    if (lane == 0) b = atomicAdd(qcount, 32u);
+    b = __shfl_sync(0xffffffffu, b, 0);
+    queue[b + (uint32_t)lane] = buf[lane];
+    const uint32_t rest = count - 32;
+    const uint32_t moved = ((uint32_t)lane < rest) ? buf[32 + lane] : 0u;
+    __syncwarp();
+    if ((uint32_t)lane < rest) buf[lane] = moved;
+    __syncwarp();
+    count = rest;
+}
+
+// Appends what stage_push still holds.  Called by all 32 lanes.
+PT_DI void stage_flush(uint32_t* buf, uint32_t count, uint32_t* queue, uint32_t* qcount, int lane) {
+    __syncwarp();
+    if (!count) return;
+    uint32_t b = 0;
+    if (lane == 0) b = atomicAdd(qcount, count);
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if ((uint32_t)lane < count) queue[b + (uint32_t)lane] = buf[lane];
+}
+
+__global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
+    WfCounters& C = *A.counters;
+    const uint32_t cur = C.cur;
+    const uint32_t n = C.n_march[cur];
+    const uint32_t* __restrict__ qin = A.q_march[cur];
+    const PoolView v = view(A);
+    const WfPool& M = A.pool;
+    const int lane = threadIdx.x & 31;
+    const int budget = A.march_budget;
+    const int refill_min = A.refill_min;
+    const int inner = A.march_inner;
+    int steps = 0;
+    // Draining only pays while the queue holds more rays than the grid has lanes.
+    const bool many = n >= 2u * gridDim.x * blockDim.x;
+    // Queue entries per claim: up to 32 while the queue is long, 1 near its end.
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    const uint32_t chunk = max(1u, min(32u, n / (4u * nwarps)));
+    uint32_t cbase = 0, cleft = 0;  // warp-uniform: unused entries of the warp's claim
+    // Finished rays are staged per warp and kind and appended to the shade
+    // queues 32 at a time.
+    __shared__ uint32_t staged[kStageThreads / 32][2][64];
+    uint32_t nstaged[2] = {0u, 0u};  // warp-uniform: primary hits, shadow results
+    const int wib = (int)(threadIdx.x >> 5);
+
+    uint32_t slot = 0;
+    const KScene* Sp = nullptr;
+    int phase = MP_EMPTY;
+    bool exhausted = false;
+    float3 org = f3(0.0f, 0.0f, 0.0f), dir = f3(0.0f, 0.0f, 1.0f), p = org;
+    float t = 0.0f, insT = 0.0f, omega = 0.0f, prevR = 0.0f, hitdist = 0.0f, k = 0.0f, nplus = 0.0f;
+    float3 nv = f3(0.0f, 0.0f, 0.0f);
+    float2 tmm = make_float2(0.0f, 0.0f);
+    uint32_t set1 = 0;
+    int points = 0, iter = 0;
+    int hit_sel = -2;  // >= -1 once the lane's march converged (scene_sdf_material_hit)
+    bool shadow_ray = false;
+    const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
+
+    for (;;) {
+        // Refill lanes that have no ray (warp-aggregated fetch), once at
+        // least refill_min of them are idle or the warp has none left.
+        // Queue entries come from a chunk the warp claimed with one atomic
+        // (cbase, cleft: warp-uniform); a refill that needs more than the
+        // chunk holds claims the next chunk.
+        const bool need = (phase == MP_EMPTY) && !exhausted;
+        const unsigned mneed = __ballot_sync(0xffffffffu, need);
+        if (mneed && (__popc(mneed) >= refill_min || __ballot_sync(0xffffffffu, phase != MP_EMPTY) == 0)) {
+            const uint32_t want = (uint32_t)__popc(mneed);
+            const uint32_t from_old = min(want, cleft);  // entries left in the current chunk
+            const uint32_t old_base = cbase;
+            uint32_t nb = 0;
+            if (want > from_old) {
+                const uint32_t ncount = max(chunk, want - from_old);
+                if (lane == 0) nb = atomicAdd(&C.march_cursor, ncount);
+                nb = __shfl_sync(0xffffffffu, nb, 0);
+                cbase = nb + (want - from_old);
+                cleft = ncount - (want - from_old);
+            } else {
+                cbase += want;
+                cleft -= want;
+            }
+            if (need) {
+                const uint32_t rank = (uint32_t)__popc(mneed & ((1u << lane) - 1u));
+                const uint32_t idx = (rank < from_old) ? old_base + rank : nb + (rank - from_old);
+                if (idx < n) {
+                    slot = qin[idx];
+                    Sp = A.jobs[slot_job(v, slot)].scene;
+                    const float4 o = v.s0[slot];
+                    const uint32_t flags = v.s8[slot].y;
+                    shadow_ray = (flags & kShadowFlag) != 0;
+                    const float4 d = shadow_ray ? v.s2[slot] : v.s1[slot];
+                    org = f3(o.x, o.y, o.z);
+                    dir = f3(d.x, d.y, d.z);
+                    hitdist = v.h0[slot].x;
+                    steps = 0;
+                    hit_sel = -2;
+                    // A ray from isect (flag bit clear: start with the sign
+                    // probe) or one suspended by an earlier launch.
+                    const uint32_t saved = M.m2[slot];
+                    const float4 a0 = M.m0[slot], a1 = M.m1[slot];
+                    t = a0.x;
+                    insT = a0.y;
+                    omega = a0.z;
+                    prevR = a0.w;
+                    tmm = make_float2(a1.x, a1.y);
+                    k = a1.z;
+                    set1 = __float_as_uint(a1.w);
+                    iter = (int)(saved & 1023u);
+                    points = (int)((saved >> 10) & 0xffffu);
+                    p = fma3s(dir, t, org);
+                    phase = (saved & 0x80000000u) ? MP_STEP : MP_SIGN;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        const unsigned live = __ballot_sync(0xffffffffu, phase != MP_EMPTY);
+        if (live == 0) break;
+        // Once the queue is drained, a warp with few rays left would run on
+        // with most lanes idle: its marching rays save their state and
+        // continue in full warps next iteration instead.
+        const bool drain = many && __ballot_sync(0xffffffffu, exhausted) != 0 && __popc(live) < A.drain_lanes;
+
+        // A.march_inner SDF evaluations per lane before the warp refills,
+        // shades finished hits and appends to the queues again: the warp
+        // pays for those once per several evaluations, and a lane whose ray
+        // finishes or is suspended on the way idles until then.
+        bool finished = false, hit = false, suspend = false;
+#pragma unroll 1
+        for (int sub = 0; sub < inner; sub++) {
+            // One SDF evaluation.
+            const bool evalLane = (phase >= MP_SIGN && phase <= MP_NORMAL5) && !finished && !suspend;
+            if (sub > 0 && __ballot_sync(0xffffffffu, evalLane) == 0) break;
+            float3 q = p;
+            if (phase == MP_SIGN) q = org;
+            if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
+                // CalculateNumericalSDFNormals (SC:721-730): p +- h.xyy, h.yxy, h.yyx
+                const int j = phase - MP_NORMAL0;
+                const float ex = (j == 0) ? e : 0.0f, ey = (j == 2) ? e : 0.0f, ez = (j == 4) ? e : 0.0f;
+                const float mx = (j == 1) ? e : 0.0f, my = (j == 3) ? e : 0.0f, mz = (j == 5) ? e : 0.0f;
+                q = (j & 1) ? f3(p.x - mx, p.y - my, p.z - mz) : f3(p.x + ex, p.y + ey, p.z + ez);
+            }
+            float val = 0.0f;
+            int esel = -1;
+            if (evalLane) val = scene_sdf_sel(*Sp, q, set1, esel);
+            if (!evalLane) continue;
+            if (phase == MP_SIGN) {
+                k = sign_glsl(val);
+                phase = MP_STEP;
+            } else if (phase == MP_STEP) {
+                const float radius = val;
+                bool exitLoop = false;
+                if (insT > (fabsf(prevR) + fabsf(radius))) {
+                    t -= insT;
+                    omega = 1.0f;
+                    insT = prevR * omega * k;
+                    t += insT;
+                    p = fma3s(dir, t, org);
+                } else if (fabsf(radius) < 1e-4f) {
+                    exitLoop = true;
+                    hit_sel = esel;
+                } else {
+                    if (t > tmm.y) {
+                        points += 1;
+                    } else {
+                        points = 0;
+                    }
+                    bool researched = false;
+                    if (points >= 2) {
+                        t = tmm.y + 1e-3f;
+                        tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
+                        const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+                        if (search_sdf(*Sp, fma3s(dir, t, org), invdir, tmm, set1)) {
+                            tmm.x += t;
+                            tmm.y += t;
+                            t = fmaxf(tmm.x, t);
+                            p = fma3s(dir, t, org);
+                            researched = true;
+                        } else {
+                            finished = true;  // left every SDF box: no SDF hit
+                        }
+                    }
+                    if (!finished && !researched) {
+                        insT = radius * omega * k;
+                        t += insT;
+                        p = fma3s(dir, t, org);
+                        const float omegaSpeedFactor = fminf(radius / prevR, 0.99f);
+                        omega += omegaSpeed * (fminf(1.0f / (1.0f - omegaSpeedFactor), omegaMax) - omega);
+                        prevR = radius;
+                    }
+                }
+                if (!finished && !exitLoop) {
+                    iter++;
+                    if (iter >= 512) exitLoop = true;
+                }
+                if (exitLoop) {
+                    if (t < hitdist) {
+                        p = fma3s(dir, t, org);
+                        phase = MP_NORMAL0;
+                    } else {
+                        finished = true;
+                    }
+                } else if (!finished && (++steps >= budget || (drain && steps >= kDrainMinSteps))) {
+                    // out of budget for this launch: save the state, continue next iteration
+                    M.m0[slot] = make_float4(t, insT, omega, prevR);
+                    M.m1[slot] = make_float4(tmm.x, tmm.y, k, __uint_as_float(set1));
+                    M.m2[slot] = 0x80000000u | ((uint32_t)min(points, 0xffff) << 10) | (uint32_t)iter;
+                    suspend = true;
+                }
+            } else if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
+                const int j = phase - MP_NORMAL0;
+                if ((j & 1) == 0) {
+                    nplus = val;
+                } else {
+                    const float dv = nplus - val;
+                    if (j == 1) nv.x = dv;
+                    else if (j == 3) nv.y = dv;
+                    else nv.z = dv;
+                }
+                phase++;
+                if (phase > MP_NORMAL5) {
+                    hit = true;
+                    finished = true;
+                }
+            }
+        }
+
+        if (finished && hit) {
+            const float3 nrm = normalize3(nv);
+            const float mat = scene_sdf_material_hit(*Sp, p, set1, hit_sel);
+            v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
+            v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        }
+        stage_push(staged[wib][0], nstaged[0], finished && !shadow_ray, slot, A.q_shade, &C.n_shade, lane);
+        stage_push(staged[wib][1], nstaged[1], finished && shadow_ray, slot, A.q_shadow, &C.n_shadow, lane);
+        q_push(A.q_march[cur ^ 1u], &C.n_march[cur ^ 1u], slot, suspend);
+        if (finished || suspend) phase = MP_EMPTY;
+    }
+    // The staged remainders.
+    stage_flush(staged[wib][0], nstaged[0], A.q_shade, &C.n_shade, lane);
+    stage_flush(staged[wib][1], nstaged[1], A.q_shadow, &C.n_shadow, lane);
+}
+
+}  // namespace

@@ -2,8 +2,10 @@
 // host-side engine that drives it (pt_engine.cu).
 #pragma once
 
+#if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 #include "pt_scene.cuh"
 
@@ -80,6 +82,8 @@ struct WfArgs {
     int persist_refill;  // idle lanes a persistent warp gathers before starting new samples together
 };
 
+// Host side (not seen by the run-time compiled program, pt_jit.cu).
+#if !defined(__CUDACC_RTC__)
 // Bytes of the engine's device buffers for a pool of `pool` slots.
 inline size_t ptk_wavefront_pool_bytes(uint32_t pool) { return (size_t)pool * (14 * 16 + 8 * 4) + 32 * 256; }
 
@@ -90,8 +94,10 @@ cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint
                                          cudaStream_t stream);
 // One iteration: isect, march, shade, gen, bookkeeping (grid = blocks per
 // stage kernel); with stage_events, 6 events bracket the 5 kernels.
+// march_kernel: a run-time compiled wf_march (pt_jit.cu) to launch instead
+// of the built-in one (scenes with SDF snippets compiled at run time).
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
-                                           cudaEvent_t* stage_events = nullptr);
+                                           cudaEvent_t* stage_events = nullptr, const void* march_kernel = nullptr);
 // Stages timed by the engine's stage-timing mode.
 enum { PT_STAGE_ISECT = 0, PT_STAGE_MARCH, PT_STAGE_SHADE, PT_STAGE_GEN, PT_STAGE_BOOK, PT_STAGE_COUNT };
 // Persistent mode: one launch of the persistent path kernel over the next
@@ -105,3 +111,4 @@ constexpr int kPersistThreads = 128;
 // Rendering/Accumulate of one job pass from its ordered sample colours.
 cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,
                                          const float4* colors, cudaStream_t stream);
+#endif  // !__CUDACC_RTC__

@@ -55,7 +55,7 @@ struct pt_ctx {
     // GLSL snippets other than the shipped four (PT_SDF_CUSTOM slots), as
     // translated by pt_glsl_translate, and the module compiled for them.
     std::vector<JitSlot> custom;
-    JitModule jit;
+    JitModule jit[kJitKinds];
     std::string err;
 };
 
@@ -100,6 +100,7 @@ cudaError_t sync_device_scene(pt_ctx* ctx) {
 
 static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push);
 static int dispatch_jit(pt_ctx* ctx, bool trace);
+static int ensure_jit(pt_ctx* ctx, JitKind kind);
 cudaError_t ptk_export_rgb8(const void* d_accum, int width, int height, int tonemap, void* d_rgb, cudaStream_t stream);
 
 extern "C" {
@@ -145,7 +146,7 @@ int pt_destroy(pt_ctx* ctx) {
     }
     if (ctx->d_colors) cudaFree(ctx->d_colors);
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
-    pt_jit_unload(ctx->jit);
+    for (JitModule& m : ctx->jit) pt_jit_unload(m);
     if (ctx->done) cudaEventDestroy(ctx->done);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx->params;
@@ -290,7 +291,12 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push) {
     P.cie = ctx->d_cie;
     P.trace = ctx->trace;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
-    if (!ctx->custom.empty()) return dispatch_jit(ctx, trace);
+    if (!ctx->custom.empty()) {
+        const bool staged = ctx->engine == PT_ENGINE_WAVEFRONT && push->pathLength > 0;
+        const int rc = ensure_jit(ctx, staged ? kJitMarch : kJitMegakernel);
+        if (rc != PT_OK) return rc;
+        if (!staged) return dispatch_jit(ctx, trace);
+    }
     if (ctx->engine == PT_ENGINE_WAVEFRONT && push->pathLength > 0) return dispatch_wavefront(ctx, push);
     PT_CUDA_TRY(ctx, ptk_launch_megakernel(&P, trace, ctx->stream));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
@@ -541,6 +547,10 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
         if (!ctx->wf) return fail(ctx, PT_ERR_OOM, "pt_dispatch: out of host memory");
         PT_CUDA_TRY(ctx, ctx->wf->create(ctx->device, ctx->stream, pool, 4096, ctx->march_budget));
     }
+    // Run-time compiled SDF snippets: their march kernel (the other stages
+    // evaluate no SDF).
+    ctx->wf->set_march_kernel(ctx->custom.empty() ? nullptr
+                                                  : reinterpret_cast<const void*>(ctx->jit[kJitMarch].kernel[0]));
     const size_t cbytes = (size_t)total * sizeof(float4);
     if (cbytes > ctx->colors_bytes) {
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -583,24 +593,29 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     return PT_OK;
 }
 
-// Scenes with GLSL snippets beyond the shipped four: the megakernel compiled
-// at run time with their translation (pt_jit.cu), rebuilt when the set of
-// snippets changes.  The wavefront engine has no run-time compiled form, so
-// these scenes always take the plain megakernel.
+// Scenes with GLSL snippets beyond the shipped four: the megakernel (plain
+// engine) or the march kernel (wavefront engine; its other stages evaluate no
+// SDF) compiled at run time with their translation (pt_jit.cu) on first use,
+// and again when the set of snippets changes.
+static int ensure_jit(pt_ctx* ctx, JitKind kind) {
+    JitModule& m = ctx->jit[kind];
+    const std::string program = pt_jit_program(ctx->custom, kind);
+    if (m.key == program) return PT_OK;
+    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (kind == kJitMarch && ctx->wf) ctx->wf->set_march_kernel(nullptr);  // no graph may keep the old kernel
+    pt_jit_unload(m);
+    std::vector<char> cubin;
+    std::string lowered[kJitMaxKernels], log;
+    int rc = pt_jit_compile(ctx->device, program, kind, cubin, lowered, log);
+    if (rc != PT_OK) return fail(ctx, rc, "compiling the scene's SDF snippets: " + log);
+    rc = pt_jit_load(cubin, kind, lowered, m, log);
+    if (rc != PT_OK) return fail(ctx, rc, log);
+    m.key = program;
+    return PT_OK;
+}
+
 static int dispatch_jit(pt_ctx* ctx, bool trace) {
-    const std::string program = pt_jit_program(ctx->custom);
-    if (ctx->jit.key != program) {
-        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        pt_jit_unload(ctx->jit);
-        std::vector<char> cubin;
-        std::string lowered[2], log;
-        int rc = pt_jit_compile(ctx->device, program, cubin, lowered, log);
-        if (rc != PT_OK) return fail(ctx, rc, "compiling the scene's SDF snippets: " + log);
-        rc = pt_jit_load(cubin, lowered, ctx->jit, log);
-        if (rc != PT_OK) return fail(ctx, rc, log);
-        ctx->jit.key = program;
-    }
-    PT_CUDA_TRY(ctx, pt_jit_launch(ctx->jit, ctx->params, trace, ctx->stream));
+    PT_CUDA_TRY(ctx, pt_jit_launch(ctx->jit[kJitMegakernel], ctx->params, trace, ctx->stream));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
 }

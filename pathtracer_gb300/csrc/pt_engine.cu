@@ -155,6 +155,11 @@ void WfEngine::set_tuning(int refill, int drain, int bps, int inner) {
 
 void WfEngine::set_persistent(bool on) { persistent = on; }
 
+void WfEngine::set_march_kernel(const void* kernel) {
+    if (kernel != march_kernel) drop_graph();
+    march_kernel = kernel;
+}
+
 cudaError_t WfEngine::reset() {
     njobs = lo = 0;
     total = 0;
@@ -194,7 +199,8 @@ cudaError_t WfEngine::build_graph() {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        for (int i = 0; i < graph_chunk && e == cudaSuccess; i++) e = ptk_wavefront_launch_iteration(&a, false, grid, cs);
+        for (int i = 0; i < graph_chunk && e == cudaSuccess; i++)
+            e = ptk_wavefront_launch_iteration(&a, false, grid, cs, nullptr, march_kernel);
         const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
         if (e == cudaSuccess) e = e2;
     }
@@ -246,7 +252,8 @@ cudaError_t WfEngine::run(int n, bool trace) {
     if (stage_timing && !persistent) {
         for (int i = 0; i < n; i++) {
             if (stage_ev_used == kStageEvRounds) EN_TRY(flush_stage_events());
-            EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, &stage_ev[stage_ev_used * 6]));
+            EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, &stage_ev[stage_ev_used * 6],
+                                                  march_kernel));
             stage_ev_used++;
         }
         return flush_stage_events();
@@ -265,7 +272,7 @@ cudaError_t WfEngine::run(int n, bool trace) {
         if (!graph) EN_TRY(build_graph());
         for (; n >= graph_chunk; n -= graph_chunk) EN_TRY(cudaGraphLaunch(graph, stream));
     }
-    for (int i = 0; i < n; i++) EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream));
+    for (int i = 0; i < n; i++) EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, nullptr, march_kernel));
     return cudaSuccess;
 }
 

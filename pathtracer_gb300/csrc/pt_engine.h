@@ -54,6 +54,9 @@ struct WfEngine {
     bool stage_timing = false;
     double stage_ms[PT_STAGE_COUNT] = {0, 0, 0, 0, 0};
     uint64_t stage_launches = 0;
+    // A run-time compiled march kernel (scenes with SDF snippets compiled
+    // by pt_jit.cu), launched instead of the built-in one; null for none.
+    const void* march_kernel = nullptr;
 
     // Bytes of device memory for `pool` slots and `max_jobs` ring entries.
     static size_t bytes_for(uint32_t pool, uint32_t max_jobs);
@@ -72,6 +75,8 @@ struct WfEngine {
     void set_march_budget(int budget);
     // March refill threshold, drain threshold and stage-kernel blocks per SM.
     void set_tuning(int refill_min, int drain_lanes, int blocks_per_sm, int march_inner);
+    // Sets march_kernel (null: the built-in kernel).
+    void set_march_kernel(const void* kernel);
     // Staged kernels (false) or the persistent path kernel (true).
     void set_persistent(bool on);
     // Persistent mode: every sample added so far is covered by a launch.

@@ -1,5 +1,6 @@
-// pt_jit.cu — megakernels compiled at run time for scenes whose SDF text is
-// not one of the four shipped snippets: the reference's InsertSDF +
+// pt_jit.cu — the megakernel and the wavefront march kernel compiled at run
+// time for scenes whose SDF text is not one of the four shipped snippets: the
+// reference's InsertSDF +
 // GLSLToSPIRV + recompile (src/pathtracer.cpp:2004-2054, 1811-1868, 3836).
 // The snippets' translation (pt_glsl.cpp) and a slot dispatcher are compiled
 // with NVRTC together with the megakernel's own source, embedded in this
@@ -34,7 +35,18 @@ const char* kPrelude =
 
 }  // namespace
 
-std::string pt_jit_program(const std::vector<JitSlot>& slots) {
+namespace {
+
+const char* const kNames[kJitKinds][kJitMaxKernels] = {
+    {"ptjit::megakernel<false, 15>", "ptjit::megakernel<true, 15>"},
+    {"ptjit::wf_march", nullptr},
+};
+
+int kernel_count(JitKind kind) { return kind == kJitMegakernel ? 2 : 1; }
+
+}  // namespace
+
+std::string pt_jit_program(const std::vector<JitSlot>& slots, JitKind kind) {
     std::string s = kPrelude;
     s += "#include \"pt_glsl_shim.h\"\n";
     for (const JitSlot& j : slots) s += j.code + "\n";
@@ -47,31 +59,31 @@ std::string pt_jit_program(const std::vector<JitSlot>& slots) {
         s += "    case " + std::to_string(j.slot) + ": return ptg::" + j.prefix +
              "sdfmaterial(ptg::vec3(p.x, p.y, p.z));\n";
     s += "    default: return 0.0f;\n  }\n}\n";
-    s += "#include \"pt_megakernel_body.cuh\"\n";
+    s += kind == kJitMegakernel ? "#include \"pt_megakernel_body.cuh\"\n" : "#include \"pt_march.cuh\"\n";
     return s;
 }
 
-int pt_jit_compile(int device, const std::string& program, std::vector<char>& cubin, std::string lowered[2],
-                   std::string& log) {
+int pt_jit_compile(int device, const std::string& program, JitKind kind, std::vector<char>& cubin,
+                   std::string lowered[kJitMaxKernels], std::string& log) {
     int major = 0, minor = 0;
     if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device) != cudaSuccess ||
         cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device) != cudaSuccess) {
         log = "no CUDA device to compile for";
         return PT_ERR_CUDA;
     }
-    return pt_jit_compile_for(major * 10 + minor, program, cubin, lowered, log);
+    return pt_jit_compile_for(major * 10 + minor, program, kind, cubin, lowered, log);
 }
 
-int pt_jit_compile_for(int sm, const std::string& program, std::vector<char>& cubin, std::string lowered[2],
-                       std::string& log) {
+int pt_jit_compile_for(int sm, const std::string& program, JitKind kind, std::vector<char>& cubin,
+                       std::string lowered[kJitMaxKernels], std::string& log) {
     nvrtcProgram prog = nullptr;
-    if (nvrtcCreateProgram(&prog, program.c_str(), "pt_jit_megakernel.cu", kJitHeaderCount, kJitHeaderTexts,
+    if (nvrtcCreateProgram(&prog, program.c_str(), "pt_jit_kernels.cu", kJitHeaderCount, kJitHeaderTexts,
                            kJitHeaderNames) != NVRTC_SUCCESS) {
         log = "nvrtcCreateProgram failed";
         return PT_ERR_UNSUPPORTED;
     }
-    const char* names[2] = {"ptjit::megakernel<false, 15>", "ptjit::megakernel<true, 15>"};
-    for (const char* n : names) nvrtcAddNameExpression(prog, n);
+    const int nk = kernel_count(kind);
+    for (int i = 0; i < nk; i++) nvrtcAddNameExpression(prog, kNames[kind][i]);
     char arch[48];
     std::snprintf(arch, sizeof arch, "--gpu-architecture=sm_%d%s", sm, sm >= 90 ? "a" : "");
     const char* opts[] = {arch, "--std=c++17", "--fmad=false", "--prec-div=true", "--prec-sqrt=true",
@@ -85,9 +97,9 @@ int pt_jit_compile_for(int sm, const std::string& program, std::vector<char>& cu
         nvrtcDestroyProgram(&prog);
         return PT_ERR_UNSUPPORTED;
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < nk; i++) {
         const char* low = nullptr;
-        if (nvrtcGetLoweredName(prog, names[i], &low) != NVRTC_SUCCESS || !low) {
+        if (nvrtcGetLoweredName(prog, kNames[kind][i], &low) != NVRTC_SUCCESS || !low) {
             nvrtcDestroyProgram(&prog);
             log = "kernel name not found in the compiled module";
             return PT_ERR_UNSUPPORTED;
@@ -116,12 +128,14 @@ extern "C" int pt_jit_check(const char* const* sources, int n, int sm, char* log
         rc = pt_jit_translate_slot(sources[i], i, j, msg);
         if (rc == PT_OK) slots.push_back(j);
     }
-    std::vector<char> cubin;
-    std::string lowered[2];
-    if (rc == PT_OK) rc = pt_jit_compile_for(sm, pt_jit_program(slots), cubin, lowered, msg);
-    if (log && log_cap) {
-        std::snprintf(log, log_cap, "%s", msg.c_str());
+    std::string all;  // the compiler's messages for both programs
+    for (int k = 0; k < kJitKinds && rc == PT_OK; k++) {
+        std::vector<char> cubin;
+        std::string lowered[kJitMaxKernels];
+        rc = pt_jit_compile_for(sm, pt_jit_program(slots, (JitKind)k), (JitKind)k, cubin, lowered, msg);
+        all += msg;
     }
+    if (log && log_cap) std::snprintf(log, log_cap, "%s", (all.empty() ? msg : all).c_str());
     return rc;
 }
 
@@ -146,9 +160,11 @@ int pt_jit_translate_slot(const char* source, int slot, JitSlot& out, std::strin
     return PT_OK;
 }
 
-int pt_jit_load(const std::vector<char>& cubin, const std::string lowered[2], JitModule& m, std::string& err) {
+int pt_jit_load(const std::vector<char>& cubin, JitKind kind, const std::string lowered[kJitMaxKernels], JitModule& m,
+                std::string& err) {
     cudaError_t e = cudaLibraryLoadData(&m.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaLibraryGetKernel(&m.kernel[i], m.lib, lowered[i].c_str());
+    for (int i = 0; i < kernel_count(kind) && e == cudaSuccess; i++)
+        e = cudaLibraryGetKernel(&m.kernel[i], m.lib, lowered[i].c_str());
     if (e != cudaSuccess) {
         err = std::string("loading the compiled module: ") + cudaGetErrorString(e);
         if (m.lib) cudaLibraryUnload(m.lib);
@@ -161,7 +177,7 @@ int pt_jit_load(const std::vector<char>& cubin, const std::string lowered[2], Ji
 void pt_jit_unload(JitModule& m) {
     if (m.lib) cudaLibraryUnload(m.lib);
     m.lib = nullptr;
-    m.kernel[0] = m.kernel[1] = nullptr;
+    for (cudaKernel_t& k : m.kernel) k = nullptr;
     m.key.clear();
 }
 

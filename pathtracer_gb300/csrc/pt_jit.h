@@ -1,4 +1,4 @@
-// pt_jit.h — run-time compiled megakernels for GLSL SDF snippets (pt_jit.cu).
+// pt_jit.h — kernels compiled at run time for GLSL SDF snippets (pt_jit.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -16,18 +16,28 @@ struct JitSlot {
     std::string code;
 };
 
+// What a module holds: the megakernel (kernel[0] without, kernel[1] with
+// path traces) or the wavefront engine's march kernel (kernel[0]).  Each is
+// its own NVRTC program, compiled when first needed.
+enum JitKind { kJitMegakernel = 0, kJitMarch = 1, kJitKinds = 2 };
+constexpr int kJitMaxKernels = 2;
+
 struct JitModule {
     std::string key;  // the program text it was compiled from
     cudaLibrary_t lib = nullptr;
-    cudaKernel_t kernel[2] = {nullptr, nullptr};  // megakernel without / with traces
+    cudaKernel_t kernel[kJitMaxKernels] = {nullptr, nullptr};
 };
 
 int pt_jit_translate_slot(const char* source, int slot, JitSlot& out, std::string& err);
-std::string pt_jit_program(const std::vector<JitSlot>& slots);
-int pt_jit_compile(int device, const std::string& program, std::vector<char>& cubin, std::string lowered[2],
-                   std::string& log);
-int pt_jit_compile_for(int sm, const std::string& program, std::vector<char>& cubin, std::string lowered[2],
-                       std::string& log);
-int pt_jit_load(const std::vector<char>& cubin, const std::string lowered[2], JitModule& m, std::string& err);
+std::string pt_jit_program(const std::vector<JitSlot>& slots, JitKind kind);
+// Compiles for the compute capability of `device` (pt_jit_compile) or for
+// sm (e.g. 103) and returns the cubin and the kernels' lowered names.
+int pt_jit_compile(int device, const std::string& program, JitKind kind, std::vector<char>& cubin,
+                   std::string lowered[kJitMaxKernels], std::string& log);
+int pt_jit_compile_for(int sm, const std::string& program, JitKind kind, std::vector<char>& cubin,
+                       std::string lowered[kJitMaxKernels], std::string& log);
+int pt_jit_load(const std::vector<char>& cubin, JitKind kind, const std::string lowered[kJitMaxKernels], JitModule& m,
+                std::string& err);
 void pt_jit_unload(JitModule& m);
+// The megakernel of a kJitMegakernel module over the dispatch in params.
 cudaError_t pt_jit_launch(const JitModule& m, const KParams* params, bool trace, cudaStream_t stream);

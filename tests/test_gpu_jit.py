@@ -1,6 +1,7 @@
 """Scenes whose SDF text is not one of the reference's four snippets: the
-text is translated (pt_glsl_translate), compiled into the megakernel with
-NVRTC on the first dispatch and cached.  Parity is against the oracle with a
+text is translated (pt_glsl_translate), compiled with NVRTC into the
+megakernel or the wavefront engine's march kernel on the first dispatch of
+that engine, and cached.  Parity is against the oracle with a
 hand restatement of each snippet in C (oracle/user_sdfs.c) registered for its
 slot; criteria as in test_gpu_parity (oracle/compare.py)."""
 import json
@@ -43,9 +44,9 @@ BULB_SDF = {"position": [0.0, 1.15, -2.0], "boundingSize": [2.5, 2.5, 2.5], "bui
 
 @pytest.mark.parametrize("engine", [0, 1])
 def test_user_snippets_match_oracle(rt, engine):
-    """Two user snippets and a shipped one in one scene, traced per path.
-    The wavefront engine setting routes such scenes to the compiled
-    megakernel as well."""
+    """Two user snippets and a shipped one in one scene, traced per path,
+    through the compiled megakernel (engine 0) and the wavefront engine with
+    the compiled march kernel (engine 1)."""
     from oracle import compare
 
     W, H, spf, depth = 64, 48, 4, 6
@@ -67,8 +68,9 @@ def test_user_snippets_match_oracle(rt, engine):
 
 
 def test_untraced_progressive_matches_oracle(rt):
-    """The untraced kernel of the compiled module over three progressive
-    dispatches (running mean), with the snippets in other slots."""
+    """The wavefront engine (the default) with the compiled march kernel over
+    three progressive dispatches (running mean), the snippets in other
+    slots."""
     from oracle import compare
 
     W, H, spf, depth = 48, 40, 2, 8
@@ -88,6 +90,27 @@ def test_untraced_progressive_matches_oracle(rt):
     rel = np.abs(acc_o - acc_g) / np.maximum(np.maximum(np.abs(acc_o), np.abs(acc_g)), 1e-6)
     frac_bad = float(np.mean(rel[..., :3].max(axis=-1) > 1e-4))
     assert frac_bad < 0.02, frac_bad
+
+
+def test_engines_agree_bitwise_on_user_snippets(rt):
+    """A larger render with several wavefront iterations (rays suspended and
+    resumed by the compiled march kernel): both engines give the same bits."""
+    W, H, spf, depth = 192, 128, 8, 6
+    scene = _scene(rt, [TORUS_SDF, LATTICE_SDF, BULB_SDF])
+    out = []
+    for engine in (0, 1):
+        with rt["Context"](0) as ctx:
+            ctx.set_engine(engine)
+            ctx.set_march_budget(8)
+            ctx.bind(scene, rt["cie"])
+            ctx.resize_accum(W, H)
+            for it in range(2):
+                ctx.dispatch(scene.push_constants(W, H, spf * (it + 1), spf * (it + 1), spf, depth))
+            ctx.wait()
+            out.append(ctx.read_accum())
+            if engine == 1:
+                assert ctx.last_iterations() > 8
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
 
 
 def test_module_is_cached_across_scene_changes(rt):
