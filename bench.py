@@ -174,7 +174,17 @@ def fp32_peak_tflops(peaks):
     return sms * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
 
 
-def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind):
+# wf_march DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum),
+# averaged over the 440 launches of one dispatch of this exact workload with
+# the default knobs, from one ncu capture (the launch-list summary for
+# mandelbulb_plane 1024x1024 64 spp in profiles/).  Other workloads report null.
+MARCH_TRAFFIC_BYTES = {"mandelbulb_plane_1024x1024_64spp_depth6": 75.83e6}
+# The wavefront knobs that capture ran with (the library defaults).
+DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
+                  "march_inner": 6}
+
+
+def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, traffic_key=None):
     """One extra step with per-stage CUDA events: each stage kernel's device
     time and, from the committed work model, its achieved FP32 rate; the
     roofline object is the march kernel's (the dominant one)."""
@@ -197,13 +207,14 @@ def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind):
                       "fp32_tflops": (work / secs / 1e12) if secs and work else None}
     march = stages["march"]
     roof = {"bound": "fp32", "kernel": "wf_march", "achieved": march["fp32_tflops"], "peak": peak,
-            "unit": "TFLOP/s", "frac": (march["fp32_tflops"] or 0.0) / peak, "traffic": None,
+            "unit": "TFLOP/s", "frac": (march["fp32_tflops"] or 0.0) / peak,
+            "traffic": MARCH_TRAFFIC_BYTES.get(traffic_key),
             "work_per_sample": ops["march"], "launches": iters,
             "note": f"peak: nominal FP32 FMA rate (SMs x 128 x 2) at the measured max SM clock ({peak_kind} peaks "
                     "hold no FP32 figure); achieved: hand-counted FP32 operations of the march stage's events "
                     "(pathtracer_gb300/workmodel.py, counts per sample from tests/golden/work_*.json) over the "
-                    "summed device time of its launches in one step timed with per-stage CUDA events; DRAM "
-                    "traffic per launch is in profiles/"}
+                    "summed device time of its launches in one step timed with per-stage CUDA events; traffic: "
+                    "DRAM bytes per launch from one ncu capture of this workload (profiles/)"}
     return roof, stages, ops
 
 
@@ -818,8 +829,9 @@ def main():
 
     peaks, peak_kind = measured_peaks()
     if args.engine == "wavefront":
+        captured = (W, H, args.spp, spf, args.depth) == (1024, 1024, 64, 64, 6) and ctx.tuning() == DEFAULT_TUNING
         roofline, stages, ops = stage_roofline(ctx, lambda: one_step(args.warmup + args.steps + 5), samples_per_step,
-                                               WORKLOAD, peaks, peak_kind)
+                                               WORKLOAD, peaks, peak_kind, WORKLOAD if captured else None)
     else:
         from pathtracer_gb300 import workmodel
 

@@ -250,3 +250,82 @@ def test_untraced_variants_match_oracle(rt, kind, seed):
         acc_p = b.read_target(tid)
     np.testing.assert_array_equal(acc_m[..., :3], acc_o[..., :3])
     np.testing.assert_array_equal(acc_p[..., :3], acc_o[..., :3])
+
+
+def _capacity_scene(rt):
+    """The uniform buffer filled to its limits: 160 spheres (960 of the 1024
+    object floats) with 24 emitters, a plane, and 32 SDFs (every bit of the
+    32-bit SDF set mask; 26 blobs, 4 mengers, 2 mandelbulbs)."""
+    import json
+
+    rng = np.random.default_rng(5)
+    spheres = []
+    for i in range(160):
+        pos = [float(rng.uniform(-6, 6)), float(rng.uniform(0.2, 3)), float(rng.uniform(-9, 1))]
+        spheres.append({"position": pos, "radius": float(rng.uniform(0.08, 0.3)),
+                        "materialID": int(i % 4), "lightID": int(1 + i % 3) if i % 7 == 0 else 0})
+    sdfs = []
+    for i in range(32):
+        x, z = -7.0 + 2.0 * (i % 8), -2.0 - 2.2 * (i // 8)
+        kind = "mandelbulb" if i in (9, 22) else "menger" if i % 8 == 3 else "blob"
+        scale = 0.45 if kind != "blob" else 0.35
+        sdfs.append({"position": [x, 1.0, z], "boundingSize": [2.6 * scale * 2, 2.6 * scale * 2, 2.6 * scale * 2],
+                     "builtin": kind})
+    data = {
+        "camera": {"numShots": 1, "position": [[0.0, 3.0, 6.0]], "angle": [[180.0, -12.0]], "ISO": 1600,
+                   "size": 0.057, "apertureSize": 0.0025, "apertureDistance": 0.049, "lensRadius": 0.01,
+                   "lensFocalLength": 0.03, "lensThickness": 0.0, "lensDistance": 0.05},
+        "sphere": spheres,
+        "plane": [{"position": [0.0, 0.0, 0.0], "materialID": 1, "lightID": 0}],
+        "sdf": sdfs,
+        "material": [{"reflection": {"peakWavelength": 450.0 + 40.0 * i, "sigma": 20.0 + 10.0 * i, "isInvert": i == 2}}
+                     for i in range(7)],
+        "light": [{"emission": {"temperature": 3000.0 + 1500.0 * i, "luminosity": 6.0}} for i in range(3)],
+    }
+    return rt["Scene"].parse(json.dumps(data))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_capacity_scene_matches_oracle(rt, engine):
+    from oracle import compare
+
+    scene = _capacity_scene(rt)
+    c = scene.counts()
+    assert c["spheres"] == 160 and c["sdfs"] == 32
+    W, H, spf, depth = 48, 32, 2, 4
+    ctx = rt["Context"](0)
+    ctx.set_engine(engine)
+    ctx.bind(scene, rt["cie"])
+    ctx.resize_accum(W, H)
+    ubo = scene.pack_ubo(rt["cie"])
+    assert ubo[5] == 32.0  # numObjects[5]: SDFs
+    push = scene.push_constants(W, H, spf, spf, spf, depth)
+    acc_o, tr_o = compare.run_oracle(ubo, push, compare.plugins_for(scene), trace_depth=depth)
+    acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
+    rep = compare.compare(acc_o, tr_o, acc_g, tr_g, spf)
+    print(rep)
+    _check(rep)
+    ctx.close()
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_empty_scene_and_single_pixel(rt, engine):
+    """A scene with no objects at all (every ray misses), and a 1x1 dispatch."""
+    import json
+
+    from oracle import compare
+
+    with open(os.path.join(SCENES, "cornell_box.json")) as f:
+        data = json.load(f)
+    empty = {k: v for k, v in data.items() if k in ("camera", "material", "light")}
+    for scene, (W, H) in ((rt["Scene"].parse(json.dumps(empty)), (24, 16)),
+                          (rt["Scene"].load(os.path.join(SCENES, "feature_mix.json")), (1, 1))):
+        ctx = rt["Context"](0)
+        ctx.set_engine(engine)
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        push = scene.push_constants(W, H, 3, 3, 3, 5)
+        acc_o, tr_o = compare.run_oracle(scene.pack_ubo(rt["cie"]), push, compare.plugins_for(scene), trace_depth=5)
+        acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=5)
+        _check(compare.compare(acc_o, tr_o, acc_g, tr_g, 3))
+        ctx.close()
