@@ -530,6 +530,20 @@ def run_serve(args, rank, world):
         if not args.burst:
             t += rng.exponential(1.0 / args.rate)
 
+    kinds = [pool[r.scene_key][0] for r in reqs]
+
+    def by_kind(res, serial):
+        """Jobs and samples per scene kind; on the serial plain path also the
+        seconds spent on each kind (admission to completion)."""
+        out = {}
+        for name, kv in (("spheres", native.PT_GEN_SPHERES), ("sdf", native.PT_GEN_SDF)):
+            sel = [r for r, k in zip(res, kinds) if k == kv]
+            out[name] = {"jobs": len(sel), "samples": sum(r.samples for r in sel)}
+            if serial:
+                secs = sum(r.t_done - r.t_admit for r in sel)
+                out[name].update({"seconds": secs, "path_samples_per_s": out[name]["samples"] / secs if secs else None})
+        return out
+
     def arm(mode):
         srv.set_mode(mode)
         with ClockSampler(local) as clk:
@@ -538,6 +552,7 @@ def run_serve(args, rank, world):
         samples = sum(r.samples for r in res)
         makespan = max(r.t_done for r in res) - min(arrivals)
         return res, {"jobs": len(res), "samples": samples, "makespan_s": makespan,
+                     "by_kind": by_kind(res, mode == native.PT_SERVE_PLAIN),
                      "path_samples_per_s": samples / makespan,
                      "time_to_target_s": {"p50": pctl(lat, 50), "p99": pctl(lat, 99), "mean": statistics.mean(lat)},
                      "queue_wait_s": {"p50": pctl([r.t_admit - r.t_submit for r in res], 50),
