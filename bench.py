@@ -178,7 +178,7 @@ def fp32_peak_tflops(peaks):
 # averaged over the 440 launches of one dispatch of this exact workload with
 # the default knobs, from one ncu capture (the launch-list summary for
 # mandelbulb_plane 1024x1024 64 spp in profiles/).  Other workloads report null.
-MARCH_TRAFFIC_BYTES = {"mandelbulb_plane_1024x1024_64spp_depth6": 75.83e6}
+MARCH_TRAFFIC_BYTES = {"mandelbulb_plane_1024x1024_64spp_depth6": 75.87e6}
 # The wavefront knobs that capture ran with (the library defaults).
 DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
                   "march_inner": 6}
