@@ -338,24 +338,13 @@ PT_DI float sdfmaterial(float3 p, const float* m) {
 }  // namespace sdf_blob
 
 namespace sdf_mandelbulb {  // sdfs/mandelbulb.glsl (power 8, 4 iterations, bailout 16)
-// pow(r, 7.0) for r = length(z) (+0, positive, +inf or NaN): ptm_powf's
-// binary powering for the exponent 7, (r * r^2) * (r^2 * r^2), without its
-// checks for the cases that powering already gets right here (1, +0, +inf);
-// a NaN r gives a NaN of another payload, which the product 8 * pow(...)
-// that consumes it makes canonical again.  Bit-identical in this use.
-PT_DI float pow7_nonneg(float r) {
-    const float r2 = r * r;
-    const float r3 = r * r2;
-    const float r4 = r2 * r2;
-    return r3 * r4;
-}
 PT_DI float sdf(float3 p) {
     float3 z = p;
     float r = length3(z);
     float dr = 1.0f;
 #pragma unroll 1
     for (int i = 0; i < 4; i++) {
-        dr = 8.0f * pow7_nonneg(r) * dr + 1.0f;
+        dr = 8.0f * pow_pos_int<7>(r) * dr + 1.0f;  // r = length(z): +0, positive, +inf or NaN
         const float invr = 1.0f / r;
         const float invl = 1.0f / sqrtf(z.x * z.x + z.z * z.z);
         r *= r;

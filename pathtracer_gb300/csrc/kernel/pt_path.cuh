@@ -47,13 +47,14 @@ PT_DI float4 evaluate_brdf(float4 l, float peak, float sigma, float invertf) {
 }
 
 // BlackBodyRadiation / Emit, SC:1040-1055.
+// pow(l, -5) as ptm_powf computes it, 1 / l^5 by binary powering (l > 0).
 PT_DI float blackbody(float l, float T) {
-    return (1.1910429724e-16f * ptm_powf(l, -5.0f)) / (ptm_expf(0.014387768775f / (l * T)) - 1.0f);
+    return (1.1910429724e-16f * (1.0f / pow_pos_int<5>(l))) / (ptm_expf(0.014387768775f / (l * T)) - 1.0f);
 }
 PT_DI float4 emit(float4 l, float temperature_in, float luminosity) {
     const float T = fmaxf(temperature_in, 0.0f);
     const float4 lm = l * 1e-9f;
-    const float peak = 4.0956746759e-6f * ptm_powf(T, 5.0f);
+    const float peak = 4.0956746759e-6f * pow_pos_int<5>(T);  // T >= 0
     const float4 e = f4(blackbody(lm.x, T) / peak, blackbody(lm.y, T) / peak, blackbody(lm.z, T) / peak,
                         blackbody(lm.w, T) / peak);
     return e * fmaxf(luminosity, 0.0f);

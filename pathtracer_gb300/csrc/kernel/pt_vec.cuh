@@ -57,6 +57,27 @@ PT_DI float step_glsl(float edge, float x) { return (x < edge) ? 0.0f : 1.0f; }
 PT_DI float mix_glsl(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 PT_DI float mod_glsl(float x, float y) { return x - y * floorf(x / y); }
 
+// pow(x, N) for a positive integer constant N: ptm_powf's binary powering
+// (include/pt_mathf.h) unrolled, without its checks for 1, 0, inf, NaN and
+// negative x, which the products get right by themselves; only a NaN x gives
+// another NaN payload than ptm_powf, so callers use it where the result is
+// consumed by arithmetic that makes any NaN canonical (or x is never NaN).
+template <int N>
+PT_DI float pow_pos_int(float x) {
+    static_assert(N > 0, "positive exponent");
+    float r = 0.0f, b = x;
+    bool have = false;
+#pragma unroll
+    for (int n = N; n != 0; n >>= 1) {
+        if (n & 1) {
+            r = have ? r * b : b;
+            have = true;
+        }
+        if (n >> 1) b = b * b;
+    }
+    return r;
+}
+
 // mat3 as three columns.
 struct m3 {
     float3 c0, c1, c2;
