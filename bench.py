@@ -178,7 +178,7 @@ def fp32_peak_tflops(peaks):
 # averaged over the 440 launches of one dispatch of this exact workload with
 # the default knobs, from one ncu capture (the launch-list summary for
 # mandelbulb_plane 1024x1024 64 spp in profiles/).  Other workloads report null.
-MARCH_TRAFFIC_BYTES = {"mandelbulb_plane_1024x1024_64spp_depth6": 75.87e6}
+MARCH_TRAFFIC_BYTES = {"mandelbulb_plane_1024x1024_64spp_depth6": 75.10e6}
 # The wavefront knobs that capture ran with (the library defaults).
 DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
                   "march_inner": 6}
@@ -363,7 +363,8 @@ def run_batch(args, rank, world):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(bstream)
-        it0 = b.stats()["iterations"]
+        st0 = b.stats()
+        it0, k0 = st0["iterations"], st0["kernel_launches"]
         for sid, tid, push in zip(sids, tids, pushes):
             b.add_pass(sid, tid, push)
         lat = {}
@@ -373,17 +374,20 @@ def run_batch(args, rank, world):
                 lat[pid] = time.perf_counter() - t0
         e1.record(bstream)
         e1.synchronize()
-        return e0.elapsed_time(e1) / 1000.0, list(lat.values()), b.stats()["iterations"] - it0
+        st1 = b.stats()
+        return (e0.elapsed_time(e1) / 1000.0, list(lat.values()), st1["iterations"] - it0,
+                st1["kernel_launches"] - k0)
 
     for _ in range(args.warmup):
         batched_step()
-    bt, blat, biters = [], [], []
+    bt, blat, biters, blaunch = [], [], [], []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            secs, lat, iters = batched_step()
+            secs, lat, iters, launches = batched_step()
             bt.append(secs)
             blat += lat
             biters.append(iters)
+            blaunch.append(launches)
     b_secs = statistics.mean(bt)
     batched_images = [b.read_target(t) for t in tids[:8]]
 
@@ -477,7 +481,7 @@ def run_batch(args, rank, world):
                                     "job_latency_s": {"p50": pctl(plat, 50), "p99": pctl(plat, 99)}},
         "speedup_vs_plain": p_secs / b_secs,
         "results_identical_to_plain": identical,
-        "gpu_launches": int(args.steps * (5 * iters + 2 * len(jobs))),
+        "gpu_launches": int(sum(blaunch)),  # the library's count (pt_batch_info.kernel_launches)
         "roofline": batch_roofline(samples, b_secs, peaks, peak_kind),
         "clocks": clk.summary(),
     }
@@ -869,7 +873,9 @@ def main():
         "engine": args.engine,
         "engines": {args.engine: {"value": value / world, "ms_per_step": ms_step}, **other},
         "wavefront_iterations_per_dispatch": iters if args.engine == "wavefront" else None,
-        "gpu_launches": args.steps * ndisp * ((5 * iters + 2) if args.engine == "wavefront" else 1),
+        # per wavefront dispatch: init, job_add, 4 kernels per iteration (graph
+        # replays counted per kernel), resolve
+        "gpu_launches": args.steps * ndisp * ((4 * iters + 3) if args.engine == "wavefront" else 1),
         "wall_s_timed_region": t_wall,
         "roofline": roofline,
         "stages": stages,

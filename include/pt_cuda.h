@@ -281,8 +281,9 @@ int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavef
                           double* best_seconds);
 
 /* Stage timing of the wavefront engine: when on, iterations are launched one
- * kernel at a time with CUDA events around each of the five stage kernels
- * (isect, march, shade, gen, bookkeeping), and pt_get_stage_times returns the
+ * kernel at a time with CUDA events around each stage (isect, march, shade,
+ * gen, bookkeeping; rays are intersected inside shade and gen, so the isect
+ * entry reads 0), and pt_get_stage_times returns the
  * device milliseconds summed per stage since timing was switched on, and the
  * iterations timed.  Off by default (it disables graph replay). */
 int pt_set_stage_timing(pt_ctx* ctx, int on);
@@ -337,6 +338,7 @@ typedef struct pt_batch_info {
     uint32_t pass_slots;    /* passes of one engine that can be in flight at once */
     uint32_t passes_staged; /* passes routed to each engine so far */
     uint32_t passes_persistent;
+    uint64_t kernel_launches; /* kernels the batch has launched (graph replays counted per kernel) */
 } pt_batch_info;
 
 /* pool_slots >= 1024 paths in flight in the staged engine; max_passes passes

@@ -16,28 +16,21 @@ namespace {
 
 constexpr uint32_t kShadowFlag = 1u << 30;
 constexpr int kStageThreads = 256;
-// Launch bounds of the queue stages: resident blocks of kStageThreads per SM
-// asked of the compiler (registers capped at 65536 / (256 x blocks)), so that
-// the default grid of 4 blocks per SM is resident at once.  Measured on
-// GB300: march, shade and isect at 4 blocks (64 registers) are 2-3 % faster
-// end to end than with the compiler's own choice (70-74 registers, 3 blocks).
-// PT_WF_<STAGE>_BLOCKS overrides the count; 0 leaves only the block size.
-#ifndef PT_WF_ISECT_BLOCKS
-#define PT_WF_ISECT_BLOCKS 4
-#endif
+// Launch bounds of the stage kernels: resident blocks of kStageThreads per SM
+// asked of the compiler (registers capped at 65536 / (256 x blocks)); the
+// host caps each kernel's grid at what is resident.  Measured on GB300: the
+// march kernel at 4 blocks (64 registers) and shade and gen, which also
+// intersect the rays they produce, at 3 (85 registers, no spills) are 1-12 %
+// faster end to end than the neighbouring choices.  PT_WF_<STAGE>_BLOCKS
+// overrides a count; 0 leaves only the block size.
 #ifndef PT_WF_SHADE_BLOCKS
-#define PT_WF_SHADE_BLOCKS 4
+#define PT_WF_SHADE_BLOCKS 3
 #endif
 #ifndef PT_WF_MARCH_BLOCKS
 #define PT_WF_MARCH_BLOCKS 4
 #endif
 #ifndef PT_WF_GEN_BLOCKS
-#define PT_WF_GEN_BLOCKS 0
-#endif
-#if PT_WF_ISECT_BLOCKS > 0
-#define PT_ISECT_BOUNDS __launch_bounds__(kStageThreads, PT_WF_ISECT_BLOCKS)
-#else
-#define PT_ISECT_BOUNDS __launch_bounds__(kStageThreads)
+#define PT_WF_GEN_BLOCKS 3
 #endif
 #if PT_WF_SHADE_BLOCKS > 0
 #define PT_SHADE_BOUNDS __launch_bounds__(kStageThreads, PT_WF_SHADE_BLOCKS)
@@ -337,14 +330,15 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
             v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
             v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
         }
-        stage_push(staged[wib][0], nstaged[0], finished && !shadow_ray, slot, A.q_shade, &C.n_shade, lane);
-        stage_push(staged[wib][1], nstaged[1], finished && shadow_ray, slot, A.q_shadow, &C.n_shadow, lane);
+        stage_push(staged[wib][0], nstaged[0], finished && !shadow_ray, slot, A.q_shade[cur], &C.n_shade[cur], lane);
+        stage_push(staged[wib][1], nstaged[1], finished && shadow_ray, slot, A.q_shadow[cur], &C.n_shadow[cur],
+                   lane);
         q_push(A.q_march[cur ^ 1u], &C.n_march[cur ^ 1u], slot, suspend);
         if (finished || suspend) phase = MP_EMPTY;
     }
     // The staged remainders.
-    stage_flush(staged[wib][0], nstaged[0], A.q_shade, &C.n_shade, lane);
-    stage_flush(staged[wib][1], nstaged[1], A.q_shadow, &C.n_shadow, lane);
+    stage_flush(staged[wib][0], nstaged[0], A.q_shade[cur], &C.n_shade[cur], lane);
+    stage_flush(staged[wib][1], nstaged[1], A.q_shadow[cur], &C.n_shadow[cur], lane);
 }
 
 }  // namespace

@@ -5,19 +5,19 @@
 // slowest neighbour's SDF march and for pixels with more work (measured:
 // 5.3 of 32 lanes active per warp instruction).  Here every path sample of a
 // dispatch is an independent work item in a pool of P slots; each iteration
-// runs four stage kernels over compacted queues:
-//   isect  analytic primitives + SDF bounding boxes for every pending ray
-//          (primary or shadow) -> rays that need sphere tracing go to MARCH,
-//          the rest to SHADE;
-//   march  persistent: each lane holds one ray and does exactly one SDF
-//          evaluation per loop iteration (sign probe, march step, normal
-//          probes), refilling from the queue the moment its ray is done, so
-//          all lanes execute the same SDF code;
-//   shade  emitter / miss / BRDF sample / light sample / shadow result /
-//          Russian roulette (the shared pt_path.cuh functions) -> next ray to
-//          the next ISECT queue, finished samples write their XYZ and free
-//          their slot;
-//   gen    start new samples in free slots.
+// runs three stage kernels over compacted queues:
+//   march  persistent: each lane holds one ray and does one SDF evaluation
+//          per step (sign probe, march step, normal probes), several steps
+//          between refills from the queue, so all lanes execute the same SDF
+//          code -> finished rays to this iteration's SHADE queues;
+//   shade  shadow-ray results, then primary hits: emitter / miss / BRDF
+//          sample / light sample / Russian roulette (the shared pt_path.cuh
+//          functions); finished samples write their XYZ and free their slot;
+//          the ray a path continues with is intersected at once (analytic
+//          primitives, SDF boxes) and goes to the next iteration's MARCH or
+//          SHADE queue;
+//   gen    start new samples in free slots, intersect their camera rays the
+//          same way.
 // A one-thread bookkeeping kernel advances the counters.  Queues are filled
 // with warp-aggregated atomics (ballot + popc + one atomicAdd per warp).
 // After the last sample, `resolve` sums each pixel's samples in sample order
@@ -106,6 +106,45 @@ PT_DI uint64_t jobs_total(const WfArgs& A, uint32_t hi) {
     return L.first + (uint64_t)L.count;
 }
 
+// Intersection for a ray a stage has just produced (the reference's
+// Intersection up to SphereTracing, SC:862-923 and SC:779-790): analytic
+// primitives, then the SDF bounding boxes.  Writes the hit record and, for a
+// ray that needs sphere tracing, the march start state (the march kernel
+// picks it up like a ray it suspended).  Returns true for such a ray.
+PT_DI bool route_ray(const WfArgs& A, const PoolView& v, const KScene& S, uint32_t slot, float3 org, float3 dir) {
+    Hit h;
+    h.hitdist = PT_MAXDIST;
+    h.normal = f3(0.0f, 0.0f, 0.0f);
+    h.materialID = 0.0f;
+    h.lightID = -1.0f;
+    int objectID = -1;
+    intersect_analytic(S, org, dir, h, objectID);
+    bool march = false;
+    if (S.meta.n[5] > 0) {
+        const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+        float2 tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
+        uint32_t set1 = 0;
+        march = search_sdf(S, org, invdir, tmm, set1);
+        if (march) {
+            A.pool.m0[slot] = make_float4(fmaxf(tmm.x, 1e-3f), 0.0f, kOmegaMax, 0.0f);
+            A.pool.m1[slot] = make_float4(tmm.x, tmm.y, 0.0f, __uint_as_float(set1));
+            A.pool.m2[slot] = 0u;
+        }
+    }
+    v.h0[slot] = make_float4(h.hitdist, h.materialID, h.lightID, __int_as_float(objectID));
+    v.h1[slot] = make_float4(h.normal.x, h.normal.y, h.normal.z, 0.0f);
+    return march;
+}
+
+// Appends a routed ray to the next iteration's queues: march, or shading of
+// a primary hit or of a shadow-ray result.  Called by all 32 lanes.
+PT_DI void push_routed(const WfArgs& A, WfCounters& C, uint32_t nxt, uint32_t slot, bool valid, bool march,
+                       bool shadow_ray) {
+    q_push(A.q_march[nxt], &C.n_march[nxt], slot, valid && march);
+    q_push(A.q_shade[nxt], &C.n_shade[nxt], slot, valid && !march && !shadow_ray);
+    q_push(A.q_shadow[nxt], &C.n_shadow[nxt], slot, valid && !march && shadow_ray);
+}
+
 __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
     const uint32_t job_lo = C.job_lo, job_hi = C.job_hi;
@@ -120,6 +159,7 @@ __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
         const uint32_t i = base + threadIdx.x;
         const bool valid = i < n;
         uint32_t slot = 0;
+        bool march = false;
         if (valid) {
             slot = A.q_free[nfree - n + i];
             const uint64_t s = first + i;
@@ -145,8 +185,9 @@ __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
             ps.shObj = 0;
             ps.ev = 0;
             store_state(v, slot, ps, 0u, local, job);
+            march = route_ray(A, v, *J.scene, slot, ps.org, ps.dir);
         }
-        q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, valid);
+        push_routed(A, C, nxt, slot, valid, march, false);
     }
 }
 
@@ -158,55 +199,6 @@ __global__ void wf_job_add(const __grid_constant__ WfArgs A, const WfJob job, ui
     WfCounters& C = *A.counters;
     C.job_hi = index + 1;
     C.job_lo = lo;
-}
-
-__global__ void PT_ISECT_BOUNDS wf_isect(const __grid_constant__ WfArgs A) {
-    WfCounters& C = *A.counters;
-    const uint32_t cur = C.cur;
-    const uint32_t n = C.n_isect[cur];
-    const uint32_t* __restrict__ q = A.q_isect[cur];
-    const PoolView v = view(A);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        const bool valid = i < n;
-        bool march = false, shadow_ray = false;
-        uint32_t slot = 0;
-        if (valid) {
-            slot = q[i];
-            const KScene& S = *A.jobs[slot_job(v, slot)].scene;
-            const float4 o = v.s0[slot];
-            const uint32_t flags = v.s8[slot].y;
-            shadow_ray = (flags & kShadowFlag) != 0;
-            const float4 d = (flags & kShadowFlag) ? v.s2[slot] : v.s1[slot];
-            const float3 org = f3(o.x, o.y, o.z), dir = f3(d.x, d.y, d.z);
-            Hit h;
-            h.hitdist = PT_MAXDIST;
-            h.normal = f3(0.0f, 0.0f, 0.0f);
-            h.materialID = 0.0f;
-            h.lightID = -1.0f;
-            int objectID = -1;
-            intersect_analytic(S, org, dir, h, objectID);
-            if (S.meta.n[5] > 0) {
-                const float3 invdir = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-                float2 tmm = make_float2(PT_MAXDIST, PT_MAXDIST);
-                uint32_t set1 = 0;
-                march = search_sdf(S, org, invdir, tmm, set1);
-                if (march) {
-                    // SphereTracing's start (SC:779-790): the march kernel
-                    // picks the ray up like one it suspended.
-                    A.pool.m0[slot] = make_float4(fmaxf(tmm.x, 1e-3f), 0.0f, kOmegaMax, 0.0f);
-                    A.pool.m1[slot] = make_float4(tmm.x, tmm.y, 0.0f, __uint_as_float(set1));
-                    A.pool.m2[slot] = 0u;
-                }
-            }
-            v.h0[slot] = make_float4(h.hitdist, h.materialID, h.lightID, __int_as_float(objectID));
-            v.h1[slot] = make_float4(h.normal.x, h.normal.y, h.normal.z, 0.0f);
-        }
-        q_push(A.q_march[cur], &C.n_march[cur], slot, valid && march);
-        q_push(A.q_shade, &C.n_shade, slot, valid && !march && !shadow_ray);
-        q_push(A.q_shadow, &C.n_shadow, slot, valid && !march && shadow_ray);
-    }
 }
 
 // Adds 1 to jobs[job].finished for every lane with pred, one atomic per
@@ -292,17 +284,17 @@ PT_DI void finish_shade(const WfArgs& A, const WfJob& J, const PathState& ps, St
 template <bool TRACE>
 __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
-    const uint32_t nxt = C.cur ^ 1u;
+    const uint32_t cur = C.cur, nxt = cur ^ 1u;
     const PoolView v = view(A);
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t ns = C.n_shadow;
+    const uint32_t ns = C.n_shadow[cur];
     for (uint32_t base = blockIdx.x * blockDim.x; base < ns; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool valid = i < ns;
         uint32_t slot = 0, job = 0;
-        bool again = false, freed = false;
+        bool again = false, freed = false, march = false;
         if (valid) {
-            slot = A.q_shadow[i];
+            slot = A.q_shadow[cur][i];
             PathState ps;
             uint32_t flags, sample;
             load_state(v, slot, ps, flags, sample, job);
@@ -313,20 +305,22 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
             if (!freed) {
                 store_after_shadow(v, slot, ps, sample, job, TRACE);
                 again = true;
+                // the bounce's next primary ray, set up with the primary hit
+                march = route_ray(A, v, *J.scene, slot, ps.org, ps.dir);
             }
         }
-        q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, again);
+        push_routed(A, C, nxt, slot, again, march, false);
         q_push(A.q_free, &C.n_free, slot, freed);
         count_finished(A.jobs, job, freed);
     }
-    const uint32_t np = C.n_shade;
+    const uint32_t np = C.n_shade[cur];
     for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool valid = i < np;
         uint32_t slot = 0, job = 0;
-        bool again = false, freed = false;
+        bool again = false, freed = false, march = false, shadow_next = false;
         if (valid) {
-            slot = A.q_shade[i];
+            slot = A.q_shade[cur][i];
             PathState ps;
             uint32_t flags, sample;
             load_for_primary(v, slot, ps, flags, sample, job);
@@ -354,9 +348,12 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
                                         sample, (uint32_t)ps.shObj);
                 v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
                 again = true;
+                // the light sample's shadow ray, or the next bounce
+                shadow_next = (r == STEP_SHADOW);
+                march = route_ray(A, v, *J.scene, slot, ps.org, shadow_next ? ps.shDir : ps.dir);
             }
         }
-        q_push(A.q_isect[nxt], &C.n_isect[nxt], slot, again);
+        push_routed(A, C, nxt, slot, again, march, shadow_next);
         q_push(A.q_free, &C.n_free, slot, freed);
         count_finished(A.jobs, job, freed);
     }
@@ -482,12 +479,11 @@ __global__ void wf_book(const __grid_constant__ WfArgs A) {
     C.total = total;
     C.next_sample += n;
     C.n_free -= n;
-    C.n_isect[C.cur] = 0;
     C.n_march[C.cur] = 0;
+    C.n_shade[C.cur] = 0;
+    C.n_shadow[C.cur] = 0;
     C.cur ^= 1u;
     C.march_cursor = 0;
-    C.n_shade = 0;
-    C.n_shadow = 0;
     C.iterations += 1;
     C.live = pool - C.n_free;
 }
@@ -497,10 +493,11 @@ __global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_fr
     if (i < pool) q_free[i] = i;
     if (i == 0) {
         WfCounters& C = *Cp;
-        C.n_isect[0] = C.n_isect[1] = 0;
         C.n_march[0] = C.n_march[1] = 0;
+        C.n_shade[0] = C.n_shade[1] = 0;
+        C.n_shadow[0] = C.n_shadow[1] = 0;
         C.cur = 0;
-        C.march_cursor = C.n_shade = C.n_shadow = 0;
+        C.march_cursor = 0;
         C.n_free = pool;
         C.next_sample = 0;
         C.total = 0;
@@ -538,12 +535,28 @@ cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint
     return cudaGetLastError();
 }
 
+// Blocks of a stage kernel resident on the device at once (SMs x the
+// kernel's occupancy), cached per kernel: a grid beyond it would leave its
+// last blocks for a second wave.
+static int resident_blocks(const void* kernel, int* cache) {
+    if (*cache) return *cache;
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kStageThreads, 0) != cudaSuccess ||
+        per_sm <= 0)
+        return 1 << 30;  // unknown: no cap
+    *cache = sms * per_sm;
+    return *cache;
+}
+
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
                                            cudaEvent_t* stage_events, const void* march_kernel) {
     // stage_events (optional): 6 events recorded before isect, march, shade,
     // gen, bookkeeping and after it, for per-stage device times.
+    // (Intersection is done by shade and gen for the rays they produce: the
+    // isect interval stays empty.)
     if (stage_events) cudaEventRecord(stage_events[0], stream);
-    wf_isect<<<grid, kStageThreads, 0, stream>>>(*a);
     if (stage_events) cudaEventRecord(stage_events[1], stream);
     if (march_kernel) {
         void* argv[] = {const_cast<WfArgs*>(a)};
@@ -553,13 +566,17 @@ cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid
         wf_march<<<grid, kStageThreads, 0, stream>>>(*a);
     }
     if (stage_events) cudaEventRecord(stage_events[2], stream);
+    static int shade_cap[2] = {0, 0}, gen_cap = 0;
     if (trace) {
-        wf_shade<true><<<grid, kStageThreads, 0, stream>>>(*a);
+        const int g = min(grid, resident_blocks(reinterpret_cast<const void*>(wf_shade<true>), &shade_cap[1]));
+        wf_shade<true><<<g, kStageThreads, 0, stream>>>(*a);
     } else {
-        wf_shade<false><<<grid, kStageThreads, 0, stream>>>(*a);
+        const int g = min(grid, resident_blocks(reinterpret_cast<const void*>(wf_shade<false>), &shade_cap[0]));
+        wf_shade<false><<<g, kStageThreads, 0, stream>>>(*a);
     }
     if (stage_events) cudaEventRecord(stage_events[3], stream);
-    wf_gen<<<grid, kStageThreads, 0, stream>>>(*a);
+    wf_gen<<<min(grid, resident_blocks(reinterpret_cast<const void*>(wf_gen), &gen_cap)), kStageThreads, 0,
+             stream>>>(*a);
     if (stage_events) cudaEventRecord(stage_events[4], stream);
     wf_book<<<1, 1, 0, stream>>>(*a);
     if (stage_events) cudaEventRecord(stage_events[5], stream);

@@ -44,11 +44,10 @@ struct WfJob {
 };
 
 struct WfCounters {
-    uint32_t n_isect[2];  // the two ISECT queues (current, next)
-    uint32_t n_march[2];  // the two MARCH queues (current, next)
+    uint32_t n_march[2];   // MARCH queues (current, next)
     uint32_t cur;
     uint32_t march_cursor;
-    uint32_t n_shade;      // primary-ray hits to shade
+    uint32_t n_shade[2];   // primary-ray hits to shade (current, next)
     uint32_t n_free;
     uint64_t next_sample;  // global samples started so far
     uint64_t total;        // global samples of every pass in the table (written by the bookkeeping kernel)
@@ -57,8 +56,7 @@ struct WfCounters {
     uint32_t job_lo;       // oldest pass that may still hold unfinished samples
     uint32_t job_hi;       // passes added so far
     uint64_t pk_end;       // persistent mode: end of the sample range of the current launch
-    uint32_t n_shadow;     // shadow-ray results to shade
-    uint32_t pad;
+    uint32_t n_shadow[2];  // shadow-ray results to shade (current, next)
 };
 
 // Everything here is fixed between resets, so a captured chain of iterations
@@ -67,10 +65,9 @@ struct WfArgs {
     WfJob* jobs;   // device job table (ring)
     uint32_t job_cap;
     WfPool pool;
-    uint32_t* q_isect[2];
     uint32_t* q_march[2];
-    uint32_t* q_shade;   // primary-ray hits
-    uint32_t* q_shadow;  // shadow-ray results
+    uint32_t* q_shade[2];   // primary-ray hits (current, next)
+    uint32_t* q_shadow[2];  // shadow-ray results (current, next)
     uint32_t* q_free;
     WfCounters* counters;
     KTrace trace;  // single-job dispatches only
@@ -92,12 +89,15 @@ cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream);
 // job_hi = index + 1, job_lo = lo.
 cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint32_t index, uint32_t lo,
                                          cudaStream_t stream);
-// One iteration: isect, march, shade, gen, bookkeeping (grid = blocks per
-// stage kernel); with stage_events, 6 events bracket the 5 kernels.
+// One iteration: march, shade, gen, bookkeeping (grid = blocks per stage
+// kernel, capped per kernel at what is resident); with stage_events, 6
+// events bracket the 5 stages (isect, done inside shade and gen, stays empty).
 // march_kernel: a run-time compiled wf_march (pt_jit.cu) to launch instead
 // of the built-in one (scenes with SDF snippets compiled at run time).
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
                                            cudaEvent_t* stage_events = nullptr, const void* march_kernel = nullptr);
+// Kernels launched per staged iteration (march, shade, gen, bookkeeping).
+constexpr int kWfKernelsPerIteration = 4;
 // Stages timed by the engine's stage-timing mode.
 enum { PT_STAGE_ISECT = 0, PT_STAGE_MARCH, PT_STAGE_SHADE, PT_STAGE_GEN, PT_STAGE_BOOK, PT_STAGE_COUNT };
 // Persistent mode: one launch of the persistent path kernel over the next

@@ -99,6 +99,7 @@ struct pt_batch {
     uint64_t samples_added = 0;
     uint64_t samples_done = 0;
     uint64_t iterations = 0;
+    uint64_t kernel_launches = 0;  // the batch's own kernels (the engines count theirs)
     uint32_t* h_finished = nullptr;  // pinned, max_passes entries
     // RMSE reductions: per item, sum of squared differences and sum of squares.
     int rmse_cap = 0;
@@ -293,6 +294,7 @@ int run_rmse(pt_batch* b, int n, double* out) {
     PT_B_TRY(b, cudaMemcpyAsync(b->d_items, b->h_items, sizeof(RmseItem) * (size_t)n, cudaMemcpyHostToDevice,
                                 b->stream));
     rmse_partial<<<dim3(kRmseBlocks, (unsigned)n), kRmseThreads, 0, b->stream>>>(b->d_items, b->d_partial);
+    b->kernel_launches += 2;
     PT_B_TRY(b, cudaGetLastError());
     rmse_final<<<(unsigned)n, 32, 0, b->stream>>>(b->d_partial, b->d_rmse);
     PT_B_TRY(b, cudaGetLastError());
@@ -450,7 +452,10 @@ int pt_batch_add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plug
         e = cudaMemcpyAsync(bs.d_cie, ubo->CIEXYZ1931, sizeof(float) * PT_CIE_TABLE_SIZE, cudaMemcpyHostToDevice,
                             b->stream);
     // Rotation matrices straight into the device copy (same kernel as pt_upload_scene).
-    if (e == cudaSuccess && S->meta.total_objects > 0) e = ptk_rotation_setup(S, &bs.d_scene->rot[0][0], b->stream);
+    if (e == cudaSuccess && S->meta.total_objects > 0) {
+        e = ptk_rotation_setup(S, &bs.d_scene->rot[0][0], b->stream);
+        b->kernel_launches += 1;
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);  // the copies read S and ubo
     delete S;
     if (e != cudaSuccess) {
@@ -600,6 +605,7 @@ int pt_batch_step(pt_batch* b, int iterations, int* completed, int capacity, int
             const WfJob& J = E.job(p.eidx);
             const uint32_t npix = (uint32_t)t.width * (uint32_t)t.height;
             const double exposure = (double)J.pc.apertureSize * (double)J.pc.apertureSize * (double)J.pc.ISO;
+            b->kernel_launches += 1;
             resolve_fp64_kernel<<<(npix + 255) / 256, 256, 0, b->stream>>>(p.d_colors, npix, J.pc.samplesPerFrame,
                                                                           exposure, t.d_sum);
             PT_B_TRY(b, cudaGetLastError());
@@ -669,6 +675,9 @@ int pt_batch_stats(pt_batch* b, pt_batch_info* out) {
     out->pass_slots = b->max_passes;
     out->passes_staged = b->engine_live[kStaged] ? b->engine[kStaged].njobs : 0;
     out->passes_persistent = b->engine_live[kPersistent] ? b->engine[kPersistent].njobs : 0;
+    out->kernel_launches = b->kernel_launches;
+    for (int e = 0; e < 2; e++)
+        if (b->engine_live[e]) out->kernel_launches += b->engine[e].kernel_launches;
     return PT_OK;
 }
 
@@ -692,6 +701,7 @@ int pt_batch_read_target(pt_batch* b, int target_id, float* host, size_t bytes) 
     } else {
         float4* tmp = nullptr;
         PT_B_TRY(b, cudaMallocFromPoolAsync(&tmp, need, b->mempool, b->stream));
+        b->kernel_launches += 1;
         fp64_to_float_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, b->stream>>>(t.d_sum, (uint32_t)npix, tmp);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(host, tmp, need, cudaMemcpyDeviceToHost, b->stream);

@@ -37,12 +37,12 @@ size_t layout(uintptr_t base, uint32_t pool, uint32_t max_jobs, WfArgs* a) {
     P.m0 = take<float4>(p, pool);
     P.m1 = take<float4>(p, pool);
     P.m2 = take<uint32_t>(p, pool);
-    a->q_isect[0] = take<uint32_t>(p, pool);
-    a->q_isect[1] = take<uint32_t>(p, pool);
     a->q_march[0] = take<uint32_t>(p, pool);
     a->q_march[1] = take<uint32_t>(p, pool);
-    a->q_shade = take<uint32_t>(p, pool);
-    a->q_shadow = take<uint32_t>(p, pool);
+    a->q_shade[0] = take<uint32_t>(p, pool);
+    a->q_shade[1] = take<uint32_t>(p, pool);
+    a->q_shadow[0] = take<uint32_t>(p, pool);
+    a->q_shadow[1] = take<uint32_t>(p, pool);
     a->q_free = take<uint32_t>(p, pool);
     a->counters = take<WfCounters>(p, 1);
     a->jobs = take<WfJob>(p, max_jobs);
@@ -164,6 +164,7 @@ cudaError_t WfEngine::reset() {
     njobs = lo = 0;
     total = 0;
     persist_issued = 0;
+    kernel_launches += 1;
     return ptk_wavefront_launch_init(&args, stream);
 }
 
@@ -179,6 +180,7 @@ cudaError_t WfEngine::add_pass(const WfJob& job, uint32_t* index) {
     // Stream-ordered: kernels launched from now on see job_hi = idx + 1 and
     // derive the sample total from this entry.
     EN_TRY(ptk_wavefront_launch_job_add(&args, &j, idx, lo, stream));
+    kernel_launches += 1;
     jobs[idx % max_jobs] = j;
     njobs = idx + 1;
     total += j.count;
@@ -254,6 +256,7 @@ cudaError_t WfEngine::run(int n, bool trace) {
             if (stage_ev_used == kStageEvRounds) EN_TRY(flush_stage_events());
             EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, &stage_ev[stage_ev_used * 6],
                                                   march_kernel));
+            kernel_launches += kWfKernelsPerIteration;
             stage_ev_used++;
         }
         return flush_stage_events();
@@ -264,15 +267,22 @@ cudaError_t WfEngine::run(int n, bool trace) {
         for (uint32_t j = lo; j < njobs; j++) variant = pt_variant_union(variant, jobs[j % max_jobs].variant);
         for (int i = 0; i < n && persist_issued < total; i++) {
             EN_TRY(ptk_persist_launch(&args, variant, sms, persist_budget, stream));
+            kernel_launches += 2;  // setup + persistent kernel
             persist_issued = (total - persist_issued > persist_budget) ? persist_issued + persist_budget : total;
         }
         return cudaSuccess;
     }
     if (use_graph && !trace && n >= graph_chunk) {
         if (!graph) EN_TRY(build_graph());
-        for (; n >= graph_chunk; n -= graph_chunk) EN_TRY(cudaGraphLaunch(graph, stream));
+        for (; n >= graph_chunk; n -= graph_chunk) {
+            EN_TRY(cudaGraphLaunch(graph, stream));
+            kernel_launches += (uint64_t)graph_chunk * kWfKernelsPerIteration;
+        }
     }
-    for (int i = 0; i < n; i++) EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, nullptr, march_kernel));
+    for (int i = 0; i < n; i++) {
+        EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, nullptr, march_kernel));
+        kernel_launches += kWfKernelsPerIteration;
+    }
     return cudaSuccess;
 }
 
@@ -301,6 +311,7 @@ cudaError_t WfEngine::read_finished(uint32_t j0, uint32_t j1, uint32_t* out) {
 cudaError_t WfEngine::resolve(uint32_t j, cudaStream_t on) {
     if (j >= njobs || j < lo) return cudaErrorInvalidValue;
     const WfJob& J = job(j);
+    kernel_launches += 1;
     return ptk_wavefront_launch_resolve(&args, j % max_jobs, &J.pc, J.accum, J.colors, on ? on : stream);
 }
 

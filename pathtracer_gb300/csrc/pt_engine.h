@@ -57,6 +57,8 @@ struct WfEngine {
     // A run-time compiled march kernel (scenes with SDF snippets compiled
     // by pt_jit.cu), launched instead of the built-in one; null for none.
     const void* march_kernel = nullptr;
+    // Kernels this engine has launched (graph replays counted per kernel).
+    uint64_t kernel_launches = 0;
 
     // Bytes of device memory for `pool` slots and `max_jobs` ring entries.
     static size_t bytes_for(uint32_t pool, uint32_t max_jobs);

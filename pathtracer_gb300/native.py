@@ -156,6 +156,7 @@ class PtBatchInfo(ctypes.Structure):
         ("pass_slots", ctypes.c_uint32),
         ("passes_staged", ctypes.c_uint32),
         ("passes_persistent", ctypes.c_uint32),
+        ("kernel_launches", ctypes.c_uint64),
     ]
 
 
