@@ -230,8 +230,10 @@ const char* pt_last_error(pt_ctx* ctx);
 int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_colors, int depth_cap);
 
 /* Evaluates one include/pt_mathf.h function on the device over device
- * arrays (fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos), so tests can
- * compare its bits with the same function on the CPU.  Synchronous. */
+ * arrays (fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos, 6 asin,
+ * 7 atan, 8 atan2(x, y) (GLSL atan(y, x) with y the first array), 9 exp2,
+ * 10 log2), so tests can compare its bits with the same function on the
+ * CPU.  Synchronous. */
 int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float* d_out, int n);
 
 /* ---- dispatch without allocating (not in the reference) -----------------

@@ -105,6 +105,15 @@ PTM_FN float ptm_from_bits(uint32_t u) {
 #define PTM_A4 2.460470796e-02f
 #define PTM_A5 7.509485353e-03f
 #define PTM_A6 3.464631364e-02f
+#define PTM_T0 -3.333329856e-01f
+#define PTM_T1 1.999854892e-01f
+#define PTM_T2 -1.426424235e-01f
+#define PTM_T3 1.095218584e-01f
+#define PTM_T4 -8.403450996e-02f
+#define PTM_T5 5.795760080e-02f
+#define PTM_T6 -3.117785044e-02f
+#define PTM_T7 1.091460884e-02f
+#define PTM_T8 -1.793622272e-03f
 
 typedef struct ptm_sc {
     float s, c;
@@ -303,5 +312,89 @@ PTM_CALL float ptm_acosf(float x) {
     if (x > 0.0f) return as2;
     return PTM_PI_1 - (as2 - PTM_PI_2);
 }
+
+/* asin(x): the polynomial on |x| <= 1/2, else pi/2 - 2 asin(sqrt((1-|x|)/2)). */
+PTM_CALL float ptm_asinf(float x) {
+    if (x != x) return x;
+    const float ax = fabsf(x);
+    if (ax > 1.0f) return PTM_NAN;
+    float r;
+    if (ax <= 0.5f) {
+        r = ptm_asin_poly(ax, ax * ax);
+    } else {
+        const float z = (1.0f - ax) * 0.5f;
+        const float s = sqrtf(z);
+        r = PTM_PIO2_1 - (2.0f * ptm_asin_poly(s, z) - PTM_PIO2_2);
+    }
+    return (ptm_bits(x) >> 31) ? -r : r;
+}
+
+/* atan(r) for r in [0, 1]: r + r^3 * T(r^2). */
+PTM_FN float ptm_atan_poly(float r) {
+    const float z = r * r;
+    float t = PTM_FMA(PTM_T8, z, PTM_T7);
+    t = PTM_FMA(t, z, PTM_T6);
+    t = PTM_FMA(t, z, PTM_T5);
+    t = PTM_FMA(t, z, PTM_T4);
+    t = PTM_FMA(t, z, PTM_T3);
+    t = PTM_FMA(t, z, PTM_T2);
+    t = PTM_FMA(t, z, PTM_T1);
+    t = PTM_FMA(t, z, PTM_T0);
+    return PTM_FMA(r * z, t, r);
+}
+
+/* atan(x): |x| > 1 through pi/2 - atan(1/|x|). */
+PTM_CALL float ptm_atanf(float x) {
+    if (x != x) return x;
+    const float a = fabsf(x);
+    float r;
+    if (a > 1.0f) {
+        const float p = ptm_atan_poly(1.0f / a);
+        r = PTM_PIO2_1 - (p - PTM_PIO2_2);
+    } else {
+        r = ptm_atan_poly(a);
+    }
+    return (ptm_bits(x) >> 31) ? -r : r;
+}
+
+/* atan2(y, x), the angle of (x, y) in [-pi, pi], with the IEEE conventions
+ * for zeros and infinities; NaN in, NaN out. */
+PTM_CALL float ptm_atan2f(float y, float x) {
+    if (x != x || y != y) return PTM_NAN;
+    const float ax = fabsf(x), ay = fabsf(y);
+    const int xneg = (int)(ptm_bits(x) >> 31);
+    float r;
+    if (ax == PTM_INF && ay == PTM_INF) {
+        r = PTM_PIO2_1 * 0.5f; /* pi/4 */
+        if (xneg) r = PTM_PI_1 - (r - PTM_PI_2);
+    } else if (ay == 0.0f) {
+        r = xneg ? PTM_PI_1 : 0.0f;
+    } else {
+        const int swap = ay > ax;
+        const float t = swap ? ax / ay : ay / ax;
+        const float p = ptm_atan_poly(t);
+        r = swap ? PTM_PIO2_1 - (p - PTM_PIO2_2) : p;
+        if (xneg) r = PTM_PI_1 - (r - PTM_PI_2);
+    }
+    return (ptm_bits(y) >> 31) ? -r : r;
+}
+
+/* 2^x: x = k + f with k integral and |f| <= 1/2, 2^f = e^(f ln2) by the
+ * exponential's polynomial. */
+PTM_CALL float ptm_exp2f(float x) {
+    if (x != x) return x;
+    if (x > 128.0f) return PTM_INF;
+    if (x < -150.0f) return 0.0f;
+    const float k = rintf(x);
+    const float f = x - k;
+    const float r = PTM_FMA(f, PTM_LN2_1, f * PTM_LN2_2);
+    const float p =
+        PTM_FMA(PTM_FMA(PTM_FMA(PTM_FMA(PTM_FMA(PTM_E5, r, PTM_E4), r, PTM_E3), r, PTM_E2), r, PTM_E1), r, PTM_E0);
+    const float em1 = PTM_FMA(r * r, p, r);
+    return ptm_scale2(1.0f + em1, (int)k);
+}
+
+/* log2(x) = log(x) * log2(e). */
+PTM_CALL float ptm_log2f(float x) { return ptm_logf(x) * PTM_LOG2E; }
 
 #endif /* PT_MATHF_H */

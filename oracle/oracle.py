@@ -139,7 +139,9 @@ def dispatch(ubo: np.ndarray, push, plugins: list, accum: np.ndarray, rect=None,
     return out
 
 
-MATHF = {"sin": 0, "cos": 1, "exp": 2, "log": 3, "pow": 4, "acos": 5}
+# atan2 takes (y, x) like GLSL's atan(y, x): the first array is y.
+MATHF = {"sin": 0, "cos": 1, "exp": 2, "log": 3, "pow": 4, "acos": 5, "asin": 6, "atan": 7, "atan2": 8, "exp2": 9,
+         "log2": 10}
 
 
 def mathf(fn: str, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:

@@ -1357,6 +1357,11 @@ int pto_mathf_eval(int fn, const float* x, const float* y, float* out, int n) {
             case 3: out[i] = ptm_logf(x[i]); break;
             case 4: out[i] = ptm_powf(x[i], y[i]); break;
             case 5: out[i] = ptm_acosf(x[i]); break;
+            case 6: out[i] = ptm_asinf(x[i]); break;
+            case 7: out[i] = ptm_atanf(x[i]); break;
+            case 8: out[i] = ptm_atan2f(x[i], y[i]); break;
+            case 9: out[i] = ptm_exp2f(x[i]); break;
+            case 10: out[i] = ptm_log2f(x[i]); break;
             default: return PT_ERR_INVALID;
         }
     }

@@ -9,7 +9,8 @@
  * Arithmetic follows GLSL's meaning of each expression in source order, with
  * the shader's conventions: single precision, no contraction (built with
  * -ffp-contract=off), mod(a, b) = a - b * floor(a / b), length = sqrt(dot),
- * and sin through the shared pt_mathf routines. */
+ * and the transcendentals through the shared pt_mathf routines (tan as sin / cos
+ * of one reduction). */
 #include <math.h>
 
 #include "../include/pt_mathf.h"
@@ -56,4 +57,24 @@ float user_lattice_material(float x, float y, float z) {
     (void)x;
     (void)z;
     return floorf(fminf(fmaxf(y + 1.0f, 0.0f), 1.5f)) + 1.0f;
+}
+
+/* ---- "spiral": a ring twisted by its polar angle ----------------------- */
+float user_spiral_sdf(float x, float y, float z) {
+    const float a = ptm_atan2f(z, x);
+    const float r = sqrtf(x * x + z * z);
+    const float twist = 0.25f * ptm_sinf(3.0f * a + 2.0f * y);
+    const float qx = r - 0.7f - 0.1f * twist;
+    const float qy = y;
+    const float k = ptm_exp2f(-2.0f) + 0.01f * ptm_log2f(1.0f + r);
+    float s, c;
+    ptm_sincosf(0.3f * y, &s, &c);
+    return sqrtf(qx * qx + qy * qy) - 0.2f - k * 0.1f + 0.02f * ptm_asinf(fminf(fmaxf(y, -1.0f), 1.0f)) +
+           0.001f * (s / c);
+}
+
+float user_spiral_material(float x, float y, float z) {
+    (void)y;
+    (void)z;
+    return roundf(ptm_atanf(x) + 2.0f);
 }

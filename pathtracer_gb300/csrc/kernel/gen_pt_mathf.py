@@ -67,6 +67,10 @@ def main():
     A, e = lawson_fit(lambda z: (np.arcsin(zs(z)) - zs(z)) / (zs(z) ** 3), 1e-12, 0.25, 6,
                       weight=lambda z: zs(z) ** 3 / np.arcsin(zs(z)))
     out["ASIN"] = (A, e)
+    # atan(r) = r + r^3 * T(r^2), r in [0, 1].
+    T, e = lawson_fit(lambda z: (np.arctan(zs(z)) - zs(z)) / (zs(z) ** 3), 1e-12, 1.0, 8,
+                      weight=lambda z: zs(z) ** 3 / np.arctan(zs(z)))
+    out["ATAN"] = (T, e)
     for name, (c, err) in out.items():
         vals = ", ".join(f"{f32(v):.9e}f" for v in c)
         print(f"/* {name}: max weighted error {err:.2e} */")

@@ -8,9 +8,10 @@
 // Covered: float/int/bool, vec2/vec3/vec4 (constructors, component access,
 // read swizzles as member calls, arithmetic with vectors and scalars),
 // mat2/mat3 (constructors from columns, matrix * vector), and the built-ins
-// abs sign floor ceil fract mod min max clamp mix step smoothstep sqrt
-// inversesqrt pow exp log sin cos acos length distance dot cross normalize
-// reflect fma radians degrees, plus the shader's smin for floats and vec2.
+// abs sign floor ceil fract round trunc mod min max clamp mix step
+// smoothstep sqrt inversesqrt pow exp exp2 log log2 sin cos tan asin acos
+// atan (one and two arguments) length distance dot cross normalize reflect
+// fma radians degrees, plus the shader's smin for floats and vec2.
 #pragma once
 
 #if defined(__CUDACC__)
@@ -131,6 +132,18 @@ PTG_FN float f_log(float a) { return ptm_logf(a); }
 PTG_FN float f_sin(float a) { return ptm_sinf(a); }
 PTG_FN float f_cos(float a) { return ptm_cosf(a); }
 PTG_FN float f_acos(float a) { return ptm_acosf(a); }
+PTG_FN float f_asin(float a) { return ptm_asinf(a); }
+PTG_FN float f_atan(float a) { return ptm_atanf(a); }
+PTG_FN float f_atan2(float y, float x) { return ptm_atan2f(y, x); }
+PTG_FN float f_tan(float a) {
+    float s, c;
+    ptm_sincosf(a, &s, &c);
+    return s / c;
+}
+PTG_FN float f_exp2(float a) { return ptm_exp2f(a); }
+PTG_FN float f_log2(float a) { return ptm_log2f(a); }
+PTG_FN float f_round(float a) { return roundf(a); }
+PTG_FN float f_trunc(float a) { return truncf(a); }
 PTG_FN float f_radians(float a) { return a * 0.01745329252f; }
 PTG_FN float f_degrees(float a) { return a * 57.29577951f; }
 PTG_FN float f_mod(float a, float b) { return a - b * floorf(a / b); }
@@ -151,6 +164,13 @@ PTG_MAP1(log, f_log)
 PTG_MAP1(sin, f_sin)
 PTG_MAP1(cos, f_cos)
 PTG_MAP1(acos, f_acos)
+PTG_MAP1(asin, f_asin)
+PTG_MAP1(atan, f_atan)
+PTG_MAP1(tan, f_tan)
+PTG_MAP1(exp2, f_exp2)
+PTG_MAP1(log2, f_log2)
+PTG_MAP1(round, f_round)
+PTG_MAP1(trunc, f_trunc)
 PTG_MAP1(radians, f_radians)
 PTG_MAP1(degrees, f_degrees)
 PTG_MAP2(mod, f_mod)
@@ -158,6 +178,7 @@ PTG_MAP2(min, f_min)
 PTG_MAP2(max, f_max)
 PTG_MAP2(pow, f_pow)
 PTG_MAP2(step, f_step)
+PTG_MAP2(atan, f_atan2)  // atan(y, x)
 PTG_FN vec2 step(float e, vec2 a) { return step(vec2(e), a); }
 PTG_FN vec3 step(float e, vec3 a) { return step(vec3(e), a); }
 

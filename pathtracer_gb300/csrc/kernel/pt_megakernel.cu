@@ -51,7 +51,12 @@ __global__ void mathf_eval_kernel(int fn, const float* __restrict__ x, const flo
         case 2: r = ptm_expf(x[i]); break;
         case 3: r = ptm_logf(x[i]); break;
         case 4: r = ptm_powf(x[i], y[i]); break;
-        default: r = ptm_acosf(x[i]); break;
+        case 5: r = ptm_acosf(x[i]); break;
+        case 6: r = ptm_asinf(x[i]); break;
+        case 7: r = ptm_atanf(x[i]); break;
+        case 8: r = ptm_atan2f(x[i], y[i]); break;
+        case 9: r = ptm_exp2f(x[i]); break;
+        default: r = ptm_log2f(x[i]); break;
     }
     out[i] = r;
 }

@@ -517,7 +517,7 @@ int pt_set_stream(pt_ctx* ctx, void* stream) {
 
 int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float* d_out, int n) {
     if (!ctx) return PT_ERR_INVALID;
-    if (fn < 0 || fn > 5 || n < 0 || (n > 0 && (!d_x || !d_out || (fn == 4 && !d_y))))
+    if (fn < 0 || fn > 10 || n < 0 || (n > 0 && (!d_x || !d_out || ((fn == 4 || fn == 8) && !d_y))))
         return fail(ctx, PT_ERR_INVALID, "pt_mathf_eval: bad arguments");
     PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     PT_CUDA_TRY(ctx, ptk_mathf_eval(fn, d_x, d_y, d_out, n, ctx->stream));

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import REFERENCE, ROOT, reference_available
-from user_snippets import LATTICE, SNIPPETS, TORUS
+from user_snippets import LATTICE, SNIPPETS, SPIRAL, TORUS
 
 KERNEL_DIR = os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel")
 BUILD_DIR = os.path.join(ROOT, "oracle", "_build")
@@ -136,9 +136,9 @@ def test_shipped_snippets_translate_to_the_builtins(pt):
 
 
 def test_jit_check_compiles_the_megakernel(pt):
-    """NVRTC builds the run-time megakernel (both trace variants) for sm_103a
-    with two user snippets in slots 0 and 1."""
-    log = pt.jit_check([TORUS, LATTICE], sm=103)
+    """NVRTC builds the run-time megakernel (both trace variants) and march
+    kernel for sm_103a with three user snippets in slots 0-2."""
+    log = pt.jit_check([TORUS, LATTICE, SPIRAL], sm=103)
     assert "error" not in log.lower()
 
 

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from conftest import SCENES
-from user_snippets import LATTICE, SNIPPETS, TORUS
+from user_snippets import LATTICE, SNIPPETS, SPIRAL, TORUS
 
 pytestmark = pytest.mark.gpu
 
@@ -40,17 +40,18 @@ def _scene(rt, sdfs):
 TORUS_SDF = {"position": [-1.3, 0.6, 0.0], "boundingSize": [2.4, 2.4, 2.4], "glsl": TORUS}
 LATTICE_SDF = {"position": [1.3, 1.0, 0.0], "boundingSize": [2.0, 2.0, 2.0], "glsl": LATTICE}
 BULB_SDF = {"position": [0.0, 1.15, -2.0], "boundingSize": [2.5, 2.5, 2.5], "builtin": "mandelbulb"}
+SPIRAL_SDF = {"position": [0.0, 0.45, 1.2], "boundingSize": [2.2, 1.2, 2.2], "glsl": SPIRAL}
 
 
 @pytest.mark.parametrize("engine", [0, 1])
 def test_user_snippets_match_oracle(rt, engine):
-    """Two user snippets and a shipped one in one scene, traced per path,
+    """Three user snippets and a shipped one in one scene, traced per path,
     through the compiled megakernel (engine 0) and the wavefront engine with
     the compiled march kernel (engine 1)."""
     from oracle import compare
 
     W, H, spf, depth = 64, 48, 4, 6
-    scene = _scene(rt, [TORUS_SDF, LATTICE_SDF, BULB_SDF])
+    scene = _scene(rt, [TORUS_SDF, LATTICE_SDF, BULB_SDF, SPIRAL_SDF])
     ubo = scene.pack_ubo(rt["cie"])
     plugins = compare.plugins_for(scene, custom=CUSTOM)
     with rt["Context"](0) as ctx:

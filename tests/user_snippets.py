@@ -4,7 +4,8 @@ restatement in C in oracle/user_sdfs.c under the function names given here.
 
 They use what scene authors write: helper functions with in/out parameters,
 file-scope constants, swizzles (.xz, rgba), vector-scalar arithmetic, and the
-built-ins length, sin, abs, max, min, mod, floor, clamp.
+built-ins length, sin, tan, asin, atan (one and two arguments), exp2, log2,
+round, abs, max, min, mod, floor, clamp.
 """
 
 TORUS = """
@@ -54,8 +55,27 @@ float sdfmaterial(vec3 p)
 }
 """
 
+SPIRAL = """
+// A ring twisted by its polar angle; inverse and binary-log built-ins.
+float sdf(vec3 p)
+{
+    float a = atan(p.z, p.x);
+    float r = length(p.xz);
+    float twist = 0.25 * sin(3.0 * a + 2.0 * p.y);
+    vec2 q = vec2(r - 0.7 - 0.1 * twist, p.y);
+    float k = exp2(-2.0) + 0.01 * log2(1.0 + r);
+    return length(q) - 0.2 - k * 0.1 + 0.02 * asin(clamp(p.y, -1.0, 1.0)) + 0.001 * tan(0.3 * p.y);
+}
+
+float sdfmaterial(vec3 p)
+{
+    return round(atan(p.x) + 2.0);
+}
+"""
+
 # name -> (GLSL, C function for sdf, C function for sdfmaterial)
 SNIPPETS = {
     "torus": (TORUS, "user_torus_sdf", "user_torus_material"),
     "lattice": (LATTICE, "user_lattice_sdf", "user_lattice_material"),
+    "spiral": (SPIRAL, "user_spiral_sdf", "user_spiral_material"),
 }
