@@ -143,7 +143,8 @@ uint64_t pt_sdf_source_fingerprint(const char* source);
 
 /* GLSL SDF snippet (a scene's `sdf[i].glsl`: `float sdf(in vec3 p)` and
  * `float sdfmaterial(in vec3 p)` plus helpers) to C++ over the GLSL shim the
- * run-time compiled kernels include, every function renamed <prefix><name>.
+ * run-time compiled kernels include, every function renamed <prefix><name>
+ * and the text wrapped in namespace ptg::<prefix> (prefix: an identifier).
  * Writes a NUL-terminated text of at most cap bytes (*needed: its size);
  * PT_ERR_UNSUPPORTED with a reason in err for what the shim does not cover. */
 int pt_glsl_translate(const char* glsl, const char* prefix, char* out, size_t cap, size_t* needed, char* err,
@@ -358,6 +359,13 @@ int pt_batch_set_persist_refill(pt_batch* batch, int lanes);
 int pt_batch_set_route(pt_batch* batch, int route);
 int pt_batch_add_scene(pt_batch* batch, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins,
                        int* scene_id);
+/* A scene whose SDFs are given as text, like pt_set_sdfs: the shipped
+ * snippets and builtin: specs select plug-ins, any other GLSL is translated
+ * here (PT_ERR_UNSUPPORTED with the reason for what the translator cannot
+ * express) and compiled with NVRTC, together with every other snippet of the
+ * batch, into the staged engine's march kernel before the next step.  Such
+ * scenes render on the staged engine (a persistent route is refused). */
+int pt_batch_add_scene_sources(pt_batch* batch, const pt_ubo* ubo, const char* const* sources, int n, int* scene_id);
 int pt_batch_add_target(pt_batch* batch, int width, int height, int kind, int* target_id);
 /* Device pointer of a target: float4 per pixel (FLOAT) or 4 doubles per pixel
  * (FP64: x, y, z sums and the sample count). */

@@ -197,6 +197,9 @@ int pt_server_set_mode(pt_server* server, int mode);
 pt_batch* pt_server_batch(pt_server* server);
 /* Makes a scene resident under `key`. */
 int pt_server_add_scene(pt_server* server, int key, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins);
+/* Makes a scene resident whose SDFs are given as text (pt_batch_add_scene_sources;
+ * the plain path sets them with pt_set_sdfs). */
+int pt_server_add_scene_sources(pt_server* server, int key, const pt_ubo* ubo, const char* const* sources, int n);
 /* Renders scene `key`'s FP64 reference for a view (push: resolution, camera,
  * path length) with spp samples per pixel from sample indices no request
  * uses; blocks until done. */

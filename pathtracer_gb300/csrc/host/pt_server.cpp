@@ -40,6 +40,7 @@ struct SceneEntry {
     int batch_scene = -1;
     pt_ubo* ubo = nullptr;  // host copy for the plain path's uploads
     std::vector<pt_sdf_plugin> plugins;
+    std::vector<std::string> sources;  // SDF texts (scenes added with sources)
     int ref_target = -1;
     int ref_w = 0, ref_h = 0;
 };
@@ -256,7 +257,14 @@ int poll_plain(pt_server* s) {
         s->active.push_back(j.id);
         const SceneEntry& sc = s->scenes[j.req.scene_key];
         if (s->ctx_scene != j.req.scene_key) {
-            int rc = pt_set_sdf_plugins(s->ctx, sc.plugins.data(), (int)sc.plugins.size());
+            int rc;
+            if (!sc.sources.empty()) {
+                std::vector<const char*> src;
+                for (const std::string& t : sc.sources) src.push_back(t.c_str());
+                rc = pt_set_sdfs(s->ctx, src.data(), (int)src.size());
+            } else {
+                rc = pt_set_sdf_plugins(s->ctx, sc.plugins.data(), (int)sc.plugins.size());
+            }
             if (rc == PT_OK) rc = pt_upload_scene(s->ctx, sc.ubo);
             if (rc != PT_OK) return from_ctx(s, rc, "upload");
             s->ctx_scene = j.req.scene_key;
@@ -364,6 +372,24 @@ int pt_server_add_scene(pt_server* s, int key, const pt_ubo* ubo, const pt_sdf_p
     if (!e.ubo) return sfail(s, PT_ERR_OOM, "pt_server_add_scene: out of host memory");
     *e.ubo = *ubo;
     e.plugins.assign(plugins, plugins + nplugins);
+    s->scenes[key] = std::move(e);
+    s->resident_bytes += sizeof(pt_ubo);
+    return PT_OK;
+}
+
+int pt_server_add_scene_sources(pt_server* s, int key, const pt_ubo* ubo, const char* const* sources, int n) {
+    if (!s) return PT_ERR_INVALID;
+    if (!ubo || n < 0 || (n > 0 && !sources) || s->scenes.count(key))
+        return sfail(s, PT_ERR_INVALID, "pt_server_add_scene_sources: bad arguments or key in use");
+    for (int i = 0; i < n; i++)
+        if (!sources[i]) return sfail(s, PT_ERR_INVALID, "pt_server_add_scene_sources: null source");
+    SceneEntry e;
+    int rc = pt_batch_add_scene_sources(s->batch, ubo, sources, n, &e.batch_scene);
+    if (rc != PT_OK) return from_batch(s, rc, "pt_server_add_scene_sources");
+    e.ubo = new (std::nothrow) pt_ubo;
+    if (!e.ubo) return sfail(s, PT_ERR_OOM, "pt_server_add_scene_sources: out of host memory");
+    *e.ubo = *ubo;
+    e.sources.assign(sources, sources + n);
     s->scenes[key] = std::move(e);
     s->resident_bytes += sizeof(pt_ubo);
     return PT_OK;

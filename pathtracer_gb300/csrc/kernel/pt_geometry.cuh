@@ -445,7 +445,7 @@ PT_DI float scene_sdf(const KScene& S, float3 p, uint32_t set1) {
         const int i = __ffs(bits) - 1;
         bits &= bits - 1u;
         const int kind = S.plug[i].kind;
-        if (kind != PT_SDF_NONE) sdf = fminf(sdf, plugin_sdf(kind, i, p - sdf_pos(S, i)));
+        if (kind != PT_SDF_NONE) sdf = fminf(sdf, plugin_sdf(kind, S.meta.custom_base + i, p - sdf_pos(S, i)));
     }
     return sdf;
 }
@@ -461,7 +461,7 @@ PT_DI float scene_sdf_sel(const KScene& S, float3 p, uint32_t set1, int& sel) {
         bits &= bits - 1u;
         const int kind = S.plug[i].kind;
         if (kind != PT_SDF_NONE) {
-            const float di = plugin_sdf(kind, i, p - sdf_pos(S, i));
+            const float di = plugin_sdf(kind, S.meta.custom_base + i, p - sdf_pos(S, i));
             if (!(sdf < di)) sel = i;
             sdf = fminf(sdf, di);
         }
@@ -482,8 +482,8 @@ static __device__ __noinline__ float scene_sdf_material(const KScene& S, float3 
         const pt_sdf_plugin pl = S.plug[i];
         if (pl.kind != PT_SDF_NONE) {
             const float3 q = p - sdf_pos(S, i);
-            const float di = plugin_sdf(pl.kind, i, q);
-            mat = (sdf < di) ? mat : plugin_material(pl, i, q);
+            const float di = plugin_sdf(pl.kind, S.meta.custom_base + i, q);
+            mat = (sdf < di) ? mat : plugin_material(pl, S.meta.custom_base + i, q);
             sdf = fminf(sdf, di);
         }
     }
@@ -497,7 +497,7 @@ static __device__ __noinline__ float scene_sdf_material(const KScene& S, float3 
 // none, without evaluating the distances again; otherwise (-2: the march ran
 // out of steps) the full selection runs.
 PT_DI float scene_sdf_material_hit(const KScene& S, float3 p, uint32_t set1, int hit_sel) {
-    if (hit_sel >= 0) return plugin_material(S.plug[hit_sel], hit_sel, p - sdf_pos(S, hit_sel));
+    if (hit_sel >= 0) return plugin_material(S.plug[hit_sel], S.meta.custom_base + hit_sel, p - sdf_pos(S, hit_sel));
     if (hit_sel == -1) return 0.0f;
     return scene_sdf_material(S, p, set1);
 }

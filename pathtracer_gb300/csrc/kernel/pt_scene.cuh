@@ -24,6 +24,8 @@ struct pt_scene_meta {
     int offset[5];      // float offset of each primitive class in objects[]
     int nplug;          // plug-ins set by pt_set_sdfs (slots beyond evaluate as absent)
     int total_objects;  // n[0] + ... + n[4]
+    int custom_base;    // run-time compiled snippets: slot i is snippet custom_base + i of the
+                        // compiled program (0 for a context; a batch numbers all its scenes' slots)
 };
 
 struct KScene {

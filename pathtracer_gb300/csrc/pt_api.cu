@@ -55,7 +55,11 @@ struct pt_ctx {
     // GLSL snippets other than the shipped four (PT_SDF_CUSTOM slots), as
     // translated by pt_glsl_translate, and the module compiled for them.
     std::vector<JitSlot> custom;
-    JitModule jit[kJitKinds];
+    // Modules compiled for this context, per kind, oldest first (at most
+    // kJitCache each, so switching between scenes does not recompile), and
+    // the one the current snippets use.
+    std::vector<JitModule> jit[kJitKinds];
+    int jit_cur[kJitKinds] = {-1, -1};
     std::string err;
 };
 
@@ -146,7 +150,8 @@ int pt_destroy(pt_ctx* ctx) {
     }
     if (ctx->d_colors) cudaFree(ctx->d_colors);
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
-    for (JitModule& m : ctx->jit) pt_jit_unload(m);
+    for (auto& cache : ctx->jit)
+        for (JitModule& m : cache) pt_jit_unload(m);
     if (ctx->done) cudaEventDestroy(ctx->done);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx->params;
@@ -550,7 +555,8 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     // Run-time compiled SDF snippets: their march kernel (the other stages
     // evaluate no SDF).
     ctx->wf->set_march_kernel(ctx->custom.empty() ? nullptr
-                                                  : reinterpret_cast<const void*>(ctx->jit[kJitMarch].kernel[0]));
+                                                  : reinterpret_cast<const void*>(
+                                                        ctx->jit[kJitMarch][(size_t)ctx->jit_cur[kJitMarch]].kernel[0]));
     const size_t cbytes = (size_t)total * sizeof(float4);
     if (cbytes > ctx->colors_bytes) {
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -595,15 +601,18 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
 
 // Scenes with GLSL snippets beyond the shipped four: the megakernel (plain
 // engine) or the march kernel (wavefront engine; its other stages evaluate no
-// SDF) compiled at run time with their translation (pt_jit.cu) on first use,
-// and again when the set of snippets changes.
+// SDF) compiled at run time with their translation (pt_jit.cu) the first time
+// a set of snippets is dispatched; the last 8 modules of each kind are kept.
 static int ensure_jit(pt_ctx* ctx, JitKind kind) {
-    JitModule& m = ctx->jit[kind];
+    constexpr size_t kJitCache = 8;
+    std::vector<JitModule>& cache = ctx->jit[kind];
     const std::string program = pt_jit_program(ctx->custom, kind);
-    if (m.key == program) return PT_OK;
-    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (kind == kJitMarch && ctx->wf) ctx->wf->set_march_kernel(nullptr);  // no graph may keep the old kernel
-    pt_jit_unload(m);
+    for (size_t i = 0; i < cache.size(); i++)
+        if (cache[i].key == program) {
+            ctx->jit_cur[kind] = (int)i;
+            return PT_OK;
+        }
+    JitModule m;
     std::vector<char> cubin;
     std::string lowered[kJitMaxKernels], log;
     int rc = pt_jit_compile(ctx->device, program, kind, cubin, lowered, log);
@@ -611,11 +620,20 @@ static int ensure_jit(pt_ctx* ctx, JitKind kind) {
     rc = pt_jit_load(cubin, kind, lowered, m, log);
     if (rc != PT_OK) return fail(ctx, rc, log);
     m.key = program;
+    if (cache.size() == kJitCache) {  // evict the oldest
+        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (kind == kJitMarch && ctx->wf) ctx->wf->set_march_kernel(nullptr);  // no graph may keep its kernel
+        pt_jit_unload(cache.front());
+        cache.erase(cache.begin());
+    }
+    cache.push_back(m);
+    ctx->jit_cur[kind] = (int)cache.size() - 1;
     return PT_OK;
 }
 
 static int dispatch_jit(pt_ctx* ctx, bool trace) {
-    PT_CUDA_TRY(ctx, pt_jit_launch(ctx->jit[kJitMegakernel], ctx->params, trace, ctx->stream));
+    PT_CUDA_TRY(ctx, pt_jit_launch(ctx->jit[kJitMegakernel][(size_t)ctx->jit_cur[kJitMegakernel]], ctx->params, trace,
+                                   ctx->stream));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
 }

@@ -33,6 +33,7 @@
 #include "kernel/pt_features.h"
 #include "kernel/pt_megakernel.h"
 #include "pt_engine.h"
+#include "pt_jit.h"
 
 namespace {
 
@@ -41,6 +42,7 @@ struct BatchScene {
     float* d_cie = nullptr;
     bool live = false;
     bool has_sdf = false;
+    bool custom = false;        // holds run-time compiled snippets (staged engine only)
     int variant = PT_FEAT_ALL;  // primitive classes present (pt_features.h)
     uint32_t passes_in_flight = 0;
 };
@@ -109,6 +111,14 @@ struct pt_batch {
     double2* d_rmse = nullptr;
     double2* h_rmse = nullptr;     // pinned
     std::vector<char> blocked;       // per target, scratch of pt_batch_step
+    // Run-time compiled SDF snippets of every scene added with sources, numbered
+    // across the batch (a scene's slot i is snippet custom_base + i), and the
+    // march kernel compiled for all of them (rebuilt before the next step
+    // after a scene brought new ones).
+    std::vector<JitSlot> custom;
+    int custom_next = 0;
+    JitModule jit;
+    bool jit_dirty = false;
     std::string err;
 };
 
@@ -157,6 +167,7 @@ cudaError_t ensure_engine(pt_batch* b, int e) {
     }
     b->engine[e].set_persistent(e == kPersistent);
     b->engine[e].args.persist_refill = b->persist_refill;
+    if (e == kStaged && b->jit.lib) b->engine[e].set_march_kernel(reinterpret_cast<const void*>(b->jit.kernel[0]));
     b->engine_live[e] = true;
     return cudaSuccess;
 }
@@ -369,6 +380,7 @@ int pt_batch_destroy(pt_batch* b) {
     if (b->mempool) cudaMemPoolDestroy(b->mempool);
     if (b->h_finished) cudaFreeHost(b->h_finished);
     free_rmse(b);
+    pt_jit_unload(b->jit);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return PT_OK;
@@ -402,10 +414,14 @@ int pt_batch_set_route(pt_batch* b, int route) {
     return PT_OK;
 }
 
-int pt_batch_add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins, int* scene_id) {
-    if (!b) return PT_ERR_INVALID;
-    if (!ubo || !scene_id || nplugins < 0 || (nplugins > 0 && !plugins))
-        return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: bad arguments");
+}  // extern "C"
+
+namespace {
+
+// The scene's device copy; plug-ins of kind PT_SDF_CUSTOM are snippets
+// custom_base + slot of the batch's compiled march kernel.
+int add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins, int custom_base,
+              int* scene_id) {
     int n[7];
     const int caps[7] = {PT_MAX_OBJECTS_SIZE / 6, PT_MAX_OBJECTS_SIZE / 5, PT_MAX_OBJECTS_SIZE / 11,
                          PT_MAX_OBJECTS_SIZE / 12, PT_MAX_OBJECTS_SIZE / 16, PT_MAX_SDFS_SIZE / 6,
@@ -418,12 +434,11 @@ int pt_batch_add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plug
         return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: objects overflow the 1024-float object array");
     if (n[5] > PT_MAX_LIVE_SDFS || nplugins > PT_MAX_LIVE_SDFS)
         return bfail(b, PT_ERR_UNSUPPORTED, "pt_batch_add_scene: at most 32 SDFs can be evaluated (32-bit set mask)");
+    bool custom = false;
     for (int i = 0; i < nplugins; i++) {
-        if (plugins[i].kind == PT_SDF_CUSTOM)
-            return bfail(b, PT_ERR_UNSUPPORTED,
-                         "pt_batch_add_scene: run-time compiled SDFs render through pt_dispatch only");
-        if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_TERRAIN)
+        if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_CUSTOM)
             return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: unknown plug-in kind");
+        custom = custom || plugins[i].kind == PT_SDF_CUSTOM;
     }
     PT_B_TRY(b, cudaSetDevice(b->device));
     KScene* S = new (std::nothrow) KScene;
@@ -444,6 +459,7 @@ int pt_batch_add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plug
     S->meta.total_objects = n[0] + n[1] + n[2] + n[3] + n[4];
     if (nplugins > 0) std::memcpy(S->plug, plugins, sizeof(pt_sdf_plugin) * (size_t)nplugins);
     S->meta.nplug = nplugins;
+    S->meta.custom_base = custom_base;
     BatchScene bs;
     cudaError_t e = cudaMalloc(&bs.d_scene, sizeof(KScene));
     if (e == cudaSuccess) e = cudaMalloc(&bs.d_cie, sizeof(float) * PT_CIE_TABLE_SIZE);
@@ -465,11 +481,16 @@ int pt_batch_add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plug
     }
     bs.live = true;
     bs.has_sdf = n[5] > 0;
+    bs.custom = custom;
     bs.variant = pt_feature_variant(n);
     *scene_id = (int)b->scenes.size();
     b->scenes.push_back(bs);
     return PT_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int pt_batch_add_target(pt_batch* b, int width, int height, int kind, int* target_id) {
     if (!b) return PT_ERR_INVALID;
@@ -502,6 +523,46 @@ void* pt_batch_target_device_ptr(pt_batch* b, int target_id) {
     return t.kind == PT_TARGET_FLOAT ? (void*)t.d_accum : (void*)t.d_sum;
 }
 
+int pt_batch_add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins, int* scene_id) {
+    if (!b) return PT_ERR_INVALID;
+    if (!ubo || !scene_id || nplugins < 0 || (nplugins > 0 && !plugins))
+        return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: bad arguments");
+    for (int i = 0; i < nplugins; i++)
+        if (plugins[i].kind == PT_SDF_CUSTOM)
+            return bfail(b, PT_ERR_UNSUPPORTED,
+                         "pt_batch_add_scene: run-time compiled SDFs need their text (pt_batch_add_scene_sources)");
+    return add_scene(b, ubo, plugins, nplugins, 0, scene_id);
+}
+
+int pt_batch_add_scene_sources(pt_batch* b, const pt_ubo* ubo, const char* const* sources, int n, int* scene_id) {
+    if (!b) return PT_ERR_INVALID;
+    if (!ubo || !scene_id || n < 0 || (n > 0 && !sources))
+        return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene_sources: bad arguments");
+    if (n > PT_MAX_LIVE_SDFS)
+        return bfail(b, PT_ERR_UNSUPPORTED, "pt_batch_add_scene_sources: at most 32 SDFs can be evaluated");
+    pt_sdf_plugin plug[PT_MAX_LIVE_SDFS];
+    std::vector<JitSlot> added;
+    const int base = b->custom_next;
+    for (int i = 0; i < n; i++) {
+        if (!sources[i]) return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene_sources: null source");
+        if (pt_parse_sdf_source(sources[i], &plug[i]) == PT_OK) continue;
+        JitSlot j;
+        std::string why;
+        const int rc = pt_jit_translate_slot(sources[i], base + i, j, why);
+        if (rc != PT_OK) return bfail(b, rc, "pt_batch_add_scene_sources: SDF " + std::to_string(i) + ": " + why);
+        plug[i] = pt_sdf_plugin{PT_SDF_CUSTOM, PT_SDFMAT_DEFAULT, {0.0f, 0.0f, 0.0f}};
+        added.push_back(j);
+    }
+    const int rc = add_scene(b, ubo, plug, n, added.empty() ? 0 : base, scene_id);
+    if (rc != PT_OK) return rc;
+    if (!added.empty()) {
+        b->custom.insert(b->custom.end(), added.begin(), added.end());
+        b->custom_next = base + n;
+        b->jit_dirty = true;
+    }
+    return PT_OK;
+}
+
 int pt_batch_add_pass(pt_batch* b, int scene_id, int target_id, const pt_push* push, int* pass_id) {
     if (!b) return PT_ERR_INVALID;
     if (!push || !pass_id) return bfail(b, PT_ERR_INVALID, "pt_batch_add_pass: bad arguments");
@@ -519,6 +580,9 @@ int pt_batch_add_pass(pt_batch* b, int scene_id, int target_id, const pt_push* p
     const int e = b->route == PT_BATCH_ROUTE_STAGED       ? kStaged
                   : b->route == PT_BATCH_ROUTE_PERSISTENT ? kPersistent
                   : (sc.has_sdf ? kStaged : kPersistent);
+    if (e == kPersistent && sc.custom && sc.has_sdf)
+        return bfail(b, PT_ERR_UNSUPPORTED,
+                     "pt_batch_add_pass: scenes with run-time compiled SDFs render on the staged engine");
     PT_B_TRY(b, cudaSetDevice(b->device));
     PT_B_TRY(b, ensure_engine(b, e));
     WfEngine& E = b->engine[e];
@@ -560,12 +624,49 @@ int pt_batch_add_pass(pt_batch* b, int scene_id, int target_id, const pt_push* p
 // then resolves every pass whose samples have all finished (and whose
 // earlier passes into the same target are resolved) and reports their ids:
 // at most `capacity`, the rest are reported by later calls.
+}  // extern "C"
+
+namespace {
+
+// Compiles the march kernel for every snippet the batch holds, if scenes
+// brought new ones since the last compile, and hands it to the staged engine.
+int prepare_jit(pt_batch* b) {
+    if (!b->jit_dirty) return PT_OK;
+    const std::string program = pt_jit_program(b->custom, kJitMarch);
+    std::vector<char> cubin;
+    std::string lowered[kJitMaxKernels], log;
+    JitModule m;
+    int rc = pt_jit_compile(b->device, program, kJitMarch, cubin, lowered, log);
+    if (rc != PT_OK) return bfail(b, rc, "compiling the batch's SDF snippets: " + log);
+    rc = pt_jit_load(cubin, kJitMarch, lowered, m, log);
+    if (rc != PT_OK) return bfail(b, rc, log);
+    m.key = program;
+    if (b->estream[kStaged]) {
+        const cudaError_t e = cudaStreamSynchronize(b->estream[kStaged]);  // the old module's launches
+        if (e != cudaSuccess) {
+            pt_jit_unload(m);
+            return bcuda(b, e, "pt_batch_step");
+        }
+    }
+    if (b->engine_live[kStaged]) b->engine[kStaged].set_march_kernel(reinterpret_cast<const void*>(m.kernel[0]));
+    pt_jit_unload(b->jit);
+    b->jit = m;
+    b->jit_dirty = false;
+    return PT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int pt_batch_step(pt_batch* b, int iterations, int* completed, int capacity, int* ncompleted) {
     if (!b) return PT_ERR_INVALID;
     if (iterations < 0 || capacity < 0 || (capacity > 0 && !completed) || !ncompleted)
         return bfail(b, PT_ERR_INVALID, "pt_batch_step: bad arguments");
     *ncompleted = 0;
     PT_B_TRY(b, cudaSetDevice(b->device));
+    const int jr = prepare_jit(b);
+    if (jr != PT_OK) return jr;
     bool busy[2];
     for (int e = 0; e < 2; e++) busy[e] = b->engine_live[e] && b->engine[e].njobs > b->engine[e].lo;
     if (iterations > 0 && (busy[0] || busy[1])) {

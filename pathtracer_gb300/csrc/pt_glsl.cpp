@@ -12,7 +12,8 @@
 //   - parameter qualifiers: `in`/`const in` are dropped, `out`/`inout` make
 //     the parameter a reference;
 //   - every function the snippet defines is renamed <prefix><name> and
-//     marked as a device function, so several snippets coexist;
+//     marked as a device function, and the whole text goes into namespace
+//     ptg::<prefix>, so several snippets (or one in several slots) coexist;
 //   - top-level `const float|int` declarations become constexpr.
 // Anything the shim does not cover (structs, uniforms, preprocessor lines,
 // swizzle assignment, arrays of vectors at file scope...) is rejected with a
@@ -135,6 +136,10 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
         return PT_ERR_UNSUPPORTED;
     };
     if (!glsl || !prefix) return PT_ERR_INVALID;
+    // the prefix names a namespace and starts function names: an identifier
+    if (!(std::isalpha((unsigned char)prefix[0]) || prefix[0] == '_')) return fail("the prefix must be an identifier");
+    for (const char* c = prefix; *c; c++)
+        if (!(std::isalnum((unsigned char)*c) || *c == '_')) return fail("the prefix must be an identifier");
     std::vector<Tok> t;
     std::string e;
     if (!tokenize(glsl, t, e)) return fail(e);
@@ -161,7 +166,9 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
     if (!funcs.count("sdf") || !funcs.count("sdfmaterial"))
         return fail("the snippet must define float sdf(vec3) and float sdfmaterial(vec3)");
 
-    std::string o = "namespace ptg {\n";
+    // Each snippet in its own namespace, so that file-scope constants of two
+    // snippets (or of one snippet in two slots) do not collide.
+    std::string o = "namespace ptg {\nnamespace " + std::string(prefix) + " {\n";
     depth = 0;
     int paren = 0;
     bool ref_pending = false;  // out/inout seen: the next type gets '&'
@@ -233,7 +240,7 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
         }
     }
     if (depth != 0 || paren != 0) return fail("unbalanced braces or parentheses");
-    o += "\n}  // namespace ptg\n";
+    o += "\n}  // namespace " + std::string(prefix) + "\n}  // namespace ptg\n";
     if (needed) *needed = o.size() + 1;
     if (!out) return PT_OK;
     if (cap < o.size() + 1) return PT_ERR_INVALID;

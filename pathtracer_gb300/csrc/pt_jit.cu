@@ -52,11 +52,12 @@ std::string pt_jit_program(const std::vector<JitSlot>& slots, JitKind kind) {
     for (const JitSlot& j : slots) s += j.code + "\n";
     s += "static __device__ __forceinline__ float pt_user_sdf(int slot, float3 p) {\n  switch (slot) {\n";
     for (const JitSlot& j : slots)
-        s += "    case " + std::to_string(j.slot) + ": return ptg::" + j.prefix + "sdf(ptg::vec3(p.x, p.y, p.z));\n";
+        s += "    case " + std::to_string(j.slot) + ": return ptg::" + j.prefix + "::" + j.prefix +
+             "sdf(ptg::vec3(p.x, p.y, p.z));\n";
     s += "    default: return 1e5f;\n  }\n}\n";
     s += "static __device__ __forceinline__ float pt_user_material(int slot, float3 p) {\n  switch (slot) {\n";
     for (const JitSlot& j : slots)
-        s += "    case " + std::to_string(j.slot) + ": return ptg::" + j.prefix +
+        s += "    case " + std::to_string(j.slot) + ": return ptg::" + j.prefix + "::" + j.prefix +
              "sdfmaterial(ptg::vec3(p.x, p.y, p.z));\n";
     s += "    default: return 0.0f;\n  }\n}\n";
     s += kind == kJitMegakernel ? "#include \"pt_megakernel_body.cuh\"\n" : "#include \"pt_march.cuh\"\n";

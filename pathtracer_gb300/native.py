@@ -276,6 +276,7 @@ CUDA_API = [
     ("pt_batch_set_route", _i, [_vp, _i]),
     ("pt_batch_set_persist_refill", _i, [_vp, _i]),
     ("pt_batch_add_scene", _i, [_vp, _vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
+    ("pt_batch_add_scene_sources", _i, [_vp, _vp, ctypes.POINTER(ctypes.c_char_p), _i, ctypes.POINTER(_i)]),
     ("pt_batch_add_target", _i, [_vp, _i, _i, _i, ctypes.POINTER(_i)]),
     ("pt_batch_target_device_ptr", _vp, [_vp, _i]),
     ("pt_batch_add_pass", _i, [_vp, _i, _i, ctypes.POINTER(PtPush), ctypes.POINTER(_i)]),
@@ -317,6 +318,7 @@ HOST_API = [
     ("pt_server_set_mode", _i, [_vp, _i]),
     ("pt_server_batch", _vp, [_vp]),
     ("pt_server_add_scene", _i, [_vp, _i, _vp, ctypes.POINTER(PtSdfPlugin), _i]),
+    ("pt_server_add_scene_sources", _i, [_vp, _i, _vp, ctypes.POINTER(ctypes.c_char_p), _i]),
     ("pt_server_render_reference", _i, [_vp, _i, ctypes.POINTER(PtPush), _i, _i]),
     ("pt_server_submit", _i, [_vp, ctypes.POINTER(PtServerJob), ctypes.POINTER(ctypes.c_uint64)]),
     ("pt_server_poll", _i, [_vp, ctypes.POINTER(PtServerResult), _i, ctypes.POINTER(_i)]),

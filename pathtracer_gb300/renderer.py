@@ -311,6 +311,16 @@ class Batch:
         self._check(self._lib.pt_batch_add_scene(self._h, native.ptr(ubo), arr, len(plugins), ctypes.byref(out)))
         return out.value
 
+    def add_scene_sources(self, ubo: np.ndarray, sources: list[str]) -> int:
+        """pt_batch_add_scene_sources: SDFs as text (shipped snippets or any GLSL)."""
+        ubo = np.ascontiguousarray(ubo, np.float32)
+        assert ubo.size == native.UBO_FLOATS
+        arr = (ctypes.c_char_p * max(1, len(sources)))(*[t.encode() for t in sources])
+        out = ctypes.c_int()
+        self._check(self._lib.pt_batch_add_scene_sources(self._h, native.ptr(ubo), arr, len(sources),
+                                                          ctypes.byref(out)))
+        return out.value
+
     def add_target(self, width: int, height: int, kind: int = native.PT_TARGET_FLOAT) -> int:
         out = ctypes.c_int()
         self._check(self._lib.pt_batch_add_target(self._h, width, height, kind, ctypes.byref(out)))
@@ -422,6 +432,11 @@ class Server:
         ubo = np.ascontiguousarray(ubo, np.float32)
         arr = (native.PtSdfPlugin * max(1, len(plugins)))(*plugins)
         self._check(self._lib.pt_server_add_scene(self._h, key, native.ptr(ubo), arr, len(plugins)))
+
+    def add_scene_sources(self, key: int, ubo: np.ndarray, sources: list[str]):
+        ubo = np.ascontiguousarray(ubo, np.float32)
+        arr = (ctypes.c_char_p * max(1, len(sources)))(*[t.encode() for t in sources])
+        self._check(self._lib.pt_server_add_scene_sources(self._h, key, native.ptr(ubo), arr, len(sources)))
 
     def render_reference(self, key: int, push: PtPush, spp: int, spp_per_pass: int = 32):
         self._check(self._lib.pt_server_render_reference(self._h, key, ctypes.byref(push), spp, spp_per_pass))

@@ -28,9 +28,10 @@ def _cpu_build(pt, name: str, snippets: dict) -> ctypes.CDLL:
     code = '#include "pt_glsl_shim.h"\n'
     for n, glsl in snippets.items():
         code += pt.glsl_translate(glsl, n + "_")
-        code += f'extern "C" float c_{n}_sdf(float x, float y, float z) {{ return ptg::{n}_sdf(ptg::vec3(x, y, z)); }}\n'
+        code += (f'extern "C" float c_{n}_sdf(float x, float y, float z) '
+                 f'{{ return ptg::{n}_::{n}_sdf(ptg::vec3(x, y, z)); }}\n')
         code += (f'extern "C" float c_{n}_mat(float x, float y, float z) '
-                 f'{{ return ptg::{n}_sdfmaterial(ptg::vec3(x, y, z)); }}\n')
+                 f'{{ return ptg::{n}_::{n}_sdfmaterial(ptg::vec3(x, y, z)); }}\n')
     os.makedirs(BUILD_DIR, exist_ok=True)
     src = os.path.join(BUILD_DIR, f"glsl_{name}.cpp")
     lib = os.path.join(BUILD_DIR, f"glsl_{name}.so")
@@ -66,11 +67,14 @@ def test_translation_rewrites_glsl(pt):
     assert "vec2(R, 0.25f)" in out and "sin(8.0f * p.z)" in out
     assert "u3_sdTorus(p, vec2(R, 0.25f), ring);" in out
     assert "PTG_FN float u3_sdf(vec3 p)" in out and "PTG_FN float u3_sdfmaterial(vec3 p)" in out
-    assert "//" not in out.replace("} // namespace ptg", "")
+    assert "//" not in out.replace("} // namespace u3_ } // namespace ptg", "")
+    assert out.startswith("namespace ptg { namespace u3_ {")
     lat = pt.glsl_translate(LATTICE, "u0_")
     assert "max(q.x, max(q.y, q.z))" in lat  # .g .b name fields
     assert "/*" not in lat
     assert "1e-3f" in pt.glsl_translate("float sdf(vec3 p){return 1e-3;} float sdfmaterial(vec3 p){return 2.;}", "a_")
+    with pytest.raises(pt.PathTracerError):
+        pt.glsl_translate(TORUS, "9bad")
 
 
 @pytest.mark.parametrize("text,why", [
@@ -137,8 +141,9 @@ def test_shipped_snippets_translate_to_the_builtins(pt):
 
 def test_jit_check_compiles_the_megakernel(pt):
     """NVRTC builds the run-time megakernel (both trace variants) and march
-    kernel for sm_103a with three user snippets in slots 0-2."""
-    log = pt.jit_check([TORUS, LATTICE, SPIRAL], sm=103)
+    kernel for sm_103a with user snippets in slots 0-3, one of them twice
+    (each slot's text has its own namespace)."""
+    log = pt.jit_check([TORUS, LATTICE, SPIRAL, TORUS], sm=103)
     assert "error" not in log.lower()
 
 

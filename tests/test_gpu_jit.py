@@ -165,3 +165,73 @@ def test_batch_rejects_run_time_snippets(rt):
         with pytest.raises(PathTracerError) as e:
             ctx.set_sdf_plugins([native.plugin(native.PT_SDF_CUSTOM)])
         assert e.value.code == native.PT_ERR_INVALID
+
+
+def _dispatch_passes(rt, scene, W, H, spf, depth, npass):
+    with rt["Context"](0) as ctx:
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        for k in range(npass):
+            ctx.dispatch(scene.push_constants(W, H, spf * (k + 1), spf * (k + 1), spf, depth))
+        ctx.wait()
+        return ctx.read_accum()
+
+
+def test_batch_renders_user_snippets_like_dispatch(rt):
+    """Two scenes with different user snippets in one batch (their slots
+    numbered across the batch, one compiled march kernel for all), two
+    progressive passes each: the same bits as pt_dispatch."""
+    from pathtracer_gb300 import Batch
+
+    W, H, spf, depth = 96, 64, 4, 6
+    scenes = [_scene(rt, [TORUS_SDF, LATTICE_SDF, BULB_SDF]), _scene(rt, [SPIRAL_SDF, TORUS_SDF])]
+    with Batch(0, pool_slots=1 << 15, max_passes=64) as b:
+        ids = [b.add_scene_sources(sc.pack_ubo(rt["cie"]), sc.sdf_sources()) for sc in scenes]
+        tgts = [b.add_target(W, H) for _ in scenes]
+        for k in range(2):
+            for sid, tid, sc in zip(ids, tgts, scenes):
+                b.add_pass(sid, tid, sc.push_constants(W, H, spf * (k + 1), spf * (k + 1), spf, depth))
+        b.run()
+        assert b.stats()["passes_staged"] == 4
+        got = [b.read_target(t) for t in tgts]
+    for sc, img in zip(scenes, got):
+        ref = _dispatch_passes(rt, sc, W, H, spf, depth, 2)
+        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+        assert img[..., :3].max() > 0
+
+
+def test_batch_user_snippets_need_the_staged_engine(rt):
+    from pathtracer_gb300 import Batch, PathTracerError, native
+
+    W, H = 32, 32
+    sc = _scene(rt, [TORUS_SDF])
+    with Batch(0, pool_slots=1 << 12, max_passes=16) as b:
+        sid = b.add_scene_sources(sc.pack_ubo(rt["cie"]), sc.sdf_sources())
+        tid = b.add_target(W, H)
+        b.set_route(native.PT_BATCH_ROUTE_PERSISTENT)
+        with pytest.raises(PathTracerError) as e:
+            b.add_pass(sid, tid, sc.push_constants(W, H, 1, 1, 1, 4))
+        assert e.value.code == native.PT_ERR_UNSUPPORTED
+        with pytest.raises(PathTracerError) as e:
+            b.add_scene_sources(sc.pack_ubo(rt["cie"]), ["struct S { float a; }; float sdf(vec3 p){return 0.0;}"])
+        assert e.value.code == native.PT_ERR_UNSUPPORTED
+
+
+def test_server_serves_user_snippets_batched_and_plain(rt):
+    """A resident scene with user snippets: a job's image is the same bits
+    through the batched server and the plain path (which sets the texts with
+    pt_set_sdfs and compiles its own megakernel)."""
+    from pathtracer_gb300 import Server, native
+
+    W, H = 48, 40
+    sc = _scene(rt, [TORUS_SDF, SPIRAL_SDF, BULB_SDF])
+    push = sc.push_constants(W, H, 1, 1, 1, 6)
+    out = []
+    for mode in (native.PT_SERVE_BATCHED, native.PT_SERVE_PLAIN):
+        with Server(0, mode=mode, keep_images=True, pool_slots=1 << 14, max_passes=64) as s:
+            s.add_scene_sources(0, sc.pack_ubo(rt["cie"]), sc.sdf_sources())
+            jid = s.submit(Server.job(0, push, 24))
+            done = s.drain()
+            assert [r.job_id for r in done] == [jid] and done[0].spp == 24
+            out.append(s.read_image(jid))
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
