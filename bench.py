@@ -94,6 +94,8 @@ def parse_args():
     ap.add_argument("--pool-scenes", type=int, default=16, help="serve: scenes in the request pool")
     ap.add_argument("--iters-per-poll", type=int, default=4, help="serve: engine iterations per server poll")
     ap.add_argument("--passes-in-flight", type=int, default=1, help="serve: passes in flight per job")
+    ap.add_argument("--sdf-scenes", default="varied", choices=["varied", "shipped"],
+                    help="serve: SDF scenes with drawn powers/levels (GLSL compiled at run time) or the shipped snippets")
     ap.add_argument("--burst", type=int, default=0,
                     help="serve: N requests all arriving at t=0 instead of the Poisson stream (saturates both arms)")
     ap.add_argument("--jobs", type=int, default=64, help="batch64: jobs per batch")
@@ -510,8 +512,9 @@ def run_serve(args, rank, world):
     n_sdf = max(1, round(0.3 * args.pool_scenes))
     n_sph = args.pool_scenes - n_sdf
     pool = []
+    sdf_kind = native.PT_GEN_SDF_VARIED if args.sdf_scenes == "varied" else native.PT_GEN_SDF
     for k in range(args.pool_scenes):
-        kind, seed = (native.PT_GEN_SPHERES, 1000 + k) if k < n_sph else (native.PT_GEN_SDF, 2000 + k)
+        kind, seed = (native.PT_GEN_SPHERES, 1000 + k) if k < n_sph else (sdf_kind, 2000 + k)
         sc, spec = Scene.generate(kind, seed + 100000 * rank)
         push = sc.push_constants(spec.width, spec.height, 1, 1, 1, spec.pathLength)
         pool.append((kind, sc, spec, push))
@@ -520,7 +523,9 @@ def run_serve(args, rank, world):
                  passes_in_flight=args.passes_in_flight)
     t0 = time.perf_counter()
     for key, (kind, sc, spec, push) in enumerate(pool):
-        srv.add_scene(key, sc.pack_ubo(cie), sc.sdf_plugins())
+        # SDFs as text: generated snippets are compiled at run time (the
+        # batch's march kernel, before its first step: here)
+        srv.add_scene_sources(key, sc.pack_ubo(cie), sc.sdf_sources())
         srv.render_reference(key, push, args.ref_spp, 32)
     ref_secs = time.perf_counter() - t0
 
@@ -540,7 +545,7 @@ def run_serve(args, rank, world):
         """Jobs and samples per scene kind; on the serial plain path also the
         seconds spent on each kind (admission to completion)."""
         out = {}
-        for name, kv in (("spheres", native.PT_GEN_SPHERES), ("sdf", native.PT_GEN_SDF)):
+        for name, kv in (("spheres", native.PT_GEN_SPHERES), ("sdf", sdf_kind)):
             sel = [r for r, k in zip(res, kinds) if k == kv]
             out[name] = {"jobs": len(sel), "samples": sum(r.samples for r in sel)}
             if serial:
@@ -565,6 +570,10 @@ def run_serve(args, rank, world):
 
     res_b, batched = arm(native.PT_SERVE_BATCHED)
     st = srv.stats()
+    # The plain path compiles its megakernel for each scene's snippets on the
+    # scene's first job: one short untimed job per scene first.
+    srv.set_mode(native.PT_SERVE_PLAIN)
+    srv.run_trace([Server.job(k, pool[k][3], 8) for k in range(len(pool))], [0.0] * len(pool))
     res_p, plain = arm(native.PT_SERVE_PLAIN)
     identical = all((a.spp, a.rmse) == (b.spp, b.rmse) for a, b in zip(res_b, res_p))
     reached = sum(1 for r in res_b if r.rmse <= args.target_rmse) / max(1, len(res_b))
@@ -582,7 +591,8 @@ def run_serve(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": 1000.0 * makespan, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, Poisson arrivals)",
-        "config": {"workload": SERVE_WORKLOAD + ("_burst" if args.burst else ""),
+        "config": {"workload": SERVE_WORKLOAD + ("_varied_sdf" if args.sdf_scenes == "varied" else "")
+                   + ("_burst" if args.burst else ""), "sdf_scenes": args.sdf_scenes,
                    "rate_jobs_per_s": None if args.burst else args.rate,
                    "duration_s": None if args.burst else args.duration, "burst_jobs": args.burst or None,
                    "target_rmse": args.target_rmse, "max_spp": args.max_spp, "spp_per_pass": 8,

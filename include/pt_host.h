@@ -86,9 +86,14 @@ int pt_scene_sdf_plugins(const pt_scene* scene, pt_sdf_plugin* out, int cap, int
  *                   path length 8.
  *   PT_GEN_SDF      a mandelbulb, menger or blob plug-in over a ground plane
  *                   under a sky and a sun; W = H uniform over {256, 512,
- *                   1024}; spp 0 (open); path length 8. */
+ *                   1024}; spp 0 (open); path length 8.
+ *   PT_GEN_SDF_VARIED  the same scenes with the mandelbulb's power uniform
+ *                   over [4, 10] (4-6 iterations) and the menger's levels
+ *                   uniform over {3, 4, 5}, given as GLSL text (compiled at
+ *                   run time: pt_set_sdfs, pt_batch_add_scene_sources). */
 #define PT_GEN_SPHERES 0
 #define PT_GEN_SDF 1
+#define PT_GEN_SDF_VARIED 2
 typedef struct pt_job_spec {
     int32_t kind;
     int32_t width, height;

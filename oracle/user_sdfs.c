@@ -78,3 +78,68 @@ float user_spiral_material(float x, float y, float z) {
     (void)z;
     return roundf(ptm_atanf(x) + 2.0f);
 }
+
+/* ---- generated scenes (PT_GEN_SDF_VARIED): mandelbulb of any power ------
+ * The text pt_scene_generate writes for a mandelbulb of power `power` and
+ * `iter` iterations; the parameters are set with user_mandelbulb_set. */
+static float g_mb_power = 8.0f;
+static int g_mb_iter = 4;
+
+void user_mandelbulb_set(float power, int iter) {
+    g_mb_power = power;
+    g_mb_iter = iter;
+}
+
+float user_mandelbulb_sdf(float x, float y, float z) {
+    float zx = x, zy = y, zz = z;
+    float dr = 1.0f;
+    float r = sqrtf(zx * zx + zy * zy + zz * zz);
+    for (int i = 0; i < g_mb_iter; i++) {
+        if (r > 2.0f) break;
+        const float theta = ptm_acosf(fminf(fmaxf(zy / r, -1.0f), 1.0f)) * g_mb_power;
+        const float phi = ptm_atan2f(zz, zx) * g_mb_power;
+        dr = ptm_powf(r, g_mb_power - 1.0f) * g_mb_power * dr + 1.0f;
+        const float zr = ptm_powf(r, g_mb_power);
+        const float st = ptm_sinf(theta), ct = ptm_cosf(theta), sp = ptm_sinf(phi), cp = ptm_cosf(phi);
+        zx = zr * (st * cp) + x;
+        zy = zr * ct + y;
+        zz = zr * (st * sp) + z;
+        r = sqrtf(zx * zx + zy * zy + zz * zz);
+    }
+    return 0.5f * ptm_logf(r) * r / dr;
+}
+
+float user_mandelbulb_material(float x, float y, float z) {
+    const float f = x * x + y * y + z * z;
+    const float t = f / (0.8f + f);
+    return 0.0f * (1.0f - t) + 1.0f * t;
+}
+
+/* ---- generated scenes: Menger sponge with `levels` levels ---------------- */
+static int g_menger_levels = 3;
+
+void user_menger_set(int levels) { g_menger_levels = levels; }
+
+float user_menger_sdf(float x, float y, float z) {
+    float d = box(x, y, z, 1.0f, 1.0f, 1.0f);
+    float s = 1.0f;
+    for (int m = 0; m < g_menger_levels; m++) {
+        const float ax = glsl_mod(x * s, 2.0f) - 1.0f;
+        const float ay = glsl_mod(y * s, 2.0f) - 1.0f;
+        const float az = glsl_mod(z * s, 2.0f) - 1.0f;
+        s *= 3.0f;
+        const float hx = fabsf(1.0f - 3.0f * fabsf(ax));
+        const float hy = fabsf(1.0f - 3.0f * fabsf(ay));
+        const float hz = fabsf(1.0f - 3.0f * fabsf(az));
+        const float c = (fminf(fmaxf(hx, hy), fminf(fmaxf(hy, hz), fmaxf(hz, hx))) - 1.0f) / s;
+        d = fmaxf(d, c);
+    }
+    return d;
+}
+
+float user_menger_material(float x, float y, float z) {
+    (void)x;
+    (void)y;
+    (void)z;
+    return 2.0f;
+}

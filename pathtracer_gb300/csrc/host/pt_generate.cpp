@@ -13,6 +13,7 @@
 // material classes of a job mix map to Lambertian spectra of their own:
 // flat (sigma 1000) and inverted-bump respectively.
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <random>
@@ -146,12 +147,49 @@ void spheres_job(Rng& r, pt_scene& S, pt_job_spec& spec) {
                (float)r.range(0.4, 0.8), lmat, light);
 }
 
+// GLSL of a mandelbulb of any power (the spherical-coordinate form: r^n,
+// angles times n), `iter` iterations, bailout 2.
+std::string mandelbulb_glsl(double power, int iter) {
+    char pw[32];
+    std::snprintf(pw, sizeof pw, "%.2f", power);
+    return std::string("// Mandelbulb of power ") + pw + ", " + std::to_string(iter) +
+           " iterations (spherical coordinates).\n"
+           "const float POWER = " + pw + ";\n"
+           "float sdf(vec3 p)\n{\n"
+           "    vec3 z = p;\n    float dr = 1.0;\n    float r = length(z);\n"
+           "    for (int i = 0; i < " + std::to_string(iter) + "; i++) {\n"
+           "        if (r > 2.0) break;\n"
+           "        float theta = acos(clamp(z.y / r, -1.0, 1.0)) * POWER;\n"
+           "        float phi = atan(z.z, z.x) * POWER;\n"
+           "        dr = pow(r, POWER - 1.0) * POWER * dr + 1.0;\n"
+           "        float zr = pow(r, POWER);\n"
+           "        z = zr * vec3(sin(theta) * cos(phi), cos(theta), sin(theta) * sin(phi)) + p;\n"
+           "        r = length(z);\n    }\n"
+           "    return 0.5 * log(r) * r / dr;\n}\n"
+           "float sdfmaterial(vec3 p)\n{\n    float f = dot(p, p);\n    return mix(0.0, 1.0, f / (0.8 + f));\n}\n";
+}
+
+// GLSL of a Menger sponge with `levels` levels of holes (unit half-size).
+std::string menger_glsl(int levels) {
+    return "// Menger sponge, " + std::to_string(levels) + " levels.\n"
+           "float box(vec3 p, vec3 b)\n{\n    vec3 q = abs(p) - b;\n"
+           "    return length(max(q, 0.0)) + min(max(q.x, max(q.y, q.z)), 0.0);\n}\n"
+           "float sdf(vec3 p)\n{\n    float d = box(p, vec3(1.0));\n    float s = 1.0;\n"
+           "    for (int m = 0; m < " + std::to_string(levels) + "; m++) {\n"
+           "        vec3 a = mod(p * s, 2.0) - 1.0;\n        s *= 3.0;\n"
+           "        vec3 h = abs(1.0 - 3.0 * abs(a));\n"
+           "        float c = (min(max(h.x, h.y), min(max(h.y, h.z), max(h.z, h.x))) - 1.0) / s;\n"
+           "        d = max(d, c);\n    }\n    return d;\n}\n"
+           "float sdfmaterial(vec3 p)\n{\n    return 2.0;\n}\n";
+}
+
 // One SDF plug-in (mandelbulb, menger or blob, with its own material
 // constants) over a ground plane, under a sky sphere and a sun sphere, both
 // blackbody emitters; resolution uniform over {256, 512, 1024}^2; samples per
 // pixel open (refined until a target error), path length 8.  The plug-ins'
-// iteration counts and powers are those of the reference snippets.
-void sdf_job(Rng& r, pt_scene& S, pt_job_spec& spec) {
+// iteration counts and powers are those of the reference snippets, or with
+// `varied` drawn per job (GLSL text compiled at run time).
+void sdf_job(Rng& r, pt_scene& S, pt_job_spec& spec, bool varied) {
     static const int kRes[3] = {256, 512, 1024};
     const int res = kRes[r.below(3)];
     spec.width = spec.height = res;
@@ -170,11 +208,22 @@ void sdf_job(Rng& r, pt_scene& S, pt_job_spec& spec) {
             d.size[0] = d.size[1] = d.size[2] = 2.5f;
             d.pos[1] = 1.15f;
             d.source = "builtin:mandelbulb:0,1";
+            if (varied) {
+                const double power = r.range(4.0, 10.0);
+                d.source = mandelbulb_glsl(power, 4 + (int)r.below(3));
+                d.is_builtin_key = false;
+                spec.sdf_kind = PT_SDF_CUSTOM;
+            }
             break;
         case 1:
             spec.sdf_kind = PT_SDF_MENGER;
             d.size[0] = d.size[1] = d.size[2] = 2.0f;
             d.source = "builtin:menger:" + std::to_string(r.below(3));
+            if (varied) {
+                d.source = menger_glsl(3 + (int)r.below(3));
+                d.is_builtin_key = false;
+                spec.sdf_kind = PT_SDF_CUSTOM;
+            }
             break;
         default:
             spec.sdf_kind = PT_SDF_BLOB;
@@ -202,7 +251,8 @@ void sdf_job(Rng& r, pt_scene& S, pt_job_spec& spec) {
 extern "C" {
 
 int pt_scene_generate(int kind, uint64_t seed, pt_scene** out, pt_job_spec* spec) {
-    if (!out || !spec || (kind != PT_GEN_SPHERES && kind != PT_GEN_SDF)) return PT_ERR_INVALID;
+    if (!out || !spec || (kind != PT_GEN_SPHERES && kind != PT_GEN_SDF && kind != PT_GEN_SDF_VARIED))
+        return PT_ERR_INVALID;
     *out = nullptr;
     pt_scene* S = new (std::nothrow) pt_scene();
     if (!S) return PT_ERR_OOM;
@@ -214,7 +264,7 @@ int pt_scene_generate(int kind, uint64_t seed, pt_scene** out, pt_job_spec* spec
         if (kind == PT_GEN_SPHERES) {
             spheres_job(r, *S, *spec);
         } else {
-            sdf_job(r, *S, *spec);
+            sdf_job(r, *S, *spec, kind == PT_GEN_SDF_VARIED);
         }
     } catch (const std::bad_alloc&) {
         delete S;

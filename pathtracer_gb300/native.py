@@ -39,6 +39,7 @@ PT_BATCH_ROUTE_PERSISTENT = 2
 
 PT_GEN_SPHERES = 0
 PT_GEN_SDF = 1
+PT_GEN_SDF_VARIED = 2
 
 PT_SERVE_BATCHED = 0
 PT_SERVE_PLAIN = 1

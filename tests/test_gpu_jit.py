@@ -235,3 +235,32 @@ def test_server_serves_user_snippets_batched_and_plain(rt):
             assert [r.job_id for r in done] == [jid] and done[0].spp == 24
             out.append(s.read_image(jid))
     assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
+@pytest.mark.parametrize("kind", ["mandelbulb", "menger"])
+def test_generated_varied_scene_matches_oracle(rt, kind):
+    """A PT_GEN_SDF_VARIED job (its SDF as generated GLSL: a mandelbulb of a
+    drawn power, or a Menger sponge of drawn levels) through the wavefront
+    engine with the compiled march kernel, against the oracle with the C
+    restatement of that text."""
+    from oracle import compare
+    from pathtracer_gb300 import native
+    from user_snippets import generated_params, set_generated
+
+    for seed in range(2000, 2100):
+        sc, spec = rt["Scene"].generate(native.PT_GEN_SDF_VARIED, seed)
+        src = sc.sdf_sources()[0]
+        if generated_params(src) and generated_params(src)[0] == kind:
+            break
+    W, H, spf, depth = 48, 40, 2, 6
+    plugins = compare.plugins_for(sc, custom={src: set_generated(src)})
+    ubo = sc.pack_ubo(rt["cie"])
+    with rt["Context"](0) as ctx:
+        ctx.bind(sc, rt["cie"])
+        ctx.resize_accum(W, H)
+        push = sc.push_constants(W, H, spf, spf, spf, depth)
+        acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=depth)
+        acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
+    rep = compare.compare(acc_o, tr_o, acc_g, tr_g, spf)
+    print(kind, generated_params(src), rep)
+    assert compare.passes(rep), rep
