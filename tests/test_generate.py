@@ -94,3 +94,33 @@ def test_generate_rejects_unknown_kind(gen):
     native, renderer = gen
     with pytest.raises(renderer.PathTracerError):
         renderer.Scene.generate(7, 0)
+
+
+def test_varied_sdf_jobs(gen):
+    """PT_GEN_SDF_VARIED: the same scene for a seed, drawn mandelbulb powers
+    in [4, 10] with 4-6 iterations and Menger levels in {3, 4, 5}, as GLSL
+    the translator accepts; blobs stay the shipped plug-in."""
+    import re
+
+    from pathtracer_gb300 import Scene, glsl_translate, native
+
+    kinds = set()
+    for seed in range(3000, 3060):
+        a, spec = Scene.generate(native.PT_GEN_SDF_VARIED, seed)
+        b, _ = Scene.generate(native.PT_GEN_SDF_VARIED, seed)
+        assert a.to_json() == b.to_json()
+        src = a.sdf_sources()[0]
+        m = re.match(r"// Mandelbulb of power ([0-9.]+), ([0-9]+) iterations", src)
+        if m:
+            assert 4.0 <= float(m.group(1)) <= 10.0 and 4 <= int(m.group(2)) <= 6
+            assert spec.sdf_kind == native.PT_SDF_CUSTOM
+            kinds.add("mandelbulb")
+        elif src.startswith("// Menger sponge"):
+            assert int(re.match(r"// Menger sponge, ([0-9]+) levels", src).group(1)) in (3, 4, 5)
+            kinds.add("menger")
+        else:
+            assert src == "builtin:blob:0,1,2" and spec.sdf_kind == native.PT_SDF_BLOB
+            kinds.add("blob")
+        if spec.sdf_kind == native.PT_SDF_CUSTOM:
+            glsl_translate(src)
+    assert kinds == {"mandelbulb", "menger", "blob"}
