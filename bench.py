@@ -1,7 +1,10 @@
 #!/usr/bin/env python3
-"""Benchmark: path samples/s of the plain megakernel on the SDF-fractal scene
-(mandelbulb over a ground plane under a 5800 K sky dome, 1024x1024, 64 spp,
-max depth 6 — the reference-expressible form of the headline config).
+"""Benchmark: path samples/s on the SDF-fractal scene: a power-8 mandelbulb
+(12 iterations, bailout 2; scene GLSL compiled at run time) over a ground
+plane under a 5800 K sky dome, 1024x1024, 64 spp, max depth 6
+(pathtracer_gb300/scenes/mandelbulb12_plane.json).  --workload mandelbulb
+renders the same scene with the shipped mandelbulb snippet (4 iterations,
+bailout 16) instead.
 
 One step = one full render of the workload: 1024*1024*64 = 67.1 M camera
 paths (4 hero wavelengths each) in ceil(64/spf) dispatches, inputs resident on
@@ -57,8 +60,26 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SCENE = os.path.join(ROOT, "pathtracer_gb300", "scenes", "mandelbulb_plane.json")
-WORKLOAD = "mandelbulb_plane_1024x1024_64spp_depth6"
+# The single-scene workloads: scene file and workload name (at the default
+# 1024x1024, 64 spp, depth 6).
+RENDER_WORKLOADS = {
+    # power-8 mandelbulb, 12 iterations, bailout 2, as scene GLSL compiled at run time
+    "mandelbulb12": ("mandelbulb12_plane.json", "mandelbulb12_plane_1024x1024_64spp_depth6"),
+    # the shipped mandelbulb snippet (power 8, 4 iterations, bailout 16)
+    "mandelbulb": ("mandelbulb_plane.json", "mandelbulb_plane_1024x1024_64spp_depth6"),
+}
+
+
+def scene_path(workload):
+    return os.path.join(ROOT, "pathtracer_gb300", "scenes", RENDER_WORKLOADS[workload][0])
+
+
+def workload_name(args):
+    name = RENDER_WORKLOADS[args.workload][1]
+    if (args.res, args.spp, args.depth) != (1024, 64, 6):
+        name = name.replace("1024x1024_64spp_depth6", f"{args.res}x{args.res}_{args.spp}spp_depth{args.depth}")
+    return name
+
 METRIC = "path_samples_per_s"
 UNIT = "path samples/s"
 
@@ -84,7 +105,8 @@ def parse_args():
     ap.add_argument("--inner", type=int, default=0, help="wavefront SDF evaluations per march lane between refills (0: default)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
-    ap.add_argument("--workload", default="mandelbulb", choices=["mandelbulb", "batch64", "serve", "progressive"])
+    ap.add_argument("--workload", default="mandelbulb12",
+                    choices=["mandelbulb12", "mandelbulb", "batch64", "serve", "progressive"])
     ap.add_argument("--pass-spp", type=int, default=16, help="progressive: samples per pixel per pass")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: Poisson arrivals per second")
     ap.add_argument("--duration", type=float, default=30.0, help="serve: seconds of arrivals")
@@ -233,7 +255,7 @@ def cpu_baseline(args, W, H, spf_total, nthreads):
     from oracle import compare
     from pathtracer_gb300 import Scene, cie_analytic
 
-    scene = Scene.load(SCENE)
+    scene = Scene.load(scene_path(args.workload))
     cie = cie_analytic()
     ubo = scene.pack_ubo(cie)
     plugins = compare.plugins_for(scene)
@@ -269,7 +291,7 @@ def run_reference(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * samples / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": WORKLOAD, "resolution": [W, H], "spp": args.spp, "max_depth": args.depth},
+        "config": {"workload": workload_name(args), "resolution": [W, H], "spp": args.spp, "max_depth": args.depth},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -754,7 +776,9 @@ def main():
     spf = min(args.spf, args.spp)
     ndisp = (args.spp + spf - 1) // spf
     samples_per_step = W * H * spf * ndisp
-    scene = Scene.load(SCENE)
+    scene = Scene.load(scene_path(args.workload))
+    workload = workload_name(args)
+    work_fixture = RENDER_WORKLOADS[args.workload][1]  # counts per sample, measured at the default size
     cie = cie_analytic()
     ctx = Context(local)
     engine_id = native.PT_ENGINE_WAVEFRONT if args.engine == "wavefront" else native.PT_ENGINE_MEGAKERNEL
@@ -858,13 +882,13 @@ def main():
 
     peaks, peak_kind = measured_peaks()
     if args.engine == "wavefront":
-        captured = (W, H, args.spp, spf, args.depth) == (1024, 1024, 64, 64, 6) and ctx.tuning() == DEFAULT_TUNING
+        captured = spf == 64 and ctx.tuning() == DEFAULT_TUNING
         roofline, stages, ops = stage_roofline(ctx, lambda: one_step(args.warmup + args.steps + 5), samples_per_step,
-                                               WORKLOAD, peaks, peak_kind, WORKLOAD if captured else None)
+                                               work_fixture, peaks, peak_kind, workload if captured else None)
     else:
         from pathtracer_gb300 import workmodel
 
-        ops = workmodel.fp32_ops_per_sample(workmodel.load(WORKLOAD)["per_sample"])
+        ops = workmodel.fp32_ops_per_sample(workmodel.load(work_fixture)["per_sample"])
         peak = fp32_peak_tflops(peaks)
         ach = ops["total"] * samples_per_step / (ms_step / 1000.0) / 1e12
         roofline = {"bound": "fp32", "kernel": "megakernel", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
@@ -874,7 +898,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "resolution": [W, H], "spp": args.spp, "max_depth": args.depth,
+        "config": {"workload": workload, "resolution": [W, H], "spp": args.spp, "max_depth": args.depth,
                    "samples_per_dispatch": spf, "dispatches_per_step": ndisp,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "wavefront_tuning": ctx.tuning() if args.engine == "wavefront" else None,

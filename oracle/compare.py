@@ -28,17 +28,19 @@ PATH_MATCH_MIN = 0.999
 
 def plugins_for(scene, custom: dict | None = None) -> list:
     """The oracle's plug-in per SDF of the scene.  Text that is not one of the
-    shipped snippets needs an entry in `custom` (source text -> the names of
-    its C restatement's sdf and material functions in user_sdfs.c), which is
-    registered for that slot as PT_SDF_CUSTOM."""
+    shipped snippets is registered for its slot as PT_SDF_CUSTOM with its C
+    restatement in user_sdfs.c: from `custom` (source text -> the names of
+    its sdf and material functions) or, for the texts of the repository's
+    scenes and generator, oracle.restatement_for."""
     out = []
     for slot, src in enumerate(scene.sdf_sources()):
         p = native.PtSdfPlugin()
         rc = native.cuda().pt_parse_sdf_source(src.encode(), ctypes.byref(p))
         if rc != native.PT_OK:
-            if not custom or src not in custom:
+            names = custom[src] if custom and src in custom else oracle.restatement_for(src)
+            if names is None:
                 raise ValueError(f"unsupported SDF source: {src[:60]!r}")
-            oracle.set_user_sdf(slot, *custom[src])
+            oracle.set_user_sdf(slot, *names)
             p = native.plugin(native.PT_SDF_CUSTOM)
         out.append(p)
     return out

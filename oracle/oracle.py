@@ -157,7 +157,9 @@ def mathf(fn: str, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
 
 COUNTERS = ["samples", "path_rays", "shadow_rays", "sphere", "plane", "bounding_sphere", "box", "lens_slice",
             "cyclide", "aabb", "march_steps", "sdf_blob", "sdf_mandelbulb", "mandelbulb_iters", "sdf_menger",
-            "sdf_terrain", "sdf_material", "emit", "brdf", "surface_hits"]
+            "sdf_terrain", "sdf_material", "emit", "brdf", "surface_hits", "sdf_custom"]
+# Loop iterations inside the C restatements of GLSL snippets (user_sdfs.c).
+USER_COUNTERS = ["bulb8_iters", "user_mandelbulb_iters"]
 
 
 def count_work(ubo: np.ndarray, push, plugins: list, rect=None, nthreads: int = 0) -> dict:
@@ -170,8 +172,60 @@ def count_work(ubo: np.ndarray, push, plugins: list, rect=None, nthreads: int = 
 
     arr = (PtSdfPlugin * max(1, len(plugins)))(*plugins)
     accum = np.zeros((H, W, 4), np.float32)
-    rc = lib().pto_dispatch(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins),
-                            accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr), nthreads)
+    user = user_sdfs()
+    user.user_count(1)
+    try:
+        rc = lib().pto_dispatch(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins),
+                                accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr), nthreads)
+        ucnt = list((ctypes.c_uint64 * len(USER_COUNTERS)).in_dll(user, "user_counters"))
+    finally:
+        user.user_count(0)
     if rc != 0:
         raise RuntimeError(f"pto_dispatch failed: {rc}")
-    return {k: int(v) for k, v in zip(COUNTERS, cnt)}
+    out = {k: int(v) for k, v in zip(COUNTERS, cnt)}
+    out.update({k: int(v) for k, v in zip(USER_COUNTERS, ucnt)})
+    return out
+
+
+def generated_params(text: str):
+    """(kind, parameters) of an SDF text pt_scene_generate writes for
+    PT_GEN_SDF_VARIED, read from its first line, or None for other text."""
+    import re
+
+    m = re.match(r"// Mandelbulb of power ([0-9.]+), ([0-9]+) iterations", text)
+    if m:
+        return "mandelbulb", (float(m.group(1)), int(m.group(2)))
+    m = re.match(r"// Menger sponge, ([0-9]+) levels", text)
+    if m:
+        return "menger", (int(m.group(1)),)
+    return None
+
+
+def set_generated(text: str):
+    """Points the restatement of a generated snippet at its parameters;
+    returns the names of its sdf and sdfmaterial functions."""
+    kind, prm = generated_params(text)
+    u = user_sdfs()
+    if kind == "mandelbulb":
+        u.user_mandelbulb_set.argtypes = [ctypes.c_float, ctypes.c_int]
+        u.user_mandelbulb_set(float(np.float32(prm[0])), prm[1])
+        return "user_mandelbulb_sdf", "user_mandelbulb_material"
+    u.user_menger_set.argtypes = [ctypes.c_int]
+    u.user_menger_set(prm[0])
+    return "user_menger_sdf", "user_menger_material"
+
+
+# First line of the SDF text of pathtracer_gb300/scenes/mandelbulb12_plane.json.
+BULB8_HEADER = "// Mandelbulb of power 8 in Chebyshev form, 12 iterations, bailout 2."
+
+
+def restatement_for(text: str):
+    """(sdf, sdfmaterial) names in user_sdfs.c of the C restatement of a
+    scene's GLSL text that the repository's scenes and generator write
+    (the generated mandelbulbs and sponges with their parameters set), or
+    None for other text."""
+    if text.startswith(BULB8_HEADER):
+        return "user_bulb8_sdf", "user_bulb8_material"
+    if generated_params(text) is not None:
+        return set_generated(text)
+    return None

@@ -666,6 +666,17 @@ static float plugin_material(const pt_sdf_plugin* pl, int slot, vec3 p) {
     }
 }
 
+/* The work counter of one plug-in evaluation, by kind. */
+static int sdf_counter(int kind) {
+    switch (kind) {
+        case PT_SDF_BLOB: return PTO_C_SDF_BLOB;
+        case PT_SDF_MANDELBULB: return PTO_C_SDF_MANDELBULB;
+        case PT_SDF_MENGER: return PTO_C_SDF_MENGER;
+        case PT_SDF_TERRAIN: return PTO_C_SDF_TERRAIN;
+        default: return PTO_C_SDF_CUSTOM;
+    }
+}
+
 static inline vec3 sdf_pos(const ctx_t* c, int i) { return mk3(SDFS(c, 6 * i), SDFS(c, 6 * i + 1), SDFS(c, 6 * i + 2)); }
 
 /* SC:706-711 with the code InsertSDF splices in (src/pathtracer.cpp:2004-2054):
@@ -676,7 +687,7 @@ static float SDF(const ctx_t* c, vec3 p, uint32_t set1) {
     for (int i = 0; i < n; i++) {
         uint32_t code = 1u << i;
         if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
-            if (c->cnt) c->cnt[PTO_C_SDF_BLOB + (c->plug[i].kind == PT_SDF_BLOB ? 0 : c->plug[i].kind == PT_SDF_MANDELBULB ? 1 : c->plug[i].kind == PT_SDF_MENGER ? 3 : 4)]++;
+            COUNT(c, sdf_counter(c->plug[i].kind));
             sdf = fminf(sdf, plugin_sdf(&c->plug[i], i, sub3(p, sdf_pos(c, i))));
         }
     }
@@ -692,7 +703,7 @@ static float SDFMATERIAL(const ctx_t* c, vec3 p, uint32_t set1) {
         uint32_t code = 1u << i;
         if ((set1 & code) == code && c->plug[i].kind != PT_SDF_NONE) {
             vec3 q = sub3(p, sdf_pos(c, i));
-            if (c->cnt) c->cnt[PTO_C_SDF_BLOB + (c->plug[i].kind == PT_SDF_BLOB ? 0 : c->plug[i].kind == PT_SDF_MANDELBULB ? 1 : c->plug[i].kind == PT_SDF_MENGER ? 3 : 4)]++;
+            COUNT(c, sdf_counter(c->plug[i].kind));
             float di = plugin_sdf(&c->plug[i], i, q);
             if (!(sdf < di)) COUNT(c, PTO_C_SDF_MATERIAL);
             mat = (sdf < di) ? mat : plugin_material(&c->plug[i], i, q);

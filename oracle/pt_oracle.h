@@ -54,6 +54,7 @@ enum {
     PTO_C_EMIT,              /* Emit (4 wavelengths) */
     PTO_C_BRDF,              /* EvaluateBRDF (4 wavelengths) */
     PTO_C_SURFACE_HITS,      /* non-emissive hits: BRDF sampling + light sampling */
+    PTO_C_SDF_CUSTOM,        /* evaluations of other GLSL text (PT_SDF_CUSTOM slots) */
     PTO_C_COUNT
 };
 

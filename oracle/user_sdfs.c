@@ -12,8 +12,25 @@
  * and the transcendentals through the shared pt_mathf routines (tan as sin / cos
  * of one reduction). */
 #include <math.h>
+#include <stdint.h>
 
 #include "../include/pt_mathf.h"
+
+/* Work counters of the restatements below (loop iterations by snippet),
+ * summed over all threads while counting is on; the work model of a
+ * workload reads them beside the oracle's own counters. */
+enum { USER_C_BULB8_ITERS = 0, USER_C_MANDELBULB_ITERS, USER_C_COUNT };
+uint64_t user_counters[USER_C_COUNT];
+static int g_counting;
+
+void user_count(int on) {
+    g_counting = on;
+    for (int k = 0; k < USER_C_COUNT; k++) user_counters[k] = 0;
+}
+
+static void user_add(int k, int n) {
+    if (g_counting) __atomic_fetch_add(&user_counters[k], (uint64_t)n, __ATOMIC_RELAXED);
+}
 
 /* ---- "twisted torus": torus (R 0.8, r 0.25) with a sin ripple ---------- */
 static float torus(float px, float py, float pz, float tx, float ty, float* ring) {
@@ -79,6 +96,53 @@ float user_spiral_material(float x, float y, float z) {
     return roundf(ptm_atanf(x) + 2.0f);
 }
 
+/* ---- "bulb8": power-8 mandelbulb, 12 iterations, bailout 2 ------------
+ * The SDF of pathtracer_gb300/scenes/mandelbulb12_plane.json: z -> z^8 + p
+ * in spherical form with the 8-fold angles from Chebyshev polynomials of the
+ * cosines (cos 8a = T8(cos a), sin 8a = sin a * U7(cos a)). */
+typedef struct {
+    float t8, u7;
+} cheb8_t;
+
+static cheb8_t cheb8(float c) {
+    const float c2 = c * c;
+    cheb8_t o;
+    o.t8 = PTM_FMA(PTM_FMA(PTM_FMA(PTM_FMA(128.0f, c2, -256.0f), c2, 160.0f), c2, -32.0f), c2, 1.0f);
+    o.u7 = PTM_FMA(PTM_FMA(PTM_FMA(128.0f, c2, -192.0f), c2, 80.0f), c2, -8.0f) * c;
+    return o;
+}
+
+float user_bulb8_sdf(float x, float y, float z) {
+    float zx = x, zy = y, zz = z;
+    float r = sqrtf(zx * zx + zy * zy + zz * zz);
+    float dr = 1.0f;
+    int i;
+    for (i = 0; i < 12; i++) {
+        if (r > 2.0f) break;
+        const float r2 = r * r;
+        const float r4 = r2 * r2;
+        dr = 8.0f * (r4 * r2 * r) * dr + 1.0f;
+        const float l = sqrtf(zx * zx + zz * zz);
+        const cheb8_t a = cheb8(zz / l);
+        const cheb8_t b = cheb8(zy / r);
+        const float st8 = a.u7 * (zx / l);
+        const float sp8 = b.u7 * (l / r);
+        const float r8 = r4 * r4;
+        zx = r8 * (st8 * sp8) + x;
+        zy = r8 * b.t8 + y;
+        zz = r8 * (a.t8 * sp8) + z;
+        r = sqrtf(zx * zx + zy * zy + zz * zz);
+    }
+    user_add(USER_C_BULB8_ITERS, i);
+    return 0.5f * ptm_logf(r) * r / dr;
+}
+
+float user_bulb8_material(float x, float y, float z) {
+    const float f = x * x + y * y + z * z;
+    const float t = f / (0.8f + f);
+    return 4.0f * (1.0f - t) + 3.0f * t;
+}
+
 /* ---- generated scenes (PT_GEN_SDF_VARIED): mandelbulb of any power ------
  * The text pt_scene_generate writes for a mandelbulb of power `power` and
  * `iter` iterations; the parameters are set with user_mandelbulb_set. */
@@ -94,7 +158,8 @@ float user_mandelbulb_sdf(float x, float y, float z) {
     float zx = x, zy = y, zz = z;
     float dr = 1.0f;
     float r = sqrtf(zx * zx + zy * zy + zz * zz);
-    for (int i = 0; i < g_mb_iter; i++) {
+    int i;
+    for (i = 0; i < g_mb_iter; i++) {
         if (r > 2.0f) break;
         const float theta = ptm_acosf(fminf(fmaxf(zy / r, -1.0f), 1.0f)) * g_mb_power;
         const float phi = ptm_atan2f(zz, zx) * g_mb_power;
@@ -106,6 +171,7 @@ float user_mandelbulb_sdf(float x, float y, float z) {
         zz = zr * (st * sp) + z;
         r = sqrtf(zx * zx + zy * zy + zz * zz);
     }
+    user_add(USER_C_MANDELBULB_ITERS, i);
     return 0.5f * ptm_logf(r) * r / dr;
 }
 

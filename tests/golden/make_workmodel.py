@@ -36,6 +36,8 @@ def main():
     out = {}
     scene = Scene.load(os.path.join(ROOT, "pathtracer_gb300", "scenes", "mandelbulb_plane.json"))
     out["mandelbulb_plane_1024x1024_64spp_depth6"] = per_sample(scene, 1024, 1024, 64, 6)
+    scene = Scene.load(os.path.join(ROOT, "pathtracer_gb300", "scenes", "mandelbulb12_plane.json"))
+    out["mandelbulb12_plane_1024x1024_64spp_depth6"] = per_sample(scene, 1024, 1024, 64, 6)
     # The mixed-job batch: the first 8 generated sphere jobs, 1 row each, weighted by their samples.
     tot, n = {}, 0
     for seed in range(8):

@@ -182,3 +182,33 @@ def test_generated_snippets_match_their_c_restatement(pt):
             bad = sum(_bits(fs(*map(float, p))) != _bits(rs(*map(float, p))) for p in pts)
             bad += sum(_bits(fm(*map(float, p))) != _bits(rm(*map(float, p))) for p in pts)
             assert bad == 0, (kind, generated_params(src), bad)
+
+
+def test_scene_snippet_matches_its_c_restatement(pt):
+    """The power-8, 12-iteration mandelbulb of scenes/mandelbulb12_plane.json,
+    translated and built for the CPU, agrees bit for bit with the oracle's
+    restatement; near the surface most points run many iterations."""
+    import os
+
+    from conftest import SCENES
+    from oracle import oracle
+    from pathtracer_gb300 import Scene
+
+    src = Scene.load(os.path.join(SCENES, "mandelbulb12_plane.json")).sdf_sources()[0]
+    assert oracle.restatement_for(src) == ("user_bulb8_sdf", "user_bulb8_material")
+    lib = _cpu_build(pt, "bulb8", {"b": src})
+    fs, fm = _fn(lib, "c_b_sdf"), _fn(lib, "c_b_mat")
+    rs, rm = oracle.user_fn("user_bulb8_sdf"), oracle.user_fn("user_bulb8_material")
+    pts = _points(n=6000, scale=1.2)
+    bad = sum(_bits(fs(*map(float, p))) != _bits(rs(*map(float, p))) for p in pts)
+    bad += sum(_bits(fm(*map(float, p))) != _bits(rm(*map(float, p))) for p in pts)
+    assert bad == 0, bad
+    u = oracle.user_sdfs()
+    u.user_count(1)
+    for p in pts[:1000]:
+        rs(*map(float, p))
+    import ctypes
+
+    iters = (ctypes.c_uint64 * len(oracle.USER_COUNTERS)).in_dll(u, "user_counters")[0]
+    u.user_count(0)
+    assert 1000 < iters < 12 * 1000

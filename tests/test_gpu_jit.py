@@ -264,3 +264,29 @@ def test_generated_varied_scene_matches_oracle(rt, kind):
     rep = compare.compare(acc_o, tr_o, acc_g, tr_g, spf)
     print(kind, generated_params(src), rep)
     assert compare.passes(rep), rep
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+def test_headline_bulb_scene_matches_oracle(rt, engine):
+    """The bench's default scene (scenes/mandelbulb12_plane.json: a power-8
+    mandelbulb of 12 iterations, bailout 2, as scene GLSL) at 96x96, 4 spp,
+    depth 6, traced per path, through the compiled megakernel (engine 0) and
+    the wavefront engine's compiled march kernel (engine 1), against the
+    oracle with the C restatement of that text."""
+    from oracle import compare
+
+    W, H, spf, depth = 96, 96, 4, 6
+    scene = rt["Scene"].load(os.path.join(SCENES, "mandelbulb12_plane.json"))
+    ubo = scene.pack_ubo(rt["cie"])
+    plugins = compare.plugins_for(scene)
+    with rt["Context"](0) as ctx:
+        ctx.set_engine(engine)
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        push = scene.push_constants(W, H, spf, spf, spf, depth)
+        acc_o, tr_o = compare.run_oracle(ubo, push, plugins, trace_depth=depth)
+        acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=depth)
+    rep = compare.compare(acc_o, tr_o, acc_g, tr_g, spf)
+    print(rep)
+    assert compare.passes(rep), rep
+    assert np.isfinite(acc_g).all() and acc_g[..., :3].max() > 0

@@ -82,34 +82,14 @@ SNIPPETS = {
 
 
 def generated_params(text: str):
-    """(kind, parameters) of an SDF text pt_scene_generate wrote for
-    PT_GEN_SDF_VARIED, read from its first line, or None for other text."""
-    import re
+    """(kind, parameters) of a text pt_scene_generate wrote (oracle.generated_params)."""
+    from oracle import oracle
 
-    m = re.match(r"// Mandelbulb of power ([0-9.]+), ([0-9]+) iterations", text)
-    if m:
-        return "mandelbulb", (float(m.group(1)), int(m.group(2)))
-    m = re.match(r"// Menger sponge, ([0-9]+) levels", text)
-    if m:
-        return "menger", (int(m.group(1)),)
-    return None
+    return oracle.generated_params(text)
 
 
 def set_generated(text: str):
-    """Points the oracle's restatement of a generated snippet at its
-    parameters; returns the names of its sdf and sdfmaterial functions."""
-    import ctypes
-
-    import numpy as np
-
+    """Sets the restatement of a generated snippet (oracle.set_generated)."""
     from oracle import oracle
 
-    kind, prm = generated_params(text)
-    lib = oracle.user_sdfs()
-    if kind == "mandelbulb":
-        lib.user_mandelbulb_set.argtypes = [ctypes.c_float, ctypes.c_int]
-        lib.user_mandelbulb_set(float(np.float32(prm[0])), prm[1])
-        return "user_mandelbulb_sdf", "user_mandelbulb_material"
-    lib.user_menger_set.argtypes = [ctypes.c_int]
-    lib.user_menger_set(prm[0])
-    return "user_menger_sdf", "user_menger_material"
+    return oracle.set_generated(text)
