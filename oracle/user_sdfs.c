@@ -123,10 +123,12 @@ float user_bulb8_sdf(float x, float y, float z) {
         const float r4 = r2 * r2;
         dr = 8.0f * (r4 * r2 * r) * dr + 1.0f;
         const float l = sqrtf(zx * zx + zz * zz);
-        const cheb8_t a = cheb8(zz / l);
-        const cheb8_t b = cheb8(zy / r);
-        const float st8 = a.u7 * (zx / l);
-        const float sp8 = b.u7 * (l / r);
+        const float il = 1.0f / l;
+        const float ir = 1.0f / r;
+        const cheb8_t a = cheb8(zz * il);
+        const cheb8_t b = cheb8(zy * ir);
+        const float st8 = a.u7 * (zx * il);
+        const float sp8 = b.u7 * (l * ir);
         const float r8 = r4 * r4;
         zx = r8 * (st8 * sp8) + x;
         zy = r8 * b.t8 + y;
