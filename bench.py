@@ -103,7 +103,6 @@ def parse_args():
     ap.add_argument("--drain", type=int, default=-1, help="wavefront march drain lanes (-1: default)")
     ap.add_argument("--blocks", type=int, default=0, help="wavefront stage blocks per SM (0: default)")
     ap.add_argument("--inner", type=int, default=0, help="wavefront SDF evaluations per march lane between refills (0: default)")
-    ap.add_argument("--regroup", type=int, default=-1, help="wavefront march blocks sort rays by SDF distance (0/1; -1: default)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
     ap.add_argument("--workload", default="mandelbulb12",
@@ -206,7 +205,7 @@ def fp32_peak_tflops(peaks):
 MARCH_TRAFFIC_BYTES = {"mandelbulb_plane_1024x1024_64spp_depth6": 75.10e6}
 # The wavefront knobs that capture ran with (the library defaults).
 DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
-                  "march_inner": 6, "march_regroup": 0}
+                  "march_inner": 6}
 
 
 def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, traffic_key=None):
@@ -790,8 +789,6 @@ def main():
         ctx.set_march_budget(args.budget)
     knobs = {k: v for k, v in (("refill_min", args.refill), ("blocks_per_sm", args.blocks),
                                ("march_inner", args.inner)) if v}
-    if args.regroup >= 0:
-        knobs["march_regroup"] = args.regroup
     if args.drain >= 0:
         knobs["drain_lanes"] = args.drain
     if knobs:

@@ -273,8 +273,6 @@ typedef struct pt_wavefront_tuning {
     int32_t drain_lanes;   /* a march warp left with fewer rays after its queue drained suspends them (0..32) */
     int32_t blocks_per_sm; /* stage-kernel blocks of 256 threads per SM (1..8) */
     int32_t march_inner;   /* SDF evaluations per march lane between the warp's refills (1..16; default 6) */
-    int32_t march_regroup; /* 1: each march block sorts its rays by SDF distance before every round of
-                              march_inner evaluations, so warps run escape-time loops of like length (0..1) */
 } pt_wavefront_tuning;
 int pt_get_wavefront_tuning(pt_ctx* ctx, pt_wavefront_tuning* out);
 int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* tuning);

@@ -117,27 +117,6 @@ PT_DI void stage_flush(uint32_t* buf, uint32_t count, uint32_t* queue, uint32_t*
     if ((uint32_t)lane < count) queue[b + (uint32_t)lane] = buf[lane];
 }
 
-// Block-wide regroup of the march lanes (WfArgs::march_regroup): before each
-// round of A.march_inner evaluations the block's 256 rays are sorted by a
-// bucket of their last SDF distance, so a warp holds rays at a like distance
-// from the surface.  An escape-time fractal iterates longer the closer the
-// point, and a warp runs its SDF loop as long as its slowest lane: grouping
-// near rays with near ones and far with far shortens the idle lane time.
-// Empty lanes sort last, which also packs the live rays into full warps.
-// The state moves through dynamic shared memory (kRegroupWords words per
-// lane, structure of arrays); results do not depend on which lane a ray is on.
-constexpr int kRegroupWords = 24;
-constexpr int kRegroupBuckets = 8;
-constexpr int kStageWarps = kStageThreads / 32;
-
-PT_DI int regroup_bucket(int phase, float prevR) {
-    if (phase == MP_EMPTY) return kRegroupBuckets - 1;
-    if (phase >= MP_NORMAL0) return 0;  // normal probes sit on the surface
-    const float a = fabsf(prevR);
-    if (phase == MP_SIGN || !(a > 0.0f)) return kRegroupBuckets - 2;  // no step taken yet
-    return a < 1e-3f ? 1 : a < 1e-2f ? 2 : a < 3e-2f ? 3 : a < 0.1f ? 4 : a < 0.3f ? 5 : 6;
-}
-
 __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
     WfCounters& C = *A.counters;
     const uint32_t cur = C.cur;
@@ -175,10 +154,6 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
     int hit_sel = -2;  // >= -1 once the lane's march converged (scene_sdf_material_hit)
     bool shadow_ray = false;
     const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
-
-    const bool regroup = A.march_regroup != 0;
-    extern __shared__ uint32_t rg_state[];  // [kRegroupWords][kStageThreads] when regrouping
-    __shared__ uint32_t rg_count[kStageWarps][kRegroupBuckets], rg_off[kStageWarps][kRegroupBuckets];
 
     for (;;) {
         // Refill lanes that have no ray (warp-aggregated fetch), once at
@@ -238,93 +213,8 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
                 }
             }
         }
-        if (regroup) {
-            // Every warp of the block takes part until the block has no ray left.
-            if (!__syncthreads_or(phase != MP_EMPTY)) break;
-            const int key = regroup_bucket(phase, prevR);
-            uint32_t rank = 0;
-#pragma unroll
-            for (int b = 0; b < kRegroupBuckets; b++) {
-                const unsigned m = __ballot_sync(0xffffffffu, key == b);
-                if (key == b) rank = (uint32_t)__popc(m & ((1u << lane) - 1u));
-                if (lane == b) rg_count[wib][b] = (uint32_t)__popc(m);
-            }
-            __syncthreads();
-            if (threadIdx.x < kStageWarps * kRegroupBuckets) {
-                // Start of (warp w, bucket b): all rays of lower buckets, then
-                // bucket b's rays of lower warps.
-                const int w = (int)threadIdx.x / kRegroupBuckets, b = (int)threadIdx.x % kRegroupBuckets;
-                uint32_t off = 0;
-                for (int b2 = 0; b2 < b; b2++)
-                    for (int w2 = 0; w2 < kStageWarps; w2++) off += rg_count[w2][b2];
-                for (int w2 = 0; w2 < w; w2++) off += rg_count[w2][b];
-                rg_off[w][b] = off;
-            }
-            __syncthreads();
-            const uint32_t dst = rg_off[wib][key] + rank;
-            const uint64_t sp = reinterpret_cast<uint64_t>(Sp);
-            uint32_t* col = rg_state + dst;
-            col[0 * kStageThreads] = slot;
-            col[1 * kStageThreads] = (uint32_t)sp;
-            col[2 * kStageThreads] = (uint32_t)(sp >> 32);
-            col[3 * kStageThreads] = __float_as_uint(org.x);
-            col[4 * kStageThreads] = __float_as_uint(org.y);
-            col[5 * kStageThreads] = __float_as_uint(org.z);
-            col[6 * kStageThreads] = __float_as_uint(dir.x);
-            col[7 * kStageThreads] = __float_as_uint(dir.y);
-            col[8 * kStageThreads] = __float_as_uint(dir.z);
-            col[9 * kStageThreads] = __float_as_uint(t);
-            col[10 * kStageThreads] = __float_as_uint(insT);
-            col[11 * kStageThreads] = __float_as_uint(omega);
-            col[12 * kStageThreads] = __float_as_uint(prevR);
-            col[13 * kStageThreads] = __float_as_uint(hitdist);
-            col[14 * kStageThreads] = __float_as_uint(k);
-            col[15 * kStageThreads] = __float_as_uint(nplus);
-            col[16 * kStageThreads] = __float_as_uint(nv.x);
-            col[17 * kStageThreads] = __float_as_uint(nv.y);
-            col[18 * kStageThreads] = __float_as_uint(nv.z);
-            col[19 * kStageThreads] = __float_as_uint(tmm.x);
-            col[20 * kStageThreads] = __float_as_uint(tmm.y);
-            col[21 * kStageThreads] = set1;
-            // phase < 16, hit_sel + 2 < 64, steps <= 512 < 2048
-            col[22 * kStageThreads] = (uint32_t)phase | ((uint32_t)shadow_ray << 4) | ((uint32_t)(hit_sel + 2) << 5) |
-                                      ((uint32_t)steps << 11);
-            // iter < 512, points < 65536 (reset or a re-search every other step)
-            col[23 * kStageThreads] = (uint32_t)iter | ((uint32_t)min(points, 0xffff) << 10);
-            __syncthreads();
-            const uint32_t* mine = rg_state + threadIdx.x;
-            slot = mine[0 * kStageThreads];
-            Sp = reinterpret_cast<const KScene*>((uint64_t)mine[1 * kStageThreads] |
-                                                 ((uint64_t)mine[2 * kStageThreads] << 32));
-            org = f3(__uint_as_float(mine[3 * kStageThreads]), __uint_as_float(mine[4 * kStageThreads]),
-                     __uint_as_float(mine[5 * kStageThreads]));
-            dir = f3(__uint_as_float(mine[6 * kStageThreads]), __uint_as_float(mine[7 * kStageThreads]),
-                     __uint_as_float(mine[8 * kStageThreads]));
-            t = __uint_as_float(mine[9 * kStageThreads]);
-            insT = __uint_as_float(mine[10 * kStageThreads]);
-            omega = __uint_as_float(mine[11 * kStageThreads]);
-            prevR = __uint_as_float(mine[12 * kStageThreads]);
-            hitdist = __uint_as_float(mine[13 * kStageThreads]);
-            k = __uint_as_float(mine[14 * kStageThreads]);
-            nplus = __uint_as_float(mine[15 * kStageThreads]);
-            nv = f3(__uint_as_float(mine[16 * kStageThreads]), __uint_as_float(mine[17 * kStageThreads]),
-                    __uint_as_float(mine[18 * kStageThreads]));
-            tmm = make_float2(__uint_as_float(mine[19 * kStageThreads]), __uint_as_float(mine[20 * kStageThreads]));
-            set1 = mine[21 * kStageThreads];
-            const uint32_t w22 = mine[22 * kStageThreads], w23 = mine[23 * kStageThreads];
-            phase = (int)(w22 & 15u);
-            shadow_ray = ((w22 >> 4) & 1u) != 0;
-            hit_sel = (int)((w22 >> 5) & 63u) - 2;
-            steps = (int)(w22 >> 11);
-            iter = (int)(w23 & 1023u);
-            points = (int)(w23 >> 10);
-            p = fma3s(dir, t, org);  // every phase keeps p at the ray's current t
-        }
         const unsigned live = __ballot_sync(0xffffffffu, phase != MP_EMPTY);
-        if (live == 0) {
-            if (regroup) continue;  // the block still has rays: stay for its regroups
-            break;
-        }
+        if (live == 0) break;
         // Once the queue is drained, a warp with few rays left would run on
         // with most lanes idle: its marching rays save their state and
         // continue in full warps next iteration instead.

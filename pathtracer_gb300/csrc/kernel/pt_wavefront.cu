@@ -558,15 +558,12 @@ cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid
     // isect interval stays empty.)
     if (stage_events) cudaEventRecord(stage_events[0], stream);
     if (stage_events) cudaEventRecord(stage_events[1], stream);
-    // the regrouping march keeps its blocks' ray state in dynamic shared memory
-    const size_t march_smem = a->march_regroup ? (size_t)kRegroupWords * kStageThreads * sizeof(uint32_t) : 0;
     if (march_kernel) {
         void* argv[] = {const_cast<WfArgs*>(a)};
-        const cudaError_t e =
-            cudaLaunchKernel(march_kernel, dim3(grid), dim3(kStageThreads), argv, march_smem, stream);
+        const cudaError_t e = cudaLaunchKernel(march_kernel, dim3(grid), dim3(kStageThreads), argv, 0, stream);
         if (e != cudaSuccess) return e;
     } else {
-        wf_march<<<grid, kStageThreads, march_smem, stream>>>(*a);
+        wf_march<<<grid, kStageThreads, 0, stream>>>(*a);
     }
     if (stage_events) cudaEventRecord(stage_events[2], stream);
     static int shade_cap[2] = {0, 0}, gen_cap = 0;

@@ -76,7 +76,6 @@ struct WfArgs {
     int refill_min;    // idle lanes a march warp gathers before it refills them at once
     int drain_lanes;   // a drained march warp with fewer rays suspends them (0: never)
     int march_inner;   // SDF evaluations per lane between a march warp's refills and queue appends
-    int march_regroup;  // 1: march blocks sort their rays by SDF distance before each round of evaluations
     int persist_refill;  // idle lanes a persistent warp gathers before starting new samples together
 };
 

@@ -44,7 +44,6 @@ struct pt_ctx {
     int refill_min = 2;    // measured best on GB300 (mandelbulb 1024x1024)
     int drain_lanes = 24;
     int march_inner = 6;
-    int march_regroup = 0;
     int blocks_per_sm = 4;
     KScene* d_scene = nullptr;     // device copy for the wavefront kernels
     WfEngine* wf = nullptr;        // wavefront driver (created on first use, grows with the dispatch)
@@ -357,7 +356,6 @@ int pt_get_wavefront_tuning(pt_ctx* ctx, pt_wavefront_tuning* out) {
     out->drain_lanes = ctx->drain_lanes;
     out->blocks_per_sm = ctx->blocks_per_sm;
     out->march_inner = ctx->march_inner;
-    out->march_regroup = ctx->march_regroup;
     return PT_OK;
 }
 
@@ -365,8 +363,7 @@ int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* t) {
     if (!ctx) return PT_ERR_INVALID;
     if (!t || t->pool_slots < 1024 || t->pool_slots > (1u << 28) || t->march_budget < 1 || t->march_budget > 512 ||
         t->refill_min < 1 || t->refill_min > 32 || t->drain_lanes < 0 || t->drain_lanes > 32 || t->blocks_per_sm < 1 ||
-        t->blocks_per_sm > 8 || t->march_inner < 1 || t->march_inner > 16 || t->march_regroup < 0 ||
-        t->march_regroup > 1)
+        t->blocks_per_sm > 8 || t->march_inner < 1 || t->march_inner > 16)
         return fail(ctx, PT_ERR_INVALID, "pt_set_wavefront_tuning: a value is out of range");
     ctx->pool_cap = t->pool_slots;
     ctx->march_budget = t->march_budget;
@@ -374,7 +371,6 @@ int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* t) {
     ctx->drain_lanes = t->drain_lanes;
     ctx->blocks_per_sm = t->blocks_per_sm;
     ctx->march_inner = t->march_inner;
-    ctx->march_regroup = t->march_regroup;
     return PT_OK;
 }
 
@@ -416,14 +412,13 @@ int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavef
     static const int kDrain[] = {0, 8, 16, 24};
     static const int kBlocks[] = {2, 3, 4};
     static const int kInner[] = {2, 4, 6, 8};
-    static const int kRegroup[] = {0, 1};
     pt_wavefront_tuning cur;
     pt_get_wavefront_tuning(ctx, &cur);
     double cur_t = 0.0;
     int rc = time_one(cur, &cur_t);
     for (int r = 0; r < rounds && rc == PT_OK; r++) {
-        for (int knob = 0; knob < 7 && rc == PT_OK; knob++) {
-            const int nvals = knob == 0 ? 5 : knob == 1 ? 3 : knob == 2 ? 4 : knob == 3 ? 4 : knob == 4 ? 3 : knob == 5 ? 4 : 2;
+        for (int knob = 0; knob < 6 && rc == PT_OK; knob++) {
+            const int nvals = knob == 0 ? 5 : knob == 1 ? 3 : knob == 2 ? 4 : knob == 3 ? 4 : knob == 4 ? 3 : 4;
             for (int i = 0; i < nvals && rc == PT_OK; i++) {
                 pt_wavefront_tuning c = cur;
                 switch (knob) {
@@ -432,8 +427,7 @@ int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavef
                     case 2: c.refill_min = kRefill[i]; break;
                     case 3: c.drain_lanes = kDrain[i]; break;
                     case 4: c.blocks_per_sm = kBlocks[i]; break;
-                    case 5: c.march_inner = kInner[i]; break;
-                    default: c.march_regroup = kRegroup[i]; break;
+                    default: c.march_inner = kInner[i]; break;
                 }
                 if (std::memcmp(&c, &cur, sizeof c) == 0) continue;
                 double t = 0.0;
@@ -575,7 +569,7 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     WfEngine& E = *ctx->wf;
     E.set_stream(ctx->stream);
     E.set_march_budget(ctx->march_budget);
-    E.set_tuning(ctx->refill_min, ctx->drain_lanes, ctx->blocks_per_sm, ctx->march_inner, ctx->march_regroup);
+    E.set_tuning(ctx->refill_min, ctx->drain_lanes, ctx->blocks_per_sm, ctx->march_inner);
     if (E.stage_timing != ctx->stage_timing) PT_CUDA_TRY(ctx, E.set_stage_timing(ctx->stage_timing));
     E.args.trace = ctx->trace;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;

@@ -77,7 +77,6 @@ static cudaError_t common_setup(WfEngine& e, int device, cudaStream_t stream, ui
     e.args.refill_min = 2;
     e.args.drain_lanes = 24;
     e.args.march_inner = 6;      // measured best on GB300 (mandelbulb, menger + terrain)
-    e.args.march_regroup = 0;
     e.args.persist_refill = 16;  // measured best on GB300 (batch of 64 sphere jobs)
     e.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
     int sms = 0;
@@ -144,14 +143,12 @@ void WfEngine::set_march_budget(int budget) {
 
 void WfEngine::set_stream(cudaStream_t s) { stream = s; }
 
-void WfEngine::set_tuning(int refill, int drain, int bps, int inner, int regroup) {
-    if (refill != args.refill_min || drain != args.drain_lanes || bps != blocks_per_sm || inner != args.march_inner ||
-        regroup != args.march_regroup)
+void WfEngine::set_tuning(int refill, int drain, int bps, int inner) {
+    if (refill != args.refill_min || drain != args.drain_lanes || bps != blocks_per_sm || inner != args.march_inner)
         drop_graph();
     args.refill_min = refill;
     args.drain_lanes = drain;
     args.march_inner = inner;
-    args.march_regroup = regroup;
     blocks_per_sm = bps;
     grid = sms_count * bps;
 }

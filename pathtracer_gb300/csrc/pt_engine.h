@@ -76,7 +76,7 @@ struct WfEngine {
     // Sphere-tracing iterations per ray per march launch.
     void set_march_budget(int budget);
     // March refill threshold, drain threshold and stage-kernel blocks per SM.
-    void set_tuning(int refill_min, int drain_lanes, int blocks_per_sm, int march_inner, int march_regroup);
+    void set_tuning(int refill_min, int drain_lanes, int blocks_per_sm, int march_inner);
     // Sets march_kernel (null: the built-in kernel).
     void set_march_kernel(const void* kernel);
     // Staged kernels (false) or the persistent path kernel (true).

@@ -143,7 +143,6 @@ class PtWavefrontTuning(ctypes.Structure):
         ("drain_lanes", ctypes.c_int32),
         ("blocks_per_sm", ctypes.c_int32),
         ("march_inner", ctypes.c_int32),
-        ("march_regroup", ctypes.c_int32),
     ]
 
 

@@ -29,9 +29,6 @@ SETTINGS = [
      "march_inner": 16},
     {"pool_slots": 1 << 16, "march_budget": 512, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 8,
      "march_inner": 3},
-    {"march_regroup": 1},
-    {"pool_slots": 4096, "march_budget": 5, "refill_min": 1, "drain_lanes": 32, "blocks_per_sm": 8,
-     "march_inner": 2, "march_regroup": 1},
 ]
 
 
@@ -69,30 +66,31 @@ def test_autotune_keeps_the_accumulator_and_installs_a_setting(env):
         assert ctx.tuning() == best and secs > 0.0
         assert 1024 <= best["pool_slots"] and 1 <= best["refill_min"] <= 32 and 1 <= best["blocks_per_sm"] <= 8
         assert 1 <= best["march_inner"] <= 16
-        assert best["march_regroup"] in (0, 1)
-        for bad in ({"refill_min": 0}, {"march_inner": 0}, {"march_inner": 17}, {"march_regroup": 2}):
+        for bad in ({"refill_min": 0}, {"march_inner": 0}, {"march_inner": 17}):
             with pytest.raises(PathTracerError) as e:
                 ctx.set_tuning(**bad)
             assert e.value.code == native.PT_ERR_INVALID
         assert ctx.tuning() == best
 
 
-def test_regroup_on_the_compiled_march_kernel(env):
+def test_knobs_on_the_compiled_march_kernel(env):
     """The bench's default scene (SDF text compiled at run time into the march
-    kernel): regrouped and plain march give the same bits."""
+    kernel): knob settings give the same bits there too."""
     Context, _, Scene, cie, native = env
     scene = Scene.load(os.path.join(SCENES, "mandelbulb12_plane.json"))
     W, H, spf = 128, 96, 4
     push = scene.push_constants(W, H, spf, spf, spf, 6)
     images = []
-    for regroup in (0, 1):
+    for knobs in SETTINGS[:3]:
         with Context(0) as ctx:
             ctx.set_engine(native.PT_ENGINE_WAVEFRONT)
-            ctx.set_tuning(march_regroup=regroup)
+            if knobs:
+                ctx.set_tuning(**knobs)
             ctx.bind(scene, cie)
             ctx.resize_accum(W, H)
             ctx.dispatch(push)
             ctx.wait()
             images.append(ctx.read_accum())
-    assert np.array_equal(images[1].view(np.uint32), images[0].view(np.uint32))
+    for img in images[1:]:
+        assert np.array_equal(img.view(np.uint32), images[0].view(np.uint32))
     assert images[0][..., :3].max() > 0
