@@ -199,16 +199,29 @@ def fp32_peak_tflops(peaks):
 
 
 # wf_march DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum),
-# averaged over the 440 launches of one dispatch of this exact workload with
-# the default knobs, from one ncu capture (the launch-list summary for
-# mandelbulb_plane 1024x1024 64 spp in profiles/).  Other workloads report null.
-MARCH_TRAFFIC_BYTES = {"mandelbulb_plane_1024x1024_64spp_depth6": 75.10e6}
-# The wavefront knobs that capture ran with (the library defaults).
+# averaged over the launches of one dispatch of the workload, from one ncu
+# capture each (the launch-list summaries in profiles/), keyed by workload
+# and path-pool size; the other knobs were the library defaults.  Other
+# settings report null.
+MARCH_TRAFFIC_BYTES = {
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 19): 78.83e6,
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): 333.27e6,
+}
+# The library's default wavefront knobs.
 DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
                   "march_inner": 6}
 
 
-def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, traffic_key=None):
+def traffic_key(workload, spf, tuning):
+    """The MARCH_TRAFFIC_BYTES key of a run, or None when its knobs differ
+    from every capture's."""
+    rest = {k: v for k, v in tuning.items() if k != "pool_slots"}
+    if spf != 64 or rest != {k: v for k, v in DEFAULT_TUNING.items() if k != "pool_slots"}:
+        return None
+    return (workload, tuning["pool_slots"])
+
+
+def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, tkey=None):
     """One extra step with per-stage CUDA events: each stage kernel's device
     time and, from the committed work model, its achieved FP32 rate; the
     roofline object is the march kernel's (the dominant one)."""
@@ -232,7 +245,7 @@ def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, traffic_k
     march = stages["march"]
     roof = {"bound": "fp32", "kernel": "wf_march", "achieved": march["fp32_tflops"], "peak": peak,
             "unit": "TFLOP/s", "frac": (march["fp32_tflops"] or 0.0) / peak,
-            "traffic": MARCH_TRAFFIC_BYTES.get(traffic_key),
+            "traffic": MARCH_TRAFFIC_BYTES.get(tkey),
             "work_per_sample": ops["march"], "launches": iters,
             "note": f"peak: nominal FP32 FMA rate (SMs x 128 x 2) at the measured max SM clock ({peak_kind} peaks "
                     "hold no FP32 figure); achieved: hand-counted FP32 operations of the march stage's events "
@@ -882,9 +895,9 @@ def main():
 
     peaks, peak_kind = measured_peaks()
     if args.engine == "wavefront":
-        captured = spf == 64 and ctx.tuning() == DEFAULT_TUNING
         roofline, stages, ops = stage_roofline(ctx, lambda: one_step(args.warmup + args.steps + 5), samples_per_step,
-                                               work_fixture, peaks, peak_kind, workload if captured else None)
+                                               work_fixture, peaks, peak_kind,
+                                               traffic_key(workload, spf, ctx.tuning()))
     else:
         from pathtracer_gb300 import workmodel
 
