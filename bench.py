@@ -198,14 +198,14 @@ def fp32_peak_tflops(peaks):
     return sms * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
 
 
-# wf_march DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum),
-# averaged over the launches of one dispatch of the workload, from one ncu
-# capture each (the launch-list summaries in profiles/), keyed by workload
-# and path-pool size; the other knobs were the library defaults.  Other
-# settings report null.
-MARCH_TRAFFIC_BYTES = {
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 19): 78.83e6,
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): 333.27e6,
+# DRAM bytes per launch of each stage kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum), averaged over the launches of one dispatch of the
+# workload, from one ncu capture each (the launch-list summaries in
+# profiles/), keyed by workload and path-pool size; the other knobs were the
+# library defaults.  Other settings report null.
+STAGE_TRAFFIC_BYTES = {
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 19): {"march": 78.83e6, "shade": 218.27e6, "gen": 100.56e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): {"march": 333.27e6, "shade": 768.34e6, "gen": 217.00e6},
 }
 # The library's default wavefront knobs.
 DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
@@ -213,7 +213,7 @@ DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "d
 
 
 def traffic_key(workload, spf, tuning):
-    """The MARCH_TRAFFIC_BYTES key of a run, or None when its knobs differ
+    """The STAGE_TRAFFIC_BYTES key of a run, or None when its knobs differ
     from every capture's."""
     rest = {k: v for k, v in tuning.items() if k != "pool_slots"}
     if spf != 64 or rest != {k: v for k, v in DEFAULT_TUNING.items() if k != "pool_slots"}:
@@ -223,7 +223,9 @@ def traffic_key(workload, spf, tuning):
 
 def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, tkey=None):
     """One extra step with per-stage CUDA events: each stage kernel's device
-    time and, from the committed work model, its achieved FP32 rate; the
+    time and, from the committed work model, its achieved FP32 rate, and for
+    a captured configuration its DRAM rate (captured bytes per launch over
+    the live time per launch) against the measured HBM bandwidth; the
     roofline object is the march kernel's (the dominant one)."""
     from pathtracer_gb300 import workmodel
 
@@ -235,17 +237,23 @@ def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, tkey=None
     ops = workmodel.fp32_ops_per_sample(workmodel.load(workload)["per_sample"])
     total_ms = sum(ms.values())
     peak = fp32_peak_tflops(peaks)
+    traffic = STAGE_TRAFFIC_BYTES.get(tkey, {})
+    hbm = peaks.get("hbm_gbs")
     stages = {}
     for st in ("isect", "march", "shade", "gen", "book"):
         secs = ms[st] / 1000.0
         work = ops.get(st, 0.0) * samples
+        per_launch = ms[st] / iters if iters else None
+        gbs = traffic[st] / (per_launch / 1000.0) / 1e9 if st in traffic and per_launch else None
         stages[st] = {"ms": ms[st], "share": ms[st] / total_ms if total_ms else None,
-                      "ms_per_launch": ms[st] / iters if iters else None,
-                      "fp32_tflops": (work / secs / 1e12) if secs and work else None}
+                      "ms_per_launch": per_launch,
+                      "fp32_tflops": (work / secs / 1e12) if secs and work else None,
+                      "dram_bytes_per_launch": traffic.get(st), "dram_gbs": gbs,
+                      "dram_frac": (gbs / hbm) if gbs and hbm else None}
     march = stages["march"]
     roof = {"bound": "fp32", "kernel": "wf_march", "achieved": march["fp32_tflops"], "peak": peak,
             "unit": "TFLOP/s", "frac": (march["fp32_tflops"] or 0.0) / peak,
-            "traffic": MARCH_TRAFFIC_BYTES.get(tkey),
+            "traffic": traffic.get("march"),
             "work_per_sample": ops["march"], "launches": iters,
             "note": f"peak: nominal FP32 FMA rate (SMs x 128 x 2) at the measured max SM clock ({peak_kind} peaks "
                     "hold no FP32 figure); achieved: hand-counted FP32 operations of the march stage's events "

@@ -1,0 +1,24 @@
+"""bench.py's reference arm (the CPU restatement timed on the host cores) on
+a tiny case of each single-scene workload: one JSON line in the bench
+contract, the workload's SDF text restated for the oracle."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("workload", ["mandelbulb12", "mandelbulb"])
+def test_reference_arm_prints_one_contract_line(built, workload):
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                          workload, "--res", "32", "--spp", "2", "--steps", "1", "--warmup", "3", "--cpu-rows", "2"],
+                         capture_output=True, text=True, timeout=600, check=True).stdout
+    lines = [ln for ln in out.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
+    assert d["config"]["workload"].startswith(workload + "_plane_32x32_2spp")
+    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
