@@ -180,3 +180,27 @@ def test_batch_errors(env):
         with pytest.raises(renderer.PathTracerError) as e:
             b.add_scene(bad, [])
         assert e.value.code == native.PT_ERR_INVALID
+
+
+def test_sdf_scenes_share_march_warps(env):
+    """Three SDF scenes of different plug-ins (mandelbulb, blob, menger) in one
+    staged pool: a march warp holds rays of several scenes, and the normals of
+    converged rays are probed across its lanes with each ray's own scene.
+    Each image equals the plain megakernel's bit for bit."""
+    native, renderer, cie = env
+    jobs = []
+    for seed, (w, h), spf in ((0, (40, 36), 3), (2, (36, 30), 2), (5, (44, 28), 2)):
+        scene, spec = renderer.Scene.generate(native.PT_GEN_SDF, seed)
+        jobs.append((scene, w, h, spf, spec.pathLength))
+    with renderer.Batch(0, pool_slots=1 << 13, max_passes=16) as b:
+        b.set_route(native.PT_BATCH_ROUTE_STAGED)
+        ids = [(b.add_scene(s.pack_ubo(cie), s.sdf_plugins()), b.add_target(w, h)) for s, w, h, _, _ in jobs]
+        for k in (1, 2):
+            for (sid, tid), (scene, w, h, spf, depth) in zip(ids, jobs):
+                b.add_pass(sid, tid, scene.push_constants(w, h, k * spf, k * spf, spf, depth))
+        b.run()
+        got = [b.read_target(tid) for _, tid in ids]
+    for g, (scene, w, h, spf, depth) in zip(got, jobs):
+        want = _dispatch_alone(renderer, cie, scene, w, h, spf, depth, 2, native.PT_ENGINE_MEGAKERNEL)
+        assert np.array_equal(g.view(np.uint32), want.view(np.uint32))
+        assert g[..., :3].sum() > 0
