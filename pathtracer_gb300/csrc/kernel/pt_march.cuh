@@ -82,28 +82,14 @@ PT_DI PoolView view(const WfArgs& A) {
 PT_DI uint32_t slot_job(const PoolView& v, uint32_t slot) { return __float_as_uint(v.s9[slot].z); }
 
 // SphereTracing (SC:779-860) with one SDF evaluation per loop iteration per
-// lane.  A converged ray takes its six normal probes on its own lane
-// (MP_NORMAL0..5) when the SDF it converged on costs the same everywhere, or
-// waits in MP_NORMAL for the warp's normal pass when its cost grows near the
-// surface (escape-time fractals: the mandelbulb, and text compiled at run
-// time, whose cost is unknown).
-enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL0 = 3, MP_NORMAL5 = 8, MP_NORMAL = 9 };
-
-// Whether a ray that converged on SDF `sel` (scene_sdf_sel; < 0: none or out
-// of steps) defers its normal probes to the warp's pass.
-PT_DI bool warp_normals(const KScene& S, int sel) {
-    if (sel < 0) return true;
-    const int kind = S.plug[sel].kind;
-    return kind == PT_SDF_MANDELBULB || kind == PT_SDF_CUSTOM;
-}
+// lane; a converged ray waits in MP_NORMAL for the warp's normal pass.
+enum MarchPhase { MP_EMPTY = 0, MP_SIGN = 1, MP_STEP = 2, MP_NORMAL = 3 };
 
 // CalculateNumericalSDFNormals (SC:721-730) for the lanes of `pending` (rays
 // converged at p): the six probes p +- h.xyy, h.yxy, h.yyx of up to five rays
 // at once, one probe per lane, so the probes (near the surface, where an
 // escape-time fractal runs its longest loops) fill the warp instead of one
-// lane each beside rays that march far from it (11 % less march time on a
-// 12-iteration mandelbulb; on SDFs of even cost the probes stay on the ray's
-// lane, where they fill the round's remaining steps).  Returns the
+// lane each beside rays that march far from it.  Returns the
 // central-difference vector (+x - -x, +y - -y, +z - -z) to the lanes of
 // `pending`.  Called by all 32 lanes with the same `pending`.
 PT_DI float3 normal_probes(unsigned pending, const KScene* Sp, float3 p, uint32_t set1, int lane) {
@@ -214,14 +200,13 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
     int phase = MP_EMPTY;
     bool exhausted = false;
     float3 org = f3(0.0f, 0.0f, 0.0f), dir = f3(0.0f, 0.0f, 1.0f), p = org;
-    float t = 0.0f, insT = 0.0f, omega = 0.0f, prevR = 0.0f, hitdist = 0.0f, k = 0.0f, nplus = 0.0f;
-    float3 nv = f3(0.0f, 0.0f, 0.0f);
+    float t = 0.0f, insT = 0.0f, omega = 0.0f, prevR = 0.0f, hitdist = 0.0f, k = 0.0f;
     float2 tmm = make_float2(0.0f, 0.0f);
     uint32_t set1 = 0;
     int points = 0, iter = 0;
     int hit_sel = -2;  // >= -1 once the lane's march converged (scene_sdf_material_hit)
     bool shadow_ray = false;
-    const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
+    const float omegaMax = kOmegaMax, omegaSpeed = 0.20f;
 
     for (;;) {
         // Refill lanes that have no ray (warp-aggregated fetch), once at
@@ -296,17 +281,9 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
 #pragma unroll 1
         for (int sub = 0; sub < inner; sub++) {
             // One SDF evaluation.
-            const bool evalLane = (phase >= MP_SIGN && phase <= MP_NORMAL5) && !finished && !suspend;
+            const bool evalLane = (phase == MP_SIGN || phase == MP_STEP) && !finished && !suspend;
             if (sub > 0 && __ballot_sync(0xffffffffu, evalLane) == 0) break;
-            float3 q = p;
-            if (phase == MP_SIGN) q = org;
-            if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
-                // CalculateNumericalSDFNormals (SC:721-730): p +- h.xyy, h.yxy, h.yyx
-                const int j = phase - MP_NORMAL0;
-                const float ex = (j == 0) ? e : 0.0f, ey = (j == 2) ? e : 0.0f, ez = (j == 4) ? e : 0.0f;
-                const float mx = (j == 1) ? e : 0.0f, my = (j == 3) ? e : 0.0f, mz = (j == 5) ? e : 0.0f;
-                q = (j & 1) ? f3(p.x - mx, p.y - my, p.z - mz) : f3(p.x + ex, p.y + ey, p.z + ez);
-            }
+            const float3 q = (phase == MP_SIGN) ? org : p;
             float val = 0.0f;
             int esel = -1;
             if (evalLane) val = scene_sdf_sel(*Sp, q, set1, esel);
@@ -363,7 +340,7 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
                 if (exitLoop) {
                     if (t < hitdist) {
                         p = fma3s(dir, t, org);
-                        phase = warp_normals(*Sp, hit_sel) ? MP_NORMAL : MP_NORMAL0;
+                        phase = MP_NORMAL;  // probed by the warp after this round
                     } else {
                         finished = true;
                     }
@@ -374,40 +351,24 @@ __global__ void PT_MARCH_BOUNDS wf_march(const __grid_constant__ WfArgs A) {
                     M.m2[slot] = 0x80000000u | ((uint32_t)min(points, 0xffff) << 10) | (uint32_t)iter;
                     suspend = true;
                 }
-            } else if (phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {
-                const int j = phase - MP_NORMAL0;
-                if ((j & 1) == 0) {
-                    nplus = val;
-                } else {
-                    const float dv = nplus - val;
-                    if (j == 1) nv.x = dv;
-                    else if (j == 3) nv.y = dv;
-                    else nv.z = dv;
-                }
-                phase++;
-                if (phase > MP_NORMAL5) {
-                    hit = true;
-                    finished = true;
-                }
             }
         }
 
-        // The deferred normals of this round's converged rays, six probes a
-        // ray across the warp.
+        // The normals of this round's converged rays, six probes a ray
+        // across the warp.
         const unsigned pending = __ballot_sync(0xffffffffu, phase == MP_NORMAL);
         if (pending) {
-            const float3 nw = normal_probes(pending, Sp, p, set1, lane);
+            const float3 nv = normal_probes(pending, Sp, p, set1, lane);
             if (phase == MP_NORMAL) {
-                nv = nw;
                 hit = true;
                 finished = true;
             }
-        }
-        if (finished && hit) {
-            const float3 nrm = normalize3(nv);
-            const float mat = scene_sdf_material_hit(*Sp, p, set1, hit_sel);
-            v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
-            v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+            if (finished && hit) {
+                const float3 nrm = normalize3(nv);
+                const float mat = scene_sdf_material_hit(*Sp, p, set1, hit_sel);
+                v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
+                v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+            }
         }
         stage_push(staged[wib][0], nstaged[0], finished && !shadow_ray, slot, A.q_shade[cur], &C.n_shade[cur], lane);
         stage_push(staged[wib][1], nstaged[1], finished && shadow_ray, slot, A.q_shadow[cur], &C.n_shadow[cur],
