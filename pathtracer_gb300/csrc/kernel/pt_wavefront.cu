@@ -550,6 +550,8 @@ static int resident_blocks(const void* kernel, int* cache) {
     return *cache;
 }
 
+const void* ptk_wavefront_march_warp_normals() { return reinterpret_cast<const void*>(wf_march_warp_normals); }
+
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
                                            cudaEvent_t* stage_events, const void* march_kernel) {
     // stage_events (optional): 6 events recorded before isect, march, shade,

@@ -96,6 +96,10 @@ cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint
 // of the built-in one (scenes with SDF snippets compiled at run time).
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
                                            cudaEvent_t* stage_events = nullptr, const void* march_kernel = nullptr);
+// The built-in march kernel that probes normals across the warp, for
+// dispatches with a mandelbulb (pass it as march_kernel; the default
+// built-in kernel probes each ray's normal on its own lane).
+const void* ptk_wavefront_march_warp_normals();
 // Kernels launched per staged iteration (march, shade, gen, bookkeeping).
 constexpr int kWfKernelsPerIteration = 4;
 // Stages timed by the engine's stage-timing mode.

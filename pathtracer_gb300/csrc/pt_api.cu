@@ -553,10 +553,14 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
         PT_CUDA_TRY(ctx, ctx->wf->create(ctx->device, ctx->stream, pool, 4096, ctx->march_budget));
     }
     // Run-time compiled SDF snippets: their march kernel (the other stages
-    // evaluate no SDF).
-    ctx->wf->set_march_kernel(ctx->custom.empty() ? nullptr
-                                                  : reinterpret_cast<const void*>(
-                                                        ctx->jit[kJitMarch][(size_t)ctx->jit_cur[kJitMarch]].kernel[0]));
+    // evaluate no SDF); a mandelbulb: the built-in kernel with the warp-wide
+    // normal pass.
+    bool bulb = false;
+    for (int i = 0; i < ctx->nplug; i++) bulb = bulb || ctx->plug[i].kind == PT_SDF_MANDELBULB;
+    ctx->wf->set_march_kernel(!ctx->custom.empty()
+                                  ? reinterpret_cast<const void*>(
+                                        ctx->jit[kJitMarch][(size_t)ctx->jit_cur[kJitMarch]].kernel[0])
+                                  : (bulb ? ptk_wavefront_march_warp_normals() : nullptr));
     const size_t cbytes = (size_t)total * sizeof(float4);
     if (cbytes > ctx->colors_bytes) {
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

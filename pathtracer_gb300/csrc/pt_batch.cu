@@ -119,6 +119,9 @@ struct pt_batch {
     int custom_next = 0;
     JitModule jit;
     bool jit_dirty = false;
+    // A scene with a mandelbulb was added: the staged engine's built-in march
+    // kernel then probes normals across the warp.
+    bool bulb = false;
     std::string err;
 };
 
@@ -151,6 +154,14 @@ BatchPass* pass_at(pt_batch* b, uint32_t j) {
     return &b->passes[j - b->pass_base];
 }
 
+// The staged engine's march kernel: the batch's run-time compiled one, else
+// the built-in one with the warp-wide normal pass when a mandelbulb is in
+// the batch, else the default built-in one (null).
+const void* staged_march_kernel(const pt_batch* b) {
+    if (b->jit.lib) return reinterpret_cast<const void*>(b->jit.kernel[0]);
+    return b->bulb ? ptk_wavefront_march_warp_normals() : nullptr;
+}
+
 // Creates engine e on first use: the staged engine with the batch's pool,
 // the persistent engine with the smallest pool (it keeps paths in registers).
 cudaError_t ensure_engine(pt_batch* b, int e) {
@@ -167,7 +178,7 @@ cudaError_t ensure_engine(pt_batch* b, int e) {
     }
     b->engine[e].set_persistent(e == kPersistent);
     b->engine[e].args.persist_refill = b->persist_refill;
-    if (e == kStaged && b->jit.lib) b->engine[e].set_march_kernel(reinterpret_cast<const void*>(b->jit.kernel[0]));
+    if (e == kStaged) b->engine[e].set_march_kernel(staged_march_kernel(b));
     b->engine_live[e] = true;
     return cudaSuccess;
 }
@@ -434,11 +445,12 @@ int add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int 
         return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: objects overflow the 1024-float object array");
     if (n[5] > PT_MAX_LIVE_SDFS || nplugins > PT_MAX_LIVE_SDFS)
         return bfail(b, PT_ERR_UNSUPPORTED, "pt_batch_add_scene: at most 32 SDFs can be evaluated (32-bit set mask)");
-    bool custom = false;
+    bool custom = false, bulb = false;
     for (int i = 0; i < nplugins; i++) {
         if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_CUSTOM)
             return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: unknown plug-in kind");
         custom = custom || plugins[i].kind == PT_SDF_CUSTOM;
+        bulb = bulb || plugins[i].kind == PT_SDF_MANDELBULB;
     }
     PT_B_TRY(b, cudaSetDevice(b->device));
     KScene* S = new (std::nothrow) KScene;
@@ -483,6 +495,7 @@ int add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int 
     bs.has_sdf = n[5] > 0;
     bs.custom = custom;
     bs.variant = pt_feature_variant(n);
+    b->bulb = b->bulb || bulb;
     *scene_id = (int)b->scenes.size();
     b->scenes.push_back(bs);
     return PT_OK;
@@ -667,6 +680,11 @@ int pt_batch_step(pt_batch* b, int iterations, int* completed, int capacity, int
     PT_B_TRY(b, cudaSetDevice(b->device));
     const int jr = prepare_jit(b);
     if (jr != PT_OK) return jr;
+    if (b->engine_live[kStaged] && b->engine[kStaged].march_kernel != staged_march_kernel(b)) {
+        // a mandelbulb scene arrived: no launch of the old kernel may be in flight
+        PT_B_TRY(b, cudaStreamSynchronize(b->estream[kStaged]));
+        b->engine[kStaged].set_march_kernel(staged_march_kernel(b));
+    }
     bool busy[2];
     for (int e = 0; e < 2; e++) busy[e] = b->engine_live[e] && b->engine[e].njobs > b->engine[e].lo;
     if (iterations > 0 && (busy[0] || busy[1])) {
