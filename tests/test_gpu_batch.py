@@ -182,14 +182,17 @@ def test_batch_errors(env):
         assert e.value.code == native.PT_ERR_INVALID
 
 
-def test_sdf_scenes_share_march_warps(env):
-    """Three SDF scenes of different plug-ins (mandelbulb, blob, menger) in one
-    staged pool: a march warp holds rays of several scenes, and the normals of
-    converged rays are probed across its lanes with each ray's own scene.
-    Each image equals the plain megakernel's bit for bit."""
+@pytest.mark.parametrize("seeds", [(0, 2, 5), (2, 5, 7)], ids=["with_mandelbulb", "even_cost_sdfs"])
+def test_sdf_scenes_share_march_warps(env, seeds):
+    """Three SDF scenes of different plug-ins in one staged pool: a march warp
+    holds rays of several scenes.  With a mandelbulb in the batch (seeds 0, 2,
+    5: mandelbulb, blob, menger) the normals of converged rays are probed
+    across the warp's lanes with each ray's own scene; without one (blob,
+    menger, menger) each ray probes on its own lane.  Each image equals the
+    plain megakernel's bit for bit."""
     native, renderer, cie = env
     jobs = []
-    for seed, (w, h), spf in ((0, (40, 36), 3), (2, (36, 30), 2), (5, (44, 28), 2)):
+    for seed, (w, h), spf in zip(seeds, ((40, 36), (36, 30), (44, 28)), (3, 2, 2)):
         scene, spec = renderer.Scene.generate(native.PT_GEN_SDF, seed)
         jobs.append((scene, w, h, spf, spec.pathLength))
     with renderer.Batch(0, pool_slots=1 << 13, max_passes=16) as b:
