@@ -1,5 +1,6 @@
-// pt_march.cuh — the wavefront engine's SDF march kernel (wf_march) and the
-// helpers every stage kernel shares.  Included by pt_wavefront.cu and, for
+// pt_march.cuh — the wavefront engine's SDF march kernels (wf_march, and
+// wf_march_warp_normals for dispatches with a mandelbulb) and the helpers
+// every stage kernel shares.  Included by pt_wavefront.cu and, for
 // scenes whose SDF text is compiled at run time, by the NVRTC program of
 // pt_jit.cu (with PT_JIT_USER_SDF, in namespace ptjit), so both builds run
 // the same source.

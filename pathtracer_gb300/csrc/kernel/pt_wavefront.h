@@ -92,8 +92,9 @@ cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint
 // One iteration: march, shade, gen, bookkeeping (grid = blocks per stage
 // kernel, capped per kernel at what is resident); with stage_events, 6
 // events bracket the 5 stages (isect, done inside shade and gen, stays empty).
-// march_kernel: a run-time compiled wf_march (pt_jit.cu) to launch instead
-// of the built-in one (scenes with SDF snippets compiled at run time).
+// march_kernel: the march kernel to launch instead of the built-in wf_march:
+// a run-time compiled one (pt_jit.cu; scenes with SDF snippets compiled at
+// run time) or ptk_wavefront_march_warp_normals().
 cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
                                            cudaEvent_t* stage_events = nullptr, const void* march_kernel = nullptr);
 // The built-in march kernel that probes normals across the warp, for

@@ -54,8 +54,9 @@ struct WfEngine {
     bool stage_timing = false;
     double stage_ms[PT_STAGE_COUNT] = {0, 0, 0, 0, 0};
     uint64_t stage_launches = 0;
-    // A run-time compiled march kernel (scenes with SDF snippets compiled
-    // by pt_jit.cu), launched instead of the built-in one; null for none.
+    // The march kernel launched instead of the built-in wf_march: a run-time
+    // compiled one (scenes with SDF snippets compiled by pt_jit.cu) or the
+    // built-in warp-wide-normals one; null for wf_march.
     const void* march_kernel = nullptr;
     // Kernels this engine has launched (graph replays counted per kernel).
     uint64_t kernel_launches = 0;
