@@ -922,6 +922,20 @@ static vec3 SampleUniformUnitSphere(uint32_t* seed) {
     float cosTheta = sqrtf(fmaf(-sinTheta, sinTheta, 1.0f));
     return mk3(ptm_cosf(phi) * cosTheta, ptm_sinf(phi) * cosTheta, sinTheta);
 }
+/* SC:999-1003 */
+static vec3 SampleCosineDirectionHemisphere(vec3 normal, uint32_t* seed) {
+    return normalize3(add3(normal, SampleUniformUnitSphere(seed)));
+}
+/* SC:1005-1010 */
+static inline float CosineDirectionPDF(float cosTheta) { return cosTheta / PI_F; }
+/* SC:1025-1028 */
+static inline float CosineUnitConePDF(float cosTheta, float cosThetaMax) {
+    return cosTheta / (PI_F * (1.0f - cosThetaMax * cosThetaMax));
+}
+/* SC:960-963 */
+static inline float SampleHeroWavelength(float l_min, float l_max, uint32_t* seed) {
+    return mixf(l_min, l_max, RandomFloatPCG32(seed));
+}
 static vec3 SampleCosineUnitCone(uint32_t* seed, float cosThetaMax) {
     float rx = RandomFloatPCG32(seed);
     float ry = RandomFloatPCG32(seed);
@@ -930,6 +944,13 @@ static vec3 SampleCosineUnitCone(uint32_t* seed, float cosThetaMax) {
     float cosTheta = (1.0f - cosAlphaMax) * rx + cosAlphaMax;
     float sinTheta = sqrtf(fmaf(-cosTheta, cosTheta, 1.0f));
     return normalize3(mk3(ptm_cosf(phi) * sinTheta, ptm_sinf(phi) * sinTheta, cosTheta + 1.0f));
+}
+
+/* SC:971-974: l_h - 390 + 0.25 * (1, 2, 3, 4) * 330 = offsets 82.5, 165, 247.5, 330 (exact) */
+static vec4 SampleWavelengths(float l_h) {
+    float base = l_h - 390.0f;
+    return mk4(390.0f + modf_glsl(base + 82.5f, 330.0f), 390.0f + modf_glsl(base + 165.0f, 330.0f),
+               390.0f + modf_glsl(base + 247.5f, 330.0f), 390.0f + modf_glsl(base + 330.0f, 330.0f));
 }
 
 /* SC:1030-1055 */
@@ -1077,7 +1098,7 @@ static vec4 SampleLightSource(ctx_t* c, vec4 l, vec4 rayradiance, vec3 outOrigin
         outRay.origin = outOrigin;
         outRay.dir = ToWorld(SampleCosineUnitCone(seed, costhetaMax), lightDir);
         lightpdf = 1.0f / c->u->numObjects[6];
-        lightpdf *= dot3(outRay.dir, lightDir) / (PI_F * (1.0f - costhetaMax * costhetaMax));
+        lightpdf *= CosineUnitConePDF(dot3(outRay.dir, lightDir), costhetaMax);
         *MISBRDFWeight = MISPowerHeuristicsBeta2(BRDFpdf, lightpdf);
         float costheta = dot3(outRay.dir, normal);
         float deathProbability = 1.25f * fmaxf(*MISBRDFWeight - 0.2f, 0.0f);
@@ -1134,8 +1155,8 @@ static vec4 TraceRay(ctx_t* c, vec4 l, vec4* rayradiance, Ray* inRay, uint32_t* 
         COUNT(c, PTO_C_BRDF);
         Ray outRay;
         outRay.origin = fma3(inRay->dir, mk3(hitdist, hitdist, hitdist), inRay->origin);
-        outRay.dir = normalize3(add3(h.normal, SampleUniformUnitSphere(seed)));
-        float BRDFpdf = dot3(outRay.dir, h.normal) / PI_F;
+        outRay.dir = SampleCosineDirectionHemisphere(h.normal, seed);
+        float BRDFpdf = CosineDirectionPDF(dot3(outRay.dir, h.normal));
         radiance = SampleLightSource(c, l, *rayradiance, outRay.origin, h.normal, mat, seed, BRDFpdf, MISBRDFWeight);
         ev |= ((uint32_t)(c->light_pick & 0x7F) << PT_EV_LIGHT_SHIFT) | ((uint32_t)c->shadow_state << PT_EV_SHADOW_SHIFT);
         float costheta = dot3(outRay.dir, h.normal);
@@ -1233,13 +1254,9 @@ static vec3 Scene(ctx_t* c, uint32_t xx, uint32_t xy_y, vec2 uv, int k, uint32_t
     vec3 pointOnAperture = add3(c->cameraPos, vec_mul_mat(mk3(ha * disk.x, ha * disk.y, pc->apertureDist), m));
     ray.dir = normalize3(sub3(pointOnAperture, ray.origin));
     vec3 forwardDir = mk3(m.c0.z, m.c1.z, m.c2.z);
-    float rh = RandomFloatPCG32(&seed);
-    float l_h = mixf(360.0f, 800.0f, rh);
+    float l_h = SampleHeroWavelength(360.0f, 800.0f, &seed);
     TracePathLens(c, l_h, &ray, forwardDir);
-    /* SampleWavelengths SC:971-974 */
-    float base = l_h - 390.0f;
-    vec4 l = mk4(390.0f + modf_glsl(base + 82.5f, 330.0f), 390.0f + modf_glsl(base + 165.0f, 330.0f),
-                 390.0f + modf_glsl(base + 247.5f, 330.0f), 390.0f + modf_glsl(base + 330.0f, 330.0f));
+    vec4 l = SampleWavelengths(l_h);
     vec4 radiance = TracePath(c, l, ray, &seed, events, depth_cap, nev);
     vec3 wx = WaveToXYZ(c, l.x), wy = WaveToXYZ(c, l.y), wz = WaveToXYZ(c, l.z), ww = WaveToXYZ(c, l.w);
     vec3 sum = add3(add3(add3(scl3(wx, radiance.x), scl3(wy, radiance.y)), scl3(wz, radiance.z)), scl3(ww, radiance.w));
@@ -1377,4 +1394,61 @@ int pto_mathf_eval(int fn, const float* x, const float* y, float* out, int n) {
         }
     }
     return PT_OK;
+}
+
+/* Single shader functions for the known-answer tests against the reference's
+ * own shader source (tests/test_oracle_reference.py): each runs the same code
+ * the dispatch above runs.  Vectors are float arrays, matrices column-major. */
+void pto_fn_sample_disk(uint32_t* seed, float* out2) {
+    vec2 v = SampleUniformUnitDisk(seed);
+    out2[0] = v.x, out2[1] = v.y;
+}
+void pto_fn_sample_sphere(uint32_t* seed, float* out3) {
+    vec3 v = SampleUniformUnitSphere(seed);
+    out3[0] = v.x, out3[1] = v.y, out3[2] = v.z;
+}
+void pto_fn_sample_hemisphere(const float* n3, uint32_t* seed, float* out3) {
+    vec3 v = SampleCosineDirectionHemisphere(mk3(n3[0], n3[1], n3[2]), seed);
+    out3[0] = v.x, out3[1] = v.y, out3[2] = v.z;
+}
+void pto_fn_sample_cone(uint32_t* seed, float cosThetaMax, float* out3) {
+    vec3 v = SampleCosineUnitCone(seed, cosThetaMax);
+    out3[0] = v.x, out3[1] = v.y, out3[2] = v.z;
+}
+void pto_fn_sample_wavelengths(float l_h, float* out4) {
+    vec4 v = SampleWavelengths(l_h);
+    out4[0] = v.x, out4[1] = v.y, out4[2] = v.z, out4[3] = v.w;
+}
+void pto_fn_spd(const float* l4, float peak, float d, int invert, float* out4) {
+    vec4 v = SpectralPowerDistribution(mk4(l4[0], l4[1], l4[2], l4[3]), peak, d, invert);
+    out4[0] = v.x, out4[1] = v.y, out4[2] = v.z, out4[3] = v.w;
+}
+void pto_fn_to_world(const float* v3, const float* n3, float* out3) {
+    vec3 v = ToWorld(mk3(v3[0], v3[1], v3[2]), mk3(n3[0], n3[1], n3[2]));
+    out3[0] = v.x, out3[1] = v.y, out3[2] = v.z;
+}
+float pto_fn_mis(float pdf1, float pdf2) { return MISPowerHeuristicsBeta2(pdf1, pdf2); }
+float pto_fn_cosine_pdf(float cosTheta) { return CosineDirectionPDF(cosTheta); }
+float pto_fn_cone_pdf(float cosTheta, float cosThetaMax) { return CosineUnitConePDF(cosTheta, cosThetaMax); }
+float pto_fn_hero_wavelength(float l_min, float l_max, uint32_t* seed) {
+    return SampleHeroWavelength(l_min, l_max, seed);
+}
+float pto_fn_smin(float x, float y) { return smin1(x, y); }
+void pto_fn_smin2(const float* x2, const float* y2, float* out2) {
+    vec2 v = smin2(mk2(x2[0], x2[1]), mk2(y2[0], y2[1]));
+    out2[0] = v.x, out2[1] = v.y;
+}
+int pto_fn_solve_cubic(float b, float c, float d, float* roots3) {
+    vec3 r = mk3(roots3[0], roots3[1], roots3[2]);
+    int n = SolveCubic(b, c, d, &r);
+    roots3[0] = r.x, roots3[1] = r.y, roots3[2] = r.z;
+    return n;
+}
+void pto_fn_solve_quartic(float a, float b, float c, float d, float e, float* roots4, int* real4) {
+    SolveQuartic(a, b, c, d, e, roots4, real4);
+}
+void pto_fn_rotation(const float* angle3, float* out9) {
+    mat3 m = RotationMatrix(mk3(angle3[0], angle3[1], angle3[2]));
+    const vec3 cols[3] = {m.c0, m.c1, m.c2};
+    for (int j = 0; j < 3; j++) out9[3 * j] = cols[j].x, out9[3 * j + 1] = cols[j].y, out9[3 * j + 2] = cols[j].z;
 }

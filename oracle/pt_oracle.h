@@ -79,6 +79,23 @@ float pto_sdf_eval(const pt_sdf_plugin* plugin, const float* p3);
 float pto_sdf_material(const pt_sdf_plugin* plugin, const float* p3);
 void pto_wave_to_xyz(const float* cie, float wave, float* out3);
 int pto_mathf_eval(int fn, const float* x, const float* y, float* out, int n);
+/* Single shader functions (SC line ranges at their definitions in pt_oracle.c). */
+void pto_fn_sample_disk(uint32_t* seed, float* out2);
+void pto_fn_sample_sphere(uint32_t* seed, float* out3);
+void pto_fn_sample_hemisphere(const float* n3, uint32_t* seed, float* out3);
+void pto_fn_sample_cone(uint32_t* seed, float cosThetaMax, float* out3);
+void pto_fn_sample_wavelengths(float l_h, float* out4);
+void pto_fn_spd(const float* l4, float peak, float d, int invert, float* out4);
+void pto_fn_to_world(const float* v3, const float* n3, float* out3);
+float pto_fn_mis(float pdf1, float pdf2);
+float pto_fn_cosine_pdf(float cosTheta);
+float pto_fn_cone_pdf(float cosTheta, float cosThetaMax);
+float pto_fn_hero_wavelength(float l_min, float l_max, uint32_t* seed);
+float pto_fn_smin(float x, float y);
+void pto_fn_smin2(const float* x2, const float* y2, float* out2);
+int pto_fn_solve_cubic(float b, float c, float d, float* roots3);
+void pto_fn_solve_quartic(float a, float b, float c, float d, float e, float* roots4, int* real4);
+void pto_fn_rotation(const float* angle3, float* out9);
 /* CPU functions of a PT_SDF_CUSTOM slot (the compiled translation of its GLSL). */
 int pto_set_user_sdf(int slot, float (*sdf)(float, float, float), float (*material)(float, float, float));
 

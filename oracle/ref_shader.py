@@ -1,0 +1,206 @@
+"""Builds oracle/_ref/libref_shader.so: single functions of the reference's own
+compute shader (src/shader.comp of the reference tree), compiled for the CPU.
+
+TEST INFRASTRUCTURE ONLY.  The reference cannot run here (it is a Vulkan
+program), but its shader functions that need no scene buffers (RNG, sampling,
+spectra, refraction, MIS, the polynomial solvers, the rotation matrix, smin)
+are plain GLSL: this recipe cuts them out of the reference source at build
+time, turns the source's numeric #defines into constants and its push
+constants into variables, runs the text through the repository's GLSL
+translator (pt_glsl_translate) and compiles it over pt_glsl_shim.h with g++
+-ffp-contract=off.  tests/test_oracle_reference.py then checks the oracle's
+restatements (oracle/pt_oracle.c) against them bit for bit.  Nothing of the
+reference is committed: the source is read from the reference tree and the
+build goes to oracle/_ref/ (git-ignored).
+
+    python oracle/ref_shader.py [reference-root]
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_ref")
+LIB = os.path.join(OUT, "libref_shader.so")
+DEFAULT_REFERENCE = "/root/reference"
+
+# The shader functions built, every overload of each name.
+FUNCTIONS = [
+    "PCG32", "RandomFloatPCG32", "GenerateSeed", "SampleHeroWavelength", "InverseSampleWavelengthPDF",
+    "SampleWavelengths", "SampleUniformUnitDisk", "SampleUniformUnitSphere", "SampleCosineDirectionHemisphere",
+    "CosineDirectionPDF", "SampleCosineUnitCone", "CosineUnitConePDF", "SpectralPowerDistribution",
+    "BlackBodyRadiation", "BlackBodyRadiationPeak", "RefractiveIndexWavelength", "RefractiveIndexBK7Glass",
+    "OrthonormalBasis", "ToWorld", "MISPowerHeuristicsBeta2", "EvalQuadratic", "EvalCubic",
+    "EvalQuartic", "SolveCubic", "SolveQuartic", "minMaterial", "smin", "RotationMatrix",
+]
+
+# C entry points (refsh_*) over the translated functions (namespace ptg::ref_).
+WRAPPERS = r"""
+using namespace ptg;
+using namespace ptg::ref_;
+extern "C" {
+uint32_t refsh_pcg32(uint32_t s) { uint x = s; ref_PCG32(x); return x; }
+float refsh_random_float(uint32_t* s) { uint x = *s; const float r = ref_RandomFloatPCG32(x); *s = x; return r; }
+uint32_t refsh_generate_seed(uint32_t x, uint32_t y, int fr, int spf, int k, int width) {
+    frame = fr;
+    samplesPerFrame = spf;
+    resolution = ivec2(width, 0);
+    return ref_GenerateSeed(uvec2(x, y), k);
+}
+float refsh_hero_wavelength(float lmin, float lmax, uint32_t* s) {
+    uint x = *s;
+    const float r = ref_SampleHeroWavelength(lmin, lmax, x);
+    *s = x;
+    return r;
+}
+float refsh_inverse_wavelength_pdf(float lmin, float lmax) { return ref_InverseSampleWavelengthPDF(lmin, lmax); }
+void refsh_sample_wavelengths(float lh, float* o) {
+    const vec4 v = ref_SampleWavelengths(lh);
+    o[0] = v.x, o[1] = v.y, o[2] = v.z, o[3] = v.w;
+}
+void refsh_sample_disk(uint32_t* s, float* o) {
+    uint x = *s;
+    const vec2 v = ref_SampleUniformUnitDisk(x);
+    *s = x;
+    o[0] = v.x, o[1] = v.y;
+}
+void refsh_sample_sphere(uint32_t* s, float* o) {
+    uint x = *s;
+    const vec3 v = ref_SampleUniformUnitSphere(x);
+    *s = x;
+    o[0] = v.x, o[1] = v.y, o[2] = v.z;
+}
+void refsh_sample_hemisphere(const float* n, uint32_t* s, float* o) {
+    uint x = *s;
+    const vec3 v = ref_SampleCosineDirectionHemisphere(vec3(n[0], n[1], n[2]), x);
+    *s = x;
+    o[0] = v.x, o[1] = v.y, o[2] = v.z;
+}
+float refsh_cosine_pdf(float c) { return ref_CosineDirectionPDF(c); }
+void refsh_sample_cone(uint32_t* s, float cmax, float* o) {
+    uint x = *s;
+    const vec3 v = ref_SampleCosineUnitCone(x, cmax);
+    *s = x;
+    o[0] = v.x, o[1] = v.y, o[2] = v.z;
+}
+float refsh_cone_pdf(float c, float cmax) { return ref_CosineUnitConePDF(c, cmax); }
+void refsh_spd(const float* l, float peak, float d, int invert, float* o) {
+    const vec4 v = ref_SpectralPowerDistribution(vec4(l[0], l[1], l[2], l[3]), peak, d, invert);
+    o[0] = v.x, o[1] = v.y, o[2] = v.z, o[3] = v.w;
+}
+void refsh_blackbody(const float* l, float T, float* o) {
+    const vec4 v = ref_BlackBodyRadiation(vec4(l[0], l[1], l[2], l[3]), T);
+    o[0] = v.x, o[1] = v.y, o[2] = v.z, o[3] = v.w;
+}
+float refsh_blackbody_peak(float T) { return ref_BlackBodyRadiationPeak(T); }
+float refsh_bk7_index(float l) { return ref_RefractiveIndexBK7Glass(l); }
+void refsh_to_world(const float* v, const float* n, float* o) {
+    const vec3 r = ref_ToWorld(vec3(v[0], v[1], v[2]), vec3(n[0], n[1], n[2]));
+    o[0] = r.x, o[1] = r.y, o[2] = r.z;
+}
+float refsh_mis(float a, float b) { return ref_MISPowerHeuristicsBeta2(a, b); }
+float refsh_smin(float x, float y) { return ref_smin(x, y); }
+void refsh_smin2(const float* x, const float* y, float* o) {
+    const vec2 v = ref_smin(vec2(x[0], x[1]), vec2(y[0], y[1]));
+    o[0] = v.x, o[1] = v.y;
+}
+float refsh_min_material(float x, float y, float m1, float m2) { return ref_minMaterial(x, y, m1, m2); }
+int refsh_solve_cubic(float b, float c, float d, float* r) {
+    vec3 v(r[0], r[1], r[2]);
+    const bvec3 real = ref_SolveCubic(b, c, d, v);
+    r[0] = v.x, r[1] = v.y, r[2] = v.z;
+    return (int)real.x + (int)real.y + (int)real.z;
+}
+void refsh_solve_quartic(float a, float b, float c, float d, float e, float* r, int* real) {
+    vec4 v(r[0], r[1], r[2], r[3]);
+    const bvec4 q = ref_SolveQuartic(a, b, c, d, e, v);
+    r[0] = v.x, r[1] = v.y, r[2] = v.z, r[3] = v.w;
+    real[0] = q.x, real[1] = q.y, real[2] = q.z, real[3] = q.w;
+}
+void refsh_rotation(const float* angle, float* o) {
+    const mat3 m = ref_RotationMatrix(vec3(angle[0], angle[1], angle[2]));
+    const vec3 c[3] = {m.c0, m.c1, m.c2};
+    for (int j = 0; j < 3; j++) o[3 * j] = c[j].x, o[3 * j + 1] = c[j].y, o[3 * j + 2] = c[j].z;
+}
+}
+"""
+
+
+def reference_root(arg: str | None = None) -> str:
+    return arg or os.environ.get("PT_REFERENCE_ROOT", DEFAULT_REFERENCE)
+
+
+def shader_path(reference: str | None = None) -> str:
+    """The reference's compute shader source (present only where the
+    reference tree is mounted)."""
+    return os.path.join(reference_root(reference), "src", "shader.comp")
+
+
+def extract(src: str) -> str:
+    """The GLSL text handed to the translator: the source's numeric #defines as
+    constants, the push constants the functions read as variables, then every
+    definition of each FUNCTIONS name in source order."""
+    out = []
+    for m in re.finditer(r"^#define\s+(\w+)\s+([-+0-9.eE]+)\s*$", src, re.M):
+        name, value = m.group(1), m.group(2)
+        kind = "float" if re.search(r"[.eE]", value) else "int"
+        out.append(f"const {kind} {name} = {value};")
+    out.append("int frame = 0;\nint samplesPerFrame = 1;\nivec2 resolution = ivec2(0);")
+    starts = []
+    for name in FUNCTIONS:
+        found = [m.start() for m in re.finditer(r"^\w+\s+" + name + r"\s*\(", src, re.M)]
+        if not found:
+            raise ValueError(f"{name} not found in the shader source")
+        starts.extend(found)
+    for s in sorted(starts):
+        depth, i = 0, src.index("{", s)
+        while True:
+            if src[i] == "{":
+                depth += 1
+            elif src[i] == "}":
+                depth -= 1
+                if depth == 0:
+                    break
+            i += 1
+        out.append(src[s:i + 1])
+    # the translator wants the two SDF entry points of a scene snippet
+    out.append("float sdf(vec3 p) { return 0.0; }\nfloat sdfmaterial(vec3 p) { return 0.0; }")
+    return "\n\n".join(out) + "\n"
+
+
+def build(reference: str | None = None) -> str:
+    """Builds (when the shader source is newer) and returns the library path."""
+    shader = shader_path(reference)
+    if not os.path.exists(shader):
+        raise FileNotFoundError(shader)
+    deps = [shader, __file__, os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel", "pt_glsl_shim.h"),
+            os.path.join(ROOT, "pathtracer_gb300", "csrc", "pt_glsl.cpp"), os.path.join(ROOT, "include", "pt_mathf.h")]
+    if os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
+        return LIB
+    sys.path.insert(0, ROOT)
+    from pathtracer_gb300 import glsl_translate
+
+    with open(shader) as f:
+        glsl = extract(f.read())
+    code = glsl_translate(glsl, "ref_")
+    os.makedirs(OUT, exist_ok=True)
+    cpp = os.path.join(OUT, "ref_shader.cpp")
+    with open(cpp, "w") as f:
+        f.write("#include <stdint.h>\n#include \"pt_glsl_shim.h\"\n" + code + WRAPPERS)
+    subprocess.run([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+                    "-fno-fast-math", "-I", os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel"), "-o", LIB, cpp],
+                   check=True)
+    return LIB
+
+
+def load(reference: str | None = None) -> ctypes.CDLL:
+    return ctypes.CDLL(build(reference))
+
+
+if __name__ == "__main__":
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None))

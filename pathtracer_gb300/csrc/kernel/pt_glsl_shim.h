@@ -5,9 +5,11 @@
 // pt_glsl_translate (pt_glsl.cpp), which rewrites float literals, swizzles and
 // parameter qualifiers into this vocabulary.
 //
-// Covered: float/int/bool, vec2/vec3/vec4 (constructors, component access,
-// read swizzles as member calls, arithmetic with vectors and scalars),
-// mat2/mat3 (constructors from columns, matrix * vector), and the built-ins
+// Covered: float/int/uint/bool, vec2/vec3/vec4 (constructors, component
+// access, read swizzles as member calls, swizzle assignment through set_<sw>
+// members, arithmetic with vectors and scalars), uvec2/ivec2 and
+// bvec2/bvec3/bvec4 (constructors, components), mat2/mat3 (constructors
+// from columns or scalars, matrix * vector, mat3 * mat3), and the built-ins
 // abs sign floor ceil fract round trunc mod min max clamp mix step
 // smoothstep sqrt inversesqrt pow exp exp2 log log2 sin cos tan asin acos
 // atan (one and two arguments) length distance dot cross normalize reflect
@@ -26,6 +28,8 @@
 
 namespace ptg {
 
+typedef unsigned int uint;
+
 struct vec2;
 struct vec3;
 struct vec4;
@@ -35,6 +39,8 @@ struct vec2 {
     PTG_M vec2() : x(0.0f), y(0.0f) {}
     PTG_M explicit vec2(float s) : x(s), y(s) {}
     PTG_M vec2(float a, float b) : x(a), y(b) {}
+    PTG_M void set_xy(vec2 v);
+    PTG_M void set_yx(vec2 v);
     PTG_M vec2 xx() const { return vec2(x, x); }
     PTG_M vec2 xy() const { return vec2(x, y); }
     PTG_M vec2 yx() const { return vec2(y, x); }
@@ -57,6 +63,9 @@ struct vec3 {
 #define PTG_S3B(A, B) PTG_S3(A, B, x) PTG_S3(A, B, y) PTG_S3(A, B, z)
 #define PTG_S3A(A) PTG_S3B(A, x) PTG_S3B(A, y) PTG_S3B(A, z)
     PTG_S3A(x) PTG_S3A(y) PTG_S3A(z)
+#define PTG_SET2(A, B) \
+    PTG_M void set_##A##B(vec2 v) { A = v.x; B = v.y; }
+    PTG_SET2(x, y) PTG_SET2(x, z) PTG_SET2(y, x) PTG_SET2(y, z) PTG_SET2(z, x) PTG_SET2(z, y)
 };
 
 struct vec4 {
@@ -69,6 +78,48 @@ struct vec4 {
     PTG_M vec3 xyz() const { return vec3(x, y, z); }
     PTG_M vec2 xy() const { return vec2(x, y); }
     PTG_M vec2 zw() const { return vec2(z, w); }
+    PTG_M void set_xy(vec2 v) { x = v.x; y = v.y; }
+    PTG_M void set_zw(vec2 v) { z = v.x; w = v.y; }
+    PTG_M void set_xyz(vec3 v) { x = v.x; y = v.y; z = v.z; }
+};
+PTG_M void vec2::set_xy(vec2 v) { x = v.x; y = v.y; }
+PTG_M void vec2::set_yx(vec2 v) { y = v.x; x = v.y; }
+
+// Integer and boolean vectors: constructors and components (GLSL's
+// arithmetic on them is not covered).
+struct uvec2 {
+    uint x, y;
+    PTG_M uvec2() : x(0u), y(0u) {}
+    PTG_M explicit uvec2(uint s) : x(s), y(s) {}
+    PTG_M uvec2(uint a, uint b) : x(a), y(b) {}
+};
+struct ivec2 {
+    int x, y;
+    PTG_M ivec2() : x(0), y(0) {}
+    PTG_M explicit ivec2(int s) : x(s), y(s) {}
+    PTG_M ivec2(int a, int b) : x(a), y(b) {}
+};
+struct bvec2 {
+    bool x, y;
+    PTG_M bvec2() : x(false), y(false) {}
+    PTG_M explicit bvec2(bool s) : x(s), y(s) {}
+    PTG_M bvec2(bool a, bool b) : x(a), y(b) {}
+};
+struct bvec3 {
+    bool x, y, z;
+    PTG_M bvec3() : x(false), y(false), z(false) {}
+    PTG_M explicit bvec3(bool s) : x(s), y(s), z(s) {}
+    PTG_M bvec3(bool a, bool b, bool c) : x(a), y(b), z(c) {}
+};
+struct bvec4 {
+    bool x, y, z, w;
+    PTG_M bvec4() : x(false), y(false), z(false), w(false) {}
+    PTG_M explicit bvec4(bool s) : x(s), y(s), z(s), w(s) {}
+    PTG_M bvec4(bool a, bool b, bool c, bool d) : x(a), y(b), z(c), w(d) {}
+    PTG_M bvec2 xy() const { return bvec2(x, y); }
+    PTG_M bvec2 zw() const { return bvec2(z, w); }
+    PTG_M void set_xy(bvec2 v) { x = v.x; y = v.y; }
+    PTG_M void set_zw(bvec2 v) { z = v.x; w = v.y; }
 };
 
 // Component-wise arithmetic.
@@ -187,6 +238,9 @@ PTG_FN vec2 fma(vec2 a, vec2 b, vec2 c) { return vec2(PTM_FMA(a.x, b.x, c.x), PT
 PTG_FN vec3 fma(vec3 a, vec3 b, vec3 c) {
     return vec3(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y), PTM_FMA(a.z, b.z, c.z));
 }
+PTG_FN vec4 fma(vec4 a, vec4 b, vec4 c) {
+    return vec4(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y), PTM_FMA(a.z, b.z, c.z), PTM_FMA(a.w, b.w, c.w));
+}
 
 template <typename V> PTG_FN V clamp(V a, V lo, V hi) { return min(max(a, lo), hi); }
 PTG_FN vec2 clamp(vec2 a, float lo, float hi) { return min(max(a, lo), hi); }
@@ -195,6 +249,8 @@ PTG_FN float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 PTG_FN vec2 mix(vec2 a, vec2 b, float t) { return a * (1.0f - t) + b * t; }
 PTG_FN vec3 mix(vec3 a, vec3 b, float t) { return a * (1.0f - t) + b * t; }
 PTG_FN vec3 mix(vec3 a, vec3 b, vec3 t) { return a * (1.0f - t) + b * t; }
+PTG_FN vec4 mix(vec4 a, vec4 b, float t) { return a * (1.0f - t) + b * t; }
+PTG_FN vec4 mix(vec4 a, vec4 b, vec4 t) { return a * (1.0f - t) + b * t; }
 PTG_FN float smoothstep(float e0, float e1, float x) {
     const float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
     return t * t * (3.0f - 2.0f * t);
@@ -223,12 +279,16 @@ PTG_FN vec2 operator*(vec2 v, mat2 m) { return vec2(dot(v, m.c0), dot(v, m.c1));
 struct mat3 {
     vec3 c0, c1, c2;
     PTG_M mat3(vec3 a, vec3 b, vec3 c) : c0(a), c1(b), c2(c) {}
+    // column-major, as GLSL fills a matrix from scalars
+    PTG_M mat3(float a, float b, float c, float d, float e, float f, float g, float h, float i)
+        : c0(a, b, c), c1(d, e, f), c2(g, h, i) {}
 };
 PTG_FN vec3 operator*(mat3 m, vec3 v) {
     return vec3(m.c0.x * v.x + m.c1.x * v.y + m.c2.x * v.z, m.c0.y * v.x + m.c1.y * v.y + m.c2.y * v.z,
                 m.c0.z * v.x + m.c1.z * v.y + m.c2.z * v.z);
 }
 PTG_FN vec3 operator*(vec3 v, mat3 m) { return vec3(dot(v, m.c0), dot(v, m.c1), dot(v, m.c2)); }
+PTG_FN mat3 operator*(mat3 a, mat3 b) { return mat3(a * b.c0, a * b.c1, a * b.c2); }
 
 // The shader's polynomial smooth minimum (src/shader.comp:686-702), k = 0.02 * 6,
 // with its ONEBYTHREE constant (src/shader.comp:10).

@@ -9,6 +9,12 @@
 //   - float literals get an f suffix (GLSL floats are single precision);
 //   - read swizzles (.xz, .zyx, .rg ...) become member calls (.xz()), and
 //     single rgba components name the fields (.g -> .y);
+//   - assignment to a swizzle of a variable, `v.xy = e;` or `v.xy op= e;`,
+//     becomes `v.set_xy(e);` or `v.set_xy(v.xy() op (e));`;
+//   - a vector constructor with two or more arguments that call a snippet
+//     function with out/inout parameters, `vec2(rnd(seed), rnd(seed))`, is
+//     braced (`vec2{...}`): GLSL evaluates arguments left to right, C++
+//     only guarantees that order in a braced list;
 //   - parameter qualifiers: `in`/`const in` are dropped, `out`/`inout` make
 //     the parameter a reference;
 //   - every function the snippet defines is renamed <prefix><name> and
@@ -16,8 +22,8 @@
 //     ptg::<prefix>, so several snippets (or one in several slots) coexist;
 //   - top-level `const float|int` declarations become constexpr.
 // Anything the shim does not cover (structs, uniforms, preprocessor lines,
-// swizzle assignment, arrays of vectors at file scope...) is rejected with a
-// message instead of being guessed at.
+// arrays of vectors at file scope...) is rejected with a message instead of
+// being guessed at.
 #include <cctype>
 #include <cstring>
 #include <set>
@@ -51,7 +57,8 @@ std::string rgba_to_xyzw(std::string s) {
 }
 
 bool is_type(const std::string& s) {
-    static const std::set<std::string> types = {"float", "int", "bool", "void", "vec2", "vec3", "vec4", "mat2", "mat3"};
+    static const std::set<std::string> types = {"float", "int",   "uint",  "bool",  "void",  "vec2",  "vec3", "vec4",
+                                                "mat2",  "mat3",  "uvec2", "ivec2", "bvec2", "bvec3", "bvec4"};
     return types.count(s) != 0;
 }
 
@@ -144,8 +151,9 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
     std::string e;
     if (!tokenize(glsl, t, e)) return fail(e);
 
-    // Functions the snippet defines: `type name (` at brace depth 0.
-    std::set<std::string> funcs;
+    // Functions the snippet defines: `type name (` at brace depth 0, and
+    // those of them with out/inout parameters (calls with side effects).
+    std::set<std::string> funcs, effect_funcs;
     int depth = 0;
     for (size_t i = 0; i < t.size(); i++) {
         if (t[i].kind == Tok::Punct) {
@@ -160,7 +168,11 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
         if (depth == 0 && is_type(t[i].text)) {
             const size_t j = next_nonspace(t, i + 1);
             const size_t k = j < t.size() ? next_nonspace(t, j + 1) : t.size();
-            if (j < t.size() && t[j].kind == Tok::Ident && k < t.size() && t[k].text == "(") funcs.insert(t[j].text);
+            if (j < t.size() && t[j].kind == Tok::Ident && k < t.size() && t[k].text == "(") {
+                funcs.insert(t[j].text);
+                for (size_t q = k + 1; q < t.size() && t[q].text != ")"; q++)
+                    if (t[q].text == "out" || t[q].text == "inout") effect_funcs.insert(t[j].text);
+            }
         }
     }
     if (!funcs.count("sdf") || !funcs.count("sdfmaterial"))
@@ -172,11 +184,19 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
     depth = 0;
     int paren = 0;
     bool ref_pending = false;  // out/inout seen: the next type gets '&'
+    std::string close_stmt;    // closes a rewritten swizzle assignment at its ';'
+    std::set<size_t> brace_close;  // ')' tokens of braced constructors
     for (size_t i = 0; i < t.size(); i++) {
         const Tok& k = t[i];
         if (k.kind == Tok::Space) {
             o += k.text;
             continue;
+        }
+        if (!close_stmt.empty() && k.kind == Tok::Punct && paren == 0 && (k.text == ";" || k.text == "," ||
+                                                                          k.text == "{" || k.text == "}")) {
+            if (k.text != ";") return fail("a swizzle assignment must be a statement of its own");
+            o += close_stmt;
+            close_stmt.clear();
         }
         if (k.kind == Tok::Number) {
             o += float_literal(k.text);
@@ -187,13 +207,44 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
             if (k.text == "}") depth--;
             if (k.text == "(") paren++;
             if (k.text == ")") paren--;
+            if (k.text == ")" && brace_close.count(i)) {
+                o += "}";
+                continue;
+            }
             if (k.text == ".") {
                 const size_t j = i + 1;  // swizzles follow the dot directly
                 if (j < t.size() && t[j].kind == Tok::Ident && is_swizzle(t[j].text)) {
+                    const std::string sw = rgba_to_xyzw(t[j].text);
                     const size_t a = next_nonspace(t, j + 1);
-                    if (a < t.size() && t[a].text == "=" && !(a + 1 < t.size() && t[a + 1].text == "="))
-                        return fail("assignment to a swizzle is not supported");
-                    o += "." + rgba_to_xyzw(t[j].text) + "()";
+                    // `=` or `op=` (the tokenizer gives single-character punctuation)
+                    std::string op;
+                    size_t eq = t.size();
+                    if (a < t.size() && t[a].text == "=" && !(a + 1 < t.size() && t[a + 1].text == "=")) {
+                        eq = a;
+                    } else if (a + 1 < t.size() && (t[a].text == "+" || t[a].text == "-" || t[a].text == "*" ||
+                                                     t[a].text == "/") &&
+                               t[a + 1].text == "=" && !(a + 2 < t.size() && t[a + 2].text == "=")) {
+                        op = t[a].text;
+                        eq = a + 1;
+                    }
+                    if (eq < t.size()) {
+                        // the target: a plain variable, written just before the dot
+                        size_t b = i;
+                        while (b > 0 && t[b - 1].kind == Tok::Space) b--;
+                        if (b == 0 || t[b - 1].kind != Tok::Ident || !close_stmt.empty())
+                            return fail("assignment to a swizzle needs a plain variable on the left");
+                        size_t bb = b - 1;
+                        while (bb > 0 && t[bb - 1].kind == Tok::Space) bb--;
+                        if (bb > 0 && (t[bb - 1].text == "." || t[bb - 1].text == "]" || t[bb - 1].text == ")"))
+                            return fail("assignment to a swizzle needs a plain variable on the left");
+                        const std::string var = t[b - 1].text;
+                        o += ".set_" + sw + "(";
+                        if (!op.empty()) o += var + "." + sw + "() " + op + " (";
+                        close_stmt = op.empty() ? ")" : "))";
+                        i = eq;
+                        continue;
+                    }
+                    o += "." + sw + "()";
                     i = j;
                     continue;
                 }
@@ -232,6 +283,36 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
         if (funcs.count(w)) {
             o += std::string(prefix) + w;
             continue;
+        }
+        if (is_type(w) && w != "void" && !effect_funcs.empty()) {
+            // a constructor call: count its arguments that call a function with side effects
+            const size_t open = next_nonspace(t, i + 1);
+            if (open < t.size() && t[open].text == "(") {
+                int d = 0, effects = 0;
+                bool arg_effect = false;
+                size_t close = open;
+                for (size_t q = open; q < t.size(); q++) {
+                    const std::string& x = t[q].text;
+                    if (x == "(") d++;
+                    if (x == ")" && --d == 0) {
+                        close = q;
+                        break;
+                    }
+                    if (d == 1 && x == ",") {
+                        effects += arg_effect;
+                        arg_effect = false;
+                    }
+                    if (t[q].kind == Tok::Ident && effect_funcs.count(x)) arg_effect = true;
+                }
+                effects += arg_effect;
+                if (close > open && effects >= 2) {
+                    o += w + "{";
+                    paren++;
+                    brace_close.insert(close);
+                    i = open;
+                    continue;
+                }
+            }
         }
         o += w;
         if (ref_pending && is_type(w)) {

@@ -81,7 +81,7 @@ def test_translation_rewrites_glsl(pt):
     ("struct S { float a; }; float sdf(vec3 p){return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "struct"),
     ("uniform float t; float sdf(vec3 p){return t;} float sdfmaterial(vec3 p){return 0.0;}", "uniform"),
     ("#define K 2.0\nfloat sdf(vec3 p){return K;} float sdfmaterial(vec3 p){return 0.0;}", "preprocessor"),
-    ("float sdf(vec3 p){p.xy = vec2(0.0); return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "swizzle"),
+    ("float sdf(vec3 p){(p).xy = vec2(0.0); return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "swizzle"),
     ("float sdf(vec3 p){return length(p) - 1.0;}", "must define"),
     ("float sdf(vec3 p){return 0.0;} float sdfmaterial(vec3 p){return 0.0;", "unbalanced"),
     ("float sdf(vec3 p){return 0.0; /* open", "unterminated"),
@@ -212,3 +212,62 @@ def test_scene_snippet_matches_its_c_restatement(pt):
     iters = (ctypes.c_uint64 * len(oracle.USER_COUNTERS)).in_dll(u, "user_counters")[0]
     u.user_count(0)
     assert 1000 < iters < 12 * 1000
+
+
+HASHED = """
+// A hashed jitter: uint arithmetic, a side-effecting helper in a vector
+// constructor, swizzle assignment and boolean vectors.
+void pcg(inout uint s)
+{
+    uint state = s * 747796405u + 2891336453u;
+    uint word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    s = (word >> 22u) ^ word;
+}
+float rnd(inout uint s) { pcg(s); return float(s) / 0xFFFFFFFFu; }
+float sdf(vec3 p)
+{
+    uint s = uint(floor(p.x * 4.0) + 64.0) * 97u + uint(floor(p.z * 4.0) + 64.0);
+    vec2 j = vec2(rnd(s), rnd(s));
+    vec4 q = vec4(p, 1.0);
+    q.xy -= 0.1 * j;
+    q.zw = vec2(q.z, 0.5);
+    bvec2 in2 = bvec2(q.x > 0.0, q.y > 0.0);
+    float r = in2.x ? 0.5 : 0.45;
+    return length(q.xyz) - r;
+}
+float sdfmaterial(vec3 p) { return 1.0; }
+"""
+
+
+def test_integer_boolean_and_swizzle_vocabulary(pt):
+    """uint hashing, bvec, swizzle assignment and a vector constructor whose
+    arguments draw random numbers: translated as GLSL means them (arguments
+    left to right through a braced constructor), compiled by NVRTC for
+    sm_103 and by g++, and the CPU build matches a Python restatement."""
+    import numpy as np
+
+    out = " ".join(pt.glsl_translate(HASHED, "h_").split())
+    assert "vec2{h_rnd(s), h_rnd(s)}" in out
+    assert "q.set_xy(q.xy() - ( 0.1f * j));" in out and "q.set_zw( vec2(q.z, 0.5f));" in out
+    assert "uint& s" in out and "bvec2 in2" in out
+    pt.jit_check([HASHED], sm=103)
+    lib = _cpu_build(pt, "hashed", {"h": HASHED})
+    f = _fn(lib, "c_h_sdf")
+
+    def pcg(s):
+        state = (s * 747796405 + 2891336453) & 0xFFFFFFFF
+        word = (((state >> ((state >> 28) + 4)) ^ state) * 277803737) & 0xFFFFFFFF
+        return ((word >> 22) ^ word) & 0xFFFFFFFF
+
+    f32 = np.float32
+    for x, y, z in _points(n=300, scale=1.0):
+        x, y, z = f32(x), f32(y), f32(z)
+        s = (int(np.floor(x * f32(4.0)) + f32(64.0)) * 97 + int(np.floor(z * f32(4.0)) + f32(64.0))) & 0xFFFFFFFF
+        s = pcg(s)
+        jx = f32(s) / f32(4294967295.0)
+        s = pcg(s)
+        jy = f32(s) / f32(4294967295.0)
+        qx, qy = x - f32(0.1) * jx, y - f32(0.1) * jy
+        r = f32(0.5) if qx > 0 else f32(0.45)
+        want = np.sqrt(f32(qx * qx + qy * qy) + z * z, dtype=np.float32) - r
+        assert abs(f(float(x), float(y), float(z)) - want) <= 1e-6 * max(1.0, abs(want))
