@@ -1452,3 +1452,61 @@ void pto_fn_rotation(const float* angle3, float* out9) {
     const vec3 cols[3] = {m.c0, m.c1, m.c2};
     for (int j = 0; j < 3; j++) out9[3 * j] = cols[j].x, out9[3 * j + 1] = cols[j].y, out9[3 * j + 2] = cols[j].z;
 }
+
+/* The analytic intersections (SC:263-448, SC:633-679) for the same tests.
+ * ray6 = origin, dir; hit6 = hitdist (in: the closest so far), normal,
+ * materialID, lightID (updated on a hit).  Object arrays follow the
+ * shader's struct fields in order, ids as floats. */
+static Ray ray_of(const float* r) { Ray ray; ray.origin = mk3(r[0], r[1], r[2]); ray.dir = mk3(r[3], r[4], r[5]); return ray; }
+static hit_t hit_of(const float* h) {
+    hit_t t;
+    t.hitdist = h[0], t.normal = mk3(h[1], h[2], h[3]), t.materialID = h[4], t.lightID = h[5];
+    return t;
+}
+static void put_hit(float* h, hit_t t) {
+    h[0] = t.hitdist, h[1] = t.normal.x, h[2] = t.normal.y, h[3] = t.normal.z, h[4] = t.materialID, h[5] = t.lightID;
+}
+int pto_fn_bounding_sphere(const float* ray6, const float* pos3, float radius2) {
+    return BoundingSphere(ray_of(ray6), mk3(pos3[0], pos3[1], pos3[2]), radius2);
+}
+void pto_fn_aabb(const float* origin3, const float* invdir3, const float* pos3, const float* size3, float* out2) {
+    vec2 v = RayIntersectAABB(mk3(origin3[0], origin3[1], origin3[2]), mk3(invdir3[0], invdir3[1], invdir3[2]),
+                              mk3(pos3[0], pos3[1], pos3[2]), mk3(size3[0], size3[1], size3[2]));
+    out2[0] = v.x, out2[1] = v.y;
+}
+int pto_fn_sphere(const float* ray6, const float* o, float* hit6) {
+    sphere_t s = {mk3(o[0], o[1], o[2]), o[3], (int)o[4], (int)o[5]};
+    hit_t h = hit_of(hit6);
+    int r = SphereIntersection(ray_of(ray6), s, &h);
+    put_hit(hit6, h);
+    return r;
+}
+int pto_fn_plane(const float* ray6, const float* o, float* hit6) {
+    plane_t p = {mk3(o[0], o[1], o[2]), (int)o[3], (int)o[4]};
+    hit_t h = hit_of(hit6);
+    int r = PlaneIntersection(ray_of(ray6), p, &h);
+    put_hit(hit6, h);
+    return r;
+}
+int pto_fn_box(const float* ray6, const float* o, float* hit6) {
+    box_t b = {mk3(o[0], o[1], o[2]), mk3(o[3], o[4], o[5]), mk3(o[6], o[7], o[8]), (int)o[9], (int)o[10]};
+    hit_t h = hit_of(hit6);
+    int r = BoxIntersection(ray_of(ray6), b, &h);
+    put_hit(hit6, h);
+    return r;
+}
+int pto_fn_lens(const float* ray6, const float* o, float* hit6, int* isOutside) {
+    lens_t l = {mk3(o[0], o[1], o[2]), mk3(o[3], o[4], o[5]), o[6], o[7], o[8], (int)o[9], (int)o[10], (int)o[11]};
+    hit_t h = hit_of(hit6);
+    int r = LensIntersection(ray_of(ray6), l, &h, isOutside);
+    put_hit(hit6, h);
+    return r;
+}
+int pto_fn_cyclide(const float* ray6, const float* o, float* hit6) {
+    cyclide_t c = {mk3(o[0], o[1], o[2]), mk3(o[3], o[4], o[5]), mk3(o[6], o[7], o[8]), o[9], o[10], o[11], o[12],
+                   o[13], (int)o[14], (int)o[15]};
+    hit_t h = hit_of(hit6);
+    int r = DupinCyclide(ray_of(ray6), c, &h);
+    put_hit(hit6, h);
+    return r;
+}

@@ -96,6 +96,13 @@ void pto_fn_smin2(const float* x2, const float* y2, float* out2);
 int pto_fn_solve_cubic(float b, float c, float d, float* roots3);
 void pto_fn_solve_quartic(float a, float b, float c, float d, float e, float* roots4, int* real4);
 void pto_fn_rotation(const float* angle3, float* out9);
+int pto_fn_bounding_sphere(const float* ray6, const float* pos3, float radius2);
+void pto_fn_aabb(const float* origin3, const float* invdir3, const float* pos3, const float* size3, float* out2);
+int pto_fn_sphere(const float* ray6, const float* sphere6, float* hit6);
+int pto_fn_plane(const float* ray6, const float* plane5, float* hit6);
+int pto_fn_box(const float* ray6, const float* box11, float* hit6);
+int pto_fn_lens(const float* ray6, const float* lens12, float* hit6, int* isOutside);
+int pto_fn_cyclide(const float* ray6, const float* cyclide16, float* hit6);
 /* CPU functions of a PT_SDF_CUSTOM slot (the compiled translation of its GLSL). */
 int pto_set_user_sdf(int slot, float (*sdf)(float, float, float), float (*material)(float, float, float));
 

@@ -3,8 +3,9 @@ compute shader (src/shader.comp of the reference tree), compiled for the CPU.
 
 TEST INFRASTRUCTURE ONLY.  The reference cannot run here (it is a Vulkan
 program), but its shader functions that need no scene buffers (RNG, sampling,
-spectra, refraction, MIS, the polynomial solvers, the rotation matrix, smin)
-are plain GLSL: this recipe cuts them out of the reference source at build
+spectra, refraction, MIS, the polynomial solvers, the rotation matrix, smin,
+and the analytic intersections with the structs they take) are plain GLSL:
+this recipe cuts them out of the reference source at build
 time, turns the source's numeric #defines into constants and its push
 constants into variables, runs the text through the repository's GLSL
 translator (pt_glsl_translate) and compiles it over pt_glsl_shim.h with g++
@@ -36,8 +37,12 @@ FUNCTIONS = [
     "CosineDirectionPDF", "SampleCosineUnitCone", "CosineUnitConePDF", "SpectralPowerDistribution",
     "BlackBodyRadiation", "BlackBodyRadiationPeak", "RefractiveIndexWavelength", "RefractiveIndexBK7Glass",
     "OrthonormalBasis", "ToWorld", "MISPowerHeuristicsBeta2", "EvalQuadratic", "EvalCubic",
-    "EvalQuartic", "SolveCubic", "SolveQuartic", "minMaterial", "smin", "RotationMatrix",
+    "EvalQuartic", "SolveCubic", "SolveQuartic", "minMaterial", "smin", "RotationMatrix", "SortMinMax",
+    "BoundingSphere", "RayIntersectAABB", "SphereIntersection", "PlaneIntersection", "BoxIntersection",
+    "SphereSliceIntersection", "LensIntersection", "DupinCyclide",
 ]
+# The shader's structs those functions take.
+STRUCTS = ["Ray", "sphere", "plane", "box", "sphereSlice", "lens", "cyclide"]
 
 # C entry points (refsh_*) over the translated functions (namespace ptg::ref_).
 WRAPPERS = r"""
@@ -127,6 +132,93 @@ void refsh_rotation(const float* angle, float* o) {
     const vec3 c[3] = {m.c0, m.c1, m.c2};
     for (int j = 0; j < 3; j++) o[3 * j] = c[j].x, o[3 * j + 1] = c[j].y, o[3 * j + 2] = c[j].z;
 }
+static Ray ray_of(const float* r) {
+    Ray ray;
+    ray.origin = vec3(r[0], r[1], r[2]);
+    ray.dir = vec3(r[3], r[4], r[5]);
+    return ray;
+}
+// hit = hitdist, normal, materialID, lightID: the inout arguments of an intersection
+struct Hit {
+    float d;
+    vec3 n;
+    float m, l;
+    explicit Hit(const float* h) : d(h[0]), n(h[1], h[2], h[3]), m(h[4]), l(h[5]) {}
+    void put(float* h) const { h[0] = d, h[1] = n.x, h[2] = n.y, h[3] = n.z, h[4] = m, h[5] = l; }
+};
+int refsh_bounding_sphere(const float* r, const float* pos, float radius2) {
+    return ref_BoundingSphere(ray_of(r), vec3(pos[0], pos[1], pos[2]), radius2);
+}
+void refsh_aabb(const float* origin, const float* invdir, const float* pos, const float* size, float* o) {
+    box b;
+    b.pos = vec3(pos[0], pos[1], pos[2]);
+    b.size = vec3(size[0], size[1], size[2]);
+    const vec2 v = ref_RayIntersectAABB(vec3(origin[0], origin[1], origin[2]), vec3(invdir[0], invdir[1], invdir[2]), b);
+    o[0] = v.x, o[1] = v.y;
+}
+int refsh_sphere(const float* r, const float* o, float* h) {
+    sphere s;
+    s.pos = vec3(o[0], o[1], o[2]);
+    s.radius = o[3];
+    s.materialID = (int)o[4];
+    s.lightID = (int)o[5];
+    Hit t(h);
+    const bool hit = ref_SphereIntersection(ray_of(r), s, t.d, t.n, t.m, t.l);
+    t.put(h);
+    return hit;
+}
+int refsh_plane(const float* r, const float* o, float* h) {
+    plane p;
+    p.pos = vec3(o[0], o[1], o[2]);
+    p.materialID = (int)o[3];
+    p.lightID = (int)o[4];
+    Hit t(h);
+    const bool hit = ref_PlaneIntersection(ray_of(r), p, t.d, t.n, t.m, t.l);
+    t.put(h);
+    return hit;
+}
+int refsh_box(const float* r, const float* o, float* h) {
+    box b;
+    b.pos = vec3(o[0], o[1], o[2]);
+    b.rotation = vec3(o[3], o[4], o[5]);
+    b.size = vec3(o[6], o[7], o[8]);
+    b.materialID = (int)o[9];
+    b.lightID = (int)o[10];
+    Hit t(h);
+    const bool hit = ref_BoxIntersection(ray_of(r), b, t.d, t.n, t.m, t.l);
+    t.put(h);
+    return hit;
+}
+int refsh_lens(const float* r, const float* o, float* h, int* isOutside) {
+    lens l;
+    l.pos = vec3(o[0], o[1], o[2]);
+    l.rotation = vec3(o[3], o[4], o[5]);
+    l.radius = o[6];
+    l.focalLength = o[7];
+    l.thickness = o[8];
+    l.isConverging = o[9] != 0.0f;
+    l.materialID = (int)o[10];
+    l.lightID = (int)o[11];
+    Hit t(h);
+    int out = *isOutside;
+    const bool hit = ref_LensIntersection(ray_of(r), l, t.d, t.n, out, t.m, t.l);
+    t.put(h);
+    *isOutside = out;
+    return hit;
+}
+int refsh_cyclide(const float* r, const float* o, float* h) {
+    cyclide c;
+    c.pos = vec3(o[0], o[1], o[2]);
+    c.rotation = vec3(o[3], o[4], o[5]);
+    c.scale = vec3(o[6], o[7], o[8]);
+    c.a = o[9], c.b = o[10], c.c = o[11], c.d = o[12], c.brad = o[13];
+    c.materialID = (int)o[14];
+    c.lightID = (int)o[15];
+    Hit t(h);
+    const bool hit = ref_DupinCyclide(ray_of(r), c, t.d, t.n, t.m, t.l);
+    t.put(h);
+    return hit;
+}
 }
 """
 
@@ -151,6 +243,11 @@ def extract(src: str) -> str:
         kind = "float" if re.search(r"[.eE]", value) else "int"
         out.append(f"const {kind} {name} = {value};")
     out.append("int frame = 0;\nint samplesPerFrame = 1;\nivec2 resolution = ivec2(0);")
+    for name in STRUCTS:
+        m = re.search(r"^struct\s+" + name + r"\s*\{.*?\};", src, re.M | re.S)
+        if not m:
+            raise ValueError(f"struct {name} not found in the shader source")
+        out.append(m.group(0))
     starts = []
     for name in FUNCTIONS:
         found = [m.start() for m in re.finditer(r"^\w+\s+" + name + r"\s*\(", src, re.M)]

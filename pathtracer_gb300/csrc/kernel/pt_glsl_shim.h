@@ -9,11 +9,12 @@
 // access, read swizzles as member calls, swizzle assignment through set_<sw>
 // members, arithmetic with vectors and scalars), uvec2/ivec2 and
 // bvec2/bvec3/bvec4 (constructors, components), mat2/mat3 (constructors
-// from columns or scalars, matrix * vector, mat3 * mat3), and the built-ins
+// from columns or scalars, matrix * vector, mat3 * mat3), vector indexing
+// v[i], structs (declared in the snippet), and the built-ins
 // abs sign floor ceil fract round trunc mod min max clamp mix step
 // smoothstep sqrt inversesqrt pow exp exp2 log log2 sin cos tan asin acos
 // atan (one and two arguments) length distance dot cross normalize reflect
-// fma radians degrees, plus the shader's smin for floats and vec2.
+// fma radians degrees faceforward, plus the shader's smin for floats and vec2.
 #pragma once
 
 #if defined(__CUDACC__)
@@ -36,6 +37,8 @@ struct vec4;
 
 struct vec2 {
     float x, y;
+    PTG_M float& operator[](int i) { return i == 0 ? x : y; }
+    PTG_M float operator[](int i) const { return i == 0 ? x : y; }
     PTG_M vec2() : x(0.0f), y(0.0f) {}
     PTG_M explicit vec2(float s) : x(s), y(s) {}
     PTG_M vec2(float a, float b) : x(a), y(b) {}
@@ -49,6 +52,8 @@ struct vec2 {
 
 struct vec3 {
     float x, y, z;
+    PTG_M float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+    PTG_M float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
     PTG_M vec3() : x(0.0f), y(0.0f), z(0.0f) {}
     PTG_M explicit vec3(float s) : x(s), y(s), z(s) {}
     PTG_M vec3(float a, float b, float c) : x(a), y(b), z(c) {}
@@ -70,6 +75,8 @@ struct vec3 {
 
 struct vec4 {
     float x, y, z, w;
+    PTG_M float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+    PTG_M float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
     PTG_M vec4() : x(0.0f), y(0.0f), z(0.0f), w(0.0f) {}
     PTG_M explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
     PTG_M vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
@@ -107,12 +114,14 @@ struct bvec2 {
 };
 struct bvec3 {
     bool x, y, z;
+    PTG_M bool operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
     PTG_M bvec3() : x(false), y(false), z(false) {}
     PTG_M explicit bvec3(bool s) : x(s), y(s), z(s) {}
     PTG_M bvec3(bool a, bool b, bool c) : x(a), y(b), z(c) {}
 };
 struct bvec4 {
     bool x, y, z, w;
+    PTG_M bool operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
     PTG_M bvec4() : x(false), y(false), z(false), w(false) {}
     PTG_M explicit bvec4(bool s) : x(s), y(s), z(s), w(s) {}
     PTG_M bvec4(bool a, bool b, bool c, bool d) : x(a), y(b), z(c), w(d) {}
@@ -268,6 +277,7 @@ PTG_FN vec3 cross(vec3 a, vec3 b) {
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
 template <typename V> PTG_FN V reflect(V i, V n) { return i - 2.0f * dot(n, i) * n; }
+template <typename V> PTG_FN V faceforward(V n, V i, V nref) { return dot(nref, i) < 0.0f ? n : -n; }
 
 struct mat2 {
     vec2 c0, c1;
@@ -289,6 +299,7 @@ PTG_FN vec3 operator*(mat3 m, vec3 v) {
 }
 PTG_FN vec3 operator*(vec3 v, mat3 m) { return vec3(dot(v, m.c0), dot(v, m.c1), dot(v, m.c2)); }
 PTG_FN mat3 operator*(mat3 a, mat3 b) { return mat3(a * b.c0, a * b.c1, a * b.c2); }
+PTG_FN vec3& operator*=(vec3& v, mat3 m) { return v = v * m; }
 
 // The shader's polynomial smooth minimum (src/shader.comp:686-702), k = 0.02 * 6,
 // with its ONEBYTHREE constant (src/shader.comp:10).

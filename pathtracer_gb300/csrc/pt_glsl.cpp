@@ -21,9 +21,11 @@
 //     marked as a device function, and the whole text goes into namespace
 //     ptg::<prefix>, so several snippets (or one in several slots) coexist;
 //   - top-level `const float|int` declarations become constexpr.
-// Anything the shim does not cover (structs, uniforms, preprocessor lines,
-// arrays of vectors at file scope...) is rejected with a message instead of
-// being guessed at.
+//   - struct declarations pass through (C++ reads them the same way), and
+//     their names count as types from then on.
+// Anything the shim does not cover (uniforms, preprocessor lines, arrays of
+// vectors at file scope...) is rejected with a message instead of being
+// guessed at.
 #include <cctype>
 #include <cstring>
 #include <set>
@@ -151,6 +153,24 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
     std::string e;
     if (!tokenize(glsl, t, e)) return fail(e);
 
+    // Struct types the snippet declares (`struct Name {` at file scope), and
+    // their member names (a member called r, g, b or a keeps its name).
+    std::set<std::string> structs, members;
+    for (size_t i = 0; i < t.size(); i++)
+        if (t[i].kind == Tok::Ident && t[i].text == "struct") {
+            const size_t j = next_nonspace(t, i + 1);
+            if (j >= t.size() || t[j].kind != Tok::Ident) return fail("a struct needs a name");
+            structs.insert(t[j].text);
+            size_t q = next_nonspace(t, j + 1);
+            if (q >= t.size() || t[q].text != "{") return fail("a struct needs a body");
+            for (size_t prev = q; q < t.size() && t[q].text != "}"; q++) {
+                if (t[q].kind == Tok::Space) continue;
+                if (t[q].text == ";" && t[prev].kind == Tok::Ident) members.insert(t[prev].text);
+                prev = q;
+            }
+        }
+    auto type_like = [&](const std::string& w) { return is_type(w) || structs.count(w) != 0; };
+
     // Functions the snippet defines: `type name (` at brace depth 0, and
     // those of them with out/inout parameters (calls with side effects).
     std::set<std::string> funcs, effect_funcs;
@@ -163,9 +183,9 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
             continue;
         }
         if (t[i].kind != Tok::Ident) continue;
-        if (t[i].text == "struct" || t[i].text == "uniform" || t[i].text == "layout" || t[i].text == "buffer")
+        if (t[i].text == "uniform" || t[i].text == "layout" || t[i].text == "buffer")
             return fail("'" + t[i].text + "' is not supported in an SDF snippet");
-        if (depth == 0 && is_type(t[i].text)) {
+        if (depth == 0 && type_like(t[i].text)) {
             const size_t j = next_nonspace(t, i + 1);
             const size_t k = j < t.size() ? next_nonspace(t, j + 1) : t.size();
             if (j < t.size() && t[j].kind == Tok::Ident && k < t.size() && t[k].text == "(") {
@@ -249,8 +269,9 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
                     continue;
                 }
                 // single components: .r .g .b .a name the fields x y z w
+                // (unless a struct of the snippet has a member of that name)
                 if (j < t.size() && t[j].kind == Tok::Ident && t[j].text.size() == 1 &&
-                    std::strchr("rgba", t[j].text[0])) {
+                    std::strchr("rgba", t[j].text[0]) && !members.count(t[j].text)) {
                     o += "." + rgba_to_xyzw(t[j].text);
                     i = j;
                     continue;
@@ -274,7 +295,7 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
             }
             return fail("file-scope constants must be float or int");
         }
-        if (depth == 0 && paren == 0 && is_type(w)) {
+        if (depth == 0 && paren == 0 && type_like(w)) {
             const size_t j = next_nonspace(t, i + 1);
             const size_t n2 = j < t.size() ? next_nonspace(t, j + 1) : t.size();
             if (j < t.size() && t[j].kind == Tok::Ident && funcs.count(t[j].text) && n2 < t.size() && t[n2].text == "(")
@@ -284,7 +305,7 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
             o += std::string(prefix) + w;
             continue;
         }
-        if (is_type(w) && w != "void" && !effect_funcs.empty()) {
+        if (type_like(w) && w != "void" && !effect_funcs.empty()) {
             // a constructor call: count its arguments that call a function with side effects
             const size_t open = next_nonspace(t, i + 1);
             if (open < t.size() && t[open].text == "(") {
@@ -315,7 +336,7 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
             }
         }
         o += w;
-        if (ref_pending && is_type(w)) {
+        if (ref_pending && type_like(w)) {
             o += "&";
             ref_pending = false;
         }

@@ -78,7 +78,8 @@ def test_translation_rewrites_glsl(pt):
 
 
 @pytest.mark.parametrize("text,why", [
-    ("struct S { float a; }; float sdf(vec3 p){return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "struct"),
+    ("layout(std430) buffer B { float a; }; float sdf(vec3 p){return 0.0;} float sdfmaterial(vec3 p){return 0.0;}",
+     "layout"),
     ("uniform float t; float sdf(vec3 p){return t;} float sdfmaterial(vec3 p){return 0.0;}", "uniform"),
     ("#define K 2.0\nfloat sdf(vec3 p){return K;} float sdfmaterial(vec3 p){return 0.0;}", "preprocessor"),
     ("float sdf(vec3 p){(p).xy = vec2(0.0); return 0.0;} float sdfmaterial(vec3 p){return 0.0;}", "swizzle"),

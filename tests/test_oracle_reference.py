@@ -214,3 +214,87 @@ def test_polynomial_solvers(libs):
         real = np.array(list(fa), bool)
         assert (_bits(np.array(list(qa))[real]) == _bits(np.array(list(qb))[real])).all()
     assert 0 < ones < N  # both branches of the cubic ran
+
+
+def _ray(rng):
+    o = rng.uniform(-3.0, 3.0, 3)
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    if rng.uniform() < 0.3:  # aim near the object at the origin region
+        d = -o / np.linalg.norm(o) + rng.normal(0, 0.2, 3)
+        d /= np.linalg.norm(d)
+    return (F * 6)(*np.concatenate([o, d]).astype(np.float32))
+
+
+def _hit(rng):
+    return [float(np.float32(1e5 if rng.uniform() < 0.7 else rng.uniform(0.5, 6.0))), 0.0, 0.0, 0.0, 0.0, -1.0]
+
+
+def _same(fa, fb, ray, obj, rng, extra=False):
+    h0 = _hit(rng)
+    ha, hb = (F * 6)(*h0), (F * 6)(*h0)
+    if extra:
+        oa, ob = ctypes.c_int(1), ctypes.c_int(1)
+        ra, rb = fa(ray, obj, ha, ctypes.byref(oa)), fb(ray, obj, hb, ctypes.byref(ob))
+        assert oa.value == ob.value
+    else:
+        ra, rb = fa(ray, obj, ha), fb(ray, obj, hb)
+    assert ra == rb
+    assert (_bits(list(ha)) == _bits(list(hb))).all()
+    return ra
+
+
+@pytest.mark.parametrize("kind", ["sphere", "plane", "box", "lens", "cyclide"])
+def test_intersections(libs, kind):
+    """SphereIntersection, PlaneIntersection, BoxIntersection (with
+    RotationMatrix), LensIntersection (two sphere slices) and DupinCyclide
+    (the quartic solver): hit flag, distance, normal and ids bit for bit."""
+    o, r = libs
+    rng = np.random.default_rng(10)
+    extra = kind == "lens"
+    args = [FP, FP, FP] + ([IP] if extra else [])
+    fa = _fn(o, f"pto_fn_{kind}", ctypes.c_int, args)
+    fb = _fn(r, f"refsh_{kind}", ctypes.c_int, args)
+    hits = 0
+    for _ in range(N):
+        pos = rng.uniform(-1.0, 1.0, 3)
+        rot = rng.uniform(-180.0, 180.0, 3)
+        ids = [float(rng.integers(1, 6)), float(rng.integers(0, 3))]
+        if kind == "sphere":
+            obj = [*pos, rng.uniform(0.1, 1.5), *ids]
+        elif kind == "plane":
+            obj = [*pos, *ids]
+        elif kind == "box":
+            obj = [*pos, *rot, *rng.uniform(0.2, 2.0, 3), *ids]
+        elif kind == "lens":
+            radius = rng.uniform(0.2, 1.0)
+            obj = [*pos, *rot, radius, rng.uniform(0.6 * radius, 3.0), rng.uniform(0.0, 0.2),
+                   float(rng.integers(0, 2)), *ids]
+        else:
+            a = rng.uniform(0.8, 1.2)
+            obj = [*pos, *rot, *rng.uniform(0.5, 1.5, 3), a, rng.uniform(0.6, 0.95) * a, rng.uniform(0.2, 0.6),
+                   rng.uniform(0.3, 0.6), 3.0, *ids]
+        hits += _same(fa, fb, _ray(rng), (F * len(obj))(*np.asarray(obj, np.float32)), rng, extra)
+    assert N // 50 < hits < N  # both outcomes ran
+
+
+def test_bounds(libs):
+    """BoundingSphere and RayIntersectAABB (with SortMinMax)."""
+    o, r = libs
+    rng = np.random.default_rng(11)
+    bs_a = _fn(o, "pto_fn_bounding_sphere", ctypes.c_int, [FP, FP, F])
+    bs_b = _fn(r, "refsh_bounding_sphere", ctypes.c_int, [FP, FP, F])
+    ab_a = _fn(o, "pto_fn_aabb", None, [FP, FP, FP, FP, FP])
+    ab_b = _fn(r, "refsh_aabb", None, [FP, FP, FP, FP, FP])
+    for _ in range(N):
+        ray = _ray(rng)
+        pos = (F * 3)(*rng.uniform(-1.0, 1.0, 3).astype(np.float32))
+        r2 = float(np.float32(rng.uniform(0.01, 4.0)))
+        assert bs_a(ray, pos, r2) == bs_b(ray, pos, r2)
+        d = np.array(list(ray)[3:], np.float32)
+        inv = (F * 3)(*(np.float32(1.0) / d))
+        size = (F * 3)(*rng.uniform(0.2, 2.0, 3).astype(np.float32))
+        oa, ob = (F * 2)(), (F * 2)()
+        ab_a(ray, inv, pos, size, oa)
+        ab_b(ray, inv, pos, size, ob)
+        assert (_bits(list(oa)) == _bits(list(ob))).all()
