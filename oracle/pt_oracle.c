@@ -1510,3 +1510,25 @@ int pto_fn_cyclide(const float* ray6, const float* o, float* hit6) {
     put_hit(hit6, h);
     return r;
 }
+
+/* Intersection (SC:862-934) of one ray with a whole packed scene, SDFs
+ * included: out6 = hitdist, normal, materialID, lightID as TraceRay sees them
+ * (hitdist MAXDIST for no hit). */
+void pto_fn_intersection(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plugins, int nplugins,
+                         const float* ray6, float* out6) {
+    ctx_t c;
+    memset(&c, 0, sizeof(c));
+    c.u = ubo;
+    c.pc = pc;
+    c.plug = plugins;
+    c.nplug = nplugins;
+    c.cameraPos = mk3(pc->cameraPosX, pc->cameraPosY, pc->cameraPosZ);
+    hit_t h;
+    h.hitdist = MAXDIST;
+    h.normal = mk3(0.0f, 0.0f, 0.0f);
+    h.materialID = 0.0f;
+    h.lightID = -1.0f;
+    int objectID = -1;
+    IntersectAll(&c, ray_of(ray6), &h, &objectID);
+    put_hit(out6, h);
+}

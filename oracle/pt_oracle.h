@@ -103,6 +103,8 @@ int pto_fn_plane(const float* ray6, const float* plane5, float* hit6);
 int pto_fn_box(const float* ray6, const float* box11, float* hit6);
 int pto_fn_lens(const float* ray6, const float* lens12, float* hit6, int* isOutside);
 int pto_fn_cyclide(const float* ray6, const float* cyclide16, float* hit6);
+void pto_fn_intersection(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plugins, int nplugins,
+                         const float* ray6, float* out6);
 /* CPU functions of a PT_SDF_CUSTOM slot (the compiled translation of its GLSL). */
 int pto_set_user_sdf(int slot, float (*sdf)(float, float, float), float (*material)(float, float, float));
 

@@ -299,5 +299,202 @@ def load(reference: str | None = None) -> ctypes.CDLL:
     return ctypes.CDLL(build(reference))
 
 
+# ---- the whole path tracer: Scene() of the shader for one sample ---------
+
+# The uniform buffer and the push constants (src/shader.comp:19-52) as
+# variables of the translated unit.  Buffer reads outside an array give 0,
+# as robust buffer access does on the device (the oracle reads them the same
+# way).
+SCENE_PRELUDE = r"""
+#include <stdint.h>
+#include <string.h>
+#include "pt_cuda.h"
+#include "pt_glsl_shim.h"
+namespace ptg {
+namespace rs_ {
+template <int N> struct Robust {
+    float v[N];
+    float operator[](int i) const { return (i >= 0 && i < N) ? v[i] : 0.0f; }
+};
+Robust<7> numObjects;
+Robust<PT_MAX_OBJECTS_SIZE> objects;
+Robust<PT_MAX_SDFS_SIZE> sdfs;
+Robust<PT_MAX_MATERIALS_SIZE> materials;
+Robust<PT_MAX_LIGHTS_SIZE> lights;
+Robust<PT_MAX_LIGHTIDS_SIZE> lightIDs;
+Robust<PT_CIE_TABLE_SIZE> CIEXYZ1931;
+ivec2 resolution;
+int frame, currentSamples, samplesPerFrame;
+float FPS, persistence;
+int pathLength;
+vec2 cameraAngle;
+float cameraPosX, cameraPosY, cameraPosZ;
+int ISO;
+float cameraSize, apertureSize, apertureDist, lensRadius, lensFocalLength, lensThickness, lensDistance;
+int tonemap;
+}  // namespace rs_
+}  // namespace ptg
+"""
+
+SCENE_WRAPPERS = r"""
+using namespace ptg;
+using namespace ptg::rs_;
+extern "C" {
+// Binds a packed scene (pt_ubo) and the push constants (pt_push), as the
+// descriptor set and vkCmdPushConstants do.
+void refsc_bind(const pt_ubo* u, const pt_push* pc) {
+    memcpy(numObjects.v, u->numObjects, sizeof numObjects.v);
+    memcpy(objects.v, u->objects, sizeof objects.v);
+    memcpy(sdfs.v, u->sdfs, sizeof sdfs.v);
+    memcpy(materials.v, u->materials, sizeof materials.v);
+    memcpy(lights.v, u->lights, sizeof lights.v);
+    memcpy(lightIDs.v, u->lightIDs, sizeof lightIDs.v);
+    memcpy(CIEXYZ1931.v, u->CIEXYZ1931, sizeof CIEXYZ1931.v);
+    resolution = ivec2(pc->resolution[0], pc->resolution[1]);
+    frame = pc->frame, currentSamples = pc->currentSamples, samplesPerFrame = pc->samplesPerFrame;
+    FPS = pc->FPS, persistence = pc->persistence, pathLength = pc->pathLength;
+    cameraAngle = vec2(pc->cameraAngle[0], pc->cameraAngle[1]);
+    cameraPosX = pc->cameraPosX, cameraPosY = pc->cameraPosY, cameraPosZ = pc->cameraPosZ;
+    ISO = pc->ISO;
+    cameraSize = pc->cameraSize, apertureSize = pc->apertureSize, apertureDist = pc->apertureDist;
+    lensRadius = pc->lensRadius, lensFocalLength = pc->lensFocalLength, lensThickness = pc->lensThickness;
+    lensDistance = pc->lensDistance, tonemap = pc->tonemap;
+    cameraPos = vec3(cameraPosX, cameraPosY, cameraPosZ);  // the shader's per-invocation global
+}
+// Scene() for invocation (x, y) and sample k, with the pixel mapping of
+// Rendering (src/shader.comp:1509-1511).
+void refsc_scene(uint32_t x, uint32_t y, int k, float* out3) {
+    const uvec2 xy = uvec2(x, (uint)resolution.y - y);
+    const vec2 uv = (2.0f * vec2((float)xy.x, (float)xy.y) - vec2((float)resolution.x, (float)resolution.y)) /
+                    (float)resolution.y;
+    const vec3 c = rs_Scene(xy, uv, k);
+    out3[0] = c.x, out3[1] = c.y, out3[2] = c.z;
+}
+// Intersection() of one ray: out6 = hitdist, normal, materialID, lightID.
+void refsc_intersection(const float* r, float* out6) {
+    Ray ray;
+    ray.origin = vec3(r[0], r[1], r[2]);
+    ray.dir = vec3(r[3], r[4], r[5]);
+    vec3 normal = vec3(0.0f);
+    float materialID = 0.0f, lightID = -1.0f;
+    const float d = rs_Intersection(ray, normal, materialID, lightID);
+    out6[0] = d, out6[1] = normal.x, out6[2] = normal.y, out6[3] = normal.z, out6[4] = materialID, out6[5] = lightID;
+}
+}
+"""
+
+
+def extract_scene(src: str) -> str:
+    """The shader without its interface and entry points: the #version,
+    #extension, precision and layout lines, the uniform and push-constant
+    blocks (SCENE_PRELUDE declares them) and Accumulate, Rendering and main
+    (they read and write the texel buffer) are left out; numeric #defines
+    become constants."""
+    text = src
+    for pat in (r"^#version[^\n]*\n", r"^#extension[^\n]*\n", r"^precision[^\n]*\n", r"^layout\([^)]*\)\s*in;\s*\n",
+                r"^layout\([^)]*\)\s*uniform\s+\w+\s*\{.*?\};", r"^layout\([^)]*\)\s*uniform\s+imageBuffer[^;]*;"):
+        text = re.sub(pat, "", text, flags=re.M | re.S)
+    consts = []
+
+    def define(m):
+        value = m.group(2)
+        kind = "float" if re.search(r"[.eE]", value) else "int"
+        consts.append(f"const {kind} {m.group(1)} = {value};")
+        return ""
+
+    text = re.sub(r"^#define\s+(\w+)\s+([-+0-9.eE]+)\s*$", define, text, flags=re.M)
+    for name in ("Accumulate", "Rendering", "main"):
+        m = re.search(r"^\w+\s+" + name + r"\s*\(", text, re.M)
+        if not m:
+            raise ValueError(f"{name} not found in the shader source")
+        depth, i = 0, text.index("{", m.start())
+        while True:
+            depth += (text[i] == "{") - (text[i] == "}")
+            if depth == 0:
+                break
+            i += 1
+        text = text[:m.start()] + text[i + 1:]
+    if "#" in text:
+        raise ValueError("a preprocessor line is left in the shader text")
+    return "\n".join(consts) + "\n" + text + "\nfloat sdf(vec3 p) { return 0.0; }\nfloat sdfmaterial(vec3 p) { return 0.0; }\n"
+
+
+def splice_sdfs(src: str, texts: list[str]) -> str:
+    """The shader with a scene's SDF snippets spliced in, as the reference's
+    host does before compiling it (InsertSDF, src/pathtracer.cpp:2004-2054):
+    snippet i (1-based n) has its first "sdf" renamed SDFn and then its first
+    "sdfmaterial" SDFnMATERIAL, and goes after the "All SDF Are Inserted
+    Here" comment; SDF() gains `if ((set1 & 2^i) == 2^i) sdf = min(sdf,
+    SDFn(p - pos_i));` and SDFMATERIAL() the material line
+    `sdfmaterial = minMaterial(sdf, SDFn(p - pos_i), sdfmaterial,
+    SDFnMATERIAL(p - pos_i));` followed by the same distance line, snippet 0
+    first.  (The host inserts at character offsets that land after those
+    comment lines with CRLF line ends; here the text goes after the comment
+    line, the same place.)"""
+    code = src
+
+    def after_line(marker):
+        j = code.find(marker)
+        if j < 0:
+            raise ValueError(f"marker {marker!r} not found")
+        return j + len(marker)
+
+    for i in reversed(range(len(texts))):
+        t = texts[i]
+        n = str(i + 1)
+        bit = str(1 << (i % 32))
+        j = t.find("sdf")
+        t = t[:j] + "SDF" + n + t[j + 3:]
+        j = t.find("sdfmaterial")
+        t = t[:j] + "SDF" + n + "MATERIAL" + t[j + 11:] + "\n"
+        pos = f"(p - vec3(sdfs[{6 * i}], sdfs[{6 * i + 1}], sdfs[{6 * i + 2}]))"
+        test = f"\n    if ((set{i // 32 + 1} & {bit}) == {bit}) sdf"
+        dist = test + f" = min(sdf, SDF{n}{pos});"
+        mat = test + f"material = minMaterial(sdf, SDF{n}{pos}, sdfmaterial, SDF{n}MATERIAL{pos});"
+        k = after_line("// Put SDF Functions Here")
+        code = code[:k] + dist + code[k:]
+        k = after_line("// Put SDFMATERIAL Functions Here")
+        code = code[:k] + mat + dist + code[k:]
+        k = after_line("// All SDF Are Inserted Here")
+        code = code[:k] + "\n" + t + code[k:]
+    return code
+
+
+def build_scene(reference: str | None = None, sdf_texts: list[str] | None = None) -> str:
+    """Builds (when the shader source is newer) the shader's path tracer for a
+    scene's SDF snippets (none: the SDF hooks stay empty, as in the source)."""
+    import hashlib
+
+    shader = shader_path(reference)
+    if not os.path.exists(shader):
+        raise FileNotFoundError(shader)
+    texts = list(sdf_texts or [])
+    key = hashlib.sha1("\0".join(texts).encode()).hexdigest()[:12] if texts else "nosdf"
+    lib = os.path.join(OUT, f"libref_scene_{key}.so")
+    deps = [shader, __file__, os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel", "pt_glsl_shim.h"),
+            os.path.join(ROOT, "pathtracer_gb300", "csrc", "pt_glsl.cpp"), os.path.join(ROOT, "include", "pt_mathf.h"),
+            os.path.join(ROOT, "include", "pt_cuda.h")]
+    if os.path.exists(lib) and all(os.path.getmtime(d) <= os.path.getmtime(lib) for d in deps):
+        return lib
+    sys.path.insert(0, ROOT)
+    from pathtracer_gb300 import glsl_translate
+
+    with open(shader) as f:
+        code = glsl_translate(extract_scene(splice_sdfs(f.read(), texts)), "rs_")
+    os.makedirs(OUT, exist_ok=True)
+    cpp = os.path.join(OUT, f"ref_scene_{key}.cpp")
+    with open(cpp, "w") as f:
+        f.write(SCENE_PRELUDE + code + SCENE_WRAPPERS)
+    subprocess.run([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+                    "-fno-fast-math", "-I", os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel"), "-I",
+                    os.path.join(ROOT, "include"), "-o", lib, cpp], check=True)
+    return lib
+
+
+def load_scene(reference: str | None = None, sdf_texts: list[str] | None = None) -> ctypes.CDLL:
+    return ctypes.CDLL(build_scene(reference, sdf_texts))
+
+
 if __name__ == "__main__":
     print(build(sys.argv[1] if len(sys.argv) > 1 else None))
+    print(build_scene(sys.argv[1] if len(sys.argv) > 1 else None))

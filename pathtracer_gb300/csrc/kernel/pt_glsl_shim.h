@@ -14,7 +14,8 @@
 // abs sign floor ceil fract round trunc mod min max clamp mix step
 // smoothstep sqrt inversesqrt pow exp exp2 log log2 sin cos tan asin acos
 // atan (one and two arguments) length distance dot cross normalize reflect
-// fma radians degrees faceforward, plus the shader's smin for floats and vec2.
+// fma radians degrees faceforward refract, plus the shader's smin for floats
+// and vec2.
 #pragma once
 
 #if defined(__CUDACC__)
@@ -48,6 +49,10 @@ struct vec2 {
     PTG_M vec2 xy() const { return vec2(x, y); }
     PTG_M vec2 yx() const { return vec2(y, x); }
     PTG_M vec2 yy() const { return vec2(y, y); }
+#define PTG_V2S3(A, B, C) PTG_M vec3 A##B##C() const;
+    PTG_V2S3(x, x, x) PTG_V2S3(x, x, y) PTG_V2S3(x, y, x) PTG_V2S3(x, y, y) PTG_V2S3(y, x, x) PTG_V2S3(y, x, y)
+    PTG_V2S3(y, y, x) PTG_V2S3(y, y, y)
+#undef PTG_V2S3
 };
 
 struct vec3 {
@@ -91,6 +96,11 @@ struct vec4 {
 };
 PTG_M void vec2::set_xy(vec2 v) { x = v.x; y = v.y; }
 PTG_M void vec2::set_yx(vec2 v) { y = v.x; x = v.y; }
+#define PTG_V2S3(A, B, C) \
+    PTG_M vec3 vec2::A##B##C() const { return vec3(A, B, C); }
+PTG_V2S3(x, x, x) PTG_V2S3(x, x, y) PTG_V2S3(x, y, x) PTG_V2S3(x, y, y) PTG_V2S3(y, x, x) PTG_V2S3(y, x, y)
+PTG_V2S3(y, y, x) PTG_V2S3(y, y, y)
+#undef PTG_V2S3
 
 // Integer and boolean vectors: constructors and components (GLSL's
 // arithmetic on them is not covered).
@@ -164,6 +174,17 @@ PTG_OPS(vec4, PTG_E4)
 PTG_FN vec2 operator-(vec2 a) { return vec2(-a.x, -a.y); }
 PTG_FN vec3 operator-(vec3 a) { return vec3(-a.x, -a.y, -a.z); }
 PTG_FN vec4 operator-(vec4 a) { return vec4(-a.x, -a.y, -a.z, -a.w); }
+
+// An integer vector in arithmetic with a float vector converts to it.
+PTG_FN vec2 to_vec2(ivec2 v) { return vec2((float)v.x, (float)v.y); }
+PTG_FN vec2 operator+(vec2 a, ivec2 b) { return a + to_vec2(b); }
+PTG_FN vec2 operator-(vec2 a, ivec2 b) { return a - to_vec2(b); }
+PTG_FN vec2 operator*(vec2 a, ivec2 b) { return a * to_vec2(b); }
+PTG_FN vec2 operator/(vec2 a, ivec2 b) { return a / to_vec2(b); }
+PTG_FN vec2& operator+=(vec2& a, ivec2 b) { return a = a + b; }
+PTG_FN vec2& operator-=(vec2& a, ivec2 b) { return a = a - b; }
+PTG_FN vec2& operator*=(vec2& a, ivec2 b) { return a = a * b; }
+PTG_FN vec2& operator/=(vec2& a, ivec2 b) { return a = a / b; }
 
 // Apply a float function component-wise.
 #define PTG_MAP1(NAME, F)                                                                       \
@@ -278,6 +299,12 @@ PTG_FN vec3 cross(vec3 a, vec3 b) {
 }
 template <typename V> PTG_FN V reflect(V i, V n) { return i - 2.0f * dot(n, i) * n; }
 template <typename V> PTG_FN V faceforward(V n, V i, V nref) { return dot(nref, i) < 0.0f ? n : -n; }
+template <typename V> PTG_FN V refract(V i, V n, float eta) {
+    const float d = dot(n, i);
+    const float k = 1.0f - eta * eta * (1.0f - d * d);
+    if (k < 0.0f) return V(0.0f);
+    return eta * i - (eta * d + sqrtf(k)) * n;
+}
 
 struct mat2 {
     vec2 c0, c1;
@@ -292,6 +319,8 @@ struct mat3 {
     // column-major, as GLSL fills a matrix from scalars
     PTG_M mat3(float a, float b, float c, float d, float e, float f, float g, float h, float i)
         : c0(a, b, c), c1(d, e, f), c2(g, h, i) {}
+    PTG_M vec3& operator[](int j) { return j == 0 ? c0 : (j == 1 ? c1 : c2); }  // column j
+    PTG_M vec3 operator[](int j) const { return j == 0 ? c0 : (j == 1 ? c1 : c2); }
 };
 PTG_FN vec3 operator*(mat3 m, vec3 v) {
     return vec3(m.c0.x * v.x + m.c1.x * v.y + m.c2.x * v.z, m.c0.y * v.x + m.c1.y * v.y + m.c2.y * v.z,

@@ -303,6 +303,10 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
         }
         if (funcs.count(w)) {
             o += std::string(prefix) + w;
+            if (ref_pending && type_like(w)) {  // a struct that shares a function's name
+                o += "&";
+                ref_pending = false;
+            }
             continue;
         }
         if (type_like(w) && w != "void" && !effect_funcs.empty()) {

@@ -1,10 +1,14 @@
-"""The oracle's restatements of single shader functions against the
-reference's own shader source: each function of oracle/ref_shader.py's list is
-cut out of the reference's src/shader.comp, translated and built for the CPU
-(oracle/_ref/libref_shader.so), and must give the oracle's results bit for bit
-on seeded random inputs (RNG streams, sampling, spectra, refraction, MIS, the
-cubic and quartic solvers, the rotation matrix, smin).  Needs the reference
-tree (skipped without it)."""
+"""The oracle against the reference's own shader source (oracle/ref_shader.py
+builds it for the CPU from the reference tree):
+- single functions cut out of src/shader.comp (RNG streams, sampling,
+  spectra, refraction, MIS, the cubic and quartic solvers, the rotation
+  matrix, smin, the analytic intersections) give the oracle's results bit for
+  bit on seeded random inputs;
+- the whole shader without its interface and entry points, with a scene's
+  SDF snippets spliced in as the reference's host does, gives the oracle's
+  XYZ for every sample of the reference's own scene files, and the same
+  Intersection() for rays into each scene.
+Needs the reference tree (skipped without it)."""
 import ctypes
 import os
 
@@ -298,3 +302,114 @@ def test_bounds(libs):
         ab_a(ray, inv, pos, size, oa)
         ab_b(ray, inv, pos, size, ob)
         assert (_bits(list(oa)) == _bits(list(ob))).all()
+
+
+ANALYTIC_SCENES = ["scene0.json", "scene1.json", "scene2.json"]  # the reference's scenes without SDFs
+
+
+def _scene_samples(lib, scene, W, H, spf, cie, plugins=()):
+    """Per-sample XYZ of the reference's own Scene() (all pixels, all samples,
+    in the oracle's trace order) and of the oracle."""
+    from oracle import oracle
+
+    ubo = scene.pack_ubo(cie)
+    push = scene.push_constants(W, H, spf, spf, spf, 8)
+    acc = np.zeros((H, W, 4), np.float32)
+    _, _, col_o = oracle.dispatch(ubo, push, list(plugins), acc, trace_depth=16)
+    lib.refsc_bind.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.refsc_scene.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, FP]
+    lib.refsc_bind(ubo.ctypes.data, ctypes.addressof(push))
+    col_r = np.zeros_like(col_o)
+    out = (F * 3)()
+    p = 0
+    for y in range(H):
+        for x in range(W):
+            for k in range(spf):
+                lib.refsc_scene(x, y, k, out)
+                col_r[p] = list(out)
+                p += 1
+    return col_o, col_r
+
+
+@pytest.mark.parametrize("name", ANALYTIC_SCENES + ["cornell_box"])
+def test_whole_shader_per_sample(built, name):
+    """The reference's whole path tracer (src/shader.comp without its
+    interface and entry points, built for the CPU over the shim, scene buffer
+    and push constants bound like the descriptor set) against the oracle on
+    the reference's own scene files (and the Cornell box): every sample's
+    XYZ bit for bit, through lens refraction, NEE, MIS and Russian roulette."""
+    from conftest import SCENES
+    from pathtracer_gb300 import Scene, cie_analytic
+
+    lib = ref_shader.load_scene(REFERENCE)
+    path = (os.path.join(SCENES, "cornell_box.json") if name == "cornell_box"
+            else os.path.join(REFERENCE, "scenes", name))
+    scene = Scene.load(path)
+    col_o, col_r = _scene_samples(lib, scene, 24, 16, 3, cie_analytic())
+    assert np.isfinite(col_o).all() and col_o.max() > 0
+    bad = np.nonzero((_bits(col_o) != _bits(col_r)).any(axis=1))[0]
+    assert bad.size == 0, (bad[:5], col_o[bad[:3]], col_r[bad[:3]])
+
+
+SDF_SCENES = ["scene3.json", "scene4.json", "scene5.json", "scene6.json", "scene7.json", "scene8.json",
+              "scene9.json", "scene10.json"]
+
+
+@pytest.mark.parametrize("name", SDF_SCENES + ["mandelbulb12_plane"])
+def test_whole_shader_with_spliced_sdfs(built, name):
+    """SDF scenes: the scene's snippet texts spliced into the shader as the
+    reference's host does (InsertSDF), the whole shader built for the CPU,
+    against the oracle with its plug-ins (the shipped snippets) or the C
+    restatement of the text (the bench's 12-iteration mandelbulb): every
+    sample's XYZ bit for bit, through sphere tracing, SDF normals and SDF
+    materials."""
+    from conftest import SCENES
+    from oracle import compare
+    from pathtracer_gb300 import Scene, cie_analytic
+
+    path = (os.path.join(SCENES, name + ".json") if name == "mandelbulb12_plane"
+            else os.path.join(REFERENCE, "scenes", name))
+    scene = Scene.load(path)
+    texts = scene.sdf_sources()
+    assert texts and not any(t.startswith("builtin:") for t in texts)
+    lib = ref_shader.load_scene(REFERENCE, texts)
+    col_o, col_r = _scene_samples(lib, scene, 16, 12, 2, cie_analytic(), compare.plugins_for(scene))
+    assert np.isfinite(col_o).all() and col_o.max() > 0
+    bad = np.nonzero((_bits(col_o) != _bits(col_r)).any(axis=1))[0]
+    assert bad.size == 0, (bad[:5], col_o[bad[:3]], col_r[bad[:3]])
+
+
+@pytest.mark.parametrize("name", ["scene0.json", "scene3.json", "scene8.json", "scene9.json", "scene10.json"])
+def test_whole_scene_intersection(built, name):
+    """Intersection() of the reference's shader (analytic objects, then sphere
+    tracing of the spliced SDFs) against the oracle's on rays aimed into the
+    scene's SDF box (or at its origin): distance, normal and ids bit for bit."""
+    from oracle import compare, oracle
+    from pathtracer_gb300 import Scene, cie_analytic
+    from pathtracer_gb300.native import PtSdfPlugin
+
+    scene = Scene.load(os.path.join(REFERENCE, "scenes", name))
+    ubo = scene.pack_ubo(cie_analytic())
+    push = scene.push_constants(16, 12, 2, 2, 2, 8)
+    plugins = compare.plugins_for(scene)
+    arr = (PtSdfPlugin * max(1, len(plugins)))(*plugins)
+    lib = ref_shader.load_scene(REFERENCE, scene.sdf_sources())
+    lib.refsc_bind.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.refsc_intersection.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.refsc_bind(ubo.ctypes.data, ctypes.addressof(push))
+    o = oracle.lib()
+    o.pto_fn_intersection.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] + [ctypes.c_void_p] * 2
+    box = ubo[7 + 1024:7 + 1024 + 6] if plugins else np.array([0, 0, 0, 2, 2, 2], np.float32)
+    rng = np.random.default_rng(12)
+    hits = 0
+    for _ in range(1500):
+        org = box[:3] + rng.uniform(-6.0, 6.0, 3)
+        d = box[:3] + rng.uniform(-0.5, 0.5, 3) * box[3:] - org
+        d /= np.linalg.norm(d)
+        ray = (F * 6)(*np.concatenate([org, d]).astype(np.float32))
+        a, b = (F * 6)(), (F * 6)()
+        o.pto_fn_intersection(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins), ray, a)
+        lib.refsc_intersection(ray, b)
+        assert (_bits(list(a)) == _bits(list(b))).all(), (list(a), list(b))
+        hits += a[0] < 1e5
+    assert hits > 100
