@@ -40,8 +40,12 @@ and by the plain megakernel, with each pass's relative RMSE against an FP64
 reference (--ref-spp samples per pixel, FP32 paths, FP64 sums).
 
 Under torchrun each rank renders its own replica (distinct sample indices,
-no exchange): weak scaling.  --impl reference times the CPU restatement of
-the reference shader (the reference itself is Vulkan-only) on the host cores.
+no exchange): weak scaling.  --impl reference times the reference's own
+compute shader on the host cores (all threads): its GLSL built for the CPU
+through the repository's translator by oracle/ref_shader.py (made by
+__graft_entry__.build() for the default scene; the reference program itself
+is Vulkan-only), or the CPU restatement of it (oracle/) where that build is
+absent.  The same figure is the `cpu_baseline` of the GPU arm's line.
 """
 from __future__ import annotations
 
@@ -271,26 +275,63 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+def reference_cpu(scene):
+    """The reference's own shader built for the CPU for this scene's SDF texts
+    (oracle/_ref, made by __graft_entry__.build()), or None where it was not
+    built (then the oracle port stands in)."""
+    import ctypes
+
+    from oracle import ref_shader
+
+    texts = scene.sdf_sources()
+    if any(t.startswith("builtin:") for t in texts):
+        return None  # a shipped plug-in named by key: no snippet text to splice
+    try:
+        lib = ctypes.CDLL(ref_shader.build_scene(None, texts))
+    except (FileNotFoundError, OSError, subprocess.CalledProcessError):
+        return None
+    lib.refsc_bind.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.refsc_render_rows.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    return lib
+
+
 def cpu_baseline(args, W, H, spf_total, nthreads):
-    """The CPU restatement (oracle, OpenMP) on a stratified sample of rows."""
+    """Path samples/s on the host cores over a stratified sample of rows: the
+    reference's own shader built for the CPU where it was built ("reference":
+    OpenMP over the rows' pixels), else the oracle (the CPU restatement,
+    "port": one row per call, rows spread over `nthreads` host threads)."""
+    import ctypes
+
     from oracle import compare
     from pathtracer_gb300 import Scene, cie_analytic
 
     scene = Scene.load(scene_path(args.workload))
     cie = cie_analytic()
     ubo = scene.pack_ubo(cie)
-    plugins = compare.plugins_for(scene)
     push = scene.push_constants(W, H, spf_total, spf_total, spf_total, args.depth)
     rows = max(1, min(args.cpu_rows, H))
     stride = H // rows
+    ref = reference_cpu(scene)
+    kind = "reference" if ref is not None else "port"
+    plugins = None if ref is not None else compare.plugins_for(scene)
+    ys = np.array([r * stride + stride // 2 for r in range(rows)], np.int32)
     acc = np.zeros((H, W, 4), np.float32)
+    out = np.zeros((rows, W, 3), np.float32)
     t0 = time.perf_counter()
-    for r in range(rows):
-        y = r * stride + stride // 2
-        compare.run_oracle(ubo, push, plugins, accum=acc, rect=(0, y, W, y + 1), nthreads=nthreads)
+    if ref is not None:
+        ref.refsc_bind(ubo.ctypes.data, ctypes.addressof(push))
+        ref.refsc_render_rows(ys.ctypes.data, rows, out.ctypes.data, nthreads)
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+
+        def one_row(y):  # ctypes releases the GIL: rows run in parallel
+            compare.run_oracle(ubo, push, plugins, accum=acc, rect=(0, int(y), W, int(y) + 1), nthreads=1)
+
+        with ThreadPoolExecutor(max_workers=nthreads) as ex:
+            list(ex.map(one_row, ys))
     dt = time.perf_counter() - t0
     samples = rows * W * spf_total
-    return samples / dt, samples, dt, rows
+    return samples / dt, samples, dt, rows, kind
 
 
 def run_reference(args, rank, world):
@@ -303,7 +344,7 @@ def run_reference(args, rank, world):
     nthreads = os.cpu_count() or 1
     vals = []
     for i in range(args.warmup + args.steps):
-        v, samples, dt, rows = cpu_baseline(args, W, H, args.spp, nthreads)
+        v, samples, dt, rows, kind = cpu_baseline(args, W, H, args.spp, nthreads)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
@@ -313,7 +354,7 @@ def run_reference(args, rank, world):
         "ms_per_step": 1000.0 * samples / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic", "impl": "reference",
         "config": {"workload": workload_name(args), "resolution": [W, H], "spp": args.spp, "max_depth": args.depth},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -343,21 +384,31 @@ def pctl(xs, q):
 
 
 def batch_cpu_baseline(jobs, nthreads, rows_per_job=2, njobs=16):
-    """The CPU restatement (oracle, OpenMP) on rows of the first jobs."""
+    """The CPU restatement (oracle) on rows of the first jobs, one row per
+    call, the rows spread over `nthreads` host threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
     from oracle import compare
 
-    samples = 0
-    t0 = time.perf_counter()
+    work = []
     for scene, spec, ubo, plugins in jobs[:njobs]:
         W, H = spec.width, spec.height
         push = scene.push_constants(W, H, spec.spp, spec.spp, spec.spp, spec.pathLength)
         acc = np.zeros((H, W, 4), np.float32)
+        plug = compare.plugins_for(scene)
         for r in range(rows_per_job):
             y = (2 * r + 1) * H // (2 * rows_per_job)
-            compare.run_oracle(ubo, push, compare.plugins_for(scene), accum=acc, rect=(0, y, W, y + 1),
-                               nthreads=nthreads)
-            samples += W * spec.spp
+            work.append((ubo, push, plug, acc, W, y, W * spec.spp))
+
+    def one_row(w):  # ctypes releases the GIL: rows run in parallel
+        ubo, push, plug, acc, W, y, _ = w
+        compare.run_oracle(ubo, push, plug, accum=acc, rect=(0, y, W, y + 1), nthreads=1)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=nthreads) as ex:
+        list(ex.map(one_row, work))
     dt = time.perf_counter() - t0
+    samples = sum(w[6] for w in work)
     return samples / dt, samples, dt
 
 
@@ -939,8 +990,8 @@ def main():
     }
     if rank == 0:
         nthreads = os.cpu_count() or 1
-        v, samples, dt, rows = cpu_baseline(args, W, H, args.spp, nthreads)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+        v, samples, dt, rows, kind = cpu_baseline(args, W, H, args.spp, nthreads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": kind,
                                 "sample": f"{rows} evenly spaced rows of {W}x{H} at {args.spp} spp "
                                           f"({samples} paths, {dt:.1f} s)"}
         print(json.dumps(line), flush=True)

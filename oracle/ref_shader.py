@@ -306,6 +306,7 @@ def load(reference: str | None = None) -> ctypes.CDLL:
 # as robust buffer access does on the device (the oracle reads them the same
 # way).
 SCENE_PRELUDE = r"""
+#include <omp.h>
 #include <stdint.h>
 #include <string.h>
 #include "pt_cuda.h"
@@ -369,6 +370,24 @@ void refsc_scene(uint32_t x, uint32_t y, int k, float* out3) {
                     (float)resolution.y;
     const vec3 c = rs_Scene(xy, uv, k);
     out3[0] = c.x, out3[1] = c.y, out3[2] = c.z;
+}
+// Rendering's sample loop over the rows listed in rows[0..n) of the bound
+// frame: Scene() for every pixel and sample k < samplesPerFrame, the colours
+// summed per pixel into out (3 floats a pixel, row by row in list order);
+// OpenMP over all (row, pixel) pairs.
+void refsc_render_rows(const int* rows, int n, float* out, int nthreads) {
+    const int W = resolution.x, spf = samplesPerFrame;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 8)
+    for (long q = 0; q < (long)n * W; q++) {
+        const int r = (int)(q / W), x = (int)(q % W);
+        float* o = out + 3 * q;
+        for (int k = 0; k < spf; k++) {
+            float c[3];
+            refsc_scene((uint32_t)x, (uint32_t)rows[r], k, c);
+            o[0] += c[0], o[1] += c[1], o[2] += c[2];
+        }
+    }
 }
 // Intersection() of one ray: out6 = hitdist, normal, materialID, lightID.
 void refsc_intersection(const float* r, float* out6) {
@@ -460,34 +479,45 @@ def splice_sdfs(src: str, texts: list[str]) -> str:
     return code
 
 
-def build_scene(reference: str | None = None, sdf_texts: list[str] | None = None) -> str:
-    """Builds (when the shader source is newer) the shader's path tracer for a
-    scene's SDF snippets (none: the SDF hooks stay empty, as in the source)."""
+def scene_key(sdf_texts: list[str] | None) -> str:
     import hashlib
 
-    shader = shader_path(reference)
-    if not os.path.exists(shader):
-        raise FileNotFoundError(shader)
     texts = list(sdf_texts or [])
-    key = hashlib.sha1("\0".join(texts).encode()).hexdigest()[:12] if texts else "nosdf"
-    lib = os.path.join(OUT, f"libref_scene_{key}.so")
-    deps = [shader, __file__, os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel", "pt_glsl_shim.h"),
-            os.path.join(ROOT, "pathtracer_gb300", "csrc", "pt_glsl.cpp"), os.path.join(ROOT, "include", "pt_mathf.h"),
-            os.path.join(ROOT, "include", "pt_cuda.h")]
-    if os.path.exists(lib) and all(os.path.getmtime(d) <= os.path.getmtime(lib) for d in deps):
-        return lib
-    sys.path.insert(0, ROOT)
-    from pathtracer_gb300 import glsl_translate
+    return hashlib.sha1("\0".join(texts).encode()).hexdigest()[:12] if texts else "nosdf"
 
-    with open(shader) as f:
-        code = glsl_translate(extract_scene(splice_sdfs(f.read(), texts)), "rs_")
-    os.makedirs(OUT, exist_ok=True)
+
+def build_scene(reference: str | None = None, sdf_texts: list[str] | None = None) -> str:
+    """The shader's path tracer for a scene's SDF snippets (none: the SDF
+    hooks stay empty, as in the source), as oracle/_ref/libref_scene_<key>.so.
+    Where the reference tree is mounted the C++ text is (re)generated from
+    it; elsewhere a text generated before is compiled, and without one this
+    raises FileNotFoundError."""
+    texts = list(sdf_texts or [])
+    key = scene_key(texts)
     cpp = os.path.join(OUT, f"ref_scene_{key}.cpp")
-    with open(cpp, "w") as f:
-        f.write(SCENE_PRELUDE + code + SCENE_WRAPPERS)
-    subprocess.run([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
-                    "-fno-fast-math", "-I", os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel"), "-I",
-                    os.path.join(ROOT, "include"), "-o", lib, cpp], check=True)
+    lib = os.path.join(OUT, f"libref_scene_{key}.so")
+    shader = shader_path(reference)
+    kernel = os.path.join(ROOT, "pathtracer_gb300", "csrc", "kernel")
+    if os.path.exists(shader):
+        deps = [shader, __file__, os.path.join(kernel, "pt_glsl_shim.h"),
+                os.path.join(ROOT, "pathtracer_gb300", "csrc", "pt_glsl.cpp")]
+        if not os.path.exists(cpp) or any(os.path.getmtime(d) > os.path.getmtime(cpp) for d in deps):
+            sys.path.insert(0, ROOT)
+            from pathtracer_gb300 import glsl_translate
+
+            with open(shader) as f:
+                code = glsl_translate(extract_scene(splice_sdfs(f.read(), texts)), "rs_")
+            os.makedirs(OUT, exist_ok=True)
+            with open(cpp, "w") as f:
+                f.write(SCENE_PRELUDE + code + SCENE_WRAPPERS)
+    elif not os.path.exists(cpp):
+        raise FileNotFoundError(shader)
+    cdeps = [cpp, os.path.join(kernel, "pt_glsl_shim.h"), os.path.join(ROOT, "include", "pt_mathf.h"),
+             os.path.join(ROOT, "include", "pt_cuda.h")]
+    if not os.path.exists(lib) or any(os.path.getmtime(d) > os.path.getmtime(lib) for d in cdeps):
+        subprocess.run([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+                        "-fno-fast-math", "-fopenmp", "-I", kernel, "-I", os.path.join(ROOT, "include"), "-o", lib,
+                        cpp], check=True)
     return lib
 
 

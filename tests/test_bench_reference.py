@@ -21,4 +21,8 @@ def test_reference_arm_prints_one_contract_line(built, workload):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["config"]["workload"].startswith(workload + "_plane_32x32_2spp")
-    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    # the reference's own shader built for the CPU for the GLSL scene, the oracle port for the keyed plug-in
+    from oracle import ref_shader
+
+    want = "reference" if workload == "mandelbulb12" and os.path.exists(ref_shader.shader_path()) else "port"
+    assert d["cpu_baseline"]["kind"] == want and d["e2e"]["h2d_bytes_per_step"] == 0
