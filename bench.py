@@ -98,7 +98,7 @@ def parse_args():
     ap.add_argument("--spp", type=int, default=64)
     ap.add_argument("--spf", type=int, default=64, help="samples per dispatch")
     ap.add_argument("--depth", type=int, default=6)
-    ap.add_argument("--cpu-rows", type=int, default=32, help="rows in the CPU baseline sample")
+    ap.add_argument("--cpu-rows", type=int, default=384, help="rows in the CPU baseline sample (about 10 s on 16 cores)")
     ap.add_argument("--engine", default="wavefront", choices=["wavefront", "megakernel"])
     ap.add_argument("--compare-engines", type=int, default=1, help="also time the other engine (1 step)")
     ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0: library default)")

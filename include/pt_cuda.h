@@ -278,8 +278,9 @@ int pt_get_wavefront_tuning(pt_ctx* ctx, pt_wavefront_tuning* out);
 int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* tuning);
 /* The autotuner: coordinate descent over the knobs above, `rounds` passes,
  * timing wavefront dispatches of `push` (its resolution must be the
- * accumulator's) on the bound scene.  Installs and returns the fastest
- * setting and its seconds per dispatch; the accumulator is left as it was. */
+ * accumulator's) on the bound scene; a knob moves only for a gain of at least
+ * 3 %.  Installs and returns the fastest setting and its seconds per
+ * dispatch; the accumulator is left as it was. */
 int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavefront_tuning* best,
                           double* best_seconds);
 

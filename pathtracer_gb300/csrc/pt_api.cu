@@ -376,7 +376,10 @@ int pt_set_wavefront_tuning(pt_ctx* ctx, const pt_wavefront_tuning* t) {
 
 // Coordinate descent over the wavefront knobs, timing real dispatches of
 // `push` (host wall clock around dispatch + wait, best of two after a
-// warm-up).  The accumulator is restored afterwards.
+// warm-up); a setting replaces the current one only when it is at least 3 %
+// faster, so run-to-run noise (about 1-2 % on GB300) does not move the
+// knobs.  The accumulator is restored afterwards.
+constexpr double kAutotuneGain = 0.97;
 int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavefront_tuning* best,
                           double* best_seconds) {
     if (!ctx) return PT_ERR_INVALID;
@@ -432,7 +435,7 @@ int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavef
                 if (std::memcmp(&c, &cur, sizeof c) == 0) continue;
                 double t = 0.0;
                 rc = time_one(c, &t);
-                if (rc == PT_OK && t < 0.99 * cur_t) {
+                if (rc == PT_OK && t < kAutotuneGain * cur_t) {
                     cur = c;
                     cur_t = t;
                 }
