@@ -333,6 +333,7 @@ float cameraPosX, cameraPosY, cameraPosZ;
 int ISO;
 float cameraSize, apertureSize, apertureDist, lensRadius, lensFocalLength, lensThickness, lensDistance;
 int tonemap;
+uvec3 gl_GlobalInvocationID;  // the invocation Rendering() runs for
 }  // namespace rs_
 }  // namespace ptg
 """
@@ -389,6 +390,14 @@ void refsc_render_rows(const int* rows, int n, float* out, int nthreads) {
         }
     }
 }
+// Rendering() of invocation (x, y): the pixel's samples of this dispatch,
+// exposure and Accumulate() over the pixel's previous value in3 (what main
+// loads from and stores to the texel buffer).
+void refsc_rendering(uint32_t x, uint32_t y, const float* in3, float* out3) {
+    gl_GlobalInvocationID = uvec3(x, y, 0u);
+    const vec3 c = rs_Rendering(vec3(in3[0], in3[1], in3[2]));
+    out3[0] = c.x, out3[1] = c.y, out3[2] = c.z;
+}
 // Intersection() of one ray: out6 = hitdist, normal, materialID, lightID.
 void refsc_intersection(const float* r, float* out6) {
     Ray ray;
@@ -404,11 +413,10 @@ void refsc_intersection(const float* r, float* out6) {
 
 
 def extract_scene(src: str) -> str:
-    """The shader without its interface and entry points: the #version,
+    """The shader without its interface and entry point: the #version,
     #extension, precision and layout lines, the uniform and push-constant
-    blocks (SCENE_PRELUDE declares them) and Accumulate, Rendering and main
-    (they read and write the texel buffer) are left out; numeric #defines
-    become constants."""
+    blocks (SCENE_PRELUDE declares them) and main (it reads and writes the
+    texel buffer) are left out; numeric #defines become constants."""
     text = src
     for pat in (r"^#version[^\n]*\n", r"^#extension[^\n]*\n", r"^precision[^\n]*\n", r"^layout\([^)]*\)\s*in;\s*\n",
                 r"^layout\([^)]*\)\s*uniform\s+\w+\s*\{.*?\};", r"^layout\([^)]*\)\s*uniform\s+imageBuffer[^;]*;"):
@@ -422,7 +430,7 @@ def extract_scene(src: str) -> str:
         return ""
 
     text = re.sub(r"^#define\s+(\w+)\s+([-+0-9.eE]+)\s*$", define, text, flags=re.M)
-    for name in ("Accumulate", "Rendering", "main"):
+    for name in ("main",):
         m = re.search(r"^\w+\s+" + name + r"\s*\(", text, re.M)
         if not m:
             raise ValueError(f"{name} not found in the shader source")

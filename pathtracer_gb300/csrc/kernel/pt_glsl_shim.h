@@ -8,7 +8,7 @@
 // Covered: float/int/uint/bool, vec2/vec3/vec4 (constructors, component
 // access, read swizzles as member calls, swizzle assignment through set_<sw>
 // members, arithmetic with vectors and scalars), uvec2/ivec2 and
-// bvec2/bvec3/bvec4 (constructors, components), mat2/mat3 (constructors
+// uvec3, bvec2/bvec3/bvec4 (constructors, components), mat2/mat3 (constructors
 // from columns or scalars, matrix * vector, mat3 * mat3), vector indexing
 // v[i], structs (declared in the snippet), and the built-ins
 // abs sign floor ceil fract round trunc mod min max clamp mix step
@@ -45,6 +45,7 @@ struct vec2 {
     PTG_M vec2(float a, float b) : x(a), y(b) {}
     PTG_M void set_xy(vec2 v);
     PTG_M void set_yx(vec2 v);
+    PTG_M explicit vec2(const struct uvec2& v);  // vec2(uvec2): component conversion
     PTG_M vec2 xx() const { return vec2(x, x); }
     PTG_M vec2 xy() const { return vec2(x, y); }
     PTG_M vec2 yx() const { return vec2(y, x); }
@@ -109,6 +110,13 @@ struct uvec2 {
     PTG_M uvec2() : x(0u), y(0u) {}
     PTG_M explicit uvec2(uint s) : x(s), y(s) {}
     PTG_M uvec2(uint a, uint b) : x(a), y(b) {}
+};
+PTG_M vec2::vec2(const uvec2& v) : x((float)v.x), y((float)v.y) {}
+struct uvec3 {
+    uint x, y, z;
+    PTG_M uvec3() : x(0u), y(0u), z(0u) {}
+    PTG_M explicit uvec3(uint s) : x(s), y(s), z(s) {}
+    PTG_M uvec3(uint a, uint b, uint c) : x(a), y(b), z(c) {}
 };
 struct ivec2 {
     int x, y;

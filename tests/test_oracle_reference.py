@@ -413,3 +413,42 @@ def test_whole_scene_intersection(built, name):
         assert (_bits(list(a)) == _bits(list(b))).all(), (list(a), list(b))
         hits += a[0] < 1e5
     assert hits > 100
+
+
+@pytest.mark.parametrize("name", ["cornell_box", "scene9.json"])
+def test_rendering_and_accumulate(built, name):
+    """Rendering() and Accumulate() of the reference's shader (the samples of
+    a dispatch, exposure, and the running mean or, on a reset frame, the
+    exponential moving average) against the oracle's accumulator: three
+    dispatches of a progressive render and one EMA frame, every pixel bit for
+    bit."""
+    from conftest import SCENES
+    from oracle import compare, oracle
+    from pathtracer_gb300 import Scene, cie_analytic
+
+    path = (os.path.join(SCENES, "cornell_box.json") if name == "cornell_box"
+            else os.path.join(REFERENCE, "scenes", name))
+    scene = Scene.load(path)
+    W, H, spf = 12, 8, 2
+    lib = ref_shader.load_scene(REFERENCE, scene.sdf_sources())
+    lib.refsc_bind.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.refsc_rendering.argtypes = [ctypes.c_uint32, ctypes.c_uint32, FP, FP]
+    ubo = scene.pack_ubo(cie_analytic())
+    plugins = compare.plugins_for(scene)
+    acc_o = np.zeros((H, W, 4), np.float32)
+    acc_r = np.zeros((H, W, 3), np.float32)
+    # (frame, currentSamples): progressive frames, then a reset frame with frame > spf (the EMA branch)
+    for frame, cur in ((spf, spf), (2 * spf, 2 * spf), (3 * spf, 3 * spf), (4 * spf, spf)):
+        push = scene.push_constants(W, H, frame, cur, spf, 6)
+        push.FPS, push.persistence = 30.0, 0.5
+        oracle.dispatch(ubo, push, plugins, acc_o)
+        lib.refsc_bind(ubo.ctypes.data, ctypes.addressof(push))
+        out = (F * 3)()
+        nxt = np.empty_like(acc_r)
+        for y in range(H):
+            for x in range(W):
+                lib.refsc_rendering(x, y, (F * 3)(*acc_r[y, x]), out)
+                nxt[y, x] = list(out)
+        acc_r = nxt
+        assert (_bits(acc_o[..., :3]) == _bits(acc_r)).all(), (frame, cur)
+    assert acc_r.max() > 0
