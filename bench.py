@@ -384,32 +384,41 @@ def pctl(xs, q):
 
 
 def batch_cpu_baseline(jobs, nthreads, rows_per_job=2, njobs=16):
-    """The CPU restatement (oracle) on rows of the first jobs, one row per
-    call, the rows spread over `nthreads` host threads."""
+    """Rows of the first jobs on the host cores: the reference's own shader
+    built for the CPU (the jobs have no SDFs; kind "reference", OpenMP over
+    each job's rows' pixels) where it was built, else the oracle (one row per
+    call, the rows spread over `nthreads` host threads; kind "port")."""
+    import ctypes
     from concurrent.futures import ThreadPoolExecutor
 
     from oracle import compare
 
+    ref = reference_cpu(jobs[0][0]) if jobs and not jobs[0][0].sdf_sources() else None
     work = []
     for scene, spec, ubo, plugins in jobs[:njobs]:
         W, H = spec.width, spec.height
         push = scene.push_constants(W, H, spec.spp, spec.spp, spec.spp, spec.pathLength)
-        acc = np.zeros((H, W, 4), np.float32)
-        plug = compare.plugins_for(scene)
-        for r in range(rows_per_job):
-            y = (2 * r + 1) * H // (2 * rows_per_job)
-            work.append((ubo, push, plug, acc, W, y, W * spec.spp))
+        ys = np.array([(2 * r + 1) * H // (2 * rows_per_job) for r in range(rows_per_job)], np.int32)
+        work.append((scene, ubo, push, W, H, ys, rows_per_job * W * spec.spp))
 
-    def one_row(w):  # ctypes releases the GIL: rows run in parallel
-        ubo, push, plug, acc, W, y, _ = w
-        compare.run_oracle(ubo, push, plug, accum=acc, rect=(0, y, W, y + 1), nthreads=1)
+    def one_row(w, y):  # ctypes releases the GIL: rows run in parallel
+        scene, ubo, push, W, H, _, _ = w
+        acc = np.zeros((H, W, 4), np.float32)
+        compare.run_oracle(ubo, push, compare.plugins_for(scene), accum=acc, rect=(0, int(y), W, int(y) + 1),
+                           nthreads=1)
 
     t0 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=nthreads) as ex:
-        list(ex.map(one_row, work))
+    if ref is not None:
+        for scene, ubo, push, W, H, ys, _ in work:
+            out = np.zeros((len(ys), W, 3), np.float32)
+            ref.refsc_bind(ubo.ctypes.data, ctypes.addressof(push))
+            ref.refsc_render_rows(ys.ctypes.data, len(ys), out.ctypes.data, nthreads)
+    else:
+        with ThreadPoolExecutor(max_workers=nthreads) as ex:
+            list(ex.map(lambda a: one_row(*a), [(w, y) for w in work for y in w[5]]))
     dt = time.perf_counter() - t0
     samples = sum(w[6] for w in work)
-    return samples / dt, samples, dt
+    return samples / dt, samples, dt, ("reference" if ref is not None else "port")
 
 
 def batch_roofline(samples, secs, peaks, peak_kind):
@@ -583,8 +592,8 @@ def run_batch(args, rank, world):
     }
     if rank == 0:
         nthreads = os.cpu_count() or 1
-        v, n, dt = batch_cpu_baseline(jobs, nthreads)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+        v, n, dt, kind = batch_cpu_baseline(jobs, nthreads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": kind,
                                 "sample": f"2 rows of each of the first 16 jobs at their spp ({n} paths, {dt:.1f} s)"}
         print(json.dumps(line), flush=True)
     return 0

@@ -26,3 +26,17 @@ def test_reference_arm_prints_one_contract_line(built, workload):
 
     want = "reference" if workload == "mandelbulb12" and os.path.exists(ref_shader.shader_path()) else "port"
     assert d["cpu_baseline"]["kind"] == want and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_batch_cpu_baseline(built):
+    """The batch workload's CPU figure: rows of generated sphere jobs through
+    the reference's own shader where it was built (kind "reference"), else
+    the oracle port."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import ref_shader
+
+    jobs, _ = bench.make_jobs(3, 0)
+    v, n, dt, kind = bench.batch_cpu_baseline(jobs, 4, rows_per_job=1, njobs=3)
+    assert v > 0 and n == sum(spec.width * spec.spp for _, spec, _, _ in jobs) and dt > 0
+    assert kind == ("reference" if os.path.exists(ref_shader.shader_path()) else "port")
