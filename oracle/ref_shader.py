@@ -1,18 +1,24 @@
-"""Builds oracle/_ref/libref_shader.so: single functions of the reference's own
-compute shader (src/shader.comp of the reference tree), compiled for the CPU.
+"""Builds the reference's own compute shader (src/shader.comp of the reference
+tree) for the CPU, in two forms, into oracle/_ref/ (git-ignored).
 
-TEST INFRASTRUCTURE ONLY.  The reference cannot run here (it is a Vulkan
-program), but its shader functions that need no scene buffers (RNG, sampling,
-spectra, refraction, MIS, the polynomial solvers, the rotation matrix, smin,
-and the analytic intersections with the structs they take) are plain GLSL:
-this recipe cuts them out of the reference source at build
-time, turns the source's numeric #defines into constants and its push
-constants into variables, runs the text through the repository's GLSL
-translator (pt_glsl_translate) and compiles it over pt_glsl_shim.h with g++
--ffp-contract=off.  tests/test_oracle_reference.py then checks the oracle's
-restatements (oracle/pt_oracle.c) against them bit for bit.  Nothing of the
-reference is committed: the source is read from the reference tree and the
-build goes to oracle/_ref/ (git-ignored).
+TEST INFRASTRUCTURE ONLY.  The reference cannot run here as a program (it is
+Vulkan), but its shader is plain GLSL that the repository's translator
+(pt_glsl_translate) and shim (pt_glsl_shim.h) take:
+- libref_shader.so: single functions cut out of the source (RNG, sampling,
+  spectra, refraction, MIS, the polynomial solvers, the rotation matrix,
+  smin, and the analytic intersections with the structs they take), the
+  source's numeric #defines as constants and its push constants as
+  variables;
+- libref_scene_<key>.so: the whole shader without its interface and `main`,
+  with a scene's SDF snippets spliced in as the reference's host does
+  (splice_sdfs), the uniform buffer and push constants as variables bound
+  from a packed scene, and Scene(), Rendering() and Intersection() exposed.
+Both compile with g++ -ffp-contract=off.  tests/test_oracle_reference.py
+checks the oracle (oracle/pt_oracle.c) against them bit for bit, and
+bench.py times the whole shader as the CPU baseline.  Nothing of the
+reference is committed: the source is read from the reference tree at build
+time; where the tree is absent (the GPU machine) a whole-shader C++ text
+generated before is compiled instead.
 
     python oracle/ref_shader.py [reference-root]
 """
