@@ -165,7 +165,8 @@ extern "C" int pt_glsl_translate(const char* glsl, const char* prefix, char* out
             if (q >= t.size() || t[q].text != "{") return fail("a struct needs a body");
             for (size_t prev = q; q < t.size() && t[q].text != "}"; q++) {
                 if (t[q].kind == Tok::Space) continue;
-                if (t[q].text == ";" && t[prev].kind == Tok::Ident) members.insert(t[prev].text);
+                if ((t[q].text == ";" || t[q].text == ",") && t[prev].kind == Tok::Ident)
+                    members.insert(t[prev].text);  // `float a, b;` declares both
                 prev = q;
             }
         }

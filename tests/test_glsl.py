@@ -272,3 +272,32 @@ def test_integer_boolean_and_swizzle_vocabulary(pt):
         r = f32(0.5) if qx > 0 else f32(0.45)
         want = np.sqrt(f32(qx * qx + qy * qy) + z * z, dtype=np.float32) - r
         assert abs(f(float(x), float(y), float(z)) - want) <= 1e-6 * max(1.0, abs(want))
+
+
+def test_structs_keep_member_names(pt):
+    """A struct declared in a snippet passes through; its members named like
+    colour components (`a`, `b`) keep their names (in such a snippet `.a` and
+    `.b` are not read as vector components), an `inout` parameter of the
+    struct type becomes a reference, and the result matches GLSL."""
+    text = """
+struct Shape { vec3 c; float a, b; };
+void grow(inout Shape s, float k) { s.a *= k; s.b += k; }
+float sdf(vec3 p)
+{
+    Shape s;
+    s.c = vec3(0.0, 0.5, 0.0);
+    s.a = 0.5;
+    s.b = 0.1;
+    grow(s, 2.0);
+    vec4 q = vec4(p - s.c, 1.0);
+    return length(q.xyz) - s.a;
+}
+float sdfmaterial(vec3 p) { return 1.0; }
+"""
+    out = " ".join(pt.glsl_translate(text, "s_").split())
+    assert "s.a *= k; s.b += k;" in out and "Shape& s" in out
+    pt.jit_check([text], sm=103)
+    f = _fn(_cpu_build(pt, "shape", {"s": text}), "c_s_sdf")
+    for x, y, z in _points(n=50, scale=1.0):
+        want = np.sqrt(np.float32(x * x + (y - 0.5) ** 2 + z * z), dtype=np.float32) - 1.0
+        assert abs(f(float(x), float(y), float(z)) - want) < 1e-5
