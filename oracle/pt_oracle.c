@@ -14,9 +14,13 @@
  * float algorithms the GPU kernels run, so both sides compute identical bits.
  * Out-of-range reads of the uniform arrays return 0 (robust buffer access).
  *
- * Parity unpinned: the reference has no tests or golden vectors and cannot
- * run here (Vulkan/Windows); primitives are pinned by known-answer values
- * derived from its formulas (tests/test_oracle_kat.py).
+ * Pinned against the reference's own shader: the reference has no tests or
+ * golden vectors and cannot run here as a program (Vulkan/Windows), but its
+ * shader builds for the CPU from its source through the repository's GLSL
+ * translator (oracle/ref_shader.py), and this restatement agrees with it bit
+ * for bit: single functions on seeded inputs, and every sample of the
+ * reference's own scene files (tests/test_oracle_reference.py).  Known-answer
+ * values derived from the formulas are in tests/test_oracle_kat.py.
  */
 #include "pt_oracle.h"
 #include "../include/pt_mathf.h"
