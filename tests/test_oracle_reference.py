@@ -304,7 +304,10 @@ def test_bounds(libs):
         assert (_bits(list(oa)) == _bits(list(ob))).all()
 
 
-ANALYTIC_SCENES = ["scene0.json", "scene1.json", "scene2.json"]  # the reference's scenes without SDFs
+# The reference's own scene files (whatever the checkout holds), and two of this repository's.
+_SCENE_DIR = os.path.join(REFERENCE, "scenes")
+REFERENCE_SCENES = sorted(f for f in os.listdir(_SCENE_DIR) if f.endswith(".json")) if os.path.isdir(_SCENE_DIR) else []
+OWN_SCENES = ["cornell_box", "mandelbulb12_plane"]
 
 
 def _scene_samples(lib, scene, W, H, spf, cie, plugins=()):
@@ -331,49 +334,28 @@ def _scene_samples(lib, scene, W, H, spf, cie, plugins=()):
     return col_o, col_r
 
 
-@pytest.mark.parametrize("name", ANALYTIC_SCENES + ["cornell_box"])
+@pytest.mark.parametrize("name", REFERENCE_SCENES + OWN_SCENES)
 def test_whole_shader_per_sample(built, name):
     """The reference's whole path tracer (src/shader.comp without its
-    interface and entry points, built for the CPU over the shim, scene buffer
-    and push constants bound like the descriptor set) against the oracle on
-    the reference's own scene files (and the Cornell box): every sample's
-    XYZ bit for bit, through lens refraction, NEE, MIS and Russian roulette."""
-    from conftest import SCENES
-    from pathtracer_gb300 import Scene, cie_analytic
-
-    lib = ref_shader.load_scene(REFERENCE)
-    path = (os.path.join(SCENES, "cornell_box.json") if name == "cornell_box"
-            else os.path.join(REFERENCE, "scenes", name))
-    scene = Scene.load(path)
-    col_o, col_r = _scene_samples(lib, scene, 24, 16, 3, cie_analytic())
-    assert np.isfinite(col_o).all() and col_o.max() > 0
-    bad = np.nonzero((_bits(col_o) != _bits(col_r)).any(axis=1))[0]
-    assert bad.size == 0, (bad[:5], col_o[bad[:3]], col_r[bad[:3]])
-
-
-SDF_SCENES = ["scene3.json", "scene4.json", "scene5.json", "scene6.json", "scene7.json", "scene8.json",
-              "scene9.json", "scene10.json"]
-
-
-@pytest.mark.parametrize("name", SDF_SCENES + ["mandelbulb12_plane"])
-def test_whole_shader_with_spliced_sdfs(built, name):
-    """SDF scenes: the scene's snippet texts spliced into the shader as the
-    reference's host does (InsertSDF), the whole shader built for the CPU,
-    against the oracle with its plug-ins (the shipped snippets) or the C
-    restatement of the text (the bench's 12-iteration mandelbulb): every
-    sample's XYZ bit for bit, through sphere tracing, SDF normals and SDF
-    materials."""
+    interface and `main`, built for the CPU over the shim, the scene buffer
+    and push constants bound like the descriptor set, the scene's SDF
+    snippets spliced in as the reference's host does) against the oracle on
+    the reference's own scene files and two of this repository's (the
+    Cornell box; the bench's 12-iteration mandelbulb, restated in C for the
+    oracle): every sample's XYZ bit for bit, through lens refraction, NEE,
+    MIS, Russian roulette, sphere tracing, SDF normals and SDF materials."""
     from conftest import SCENES
     from oracle import compare
     from pathtracer_gb300 import Scene, cie_analytic
 
-    path = (os.path.join(SCENES, name + ".json") if name == "mandelbulb12_plane"
-            else os.path.join(REFERENCE, "scenes", name))
+    path = (os.path.join(SCENES, name + ".json") if name in OWN_SCENES
+            else os.path.join(_SCENE_DIR, name))
     scene = Scene.load(path)
     texts = scene.sdf_sources()
-    assert texts and not any(t.startswith("builtin:") for t in texts)
+    assert not any(t.startswith("builtin:") for t in texts)
     lib = ref_shader.load_scene(REFERENCE, texts)
-    col_o, col_r = _scene_samples(lib, scene, 16, 12, 2, cie_analytic(), compare.plugins_for(scene))
+    W, H, spf = (24, 16, 3) if not texts else (16, 12, 2)
+    col_o, col_r = _scene_samples(lib, scene, W, H, spf, cie_analytic(), compare.plugins_for(scene))
     assert np.isfinite(col_o).all() and col_o.max() > 0
     bad = np.nonzero((_bits(col_o) != _bits(col_r)).any(axis=1))[0]
     assert bad.size == 0, (bad[:5], col_o[bad[:3]], col_r[bad[:3]])
