@@ -299,21 +299,23 @@ def cpu_baseline(args, W, H, spf_total, nthreads):
     """Path samples/s on the host cores over a stratified sample of rows: the
     reference's own shader built for the CPU where it was built ("reference":
     OpenMP over the rows' pixels), else the oracle (the CPU restatement,
-    "port": one row per call, rows spread over `nthreads` host threads)."""
+    "port": one row per call, rows spread over `nthreads` host threads).
+    The scene is read, packed and given its CIE table by the checker-side
+    restatement of the reference host (oracle/pack.py): no library of the
+    product is loaded on this path."""
     import ctypes
 
-    from oracle import compare
-    from pathtracer_gb300 import Scene, cie_analytic
+    from oracle import oracle as _o
+    from oracle import pack
 
-    scene = Scene.load(scene_path(args.workload))
-    cie = cie_analytic()
-    ubo = scene.pack_ubo(cie)
+    scene = pack.load_scene(scene_path(args.workload))
+    ubo = scene.pack_ubo(pack.cie_analytic())
     push = scene.push_constants(W, H, spf_total, spf_total, spf_total, args.depth)
     rows = max(1, min(args.cpu_rows, H))
     stride = H // rows
     ref = reference_cpu(scene)
     kind = "reference" if ref is not None else "port"
-    plugins = None if ref is not None else compare.plugins_for(scene)
+    plugins = None if ref is not None else _o.plugins_for_sources(scene.sdf_sources())
     ys = np.array([r * stride + stride // 2 for r in range(rows)], np.int32)
     acc = np.zeros((H, W, 4), np.float32)
     out = np.zeros((rows, W, 3), np.float32)
@@ -325,7 +327,7 @@ def cpu_baseline(args, W, H, spf_total, nthreads):
         from concurrent.futures import ThreadPoolExecutor
 
         def one_row(y):  # ctypes releases the GIL: rows run in parallel
-            compare.run_oracle(ubo, push, plugins, accum=acc, rect=(0, int(y), W, int(y) + 1), nthreads=1)
+            _o.dispatch(ubo, push, plugins, acc, rect=(0, int(y), W, int(y) + 1), nthreads=1)
 
         with ThreadPoolExecutor(max_workers=nthreads) as ex:
             list(ex.map(one_row, ys))

@@ -241,22 +241,25 @@ int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float
  * No counterpart in the reference.  One wavefront dispatch (the engine
  * PT_ENGINE_WAVEFRONT runs, bit-identical results) for callers that cannot
  * allocate device memory while they render: a plug-in whose host application
- * owns the GPU memory budget and forbids allocations after start-up, a
- * real-time loop that cannot pay an allocator's latency or fragmentation,
- * or code recorded into a stream capture, where cudaMalloc is not allowed.
- * It allocates nothing: the caller passes the scene and push constants in
- * host memory and the accumulator (W*H float4, read and written as by
- * pt_dispatch) in its own device memory; all working memory of the call
- * lives in one fixed array of PT_NOALLOC_SCRATCH_BYTES (32 MiB) in the
- * library's device image, which every GPU that loads the library holds
- * until the process exits.  Limits: W*H*samplesPerFrame <=
- * PT_NOALLOC_MAX_SAMPLES per call (else PT_ERR_TOO_LARGE), and
- * PT_NOALLOC_POOL_SLOTS path slots.  The first call on each device looks up
- * the array's device address (make it before any stream capture).  All calls
- * share the array, so calls that overlap on the GPU (on two streams at once)
- * race; the counters are reset at the start of every call.  Runs on
- * `stream` (NULL: the default stream) and returns when the dispatch is
- * complete.  No per-path trace. */
+ * owns the GPU memory budget and forbids allocations after start-up, or a
+ * real-time loop that cannot pay an allocator's latency or fragmentation.
+ * The caller passes the scene and push constants in host memory and the
+ * accumulator (W*H float4, read and written as by pt_dispatch) in its own
+ * device memory; all working memory of the call lives in one fixed array of
+ * PT_NOALLOC_SCRATCH_BYTES (32 MiB) in the library's device image, which
+ * every GPU that loads the library holds until the process exits.
+ * Limits: W*H*samplesPerFrame <= PT_NOALLOC_MAX_SAMPLES per call (else
+ * PT_ERR_TOO_LARGE), PT_NOALLOC_POOL_SLOTS path slots, devices 0..63, the
+ * shipped SDF plug-ins only (PT_SDF_CUSTOM: PT_ERR_UNSUPPORTED).
+ * The first call on each device looks up the array's device address; with
+ * lazy module loading (the CUDA default) that first call also commits the
+ * array's 32 MiB, so make it once as a warm-up (before any stream capture):
+ * later calls allocate nothing.  All calls share the array, so calls that
+ * overlap on the GPU race; the counters are reset at the start of every
+ * call.  A per-device host lock is held for the whole call and the call
+ * returns only when the dispatch is complete on `stream` (NULL: the default
+ * stream), so calls from several host threads run one after another.  No
+ * per-path trace. */
 #define PT_NOALLOC_SCRATCH_BYTES (32u << 20)
 #define PT_NOALLOC_MAX_SAMPLES (1u << 20)
 #define PT_NOALLOC_POOL_SLOTS (15u << 12) /* 61,440 */

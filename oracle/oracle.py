@@ -128,15 +128,25 @@ def dispatch(ubo: np.ndarray, push, plugins: list, accum: np.ndarray, rect=None,
         col = np.zeros(npaths * 3, np.float32)
         tr = PtoTrace(trace_depth, ev.ctypes.data, nev.ctypes.data, col.ctypes.data, None)
         out = (ev.reshape(npaths, trace_depth), nev, col.reshape(npaths, 3))
-    from pathtracer_gb300.native import PtSdfPlugin  # struct layout only
-
-    arr = (PtSdfPlugin * max(1, len(plugins)))(*plugins)
+    arr = _plugin_array(plugins)
     assert accum.dtype == np.float32 and accum.flags["C_CONTIGUOUS"] and accum.size == W * H * 4
     rc = lib().pto_dispatch(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins),
                             accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr) if tr else None, nthreads)
     if rc != 0:
         raise RuntimeError(f"pto_dispatch failed: {rc}")
     return out
+
+
+def _plugin_array(plugins: list):
+    """The plug-ins as a C array of the oracle's slot struct (same layout as
+    pt_sdf_plugin: kind, material mode, three material constants)."""
+    from .pack import PtoSdfPlugin
+
+    arr = (PtoSdfPlugin * max(1, len(plugins)))()
+    for i, p in enumerate(plugins):
+        arr[i].kind, arr[i].material_mode = p.kind, p.material_mode
+        arr[i].material[:] = list(p.material)
+    return arr
 
 
 # atan2 takes (y, x) like GLSL's atan(y, x): the first array is y.
@@ -168,9 +178,7 @@ def count_work(ubo: np.ndarray, push, plugins: list, rect=None, nthreads: int = 
     x0, y0, x1, y1 = rect if rect is not None else (0, 0, W, H)
     cnt = np.zeros(len(COUNTERS), np.uint64)
     tr = PtoTrace(0, None, None, None, cnt.ctypes.data)
-    from pathtracer_gb300.native import PtSdfPlugin  # struct layout only
-
-    arr = (PtSdfPlugin * max(1, len(plugins)))(*plugins)
+    arr = _plugin_array(plugins)
     accum = np.zeros((H, W, 4), np.float32)
     user = user_sdfs()
     user.user_count(1)
@@ -213,6 +221,24 @@ def set_generated(text: str):
     u.user_menger_set.argtypes = [ctypes.c_int]
     u.user_menger_set(prm[0])
     return "user_menger_sdf", "user_menger_material"
+
+
+def plugins_for_sources(sources: list[str]) -> list:
+    """The oracle's plug-in per SDF slot from the scene's texts alone (no
+    product library): shipped snippets and builtin keys by oracle/pack.py,
+    other text by its C restatement in user_sdfs.c (restatement_for)."""
+    from . import pack
+
+    out = []
+    for slot, src in enumerate(sources):
+        p = pack.plugin_for(src)
+        if p.kind == pack.SDF_CUSTOM:
+            names = restatement_for(src)
+            if names is None:
+                raise ValueError(f"no C restatement of the SDF text: {src[:60]!r}")
+            set_user_sdf(slot, *names)
+        out.append(p)
+    return out
 
 
 # First line of the SDF text of pathtracer_gb300/scenes/mandelbulb12_plane.json.

@@ -3,22 +3,26 @@
 //
 // Some callers cannot allocate device memory when they render: a plug-in
 // inside a host application that owns the GPU's memory budget and forbids
-// allocations after start-up, a real-time loop that cannot afford an
-// allocator's latency or fragmentation, or code recorded into a stream
-// capture where cudaMalloc is not allowed.  This entry point takes the scene
+// allocations after start-up, or a real-time loop that cannot afford an
+// allocator's latency or fragmentation.  This entry point takes the scene
 // and push constants by host pointer and the accumulator as caller-owned
 // device memory, and keeps all of its own working memory — the device copy
 // of the scene, the CIE table, the path pool, the ray queues, the per-sample
 // colours and the counters — in one file-scope __device__ array of fixed size
-// (PT_NOALLOC_SCRATCH_BYTES, about 32.5 MB), which every GPU that loads the
+// (PT_NOALLOC_SCRATCH_BYTES = 32 MiB), which every GPU that loads the
 // library holds until the process exits.
 //
 // In host code the array's name is only a host-side stand-in, so the first
 // call on each device looks up its device address with cudaGetSymbolAddress
-// (with that device current) and caches it; make that first call before any
-// stream capture.  Every call shares the array and overwrites what it needs
-// (the counters are reset, the colours and path slots are rewritten), so
-// calls that overlap on the GPU — on two streams at once — race.
+// (with that device current) and caches it (devices 0..63).  With lazy module
+// loading (the CUDA default) that lookup is also what loads this file's
+// module, so the first call on a device commits the array's 32 MiB; later
+// calls allocate nothing.  Make the first call (a warm-up) before any stream
+// capture.  Every call shares the array and overwrites what it needs (the
+// counters are reset, the colours and path slots are rewritten), so calls
+// that overlap on the GPU race.  A per-device host lock is held for the whole
+// call and each call returns only once its work on the stream is complete,
+// so calls from several host threads run one after another.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -53,11 +57,13 @@ static __device__ __align__(256) unsigned char pt_noalloc_scratch[PT_NOALLOC_SCR
 
 namespace {
 
+constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
-void* g_scratch[64] = {};  // device address of pt_noalloc_scratch per device
+void* g_scratch[kMaxDevices] = {};  // device address of pt_noalloc_scratch per device
+std::mutex g_call[kMaxDevices];     // held for a whole call on that device
 
 int scratch_address(int device, unsigned char** out) {
-    if (device < 0 || device >= 64) return PT_ERR_INVALID;
+    if (device < 0 || device >= kMaxDevices) return PT_ERR_INVALID;
     std::lock_guard<std::mutex> lock(g_mutex);
     if (!g_scratch[device]) {
         void* p = nullptr;
@@ -134,6 +140,8 @@ extern "C" int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugi
 
     int device = 0;
     PT_NA_TRY(cudaGetDevice(&device));
+    if (device < 0 || device >= kMaxDevices) return PT_ERR_INVALID;
+    std::lock_guard<std::mutex> call_lock(g_call[device]);
     unsigned char* base = nullptr;
     const int rs = scratch_address(device, &base);
     if (rs != PT_OK) return rs;
@@ -164,6 +172,10 @@ extern "C" int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugi
     WfJob job_table[1];
     PT_NA_TRY(engine.attach(device, stream, total < kPool ? (total < 1024u ? 1024u : total) : kPool, 1, 64,
                             base + kEngineOff, kEngineBytes, &counters, job_table));
+    // A mandelbulb marches with the warp-wide normal pass, as pt_dispatch does.
+    bool bulb = false;
+    for (int i = 0; i < nplugins; i++) bulb = bulb || plugins[i].kind == PT_SDF_MANDELBULB;
+    engine.set_march_kernel(bulb ? ptk_wavefront_march_warp_normals() : nullptr);
     WfJob j;
     std::memset(&j, 0, sizeof j);
     j.scene = d_scene;

@@ -9,7 +9,12 @@ if ROOT not in sys.path:
 
 SCENES = os.path.join(ROOT, "pathtracer_gb300", "scenes")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = "/root/reference"
+# The reference tree, where it is mounted (the recipe oracle/ref_shader.py
+# names its default location; PT_REFERENCE_ROOT overrides it).  Tests that
+# read it skip where it is absent.
+from oracle.ref_shader import reference_root  # noqa: E402
+
+REFERENCE = reference_root()
 
 
 def pytest_configure(config):

@@ -40,3 +40,25 @@ def test_batch_cpu_baseline(built):
     v, n, dt, kind = bench.batch_cpu_baseline(jobs, 4, rows_per_job=1, njobs=3)
     assert v > 0 and n == sum(spec.width * spec.spp for _, spec, _, _ in jobs) and dt > 0
     assert kind == ("reference" if os.path.exists(ref_shader.shader_path()) else "port")
+
+
+@pytest.mark.parametrize("workload", ["mandelbulb12", "mandelbulb"])
+def test_reference_arm_loads_no_product_library(built, workload):
+    """The reference arm packs the scene and builds its CIE table with the
+    checker-side restatement (oracle/pack.py): only libraries under oracle/
+    are mapped into the process, none of the product's."""
+    code = (
+        "import sys; sys.argv = ['bench.py', '--impl', 'reference', '--workload', %r, '--res', '32', '--spp', '2',"
+        " '--steps', '1', '--warmup', '3', '--cpu-rows', '2']\n"
+        "sys.path.insert(0, %r)\n"
+        "import bench\n"
+        "args = bench.parse_args()\n"
+        "assert bench.run_reference(args, 0, 1) == 0\n"
+        "libs = sorted({l.split()[-1] for l in open('/proc/self/maps') if l.rstrip().endswith('.so')"
+        " and l.split()[-1].startswith(%r)})\n"
+        "print('LIBS', libs)\n" % (workload, ROOT, ROOT))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, check=True,
+                         cwd=ROOT).stdout
+    libs = eval([ln for ln in out.splitlines() if ln.startswith("LIBS")][0][5:])
+    assert libs, out
+    assert all(os.path.relpath(p, ROOT).startswith("oracle" + os.sep) for p in libs), libs

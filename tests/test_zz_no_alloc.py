@@ -2,12 +2,13 @@
 
 It serves callers that cannot call cudaMalloc while they render — a plug-in
 whose host application owns the GPU memory budget, a real-time loop that
-cannot pay for an allocator, code recorded into a stream capture — by keeping
-its working memory in a fixed array inside the library.  Its output must be
-that of the regular entry point (pt_dispatch with the wavefront engine) on
-two calls in a row: the second call starts from the first call's
-accumulator and reuses the shared array, so leftovers from the first call
-would show.  Called through the C ABI with a caller-owned device accumulator.
+cannot pay for an allocator — by keeping its working memory in a fixed array
+inside the library.  Its output must be that of the regular entry point
+(pt_dispatch with the wavefront engine) on two calls in a row: the second
+call starts from the first call's accumulator and reuses the shared array,
+so leftovers from the first call would show.  The device's free memory must
+not change across a call after the first (the warm-up, which may commit the
+array).  Called through the C ABI with a caller-owned device accumulator.
 """
 import ctypes
 import os
@@ -60,9 +61,13 @@ def test_noalloc_matches_dispatch_on_two_calls(built):
     arr = (native.PtSdfPlugin * max(1, len(plugins)))(*plugins)
     d_accum = torch.zeros(H * W * 4, dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
-    for push, w in zip(pushes, want):
+    for i, (push, w) in enumerate(zip(pushes, want)):
+        free_before = torch.cuda.mem_get_info()[0]
         rc = lib.pt_dispatch_noalloc(ubo.ctypes.data, arr, len(plugins), ctypes.byref(push), d_accum.data_ptr(), None)
         assert rc == native.PT_OK, rc
+        free_after = torch.cuda.mem_get_info()[0]
+        if i > 0:  # after the warm-up call nothing is allocated on the device
+            assert free_after == free_before, (free_before, free_after)
         got = d_accum.cpu().numpy().reshape(H, W, 4)
         rel = np.abs(got - w) / np.maximum(np.maximum(np.abs(got), np.abs(w)), 1e-6)
         assert float(rel.max()) <= REL_TOL
@@ -71,3 +76,34 @@ def test_noalloc_matches_dispatch_on_two_calls(built):
     big = scene.push_constants(1024, 1024, 2, 2, 2, depth)  # 2,097,152 samples > PT_NOALLOC_MAX_SAMPLES
     rc = lib.pt_dispatch_noalloc(ubo.ctypes.data, arr, len(plugins), ctypes.byref(big), d_accum.data_ptr(), None)
     assert rc == native.PT_ERR_TOO_LARGE
+
+
+def test_noalloc_path_length_zero_matches_dispatch(built):
+    """pathLength 0 traces no bounce: the call takes its megakernel branch."""
+    import torch
+
+    from pathtracer_gb300 import Context, Scene, cie_analytic, native
+
+    assert torch.cuda.is_available(), "needs a GPU"
+    scene = Scene.load(os.path.join(SCENES, "feature_mix.json"))
+    cie = cie_analytic()
+    ubo = scene.pack_ubo(cie)
+    plugins = _plugins(scene, native)
+    W, H, spf = 40, 24, 3
+    push = scene.push_constants(W, H, spf, spf, spf, 0)
+    with Context(0) as ctx:
+        ctx.set_engine(native.PT_ENGINE_WAVEFRONT)
+        ctx.bind(scene, cie)
+        ctx.resize_accum(W, H)
+        ctx.dispatch(push)
+        ctx.wait()
+        want = ctx.read_accum().copy()
+    lib = native.cuda()
+    arr = (native.PtSdfPlugin * max(1, len(plugins)))(*plugins)
+    d_accum = torch.zeros(H * W * 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    rc = lib.pt_dispatch_noalloc(ubo.ctypes.data, arr, len(plugins), ctypes.byref(push), d_accum.data_ptr(), None)
+    assert rc == native.PT_OK, rc
+    got = d_accum.cpu().numpy().reshape(H, W, 4)
+    rel = np.abs(got - want) / np.maximum(np.maximum(np.abs(got), np.abs(want)), 1e-6)
+    assert float(rel.max()) <= REL_TOL
