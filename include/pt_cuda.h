@@ -50,7 +50,7 @@ extern "C" {
 #define PT_ERR_UNSUPPORTED 4   /* e.g. an SDF plug-in source that is not recognised */
 #define PT_ERR_NO_SCENE 5      /* dispatch before pt_upload_scene / pt_resize_accum */
 #define PT_ERR_OOM 6           /* device allocation failed */
-#define PT_ERR_KERNEL 7        /* a kernel reported an error through its status word */
+#define PT_ERR_KERNEL 7        /* the device work did not complete within its iteration limit (wavefront drain, batch run) */
 #define PT_ERR_TOO_LARGE 8     /* the request exceeds pt_dispatch_noalloc's fixed scratch */
 #define PT_ERR_BUSY 9          /* the resource is still in use by passes in flight */
 #define PT_ERR_CANCELLED 10    /* a served job was cancelled (pt_server_cancel) */
@@ -229,6 +229,13 @@ const char* pt_last_error(pt_ctx* ctx);
  * the number of bounces, colors[p*3..] the sample's XYZ before averaging.
  * Device pointers owned by the caller; pass NULLs to disable. */
 int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_colors, int depth_cap);
+
+/* Caps the iterations of the next wavefront dispatches' drain (0: the bound
+ * the library computes from the dispatch's size, path length and march
+ * budget, which a correct dispatch never reaches).  A dispatch that reaches
+ * the cap returns PT_ERR_KERNEL with its accumulator unchanged; the context
+ * stays usable.  For tests of that limit. */
+int pt_set_drain_limit(pt_ctx* ctx, uint64_t max_iterations);
 
 /* Evaluates one include/pt_mathf.h function on the device over device
  * arrays (fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos, 6 asin,

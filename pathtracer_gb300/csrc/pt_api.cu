@@ -52,6 +52,7 @@ struct pt_ctx {
     size_t rgb_bytes = 0;
     size_t colors_bytes = 0;
     uint32_t last_iterations = 0;
+    uint64_t drain_limit = 0;      // iteration cap of the wavefront drain (0: the bound computed per dispatch)
     // GLSL snippets other than the shipped four (PT_SDF_CUSTOM slots), as
     // translated by pt_glsl_translate, and the module compiled for them.
     std::vector<JitSlot> custom;
@@ -278,6 +279,12 @@ int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_
     if (!ctx) return PT_ERR_INVALID;
     if (depth_cap < 0 || (d_events && depth_cap == 0)) return fail(ctx, PT_ERR_INVALID, "pt_set_trace: bad depth_cap");
     ctx->trace = KTrace{d_events, d_nevents, d_colors, depth_cap};
+    return PT_OK;
+}
+
+int pt_set_drain_limit(pt_ctx* ctx, uint64_t max_iterations) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->drain_limit = max_iterations;
     return PT_OK;
 }
 
@@ -594,8 +601,8 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     // Every iteration moves every live path by one ray; a ray's march spans at
     // most ceil(512 / budget) + 1 iterations.
     const uint64_t march_iters = 512ull / (uint64_t)ctx->march_budget + 2;
-    const uint64_t max_iter =
-        ((uint64_t)total / E.pool + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
+    uint64_t max_iter = ((uint64_t)total / E.pool + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
+    if (ctx->drain_limit > 0 && ctx->drain_limit < max_iter) max_iter = ctx->drain_limit;
     const cudaError_t e = E.drain(trace, max_iter);
     if (e == cudaErrorTimeout) return fail(ctx, PT_ERR_KERNEL, "pt_dispatch: wavefront did not drain");
     PT_CUDA_TRY(ctx, e);

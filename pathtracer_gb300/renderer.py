@@ -252,6 +252,10 @@ class Context:
     def last_iterations(self) -> int:
         return self._lib.pt_last_iterations(self._h)
 
+    def set_drain_limit(self, max_iterations: int):
+        """Caps the wavefront drain's iterations (0: the library's bound)."""
+        self._check(self._lib.pt_set_drain_limit(self._h, max_iterations))
+
     def set_trace(self, events_ptr: int, nevents_ptr: int, colors_ptr: int, depth_cap: int):
         self._check(self._lib.pt_set_trace(self._h, events_ptr or None, nevents_ptr or None, colors_ptr or None,
                                            depth_cap))
