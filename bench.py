@@ -71,6 +71,10 @@ RENDER_WORKLOADS = {
     "mandelbulb12": ("mandelbulb12_plane.json", "mandelbulb12_plane_1024x1024_64spp_depth6"),
     # the shipped mandelbulb snippet (power 8, 4 iterations, bailout 16)
     "mandelbulb": ("mandelbulb_plane.json", "mandelbulb_plane_1024x1024_64spp_depth6"),
+    # the SDF-fractal configuration in its full form: the same fractal with a smooth bulb spectrum, a flat
+    # 0.5 plane, a 5800 K environment sky, a 256-step march capped at distance 50, 380-780 nm and the
+    # analytic CIE fit (scene extensions the reference's shader does not have)
+    "mandelbulb12_full": ("mandelbulb12_plane_full.json", "mandelbulb12_plane_full_1024x1024_64spp_depth6"),
 }
 
 
@@ -110,7 +114,7 @@ def parse_args():
     ap.add_argument("--autotune", type=int, default=1,
                     help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
     ap.add_argument("--workload", default="mandelbulb12",
-                    choices=["mandelbulb12", "mandelbulb", "batch64", "serve", "progressive"])
+                    choices=["mandelbulb12", "mandelbulb", "mandelbulb12_full", "batch64", "serve", "progressive"])
     ap.add_argument("--pass-spp", type=int, default=16, help="progressive: samples per pixel per pass")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: Poisson arrivals per second")
     ap.add_argument("--duration", type=float, default=30.0, help="serve: seconds of arrivals")
@@ -125,6 +129,9 @@ def parse_args():
     ap.add_argument("--burst", type=int, default=0,
                     help="serve: N requests all arriving at t=0 instead of the Poisson stream (saturates both arms)")
     ap.add_argument("--jobs", type=int, default=64, help="batch64: jobs per batch")
+    ap.add_argument("--serve-jobs", type=int, default=16,
+                    help="render workloads: jobs of the saturated serve burst reported in the line's `serve` object "
+                         "(batched-served vs plain at equal per-job RMSE; 0: off; N=1 only)")
     ap.add_argument("--route", default="auto", choices=["auto", "staged", "persistent"],
                     help="batch64: engine route of the passes")
     return ap.parse_args()
@@ -310,10 +317,12 @@ def cpu_baseline(args, W, H, spf_total, nthreads):
 
     scene = pack.load_scene(scene_path(args.workload))
     ubo = scene.pack_ubo(pack.cie_analytic())
+    ext = scene.pack_ext()
     push = scene.push_constants(W, H, spf_total, spf_total, spf_total, args.depth)
     rows = max(1, min(args.cpu_rows, H))
     stride = H // rows
-    ref = reference_cpu(scene)
+    # the reference's own shader has none of the full-form extensions: such scenes run on the oracle port
+    ref = reference_cpu(scene) if not ext.flags else None
     kind = "reference" if ref is not None else "port"
     plugins = None if ref is not None else _o.plugins_for_sources(scene.sdf_sources())
     ys = np.array([r * stride + stride // 2 for r in range(rows)], np.int32)
@@ -327,7 +336,7 @@ def cpu_baseline(args, W, H, spf_total, nthreads):
         from concurrent.futures import ThreadPoolExecutor
 
         def one_row(y):  # ctypes releases the GIL: rows run in parallel
-            _o.dispatch(ubo, push, plugins, acc, rect=(0, int(y), W, int(y) + 1), nthreads=1)
+            _o.dispatch(ubo, push, plugins, acc, rect=(0, int(y), W, int(y) + 1), nthreads=1, ext=ext)
 
         with ThreadPoolExecutor(max_workers=nthreads) as ex:
             list(ex.map(one_row, ys))
@@ -604,45 +613,44 @@ def run_batch(args, rank, world):
 SERVE_WORKLOAD = "serve_poisson_70pct_spheres_30pct_sdf_rmse2pct_8spp_passes"
 
 
-def run_serve(args, rank, world):
-    """Poisson request stream through pt_server, batched vs plain."""
-    import torch
+def serve_measure(opts, local, rank):
+    """A request stream through pt_server, batched then plain on the same
+    trace: pool of opts.pool_scenes generated scenes (70 % sphere jobs, 30 %
+    SDF jobs) with FP64 references, jobs refined in 8-spp passes until their
+    relative RMSE is at most opts.target_rmse (or opts.max_spp).  Returns the
+    per-arm figures and the comparison."""
+    from pathtracer_gb300 import Scene, Server, cie_analytic, native
 
-    from pathtracer_gb300 import Scene, Server, build, cie_analytic, native
-
-    build.build()
-    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
-    local = torch.cuda.current_device()
     cie = cie_analytic()
-    n_sdf = max(1, round(0.3 * args.pool_scenes))
-    n_sph = args.pool_scenes - n_sdf
+    n_sdf = max(1, round(0.3 * opts.pool_scenes))
+    n_sph = opts.pool_scenes - n_sdf
     pool = []
-    sdf_kind = native.PT_GEN_SDF_VARIED if args.sdf_scenes == "varied" else native.PT_GEN_SDF
-    for k in range(args.pool_scenes):
+    sdf_kind = native.PT_GEN_SDF_VARIED if opts.sdf_scenes == "varied" else native.PT_GEN_SDF
+    for k in range(opts.pool_scenes):
         kind, seed = (native.PT_GEN_SPHERES, 1000 + k) if k < n_sph else (sdf_kind, 2000 + k)
         sc, spec = Scene.generate(kind, seed + 100000 * rank)
         push = sc.push_constants(spec.width, spec.height, 1, 1, 1, spec.pathLength)
         pool.append((kind, sc, spec, push))
     srv = Server(local, mode=native.PT_SERVE_BATCHED, spp_per_pass=8, hbm_budget=64 << 30,
-                 pool_slots=args.pool or (1 << 19), iterations_per_poll=args.iters_per_poll,
-                 passes_in_flight=args.passes_in_flight)
+                 pool_slots=opts.pool or (1 << 19), iterations_per_poll=opts.iters_per_poll,
+                 passes_in_flight=opts.passes_in_flight)
     t0 = time.perf_counter()
     for key, (kind, sc, spec, push) in enumerate(pool):
         # SDFs as text: generated snippets are compiled at run time (the
         # batch's march kernel, before its first step: here)
         srv.add_scene_sources(key, sc.pack_ubo(cie), sc.sdf_sources())
-        srv.render_reference(key, push, args.ref_spp, 32)
+        srv.render_reference(key, push, opts.ref_spp, 32)
     ref_secs = time.perf_counter() - t0
 
     rng = np.random.default_rng(7 + rank)
     arrivals, reqs = [], []
-    t = 0.0 if args.burst else rng.exponential(1.0 / args.rate)
-    while (len(reqs) < args.burst) if args.burst else (t < args.duration):
+    t = 0.0 if opts.burst else rng.exponential(1.0 / opts.rate)
+    while (len(reqs) < opts.burst) if opts.burst else (t < opts.duration):
         key = int(rng.integers(0, n_sph)) if rng.random() < 0.7 else n_sph + int(rng.integers(0, n_sdf))
-        reqs.append(Server.job(key, pool[key][3], args.max_spp, args.target_rmse))
+        reqs.append(Server.job(key, pool[key][3], opts.max_spp, opts.target_rmse))
         arrivals.append(float(t))
-        if not args.burst:
-            t += rng.exponential(1.0 / args.rate)
+        if not opts.burst:
+            t += rng.exponential(1.0 / opts.rate)
 
     kinds = [pool[r.scene_key][0] for r in reqs]
 
@@ -681,39 +689,54 @@ def run_serve(args, rank, world):
     srv.run_trace([Server.job(k, pool[k][3], 8) for k in range(len(pool))], [0.0] * len(pool))
     res_p, plain = arm(native.PT_SERVE_PLAIN)
     identical = all((a.spp, a.rmse) == (b.spp, b.rmse) for a, b in zip(res_b, res_p))
-    reached = sum(1 for r in res_b if r.rmse <= args.target_rmse) / max(1, len(res_b))
+    reached = sum(1 for r in res_b if r.rmse <= opts.target_rmse) / max(1, len(res_b))
     per_job = [r.samples for r in res_b]
     srv.close()
+    span = opts.duration if not opts.burst else None
+    mean_job = sum(per_job) / max(1, len(per_job))
+    return {"batched": batched, "plain_megakernel_serial": plain,
+            "throughput_speedup_vs_plain": batched["path_samples_per_s"] / plain["path_samples_per_s"],
+            "p50_speedup_vs_plain": plain["time_to_target_s"]["p50"] / batched["time_to_target_s"]["p50"],
+            "p99_speedup_vs_plain": plain["time_to_target_s"]["p99"] / batched["time_to_target_s"]["p99"],
+            "rmse_identical_per_job": identical, "reached_target_fraction": reached,
+            "final_rmse_per_job": [r.rmse for r in res_b], "spp_per_job": [r.spp for r in res_b],
+            "offered_samples_per_s": sum(per_job) / span if span else None, "mean_samples_per_job": mean_job,
+            "offered_at_200_jobs_per_s": mean_job * 200.0,
+            "saturates_at_200_jobs_per_s": mean_job * 200.0 > batched["path_samples_per_s"],
+            "reference_render_s": ref_secs, "hbm_peak_bytes": st["bytes_peak"],
+            "resident_bytes": st["resident_bytes"]}
 
-    from pathtracer_gb300 import replicas
 
+def serve_config(opts):
+    return {"workload": SERVE_WORKLOAD + ("_varied_sdf" if opts.sdf_scenes == "varied" else "")
+            + ("_burst" if opts.burst else ""), "sdf_scenes": opts.sdf_scenes,
+            "rate_jobs_per_s": None if opts.burst else opts.rate,
+            "duration_s": None if opts.burst else opts.duration, "burst_jobs": opts.burst or None,
+            "target_rmse": opts.target_rmse, "max_spp": opts.max_spp, "spp_per_pass": 8,
+            "reference_spp": opts.ref_spp, "reference": "FP32 paths summed in FP64",
+            "pool_scenes": opts.pool_scenes, "hbm_budget_gib": 64,
+            "iterations_per_poll": opts.iters_per_poll, "passes_in_flight": opts.passes_in_flight}
+
+
+def run_serve(args, rank, world):
+    """Poisson request stream through pt_server, batched vs plain."""
+    import torch
+
+    from pathtracer_gb300 import build, replicas
+
+    build.build()
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0")))
+    local = torch.cuda.current_device()
+    serve = serve_measure(args, local, rank)
+    batched = serve["batched"]
     makespan = replicas.max_over_ranks([batched["makespan_s"]])[0]
     value = replicas.whole_job_rate(batched["samples"], world, makespan)
-    span = args.duration if not args.burst else None
-    offered = sum(per_job) / span if span else None
-    mean_job = sum(per_job) / max(1, len(per_job))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": 1000.0 * makespan, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, Poisson arrivals)",
-        "config": {"workload": SERVE_WORKLOAD + ("_varied_sdf" if args.sdf_scenes == "varied" else "")
-                   + ("_burst" if args.burst else ""), "sdf_scenes": args.sdf_scenes,
-                   "rate_jobs_per_s": None if args.burst else args.rate,
-                   "duration_s": None if args.burst else args.duration, "burst_jobs": args.burst or None,
-                   "target_rmse": args.target_rmse, "max_spp": args.max_spp, "spp_per_pass": 8,
-                   "reference_spp": args.ref_spp, "pool_scenes": args.pool_scenes,
-                   "parallelism": f"replicas x{world}", "hbm_budget_gib": 64,
-                   "iterations_per_poll": args.iters_per_poll, "passes_in_flight": args.passes_in_flight},
-        "serve": {"batched": batched, "plain_megakernel_serial": plain,
-                  "throughput_speedup_vs_plain": batched["path_samples_per_s"] / plain["path_samples_per_s"],
-                  "p50_speedup_vs_plain": plain["time_to_target_s"]["p50"] / batched["time_to_target_s"]["p50"],
-                  "p99_speedup_vs_plain": plain["time_to_target_s"]["p99"] / batched["time_to_target_s"]["p99"],
-                  "rmse_identical_per_job": identical, "reached_target_fraction": reached,
-                  "offered_samples_per_s": offered, "mean_samples_per_job": mean_job,
-                  "offered_at_200_jobs_per_s": mean_job * 200.0,
-                  "saturates_at_200_jobs_per_s": mean_job * 200.0 > batched["path_samples_per_s"],
-                  "reference_render_s": ref_secs, "hbm_peak_bytes": st["bytes_peak"],
-                  "resident_bytes": st["resident_bytes"]},
+        "config": {**serve_config(args), "parallelism": f"replicas x{world}"},
+        "serve": serve,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "note": "requests carry no host buffers; scenes are resident"},
         "gpu_launches": None,
@@ -999,6 +1022,21 @@ def main():
         "fp32_ops_per_sample": ops,
         "clocks": clk.summary(),
     }
+    if args.serve_jobs and world == 1:
+        # The spec comparison on the serving workload: a saturated burst
+        # of jobs drawn from the serving distribution (70 % sphere jobs, 30 %
+        # SDF jobs with drawn mandelbulb powers / Menger levels), each refined
+        # to 2 % relative RMSE against its FP64-summed reference, batched and
+        # served vs one after another through the plain megakernel.
+        sopts = argparse.Namespace(pool_scenes=8, burst=args.serve_jobs, rate=args.rate, duration=args.duration,
+                                   ref_spp=1024, max_spp=512, target_rmse=0.02, sdf_scenes="varied",
+                                   iters_per_poll=4, passes_in_flight=1, pool=0)
+        t0 = time.perf_counter()
+        serve = serve_measure(sopts, local, rank)
+        line["serve"] = {"config": serve_config(sopts), **serve, "wall_s": time.perf_counter() - t0,
+                         "note": "a saturated burst of jobs from the serving configuration's job distribution; its "
+                                 "200 jobs/s x 60 s stream offers far more work than one GPU serves "
+                                 "(saturates_at_200_jobs_per_s)"}
     if rank == 0:
         nthreads = os.cpu_count() or 1
         v, samples, dt, rows, kind = cpu_baseline(args, W, H, args.spp, nthreads)

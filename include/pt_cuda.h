@@ -157,6 +157,55 @@ int pt_jit_check(const char* const* sources, int n, int sm, char* log, size_t lo
 /* Replaces the UBO upload (src/pathtracer.cpp:3805-3807). */
 int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo);
 
+/* ---- full-form scene extensions (not in the reference) ------------------
+ * The reference shades every surface with one Lambertian BRDF whose
+ * reflectance is a Gaussian bump (src/shader.comp:1030-1038, :1075-1091), a
+ * ray that leaves the scene returns nothing (:1383-1389), hero wavelengths
+ * rotate through [390, 720) nm with the tabulated CIE table (:960-974,
+ * :129-140) and sphere tracing runs up to 512 steps with no distance cap
+ * (:779-860).  A pt_scene_ext adds, per scene and only where its flag is
+ * set: an environment sky (blackbody, PT_EXT_SKY), a wavelength range other
+ * than the reference's (PT_EXT_WAVELENGTHS), the analytic multi-lobe CIE fit
+ * evaluated per wavelength instead of the table (PT_EXT_ANALYTIC_CMF), march
+ * limits (PT_EXT_MARCH), and other surface models for materials 1..nmat
+ * (PT_EXT_MATERIALS).  A zeroed pt_scene_ext is the reference's method,
+ * bit for bit; the scene JSON carries the same fields under keys the
+ * reference's loader ignores. */
+enum {
+    PT_EXT_SKY = 1,
+    PT_EXT_WAVELENGTHS = 2,
+    PT_EXT_ANALYTIC_CMF = 4,
+    PT_EXT_MARCH = 8,
+    PT_EXT_MATERIALS = 16
+};
+enum {
+    PT_BSDF_REFERENCE = 0, /* the reference's Lambertian with its Gaussian-bump reflectance */
+    PT_BSDF_FLAT = 1,      /* Lambertian, reflectance p[0] at every wavelength */
+    PT_BSDF_SMOOTH = 2,    /* Lambertian, reflectance p[0] + p[1] exp(-((l - p[2]) / p[3])^2), l in nm */
+    PT_BSDF_MIRROR = 3,    /* conductor mirror: specular reflection, reflectance p[0] */
+    PT_BSDF_CAUCHY = 4,    /* dielectric, n(l) = p[0] + p[1] / l^2 (l in um) */
+    PT_BSDF_SELLMEIER = 5  /* dielectric, n(l)^2 = 1 + sum_i p[i] l^2 / (l^2 - p[3+i]) (l in um, C in um^2) */
+};
+#define PT_MAX_EXT_MATERIALS 128
+typedef struct pt_material_ext {
+    int32_t type; /* PT_BSDF_* */
+    float p[6];
+} pt_material_ext;
+typedef struct pt_scene_ext {
+    int32_t flags;            /* PT_EXT_* */
+    float sky_temperature;    /* K: the sky's emission is Emit's normalised Planck spectrum x luminosity */
+    float sky_luminosity;
+    float lambda_min;         /* nm: hero and rotated wavelengths uniform over [lambda_min, lambda_max) */
+    float lambda_max;
+    int32_t march_max_steps;  /* sphere-tracing steps (the reference: 512); exhausting them counts as a hit */
+    float march_epsilon;      /* hit when |d| < epsilon (the reference: 1e-4) */
+    float march_max_distance; /* a march past this ray distance misses (the reference: none) */
+    int32_t nmat;             /* materials 1..nmat have an entry below (<= PT_MAX_EXT_MATERIALS) */
+    pt_material_ext mat[PT_MAX_EXT_MATERIALS];
+} pt_scene_ext;
+/* pt_upload_scene with extensions (NULL: the reference's method). */
+int pt_upload_scene_ext(pt_ctx* ctx, const pt_ubo* ubo, const pt_scene_ext* ext);
+
 /* Replaces CreateTexelBuffer (src/pathtracer.cpp:2250-2256): a zeroed
  * W*H float4 accumulator. */
 int pt_resize_accum(pt_ctx* ctx, int width, int height);
@@ -370,6 +419,9 @@ int pt_batch_set_persist_refill(pt_batch* batch, int lanes);
 int pt_batch_set_route(pt_batch* batch, int route);
 int pt_batch_add_scene(pt_batch* batch, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins,
                        int* scene_id);
+/* Extensions of an added scene (NULL: the reference's method), used by
+ * passes added from now on; PT_ERR_BUSY while passes of the scene are in flight. */
+int pt_batch_set_scene_ext(pt_batch* batch, int scene_id, const pt_scene_ext* ext);
 /* A scene whose SDFs are given as text, like pt_set_sdfs: the shipped
  * snippets and builtin: specs select plug-ins, any other GLSL is translated
  * here (PT_ERR_UNSUPPORTED with the reason for what the translator cannot
@@ -415,6 +467,8 @@ int pt_batch_release_scene(pt_batch* batch, int scene_id);
 #define PT_EV_SHADOW_SHIFT 20     /* 2 bits: 0 none, 1 RR-culled, 2 occluded, 3 visible */
 #define PT_EV_RR_KILL (1u << 22)  /* terminated by Russian roulette */
 #define PT_EV_VALID (1u << 23)
+#define PT_EV_SPECULAR (1u << 24) /* extension materials: a specular bounce (mirror or dielectric reflection) */
+#define PT_EV_REFRACT (1u << 25)  /* extension materials: a dielectric transmission */
 
 #ifdef __cplusplus
 }

@@ -44,6 +44,16 @@ int pt_scene_counts(const pt_scene* scene, int counts[9]);
  * the scene overflows the fixed arrays (the reference truncates silently). */
 int pt_scene_pack_ubo(const pt_scene* scene, const float* cie, pt_ubo* out);
 
+/* The scene's full-form extensions (include/pt_cuda.h, pt_scene_ext) from
+ * the JSON keys the reference's loader ignores: "environment"
+ * {temperature, luminosity} (a blackbody sky), "spectral" {range: [min, max]
+ * nm, cmf: "analytic" | "table"}, "march" {maxSteps, epsilon, maxDistance}
+ * and per material "bsdf" {type: "flat" albedo | "smooth" base, amplitude,
+ * center, width | "mirror" reflectance | "cauchy" A, B | "sellmeier" B[3],
+ * C[3]}.  A scene without them gives flags == 0.  pt_scene_bind uploads
+ * them with the scene. */
+int pt_scene_pack_ext(const pt_scene* scene, pt_scene_ext* out);
+
 /* The host's progressive-render state that UpdatePushConstant reads. */
 typedef struct pt_frame_state {
     int32_t width, height;
@@ -94,6 +104,7 @@ int pt_scene_sdf_plugins(const pt_scene* scene, pt_sdf_plugin* out, int cap, int
 #define PT_GEN_SPHERES 0
 #define PT_GEN_SDF 1
 #define PT_GEN_SDF_VARIED 2
+#define PT_GEN_SPHERES_FULL 3 /* PT_GEN_SPHERES' scenes with mirror and Cauchy dielectric models (extension "bsdf") */
 typedef struct pt_job_spec {
     int32_t kind;
     int32_t width, height;
@@ -208,6 +219,9 @@ int pt_server_add_scene_sources(pt_server* server, int key, const pt_ubo* ubo, c
 /* Renders scene `key`'s FP64 reference for a view (push: resolution, camera,
  * path length) with spp samples per pixel from sample indices no request
  * uses; blocks until done. */
+/* Full-form extensions of a resident scene (NULL: the reference's method),
+ * for both modes; PT_ERR_BUSY while jobs of the scene are in flight. */
+int pt_server_set_scene_ext(pt_server* server, int key, const pt_scene_ext* ext);
 int pt_server_render_reference(pt_server* server, int key, const pt_push* push, int spp, int spp_per_pass);
 int pt_server_submit(pt_server* server, const pt_server_job* job, uint64_t* job_id);
 /* Admits, feeds and advances the work once; returns jobs finished since the

@@ -46,11 +46,11 @@ def plugins_for(scene, custom: dict | None = None) -> list:
     return out
 
 
-def run_oracle(ubo, push, plugins, accum=None, rect=None, trace_depth=0, nthreads=0):
+def run_oracle(ubo, push, plugins, accum=None, rect=None, trace_depth=0, nthreads=0, ext=None):
     W, H = push.resolution[0], push.resolution[1]
     if accum is None:
         accum = np.zeros((H, W, 4), np.float32)
-    tr = oracle.dispatch(ubo, push, plugins, accum, rect=rect, trace_depth=trace_depth, nthreads=nthreads)
+    tr = oracle.dispatch(ubo, push, plugins, accum, rect=rect, trace_depth=trace_depth, nthreads=nthreads, ext=ext)
     return accum, tr
 
 

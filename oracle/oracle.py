@@ -82,6 +82,10 @@ def lib() -> ctypes.CDLL:
         L.pto_dispatch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.POINTER(PtoTrace), ctypes.c_int]
+        L.pto_dispatch_ext.restype = ctypes.c_int
+        L.pto_dispatch_ext.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.POINTER(PtoTrace), ctypes.c_int]
         L.pto_pcg32.restype = ctypes.c_uint32
         L.pto_pcg32.argtypes = [ctypes.c_uint32]
         L.pto_random_float.restype = ctypes.c_float
@@ -110,7 +114,7 @@ def lib() -> ctypes.CDLL:
 
 
 def dispatch(ubo: np.ndarray, push, plugins: list, accum: np.ndarray, rect=None, trace_depth: int = 0,
-             nthreads: int = 0):
+             nthreads: int = 0, ext=None):
     """Runs the shader over rect=(x0, y0, x1, y1) (default: the whole frame).
 
     Returns (events, nevents, colors) when trace_depth > 0, else None.
@@ -130,11 +134,20 @@ def dispatch(ubo: np.ndarray, push, plugins: list, accum: np.ndarray, rect=None,
         out = (ev.reshape(npaths, trace_depth), nev, col.reshape(npaths, 3))
     arr = _plugin_array(plugins)
     assert accum.dtype == np.float32 and accum.flags["C_CONTIGUOUS"] and accum.size == W * H * 4
-    rc = lib().pto_dispatch(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins),
-                            accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr) if tr else None, nthreads)
+    rc = lib().pto_dispatch_ext(ubo.ctypes.data, _ext_ptr(ext), ctypes.addressof(push), ctypes.addressof(arr),
+                                len(plugins), accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr) if tr else None,
+                                nthreads)
     if rc != 0:
         raise RuntimeError(f"pto_dispatch failed: {rc}")
     return out
+
+
+def _ext_ptr(ext):
+    """The address of a scene extension block (any ctypes struct of the
+    pt_scene_ext layout) or None for the reference's method."""
+    if ext is None or not ext.flags:
+        return None
+    return ctypes.addressof(ext)
 
 
 def _plugin_array(plugins: list):
@@ -172,7 +185,7 @@ COUNTERS = ["samples", "path_rays", "shadow_rays", "sphere", "plane", "bounding_
 USER_COUNTERS = ["bulb8_iters", "user_mandelbulb_iters"]
 
 
-def count_work(ubo: np.ndarray, push, plugins: list, rect=None, nthreads: int = 0) -> dict:
+def count_work(ubo: np.ndarray, push, plugins: list, rect=None, nthreads: int = 0, ext=None) -> dict:
     """Runs the shader over rect with the work counters on; returns them by name."""
     W, H = push.resolution[0], push.resolution[1]
     x0, y0, x1, y1 = rect if rect is not None else (0, 0, W, H)
@@ -183,8 +196,8 @@ def count_work(ubo: np.ndarray, push, plugins: list, rect=None, nthreads: int = 
     user = user_sdfs()
     user.user_count(1)
     try:
-        rc = lib().pto_dispatch(ubo.ctypes.data, ctypes.addressof(push), ctypes.addressof(arr), len(plugins),
-                                accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr), nthreads)
+        rc = lib().pto_dispatch_ext(ubo.ctypes.data, _ext_ptr(ext), ctypes.addressof(push), ctypes.addressof(arr),
+                                    len(plugins), accum.ctypes.data, x0, y0, x1, y1, ctypes.byref(tr), nthreads)
         ucnt = list((ctypes.c_uint64 * len(USER_COUNTERS)).in_dll(user, "user_counters"))
     finally:
         user.user_count(0)
@@ -243,6 +256,8 @@ def plugins_for_sources(sources: list[str]) -> list:
 
 # First line of the SDF text of pathtracer_gb300/scenes/mandelbulb12_plane.json.
 BULB8_HEADER = "// Mandelbulb of power 8 in Chebyshev form, 12 iterations, bailout 2."
+# First line of the terrain text of pathtracer_gb300/scenes/menger_terrain_full.json.
+FBM_HEADER = "// Terrain: 8-octave value-noise fBm height field, amplitude 0.3, seed 7."
 
 
 def restatement_for(text: str):
@@ -252,6 +267,8 @@ def restatement_for(text: str):
     None for other text."""
     if text.startswith(BULB8_HEADER):
         return "user_bulb8_sdf", "user_bulb8_material"
+    if text.startswith(FBM_HEADER):
+        return "user_fbm_sdf", "user_fbm_material"
     if generated_params(text) is not None:
         return set_generated(text)
     return None

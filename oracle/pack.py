@@ -82,6 +82,58 @@ class PtoPush(ctypes.Structure):
 assert ctypes.sizeof(PtoPush) == 88
 
 
+EXT_SKY, EXT_WAVELENGTHS, EXT_ANALYTIC_CMF, EXT_MARCH, EXT_MATERIALS = 1, 2, 4, 8, 16
+BSDF_REFERENCE, BSDF_FLAT, BSDF_SMOOTH, BSDF_MIRROR, BSDF_CAUCHY, BSDF_SELLMEIER = range(6)
+MAX_EXT_MATERIALS = 128
+
+
+class PtoMaterialExt(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("p", ctypes.c_float * 6)]
+
+
+class PtoSceneExt(ctypes.Structure):
+    """A scene's full-form extensions as the oracle takes them (all zero: the
+    reference's method): sky, wavelength range, analytic CMF, march limits,
+    and surface models per material."""
+
+    _fields_ = [
+        ("flags", ctypes.c_int32),
+        ("sky_temperature", ctypes.c_float),
+        ("sky_luminosity", ctypes.c_float),
+        ("lambda_min", ctypes.c_float),
+        ("lambda_max", ctypes.c_float),
+        ("march_max_steps", ctypes.c_int32),
+        ("march_epsilon", ctypes.c_float),
+        ("march_max_distance", ctypes.c_float),
+        ("nmat", ctypes.c_int32),
+        ("mat", PtoMaterialExt * MAX_EXT_MATERIALS),
+    ]
+
+
+_BSDF_KEYS = {
+    "flat": (BSDF_FLAT, ("albedo",)),
+    "smooth": (BSDF_SMOOTH, ("base", "amplitude", "center", "width")),
+    "mirror": (BSDF_MIRROR, ("reflectance",)),
+    "cauchy": (BSDF_CAUCHY, ("A", "B")),
+}
+
+
+def _bsdf(b) -> tuple[int, list]:
+    """A material's "bsdf" object: (model, six parameters)."""
+    if b is None:
+        return BSDF_REFERENCE, [np.float32(0)] * 6
+    t = b["type"]
+    if t == "reference":
+        return BSDF_REFERENCE, [np.float32(0)] * 6
+    if t == "sellmeier":
+        return BSDF_SELLMEIER, _vec(b["B"], 3) + _vec(b["C"], 3)
+    if t not in _BSDF_KEYS:
+        raise ValueError(f"material.bsdf.type: unknown {t!r}")
+    kind, keys = _BSDF_KEYS[t]
+    p = [_f(b[k]) for k in keys]
+    return kind, p + [np.float32(0)] * (6 - len(p))
+
+
 class PtoSdfPlugin(ctypes.Structure):
     """One SDF slot of the oracle: which shipped snippet, and the material
     constants the scene files vary in their copies of sdfmaterial."""
@@ -165,6 +217,11 @@ class RefScene:
                           for o in _list(root, "material")]
         self.lights = [[_f(o["emission"]["temperature"]), _f(o["emission"]["luminosity"])]
                        for o in _list(root, "light")]
+        # Full-form extensions: keys the reference's loader does not read.
+        self.bsdfs = [_bsdf(o.get("bsdf")) for o in _list(root, "material")]
+        self.environment = root.get("environment")
+        self.spectral = root.get("spectral") or {}
+        self.march = root.get("march")
 
     def sdf_sources(self) -> list[str]:
         return [d["src"] for d in self.sdfs]
@@ -238,6 +295,39 @@ class RefScene:
         p.lensDistance = float(self.cam["lensDistance"])
         p.tonemap = tonemap
         return p
+
+    def pack_ext(self) -> PtoSceneExt:
+        """The scene's extension block (flags 0 for a reference-method scene)."""
+        x = PtoSceneExt()
+        if self.environment is not None:
+            x.flags |= EXT_SKY
+            x.sky_temperature = float(_f(self.environment["temperature"]))
+            x.sky_luminosity = float(_f(self.environment["luminosity"]))
+        if self.spectral.get("range") is not None:
+            lo, hi = _vec(self.spectral["range"], 2)
+            x.flags |= EXT_WAVELENGTHS
+            x.lambda_min, x.lambda_max = float(lo), float(hi)
+        if self.spectral.get("cmf") is not None:
+            if self.spectral["cmf"] not in ("analytic", "table"):
+                raise ValueError('spectral.cmf: "analytic" or "table"')
+            if self.spectral["cmf"] == "analytic":
+                x.flags |= EXT_ANALYTIC_CMF
+        if self.march is not None:
+            x.flags |= EXT_MARCH
+            x.march_max_steps = _i(self.march["maxSteps"])
+            x.march_epsilon = float(_f(self.march["epsilon"]))
+            x.march_max_distance = float(_f(self.march["maxDistance"]))
+        last = max((i + 1 for i, (k, _) in enumerate(self.bsdfs) if k != BSDF_REFERENCE), default=0)
+        if last > MAX_EXT_MATERIALS:
+            raise ValueError(f"{last} materials with extension models exceed {MAX_EXT_MATERIALS}")
+        if last:
+            x.flags |= EXT_MATERIALS
+            x.nmat = last
+            for i in range(last):
+                k, p = self.bsdfs[i]
+                x.mat[i].type = k
+                x.mat[i].p[:] = [float(v) for v in p]
+        return x
 
     def plugins(self) -> list:
         """The oracle's plug-in per SDF slot (kind SDF_CUSTOM for text that is

@@ -112,7 +112,11 @@ typedef struct {
     int light_pick;
     int shadow_state;
     uint64_t* cnt;     /* work counters of this thread (PTO_C_*) or NULL */
+    const pt_scene_ext* x; /* full-form extensions (all zero: the reference's method) */
+    int medium;        /* extension dielectrics: bit 0 inside one, bit 1 once the path carries l.x alone */
 } ctx_t;
+
+static const pt_scene_ext kNoExt; /* all zero: the reference's method */
 
 static inline float OBJ(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_OBJECTS_SIZE) ? c->u->objects[i] : 0.0f; }
 static inline float SDFS(const ctx_t* c, int i) { return (i >= 0 && i < PT_MAX_SDFS_SIZE) ? c->u->sdfs[i] : 0.0f; }
@@ -142,6 +146,24 @@ static vec3 WaveToXYZ(const ctx_t* c, float wave) {
         XYZ = mk3(mixf(t1.x, t2.x, a), mixf(t1.y, t2.y, a), mixf(t1.z, t2.z, a));
     }
     return XYZ;
+}
+
+/* Extension PT_EXT_ANALYTIC_CMF: the multi-lobe Gaussian fit of the CIE 1931
+ * matching functions (Wyman, Sloan and Shirley 2013) evaluated at the
+ * wavelength; each lobe has a different width on each side of its peak. */
+static inline float cmf_lobe(float x, float mu, float s1, float s2) {
+    float t = (x - mu) / ((x < mu) ? s1 : s2);
+    return ptm_expf(-0.5f * t * t);
+}
+static vec3 cmf_analytic(float wave) {
+    float x = (1.056f * cmf_lobe(wave, 599.8f, 37.9f, 31.0f) + 0.362f * cmf_lobe(wave, 442.0f, 16.0f, 26.7f)) -
+              0.065f * cmf_lobe(wave, 501.1f, 20.4f, 26.2f);
+    float y = 0.821f * cmf_lobe(wave, 568.8f, 46.9f, 40.5f) + 0.286f * cmf_lobe(wave, 530.9f, 16.3f, 31.1f);
+    float z = 1.217f * cmf_lobe(wave, 437.0f, 11.8f, 36.0f) + 0.681f * cmf_lobe(wave, 459.0f, 26.0f, 13.8f);
+    return mk3(x, y, z);
+}
+static vec3 WaveToXYZx(const ctx_t* c, float wave) {
+    return (c->x->flags & PT_EXT_ANALYTIC_CMF) ? cmf_analytic(wave) : WaveToXYZ(c, wave);
 }
 
 /* SC:143-152 */
@@ -787,7 +809,13 @@ static int SphereTracing(const ctx_t* c, Ray ray, hit_t* h) {
         return 0;
     }
     float k = signf_glsl(SDF(c, ray.origin, set1));
-    for (int i = 0; i < 512; i++) {
+    /* Extension PT_EXT_MARCH: the scene's step count, hit epsilon and
+     * distance cap instead of 512 steps, 1e-4 and none. */
+    const int xm = (c->x->flags & PT_EXT_MARCH) != 0;
+    const int maxSteps = xm ? c->x->march_max_steps : 512;
+    const float eps = xm ? c->x->march_epsilon : 1e-4f;
+    for (int i = 0; i < maxSteps; i++) {
+        if (xm && t > c->x->march_max_distance) return 0;
         COUNT(c, PTO_C_MARCH_STEPS);
         float radius = SDF(c, p, set1);
         if (insT > (fabsf(previousRadius) + fabsf(radius))) {
@@ -798,7 +826,7 @@ static int SphereTracing(const ctx_t* c, Ray ray, hit_t* h) {
             p = fma3(ray.dir, mk3(t, t, t), ray.origin);
             continue;
         }
-        if (fabsf(radius) < 1e-4f) break;
+        if (fabsf(radius) < eps) break;
         if (t > tMinMax.y) {
             points += 1;
         } else {
@@ -1000,6 +1028,13 @@ static vec4 EvaluateBRDF(vec4 l, material_t mat) {
     return div4s(s, PI_F);
 }
 
+/* EvaluateBRDF, or the extension Lambertian of the hit's material. */
+static vec4 ExtLambert(const pt_material_ext* m, vec4 l);
+static vec4 EvaluateBRDFx(const ctx_t* c, vec4 l, material_t mat, const pt_material_ext* xm) {
+    (void)c;
+    return xm ? ExtLambert(xm, l) : EvaluateBRDF(l, mat);
+}
+
 /* SC:1093-1119 */
 static vec3 ToWorld(vec3 v, vec3 n) {
     vec3 b1 = mk3(0.0f, -1.0f, 0.0f);
@@ -1083,7 +1118,7 @@ static inline float MISPowerHeuristicsBeta2(float pdf1, float pdf2) { return pdf
 
 /* SC:1298-1343 */
 static vec4 SampleLightSource(ctx_t* c, vec4 l, vec4 rayradiance, vec3 outOrigin, vec3 normal, material_t mat,
-                              uint32_t* seed, float BRDFpdf, float* MISBRDFWeight) {
+                              const pt_material_ext* xm, uint32_t* seed, float BRDFpdf, float* MISBRDFWeight) {
     float boundingRadius = 0.0f;
     vec3 lightPos = mk3(0.0f, 0.0f, 0.0f);
     float lightIDOut = -1.0f;
@@ -1114,7 +1149,7 @@ static vec4 SampleLightSource(ctx_t* c, vec4 l, vec4 rayradiance, vec3 outOrigin
                     COUNT(c, PTO_C_EMIT);
                     COUNT(c, PTO_C_BRDF);
                     light_t lt = GetLightMix(c, lightIDOut);
-                    vec4 brdf = EvaluateBRDF(l, mat);
+                    vec4 brdf = EvaluateBRDFx(c, l, mat, xm);
                     vec4 f = div4s(scl4(brdf, costheta), lightpdf);
                     rayradiance = mul4(rayradiance, f);
                     return scl4(mul4(Emit(l, lt), rayradiance), 1.0f - *MISBRDFWeight);
@@ -1128,6 +1163,96 @@ static vec4 SampleLightSource(ctx_t* c, vec4 l, vec4 rayradiance, vec3 outOrigin
     }
     *MISBRDFWeight = MISPowerHeuristicsBeta2(BRDFpdf, lightpdf);
     return s4(0.0f);
+}
+
+/* ---- Extension surface models (PT_EXT_MATERIALS) ---- */
+static const pt_material_ext* ExtMaterial(const ctx_t* c, float materialID) {
+    if (!(c->x->flags & PT_EXT_MATERIALS)) return NULL;
+    int mi = (int)floorf(materialID);
+    if (mi < 0 || mi >= c->x->nmat || mi >= PT_MAX_EXT_MATERIALS) return NULL;
+    const pt_material_ext* m = &c->x->mat[mi];
+    return (m->type == PT_BSDF_REFERENCE) ? NULL : m;
+}
+/* Cauchy n = A + B / l^2, or Sellmeier n^2 = 1 + sum B l^2 / (l^2 - C), l in um. */
+static float ExtIOR(const pt_material_ext* m, float l) {
+    float u = l * 1e-3f;
+    float u2 = u * u;
+    if (m->type == PT_BSDF_CAUCHY) return m->p[0] + m->p[1] / u2;
+    float n2 = 1.0f;
+    n2 += (m->p[0] * u2) / (u2 - m->p[3]);
+    n2 += (m->p[1] * u2) / (u2 - m->p[4]);
+    n2 += (m->p[2] * u2) / (u2 - m->p[5]);
+    return sqrtf(n2);
+}
+/* Unpolarised Fresnel reflectance for eta = n1/n2 at incidence cosine cosi;
+ * 1 under total internal reflection; *cost: the transmitted cosine. */
+static float FresnelDielectric(float eta, float cosi, float* cost) {
+    float sin2t = (eta * eta) * (1.0f - cosi * cosi);
+    if (sin2t >= 1.0f) {
+        *cost = 0.0f;
+        return 1.0f;
+    }
+    float ct = sqrtf(1.0f - sin2t);
+    float rs = (eta * cosi - ct) / (eta * cosi + ct);
+    float rp = (cosi - eta * ct) / (cosi + eta * ct);
+    *cost = ct;
+    return 0.5f * (rs * rs + rp * rp);
+}
+/* Lambertian extension reflectance at four wavelengths, / PI. */
+static vec4 ExtLambert(const pt_material_ext* m, vec4 l) {
+    if (m->type == PT_BSDF_FLAT) return div4s(s4(m->p[0]), PI_F);
+    vec4 x = mk4((l.x - m->p[2]) / m->p[3], (l.y - m->p[2]) / m->p[3], (l.z - m->p[2]) / m->p[3],
+                 (l.w - m->p[2]) / m->p[3]);
+    vec4 v = mk4(m->p[0] + m->p[1] * ptm_expf(-(x.x * x.x)), m->p[0] + m->p[1] * ptm_expf(-(x.y * x.y)),
+                 m->p[0] + m->p[1] * ptm_expf(-(x.z * x.z)), m->p[0] + m->p[1] * ptm_expf(-(x.w * x.w)));
+    return div4s(v, PI_F);
+}
+/* A specular bounce (mirror, dielectric): new direction from the hit point,
+ * throughput, MIS weight 1 for the next emitter hit.  A dielectric chooses
+ * reflection or transmission by the Fresnel reflectance at l.x; reflection
+ * keeps every wavelength weighted by its reflectance over the chosen one;
+ * from the first transmission on the path carries l.x alone at 4x (each
+ * wavelength bends differently).
+ * Russian roulette follows in the caller.  Returns the event bits. */
+static uint32_t ExtSpecular(ctx_t* c, const pt_material_ext* m, vec4 l, vec4* rayradiance, Ray* ray, float hitdist,
+                            vec3 normal, uint32_t* seed, float* MISBRDFWeight) {
+    ray->origin = fma3(ray->dir, mk3(hitdist, hitdist, hitdist), ray->origin);
+    vec3 n = normal;
+    float cdot = dot3(ray->dir, n);
+    if (cdot > 0.0f) {
+        n = neg3(n);
+        cdot = -cdot;
+    }
+    *MISBRDFWeight = 1.0f;
+    float cosi = -cdot;
+    if (m->type == PT_BSDF_MIRROR) {
+        ray->dir = add3(ray->dir, scl3(n, 2.0f * cosi));
+        *rayradiance = scl4(*rayradiance, m->p[0]);
+        return PT_EV_SPECULAR;
+    }
+    int inside = (c->medium & 1) != 0;
+    float nh = ExtIOR(m, l.x);
+    float eta = inside ? nh : 1.0f / nh;
+    float cost = 0.0f;
+    float F = FresnelDielectric(eta, cosi, &cost);
+    if (RandomFloatPCG32(seed) < F) {
+        ray->dir = add3(ray->dir, scl3(n, 2.0f * cosi));
+        float ct;
+        float ny = ExtIOR(m, l.y), nz = ExtIOR(m, l.z), nw = ExtIOR(m, l.w);
+        float Fy = FresnelDielectric(inside ? ny : 1.0f / ny, cosi, &ct);
+        float Fz = FresnelDielectric(inside ? nz : 1.0f / nz, cosi, &ct);
+        float Fw = FresnelDielectric(inside ? nw : 1.0f / nw, cosi, &ct);
+        vec4 r = *rayradiance;
+        *rayradiance = mk4(r.x, r.y * (Fy / F), r.z * (Fz / F), r.w * (Fw / F));
+        return PT_EV_SPECULAR;
+    }
+    ray->dir = normalize3(add3(scl3(ray->dir, eta), scl3(n, eta * cosi - cost)));
+    if (!(c->medium & 2)) { /* the first transmission: l.x alone from here on */
+        *rayradiance = mk4(rayradiance->x * 4.0f, 0.0f, 0.0f, 0.0f);
+        c->medium |= 2;
+    }
+    c->medium ^= 1;
+    return PT_EV_REFRACT;
 }
 
 /* SC:1345-1391; *event receives the trace word of this bounce. */
@@ -1156,15 +1281,30 @@ static vec4 TraceRay(ctx_t* c, vec4 l, vec4* rayradiance, Ray* inRay, uint32_t* 
             return radiance;
         }
         COUNT(c, PTO_C_SURFACE_HITS);
+        const pt_material_ext* xm = ExtMaterial(c, h.materialID);
+        if (xm && xm->type >= PT_BSDF_MIRROR) {
+            ev |= ExtSpecular(c, xm, l, rayradiance, inRay, hitdist, h.normal, seed, MISBRDFWeight);
+            vec4 rr = *rayradiance;
+            float rp = fminf(fmaxf(fmaxf(rr.x, fmaxf(rr.y, fmaxf(rr.z, rr.w))), 0.0f), 0.99f);
+            if (RandomFloatPCG32(seed) > rp) {
+                *isTerminate = 1;
+                *event = ev | PT_EV_RR_KILL;
+                return radiance;
+            }
+            *rayradiance = scl4(*rayradiance, 1.0f / rp);
+            *event = ev;
+            return radiance;
+        }
         COUNT(c, PTO_C_BRDF);
         Ray outRay;
         outRay.origin = fma3(inRay->dir, mk3(hitdist, hitdist, hitdist), inRay->origin);
         outRay.dir = SampleCosineDirectionHemisphere(h.normal, seed);
         float BRDFpdf = CosineDirectionPDF(dot3(outRay.dir, h.normal));
-        radiance = SampleLightSource(c, l, *rayradiance, outRay.origin, h.normal, mat, seed, BRDFpdf, MISBRDFWeight);
+        radiance = SampleLightSource(c, l, *rayradiance, outRay.origin, h.normal, mat, xm, seed, BRDFpdf,
+                                     MISBRDFWeight);
         ev |= ((uint32_t)(c->light_pick & 0x7F) << PT_EV_LIGHT_SHIFT) | ((uint32_t)c->shadow_state << PT_EV_SHADOW_SHIFT);
         float costheta = dot3(outRay.dir, h.normal);
-        vec4 brdf = EvaluateBRDF(l, mat);
+        vec4 brdf = EvaluateBRDFx(c, l, mat, xm);
         vec4 f = div4s(scl4(brdf, costheta), BRDFpdf);
         *rayradiance = mul4(*rayradiance, f);
         vec4 rr = *rayradiance;
@@ -1178,6 +1318,13 @@ static vec4 TraceRay(ctx_t* c, vec4 l, vec4* rayradiance, Ray* inRay, uint32_t* 
         *inRay = outRay;
     } else {
         ev |= PT_EV_HIT_MISS;
+        if (c->x->flags & PT_EXT_SKY) { /* extension: the sky, weight 1 (no light sample reaches it) */
+            light_t sky;
+            sky.x = c->x->sky_temperature;
+            sky.y = c->x->sky_luminosity;
+            COUNT(c, PTO_C_EMIT);
+            radiance = mul4(Emit(l, sky), *rayradiance);
+        }
         *isTerminate = 1;
     }
     *event = ev;
@@ -1191,6 +1338,7 @@ static vec4 TracePath(ctx_t* c, vec4 l, Ray ray, uint32_t* seed, uint32_t* event
     float MISBRDFWeight = 1.0f;
     int isTerminate = 0;
     int n = 0;
+    c->medium = 0;
     for (int i = 0; i < c->pc->pathLength; i++) {
         uint32_t ev = 0;
         radiance = add4(radiance, TraceRay(c, l, &rayradiance, &ray, seed, &MISBRDFWeight, &isTerminate, &ev));
@@ -1258,13 +1406,26 @@ static vec3 Scene(ctx_t* c, uint32_t xx, uint32_t xy_y, vec2 uv, int k, uint32_t
     vec3 pointOnAperture = add3(c->cameraPos, vec_mul_mat(mk3(ha * disk.x, ha * disk.y, pc->apertureDist), m));
     ray.dir = normalize3(sub3(pointOnAperture, ray.origin));
     vec3 forwardDir = mk3(m.c0.z, m.c1.z, m.c2.z);
-    float l_h = SampleHeroWavelength(360.0f, 800.0f, &seed);
+    const int xr = (c->x->flags & PT_EXT_WAVELENGTHS) != 0;
+    float l_h = xr ? SampleHeroWavelength(c->x->lambda_min, c->x->lambda_max, &seed)
+                   : SampleHeroWavelength(360.0f, 800.0f, &seed);
     TracePathLens(c, l_h, &ray, forwardDir);
-    vec4 l = SampleWavelengths(l_h);
+    vec4 l;
+    float range;
+    if (xr) { /* extension: the hero and three rotations a quarter of the range apart */
+        float lo = c->x->lambda_min, R = c->x->lambda_max - c->x->lambda_min;
+        float base = l_h - lo, q = R * 0.25f;
+        l = mk4(lo + modf_glsl(base + q, R), lo + modf_glsl(base + q * 2.0f, R), lo + modf_glsl(base + q * 3.0f, R),
+                lo + modf_glsl(base + R, R));
+        range = R;
+    } else {
+        l = SampleWavelengths(l_h);
+        range = 720.0f - 390.0f;
+    }
     vec4 radiance = TracePath(c, l, ray, &seed, events, depth_cap, nev);
-    vec3 wx = WaveToXYZ(c, l.x), wy = WaveToXYZ(c, l.y), wz = WaveToXYZ(c, l.z), ww = WaveToXYZ(c, l.w);
+    vec3 wx = WaveToXYZx(c, l.x), wy = WaveToXYZx(c, l.y), wz = WaveToXYZx(c, l.z), ww = WaveToXYZx(c, l.w);
     vec3 sum = add3(add3(add3(scl3(wx, radiance.x), scl3(wy, radiance.y)), scl3(wz, radiance.z)), scl3(ww, radiance.w));
-    vec3 color = scl3(scl3(sum, 720.0f - 390.0f), 0.25f);
+    vec3 color = scl3(scl3(sum, range), 0.25f);
     if (color.x != color.x) return mk3(0.0f, 0.0f, 0.0f);
     if (color.y != color.y) return mk3(0.0f, 0.0f, 0.0f);
     if (color.z != color.z) return mk3(0.0f, 0.0f, 0.0f);
@@ -1284,6 +1445,7 @@ void pto_wave_to_xyz(const float* cie, float wave, float* out3) {
     ctx_t c;
     memset(&c, 0, sizeof(c));
     c.u = u;
+    c.x = &kNoExt;
     vec3 r = WaveToXYZ(&c, wave);
     out3[0] = r.x;
     out3[1] = r.y;
@@ -1297,6 +1459,12 @@ float pto_sdf_material(const pt_sdf_plugin* pl, const float* p) { return plugin_
 /* SC:1492-1533 */
 int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plugins, int nplugins, float* accum,
                  int x0, int y0, int x1, int y1, const pto_trace* trace, int nthreads) {
+    return pto_dispatch_ext(ubo, NULL, pc, plugins, nplugins, accum, x0, y0, x1, y1, trace, nthreads);
+}
+
+int pto_dispatch_ext(const pt_ubo* ubo, const pt_scene_ext* ext, const pt_push* pc, const pt_sdf_plugin* plugins,
+                     int nplugins, float* accum, int x0, int y0, int x1, int y1, const pto_trace* trace, int nthreads) {
+    if (!ext) ext = &kNoExt;
     if (!ubo || !pc || !accum) return PT_ERR_INVALID;
     const int W = pc->resolution[0], H = pc->resolution[1];
     if (W <= 0 || H <= 0 || pc->samplesPerFrame <= 0) return PT_ERR_INVALID;
@@ -1320,6 +1488,7 @@ int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plug
         c.plug = plugins;
         c.nplug = nplugins;
         c.cameraPos = mk3(pc->cameraPosX, pc->cameraPosY, pc->cameraPosZ);
+        c.x = ext;
         c.cnt = (trace && trace->counters) ? cnt : NULL;
         tl_cnt = c.cnt;
         for (int x = x0; x < x1; x++) {
@@ -1527,6 +1696,7 @@ void pto_fn_intersection(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plug
     c.plug = plugins;
     c.nplug = nplugins;
     c.cameraPos = mk3(pc->cameraPosX, pc->cameraPosY, pc->cameraPosZ);
+    c.x = &kNoExt;
     hit_t h;
     h.hitdist = MAXDIST;
     h.normal = mk3(0.0f, 0.0f, 0.0f);

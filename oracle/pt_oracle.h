@@ -67,6 +67,10 @@ enum {
  */
 int pto_dispatch(const pt_ubo* ubo, const pt_push* pc, const pt_sdf_plugin* plugins, int nplugins,
                  float* accum, int x0, int y0, int x1, int y1, const pto_trace* trace, int nthreads);
+/* The same with the scene's full-form extensions (ext NULL: the reference's
+ * method; include/pt_cuda.h, pt_scene_ext). */
+int pto_dispatch_ext(const pt_ubo* ubo, const pt_scene_ext* ext, const pt_push* pc, const pt_sdf_plugin* plugins,
+                     int nplugins, float* accum, int x0, int y0, int x1, int y1, const pto_trace* trace, int nthreads);
 
 /* Primitives exposed for known-answer tests. */
 uint32_t pto_pcg32(uint32_t seed);

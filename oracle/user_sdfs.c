@@ -211,3 +211,50 @@ float user_menger_material(float x, float y, float z) {
     (void)z;
     return 2.0f;
 }
+
+/* ---- "fbm terrain": 8-octave value-noise height field ------------------
+ * The terrain SDF of pathtracer_gb300/scenes/menger_terrain_full.json: value
+ * noise on the integer lattice of the xz plane (an integer hash of the
+ * lattice point and the seed 7 to [0, 1)), smoothstep-weighted bilinear
+ * interpolation, 8 octaves of doubling frequency and halving amplitude,
+ * height scale 0.3; distance = half the vertical gap to the surface. */
+static float fbm_lattice(int ix, int iz) {
+    uint32_t h = (uint32_t)ix * 1597334677u + (uint32_t)iz * 3812015801u + 7u * 2654435761u;
+    h = (h ^ (h >> 16u)) * 2246822519u;
+    h = (h ^ (h >> 13u)) * 3266489917u;
+    h = h ^ (h >> 16u);
+    return (float)(h >> 8u) * (1.0f / 16777216.0f);
+}
+
+static float fbm_value_noise(float qx, float qz) {
+    const float ix = floorf(qx), iz = floorf(qz);
+    const float fx = qx - ix, fz = qz - iz;
+    const float ux = fx * fx * (3.0f - 2.0f * fx), uz = fz * fz * (3.0f - 2.0f * fz);
+    const int jx = (int)ix, jz = (int)iz;
+    const float a = fbm_lattice(jx, jz);
+    const float b = fbm_lattice(jx + 1, jz);
+    const float c = fbm_lattice(jx, jz + 1);
+    const float d = fbm_lattice(jx + 1, jz + 1);
+    const float ab = a * (1.0f - ux) + b * ux;
+    const float cd = c * (1.0f - ux) + d * ux;
+    return ab * (1.0f - uz) + cd * uz;
+}
+
+static float fbm_height(float x, float z) {
+    float h = 0.0f, amp = 0.5f, freq = 1.0f;
+    for (int o = 0; o < 8; o++) {
+        h += amp * (2.0f * fbm_value_noise(x * freq, z * freq) - 1.0f);
+        freq *= 2.0f;
+        amp *= 0.5f;
+    }
+    return 0.3f * h;
+}
+
+float user_fbm_sdf(float x, float y, float z) { return 0.5f * (y - fbm_height(x, z)); }
+
+float user_fbm_material(float x, float y, float z) {
+    (void)x;
+    (void)y;
+    (void)z;
+    return 0.0f;
+}

@@ -6,12 +6,17 @@
 // transforms written here with additions and multiplications only (no libm),
 // so a seed gives the same scene on every platform.
 //
-// Everything generated is expressible in the reference's scene schema
-// (src/pathtracer.cpp:110-185) and renders with its unmodified method.  The
-// reference's only surface model is the Lambertian Gaussian-spectrum BRDF
-// (src/shader.comp:1030-1038, 1075-1091), so the "mirror" and "dielectric"
-// material classes of a job mix map to Lambertian spectra of their own:
-// flat (sigma 1000) and inverted-bump respectively.
+// PT_GEN_SPHERES, PT_GEN_SDF and PT_GEN_SDF_VARIED are expressible in the
+// reference's scene schema (src/pathtracer.cpp:110-185) and render with its
+// unmodified method.  The reference's only surface model is the Lambertian
+// Gaussian-spectrum BRDF (src/shader.comp:1030-1038, 1075-1091), so there
+// the "mirror" and "dielectric" material classes of a job mix map to
+// Lambertian spectra of their own: flat (sigma 1000) and inverted-bump.
+// PT_GEN_SPHERES_FULL draws the same scenes (the same random stream) and
+// gives those two classes their full-form surface models (extension
+// "bsdf"): a conductor mirror of reflectance 0.9, and a Cauchy dielectric
+// whose A in [1.4, 1.7] and B in [0.002, 0.008] um^2 follow from the
+// inverted bump's two draws.
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -105,7 +110,7 @@ void add_sphere(pt_scene& S, float x, float y, float z, float r, int material, i
 // clamped to [0.03, 1]) on a ground plane at y = -2, lit by one blackbody
 // sphere light at 3000-9000 K; resolution uniform over {128, 256, 512,
 // 1024}^2, samples per pixel log-uniform over [4, 256], path length 8.
-void spheres_job(Rng& r, pt_scene& S, pt_job_spec& spec) {
+void spheres_job(Rng& r, pt_scene& S, pt_job_spec& spec, bool full) {
     static const int kRes[4] = {128, 256, 512, 1024};
     const int res = kRes[r.below(4)];
     spec.width = spec.height = res;
@@ -127,10 +132,21 @@ void spheres_job(Rng& r, pt_scene& S, pt_job_spec& spec) {
                 break;
             case 1:  // "mirror" class: flat spectrum
                 mat = add_material(S, 550.0f, 1000.0f, false);
+                if (full) {
+                    S.materials.back().bsdf = PT_BSDF_MIRROR;
+                    S.materials.back().bsdf_p[0] = 0.9f;
+                }
                 break;
-            default:  // "dielectric" class: inverted bump
+            default: {  // "dielectric" class: inverted bump
                 mat = add_material(S, (float)r.range(400.0, 700.0), (float)r.range(6.0, 12.0), true);
+                if (full) {
+                    MaterialD& m = S.materials.back();
+                    m.bsdf = PT_BSDF_CAUCHY;
+                    m.bsdf_p[0] = 1.4f + 0.3f * (m.reflection[0] - 400.0f) / 300.0f;
+                    m.bsdf_p[1] = 0.002f + 0.006f * (m.reflection[1] - 6.0f) / 6.0f;
+                }
                 break;
+            }
         }
         add_sphere(S, x, y, z, (float)rad, mat, 0);
     }
@@ -251,7 +267,8 @@ void sdf_job(Rng& r, pt_scene& S, pt_job_spec& spec, bool varied) {
 extern "C" {
 
 int pt_scene_generate(int kind, uint64_t seed, pt_scene** out, pt_job_spec* spec) {
-    if (!out || !spec || (kind != PT_GEN_SPHERES && kind != PT_GEN_SDF && kind != PT_GEN_SDF_VARIED))
+    if (!out || !spec ||
+        (kind != PT_GEN_SPHERES && kind != PT_GEN_SDF && kind != PT_GEN_SDF_VARIED && kind != PT_GEN_SPHERES_FULL))
         return PT_ERR_INVALID;
     *out = nullptr;
     pt_scene* S = new (std::nothrow) pt_scene();
@@ -261,8 +278,8 @@ int pt_scene_generate(int kind, uint64_t seed, pt_scene** out, pt_job_spec* spec
     spec->seed = seed;
     Rng r(seed);
     try {
-        if (kind == PT_GEN_SPHERES) {
-            spheres_job(r, *S, *spec);
+        if (kind == PT_GEN_SPHERES || kind == PT_GEN_SPHERES_FULL) {
+            spheres_job(r, *S, *spec, kind == PT_GEN_SPHERES_FULL);
         } else {
             sdf_job(r, *S, *spec, kind == PT_GEN_SDF_VARIED);
         }

@@ -56,6 +56,42 @@ const std::vector<Value>& list(const Value& root, const char* key) {
     return x->arr;
 }
 
+// A material's "bsdf" object (full-form extension): {"type": "flat",
+// "albedo"}, {"type": "smooth", "base", "amplitude", "center", "width"},
+// {"type": "mirror", "reflectance"}, {"type": "cauchy", "A", "B"},
+// {"type": "sellmeier", "B": [3], "C": [3]}.
+void load_bsdf(const Value& b, MaterialD& d) {
+    if (b.type == Value::Null) return;
+    const Value& t = req(b, "type", "material.bsdf");
+    if (t.type != Value::String) throw LoadError{"material.bsdf.type: expected a string"};
+    const std::string& k = t.s;
+    if (k == "flat") {
+        d.bsdf = PT_BSDF_FLAT;
+        d.bsdf_p[0] = num_f(req(b, "albedo", "material.bsdf"), "material.bsdf.albedo");
+    } else if (k == "smooth") {
+        d.bsdf = PT_BSDF_SMOOTH;
+        d.bsdf_p[0] = num_f(req(b, "base", "material.bsdf"), "material.bsdf.base");
+        d.bsdf_p[1] = num_f(req(b, "amplitude", "material.bsdf"), "material.bsdf.amplitude");
+        d.bsdf_p[2] = num_f(req(b, "center", "material.bsdf"), "material.bsdf.center");
+        d.bsdf_p[3] = num_f(req(b, "width", "material.bsdf"), "material.bsdf.width");
+    } else if (k == "mirror") {
+        d.bsdf = PT_BSDF_MIRROR;
+        d.bsdf_p[0] = num_f(req(b, "reflectance", "material.bsdf"), "material.bsdf.reflectance");
+    } else if (k == "cauchy") {
+        d.bsdf = PT_BSDF_CAUCHY;
+        d.bsdf_p[0] = num_f(req(b, "A", "material.bsdf"), "material.bsdf.A");
+        d.bsdf_p[1] = num_f(req(b, "B", "material.bsdf"), "material.bsdf.B");
+    } else if (k == "sellmeier") {
+        d.bsdf = PT_BSDF_SELLMEIER;
+        vec_f(req(b, "B", "material.bsdf"), d.bsdf_p, 3, "material.bsdf.B");
+        vec_f(req(b, "C", "material.bsdf"), d.bsdf_p + 3, 3, "material.bsdf.C");
+    } else if (k == "reference") {
+        d.bsdf = PT_BSDF_REFERENCE;
+    } else {
+        throw LoadError{"material.bsdf.type: unknown \"" + k + "\""};
+    }
+}
+
 void load(const Value& root, pt_scene& S) {
     if (root.type != Value::Object) throw LoadError{"scene: expected an object"};
     // Camera, PT:2576-2613.
@@ -155,6 +191,7 @@ void load(const Value& root, pt_scene& S) {
         d.reflection[0] = num_f(req(r, "peakWavelength", "material.reflection"), "material.peakWavelength");
         d.reflection[1] = num_f(req(r, "sigma", "material.reflection"), "material.sigma");
         d.reflection[2] = num_b(req(r, "isInvert", "material.reflection"), "material.isInvert") ? 1.0f : 0.0f;
+        if (const Value* b = o.find("bsdf")) load_bsdf(*b, d);
         S.materials.push_back(d);
     }
     for (const Value& o : list(root, "light")) {
@@ -163,6 +200,32 @@ void load(const Value& root, pt_scene& S) {
         d.emission[0] = num_f(req(e, "temperature", "light.emission"), "light.temperature");
         d.emission[1] = num_f(req(e, "luminosity", "light.emission"), "light.luminosity");
         S.lights.push_back(d);
+    }
+    // Full-form extensions (keys the reference's loader does not read).
+    if (const Value* env = root.find("environment"); env && env->type != Value::Null) {
+        S.ext.sky = true;
+        S.ext.sky_temperature = num_f(req(*env, "temperature", "environment"), "environment.temperature");
+        S.ext.sky_luminosity = num_f(req(*env, "luminosity", "environment"), "environment.luminosity");
+    }
+    if (const Value* sp = root.find("spectral"); sp && sp->type != Value::Null) {
+        if (const Value* r = sp->find("range"); r && r->type != Value::Null) {
+            float lr[2];
+            vec_f(*r, lr, 2, "spectral.range");
+            S.ext.range = true;
+            S.ext.lambda_min = lr[0];
+            S.ext.lambda_max = lr[1];
+        }
+        if (const Value* c = sp->find("cmf"); c && c->type != Value::Null) {
+            if (c->type != Value::String || (c->s != "analytic" && c->s != "table"))
+                throw LoadError{"spectral.cmf: \"analytic\" or \"table\""};
+            S.ext.analytic_cmf = c->s == "analytic";
+        }
+    }
+    if (const Value* m = root.find("march"); m && m->type != Value::Null) {
+        S.ext.march = true;
+        S.ext.march_max_steps = num_i(req(*m, "maxSteps", "march"), "march.maxSteps");
+        S.ext.march_epsilon = num_f(req(*m, "epsilon", "march"), "march.epsilon");
+        S.ext.march_max_distance = num_f(req(*m, "maxDistance", "march"), "march.maxDistance");
     }
 }
 
@@ -311,6 +374,44 @@ int pt_scene_pack_ubo(const pt_scene* s, const float* cie, pt_ubo* out) {
     std::copy(lights.begin(), lights.end(), out->lights);
     std::copy(lightIDs.begin(), lightIDs.end(), out->lightIDs);
     if (cie) std::memcpy(out->CIEXYZ1931, cie, sizeof(out->CIEXYZ1931));
+    return PT_OK;
+}
+
+// The scene's full-form extensions as the kernels take them; a scene
+// without any gives a zeroed block (the reference's method).
+int pt_scene_pack_ext(const pt_scene* s, pt_scene_ext* out) {
+    if (!s || !out) return PT_ERR_INVALID;
+    std::memset(out, 0, sizeof(pt_scene_ext));
+    const ExtD& x = s->ext;
+    if (x.sky) {
+        out->flags |= PT_EXT_SKY;
+        out->sky_temperature = x.sky_temperature;
+        out->sky_luminosity = x.sky_luminosity;
+    }
+    if (x.range) {
+        out->flags |= PT_EXT_WAVELENGTHS;
+        out->lambda_min = x.lambda_min;
+        out->lambda_max = x.lambda_max;
+    }
+    if (x.analytic_cmf) out->flags |= PT_EXT_ANALYTIC_CMF;
+    if (x.march) {
+        out->flags |= PT_EXT_MARCH;
+        out->march_max_steps = x.march_max_steps;
+        out->march_epsilon = x.march_epsilon;
+        out->march_max_distance = x.march_max_distance;
+    }
+    int last = 0;  // materials up to the last one with a model of its own
+    for (size_t i = 0; i < s->materials.size(); i++)
+        if (s->materials[i].bsdf != PT_BSDF_REFERENCE) last = (int)i + 1;
+    if (last > PT_MAX_EXT_MATERIALS) return PT_ERR_INVALID;
+    if (last > 0) {
+        out->flags |= PT_EXT_MATERIALS;
+        out->nmat = last;
+        for (int i = 0; i < last; i++) {
+            out->mat[i].type = s->materials[(size_t)i].bsdf;
+            std::memcpy(out->mat[i].p, s->materials[(size_t)i].bsdf_p, sizeof(out->mat[i].p));
+        }
+    }
     return PT_OK;
 }
 
@@ -476,6 +577,37 @@ int pt_scene_to_json(const pt_scene* s, char* buf, size_t cap, size_t* needed) {
             r.at_or_insert("peakWavelength") = rnum(d.reflection[0]);
             r.at_or_insert("sigma") = rnum(d.reflection[1]);
             r.at_or_insert("isInvert") = Value::make_bool(d.reflection[2] != 0.0f);
+            if (d.bsdf != PT_BSDF_REFERENCE) {
+                Value& b = o.at_or_insert("bsdf");
+                const float* p = d.bsdf_p;
+                switch (d.bsdf) {
+                    case PT_BSDF_FLAT:
+                        b.at_or_insert("type") = Value::make_string("flat");
+                        b.at_or_insert("albedo") = rnum(p[0]);
+                        break;
+                    case PT_BSDF_SMOOTH:
+                        b.at_or_insert("type") = Value::make_string("smooth");
+                        b.at_or_insert("base") = rnum(p[0]);
+                        b.at_or_insert("amplitude") = rnum(p[1]);
+                        b.at_or_insert("center") = rnum(p[2]);
+                        b.at_or_insert("width") = rnum(p[3]);
+                        break;
+                    case PT_BSDF_MIRROR:
+                        b.at_or_insert("type") = Value::make_string("mirror");
+                        b.at_or_insert("reflectance") = rnum(p[0]);
+                        break;
+                    case PT_BSDF_CAUCHY:
+                        b.at_or_insert("type") = Value::make_string("cauchy");
+                        b.at_or_insert("A") = rnum(p[0]);
+                        b.at_or_insert("B") = rnum(p[1]);
+                        break;
+                    default:
+                        b.at_or_insert("type") = Value::make_string("sellmeier");
+                        b.at_or_insert("B") = rvec(p, 3);
+                        b.at_or_insert("C") = rvec(p + 3, 3);
+                        break;
+                }
+            }
             a.arr.push_back(o);
         }
     }
@@ -488,6 +620,29 @@ int pt_scene_to_json(const pt_scene* s, char* buf, size_t cap, size_t* needed) {
             e.at_or_insert("luminosity") = rnum(d.emission[1]);
             a.arr.push_back(o);
         }
+    }
+    const ExtD& x = s->ext;
+    if (x.sky) {
+        Value& e = root.at_or_insert("environment");
+        e = Value::make_object();
+        e.at_or_insert("temperature") = rnum(x.sky_temperature);
+        e.at_or_insert("luminosity") = rnum(x.sky_luminosity);
+    }
+    if (x.range || x.analytic_cmf) {
+        Value& sp = root.at_or_insert("spectral");
+        sp = Value::make_object();
+        if (x.range) {
+            const float lr[2] = {x.lambda_min, x.lambda_max};
+            sp.at_or_insert("range") = rvec(lr, 2);
+        }
+        if (x.analytic_cmf) sp.at_or_insert("cmf") = Value::make_string("analytic");
+    }
+    if (x.march) {
+        Value& m = root.at_or_insert("march");
+        m = Value::make_object();
+        m.at_or_insert("maxSteps") = Value::make_int(x.march_max_steps);
+        m.at_or_insert("epsilon") = Value::make_float((double)x.march_epsilon);
+        m.at_or_insert("maxDistance") = rnum(x.march_max_distance);
     }
     const std::string text = ptjson::dump(root, 4);
     if (needed) *needed = text.size() + 1;
@@ -506,7 +661,14 @@ int pt_scene_bind(pt_ctx* ctx, const pt_scene* s, const float* cie) {
         for (const SdfD& d : s->sdfs) src.push_back(d.source.c_str());
         rc = pt_set_sdfs(ctx, src.data(), (int)src.size());
     }
-    if (rc == PT_OK) rc = pt_upload_scene(ctx, ubo);
+    pt_scene_ext* ext = nullptr;
+    if (rc == PT_OK) {
+        ext = new (std::nothrow) pt_scene_ext;
+        if (!ext) rc = PT_ERR_OOM;
+    }
+    if (rc == PT_OK) rc = pt_scene_pack_ext(s, ext);
+    if (rc == PT_OK) rc = pt_upload_scene_ext(ctx, ubo, ext->flags ? ext : nullptr);
+    delete ext;
     delete ubo;
     return rc;
 }

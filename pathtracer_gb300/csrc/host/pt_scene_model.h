@@ -36,6 +36,10 @@ struct SdfD {
 };
 struct MaterialD {
     float reflection[3];  // peak wavelength, sigma, isInvert (0/1)
+    // Full-form extension ("bsdf" key, not read by the reference):
+    // PT_BSDF_* and its parameters (pt_cuda.h, pt_material_ext).
+    int bsdf = 0;
+    float bsdf_p[6] = {0, 0, 0, 0, 0, 0};
 };
 struct LightD {
     float emission[2];  // temperature, luminosity
@@ -49,8 +53,22 @@ struct CameraD {
     float size, apertureSize, apertureDist, lensRadius, lensFocalLength, lensThickness, lensDistance;
 };
 
+// Scene-level full-form extensions ("environment", "spectral", "march" keys,
+// not read by the reference): pt_scene_ext without the material table.
+struct ExtD {
+    bool sky = false;
+    float sky_temperature = 0, sky_luminosity = 0;
+    bool range = false;
+    float lambda_min = 0, lambda_max = 0;
+    bool analytic_cmf = false;
+    bool march = false;
+    int march_max_steps = 512;
+    float march_epsilon = 1e-4f, march_max_distance = 0;
+};
+
 struct pt_scene {
     CameraD camera{};
+    ExtD ext;
     std::vector<ShotD> shots;
     std::vector<SphereD> spheres;
     std::vector<PlaneD> planes;

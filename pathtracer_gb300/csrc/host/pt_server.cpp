@@ -26,6 +26,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <new>
 #include <string>
 #include <thread>
@@ -41,6 +42,7 @@ struct SceneEntry {
     pt_ubo* ubo = nullptr;  // host copy for the plain path's uploads
     std::vector<pt_sdf_plugin> plugins;
     std::vector<std::string> sources;  // SDF texts (scenes added with sources)
+    std::shared_ptr<pt_scene_ext> ext;  // full-form extensions (null: the reference's method)
     int ref_target = -1;
     int ref_w = 0, ref_h = 0;
 };
@@ -265,7 +267,7 @@ int poll_plain(pt_server* s) {
             } else {
                 rc = pt_set_sdf_plugins(s->ctx, sc.plugins.data(), (int)sc.plugins.size());
             }
-            if (rc == PT_OK) rc = pt_upload_scene(s->ctx, sc.ubo);
+            if (rc == PT_OK) rc = pt_upload_scene_ext(s->ctx, sc.ubo, sc.ext.get());
             if (rc != PT_OK) return from_ctx(s, rc, "upload");
             s->ctx_scene = j.req.scene_key;
         }
@@ -392,6 +394,17 @@ int pt_server_add_scene_sources(pt_server* s, int key, const pt_ubo* ubo, const 
     e.sources.assign(sources, sources + n);
     s->scenes[key] = std::move(e);
     s->resident_bytes += sizeof(pt_ubo);
+    return PT_OK;
+}
+
+int pt_server_set_scene_ext(pt_server* s, int key, const pt_scene_ext* ext) {
+    if (!s) return PT_ERR_INVALID;
+    auto it = s->scenes.find(key);
+    if (it == s->scenes.end()) return sfail(s, PT_ERR_INVALID, "pt_server_set_scene_ext: unknown scene key");
+    const int rc = pt_batch_set_scene_ext(s->batch, it->second.batch_scene, ext);
+    if (rc != PT_OK) return from_batch(s, rc, "pt_server_set_scene_ext");
+    it->second.ext = ext ? std::make_shared<pt_scene_ext>(*ext) : nullptr;
+    if (s->ctx_scene == key) s->ctx_scene = -1;  // the plain path uploads it again
     return PT_OK;
 }
 

@@ -564,8 +564,15 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
     }
     const float k = sign_glsl(scene_sdf_cold(S, org, set1));
     int hit_sel = -2;  // >= -1 once the march converged (scene_sdf_material_hit)
+    // The reference's limits (512 steps, |d| < 1e-4, no distance cap) or the
+    // scene's PT_EXT_MARCH ones.
+    const bool xm = (S.ext.flags & PT_EXT_MARCH) != 0;
+    const int maxSteps = xm ? S.ext.march_max_steps : 512;
+    const float eps = xm ? S.ext.march_epsilon : 1e-4f;
+    const float tmax = xm ? S.ext.march_max_distance : __int_as_float(0x7f800000);
 #pragma unroll 1
-    for (int i = 0; i < 512; i++) {
+    for (int i = 0; i < maxSteps; i++) {
+        if (t > tmax) return false;  // past the distance cap: no SDF hit
         int sel;
         const float radius = scene_sdf_sel(S, p, set1, sel);
         if (insT > (fabsf(previousRadius) + fabsf(radius))) {
@@ -576,7 +583,7 @@ PT_DI bool sphere_trace(const KScene& S, float3 org, float3 dir, Hit& h) {
             p = fma3s(dir, t, org);
             continue;
         }
-        if (fabsf(radius) < 1e-4f) {
+        if (fabsf(radius) < eps) {
             hit_sel = sel;
             break;
         }

@@ -215,6 +215,7 @@ PT_DI void march_rays(const WfArgs& A) {
     float2 tmm = make_float2(0.0f, 0.0f);
     uint32_t set1 = 0;
     int points = 0, iter = 0;
+    bool xmarch = false;  // the ray's scene sets march limits (PT_EXT_MARCH; read from it where used)
     int hit_sel = -2;  // >= -1 once the lane's march converged (scene_sdf_material_hit)
     bool shadow_ray = false;
     const float omegaMax = kOmegaMax, omegaSpeed = 0.20f, e = 1e-4f;
@@ -270,6 +271,7 @@ PT_DI void march_rays(const WfArgs& A) {
                     set1 = __float_as_uint(a1.w);
                     iter = (int)(saved & 1023u);
                     points = (int)((saved >> 10) & 0xffffu);
+                    xmarch = (Sp->ext.flags & PT_EXT_MARCH) != 0;
                     p = fma3s(dir, t, org);
                     phase = (saved & 0x80000000u) ? MP_STEP : MP_SIGN;
                 } else {
@@ -313,13 +315,15 @@ PT_DI void march_rays(const WfArgs& A) {
             } else if (phase == MP_STEP) {
                 const float radius = val;
                 bool exitLoop = false;
-                if (insT > (fabsf(prevR) + fabsf(radius))) {
+                if (xmarch && t > Sp->ext.march_max_distance) {
+                    finished = true;  // past the distance cap: no SDF hit
+                } else if (insT > (fabsf(prevR) + fabsf(radius))) {
                     t -= insT;
                     omega = 1.0f;
                     insT = prevR * omega * k;
                     t += insT;
                     p = fma3s(dir, t, org);
-                } else if (fabsf(radius) < 1e-4f) {
+                } else if (fabsf(radius) < (xmarch ? Sp->ext.march_epsilon : 1e-4f)) {
                     exitLoop = true;
                     hit_sel = esel;
                 } else {
@@ -354,7 +358,7 @@ PT_DI void march_rays(const WfArgs& A) {
                 }
                 if (!finished && !exitLoop) {
                     iter++;
-                    if (iter >= 512) exitLoop = true;
+                    if (iter >= (xmarch ? Sp->ext.march_max_steps : 512)) exitLoop = true;
                 }
                 if (exitLoop) {
                     if (t < hitdist) {

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
         if (!active) {
             // Finish sample k-1 (SC:1477-1489, SC:1514-1516) and start sample k.
             if (k > 0) {
-                const float3 color = sample_color(ps, P.cie);
+                const float3 color = sample_color(ps, S, P.cie);
                 if (TRACE) {
                     const size_t p = pix * (size_t)spf + (size_t)(k - 1);
                     if (P.trace.nevents) P.trace.nevents[p] = (uint32_t)ps.bounce;
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
                 sum = sum + color;
             }
             if (k >= spf) break;
-            start_sample(ps, pc, camS, xx, yy, uvx, uvy, k);
+            start_sample(ps, S, pc, camS, xx, yy, uvx, uvy, k);
             k++;
             shadow = false;
             active = depth > 0;

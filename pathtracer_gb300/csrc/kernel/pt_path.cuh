@@ -24,6 +24,20 @@ PT_DI float rnd(uint32_t& seed) {
 PT_DI float cie_at(const float* __restrict__ cie, int i) {
     return ((unsigned)i < (unsigned)PT_CIE_TABLE_SIZE) ? __ldg(cie + i) : 0.0f;
 }
+// One lobe of the multi-lobe Gaussian CIE fit (Wyman, Sloan and Shirley
+// 2013): a Gaussian with a different width on each side of its peak.
+PT_DI float cmf_lobe(float x, float mu, float s1, float s2) {
+    const float t = (x - mu) / ((x < mu) ? s1 : s2);
+    return ptm_expf(-0.5f * t * t);
+}
+// The fit itself at wavelength `wave` (nm), for PT_EXT_ANALYTIC_CMF.
+PT_DI float3 cmf_analytic(float wave) {
+    const float x = (1.056f * cmf_lobe(wave, 599.8f, 37.9f, 31.0f) + 0.362f * cmf_lobe(wave, 442.0f, 16.0f, 26.7f)) -
+                    0.065f * cmf_lobe(wave, 501.1f, 20.4f, 26.2f);
+    const float y = 0.821f * cmf_lobe(wave, 568.8f, 46.9f, 40.5f) + 0.286f * cmf_lobe(wave, 530.9f, 16.3f, 31.1f);
+    const float z = 1.217f * cmf_lobe(wave, 437.0f, 11.8f, 36.0f) + 0.681f * cmf_lobe(wave, 459.0f, 26.0f, 13.8f);
+    return f3(x, y, z);
+}
 PT_DI float3 wave_to_xyz(const float* __restrict__ cie, float wave) {
     float3 r = f3(0.0f, 0.0f, 0.0f);
     if ((wave >= 360.0f) && (wave <= 800.0f)) {
@@ -175,6 +189,7 @@ struct PathState {
     float mis;               // MISBRDFWeight
     uint32_t seed;
     int bounce;
+    int medium;  // extension dielectrics: bit 0 while the path is inside one, bit 1 once it carries l.x alone
     // Between a primary hit and its shadow ray:
     float3 nrm, shDir;
     float4 brdf;
@@ -186,8 +201,8 @@ struct PathState {
 // GenerateSeed + SSAA + camera + aperture + hero wavelength + TracePathLens +
 // SampleWavelengths (SC:948-974, SC:1446-1472) for sample k of pixel
 // (xx, yy) with uv the pixel's centre coordinate.
-PT_DI void start_sample(PathState& ps, const pt_push& pc, const CamInfo& cam, uint32_t xx, uint32_t yy, float uvx,
-                        float uvy, int k) {
+PT_DI void start_sample(PathState& ps, const KScene& S, const pt_push& pc, const CamInfo& cam, uint32_t xx,
+                        uint32_t yy, float uvx, float uvy, int k) {
     const int W = pc.resolution[0], H = pc.resolution[1];
     uint32_t seed = pcg32((uint32_t)(pc.frame - pc.samplesPerFrame + k)) + (xx + (uint32_t)W * yy);
     const float jx = 2.0f * rnd(seed) - 0.5f;
@@ -206,7 +221,8 @@ PT_DI void start_sample(PathState& ps, const pt_push& pc, const CamInfo& cam, ui
     ptm_sincosf(phi, &sp, &cp);
     const float3 poa = camPos + mul_vm(f3(ha * (dd * cp), ha * (dd * sp), pc.apertureDist), cam.cam);
     float3 dir = normalize3(poa - org);
-    const float lh = mix_glsl(360.0f, 800.0f, rnd(seed));
+    const bool xrange = (S.ext.flags & PT_EXT_WAVELENGTHS) != 0;
+    const float lh = xrange ? mix_glsl(S.ext.lambda_min, S.ext.lambda_max, rnd(seed)) : mix_glsl(360.0f, 800.0f, rnd(seed));
     {
         LensGeom cl;
         cl.pos = cam.lensPos;
@@ -239,9 +255,16 @@ PT_DI void start_sample(PathState& ps, const pt_push& pc, const CamInfo& cam, ui
             dir = refract3(dir, h.normal, n12);
         }
     }
-    const float base = lh - 390.0f;
-    ps.l = f4(390.0f + mod_glsl(base + 82.5f, 330.0f), 390.0f + mod_glsl(base + 165.0f, 330.0f),
-              390.0f + mod_glsl(base + 247.5f, 330.0f), 390.0f + mod_glsl(base + 330.0f, 330.0f));
+    if (xrange) {  // the hero and three rotations a quarter of the range apart
+        const float lo = S.ext.lambda_min, R = S.ext.lambda_max - S.ext.lambda_min;
+        const float base = lh - lo, q = R * 0.25f;
+        ps.l = f4(lo + mod_glsl(base + q, R), lo + mod_glsl(base + q * 2.0f, R), lo + mod_glsl(base + q * 3.0f, R),
+                  lo + mod_glsl(base + R, R));
+    } else {
+        const float base = lh - 390.0f;
+        ps.l = f4(390.0f + mod_glsl(base + 82.5f, 330.0f), 390.0f + mod_glsl(base + 165.0f, 330.0f),
+                  390.0f + mod_glsl(base + 247.5f, 330.0f), 390.0f + mod_glsl(base + 330.0f, 330.0f));
+    }
     ps.org = org;
     ps.dir = dir;
     ps.seed = seed;
@@ -249,6 +272,7 @@ PT_DI void start_sample(PathState& ps, const pt_push& pc, const CamInfo& cam, ui
     ps.rr = f4s(1.0f);
     ps.mis = 1.0f;
     ps.bounce = 0;
+    ps.medium = 0;
 }
 
 // What the caller does after a shading step.
@@ -261,9 +285,7 @@ enum StepResult {
 // BRDF throughput and Russian roulette, SC:1373-1385, then the pathLength
 // check of TracePath (SC:1400).
 template <bool TRACE>
-PT_DI StepResult finish_bounce(PathState& ps, int depth) {
-    const float costheta = dot3(ps.dir, ps.nrm);
-    ps.rr = ps.rr * ((ps.brdf * costheta) / ps.brdfPdf);
+PT_DI StepResult roulette(PathState& ps, int depth) {
     const float rp = fminf(fmaxf(fmaxf(ps.rr.x, fmaxf(ps.rr.y, fmaxf(ps.rr.z, ps.rr.w))), 0.0f), 0.99f);
     if (rnd(ps.seed) > rp) {
         if (TRACE) ps.ev |= PT_EV_RR_KILL;
@@ -274,6 +296,110 @@ PT_DI StepResult finish_bounce(PathState& ps, int depth) {
     ps.bounce++;
     return (ps.bounce >= depth) ? STEP_TERMINATED : STEP_CONTINUE;
 }
+template <bool TRACE>
+PT_DI StepResult finish_bounce(PathState& ps, int depth) {
+    const float costheta = dot3(ps.dir, ps.nrm);
+    ps.rr = ps.rr * ((ps.brdf * costheta) / ps.brdfPdf);
+    return roulette<TRACE>(ps, depth);
+}
+
+// ---- extension surface models (PT_EXT_MATERIALS) ----
+// The extension entry of a hit's material (0-based index floor(materialID)),
+// or null for the reference's Lambertian.
+PT_DI const pt_material_ext* ext_material(const KScene& S, float materialID) {
+    if (!(S.ext.flags & PT_EXT_MATERIALS)) return nullptr;
+    const int mi = (int)floorf(materialID);
+    if (mi < 0 || mi >= S.ext.nmat || mi >= PT_MAX_EXT_MATERIALS) return nullptr;
+    const pt_material_ext* m = &S.ext.mat[mi];
+    return (m->type == PT_BSDF_REFERENCE) ? nullptr : m;
+}
+// Refractive index of an extension dielectric at wavelength l (nm).
+PT_DI float ext_ior(const pt_material_ext& m, float l) {
+    const float u = l * 1e-3f;
+    const float u2 = u * u;
+    if (m.type == PT_BSDF_CAUCHY) return m.p[0] + m.p[1] / u2;
+    float n2 = 1.0f;
+    n2 += (m.p[0] * u2) / (u2 - m.p[3]);
+    n2 += (m.p[1] * u2) / (u2 - m.p[4]);
+    n2 += (m.p[2] * u2) / (u2 - m.p[5]);
+    return sqrtf(n2);
+}
+// Unpolarised Fresnel reflectance for relative index eta = n1 / n2 at
+// incidence cosine cosi (>= 0); 1 under total internal reflection.  *cost
+// receives the transmitted cosine.
+PT_DI float fresnel_dielectric(float eta, float cosi, float* cost) {
+    const float sin2t = (eta * eta) * (1.0f - cosi * cosi);
+    if (sin2t >= 1.0f) {
+        *cost = 0.0f;
+        return 1.0f;
+    }
+    const float ct = sqrtf(1.0f - sin2t);
+    const float rs = (eta * cosi - ct) / (eta * cosi + ct);
+    const float rp = (cosi - eta * ct) / (cosi + eta * ct);
+    *cost = ct;
+    return 0.5f * (rs * rs + rp * rp);
+}
+// The reflectance of a Lambertian extension material at the four wavelengths, / PI.
+PT_DI float4 ext_lambert(const pt_material_ext& m, float4 l) {
+    if (m.type == PT_BSDF_FLAT) return f4s(m.p[0]) / PT_PI;
+    const float4 x = f4((l.x - m.p[2]) / m.p[3], (l.y - m.p[2]) / m.p[3], (l.z - m.p[2]) / m.p[3],
+                        (l.w - m.p[2]) / m.p[3]);
+    const float4 v = f4(m.p[0] + m.p[1] * ptm_expf(-(x.x * x.x)), m.p[0] + m.p[1] * ptm_expf(-(x.y * x.y)),
+                        m.p[0] + m.p[1] * ptm_expf(-(x.z * x.z)), m.p[0] + m.p[1] * ptm_expf(-(x.w * x.w)));
+    return v / PT_PI;
+}
+// A specular bounce off a mirror or dielectric: the new direction from the
+// hit point, the throughput, MIS weight 1 for the emitter the next ray may
+// hit (no light sample was taken here), then Russian roulette.  Dielectrics
+// choose reflection or transmission by the Fresnel reflectance at the first
+// wavelength (l.x); a reflection keeps every wavelength, weighted by its own
+// reflectance over the chosen one; a transmission bends each wavelength
+// differently, so from the first transmission on the path carries l.x
+// alone, with 4x its throughput (the sample's colour averages the four
+// wavelengths).  Returns the step result.
+template <bool TRACE>
+PT_DI StepResult shade_specular(PathState& ps, const pt_material_ext& m, const Hit& h, int depth) {
+    ps.org = fma3s(ps.dir, h.hitdist, ps.org);
+    float3 n = h.normal;
+    float c = dot3(ps.dir, n);
+    if (c > 0.0f) {  // face the incoming ray
+        n = f3(-n.x, -n.y, -n.z);
+        c = -c;
+    }
+    ps.nrm = n;
+    ps.mis = 1.0f;
+    const float cosi = -c;
+    if (m.type == PT_BSDF_MIRROR) {
+        ps.dir = ps.dir + n * (2.0f * cosi);
+        ps.rr = ps.rr * m.p[0];
+        if (TRACE) ps.ev |= PT_EV_SPECULAR;
+        return roulette<TRACE>(ps, depth);
+    }
+    const bool inside = (ps.medium & 1) != 0;
+    const float nh = ext_ior(m, ps.l.x);
+    const float eta = inside ? nh : 1.0f / nh;
+    float cost = 0.0f;
+    const float F = fresnel_dielectric(eta, cosi, &cost);
+    if (rnd(ps.seed) < F) {
+        ps.dir = ps.dir + n * (2.0f * cosi);
+        float ct;
+        const float ny = ext_ior(m, ps.l.y), nz = ext_ior(m, ps.l.z), nw = ext_ior(m, ps.l.w);
+        const float Fy = fresnel_dielectric(inside ? ny : 1.0f / ny, cosi, &ct);
+        const float Fz = fresnel_dielectric(inside ? nz : 1.0f / nz, cosi, &ct);
+        const float Fw = fresnel_dielectric(inside ? nw : 1.0f / nw, cosi, &ct);
+        ps.rr = f4(ps.rr.x, ps.rr.y * (Fy / F), ps.rr.z * (Fz / F), ps.rr.w * (Fw / F));
+        if (TRACE) ps.ev |= PT_EV_SPECULAR;
+    } else {
+        ps.dir = normalize3(ps.dir * eta + n * (eta * cosi - cost));
+        if (!(ps.medium & 2)) {  // the first transmission: l.x alone from here on
+            ps.rr = f4(ps.rr.x * 4.0f, 0.0f, 0.0f, 0.0f);
+            ps.medium |= 2;
+        }
+        ps.medium ^= 1;
+        if (TRACE) ps.ev |= PT_EV_REFRACT;
+    }
+    return roulette<TRACE>(ps, depth);
+}
 
 // TraceRay after Intersection (SC:1345-1391) for the path ray: emitter, miss,
 // or BRDF sampling + SampleLightSource (SC:1298-1343) up to the shadow ray.
@@ -282,7 +408,11 @@ PT_DI StepResult shade_primary(PathState& ps, const KScene& S, const Hit& h, int
     if (TRACE) ps.ev = PT_EV_VALID;
     if (!(h.hitdist < PT_MAXDIST)) {
         if (TRACE) ps.ev |= PT_EV_HIT_MISS;
-        ps.radiance = ps.radiance + f4s(0.0f);
+        if (S.ext.flags & PT_EXT_SKY) {  // no light sample reaches the sky: weight 1
+            ps.radiance = ps.radiance + emit(ps.l, S.ext.sky_temperature, S.ext.sky_luminosity) * ps.rr;
+        } else {
+            ps.radiance = ps.radiance + f4s(0.0f);
+        }
         ps.bounce++;
         return STEP_TERMINATED;
     }
@@ -294,8 +424,14 @@ PT_DI StepResult shade_primary(PathState& ps, const KScene& S, const Hit& h, int
         ps.bounce++;
         return STEP_TERMINATED;
     }
-    const float3 mat = material_mix(S, h.materialID);
-    ps.brdf = evaluate_brdf(ps.l, mat.x, mat.y, mat.z);
+    const pt_material_ext* xm = ext_material(S, h.materialID);
+    if (xm && xm->type >= PT_BSDF_MIRROR) return shade_specular<TRACE>(ps, *xm, h, depth);
+    if (xm) {
+        ps.brdf = ext_lambert(*xm, ps.l);
+    } else {
+        const float3 mat = material_mix(S, h.materialID);
+        ps.brdf = evaluate_brdf(ps.l, mat.x, mat.y, mat.z);
+    }
     ps.nrm = h.normal;
     ps.org = fma3s(ps.dir, h.hitdist, ps.org);
     {  // SampleBRDF: cosine direction via the unit sphere, SC:984-1003.
@@ -374,11 +510,23 @@ PT_DI StepResult shade_shadow(PathState& ps, const KScene& S, int objectID, int 
 }
 
 // SC:1477-1489: the sample's XYZ with NaN rejection.
-PT_DI float3 sample_color(const PathState& ps, const float* __restrict__ cie) {
-    const float3 wx = wave_to_xyz(cie, ps.l.x), wy = wave_to_xyz(cie, ps.l.y);
-    const float3 wz = wave_to_xyz(cie, ps.l.z), ww = wave_to_xyz(cie, ps.l.w);
-    float3 color = (((wx * ps.radiance.x + wy * ps.radiance.y) + wz * ps.radiance.z) + ww * ps.radiance.w) *
-                   (720.0f - 390.0f) * 0.25f;
+PT_DI float3 sample_color(const PathState& ps, const KScene& S, const float* __restrict__ cie) {
+    float3 wx, wy, wz, ww;
+    if (S.ext.flags & PT_EXT_ANALYTIC_CMF) {
+        wx = cmf_analytic(ps.l.x);
+        wy = cmf_analytic(ps.l.y);
+        wz = cmf_analytic(ps.l.z);
+        ww = cmf_analytic(ps.l.w);
+    } else {
+        wx = wave_to_xyz(cie, ps.l.x);
+        wy = wave_to_xyz(cie, ps.l.y);
+        wz = wave_to_xyz(cie, ps.l.z);
+        ww = wave_to_xyz(cie, ps.l.w);
+    }
+    // 1 / pdf of a wavelength: the width of the range it is uniform over
+    const float range = (S.ext.flags & PT_EXT_WAVELENGTHS) ? (S.ext.lambda_max - S.ext.lambda_min) : (720.0f - 390.0f);
+    float3 color = (((wx * ps.radiance.x + wy * ps.radiance.y) + wz * ps.radiance.z) + ww * ps.radiance.w) * range *
+                   0.25f;
     if (color.x != color.x || color.y != color.y || color.z != color.z) color = f3(0.0f, 0.0f, 0.0f);
     return color;
 }

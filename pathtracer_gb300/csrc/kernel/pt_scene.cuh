@@ -38,6 +38,7 @@ struct KScene {
     pt_scene_meta meta;
     pt_sdf_plugin plug[PT_MAX_LIVE_SDFS];
     float rot[PT_MAX_SCENE_OBJECTS][9];
+    pt_scene_ext ext;  // full-form extensions; all zero: the reference's method
 };
 
 // Camera quantities that depend only on the push constants (SC:1456,

@@ -34,6 +34,15 @@
 
 namespace {
 
+// The flags word of s8: bit 30 the shadow-ray flag (kShadowFlag), bits
+// 28-29 the extension dielectrics' path bits (PathState::medium), the bounce
+// count below.
+constexpr uint32_t kMediumShift = 28;
+constexpr uint32_t kBounceMask = (1u << kMediumShift) - 1u;
+PT_DI uint32_t bounce_word(const PathState& ps) {
+    return ((uint32_t)ps.medium << kMediumShift) | ((uint32_t)ps.bounce & kBounceMask);
+}
+
 PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t& flags, uint32_t& sample,
                       uint32_t& job) {
     const float4 a = v.s0[slot], b = v.s1[slot], c = v.s2[slot], d = v.s3[slot];
@@ -52,7 +61,8 @@ PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t&
     const uint4 m = v.s8[slot];
     ps.seed = m.x;
     flags = m.y;
-    ps.bounce = (int)(m.y & 0x3fffffffu);
+    ps.bounce = (int)(m.y & kBounceMask);
+    ps.medium = (int)((m.y >> kMediumShift) & 3u);
     sample = m.z;
     ps.shObj = (int)m.w;
     const float4 e = v.s9[slot];
@@ -71,7 +81,7 @@ PT_DI void store_state(const PoolView& v, uint32_t slot, const PathState& ps, ui
     v.s5[slot] = ps.rr;
     v.s6[slot] = ps.radiance;
     v.s7[slot] = ps.l;
-    v.s8[slot] = make_uint4(ps.seed, flags | ((uint32_t)ps.bounce & 0x3fffffffu), sample, (uint32_t)ps.shObj);
+    v.s8[slot] = make_uint4(ps.seed, flags | bounce_word(ps), sample, (uint32_t)ps.shObj);
     v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
 }
 
@@ -176,7 +186,7 @@ __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
             const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
             const CamInfo cam = J.cam;
             PathState ps;
-            start_sample(ps, pc, cam, xx, yy, uvx, uvy, (int)k);
+            start_sample(ps, *J.scene, pc, cam, xx, yy, uvx, uvy, (int)k);
             ps.nrm = f3(0.0f, 0.0f, 0.0f);
             ps.shDir = f3(0.0f, 0.0f, 1.0f);
             ps.brdf = f4s(0.0f);
@@ -231,7 +241,8 @@ PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uin
     const uint4 m = v.s8[slot];
     ps.seed = m.x;
     flags = m.y;
-    ps.bounce = (int)(m.y & 0x3fffffffu);
+    ps.bounce = (int)(m.y & kBounceMask);
+    ps.medium = (int)((m.y >> kMediumShift) & 3u);
     sample = m.z;
     ps.shObj = (int)m.w;
     const float4 e = v.s9[slot];
@@ -246,7 +257,7 @@ PT_DI void store_after_shadow(const PoolView& v, uint32_t slot, const PathState&
                               bool trace) {
     v.s5[slot] = ps.rr;
     v.s6[slot] = ps.radiance;
-    v.s8[slot] = make_uint4(ps.seed, (uint32_t)ps.bounce & 0x3fffffffu, sample, (uint32_t)ps.shObj);
+    v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, (uint32_t)ps.shObj);
     if (trace) v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
 }
 
@@ -262,7 +273,7 @@ PT_DI void finish_shade(const WfArgs& A, const WfJob& J, const PathState& ps, St
         if (b < A.trace.cap) A.trace.events[p * (size_t)A.trace.cap + b] = ps.ev;
     }
     if (r == STEP_TERMINATED) {
-        const float3 col = sample_color(ps, J.cie);
+        const float3 col = sample_color(ps, *J.scene, J.cie);
         J.colors[sample] = make_float4(col.x, col.y, col.z, 0.0f);
         if (TRACE) {
             const size_t p = trace_index(pc, sample);
@@ -343,9 +354,8 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
                 v.s4[slot] = ps.brdf;
                 v.s5[slot] = ps.rr;
                 v.s6[slot] = ps.radiance;
-                v.s8[slot] = make_uint4(ps.seed, ((r == STEP_SHADOW) ? kShadowFlag : 0u) |
-                                                     ((uint32_t)ps.bounce & 0x3fffffffu),
-                                        sample, (uint32_t)ps.shObj);
+                v.s8[slot] = make_uint4(ps.seed, ((r == STEP_SHADOW) ? kShadowFlag : 0u) | bounce_word(ps), sample,
+                                        (uint32_t)ps.shObj);
                 v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
                 again = true;
                 // the light sample's shadow ray, or the next bounce
@@ -436,7 +446,7 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
                 const float uvx = (2.0f * (float)xx - (float)W) / (float)H;
                 const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
                 const CamInfo cam = J.cam;
-                start_sample(ps, pc, cam, xx, yy, uvx, uvy, (int)k);
+                start_sample(ps, *J.scene, pc, cam, xx, yy, uvx, uvy, (int)k);
                 shadow = false;
                 active = true;
             }
@@ -461,7 +471,7 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
                                         : shade_primary<false>(ps, S, h, objectID, depth);
             shadow = (r == STEP_SHADOW);
             if (r == STEP_TERMINATED) {
-                const float3 col = sample_color(ps, J.cie);
+                const float3 col = sample_color(ps, S, J.cie);
                 J.colors[local] = make_float4(col.x, col.y, col.z, 0.0f);
                 finished = true;
                 active = false;

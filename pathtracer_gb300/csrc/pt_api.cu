@@ -206,9 +206,15 @@ int pt_set_sdfs(pt_ctx* ctx, const char* const* sources, int n) {
     return PT_OK;
 }
 
-int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo) {
+int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo) { return pt_upload_scene_ext(ctx, ubo, nullptr); }
+
+int pt_upload_scene_ext(pt_ctx* ctx, const pt_ubo* ubo, const pt_scene_ext* ext) {
     if (!ctx) return PT_ERR_INVALID;
     if (!ubo) return fail(ctx, PT_ERR_INVALID, "pt_upload_scene: null ubo");
+    {
+        std::string why;
+        if (!pt_ext_valid(ext, &why)) return fail(ctx, PT_ERR_INVALID, "pt_upload_scene_ext: " + why);
+    }
     int n[7];
     const int caps[7] = {PT_MAX_OBJECTS_SIZE / 6, PT_MAX_OBJECTS_SIZE / 5, PT_MAX_OBJECTS_SIZE / 11,
                          PT_MAX_OBJECTS_SIZE / 12, PT_MAX_OBJECTS_SIZE / 16, PT_MAX_SDFS_SIZE / 6,
@@ -238,6 +244,11 @@ int pt_upload_scene(pt_ctx* ctx, const pt_ubo* ubo) {
     S.meta.offset[3] = S.meta.offset[2] + 11 * n[2];
     S.meta.offset[4] = S.meta.offset[3] + 12 * n[3];
     S.meta.total_objects = n[0] + n[1] + n[2] + n[3] + n[4];
+    if (ext) {
+        S.ext = *ext;
+    } else {
+        std::memset(&S.ext, 0, sizeof(S.ext));
+    }
     refresh_plugins(ctx);
 
     PT_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_cie, ubo->CIEXYZ1931, sizeof(float) * PT_CIE_TABLE_SIZE,

@@ -885,6 +885,28 @@ int pt_batch_release_target(pt_batch* b, int target_id) {
     return PT_OK;
 }
 
+int pt_batch_set_scene_ext(pt_batch* b, int scene_id, const pt_scene_ext* ext) {
+    if (!b) return PT_ERR_INVALID;
+    if (scene_id < 0 || scene_id >= (int)b->scenes.size() || !b->scenes[(size_t)scene_id].live)
+        return bfail(b, PT_ERR_INVALID, "pt_batch_set_scene_ext: unknown or released scene");
+    BatchScene& s = b->scenes[(size_t)scene_id];
+    if (s.passes_in_flight) return bfail(b, PT_ERR_BUSY, "pt_batch_set_scene_ext: passes still read the scene");
+    std::string why;
+    if (!pt_ext_valid(ext, &why)) return bfail(b, PT_ERR_INVALID, "pt_batch_set_scene_ext: " + why);
+    pt_scene_ext x;
+    if (ext) {
+        x = *ext;
+    } else {
+        std::memset(&x, 0, sizeof x);
+    }
+    PT_B_TRY(b, cudaSetDevice(b->device));
+    for (int e = 0; e < 2; e++)
+        if (b->engine_live[e]) PT_B_TRY(b, cudaStreamSynchronize(b->engine[e].stream));
+    PT_B_TRY(b, cudaMemcpyAsync(&s.d_scene->ext, &x, sizeof x, cudaMemcpyHostToDevice, b->stream));
+    PT_B_TRY(b, cudaStreamSynchronize(b->stream));  // the copy reads the stack
+    return PT_OK;
+}
+
 int pt_batch_release_scene(pt_batch* b, int scene_id) {
     if (!b) return PT_ERR_INVALID;
     if (scene_id < 0 || scene_id >= (int)b->scenes.size() || !b->scenes[(size_t)scene_id].live)

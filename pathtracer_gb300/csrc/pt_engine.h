@@ -19,6 +19,43 @@
 
 #include "kernel/pt_wavefront.h"
 
+#include <cmath>
+#include <string>
+
+// Checks a scene's extension block (NULL is the reference's method and
+// valid); *why receives the reason for a refusal.
+inline bool pt_ext_valid(const pt_scene_ext* x, std::string* why) {
+    if (!x) return true;
+    const int known = PT_EXT_SKY | PT_EXT_WAVELENGTHS | PT_EXT_ANALYTIC_CMF | PT_EXT_MARCH | PT_EXT_MATERIALS;
+    if (x->flags & ~known) return (*why = "unknown extension flags", false);
+    if ((x->flags & PT_EXT_SKY) && !(x->sky_temperature >= 0.0f && x->sky_luminosity >= 0.0f))
+        return (*why = "sky temperature and luminosity must be >= 0", false);
+    if (x->flags & PT_EXT_WAVELENGTHS) {
+        if (!(x->lambda_min > 0.0f && x->lambda_max > x->lambda_min && x->lambda_max < 1e5f))
+            return (*why = "wavelength range must satisfy 0 < min < max", false);
+        if (!(x->flags & PT_EXT_ANALYTIC_CMF) && (x->lambda_min < 360.0f || x->lambda_max > 800.0f))
+            return (*why = "the tabulated CIE table covers 360-800 nm: use the analytic CMF beyond it", false);
+    }
+    if ((x->flags & PT_EXT_MARCH) && !(x->march_max_steps >= 1 && x->march_max_steps <= 1023 &&
+                                        x->march_epsilon > 0.0f && x->march_max_distance > 0.0f))
+        return (*why = "march limits: 1..1023 steps, epsilon > 0, distance > 0", false);
+    if (x->flags & PT_EXT_MATERIALS) {
+        if (x->nmat < 0 || x->nmat > PT_MAX_EXT_MATERIALS) return (*why = "nmat out of range", false);
+        for (int i = 0; i < x->nmat; i++) {
+            const pt_material_ext& m = x->mat[i];
+            if (m.type < PT_BSDF_REFERENCE || m.type > PT_BSDF_SELLMEIER)
+                return (*why = "material " + std::to_string(i + 1) + ": unknown type", false);
+            for (int j = 0; j < 6; j++)
+                if (!std::isfinite(m.p[j])) return (*why = "material " + std::to_string(i + 1) + ": non-finite parameter", false);
+            if (m.type == PT_BSDF_SMOOTH && m.p[3] == 0.0f)
+                return (*why = "material " + std::to_string(i + 1) + ": zero width", false);
+            if (m.type == PT_BSDF_CAUCHY && !(m.p[0] > 0.0f))
+                return (*why = "material " + std::to_string(i + 1) + ": Cauchy A must be > 0", false);
+        }
+    }
+    return true;
+}
+
 struct WfEngine {
     int device = 0;
     cudaStream_t stream = nullptr;

@@ -40,6 +40,7 @@ PT_BATCH_ROUTE_PERSISTENT = 2
 PT_GEN_SPHERES = 0
 PT_GEN_SDF = 1
 PT_GEN_SDF_VARIED = 2
+PT_GEN_SPHERES_FULL = 3
 
 PT_SERVE_BATCHED = 0
 PT_SERVE_PLAIN = 1
@@ -104,6 +105,34 @@ class PtSdfPlugin(ctypes.Structure):
         ("kind", ctypes.c_int32),
         ("material_mode", ctypes.c_int32),
         ("material", ctypes.c_float * 3),
+    ]
+
+
+PT_EXT_SKY, PT_EXT_WAVELENGTHS, PT_EXT_ANALYTIC_CMF, PT_EXT_MARCH, PT_EXT_MATERIALS = 1, 2, 4, 8, 16
+PT_BSDF_REFERENCE, PT_BSDF_FLAT, PT_BSDF_SMOOTH, PT_BSDF_MIRROR, PT_BSDF_CAUCHY, PT_BSDF_SELLMEIER = range(6)
+PT_MAX_EXT_MATERIALS = 128
+PT_EV_SPECULAR = 1 << 24
+PT_EV_REFRACT = 1 << 25
+
+
+class PtMaterialExt(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("p", ctypes.c_float * 6)]
+
+
+class PtSceneExt(ctypes.Structure):
+    """pt_scene_ext: a scene's full-form extensions (all zero: the reference's method)."""
+
+    _fields_ = [
+        ("flags", ctypes.c_int32),
+        ("sky_temperature", ctypes.c_float),
+        ("sky_luminosity", ctypes.c_float),
+        ("lambda_min", ctypes.c_float),
+        ("lambda_max", ctypes.c_float),
+        ("march_max_steps", ctypes.c_int32),
+        ("march_epsilon", ctypes.c_float),
+        ("march_max_distance", ctypes.c_float),
+        ("nmat", ctypes.c_int32),
+        ("mat", PtMaterialExt * PT_MAX_EXT_MATERIALS),
     ]
 
 
@@ -240,6 +269,7 @@ CUDA_API = [
     ("pt_set_sdf_plugins", _i, [_vp, ctypes.POINTER(PtSdfPlugin), _i]),
     ("pt_parse_sdf_source", _i, [ctypes.c_char_p, ctypes.POINTER(PtSdfPlugin)]),
     ("pt_upload_scene", _i, [_vp, _vp]),
+    ("pt_upload_scene_ext", _i, [_vp, _vp, _vp]),
     ("pt_jit_check", _i, [ctypes.POINTER(ctypes.c_char_p), _i, _i, ctypes.c_char_p, _sz]),
     ("pt_glsl_translate", _i, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _sz, ctypes.POINTER(_sz),
                                ctypes.c_char_p, _sz]),
@@ -278,6 +308,7 @@ CUDA_API = [
     ("pt_batch_set_route", _i, [_vp, _i]),
     ("pt_batch_set_persist_refill", _i, [_vp, _i]),
     ("pt_batch_add_scene", _i, [_vp, _vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
+    ("pt_batch_set_scene_ext", _i, [_vp, _i, _vp]),
     ("pt_batch_add_scene_sources", _i, [_vp, _vp, ctypes.POINTER(ctypes.c_char_p), _i, ctypes.POINTER(_i)]),
     ("pt_batch_add_target", _i, [_vp, _i, _i, _i, ctypes.POINTER(_i)]),
     ("pt_batch_target_device_ptr", _vp, [_vp, _i]),
@@ -302,6 +333,7 @@ HOST_API = [
     ("pt_scene_free", None, [_vp]),
     ("pt_scene_counts", _i, [_vp, ctypes.POINTER(_i)]),
     ("pt_scene_pack_ubo", _i, [_vp, _vp, _vp]),
+    ("pt_scene_pack_ext", _i, [_vp, _vp]),
     ("pt_scene_push_constants", _i, [_vp, ctypes.POINTER(PtFrameState), ctypes.POINTER(PtPush)]),
     ("pt_scene_sdf_source", ctypes.c_char_p, [_vp, _i]),
     ("pt_scene_to_json", _i, [_vp, ctypes.c_char_p, _sz, ctypes.POINTER(_sz)]),
@@ -322,6 +354,7 @@ HOST_API = [
     ("pt_server_add_scene", _i, [_vp, _i, _vp, ctypes.POINTER(PtSdfPlugin), _i]),
     ("pt_server_add_scene_sources", _i, [_vp, _i, _vp, ctypes.POINTER(ctypes.c_char_p), _i]),
     ("pt_server_render_reference", _i, [_vp, _i, ctypes.POINTER(PtPush), _i, _i]),
+    ("pt_server_set_scene_ext", _i, [_vp, _i, _vp]),
     ("pt_server_submit", _i, [_vp, ctypes.POINTER(PtServerJob), ctypes.POINTER(ctypes.c_uint64)]),
     ("pt_server_poll", _i, [_vp, ctypes.POINTER(PtServerResult), _i, ctypes.POINTER(_i)]),
     ("pt_server_pending", _i, [_vp]),

@@ -87,6 +87,19 @@ class Scene:
             raise PathTracerError(rc, "scene overflows the uniform buffer arrays")
         return ubo
 
+    def pack_ext(self) -> native.PtSceneExt:
+        """pt_scene_pack_ext: the scene's full-form extensions (flags 0: none)."""
+        out = native.PtSceneExt()
+        rc = self._lib.pt_scene_pack_ext(self._h, ctypes.byref(out))
+        if rc != native.PT_OK:
+            raise PathTracerError(rc, "scene extensions do not fit pt_scene_ext")
+        return out
+
+    def ext_or_none(self):
+        """pack_ext(), or None for a scene of the reference's method."""
+        x = self.pack_ext()
+        return x if x.flags else None
+
     def push_constants(self, width: int, height: int, frame: int, current_samples: int, spf: int,
                        path_length: int, shot: int = 1, fps: float = 1.0 / 0.0166, persistence: float = 0.0625,
                        tonemap: int = 3) -> PtPush:
@@ -162,10 +175,13 @@ class Context:
         arr = (native.PtSdfPlugin * max(1, len(plugins)))(*plugins)
         self._check(self._lib.pt_set_sdf_plugins(self._h, arr, len(plugins)))
 
-    def upload_scene(self, ubo: np.ndarray):
+    def upload_scene(self, ubo: np.ndarray, ext=None):
         ubo = np.ascontiguousarray(ubo, np.float32)
         assert ubo.size == native.UBO_FLOATS
-        self._check(self._lib.pt_upload_scene(self._h, native.ptr(ubo)))
+        if ext is None:
+            self._check(self._lib.pt_upload_scene(self._h, native.ptr(ubo)))
+        else:
+            self._check(self._lib.pt_upload_scene_ext(self._h, native.ptr(ubo), ctypes.byref(ext)))
 
     def bind(self, scene: Scene, cie: np.ndarray):
         cie = np.ascontiguousarray(cie, np.float32)
@@ -315,6 +331,10 @@ class Batch:
         self._check(self._lib.pt_batch_add_scene(self._h, native.ptr(ubo), arr, len(plugins), ctypes.byref(out)))
         return out.value
 
+    def set_scene_ext(self, scene_id: int, ext):
+        """pt_batch_set_scene_ext (ext None: the reference's method)."""
+        self._check(self._lib.pt_batch_set_scene_ext(self._h, scene_id, ctypes.byref(ext) if ext is not None else None))
+
     def add_scene_sources(self, ubo: np.ndarray, sources: list[str]) -> int:
         """pt_batch_add_scene_sources: SDFs as text (shipped snippets or any GLSL)."""
         ubo = np.ascontiguousarray(ubo, np.float32)
@@ -441,6 +461,10 @@ class Server:
         ubo = np.ascontiguousarray(ubo, np.float32)
         arr = (ctypes.c_char_p * max(1, len(sources)))(*[t.encode() for t in sources])
         self._check(self._lib.pt_server_add_scene_sources(self._h, key, native.ptr(ubo), arr, len(sources)))
+
+    def set_scene_ext(self, key: int, ext):
+        """pt_server_set_scene_ext (ext None: the reference's method)."""
+        self._check(self._lib.pt_server_set_scene_ext(self._h, key, ctypes.byref(ext) if ext is not None else None))
 
     def render_reference(self, key: int, push: PtPush, spp: int, spp_per_pass: int = 32):
         self._check(self._lib.pt_server_render_reference(self._h, key, ctypes.byref(push), spp, spp_per_pass))

@@ -25,7 +25,7 @@ def per_sample(scene, W, H, spp, depth, rows=ROWS):
     tot = None
     for r in range(rows):
         y = (2 * r + 1) * H // (2 * rows)
-        c = oracle.count_work(ubo, push, compare.plugins_for(scene), rect=(0, y, W, y + 1))
+        c = oracle.count_work(ubo, push, compare.plugins_for(scene), rect=(0, y, W, y + 1), ext=scene.ext_or_none())
         tot = c if tot is None else {k: tot[k] + c[k] for k in c}
     n = tot["samples"]
     return {k: v / n for k, v in tot.items()}, {"rows": rows, "samples": n}
@@ -38,6 +38,9 @@ def main():
     out["mandelbulb_plane_1024x1024_64spp_depth6"] = per_sample(scene, 1024, 1024, 64, 6)
     scene = Scene.load(os.path.join(ROOT, "pathtracer_gb300", "scenes", "mandelbulb12_plane.json"))
     out["mandelbulb12_plane_1024x1024_64spp_depth6"] = per_sample(scene, 1024, 1024, 64, 6)
+    # the same fractal in the SDF-fractal configuration's full form (sky, spectra, march limits)
+    scene = Scene.load(os.path.join(ROOT, "pathtracer_gb300", "scenes", "mandelbulb12_plane_full.json"))
+    out["mandelbulb12_plane_full_1024x1024_64spp_depth6"] = per_sample(scene, 1024, 1024, 64, 6)
     # The mixed-job batch: the first 8 generated sphere jobs, 1 row each, weighted by their samples.
     tot, n = {}, 0
     for seed in range(8):

@@ -215,6 +215,30 @@ def test_scene_snippet_matches_its_c_restatement(pt):
     assert 1000 < iters < 12 * 1000
 
 
+def test_fbm_terrain_matches_its_c_restatement(pt):
+    """The value-noise fBm terrain of scenes/menger_terrain_full.json (uint
+    hashing, int lattice coordinates, 8 octaves), translated and built for the
+    CPU, agrees bit for bit with the oracle's restatement, negative lattice
+    coordinates included."""
+    import os
+
+    from conftest import SCENES
+    from oracle import oracle
+    from pathtracer_gb300 import Scene
+
+    src = Scene.load(os.path.join(SCENES, "menger_terrain_full.json")).sdf_sources()[1]
+    assert oracle.restatement_for(src) == ("user_fbm_sdf", "user_fbm_material")
+    lib = _cpu_build(pt, "fbm", {"t": src})
+    fs, fm = _fn(lib, "c_t_sdf"), _fn(lib, "c_t_mat")
+    rs, rm = oracle.user_fn("user_fbm_sdf"), oracle.user_fn("user_fbm_material")
+    pts = _points(n=6000, scale=20.0)
+    bad = sum(_bits(fs(*map(float, p))) != _bits(rs(*map(float, p))) for p in pts)
+    bad += sum(_bits(fm(*map(float, p))) != _bits(rm(*map(float, p))) for p in pts)
+    assert bad == 0, bad
+    vals = [rs(float(x), 0.0, float(z)) for x, _, z in pts[:500]]
+    assert max(abs(v) for v in vals) < 0.2 and len(set(vals)) > 400  # heights within +-0.3, a varied field
+
+
 HASHED = """
 // A hashed jitter: uint arithmetic, a side-effecting helper in a vector
 // constructor, swizzle assignment and boolean vectors.

@@ -35,6 +35,7 @@ def _check_same(text, product_scene, cie):
     b = product_scene.pack_ubo(cie)
     assert a.tobytes() == b.tobytes()
     assert ref.sdf_sources() == product_scene.sdf_sources()
+    assert bytes(ref.pack_ext()) == bytes(product_scene.pack_ext())  # full-form extensions (zero when absent)
     for shot in range(1, len(ref.shots) + 1):
         for args in ((64, 48, 8, 8, 8, 6), (1024, 1024, 64, 16, 16, 12), (37, 23, 3, 3, 3, 0)):
             pa = ref.push_constants(*args, shot=shot)
@@ -57,7 +58,7 @@ def test_pack_matches_on_generated_jobs(built):
     from pathtracer_gb300 import Scene, cie_analytic, native
 
     cie = cie_analytic()
-    for kind in (native.PT_GEN_SPHERES, native.PT_GEN_SDF, native.PT_GEN_SDF_VARIED):
+    for kind in (native.PT_GEN_SPHERES, native.PT_GEN_SDF, native.PT_GEN_SDF_VARIED, native.PT_GEN_SPHERES_FULL):
         for seed in range(6):
             text = Scene.generate(kind, seed)[0].to_json()  # the JSON writer rounds to 1e-5, as the reference's
             _check_same(text, Scene.parse(text), cie)
@@ -111,3 +112,47 @@ def test_pack_rejects_overflow():
     root["sphere"] = root["sphere"][:3]
     ubo = pack.RefScene(root).pack_ubo(None)
     assert ubo.dtype == np.float32 and ubo.size == pack.UBO_FLOATS and ubo[0] == 3.0
+
+
+def test_full_form_scenes_carry_their_extensions(built):
+    """The full-form scene files set exactly the extensions their
+    configurations name, and a reference-method scene sets none."""
+    import os
+
+    from oracle import pack
+
+    x = pack.load_scene(os.path.join(SCENES, "cornell_box_full.json")).pack_ext()
+    assert x.flags == pack.EXT_WAVELENGTHS | pack.EXT_ANALYTIC_CMF | pack.EXT_MATERIALS
+    assert (x.lambda_min, x.lambda_max) == (380.0, 780.0)
+    kinds = [x.mat[i].type for i in range(x.nmat)]
+    assert kinds[-2:] == [pack.BSDF_FLAT, pack.BSDF_CAUCHY] and set(kinds[:-2]) == {pack.BSDF_REFERENCE}
+    x = pack.load_scene(os.path.join(SCENES, "mandelbulb12_plane_full.json")).pack_ext()
+    assert x.flags == (pack.EXT_SKY | pack.EXT_WAVELENGTHS | pack.EXT_ANALYTIC_CMF | pack.EXT_MARCH |
+                       pack.EXT_MATERIALS)
+    assert (x.march_max_steps, np.float32(x.march_epsilon), x.march_max_distance) == (256, np.float32(1e-4), 50.0)
+    assert (x.sky_temperature, x.sky_luminosity) == (5800.0, 1.0)
+    x = pack.load_scene(os.path.join(SCENES, "menger_terrain_full.json")).pack_ext()
+    assert x.mat[x.nmat - 1].type == pack.BSDF_SELLMEIER
+    assert [round(v, 4) for v in x.mat[x.nmat - 1].p] == [1.04, 0.23, 1.01, 0.006, 0.02, 103.6]
+    assert pack.load_scene(os.path.join(SCENES, "cornell_box.json")).pack_ext().flags == 0
+
+
+def test_extension_json_round_trip(built):
+    """pt_scene_to_json writes the extension keys back; the written scene packs
+    to the same extension block."""
+    import os
+
+    from pathtracer_gb300 import Scene, native
+
+    for name in ("cornell_box_full", "mandelbulb12_plane_full", "menger_terrain_full"):
+        a = Scene.load(os.path.join(SCENES, name + ".json"))
+        b = Scene.parse(a.to_json())
+        assert bytes(a.pack_ext()) == bytes(b.pack_ext()), name
+    for seed in range(4):
+        a, _ = Scene.generate(native.PT_GEN_SPHERES_FULL, seed)
+        r, _ = Scene.generate(native.PT_GEN_SPHERES, seed)
+        assert a.pack_ubo(None).tobytes() == r.pack_ubo(None).tobytes()  # same scene, same random stream
+        x = a.pack_ext()
+        assert x.flags == native.PT_EXT_MATERIALS
+        kinds = {x.mat[i].type for i in range(x.nmat)}
+        assert kinds <= {native.PT_BSDF_REFERENCE, native.PT_BSDF_MIRROR, native.PT_BSDF_CAUCHY}
