@@ -293,6 +293,15 @@ int pt_set_drain_limit(pt_ctx* ctx, uint64_t max_iterations);
  * CPU.  Synchronous. */
 int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float* d_out, int n);
 
+/* Evaluates the two quartic surfaces the reference's shader defines but
+ * never calls (Thritorius, src/shader.comp:543-588, which 0; SmoothCuboid,
+ * :590-631, which 1; their call sites :926-931 and :1207-1216 are commented
+ * out, so no scene reaches them) for n rays: d_rays6 origin + direction per
+ * ray, d_hits6 the hit record (hitdist, normal, materialID, lightID) read and
+ * updated as the shader's inout arguments, d_flags the boolean result.
+ * Device arrays; synchronous.  For tests against the CPU restatement. */
+int pt_quartic_surface_eval(pt_ctx* ctx, int which, const float* d_rays6, float* d_hits6, int* d_flags, int n);
+
 /* ---- dispatch without allocating (not in the reference) -----------------
  * No counterpart in the reference.  One wavefront dispatch (the engine
  * PT_ENGINE_WAVEFRONT runs, bit-identical results) for callers that cannot

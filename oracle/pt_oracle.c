@@ -863,6 +863,96 @@ static int SphereTracing(const ctx_t* c, Ray ray, hit_t* h) {
     return 0;
 }
 
+/* SC:543-588: the quartic surface x^2(x^2 + 2y^2 - 6y + 2z^2) +
+ * y^2(y^2 + 2y + 2z^2) + z^2(10z^2 - 12) + 1 = 0 at the origin, in the
+ * ray's xzy frame.  The reference defines it but its call sites are
+ * commented out (SC:926-931, :1207-1216), so no scene reaches it. */
+static int Thritorius(Ray ray, hit_t* h) {
+    if (!BoundingSphere(ray, mk3(0.0f, 0.0f, 0.0f), 4.05f)) return 0;
+    vec3 o = xzy(ray.origin);
+    vec3 d = xzy(ray.dir);
+    vec3 ddd = mul3(mul3(d, d), d);
+    vec3 d10 = mk3(d.x, d.y, 10.0f * d.z);
+    vec3 o10 = mk3(o.x, o.y, 10.0f * o.z);
+    float a4 = dot3(d10, ddd) + 2.0f * dot3(mul3(d, d), mul3(yzx(d), yzx(d)));
+    vec3 dd2 = mk3(d.y * d.y + d.z * d.z, d.x * d.x + d.z * d.z, d.x * d.x + d.y * d.y);
+    float a3 = 4.0f * (dot3(o10, ddd) + dot3(mul3(o, d), dd2)) + 2.0f * d.y * d.y * d.y - 6.0f * d.x * d.x * d.y;
+    vec3 oxxy = mk3(o.x, o.x, o.y), dxxy = mk3(d.x, d.x, d.y), oyzz = mk3(o.y, o.z, o.z), dyzz = mk3(d.y, d.z, d.z);
+    float a2 = 6.0f * dot3(o10, mul3(mul3(o, d), d)) +
+               2.0f * ((o.x * o.x * (d.y * d.y) + o.y * o.y * (d.x * d.x)) +
+                       (o.x * o.x * (d.z * d.z) + o.z * o.z * (d.x * d.x)) +
+                       (o.y * o.y * (d.z * d.z) + o.z * o.z * (d.y * d.y))) +
+               8.0f * dot3(mul3(oxxy, dxxy), mul3(oyzz, dyzz)) + 6.0f * o.y * d.y * d.y - 6.0f * o.y * d.x * d.x -
+               12.0f * o.x * d.x * d.y - 12.0f * d.z * d.z;
+    float a1 = 4.0f * (dot3(mul3(mul3(o10, o), o), d) + (o.x * o.x * (o.y * d.y) + o.x * o.x * (o.z * d.z)) +
+                       (o.y * o.y * (o.x * d.x) + o.y * o.y * (o.z * d.z)) +
+                       (o.z * o.z * (o.x * d.x) + o.z * o.z * (o.y * d.y))) +
+               6.0f * o.y * o.y * d.y - 6.0f * o.x * o.x * d.y - 12.0f * o.x * o.y * d.x - 24.0f * o.z * d.z;
+    float a0 = dot3(o10, mul3(mul3(o, o), o)) + 2.0f * dot3(mul3(oxxy, oxxy), mul3(oyzz, oyzz)) +
+               2.0f * o.y * o.y * o.y - 6.0f * o.x * o.x * o.y - 12.0f * o.z * o.z + 1.0f;
+    float roots[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    int real[4];
+    SolveQuartic(a4, a3, a2, a1, a0, roots, real);
+    float t = 1e6f;
+    for (int i = 0; i < 4; i++) {
+        if (real[i]) {
+            if ((roots[i] < t) && (roots[i] > 0.0f)) t = roots[i];
+        }
+    }
+    if (t < h->hitdist) {
+        h->hitdist = t;
+        float x = o.x + d.x * t;
+        float y = o.y + d.y * t;
+        float z = o.z + d.z * t;
+        vec3 n;
+        n.x = 4.0f * x * x * x + 4.0f * x * y * y - 12.0f * x * y + 4.0f * x * z * z;
+        n.y = 40.0f * z * z * z + 4.0f * x * x * z + 4.0f * y * y * z - 24.0f * z;
+        n.z = 4.0f * y * y * y + 4.0f * x * x * y - 6.0f * x * x + 6.0f * y * y + 4.0f * y * z * z;
+        if ((o.x * o.x * (o.x * o.x + 2.0f * o.y * o.y - 6.0f * o.y + 2.0f * o.z * o.z) +
+             o.y * o.y * (o.y * o.y + 2.0f * o.y + 2.0f * o.z * o.z) + o.z * o.z * (10.0f * o.z * o.z - 12.0f) +
+             1.0f) < 0.0f)
+            n = scl3(n, -1.0f);
+        h->normal = normalize3(n);
+        h->materialID = 1.0f;
+        h->lightID = -1.0f;
+        return 1;
+    }
+    return 0;
+}
+
+/* SC:590-631: the superquadric x^4 + y^4 + z^4 = 1 at the origin (disabled
+ * in the reference like Thritorius). */
+static int SmoothCuboid(Ray ray, hit_t* h) {
+    if (!BoundingSphere(ray, mk3(0.0f, 0.0f, 0.0f), 1.80f)) return 0;
+    vec3 o = ray.origin;
+    vec3 d = ray.dir;
+    float a4 = dot3(mul3(d, d), mul3(d, d));
+    float a3 = 4.0f * dot3(o, mul3(mul3(d, d), d));
+    float a2 = 6.0f * dot3(mul3(o, o), mul3(d, d));
+    float a1 = 4.0f * dot3(mul3(mul3(o, o), o), d);
+    float a0 = dot3(mul3(o, o), mul3(o, o)) - 1.0f;
+    float roots[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    int real[4];
+    SolveQuartic(a4, a3, a2, a1, a0, roots, real);
+    float t = 1e6f;
+    for (int i = 0; i < 4; i++) {
+        if (real[i]) {
+            if ((roots[i] < t) && (roots[i] > 0.0f)) t = roots[i];
+        }
+    }
+    if (t < h->hitdist) {
+        h->hitdist = t;
+        vec3 n = fma3(d, mk3(t, t, t), o);
+        n = mul3(mul3(n, n), n);
+        if (dot3(mul3(o, o), mul3(o, o)) < 1.0f) n = scl3(n, -1.0f);
+        h->normal = normalize3(n);
+        h->materialID = 3.0f;
+        h->lightID = -1.0f;
+        return 1;
+    }
+    return 0;
+}
+
 static inline int NUM(const ctx_t* c, int k) { return (int)c->u->numObjects[k]; }
 
 static float lens_bounding_radius(lens_t o) {
@@ -1680,6 +1770,21 @@ int pto_fn_cyclide(const float* ray6, const float* o, float* hit6) {
                    o[13], (int)o[14], (int)o[15]};
     hit_t h = hit_of(hit6);
     int r = DupinCyclide(ray_of(ray6), c, &h);
+    put_hit(hit6, h);
+    return r;
+}
+
+int pto_fn_thritorius(const float* ray6, const float* o, float* hit6) {
+    (void)o;
+    hit_t h = hit_of(hit6);
+    int r = Thritorius(ray_of(ray6), &h);
+    put_hit(hit6, h);
+    return r;
+}
+int pto_fn_smooth_cuboid(const float* ray6, const float* o, float* hit6) {
+    (void)o;
+    hit_t h = hit_of(hit6);
+    int r = SmoothCuboid(ray_of(ray6), &h);
     put_hit(hit6, h);
     return r;
 }

@@ -45,7 +45,7 @@ FUNCTIONS = [
     "OrthonormalBasis", "ToWorld", "MISPowerHeuristicsBeta2", "EvalQuadratic", "EvalCubic",
     "EvalQuartic", "SolveCubic", "SolveQuartic", "minMaterial", "smin", "RotationMatrix", "SortMinMax",
     "BoundingSphere", "RayIntersectAABB", "SphereIntersection", "PlaneIntersection", "BoxIntersection",
-    "SphereSliceIntersection", "LensIntersection", "DupinCyclide",
+    "SphereSliceIntersection", "LensIntersection", "DupinCyclide", "Thritorius", "SmoothCuboid",
 ]
 # The shader's structs those functions take.
 STRUCTS = ["Ray", "sphere", "plane", "box", "sphereSlice", "lens", "cyclide"]
@@ -222,6 +222,18 @@ int refsh_cyclide(const float* r, const float* o, float* h) {
     c.lightID = (int)o[15];
     Hit t(h);
     const bool hit = ref_DupinCyclide(ray_of(r), c, t.d, t.n, t.m, t.l);
+    t.put(h);
+    return hit;
+}
+int refsh_thritorius(const float* r, const float*, float* h) {
+    Hit t(h);
+    const bool hit = ref_Thritorius(ray_of(r), t.d, t.n, t.m, t.l);
+    t.put(h);
+    return hit;
+}
+int refsh_smooth_cuboid(const float* r, const float*, float* h) {
+    Hit t(h);
+    const bool hit = ref_SmoothCuboid(ray_of(r), t.d, t.n, t.m, t.l);
     t.put(h);
     return hit;
 }

@@ -297,6 +297,76 @@ PT_DI bool cyclide_intersect(const KScene& S, float3 org, float3 dir, int base, 
     return false;
 }
 
+// The smallest positive real root of a4 t^4 + ... + a0 below 1e6 by the
+// shader's SolveQuartic and root scan (SC:505-541 with the loop of SC:560-567).
+// Thritorius, SC:543-588: a quartic surface at the origin in the ray's xzy
+// frame.  The shader defines it and SmoothCuboid but comments out their call
+// sites (SC:926-931, :1207-1216), so no scene reaches either; they are
+// built for completeness and evaluated through pt_quartic_surface_eval.
+PT_DI bool thritorius_intersect(float3 org, float3 dir, Hit& h) {
+    if (!bounding_sphere(org, dir, f3(0.0f, 0.0f, 0.0f), 4.05f)) return false;
+    const float3 o = sw_xzy(org), d = sw_xzy(dir);
+    const float3 ddd = (d * d) * d;
+    const float3 d10 = f3(d.x, d.y, 10.0f * d.z), o10 = f3(o.x, o.y, 10.0f * o.z);
+    const float a4 = dot3(d10, ddd) + 2.0f * dot3(d * d, sw_yzx(d) * sw_yzx(d));
+    const float3 dd2 = f3(d.y * d.y + d.z * d.z, d.x * d.x + d.z * d.z, d.x * d.x + d.y * d.y);
+    const float a3 = 4.0f * (dot3(o10, ddd) + dot3(o * d, dd2)) + 2.0f * d.y * d.y * d.y - 6.0f * d.x * d.x * d.y;
+    const float3 oxxy = f3(o.x, o.x, o.y), dxxy = f3(d.x, d.x, d.y), oyzz = f3(o.y, o.z, o.z), dyzz = f3(d.y, d.z, d.z);
+    const float a2 = 6.0f * dot3(o10, (o * d) * d) +
+                     2.0f * ((o.x * o.x * (d.y * d.y) + o.y * o.y * (d.x * d.x)) +
+                             (o.x * o.x * (d.z * d.z) + o.z * o.z * (d.x * d.x)) +
+                             (o.y * o.y * (d.z * d.z) + o.z * o.z * (d.y * d.y))) +
+                     8.0f * dot3(oxxy * dxxy, oyzz * dyzz) + 6.0f * o.y * d.y * d.y - 6.0f * o.y * d.x * d.x -
+                     12.0f * o.x * d.x * d.y - 12.0f * d.z * d.z;
+    const float a1 = 4.0f * (dot3((o10 * o) * o, d) + (o.x * o.x * (o.y * d.y) + o.x * o.x * (o.z * d.z)) +
+                             (o.y * o.y * (o.x * d.x) + o.y * o.y * (o.z * d.z)) +
+                             (o.z * o.z * (o.x * d.x) + o.z * o.z * (o.y * d.y))) +
+                     6.0f * o.y * o.y * d.y - 6.0f * o.x * o.x * d.y - 12.0f * o.x * o.y * d.x - 24.0f * o.z * d.z;
+    const float a0 = dot3(o10, (o * o) * o) + 2.0f * dot3(oxxy * oxxy, oyzz * oyzz) + 2.0f * o.y * o.y * o.y -
+                     6.0f * o.x * o.x * o.y - 12.0f * o.z * o.z + 1.0f;
+    const float t = solve_quartic_min_positive(a4, a3, a2, a1, a0);
+    if (t < h.hitdist) {
+        h.hitdist = t;
+        const float x = o.x + d.x * t;
+        const float y = o.y + d.y * t;
+        const float z = o.z + d.z * t;
+        float3 n = f3(4.0f * x * x * x + 4.0f * x * y * y - 12.0f * x * y + 4.0f * x * z * z,
+                      40.0f * z * z * z + 4.0f * x * x * z + 4.0f * y * y * z - 24.0f * z,
+                      4.0f * y * y * y + 4.0f * x * x * y - 6.0f * x * x + 6.0f * y * y + 4.0f * y * z * z);
+        if ((o.x * o.x * (o.x * o.x + 2.0f * o.y * o.y - 6.0f * o.y + 2.0f * o.z * o.z) +
+             o.y * o.y * (o.y * o.y + 2.0f * o.y + 2.0f * o.z * o.z) + o.z * o.z * (10.0f * o.z * o.z - 12.0f) +
+             1.0f) < 0.0f)
+            n = n * -1.0f;
+        h.normal = normalize3(n);
+        h.materialID = 1.0f;
+        h.lightID = -1.0f;
+        return true;
+    }
+    return false;
+}
+
+// SmoothCuboid, SC:590-631: x^4 + y^4 + z^4 = 1 at the origin.
+PT_DI bool smooth_cuboid_intersect(float3 o, float3 d, Hit& h) {
+    if (!bounding_sphere(o, d, f3(0.0f, 0.0f, 0.0f), 1.80f)) return false;
+    const float a4 = dot3(d * d, d * d);
+    const float a3 = 4.0f * dot3(o, (d * d) * d);
+    const float a2 = 6.0f * dot3(o * o, d * d);
+    const float a1 = 4.0f * dot3((o * o) * o, d);
+    const float a0 = dot3(o * o, o * o) - 1.0f;
+    const float t = solve_quartic_min_positive(a4, a3, a2, a1, a0);
+    if (t < h.hitdist) {
+        h.hitdist = t;
+        float3 n = fma3s(d, t, o);
+        n = (n * n) * n;
+        if (dot3(o * o, o * o) < 1.0f) n = n * -1.0f;
+        h.normal = normalize3(n);
+        h.materialID = 3.0f;
+        h.lightID = -1.0f;
+        return true;
+    }
+    return false;
+}
+
 // ---------------------------------------------------------------------------
 // SDF plug-ins: the four snippets of sdfs/<name>.glsl as __device__ functions
 // with the snippets' signature `float sdf(vec3 p)` / `float sdfmaterial(vec3 p)`.

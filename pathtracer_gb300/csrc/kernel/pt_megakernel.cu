@@ -62,6 +62,37 @@ __global__ void mathf_eval_kernel(int fn, const float* __restrict__ x, const flo
 }
 }  // namespace
 
+namespace {
+__global__ void quartic_surface_kernel(int which, const float* __restrict__ rays, float* __restrict__ hits,
+                                       int* __restrict__ flags, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* r = rays + 6 * (size_t)i;
+    float* hp = hits + 6 * (size_t)i;
+    Hit h;
+    h.hitdist = hp[0];
+    h.normal = f3(hp[1], hp[2], hp[3]);
+    h.materialID = hp[4];
+    h.lightID = hp[5];
+    const float3 o = f3(r[0], r[1], r[2]), d = f3(r[3], r[4], r[5]);
+    const bool hit = (which == 0) ? thritorius_intersect(o, d, h) : smooth_cuboid_intersect(o, d, h);
+    hp[0] = h.hitdist;
+    hp[1] = h.normal.x;
+    hp[2] = h.normal.y;
+    hp[3] = h.normal.z;
+    hp[4] = h.materialID;
+    hp[5] = h.lightID;
+    flags[i] = hit ? 1 : 0;
+}
+}  // namespace
+
+cudaError_t ptk_quartic_surface_eval(int which, const float* rays6, float* hits6, int* flags, int n,
+                                     cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    quartic_surface_kernel<<<(n + 127) / 128, 128, 0, stream>>>(which, rays6, hits6, flags, n);
+    return cudaGetLastError();
+}
+
 cudaError_t ptk_mathf_eval(int fn, const float* x, const float* y, float* out, int n, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     mathf_eval_kernel<<<(n + 255) / 256, 256, 0, stream>>>(fn, x, y, out, n);

@@ -27,4 +27,8 @@ cudaError_t ptk_launch_megakernel_analytic(const KParams* params, int variant, d
 // Evaluates a pt_mathf function over device arrays (verification hook):
 // fn 0 sin, 1 cos, 2 exp, 3 log, 4 pow(x, y), 5 acos.
 cudaError_t ptk_mathf_eval(int fn, const float* x, const float* y, float* out, int n, cudaStream_t stream);
+// thritorius_intersect (which 0) or smooth_cuboid_intersect (1) per ray:
+// rays6 origin + direction, hits6 the hit record in and out, flags the result.
+cudaError_t ptk_quartic_surface_eval(int which, const float* rays6, float* hits6, int* flags, int n,
+                                     cudaStream_t stream);
 #endif

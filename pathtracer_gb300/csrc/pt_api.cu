@@ -551,6 +551,16 @@ int pt_mathf_eval(pt_ctx* ctx, int fn, const float* d_x, const float* d_y, float
     return PT_OK;
 }
 
+int pt_quartic_surface_eval(pt_ctx* ctx, int which, const float* d_rays6, float* d_hits6, int* d_flags, int n) {
+    if (!ctx) return PT_ERR_INVALID;
+    if ((which != 0 && which != 1) || n < 0 || (n > 0 && (!d_rays6 || !d_hits6 || !d_flags)))
+        return fail(ctx, PT_ERR_INVALID, "pt_quartic_surface_eval: bad arguments");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    PT_CUDA_TRY(ctx, ptk_quartic_surface_eval(which, d_rays6, d_hits6, d_flags, n, ctx->stream));
+    PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return PT_OK;
+}
+
 const char* pt_last_error(pt_ctx* ctx) {
     if (!ctx) return "null context";
     return ctx->err.c_str();

@@ -329,3 +329,46 @@ def test_empty_scene_and_single_pixel(rt, engine):
         acc_g, tr_g = compare.run_gpu(ctx, push, trace_depth=5)
         _check(compare.compare(acc_o, tr_o, acc_g, tr_g, 3))
         ctx.close()
+
+
+@pytest.mark.parametrize("which,name", [(0, "thritorius"), (1, "smooth_cuboid")])
+def test_disabled_quartic_surfaces_match_oracle(rt, which, name):
+    """The two quartic surfaces the reference's shader defines but never calls
+    (Thritorius, SmoothCuboid; src/shader.comp:543-631) on the GPU against the
+    oracle's restatement (itself pinned to the reference's own functions):
+    hit flag and hit record bit for bit on rays aimed at and around them."""
+    import ctypes
+
+    import torch
+
+    from oracle import oracle
+
+    rng = np.random.default_rng(17 + which)
+    n = 20000
+    o = rng.uniform(-3.0, 3.0, (n, 3))
+    d = rng.normal(size=(n, 3))
+    aim = rng.uniform(size=n) < 0.5
+    d[aim] = -o[aim] + rng.normal(0, 0.3, (int(aim.sum()), 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, d], axis=1).astype(np.float32)
+    hits = np.zeros((n, 6), np.float32)
+    hits[:, 0] = np.where(rng.uniform(size=n) < 0.7, 1e5, rng.uniform(0.5, 6.0, n)).astype(np.float32)
+    hits[:, 5] = -1.0
+    fn = getattr(oracle.lib(), f"pto_fn_{name}")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    want = hits.copy()
+    want_f = np.array([fn(rays[i].ctypes.data, None, want[i].ctypes.data) for i in range(n)], np.int32)
+    with rt["Context"](0) as ctx:
+        d_rays = torch.from_numpy(rays).cuda()
+        d_hits = torch.from_numpy(hits).cuda()
+        d_flags = torch.zeros(n, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        from pathtracer_gb300 import native
+
+        assert native.cuda().pt_quartic_surface_eval(ctx.handle, which, d_rays.data_ptr(), d_hits.data_ptr(),
+                                                     d_flags.data_ptr(), n) == native.PT_OK
+        got, got_f = d_hits.cpu().numpy(), d_flags.cpu().numpy()
+    assert np.array_equal(got_f, want_f)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert n // 50 < int(want_f.sum()) < n

@@ -248,11 +248,13 @@ def _same(fa, fb, ray, obj, rng, extra=False):
     return ra
 
 
-@pytest.mark.parametrize("kind", ["sphere", "plane", "box", "lens", "cyclide"])
+@pytest.mark.parametrize("kind", ["sphere", "plane", "box", "lens", "cyclide", "thritorius", "smooth_cuboid"])
 def test_intersections(libs, kind):
     """SphereIntersection, PlaneIntersection, BoxIntersection (with
-    RotationMatrix), LensIntersection (two sphere slices) and DupinCyclide
-    (the quartic solver): hit flag, distance, normal and ids bit for bit."""
+    RotationMatrix), LensIntersection (two sphere slices), DupinCyclide (the
+    quartic solver), and the two quartic surfaces the shader defines but
+    never calls (Thritorius, SmoothCuboid): hit flag, distance, normal and
+    ids bit for bit."""
     o, r = libs
     rng = np.random.default_rng(10)
     extra = kind == "lens"
@@ -274,6 +276,8 @@ def test_intersections(libs, kind):
             radius = rng.uniform(0.2, 1.0)
             obj = [*pos, *rot, radius, rng.uniform(0.6 * radius, 3.0), rng.uniform(0.0, 0.2),
                    float(rng.integers(0, 2)), *ids]
+        elif kind in ("thritorius", "smooth_cuboid"):
+            obj = [0.0]  # fixed surfaces at the origin
         else:
             a = rng.uniform(0.8, 1.2)
             obj = [*pos, *rot, *rng.uniform(0.5, 1.5, 3), a, rng.uniform(0.6, 0.95) * a, rng.uniform(0.2, 0.6),
