@@ -215,6 +215,18 @@ int pt_resize_accum(pt_ctx* ctx, int width, int height);
  * stream; resolution must equal the accumulator size. */
 int pt_dispatch(pt_ctx* ctx, const pt_push* push);
 
+/* The FP64 reference renderer (no counterpart in the reference): the
+ * dispatch's paths (push: resolution, samples, path length, camera) traced
+ * with the same method in double precision, each pixel's exposed colour
+ * sum (Rendering's apertureSize^2 * ISO, src/shader.comp:1517) and sample
+ * count added to d_sums (W*H*4 doubles, device memory, zeroed by the
+ * caller before the first call; mean = sum / count).  It draws the same
+ * random stream as pt_dispatch for the same push constants, so the two
+ * images differ only by the FP32 arithmetic's error and the few paths whose
+ * branches it changes.  Scenes with run-time compiled SDF text: PT_ERR_UNSUPPORTED.
+ * Asynchronous on the context's stream (pt_wait); pt_set_trace applies. */
+int pt_render_fp64(pt_ctx* ctx, const pt_push* push, double* d_sums);
+
 /* Engines behind pt_dispatch; both compute the reference's per-sample
  * arithmetic bit for bit and differ only in scheduling.
  *   PT_ENGINE_MEGAKERNEL: one thread per pixel, samples in order (the plain

@@ -26,6 +26,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wal
 CUDA_SOURCES = [
     "kernel/pt_megakernel.cu",
     "kernel/pt_megakernel_analytic.cu",
+    "kernel/pt_fp64.cu",
     "kernel/pt_wavefront.cu",
     "pt_api.cu",
     "pt_engine.cu",

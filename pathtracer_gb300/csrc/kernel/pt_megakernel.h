@@ -19,6 +19,10 @@ cudaError_t ptk_rotation_setup(const KScene* scene, float* d_out, cudaStream_t s
 
 // One dispatch of the plain megakernel over params->pc.resolution.
 cudaError_t ptk_launch_megakernel(const KParams* params, bool trace, cudaStream_t stream);
+// One dispatch of the FP64 reference renderer (pt_fp64.cu): the same paths
+// in double precision, adding exposed colour sums and sample counts to
+// params->sums (4 doubles per pixel).
+cudaError_t ptk_launch_fp64(const KParams* params, bool trace, cudaStream_t stream);
 // The analytic-scene variants (PT_FEAT_* 0, BOX, ANALYTIC), from their own
 // translation unit.
 cudaError_t ptk_launch_megakernel_analytic(const KParams* params, int variant, dim3 grid, dim3 block,

@@ -24,12 +24,16 @@ namespace ptjit {
 namespace {
 #endif
 
-template <bool TRACE, int FEAT>
+// R = float: the shader's method, into the float accumulator.  R = double:
+// the FP64 reference renderer (pt_fp64.cu), the same method in double
+// precision, adding each pixel's exposed colour sum and sample count to
+// P.sums.
+template <bool TRACE, int FEAT, typename R = float>
 __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constant__ KParams P) {
     const KScene& S = P.s;
     const pt_push& pc = P.pc;
-    __shared__ CamInfo camS;
-    if (threadIdx.x == 0 && threadIdx.y == 0) camS = make_camera(pc);
+    __shared__ CamInfoT<R> camS;
+    if (threadIdx.x == 0 && threadIdx.y == 0) camS = make_camera<R>(pc);
     __syncthreads();
 
     const int W = pc.resolution[0], H = pc.resolution[1];
@@ -39,28 +43,28 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
 
     const uint32_t xx = (uint32_t)x;
     const uint32_t yy = (uint32_t)H - (uint32_t)y;  // SC:1510
-    const float uvx = (2.0f * (float)xx - (float)W) / (float)H;
-    const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
+    const R uvx = (R(2) * (R)xx - (R)W) / (R)H;
+    const R uvy = (R(2) * (R)yy - (R)H) / (R)H;
     const int spf = pc.samplesPerFrame;
     const int depth = pc.pathLength;
     const size_t pix = (size_t)y * (size_t)W + (size_t)x;
 
-    float3 sum = f3(0.0f, 0.0f, 0.0f);
+    V3<R> sum = v3<R>(R(0), R(0), R(0));
     int k = 0;
-    PathState ps;
+    PathStateT<R> ps;
     bool active = false, shadow = false;
     for (;;) {
         if (!active) {
             // Finish sample k-1 (SC:1477-1489, SC:1514-1516) and start sample k.
             if (k > 0) {
-                const float3 color = sample_color(ps, S, P.cie);
+                const V3<R> color = sample_color(ps, S, P.cie);
                 if (TRACE) {
                     const size_t p = pix * (size_t)spf + (size_t)(k - 1);
                     if (P.trace.nevents) P.trace.nevents[p] = (uint32_t)ps.bounce;
                     if (P.trace.colors) {
-                        P.trace.colors[3 * p] = color.x;
-                        P.trace.colors[3 * p + 1] = color.y;
-                        P.trace.colors[3 * p + 2] = color.z;
+                        P.trace.colors[3 * p] = (float)color.x;
+                        P.trace.colors[3 * p + 1] = (float)color.y;
+                        P.trace.colors[3 * p + 2] = (float)color.z;
                     }
                 }
                 sum = sum + color;
@@ -73,11 +77,11 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
             continue;
         }
         // ---- the single scene intersection of the loop ----
-        Hit h;
-        h.hitdist = PT_MAXDIST;
-        h.normal = f3(0.0f, 0.0f, 0.0f);
-        h.materialID = 0.0f;
-        h.lightID = -1.0f;
+        HitT<R> h;
+        h.hitdist = R(PT_MAXDIST);
+        h.normal = v3<R>(R(0), R(0), R(0));
+        h.materialID = R(0);
+        h.lightID = R(-1);
         int objectID = -1;
         intersect_all<FEAT>(S, ps.org, shadow ? ps.shDir : ps.dir, h, objectID);
         const StepResult r =
@@ -90,7 +94,17 @@ __global__ void __launch_bounds__(PT_MK_THREADS) megakernel(const __grid_constan
         }
         if (r == STEP_TERMINATED) active = false;
     }
-    P.accum[pix] = accumulate(pc, sum, P.accum[pix]);
+    if constexpr (sizeof(R) == 4) {
+        P.accum[pix] = accumulate(pc, sum, P.accum[pix]);
+    } else {
+        // Rendering's exposure (SC:1517), each sample's colour summed at full precision.
+        const double exposure = (double)pc.apertureSize * (double)pc.apertureSize * (double)pc.ISO;
+        double* s4 = P.sums + 4 * pix;
+        s4[0] += (double)sum.x * exposure;
+        s4[1] += (double)sum.y * exposure;
+        s4[2] += (double)sum.z * exposure;
+        s4[3] += (double)spf;
+    }
 }
 
 }  // namespace

@@ -43,11 +43,12 @@ struct KScene {
 
 // Camera quantities that depend only on the push constants (SC:1456,
 // SC:1409-1418): derived once per block (megakernel) or per job (wavefront).
-struct CamInfo {
-    m3 cam;
-    m3 lensRot;
-    float3 lensPos;
+template <typename R> struct CamInfoT {
+    M3<R> cam;
+    M3<R> lensRot;
+    V3<R> lensPos;
 };
+using CamInfo = CamInfoT<float>;
 
 struct KTrace {
     uint32_t* events;
@@ -62,6 +63,7 @@ struct KParams {
     float4* accum;
     const float* cie;  // 1323 floats in global memory
     KTrace trace;
+    double* sums;      // the FP64 renderer's target: x, y, z sums of exposed colours and the sample count per pixel
 };
 
 // Guarded reads for indices that come from scene data rather than loop
@@ -74,4 +76,9 @@ PT_DI float s_lightid(const KScene& S, int i) { return ((unsigned)i < (unsigned)
 PT_DI m3 s_rotation(const KScene& S, int global_index) {
     const float* r = S.rot[global_index];
     return m3{f3(r[0], r[1], r[2]), f3(r[3], r[4], r[5]), f3(r[6], r[7], r[8])};
+}
+// The same matrix in precision R (the double renderer widens the table's floats).
+template <typename R> PT_DI M3<R> s_rotation_r(const KScene& S, int global_index) {
+    const float* r = S.rot[global_index];
+    return M3<R>{v3<R>(r[0], r[1], r[2]), v3<R>(r[3], r[4], r[5]), v3<R>(r[6], r[7], r[8])};
 }

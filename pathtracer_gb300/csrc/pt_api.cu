@@ -326,6 +326,29 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push) {
     return PT_OK;
 }
 
+int pt_render_fp64(pt_ctx* ctx, const pt_push* push, double* d_sums) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (!push || !d_sums) return fail(ctx, PT_ERR_INVALID, "pt_render_fp64: null push constants or sums");
+    if (!ctx->has_scene) return fail(ctx, PT_ERR_NO_SCENE, "pt_render_fp64: no scene uploaded");
+    if (push->resolution[0] <= 0 || push->resolution[1] <= 0 || push->samplesPerFrame <= 0)
+        return fail(ctx, PT_ERR_INVALID, "pt_render_fp64: bad resolution or samplesPerFrame");
+    if (!ctx->custom.empty())
+        return fail(ctx, PT_ERR_UNSUPPORTED, "pt_render_fp64: SDF text compiled at run time has no double form");
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    KParams& P = *ctx->params;
+    P.pc = *push;
+    P.accum = nullptr;
+    P.sums = d_sums;
+    P.cie = ctx->d_cie;
+    P.trace = ctx->trace;
+    const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
+    const cudaError_t e = ptk_launch_fp64(&P, trace, ctx->stream);
+    P.sums = nullptr;
+    PT_CUDA_TRY(ctx, e);
+    PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
+    return PT_OK;
+}
+
 int pt_set_engine(pt_ctx* ctx, int engine) {
     if (!ctx) return PT_ERR_INVALID;
     if (engine != PT_ENGINE_MEGAKERNEL && engine != PT_ENGINE_WAVEFRONT)

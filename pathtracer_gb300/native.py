@@ -275,6 +275,7 @@ CUDA_API = [
                                ctypes.c_char_p, _sz]),
     ("pt_resize_accum", _i, [_vp, _i, _i]),
     ("pt_dispatch", _i, [_vp, ctypes.POINTER(PtPush)]),
+    ("pt_render_fp64", _i, [_vp, ctypes.POINTER(PtPush), _vp]),
     ("pt_wait", _i, [_vp, ctypes.c_uint64]),
     ("pt_read_accum", _i, [_vp, _vp, _sz]),
     ("pt_write_accum", _i, [_vp, _vp, _sz]),

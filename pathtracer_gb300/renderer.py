@@ -194,6 +194,11 @@ class Context:
     def dispatch(self, push: PtPush):
         self._check(self._lib.pt_dispatch(self._h, ctypes.byref(push)))
 
+    def render_fp64(self, push: PtPush, d_sums: int):
+        """pt_render_fp64: the dispatch's paths in double precision, summed
+        into the caller's device array of W*H*4 doubles (x, y, z, count)."""
+        self._check(self._lib.pt_render_fp64(self._h, ctypes.byref(push), d_sums))
+
     def wait(self, timeout_ns: int = 2**64 - 1):
         self._check(self._lib.pt_wait(self._h, ctypes.c_uint64(timeout_ns)))
 
