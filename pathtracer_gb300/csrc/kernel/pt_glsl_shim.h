@@ -149,12 +149,43 @@ struct bvec4 {
     PTG_M void set_zw(bvec2 v) { z = v.x; w = v.y; }
 };
 
-// Component-wise arithmetic.
-#define PTG_OPS(V, EXPAND)                                                                     \
-    PTG_FN V operator+(V a, V b) { return EXPAND(a, +, b); }                                   \
-    PTG_FN V operator-(V a, V b) { return EXPAND(a, -, b); }                                   \
-    PTG_FN V operator*(V a, V b) { return EXPAND(a, *, b); }                                   \
-    PTG_FN V operator/(V a, V b) { return EXPAND(a, /, b); }                                   \
+// Component-wise arithmetic.  On Blackwell (sm_100 and later), + - * of
+// vector components go two at a time through the paired FP32 instructions
+// (FADD2, FMUL2, FFMA2): each lane of a pair is an IEEE round-to-nearest
+// operation, so the results are the bits of the scalar operations the CPU
+// build performs (a - b as a + (-b): the same bits).  Division stays scalar.
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+#define PTG_PAIRED 1
+PTG_FN float2 ptg_pair(float a, float b) { return make_float2(a, b); }
+PTG_FN vec2 ptg_v2(float2 p) { return vec2(p.x, p.y); }
+PTG_FN vec3 ptg_v3(float2 p, float z) { return vec3(p.x, p.y, z); }
+PTG_FN vec4 ptg_v4(float2 p, float2 q) { return vec4(p.x, p.y, q.x, q.y); }
+PTG_FN float2 ptg_add2(float ax, float ay, float bx, float by) { return __fadd2_rn(ptg_pair(ax, ay), ptg_pair(bx, by)); }
+PTG_FN float2 ptg_sub2(float ax, float ay, float bx, float by) { return __fadd2_rn(ptg_pair(ax, ay), ptg_pair(-bx, -by)); }
+PTG_FN float2 ptg_mul2(float ax, float ay, float bx, float by) { return __fmul2_rn(ptg_pair(ax, ay), ptg_pair(bx, by)); }
+#define PTG_VV(NAME, OP)                                                                                     \
+    PTG_FN vec2 operator OP(vec2 a, vec2 b) { return ptg_v2(NAME(a.x, a.y, b.x, b.y)); }                   \
+    PTG_FN vec3 operator OP(vec3 a, vec3 b) { return ptg_v3(NAME(a.x, a.y, b.x, b.y), a.z OP b.z); }       \
+    PTG_FN vec4 operator OP(vec4 a, vec4 b) { return ptg_v4(NAME(a.x, a.y, b.x, b.y), NAME(a.z, a.w, b.z, b.w)); }
+PTG_VV(ptg_add2, +)
+PTG_VV(ptg_sub2, -)
+PTG_VV(ptg_mul2, *)
+#undef PTG_VV
+#else
+#define PTG_VV(OP)                                                                                      \
+    PTG_FN vec2 operator OP(vec2 a, vec2 b) { return vec2(a.x OP b.x, a.y OP b.y); }                  \
+    PTG_FN vec3 operator OP(vec3 a, vec3 b) { return vec3(a.x OP b.x, a.y OP b.y, a.z OP b.z); }      \
+    PTG_FN vec4 operator OP(vec4 a, vec4 b) { return vec4(a.x OP b.x, a.y OP b.y, a.z OP b.z, a.w OP b.w); }
+PTG_VV(+)
+PTG_VV(-)
+PTG_VV(*)
+#undef PTG_VV
+#endif
+PTG_FN vec2 operator/(vec2 a, vec2 b) { return vec2(a.x / b.x, a.y / b.y); }
+PTG_FN vec3 operator/(vec3 a, vec3 b) { return vec3(a.x / b.x, a.y / b.y, a.z / b.z); }
+PTG_FN vec4 operator/(vec4 a, vec4 b) { return vec4(a.x / b.x, a.y / b.y, a.z / b.z, a.w / b.w); }
+// With a scalar on either side, and the assignment forms.
+#define PTG_OPS(V)                                                                             \
     PTG_FN V operator+(V a, float s) { return a + V(s); }                                      \
     PTG_FN V operator-(V a, float s) { return a - V(s); }                                      \
     PTG_FN V operator*(V a, float s) { return a * V(s); }                                      \
@@ -171,12 +202,9 @@ struct bvec4 {
     PTG_FN V& operator-=(V& a, float s) { return a = a - s; }                                  \
     PTG_FN V& operator*=(V& a, float s) { return a = a * s; }                                  \
     PTG_FN V& operator/=(V& a, float s) { return a = a / s; }
-#define PTG_E2(a, op, b) vec2(a.x op b.x, a.y op b.y)
-#define PTG_E3(a, op, b) vec3(a.x op b.x, a.y op b.y, a.z op b.z)
-#define PTG_E4(a, op, b) vec4(a.x op b.x, a.y op b.y, a.z op b.z, a.w op b.w)
-PTG_OPS(vec2, PTG_E2)
-PTG_OPS(vec3, PTG_E3)
-PTG_OPS(vec4, PTG_E4)
+PTG_OPS(vec2)
+PTG_OPS(vec3)
+PTG_OPS(vec4)
 
 // Negation flips signs (-(+0) is -0, unlike 0 - a).
 PTG_FN vec2 operator-(vec2 a) { return vec2(-a.x, -a.y); }
@@ -272,6 +300,16 @@ PTG_FN vec2 step(float e, vec2 a) { return step(vec2(e), a); }
 PTG_FN vec3 step(float e, vec3 a) { return step(vec3(e), a); }
 
 PTG_FN float fma(float a, float b, float c) { return PTM_FMA(a, b, c); }
+#if defined(PTG_PAIRED)
+PTG_FN float2 ptg_fma2(float ax, float ay, float bx, float by, float cx, float cy) {
+    return __ffma2_rn(ptg_pair(ax, ay), ptg_pair(bx, by), ptg_pair(cx, cy));
+}
+PTG_FN vec2 fma(vec2 a, vec2 b, vec2 c) { return ptg_v2(ptg_fma2(a.x, a.y, b.x, b.y, c.x, c.y)); }
+PTG_FN vec3 fma(vec3 a, vec3 b, vec3 c) { return ptg_v3(ptg_fma2(a.x, a.y, b.x, b.y, c.x, c.y), PTM_FMA(a.z, b.z, c.z)); }
+PTG_FN vec4 fma(vec4 a, vec4 b, vec4 c) {
+    return ptg_v4(ptg_fma2(a.x, a.y, b.x, b.y, c.x, c.y), ptg_fma2(a.z, a.w, b.z, b.w, c.z, c.w));
+}
+#else
 PTG_FN vec2 fma(vec2 a, vec2 b, vec2 c) { return vec2(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y)); }
 PTG_FN vec3 fma(vec3 a, vec3 b, vec3 c) {
     return vec3(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y), PTM_FMA(a.z, b.z, c.z));
@@ -279,6 +317,7 @@ PTG_FN vec3 fma(vec3 a, vec3 b, vec3 c) {
 PTG_FN vec4 fma(vec4 a, vec4 b, vec4 c) {
     return vec4(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y), PTM_FMA(a.z, b.z, c.z), PTM_FMA(a.w, b.w, c.w));
 }
+#endif
 
 template <typename V> PTG_FN V clamp(V a, V lo, V hi) { return min(max(a, lo), hi); }
 PTG_FN vec2 clamp(vec2 a, float lo, float hi) { return min(max(a, lo), hi); }
@@ -295,9 +334,26 @@ PTG_FN float smoothstep(float e0, float e1, float x) {
 }
 
 PTG_FN float dot(float a, float b) { return a * b; }
+#if defined(PTG_PAIRED)
+// The products in pairs (FMUL2), summed left to right as written.
+PTG_FN float dot(vec2 a, vec2 b) {
+    const float2 p = __fmul2_rn(ptg_pair(a.x, a.y), ptg_pair(b.x, b.y));
+    return p.x + p.y;
+}
+PTG_FN float dot(vec3 a, vec3 b) {
+    const float2 p = __fmul2_rn(ptg_pair(a.x, a.y), ptg_pair(b.x, b.y));
+    return p.x + p.y + a.z * b.z;
+}
+PTG_FN float dot(vec4 a, vec4 b) {
+    const float2 p = __fmul2_rn(ptg_pair(a.x, a.y), ptg_pair(b.x, b.y));
+    const float2 q = __fmul2_rn(ptg_pair(a.z, a.w), ptg_pair(b.z, b.w));
+    return p.x + p.y + q.x + q.y;
+}
+#else
 PTG_FN float dot(vec2 a, vec2 b) { return a.x * b.x + a.y * b.y; }
 PTG_FN float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 PTG_FN float dot(vec4 a, vec4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+#endif
 template <typename V> PTG_FN float length(V a) { return sqrtf(dot(a, a)); }
 PTG_FN float length(float a) { return fabsf(a); }
 template <typename V> PTG_FN float distance(V a, V b) { return length(a - b); }
