@@ -111,6 +111,8 @@ def parse_args():
     ap.add_argument("--drain", type=int, default=-1, help="wavefront march drain lanes (-1: default)")
     ap.add_argument("--blocks", type=int, default=0, help="wavefront stage blocks per SM (0: default)")
     ap.add_argument("--inner", type=int, default=0, help="wavefront SDF evaluations per march lane between refills (0: default)")
+    ap.add_argument("--fp-contract", type=int, default=0,
+                    help="FMA contraction in run-time compiled kernels (1: faster, not bit-exact; 0: the shader's rounding)")
     ap.add_argument("--autotune", type=int, default=1,
                     help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
     ap.add_argument("--workload", default="mandelbulb12",
@@ -891,6 +893,8 @@ def main():
     ctx.set_engine(engine_id)
     if args.pool:
         ctx.set_wavefront_pool(args.pool)
+    if args.fp_contract:
+        ctx.set_fp_contract(True)
     if args.budget:
         ctx.set_march_budget(args.budget)
     knobs = {k: v for k, v in (("refill_min", args.refill), ("blocks_per_sm", args.blocks),
@@ -1008,7 +1012,8 @@ def main():
                    "samples_per_dispatch": spf, "dispatches_per_step": ndisp,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "wavefront_tuning": ctx.tuning() if args.engine == "wavefront" else None,
-                   "autotuned": bool(tuned), "autotune_s": tune_secs},
+                   "autotuned": bool(tuned), "autotune_s": tune_secs,
+                   "fp_contract": bool(args.fp_contract)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "engine": args.engine,
         "engines": {args.engine: {"value": value / world, "ms_per_step": ms_step}, **other},

@@ -291,6 +291,16 @@ const char* pt_last_error(pt_ctx* ctx);
  * Device pointers owned by the caller; pass NULLs to disable. */
 int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_colors, int depth_cap);
 
+/* FMA contraction for the kernels this context compiles at run time (scene
+ * GLSL beyond the shipped snippets: the megakernel, or the wavefront engine's
+ * march kernel), from their next compilation on (no counterpart in the
+ * reference).  Off (the default): every a*b+c rounds twice, as the shader's
+ * expressions are written, and results are the reference's bit for bit.  On:
+ * the compiler may fuse a*b+c into one fma — fewer instructions in the
+ * issue-bound march, results within FP32 rounding of the method, no longer
+ * bit-identical. */
+int pt_set_fp_contract(pt_ctx* ctx, int on);
+
 /* Caps the iterations of the next wavefront dispatches' drain (0: the bound
  * the library computes from the dispatch's size, path length and march
  * budget, which a correct dispatch never reaches).  A dispatch that reaches

@@ -1302,7 +1302,10 @@ static vec4 ExtLambert(const pt_material_ext* m, vec4 l) {
  * reflection or transmission by the Fresnel reflectance at l.x; reflection
  * keeps every wavelength weighted by its reflectance over the chosen one;
  * from the first transmission on the path carries l.x alone at 4x (each
- * wavelength bends differently).
+ * wavelength bends differently).  The new ray starts 2e-4 along its
+ * direction (from the surface point itself the sphere test's near root can
+ * round to a tiny positive distance below the 1e-4 threshold and the ray
+ * would miss the sphere's far side).
  * Russian roulette follows in the caller.  Returns the event bits. */
 static uint32_t ExtSpecular(ctx_t* c, const pt_material_ext* m, vec4 l, vec4* rayradiance, Ray* ray, float hitdist,
                             vec3 normal, uint32_t* seed, float* MISBRDFWeight) {
@@ -1317,6 +1320,7 @@ static uint32_t ExtSpecular(ctx_t* c, const pt_material_ext* m, vec4 l, vec4* ra
     float cosi = -cdot;
     if (m->type == PT_BSDF_MIRROR) {
         ray->dir = add3(ray->dir, scl3(n, 2.0f * cosi));
+        ray->origin = fma3(ray->dir, mk3(2e-4f, 2e-4f, 2e-4f), ray->origin);
         *rayradiance = scl4(*rayradiance, m->p[0]);
         return PT_EV_SPECULAR;
     }
@@ -1334,6 +1338,7 @@ static uint32_t ExtSpecular(ctx_t* c, const pt_material_ext* m, vec4 l, vec4* ra
         float Fw = FresnelDielectric(inside ? nw : 1.0f / nw, cosi, &ct);
         vec4 r = *rayradiance;
         *rayradiance = mk4(r.x, r.y * (Fy / F), r.z * (Fz / F), r.w * (Fw / F));
+        ray->origin = fma3(ray->dir, mk3(2e-4f, 2e-4f, 2e-4f), ray->origin);
         return PT_EV_SPECULAR;
     }
     ray->dir = normalize3(add3(scl3(ray->dir, eta), scl3(n, eta * cosi - cost)));
@@ -1342,6 +1347,7 @@ static uint32_t ExtSpecular(ctx_t* c, const pt_material_ext* m, vec4 l, vec4* ra
         c->medium |= 2;
     }
     c->medium ^= 1;
+    ray->origin = fma3(ray->dir, mk3(2e-4f, 2e-4f, 2e-4f), ray->origin);
     return PT_EV_REFRACT;
 }
 

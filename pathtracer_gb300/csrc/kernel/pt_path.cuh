@@ -367,7 +367,10 @@ template <typename V, typename R = SOf<V>> PT_DI V ext_lambert(const pt_material
 // reflectance over the chosen one; a transmission bends each wavelength
 // differently, so from the first transmission on the path carries l.x
 // alone, with 4x its throughput (the sample's colour averages the four
-// wavelengths).  Returns the step result.
+// wavelengths).  The new ray starts 2e-4 along its direction: from the
+// surface point itself, the sphere test's near root can round to a tiny
+// positive distance, below the 1e-4 hit threshold, and a ray entering a
+// glass sphere would then miss its far side.  Returns the step result.
 template <bool TRACE, typename R>
 PT_DI StepResult shade_specular(PathStateT<R>& ps, const pt_material_ext& m, const HitT<R>& h, int depth) {
     ps.org = fma3s(ps.dir, h.hitdist, ps.org);
@@ -382,6 +385,7 @@ PT_DI StepResult shade_specular(PathStateT<R>& ps, const pt_material_ext& m, con
     const R cosi = -c;
     if (m.type == PT_BSDF_MIRROR) {
         ps.dir = ps.dir + n * (PT_LIT(R, 2.0) * cosi);
+        ps.org = fma3s(ps.dir, PT_LIT(R, 2e-4), ps.org);
         ps.rr = ps.rr * m.p[0];
         if (TRACE) ps.ev |= PT_EV_SPECULAR;
         return roulette<TRACE>(ps, depth);
@@ -409,6 +413,7 @@ PT_DI StepResult shade_specular(PathStateT<R>& ps, const pt_material_ext& m, con
         ps.medium ^= 1;
         if (TRACE) ps.ev |= PT_EV_REFRACT;
     }
+    ps.org = fma3s(ps.dir, PT_LIT(R, 2e-4), ps.org);
     return roulette<TRACE>(ps, depth);
 }
 

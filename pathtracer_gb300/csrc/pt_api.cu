@@ -53,6 +53,7 @@ struct pt_ctx {
     size_t colors_bytes = 0;
     uint32_t last_iterations = 0;
     uint64_t drain_limit = 0;      // iteration cap of the wavefront drain (0: the bound computed per dispatch)
+    bool fp_contract = false;      // run-time compiled kernels with FMA contraction (pt_set_fp_contract)
     // GLSL snippets other than the shipped four (PT_SDF_CUSTOM slots), as
     // translated by pt_glsl_translate, and the module compiled for them.
     std::vector<JitSlot> custom;
@@ -290,6 +291,12 @@ int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_
     if (!ctx) return PT_ERR_INVALID;
     if (depth_cap < 0 || (d_events && depth_cap == 0)) return fail(ctx, PT_ERR_INVALID, "pt_set_trace: bad depth_cap");
     ctx->trace = KTrace{d_events, d_nevents, d_colors, depth_cap};
+    return PT_OK;
+}
+
+int pt_set_fp_contract(pt_ctx* ctx, int on) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->fp_contract = on != 0;
     return PT_OK;
 }
 
@@ -664,7 +671,8 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
 static int ensure_jit(pt_ctx* ctx, JitKind kind) {
     constexpr size_t kJitCache = 8;
     std::vector<JitModule>& cache = ctx->jit[kind];
-    const std::string program = pt_jit_program(ctx->custom, kind);
+    // the cache key carries the contraction choice with the program text
+    const std::string program = pt_jit_program(ctx->custom, kind) + (ctx->fp_contract ? "// fmad\n" : "");
     for (size_t i = 0; i < cache.size(); i++)
         if (cache[i].key == program) {
             ctx->jit_cur[kind] = (int)i;
@@ -673,7 +681,7 @@ static int ensure_jit(pt_ctx* ctx, JitKind kind) {
     JitModule m;
     std::vector<char> cubin;
     std::string lowered[kJitMaxKernels], log;
-    int rc = pt_jit_compile(ctx->device, program, kind, cubin, lowered, log);
+    int rc = pt_jit_compile(ctx->device, program, kind, cubin, lowered, log, ctx->fp_contract);
     if (rc != PT_OK) return fail(ctx, rc, "compiling the scene's SDF snippets: " + log);
     rc = pt_jit_load(cubin, kind, lowered, m, log);
     if (rc != PT_OK) return fail(ctx, rc, log);

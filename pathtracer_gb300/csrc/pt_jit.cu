@@ -65,18 +65,18 @@ std::string pt_jit_program(const std::vector<JitSlot>& slots, JitKind kind) {
 }
 
 int pt_jit_compile(int device, const std::string& program, JitKind kind, std::vector<char>& cubin,
-                   std::string lowered[kJitMaxKernels], std::string& log) {
+                   std::string lowered[kJitMaxKernels], std::string& log, bool contract) {
     int major = 0, minor = 0;
     if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device) != cudaSuccess ||
         cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device) != cudaSuccess) {
         log = "no CUDA device to compile for";
         return PT_ERR_CUDA;
     }
-    return pt_jit_compile_for(major * 10 + minor, program, kind, cubin, lowered, log);
+    return pt_jit_compile_for(major * 10 + minor, program, kind, cubin, lowered, log, contract);
 }
 
 int pt_jit_compile_for(int sm, const std::string& program, JitKind kind, std::vector<char>& cubin,
-                       std::string lowered[kJitMaxKernels], std::string& log) {
+                       std::string lowered[kJitMaxKernels], std::string& log, bool contract) {
     nvrtcProgram prog = nullptr;
     if (nvrtcCreateProgram(&prog, program.c_str(), "pt_jit_kernels.cu", kJitHeaderCount, kJitHeaderTexts,
                            kJitHeaderNames) != NVRTC_SUCCESS) {
@@ -87,8 +87,10 @@ int pt_jit_compile_for(int sm, const std::string& program, JitKind kind, std::ve
     for (int i = 0; i < nk; i++) nvrtcAddNameExpression(prog, kNames[kind][i]);
     char arch[48];
     std::snprintf(arch, sizeof arch, "--gpu-architecture=sm_%d%s", sm, sm >= 90 ? "a" : "");
-    const char* opts[] = {arch, "--std=c++17", "--fmad=false", "--prec-div=true", "--prec-sqrt=true",
-                          "--ftz=false", "-lineinfo", "-default-device"};
+    // contract: a*b+c may become one fma (pt_set_fp_contract; not the
+    // shader's rounding, so results leave the bit-exact method)
+    const char* opts[] = {arch, "--std=c++17", contract ? "--fmad=true" : "--fmad=false", "--prec-div=true",
+                          "--prec-sqrt=true", "--ftz=false", "-lineinfo", "-default-device"};
     const nvrtcResult rc = nvrtcCompileProgram(prog, (int)(sizeof opts / sizeof opts[0]), opts);
     size_t n = 0;
     nvrtcGetProgramLogSize(prog, &n);

@@ -32,10 +32,12 @@ int pt_jit_translate_slot(const char* source, int slot, JitSlot& out, std::strin
 std::string pt_jit_program(const std::vector<JitSlot>& slots, JitKind kind);
 // Compiles for the compute capability of `device` (pt_jit_compile) or for
 // sm (e.g. 103) and returns the cubin and the kernels' lowered names.
+// contract: compile with FMA contraction (--fmad=true) instead of the
+// shader's separate roundings.
 int pt_jit_compile(int device, const std::string& program, JitKind kind, std::vector<char>& cubin,
-                   std::string lowered[kJitMaxKernels], std::string& log);
+                   std::string lowered[kJitMaxKernels], std::string& log, bool contract = false);
 int pt_jit_compile_for(int sm, const std::string& program, JitKind kind, std::vector<char>& cubin,
-                       std::string lowered[kJitMaxKernels], std::string& log);
+                       std::string lowered[kJitMaxKernels], std::string& log, bool contract = false);
 int pt_jit_load(const std::vector<char>& cubin, JitKind kind, const std::string lowered[kJitMaxKernels], JitModule& m,
                 std::string& err);
 void pt_jit_unload(JitModule& m);

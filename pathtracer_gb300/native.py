@@ -287,6 +287,7 @@ CUDA_API = [
     ("pt_last_error", ctypes.c_char_p, [_vp]),
     ("pt_set_trace", _i, [_vp, _vp, _vp, _vp, _i]),
     ("pt_set_drain_limit", _i, [_vp, ctypes.c_uint64]),
+    ("pt_set_fp_contract", _i, [_vp, _i]),
     ("pt_sdf_source_fingerprint", ctypes.c_uint64, [ctypes.c_char_p]),
     ("pt_mathf_eval", _i, [_vp, _i, _vp, _vp, _vp, _i]),
     ("pt_quartic_surface_eval", _i, [_vp, _i, _vp, _vp, _vp, _i]),

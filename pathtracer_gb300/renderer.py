@@ -273,6 +273,10 @@ class Context:
     def last_iterations(self) -> int:
         return self._lib.pt_last_iterations(self._h)
 
+    def set_fp_contract(self, on: bool):
+        """pt_set_fp_contract: FMA contraction in run-time compiled kernels (off: bit-exact)."""
+        self._check(self._lib.pt_set_fp_contract(self._h, int(bool(on))))
+
     def set_drain_limit(self, max_iterations: int):
         """Caps the wavefront drain's iterations (0: the library's bound)."""
         self._check(self._lib.pt_set_drain_limit(self._h, max_iterations))

@@ -1,0 +1,66 @@
+"""FMA contraction in the run-time compiled march kernel (pt_set_fp_contract).
+
+Off by default: every a*b+c rounds twice as the shader's expressions are
+written, and results are the oracle's bit for bit (test_gpu_fullsize.py).
+On, the march kernel may fuse them: fewer instructions in the issue-bound
+march, arithmetic within FP32 rounding of the method.  This measures, at
+the SDF-fractal workload's size (the 12-iteration mandelbulb, 1024x1024,
+64 spp, depth 6, 16 rows), how far that moves the paths from the oracle:
+the fraction of paths with an identical branch sequence, the colour error of
+those paths, and the frame's total.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import SCENES
+
+pytestmark = pytest.mark.gpu
+
+
+def test_contracted_march_against_the_oracle(built):
+    import torch
+
+    from oracle import compare, oracle, pack
+    from pathtracer_gb300 import Context, Scene, cie_analytic
+
+    W, H, spf, depth = 1024, 1024, 64, 6
+    ys = sorted({int(round(i * (H - 1) / 15)) for i in range(16)})
+    path = os.path.join(SCENES, "mandelbulb12_plane.json")
+    osc = pack.load_scene(path)
+    ubo = osc.pack_ubo(pack.cie_analytic())
+    plugins = oracle.plugins_for_sources(osc.sdf_sources())
+    opush = osc.push_constants(W, H, spf, spf, spf, depth)
+    acc_o = np.zeros((H, W, 4), np.float32)
+    parts = [compare.run_oracle(ubo, opush, plugins, accum=acc_o, rect=(0, y, W, y + 1), trace_depth=depth)[1]
+             for y in ys]
+    tr_o = tuple(np.concatenate([p[i] for p in parts]) for i in range(3))
+    scene = Scene.load(path)
+    n = W * H * spf
+    with Context(0) as ctx:
+        ctx.set_fp_contract(True)
+        ctx.bind(scene, cie_analytic())
+        ctx.resize_accum(W, H)
+        ev = torch.zeros(n * depth, dtype=torch.int32, device="cuda")
+        nev = torch.zeros(n, dtype=torch.int32, device="cuda")
+        col = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        ctx.set_trace(ev.data_ptr(), nev.data_ptr(), col.data_ptr(), depth)
+        ctx.dispatch(scene.push_constants(W, H, spf, spf, spf, depth))
+        ctx.wait()
+        ctx.set_trace(0, 0, 0, 0)
+        acc_g = ctx.read_accum()
+        idx = torch.tensor(ys, device="cuda")
+        tr_g = (ev.view(H, W, spf, depth).index_select(0, idx).reshape(-1, depth).cpu().numpy().view(np.uint32),
+                nev.view(H, W, spf).index_select(0, idx).reshape(-1).cpu().numpy().view(np.uint32),
+                col.view(H, W, spf, 3).index_select(0, idx).reshape(-1, 3).cpu().numpy())
+    rep = compare.compare(acc_o[ys], tr_o, acc_g[ys], tr_g, spf)
+    tot_o, tot_g = acc_o[ys][..., :3].sum(axis=(0, 1)), acc_g[ys][..., :3].sum(axis=(0, 1))
+    rep["frame_total_rel"] = float(np.max(np.abs(tot_g - tot_o) / np.abs(tot_o)))
+    print("contracted march, 12-iteration mandelbulb 1024x1024x64, 16 rows", rep)
+    # Not the bit-exact method: measured, with bounds that hold for FP32-level
+    # perturbations (paths part where a comparison sits at its threshold).
+    assert rep["path_match"] >= 0.95
+    assert rep["color_max_rel_matched"] < 5e-2
+    assert rep["frame_total_rel"] < 1e-2

@@ -104,14 +104,15 @@ def test_fp64_paths_follow_the_fp32_paths(rt, name, W, H, spf, depth):
     # FP32 rounding sends some paths another way at a comparison near its
     # threshold (a grazing hit, an SDF march converging one step apart, a light
     # sample at a shadow edge); from there the two paths are independent.
-    assert frac >= 0.85
+    assert frac >= 0.9
     # identical paths: FP32 accuracy, except the cone pdf's cancellation near
     # small lights (up to ~1e-2 relative, the error the FP64 reference exposes)
     assert np.median(rel) < 1e-5 and np.percentile(rel, 99) < 2e-2
     assert np.all(s64[..., 3] == spf)
     mean64 = s64[..., :3] / s64[..., 3:4]
-    diff = np.abs(mean64 - acc32[..., :3]).sum() / max(1e-12, np.abs(mean64).sum())
-    assert diff < 0.05, diff  # the images differ only where a few paths parted
+    # the image's total: the parted paths' noise averages out over the frame
+    bias = np.abs(mean64.sum(axis=(0, 1)) - acc32[..., :3].sum(axis=(0, 1))) / np.abs(mean64.sum(axis=(0, 1)))
+    assert np.all(bias < 0.02), bias
 
 
 def test_fp64_sums_accumulate_and_jit_text_is_refused(rt):
