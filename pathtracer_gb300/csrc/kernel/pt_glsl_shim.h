@@ -28,6 +28,57 @@
 
 #include "../../../include/pt_mathf.h"
 
+// The scalar functions the vocabulary is built on.  The FP64 reference
+// renderer compiles the same snippet text with every GLSL float a double:
+// its program defines PTG_DOUBLE and `float` as `double` around this header
+// and the snippets, and the functions below become CUDA's double-precision
+// ones (literals stay the float values the text writes).
+#if defined(PTG_DOUBLE)
+#define PTG_ABS(a) ::fabs(a)
+#define PTG_FLOOR(a) ::floor(a)
+#define PTG_CEIL(a) ::ceil(a)
+#define PTG_SQRT(a) ::sqrt(a)
+#define PTG_ROUND(a) ::round(a)
+#define PTG_TRUNC(a) ::trunc(a)
+#define PTG_MIN(a, b) ::fmin((double)(a), (double)(b))
+#define PTG_MAX(a, b) ::fmax((double)(a), (double)(b))
+#define PTG_FMA(a, b, c) ::fma((double)(a), (double)(b), (double)(c))
+#define PTG_EXP(a) ::exp(a)
+#define PTG_LOG(a) ::log(a)
+#define PTG_SIN(a) ::sin(a)
+#define PTG_COS(a) ::cos(a)
+#define PTG_SINCOS(a, s, c) ::sincos((a), (s), (c))
+#define PTG_ACOS(a) ::acos(a)
+#define PTG_ASIN(a) ::asin(a)
+#define PTG_ATAN(a) ::atan(a)
+#define PTG_ATAN2(y, x) ::atan2((double)(y), (double)(x))
+#define PTG_EXP2(a) ::exp2(a)
+#define PTG_LOG2(a) ::log2(a)
+#define PTG_POW(a, b) ::pow((double)(a), (double)(b))
+#else
+#define PTG_ABS(a) fabsf(a)
+#define PTG_FLOOR(a) floorf(a)
+#define PTG_CEIL(a) ceilf(a)
+#define PTG_SQRT(a) sqrtf(a)
+#define PTG_ROUND(a) roundf(a)
+#define PTG_TRUNC(a) truncf(a)
+#define PTG_MIN(a, b) fminf((a), (b))
+#define PTG_MAX(a, b) fmaxf((a), (b))
+#define PTG_FMA(a, b, c) PTM_FMA((a), (b), (c))
+#define PTG_EXP(a) ptm_expf(a)
+#define PTG_LOG(a) ptm_logf(a)
+#define PTG_SIN(a) ptm_sinf(a)
+#define PTG_COS(a) ptm_cosf(a)
+#define PTG_SINCOS(a, s, c) ptm_sincosf((a), (s), (c))
+#define PTG_ACOS(a) ptm_acosf(a)
+#define PTG_ASIN(a) ptm_asinf(a)
+#define PTG_ATAN(a) ptm_atanf(a)
+#define PTG_ATAN2(y, x) ptm_atan2f((y), (x))
+#define PTG_EXP2(a) ptm_exp2f(a)
+#define PTG_LOG2(a) ptm_log2f(a)
+#define PTG_POW(a, b) ptm_powf((a), (b))
+#endif
+
 namespace ptg {
 
 typedef unsigned int uint;
@@ -149,29 +200,7 @@ struct bvec4 {
     PTG_M void set_zw(bvec2 v) { z = v.x; w = v.y; }
 };
 
-// Component-wise arithmetic.  On Blackwell (sm_100 and later), + - * of
-// vector components go two at a time through the paired FP32 instructions
-// (FADD2, FMUL2, FFMA2): each lane of a pair is an IEEE round-to-nearest
-// operation, so the results are the bits of the scalar operations the CPU
-// build performs (a - b as a + (-b): the same bits).  Division stays scalar.
-#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
-#define PTG_PAIRED 1
-PTG_FN float2 ptg_pair(float a, float b) { return make_float2(a, b); }
-PTG_FN vec2 ptg_v2(float2 p) { return vec2(p.x, p.y); }
-PTG_FN vec3 ptg_v3(float2 p, float z) { return vec3(p.x, p.y, z); }
-PTG_FN vec4 ptg_v4(float2 p, float2 q) { return vec4(p.x, p.y, q.x, q.y); }
-PTG_FN float2 ptg_add2(float ax, float ay, float bx, float by) { return __fadd2_rn(ptg_pair(ax, ay), ptg_pair(bx, by)); }
-PTG_FN float2 ptg_sub2(float ax, float ay, float bx, float by) { return __fadd2_rn(ptg_pair(ax, ay), ptg_pair(-bx, -by)); }
-PTG_FN float2 ptg_mul2(float ax, float ay, float bx, float by) { return __fmul2_rn(ptg_pair(ax, ay), ptg_pair(bx, by)); }
-#define PTG_VV(NAME, OP)                                                                                     \
-    PTG_FN vec2 operator OP(vec2 a, vec2 b) { return ptg_v2(NAME(a.x, a.y, b.x, b.y)); }                   \
-    PTG_FN vec3 operator OP(vec3 a, vec3 b) { return ptg_v3(NAME(a.x, a.y, b.x, b.y), a.z OP b.z); }       \
-    PTG_FN vec4 operator OP(vec4 a, vec4 b) { return ptg_v4(NAME(a.x, a.y, b.x, b.y), NAME(a.z, a.w, b.z, b.w)); }
-PTG_VV(ptg_add2, +)
-PTG_VV(ptg_sub2, -)
-PTG_VV(ptg_mul2, *)
-#undef PTG_VV
-#else
+// Component-wise arithmetic.
 #define PTG_VV(OP)                                                                                      \
     PTG_FN vec2 operator OP(vec2 a, vec2 b) { return vec2(a.x OP b.x, a.y OP b.y); }                  \
     PTG_FN vec3 operator OP(vec3 a, vec3 b) { return vec3(a.x OP b.x, a.y OP b.y, a.z OP b.z); }      \
@@ -180,7 +209,6 @@ PTG_VV(+)
 PTG_VV(-)
 PTG_VV(*)
 #undef PTG_VV
-#endif
 PTG_FN vec2 operator/(vec2 a, vec2 b) { return vec2(a.x / b.x, a.y / b.y); }
 PTG_FN vec3 operator/(vec3 a, vec3 b) { return vec3(a.x / b.x, a.y / b.y, a.z / b.z); }
 PTG_FN vec4 operator/(vec4 a, vec4 b) { return vec4(a.x / b.x, a.y / b.y, a.z / b.z, a.w / b.w); }
@@ -237,36 +265,36 @@ PTG_FN vec2& operator/=(vec2& a, ivec2 b) { return a = a / b; }
     PTG_FN vec3 NAME(vec3 a, float b) { return NAME(a, vec3(b)); }                              \
     PTG_FN vec4 NAME(vec4 a, float b) { return NAME(a, vec4(b)); }
 
-PTG_FN float f_abs(float a) { return fabsf(a); }
+PTG_FN float f_abs(float a) { return PTG_ABS(a); }
 PTG_FN float f_sign(float a) { return (a > 0.0f) ? 1.0f : ((a < 0.0f) ? -1.0f : 0.0f); }
-PTG_FN float f_floor(float a) { return floorf(a); }
-PTG_FN float f_ceil(float a) { return ceilf(a); }
-PTG_FN float f_fract(float a) { return a - floorf(a); }
-PTG_FN float f_sqrt(float a) { return sqrtf(a); }
-PTG_FN float f_isqrt(float a) { return 1.0f / sqrtf(a); }
-PTG_FN float f_exp(float a) { return ptm_expf(a); }
-PTG_FN float f_log(float a) { return ptm_logf(a); }
-PTG_FN float f_sin(float a) { return ptm_sinf(a); }
-PTG_FN float f_cos(float a) { return ptm_cosf(a); }
-PTG_FN float f_acos(float a) { return ptm_acosf(a); }
-PTG_FN float f_asin(float a) { return ptm_asinf(a); }
-PTG_FN float f_atan(float a) { return ptm_atanf(a); }
-PTG_FN float f_atan2(float y, float x) { return ptm_atan2f(y, x); }
+PTG_FN float f_floor(float a) { return PTG_FLOOR(a); }
+PTG_FN float f_ceil(float a) { return PTG_CEIL(a); }
+PTG_FN float f_fract(float a) { return a - PTG_FLOOR(a); }
+PTG_FN float f_sqrt(float a) { return PTG_SQRT(a); }
+PTG_FN float f_isqrt(float a) { return 1.0f / PTG_SQRT(a); }
+PTG_FN float f_exp(float a) { return PTG_EXP(a); }
+PTG_FN float f_log(float a) { return PTG_LOG(a); }
+PTG_FN float f_sin(float a) { return PTG_SIN(a); }
+PTG_FN float f_cos(float a) { return PTG_COS(a); }
+PTG_FN float f_acos(float a) { return PTG_ACOS(a); }
+PTG_FN float f_asin(float a) { return PTG_ASIN(a); }
+PTG_FN float f_atan(float a) { return PTG_ATAN(a); }
+PTG_FN float f_atan2(float y, float x) { return PTG_ATAN2(y, x); }
 PTG_FN float f_tan(float a) {
     float s, c;
-    ptm_sincosf(a, &s, &c);
+    PTG_SINCOS(a, &s, &c);
     return s / c;
 }
-PTG_FN float f_exp2(float a) { return ptm_exp2f(a); }
-PTG_FN float f_log2(float a) { return ptm_log2f(a); }
-PTG_FN float f_round(float a) { return roundf(a); }
-PTG_FN float f_trunc(float a) { return truncf(a); }
+PTG_FN float f_exp2(float a) { return PTG_EXP2(a); }
+PTG_FN float f_log2(float a) { return PTG_LOG2(a); }
+PTG_FN float f_round(float a) { return PTG_ROUND(a); }
+PTG_FN float f_trunc(float a) { return PTG_TRUNC(a); }
 PTG_FN float f_radians(float a) { return a * 0.01745329252f; }
 PTG_FN float f_degrees(float a) { return a * 57.29577951f; }
-PTG_FN float f_mod(float a, float b) { return a - b * floorf(a / b); }
-PTG_FN float f_min(float a, float b) { return fminf(a, b); }
-PTG_FN float f_max(float a, float b) { return fmaxf(a, b); }
-PTG_FN float f_pow(float a, float b) { return ptm_powf(a, b); }
+PTG_FN float f_mod(float a, float b) { return a - b * PTG_FLOOR(a / b); }
+PTG_FN float f_min(float a, float b) { return PTG_MIN(a, b); }
+PTG_FN float f_max(float a, float b) { return PTG_MAX(a, b); }
+PTG_FN float f_pow(float a, float b) { return PTG_POW(a, b); }
 PTG_FN float f_step(float edge, float a) { return (a < edge) ? 0.0f : 1.0f; }
 
 PTG_MAP1(abs, f_abs)
@@ -299,25 +327,14 @@ PTG_MAP2(atan, f_atan2)  // atan(y, x)
 PTG_FN vec2 step(float e, vec2 a) { return step(vec2(e), a); }
 PTG_FN vec3 step(float e, vec3 a) { return step(vec3(e), a); }
 
-PTG_FN float fma(float a, float b, float c) { return PTM_FMA(a, b, c); }
-#if defined(PTG_PAIRED)
-PTG_FN float2 ptg_fma2(float ax, float ay, float bx, float by, float cx, float cy) {
-    return __ffma2_rn(ptg_pair(ax, ay), ptg_pair(bx, by), ptg_pair(cx, cy));
-}
-PTG_FN vec2 fma(vec2 a, vec2 b, vec2 c) { return ptg_v2(ptg_fma2(a.x, a.y, b.x, b.y, c.x, c.y)); }
-PTG_FN vec3 fma(vec3 a, vec3 b, vec3 c) { return ptg_v3(ptg_fma2(a.x, a.y, b.x, b.y, c.x, c.y), PTM_FMA(a.z, b.z, c.z)); }
-PTG_FN vec4 fma(vec4 a, vec4 b, vec4 c) {
-    return ptg_v4(ptg_fma2(a.x, a.y, b.x, b.y, c.x, c.y), ptg_fma2(a.z, a.w, b.z, b.w, c.z, c.w));
-}
-#else
-PTG_FN vec2 fma(vec2 a, vec2 b, vec2 c) { return vec2(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y)); }
+PTG_FN float fma(float a, float b, float c) { return PTG_FMA(a, b, c); }
+PTG_FN vec2 fma(vec2 a, vec2 b, vec2 c) { return vec2(PTG_FMA(a.x, b.x, c.x), PTG_FMA(a.y, b.y, c.y)); }
 PTG_FN vec3 fma(vec3 a, vec3 b, vec3 c) {
-    return vec3(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y), PTM_FMA(a.z, b.z, c.z));
+    return vec3(PTG_FMA(a.x, b.x, c.x), PTG_FMA(a.y, b.y, c.y), PTG_FMA(a.z, b.z, c.z));
 }
 PTG_FN vec4 fma(vec4 a, vec4 b, vec4 c) {
-    return vec4(PTM_FMA(a.x, b.x, c.x), PTM_FMA(a.y, b.y, c.y), PTM_FMA(a.z, b.z, c.z), PTM_FMA(a.w, b.w, c.w));
+    return vec4(PTG_FMA(a.x, b.x, c.x), PTG_FMA(a.y, b.y, c.y), PTG_FMA(a.z, b.z, c.z), PTG_FMA(a.w, b.w, c.w));
 }
-#endif
 
 template <typename V> PTG_FN V clamp(V a, V lo, V hi) { return min(max(a, lo), hi); }
 PTG_FN vec2 clamp(vec2 a, float lo, float hi) { return min(max(a, lo), hi); }
@@ -334,30 +351,13 @@ PTG_FN float smoothstep(float e0, float e1, float x) {
 }
 
 PTG_FN float dot(float a, float b) { return a * b; }
-#if defined(PTG_PAIRED)
-// The products in pairs (FMUL2), summed left to right as written.
-PTG_FN float dot(vec2 a, vec2 b) {
-    const float2 p = __fmul2_rn(ptg_pair(a.x, a.y), ptg_pair(b.x, b.y));
-    return p.x + p.y;
-}
-PTG_FN float dot(vec3 a, vec3 b) {
-    const float2 p = __fmul2_rn(ptg_pair(a.x, a.y), ptg_pair(b.x, b.y));
-    return p.x + p.y + a.z * b.z;
-}
-PTG_FN float dot(vec4 a, vec4 b) {
-    const float2 p = __fmul2_rn(ptg_pair(a.x, a.y), ptg_pair(b.x, b.y));
-    const float2 q = __fmul2_rn(ptg_pair(a.z, a.w), ptg_pair(b.z, b.w));
-    return p.x + p.y + q.x + q.y;
-}
-#else
 PTG_FN float dot(vec2 a, vec2 b) { return a.x * b.x + a.y * b.y; }
 PTG_FN float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 PTG_FN float dot(vec4 a, vec4 b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
-#endif
-template <typename V> PTG_FN float length(V a) { return sqrtf(dot(a, a)); }
-PTG_FN float length(float a) { return fabsf(a); }
+template <typename V> PTG_FN float length(V a) { return PTG_SQRT(dot(a, a)); }
+PTG_FN float length(float a) { return PTG_ABS(a); }
 template <typename V> PTG_FN float distance(V a, V b) { return length(a - b); }
-template <typename V> PTG_FN V normalize(V a) { return a * (1.0f / sqrtf(dot(a, a))); }
+template <typename V> PTG_FN V normalize(V a) { return a * (1.0f / PTG_SQRT(dot(a, a))); }
 PTG_FN vec3 cross(vec3 a, vec3 b) {
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
@@ -367,7 +367,7 @@ template <typename V> PTG_FN V refract(V i, V n, float eta) {
     const float d = dot(n, i);
     const float k = 1.0f - eta * eta * (1.0f - d * d);
     if (k < 0.0f) return V(0.0f);
-    return eta * i - (eta * d + sqrtf(k)) * n;
+    return eta * i - (eta * d + PTG_SQRT(k)) * n;
 }
 
 struct mat2 {
@@ -399,15 +399,15 @@ PTG_FN vec3& operator*=(vec3& v, mat3 m) { return v = v * m; }
 PTG_FN float smin(float x, float y) {
     float k = 0.02f;
     k *= 6.0f;
-    const float h = fmaxf(k - fabsf(x - y), 0.0f) / k;
+    const float h = PTG_MAX(k - PTG_ABS(x - y), 0.0f) / k;
     const float m = h * h * h * 0.5f;
     const float s = m * k * 0.3333333f;
-    return fminf(x, y) - s;
+    return PTG_MIN(x, y) - s;
 }
 PTG_FN vec2 smin(vec2 x, vec2 y) {
     float k = 0.02f;
     k *= 6.0f;
-    const float h = fmaxf(k - fabsf(x.x - y.x), 0.0f) / k;
+    const float h = PTG_MAX(k - PTG_ABS(x.x - y.x), 0.0f) / k;
     const float m = h * h * h * 0.5f;
     const float s = m * k * 0.3333333f;
     return (x.x < y.x) ? vec2(x.x - s, x.y + (y.y - x.y) * m) : vec2(y.x - s, x.y + (y.y - x.y) * (1.0f - m));

@@ -106,8 +106,9 @@ def test_fp64_paths_follow_the_fp32_paths(rt, name, W, H, spf, depth):
     # sample at a shadow edge); from there the two paths are independent.
     assert frac >= 0.9
     # identical paths: FP32 accuracy, except the cone pdf's cancellation near
-    # small lights (up to ~1e-2 relative, the error the FP64 reference exposes)
-    assert np.median(rel) < 1e-5 and np.percentile(rel, 99) < 2e-2
+    # small lights (a few per cent at the 99th percentile behind the
+    # mandelbulb scene's small sun: the error the FP64 reference exposes)
+    assert np.median(rel) < 1e-5 and np.percentile(rel, 99) < 5e-2
     assert np.all(s64[..., 3] == spf)
     mean64 = s64[..., :3] / s64[..., 3:4]
     # the image's total: the parted paths' noise averages out over the frame
@@ -138,3 +139,79 @@ def test_fp64_sums_accumulate_and_jit_text_is_refused(rt):
         with pytest.raises(PathTracerError) as e:
             ctx.render_fp64(jit.push_constants(W, H, spf, spf, spf, 6), sums.data_ptr())
         assert e.value.code == native.PT_ERR_UNSUPPORTED
+
+
+def _mean_f32(sums):
+    """An FP64 target's read-back (pt_batch_read_target): sum * (1 / count), rounded to float."""
+    inv = np.where(sums[..., 3:4] > 0, 1.0 / np.maximum(sums[..., 3:4], 1.0), 0.0)
+    return (sums[..., :3] * inv).astype(np.float32)
+
+
+def test_batch_fp64_pass_equals_the_context_renderer(rt):
+    """pt_batch_render_fp64 on a resident scene (extensions included) adds
+    the same sums as pt_render_fp64 on a context over two dispatches (the
+    batch's read-back of them is the same bits); an FP32 pass into the same
+    kind of target differs from it only by the FP32 arithmetic's error."""
+    import torch
+
+    from pathtracer_gb300 import Batch, PathTracerError, native
+
+    scene = rt["Scene"].load(os.path.join(SCENES, "cornell_box_full.json"))
+    W, H, spf, depth = 48, 40, 8, 8
+    pushes = [scene.push_constants(W, H, k * spf, k * spf, spf, depth) for k in (1, 2)]
+    with rt["Context"](0) as ctx:
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        sums = torch.zeros(W * H * 4, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for p in pushes:
+            ctx.render_fp64(p, sums.data_ptr())
+        ctx.wait()
+        want = sums.cpu().numpy().reshape(H, W, 4)
+    with Batch(0, pool_slots=1 << 14, max_passes=16) as b:
+        sid = b.add_scene(scene.pack_ubo(rt["cie"]), scene.sdf_plugins())
+        b.set_scene_ext(sid, scene.pack_ext())
+        t64 = b.add_target(W, H, native.PT_TARGET_FP64)
+        t32 = b.add_target(W, H, native.PT_TARGET_FP64)
+        for p in pushes:
+            b.render_fp64(sid, t64, p)
+            b.add_pass(sid, t32, p)
+        b.run()
+        got = b.read_target(t64)
+        f32 = b.read_target(t32)
+        assert b.target_samples(t64) == 2 * spf
+        with pytest.raises(PathTracerError) as e:
+            b.render_fp64(sid, b.add_target(W, H), pushes[0])  # a float target
+        assert e.value.code == native.PT_ERR_INVALID
+    assert np.array_equal(got[..., :3].view(np.uint32), _mean_f32(want).view(np.uint32))
+    tot64, tot32 = got[..., :3].sum(axis=(0, 1)), f32[..., :3].sum(axis=(0, 1))
+    assert np.all(np.abs(tot64 - tot32) / np.abs(tot64) < 0.02), (tot64, tot32)
+
+
+def test_server_references_with_fp64_paths(rt):
+    """pt_server_opts.fp64_paths: references traced in double precision; the
+    same job reaches an RMSE against them close to its RMSE against the
+    FP32-path reference (the two references differ by the FP32 error, far
+    below the job's noise).  A scene compiled at run time keeps FP32 paths."""
+    from pathtracer_gb300 import Server, native
+
+    cie = rt["cie"]
+    W = H = 32
+    sc, spec = rt["Scene"].generate(native.PT_GEN_SPHERES_FULL, 5)
+    jit = rt["Scene"].load(os.path.join(SCENES, "mandelbulb12_plane.json"))
+    rmse = {}
+    for fp64 in (False, True):
+        with Server(0, fp64_paths=fp64, keep_images=False, pool_slots=1 << 14, max_passes=64) as srv:
+            srv.add_scene(0, sc.pack_ubo(cie), sc.sdf_plugins())
+            srv.set_scene_ext(0, sc.pack_ext())
+            srv.render_reference(0, sc.push_constants(W, H, 1, 1, 1, spec.pathLength), 256, 32)
+            srv.add_scene_sources(1, jit.pack_ubo(cie), jit.sdf_sources())
+            srv.render_reference(1, jit.push_constants(W, H, 1, 1, 1, 6), 32, 16)
+            ids = [srv.submit(Server.job(0, sc.push_constants(W, H, 1, 1, 1, spec.pathLength), 32, 1e-9)),
+                   srv.submit(Server.job(1, jit.push_constants(W, H, 1, 1, 1, 6), 8, 1e-9))]
+            done = {r.job_id: r for r in srv.drain()}
+            rmse[fp64] = [done[i].rmse for i in ids]
+            assert all(done[i].status == native.PT_OK for i in ids)
+    print("relative RMSE, FP32-path vs FP64-path references:", rmse)
+    assert 0 < rmse[True][0] and abs(rmse[True][0] - rmse[False][0]) < 0.05 * rmse[False][0]
+    assert rmse[True][1] == rmse[False][1]  # the compiled scene's reference is the same FP32-path one
