@@ -50,7 +50,8 @@ extern "C" {
 #define PT_ERR_UNSUPPORTED 4   /* e.g. an SDF plug-in source that is not recognised */
 #define PT_ERR_NO_SCENE 5      /* dispatch before pt_upload_scene / pt_resize_accum */
 #define PT_ERR_OOM 6           /* device allocation failed */
-#define PT_ERR_KERNEL 7        /* the device work did not complete within its iteration limit (wavefront drain, batch run) */
+#define PT_ERR_KERNEL 7        /* the device work did not complete within its iteration limit (wavefront drain,
+                                  batch run), or an index check of the checked kernel build failed */
 #define PT_ERR_TOO_LARGE 8     /* the request exceeds pt_dispatch_noalloc's fixed scratch */
 #define PT_ERR_BUSY 9          /* the resource is still in use by passes in flight */
 #define PT_ERR_CANCELLED 10    /* a served job was cancelled (pt_server_cancel) */
@@ -301,6 +302,17 @@ int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_
  * bit-identical. */
 int pt_set_fp_contract(pt_ctx* ctx, int on);
 
+/* The wavefront engine's kernels built with index checks (no counterpart
+ * in the reference; a substitute for a device memory checker): every queue
+ * append, slot read from a queue or the free list, pass index and sample
+ * index is checked before use.  A failed check skips its access and makes
+ * the dispatch return PT_ERR_KERNEL, naming the site and the index, with
+ * the accumulator unchanged.  With every check passing, results are the
+ * unchecked kernels' bit for bit.  Off by default (the checks cost time);
+ * run-time compiled march kernels are compiled again for the checked build.
+ * The plain megakernel has no queues and is not affected. */
+int pt_set_device_checks(pt_ctx* ctx, int on);
+
 /* Caps the iterations of the next wavefront dispatches' drain (0: the bound
  * the library computes from the dispatch's size, path length and march
  * budget, which a correct dispatch never reaches).  A dispatch that reaches
@@ -467,6 +479,18 @@ void* pt_batch_target_device_ptr(pt_batch* batch, int target_id);
 /* Queues a pass; push->resolution must be the target's.  PT_ERR_BUSY when
  * max_passes passes are in flight. */
 int pt_batch_add_pass(pt_batch* batch, int scene_id, int target_id, const pt_push* push, int* pass_id);
+/* An FP64 reference pass (no counterpart in the reference): one dispatch's
+ * samples (push) of a resident scene traced in double precision by
+ * pt_render_fp64's kernel and added to an FP64 target, instead of FP32
+ * paths summed in double as a pass does.  Asynchronous on the batch's
+ * stream, ordered before every later RMSE reduction of the batch; it is no
+ * pass (no pass id, nothing for pt_batch_step to return).  Scenes with
+ * run-time compiled SDF text: PT_ERR_UNSUPPORTED. */
+int pt_batch_render_fp64(pt_batch* batch, int scene_id, int target_id, const pt_push* push);
+/* pt_set_device_checks for both of the batch's engines; a failed check
+ * makes pt_batch_step (and pt_batch_run) return PT_ERR_KERNEL.  PT_ERR_BUSY
+ * while passes are in flight. */
+int pt_batch_set_device_checks(pt_batch* batch, int on);
 int pt_batch_step(pt_batch* batch, int iterations, int* completed, int capacity, int* ncompleted);
 int pt_batch_pending(pt_batch* batch);
 int pt_batch_run(pt_batch* batch, uint64_t max_iterations);

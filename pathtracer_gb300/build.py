@@ -28,6 +28,7 @@ CUDA_SOURCES = [
     "kernel/pt_megakernel_analytic.cu",
     "kernel/pt_fp64.cu",
     "kernel/pt_wavefront.cu",
+    "kernel/pt_wavefront_checked.cu",
     "pt_api.cu",
     "pt_engine.cu",
     "pt_noalloc.cu",

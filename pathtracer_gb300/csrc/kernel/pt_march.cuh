@@ -56,9 +56,26 @@ constexpr int kDrainMinSteps = 8;
 // SphereTracing's over-relaxation start (SC:781).
 constexpr float kOmegaMax = 1.70f;
 
+// Index checks of the checked build (PT_DEBUG_CHECKS, the kernels of
+// pt_wavefront_checked.cu and checked run-time compiled march kernels):
+// true when i < n; otherwise the first failure since the last reset is
+// recorded in the counters (site, index) for the host, and the caller skips
+// the access.  The default build checks nothing: the function is constant
+// true and its arguments are dead code.
+#if defined(PT_DEBUG_CHECKS)
+PT_DI bool pt_check(const WfArgs& A, uint32_t i, uint32_t n, uint32_t site) {
+    if (i < n) return true;
+    if (atomicCAS(&A.counters->check_site, 0u, site) == 0u) A.counters->check_index = i;
+    return false;
+}
+#else
+PT_DI constexpr bool pt_check(const WfArgs&, uint32_t, uint32_t, uint32_t) { return true; }
+#endif
+
 // Warp-aggregated append of `value` to queue[count++] for lanes with pred.
-// Must be called by all 32 lanes of the warp.
-PT_DI void q_push(uint32_t* __restrict__ queue, uint32_t* count, uint32_t value, bool pred) {
+// Must be called by all 32 lanes of the warp.  Every queue holds up to
+// pool_size entries.
+PT_DI void q_push(const WfArgs& A, uint32_t* __restrict__ queue, uint32_t* count, uint32_t value, bool pred) {
     const unsigned mask = __ballot_sync(0xffffffffu, pred);
     if (mask == 0) return;
     const int lane = threadIdx.x & 31;
@@ -66,7 +83,8 @@ PT_DI void q_push(uint32_t* __restrict__ queue, uint32_t* count, uint32_t value,
     uint32_t base = 0;
     if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (pred) queue[base + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = value;
+    const uint32_t at = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+    if (pred && pt_check(A, at, A.pool_size, PT_CHECK_QUEUE_APPEND)) queue[at] = value;
 }
 
 struct PoolView {
@@ -148,8 +166,8 @@ PT_DI float3 normal_probes(unsigned pending, const KScene* Sp, float3 p, uint32_
 // Warp-staged queue appends: lanes with pred add `value` to a per-warp
 // buffer of 64 in shared memory (count warp-uniform); every 32 entries go to
 // the queue with one atomic and one coalesced store.  Called by all 32 lanes.
-PT_DI void stage_push(uint32_t* buf, uint32_t& count, bool pred, uint32_t value, uint32_t* queue, uint32_t* qcount,
-                      int lane) {
+PT_DI void stage_push(const WfArgs& A, uint32_t* buf, uint32_t& count, bool pred, uint32_t value, uint32_t* queue,
+                      uint32_t* qcount, int lane) {
     const unsigned m = __ballot_sync(0xffffffffu, pred);
     if (!m) return;
     if (pred) buf[count + (uint32_t)__popc(m & ((1u << lane) - 1u))] = value;
@@ -159,7 +177,7 @@ PT_DI void stage_push(uint32_t* buf, uint32_t& count, bool pred, uint32_t value,
     uint32_t b = 0;
     if (lane == 0) b = atomicAdd(qcount, 32u);
     b = __shfl_sync(0xffffffffu, b, 0);
-    queue[b + (uint32_t)lane] = buf[lane];
+    if (pt_check(A, b + (uint32_t)lane, A.pool_size, PT_CHECK_QUEUE_APPEND)) queue[b + (uint32_t)lane] = buf[lane];
     const uint32_t rest = count - 32;
     const uint32_t moved = ((uint32_t)lane < rest) ? buf[32 + lane] : 0u;
     __syncwarp();
@@ -169,13 +187,14 @@ PT_DI void stage_push(uint32_t* buf, uint32_t& count, bool pred, uint32_t value,
 }
 
 // Appends what stage_push still holds.  Called by all 32 lanes.
-PT_DI void stage_flush(uint32_t* buf, uint32_t count, uint32_t* queue, uint32_t* qcount, int lane) {
+PT_DI void stage_flush(const WfArgs& A, uint32_t* buf, uint32_t count, uint32_t* queue, uint32_t* qcount, int lane) {
     __syncwarp();
     if (!count) return;
     uint32_t b = 0;
     if (lane == 0) b = atomicAdd(qcount, count);
     b = __shfl_sync(0xffffffffu, b, 0);
-    if ((uint32_t)lane < count) queue[b + (uint32_t)lane] = buf[lane];
+    if ((uint32_t)lane < count && pt_check(A, b + (uint32_t)lane, A.pool_size, PT_CHECK_QUEUE_APPEND))
+        queue[b + (uint32_t)lane] = buf[lane];
 }
 
 // The march loop; WARP_NORMALS: normal probes in the warp's pass
@@ -246,7 +265,8 @@ PT_DI void march_rays(const WfArgs& A) {
             if (need) {
                 const uint32_t rank = (uint32_t)__popc(mneed & ((1u << lane) - 1u));
                 const uint32_t idx = (rank < from_old) ? old_base + rank : nb + (rank - from_old);
-                if (idx < n) {
+                if (idx < n && pt_check(A, qin[idx], A.pool_size, PT_CHECK_QUEUE_SLOT) &&
+                    pt_check(A, slot_job(v, qin[idx]), A.job_cap, PT_CHECK_JOB)) {
                     slot = qin[idx];
                     Sp = A.jobs[slot_job(v, slot)].scene;
                     const float4 o = v.s0[slot];
@@ -274,7 +294,7 @@ PT_DI void march_rays(const WfArgs& A) {
                     xmarch = (Sp->ext.flags & PT_EXT_MARCH) != 0;
                     p = fma3s(dir, t, org);
                     phase = (saved & 0x80000000u) ? MP_STEP : MP_SIGN;
-                } else {
+                } else if (idx >= n) {
                     exhausted = true;
                 }
             }
@@ -413,15 +433,16 @@ PT_DI void march_rays(const WfArgs& A) {
             v.h0[slot] = make_float4(t - 1e-3f, mat, -1.0f, __int_as_float(-2));
             v.h1[slot] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
         }
-        stage_push(staged[wib][0], nstaged[0], finished && !shadow_ray, slot, A.q_shade[cur], &C.n_shade[cur], lane);
-        stage_push(staged[wib][1], nstaged[1], finished && shadow_ray, slot, A.q_shadow[cur], &C.n_shadow[cur],
+        stage_push(A, staged[wib][0], nstaged[0], finished && !shadow_ray, slot, A.q_shade[cur], &C.n_shade[cur],
                    lane);
-        q_push(A.q_march[cur ^ 1u], &C.n_march[cur ^ 1u], slot, suspend);
+        stage_push(A, staged[wib][1], nstaged[1], finished && shadow_ray, slot, A.q_shadow[cur], &C.n_shadow[cur],
+                   lane);
+        q_push(A, A.q_march[cur ^ 1u], &C.n_march[cur ^ 1u], slot, suspend);
         if (finished || suspend) phase = MP_EMPTY;
     }
     // The staged remainders.
-    stage_flush(staged[wib][0], nstaged[0], A.q_shade[cur], &C.n_shade[cur], lane);
-    stage_flush(staged[wib][1], nstaged[1], A.q_shadow[cur], &C.n_shadow[cur], lane);
+    stage_flush(A, staged[wib][0], nstaged[0], A.q_shade[cur], &C.n_shade[cur], lane);
+    stage_flush(A, staged[wib][1], nstaged[1], A.q_shadow[cur], &C.n_shadow[cur], lane);
 }
 
 #if defined(PT_JIT_USER_SDF)

@@ -25,8 +25,17 @@
 // order, as the megakernel and the shader, so results are bit-identical.
 // The larger pt_mathf functions are called out of line here (smaller stage
 // and persistent kernels); the SDF plug-ins use inlined math regardless.
+//
+// pt_wavefront_checked.cu compiles this file a second time with
+// PT_DEBUG_CHECKS (every queue, pool-slot, ring and sample index checked
+// before use; pt_check in pt_march.cuh) and its launch functions renamed by
+// PTK_WF; the engine picks either set (ptk_wavefront_kernels).
 #define PTM_OUTLINE
 #include <cuda_runtime.h>
+
+#ifndef PTK_WF
+#define PTK_WF(name) name
+#endif
 
 #include "pt_march.cuh"
 #include "pt_path.cuh"
@@ -150,9 +159,9 @@ PT_DI bool route_ray(const WfArgs& A, const PoolView& v, const KScene& S, uint32
 // a primary hit or of a shadow-ray result.  Called by all 32 lanes.
 PT_DI void push_routed(const WfArgs& A, WfCounters& C, uint32_t nxt, uint32_t slot, bool valid, bool march,
                        bool shadow_ray) {
-    q_push(A.q_march[nxt], &C.n_march[nxt], slot, valid && march);
-    q_push(A.q_shade[nxt], &C.n_shade[nxt], slot, valid && !march && !shadow_ray);
-    q_push(A.q_shadow[nxt], &C.n_shadow[nxt], slot, valid && !march && shadow_ray);
+    q_push(A, A.q_march[nxt], &C.n_march[nxt], slot, valid && march);
+    q_push(A, A.q_shade[nxt], &C.n_shade[nxt], slot, valid && !march && !shadow_ray);
+    q_push(A, A.q_shadow[nxt], &C.n_shadow[nxt], slot, valid && !march && shadow_ray);
 }
 
 __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
@@ -167,11 +176,15 @@ __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
-        const bool valid = i < n;
+        bool valid = i < n;
         uint32_t slot = 0;
         bool march = false;
+        if (valid) valid = pt_check(A, nfree - n + i, A.pool_size, PT_CHECK_FREE_INDEX);
         if (valid) {
             slot = A.q_free[nfree - n + i];
+            valid = pt_check(A, slot, A.pool_size, PT_CHECK_QUEUE_SLOT);
+        }
+        if (valid) {
             const uint64_t s = first + i;
             const uint32_t job = find_job(A.jobs, A.job_cap, job_lo, job_hi, s);
             const WfJob& J = A.jobs[job];
@@ -267,12 +280,15 @@ template <bool TRACE>
 PT_DI void finish_shade(const WfArgs& A, const WfJob& J, const PathState& ps, StepResult r, uint32_t sample,
                         bool& freed) {
     const pt_push& pc = J.pc;
-    if (TRACE && r != STEP_SHADOW && A.trace.events) {
+    const bool in_pass = pt_check(A, sample, J.count, PT_CHECK_SAMPLE);  // trace and colour indices
+    if (TRACE && r != STEP_SHADOW && A.trace.events && in_pass) {
         const size_t p = trace_index(pc, sample);
         const int b = ps.bounce - 1;
         if (b < A.trace.cap) A.trace.events[p * (size_t)A.trace.cap + b] = ps.ev;
     }
-    if (r == STEP_TERMINATED) {
+    if (r == STEP_TERMINATED && !in_pass) {
+        freed = true;
+    } else if (r == STEP_TERMINATED) {
         const float3 col = sample_color(ps, *J.scene, J.cie);
         J.colors[sample] = make_float4(col.x, col.y, col.z, 0.0f);
         if (TRACE) {
@@ -301,11 +317,15 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
     const uint32_t ns = C.n_shadow[cur];
     for (uint32_t base = blockIdx.x * blockDim.x; base < ns; base += stride) {
         const uint32_t i = base + threadIdx.x;
-        const bool valid = i < ns;
+        bool valid = i < ns;
         uint32_t slot = 0, job = 0;
         bool again = false, freed = false, march = false;
         if (valid) {
             slot = A.q_shadow[cur][i];
+            valid = pt_check(A, slot, A.pool_size, PT_CHECK_QUEUE_SLOT) &&
+                    pt_check(A, slot_job(v, slot), A.job_cap, PT_CHECK_JOB);
+        }
+        if (valid) {
             PathState ps;
             uint32_t flags, sample;
             load_state(v, slot, ps, flags, sample, job);
@@ -321,17 +341,21 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
             }
         }
         push_routed(A, C, nxt, slot, again, march, false);
-        q_push(A.q_free, &C.n_free, slot, freed);
+        q_push(A, A.q_free, &C.n_free, slot, freed);
         count_finished(A.jobs, job, freed);
     }
     const uint32_t np = C.n_shade[cur];
     for (uint32_t base = blockIdx.x * blockDim.x; base < np; base += stride) {
         const uint32_t i = base + threadIdx.x;
-        const bool valid = i < np;
+        bool valid = i < np;
         uint32_t slot = 0, job = 0;
         bool again = false, freed = false, march = false, shadow_next = false;
         if (valid) {
             slot = A.q_shade[cur][i];
+            valid = pt_check(A, slot, A.pool_size, PT_CHECK_QUEUE_SLOT) &&
+                    pt_check(A, slot_job(v, slot), A.job_cap, PT_CHECK_JOB);
+        }
+        if (valid) {
             PathState ps;
             uint32_t flags, sample;
             load_for_primary(v, slot, ps, flags, sample, job);
@@ -364,7 +388,7 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
             }
         }
         push_routed(A, C, nxt, slot, again, march, shadow_next);
-        q_push(A.q_free, &C.n_free, slot, freed);
+        q_push(A, A.q_free, &C.n_free, slot, freed);
         count_finished(A.jobs, job, freed);
     }
 }
@@ -472,7 +496,8 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
             shadow = (r == STEP_SHADOW);
             if (r == STEP_TERMINATED) {
                 const float3 col = sample_color(ps, S, J.cie);
-                J.colors[local] = make_float4(col.x, col.y, col.z, 0.0f);
+                if (pt_check(A, local, J.count, PT_CHECK_SAMPLE))
+                    J.colors[local] = make_float4(col.x, col.y, col.z, 0.0f);
                 finished = true;
                 active = false;
             }
@@ -496,6 +521,12 @@ __global__ void wf_book(const __grid_constant__ WfArgs A) {
     C.march_cursor = 0;
     C.iterations += 1;
     C.live = pool - C.n_free;
+    // the next iteration's queues and the free list fit the pool
+    const uint32_t c = C.cur;
+    (void)(pt_check(A, C.n_march[c], pool + 1u, PT_CHECK_QUEUE_COUNT) &&
+           pt_check(A, C.n_shade[c], pool + 1u, PT_CHECK_QUEUE_COUNT) &&
+           pt_check(A, C.n_shadow[c], pool + 1u, PT_CHECK_QUEUE_COUNT) &&
+           pt_check(A, C.n_free, pool + 1u, PT_CHECK_QUEUE_COUNT));
 }
 
 __global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_free, uint32_t pool) {
@@ -515,6 +546,8 @@ __global__ void wf_init(WfCounters* __restrict__ Cp, uint32_t* __restrict__ q_fr
         C.live = 0;
         C.job_lo = C.job_hi = 0;
         C.pk_end = 0;
+        C.check_site = 0;
+        C.check_index = 0;
     }
 }
 
@@ -534,12 +567,12 @@ __global__ void __launch_bounds__(kStageThreads) wf_resolve(const pt_push pc, fl
 
 }  // namespace
 
-cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream) {
+cudaError_t PTK_WF(ptk_wavefront_launch_init)(const WfArgs* a, cudaStream_t stream) {
     wf_init<<<(a->pool_size + 255) / 256, 256, 0, stream>>>(a->counters, a->q_free, a->pool_size);
     return cudaGetLastError();
 }
 
-cudaError_t ptk_wavefront_launch_job_add(const WfArgs* a, const WfJob* job, uint32_t index, uint32_t lo,
+cudaError_t PTK_WF(ptk_wavefront_launch_job_add)(const WfArgs* a, const WfJob* job, uint32_t index, uint32_t lo,
                                          cudaStream_t stream) {
     wf_job_add<<<1, 1, 0, stream>>>(*a, *job, index, lo);
     return cudaGetLastError();
@@ -560,9 +593,11 @@ static int resident_blocks(const void* kernel, int* cache) {
     return *cache;
 }
 
-const void* ptk_wavefront_march_warp_normals() { return reinterpret_cast<const void*>(wf_march_warp_normals); }
+const void* PTK_WF(ptk_wavefront_march_warp_normals)() {
+    return reinterpret_cast<const void*>(wf_march_warp_normals);
+}
 
-cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
+cudaError_t PTK_WF(ptk_wavefront_launch_iteration)(const WfArgs* a, bool trace, int grid, cudaStream_t stream,
                                            cudaEvent_t* stage_events, const void* march_kernel) {
     // stage_events (optional): 6 events recorded before isect, march, shade,
     // gen, bookkeeping and after it, for per-stage device times.
@@ -595,25 +630,30 @@ cudaError_t ptk_wavefront_launch_iteration(const WfArgs* a, bool trace, int grid
     return cudaGetLastError();
 }
 
-cudaError_t ptk_persist_launch(const WfArgs* a, int variant, int sms, uint64_t budget, cudaStream_t stream) {
+int PTK_WF(ptk_persist_blocks_per_sm)(int variant);
+
+cudaError_t PTK_WF(ptk_persist_launch)(const WfArgs* a, int variant, int sms, uint64_t budget,
+                                       cudaStream_t stream) {
     wf_persist_setup<<<1, 1, 0, stream>>>(*a, budget);
     switch (variant) {
-        case 0: wf_persist<0><<<sms * ptk_persist_blocks_per_sm(0), kPersistThreads, 0, stream>>>(*a); break;
+        case 0: wf_persist<0><<<sms * PTK_WF(ptk_persist_blocks_per_sm)(0), kPersistThreads, 0, stream>>>(*a); break;
         case PT_FEAT_BOX:
-            wf_persist<PT_FEAT_BOX><<<sms * ptk_persist_blocks_per_sm(PT_FEAT_BOX), kPersistThreads, 0, stream>>>(*a);
+            wf_persist<PT_FEAT_BOX>
+                <<<sms * PTK_WF(ptk_persist_blocks_per_sm)(PT_FEAT_BOX), kPersistThreads, 0, stream>>>(*a);
             break;
         case PT_FEAT_ANALYTIC:
             wf_persist<PT_FEAT_ANALYTIC>
-                <<<sms * ptk_persist_blocks_per_sm(PT_FEAT_ANALYTIC), kPersistThreads, 0, stream>>>(*a);
+                <<<sms * PTK_WF(ptk_persist_blocks_per_sm)(PT_FEAT_ANALYTIC), kPersistThreads, 0, stream>>>(*a);
             break;
         default:
-            wf_persist<PT_FEAT_ALL><<<sms * ptk_persist_blocks_per_sm(PT_FEAT_ALL), kPersistThreads, 0, stream>>>(*a);
+            wf_persist<PT_FEAT_ALL>
+                <<<sms * PTK_WF(ptk_persist_blocks_per_sm)(PT_FEAT_ALL), kPersistThreads, 0, stream>>>(*a);
             break;
     }
     return cudaGetLastError();
 }
 
-int ptk_persist_blocks_per_sm(int variant) {
+int PTK_WF(ptk_persist_blocks_per_sm)(int variant) {
     static int cache[16] = {0};
     const int v = variant & 15;
     if (cache[v]) return cache[v];
@@ -636,7 +676,7 @@ int ptk_persist_blocks_per_sm(int variant) {
     return n;
 }
 
-cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,
+cudaError_t PTK_WF(ptk_wavefront_launch_resolve)(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,
                                          const float4* colors, cudaStream_t stream) {
     (void)a;
     (void)job;
@@ -644,3 +684,11 @@ cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt
     wf_resolve<<<(npix + kStageThreads - 1) / kStageThreads, kStageThreads, 0, stream>>>(*pc, accum, colors);
     return cudaGetLastError();
 }
+
+extern const WfKernelSet PTK_WF(ptk_wavefront_kernel_set);
+const WfKernelSet PTK_WF(ptk_wavefront_kernel_set) = {
+    PTK_WF(ptk_wavefront_launch_init),        PTK_WF(ptk_wavefront_launch_job_add),
+    PTK_WF(ptk_wavefront_launch_iteration),   PTK_WF(ptk_wavefront_march_warp_normals),
+    PTK_WF(ptk_persist_launch),               PTK_WF(ptk_persist_blocks_per_sm),
+    PTK_WF(ptk_wavefront_launch_resolve),
+};

@@ -57,6 +57,21 @@ struct WfCounters {
     uint32_t job_hi;       // passes added so far
     uint64_t pk_end;       // persistent mode: end of the sample range of the current launch
     uint32_t n_shadow[2];  // shadow-ray results to shade (current, next)
+    // Kernels built with PT_DEBUG_CHECKS: the first index check that failed
+    // since the last reset (PT_CHECK_* site, 0: none) and the index it saw.
+    uint32_t check_site;
+    uint32_t check_index;
+};
+
+// Sites of the index checks of the checked kernel build (PT_DEBUG_CHECKS).
+enum {
+    PT_CHECK_NONE = 0,
+    PT_CHECK_QUEUE_APPEND = 1,  // an append past a queue's capacity (the pool size)
+    PT_CHECK_QUEUE_SLOT = 2,    // a slot read from a queue outside the pool
+    PT_CHECK_FREE_INDEX = 3,    // a free-list read outside the list
+    PT_CHECK_JOB = 4,           // a pass index outside the job ring
+    PT_CHECK_SAMPLE = 5,        // a sample index outside its pass (colour buffer)
+    PT_CHECK_QUEUE_COUNT = 6,   // a queue or free-list length above the pool size after an iteration
 };
 
 // Everything here is fixed between resets, so a captured chain of iterations
@@ -116,4 +131,21 @@ constexpr int kPersistThreads = 128;
 // Rendering/Accumulate of one job pass from its ordered sample colours.
 cudaError_t ptk_wavefront_launch_resolve(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,
                                          const float4* colors, cudaStream_t stream);
+
+// The launch functions above as a set, for the engine to switch between the
+// default build of the wavefront kernels and the checked one.
+struct WfKernelSet {
+    cudaError_t (*init)(const WfArgs*, cudaStream_t);
+    cudaError_t (*job_add)(const WfArgs*, const WfJob*, uint32_t, uint32_t, cudaStream_t);
+    cudaError_t (*iteration)(const WfArgs*, bool, int, cudaStream_t, cudaEvent_t*, const void*);
+    const void* (*march_warp_normals)();
+    cudaError_t (*persist)(const WfArgs*, int, int, uint64_t, cudaStream_t);
+    int (*persist_blocks_per_sm)(int);
+    cudaError_t (*resolve)(const WfArgs*, uint32_t, const pt_push*, float4*, const float4*, cudaStream_t);
+};
+// checked = false: the kernels above; true: the same kernels built with
+// PT_DEBUG_CHECKS (pt_wavefront_checked.cu): every queue, pool-slot, ring and
+// sample index is checked before use, a failed check is recorded in the
+// counters (check_site, check_index) and its access skipped.
+const WfKernelSet* ptk_wavefront_kernels(bool checked);
 #endif  // !__CUDACC_RTC__

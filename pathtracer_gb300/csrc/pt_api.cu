@@ -54,6 +54,7 @@ struct pt_ctx {
     uint32_t last_iterations = 0;
     uint64_t drain_limit = 0;      // iteration cap of the wavefront drain (0: the bound computed per dispatch)
     bool fp_contract = false;      // run-time compiled kernels with FMA contraction (pt_set_fp_contract)
+    bool device_checks = false;    // the wavefront engine's checked kernel build (pt_set_device_checks)
     // GLSL snippets other than the shipped four (PT_SDF_CUSTOM slots), as
     // translated by pt_glsl_translate, and the module compiled for them.
     std::vector<JitSlot> custom;
@@ -297,6 +298,12 @@ int pt_set_trace(pt_ctx* ctx, uint32_t* d_events, uint32_t* d_nevents, float* d_
 int pt_set_fp_contract(pt_ctx* ctx, int on) {
     if (!ctx) return PT_ERR_INVALID;
     ctx->fp_contract = on != 0;
+    return PT_OK;
+}
+
+int pt_set_device_checks(pt_ctx* ctx, int on) {
+    if (!ctx) return PT_ERR_INVALID;
+    ctx->device_checks = on != 0;
     return PT_OK;
 }
 
@@ -618,10 +625,11 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     // normal pass.
     bool bulb = false;
     for (int i = 0; i < ctx->nplug; i++) bulb = bulb || ctx->plug[i].kind == PT_SDF_MANDELBULB;
+    ctx->wf->set_checks(ctx->device_checks);
     ctx->wf->set_march_kernel(!ctx->custom.empty()
                                   ? reinterpret_cast<const void*>(
                                         ctx->jit[kJitMarch][(size_t)ctx->jit_cur[kJitMarch]].kernel[0])
-                                  : (bulb ? ptk_wavefront_march_warp_normals() : nullptr));
+                                  : (bulb ? ctx->wf->kernels->march_warp_normals() : nullptr));
     const size_t cbytes = (size_t)total * sizeof(float4);
     if (cbytes > ctx->colors_bytes) {
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -657,6 +665,10 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     const cudaError_t e = E.drain(trace, max_iter);
     if (e == cudaErrorTimeout) return fail(ctx, PT_ERR_KERNEL, "pt_dispatch: wavefront did not drain");
     PT_CUDA_TRY(ctx, e);
+    uint32_t bad_index = 0;
+    if (const uint32_t site = E.check_failed(&bad_index))
+        return fail(ctx, PT_ERR_KERNEL, std::string("pt_dispatch: device index check failed: ") +
+                                            pt_check_site_name(site) + " (index " + std::to_string(bad_index) + ")");
     ctx->last_iterations = E.host_counters->iterations;
     E.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
     PT_CUDA_TRY(ctx, E.resolve(idx));
@@ -671,8 +683,10 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
 static int ensure_jit(pt_ctx* ctx, JitKind kind) {
     constexpr size_t kJitCache = 8;
     std::vector<JitModule>& cache = ctx->jit[kind];
-    // the cache key carries the contraction choice with the program text
-    const std::string program = pt_jit_program(ctx->custom, kind) + (ctx->fp_contract ? "// fmad\n" : "");
+    // the cache key carries the contraction choice with the program text;
+    // a checked march kernel is the same source with PT_DEBUG_CHECKS
+    const std::string program = (kind == kJitMarch && ctx->device_checks ? "#define PT_DEBUG_CHECKS 1\n" : "") +
+                                pt_jit_program(ctx->custom, kind) + (ctx->fp_contract ? "// fmad\n" : "");
     for (size_t i = 0; i < cache.size(); i++)
         if (cache[i].key == program) {
             ctx->jit_cur[kind] = (int)i;

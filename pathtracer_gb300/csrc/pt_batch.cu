@@ -93,6 +93,7 @@ struct pt_batch {
     int route = PT_BATCH_ROUTE_AUTO;
     int march_budget = 64;
     int persist_refill = 16;
+    bool device_checks = false;  // both engines on the checked kernel build (pt_batch_set_device_checks)
     std::vector<BatchScene> scenes;
     std::vector<BatchTarget> targets;
     std::deque<BatchPass> passes;  // indexed by pass id - pass_base
@@ -159,7 +160,7 @@ BatchPass* pass_at(pt_batch* b, uint32_t j) {
 // the batch, else the default built-in one (null).
 const void* staged_march_kernel(const pt_batch* b) {
     if (b->jit.lib) return reinterpret_cast<const void*>(b->jit.kernel[0]);
-    return b->bulb ? ptk_wavefront_march_warp_normals() : nullptr;
+    return b->bulb ? ptk_wavefront_kernels(b->device_checks)->march_warp_normals() : nullptr;
 }
 
 // Creates engine e on first use: the staged engine with the batch's pool,
@@ -178,6 +179,7 @@ cudaError_t ensure_engine(pt_batch* b, int e) {
     }
     b->engine[e].set_persistent(e == kPersistent);
     b->engine[e].args.persist_refill = b->persist_refill;
+    b->engine[e].set_checks(b->device_checks);
     if (e == kStaged) b->engine[e].set_march_kernel(staged_march_kernel(b));
     b->engine_live[e] = true;
     return cudaSuccess;
@@ -645,7 +647,8 @@ namespace {
 // brought new ones since the last compile, and hands it to the staged engine.
 int prepare_jit(pt_batch* b) {
     if (!b->jit_dirty) return PT_OK;
-    const std::string program = pt_jit_program(b->custom, kJitMarch);
+    const std::string program =
+        (b->device_checks ? "#define PT_DEBUG_CHECKS 1\n" : "") + pt_jit_program(b->custom, kJitMarch);
     std::vector<char> cubin;
     std::string lowered[kJitMaxKernels], log;
     JitModule m;
@@ -700,6 +703,14 @@ int pt_batch_step(pt_batch* b, int iterations, int* completed, int capacity, int
     for (int e = 0; e < 2; e++) {
         if (!busy[e]) continue;
         WfEngine& E = b->engine[e];
+        if (E.checks) {
+            PT_B_TRY(b, E.read_counters(E.host_counters));
+            uint32_t bad_index = 0;
+            if (const uint32_t site = E.check_failed(&bad_index))
+                return bfail(b, PT_ERR_KERNEL, std::string("pt_batch_step: device index check failed: ") +
+                                                   pt_check_site_name(site) + " (index " +
+                                                   std::to_string(bad_index) + ")");
+        }
         PT_B_TRY(b, E.read_finished(E.lo, E.njobs, b->h_finished));
         for (uint32_t j = E.lo; j < E.njobs; j++) {
             BatchPass& p = *pass_at(b, b->eorder[e][j - E.lo]);
@@ -763,6 +774,56 @@ int pt_batch_pending(pt_batch* b) {
     for (const BatchPass& p : b->passes)
         if (!p.done) n++;
     return n;
+}
+
+int pt_batch_set_device_checks(pt_batch* b, int on) {
+    if (!b) return PT_ERR_INVALID;
+    if (pt_batch_pending(b) > 0) return bfail(b, PT_ERR_BUSY, "pt_batch_set_device_checks: passes are in flight");
+    PT_B_TRY(b, cudaSetDevice(b->device));
+    b->device_checks = on != 0;
+    for (int e = 0; e < 2; e++) {
+        if (!b->engine_live[e]) continue;
+        PT_B_TRY(b, cudaStreamSynchronize(b->engine[e].stream));
+        b->engine[e].set_checks(b->device_checks);
+    }
+    if (!b->custom.empty()) b->jit_dirty = true;  // the march kernel of the other build
+    if (b->engine_live[kStaged] && !b->jit_dirty) b->engine[kStaged].set_march_kernel(staged_march_kernel(b));
+    return PT_OK;
+}
+
+int pt_batch_render_fp64(pt_batch* b, int scene_id, int target_id, const pt_push* push) {
+    if (!b) return PT_ERR_INVALID;
+    if (!push) return bfail(b, PT_ERR_INVALID, "pt_batch_render_fp64: null push constants");
+    if (scene_id < 0 || scene_id >= (int)b->scenes.size() || !b->scenes[(size_t)scene_id].live)
+        return bfail(b, PT_ERR_INVALID, "pt_batch_render_fp64: unknown or released scene");
+    if (check_target(b, target_id, "pt_batch_render_fp64") != PT_OK) return PT_ERR_INVALID;
+    BatchTarget& t = b->targets[(size_t)target_id];
+    if (t.kind != PT_TARGET_FP64) return bfail(b, PT_ERR_INVALID, "pt_batch_render_fp64: the target is not FP64");
+    if (push->resolution[0] != t.width || push->resolution[1] != t.height)
+        return bfail(b, PT_ERR_INVALID, "pt_batch_render_fp64: resolution differs from the target's");
+    if (push->samplesPerFrame <= 0) return bfail(b, PT_ERR_INVALID, "pt_batch_render_fp64: samplesPerFrame <= 0");
+    const BatchScene& sc = b->scenes[(size_t)scene_id];
+    if (sc.custom)
+        return bfail(b, PT_ERR_UNSUPPORTED, "pt_batch_render_fp64: SDF text compiled at run time has no double form");
+    PT_B_TRY(b, cudaSetDevice(b->device));
+    // The kernel takes the scene by value (its launch's constant bank): read
+    // the resident copy back, rotation matrices and extensions included.
+    KParams* P = new (std::nothrow) KParams;
+    if (!P) return bfail(b, PT_ERR_OOM, "pt_batch_render_fp64: out of host memory");
+    std::memset(P, 0, sizeof *P);
+    cudaError_t e = cudaMemcpyAsync(&P->s, sc.d_scene, sizeof(KScene), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e == cudaSuccess) {
+        P->pc = *push;
+        P->cie = sc.d_cie;
+        P->sums = t.d_sum;
+        e = ptk_launch_fp64(P, false, b->stream);
+        b->kernel_launches += 1;
+    }
+    delete P;
+    if (e != cudaSuccess) return bcuda(b, e, "pt_batch_render_fp64");
+    t.samples += (uint64_t)push->samplesPerFrame;
+    return PT_OK;
 }
 
 int pt_batch_run(pt_batch* b, uint64_t max_iterations) {

@@ -155,6 +155,24 @@ void WfEngine::set_tuning(int refill, int drain, int bps, int inner) {
 
 void WfEngine::set_persistent(bool on) { persistent = on; }
 
+void WfEngine::set_checks(bool on) {
+    if (on != checks) drop_graph();
+    checks = on;
+    kernels = ptk_wavefront_kernels(on);
+}
+
+uint32_t WfEngine::check_failed(uint32_t* index) const {
+    if (!checks || !host_counters || host_counters->check_site == PT_CHECK_NONE) return PT_CHECK_NONE;
+    if (index) *index = host_counters->check_index;
+    return host_counters->check_site;
+}
+
+extern const WfKernelSet ptk_wavefront_kernel_set;
+extern const WfKernelSet ptk_wavefront_kernel_set_checked;
+const WfKernelSet* ptk_wavefront_kernels(bool checked) {
+    return checked ? &ptk_wavefront_kernel_set_checked : &ptk_wavefront_kernel_set;
+}
+
 void WfEngine::set_march_kernel(const void* kernel) {
     if (kernel != march_kernel) drop_graph();
     march_kernel = kernel;
@@ -165,7 +183,7 @@ cudaError_t WfEngine::reset() {
     total = 0;
     persist_issued = 0;
     kernel_launches += 1;
-    return ptk_wavefront_launch_init(&args, stream);
+    return kernels->init(&args, stream);
 }
 
 cudaError_t WfEngine::add_pass(const WfJob& job, uint32_t* index) {
@@ -179,7 +197,7 @@ cudaError_t WfEngine::add_pass(const WfJob& job, uint32_t* index) {
     const uint32_t idx = njobs;
     // Stream-ordered: kernels launched from now on see job_hi = idx + 1 and
     // derive the sample total from this entry.
-    EN_TRY(ptk_wavefront_launch_job_add(&args, &j, idx, lo, stream));
+    EN_TRY(kernels->job_add(&args, &j, idx, lo, stream));
     kernel_launches += 1;
     jobs[idx % max_jobs] = j;
     njobs = idx + 1;
@@ -202,7 +220,7 @@ cudaError_t WfEngine::build_graph() {
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         for (int i = 0; i < graph_chunk && e == cudaSuccess; i++)
-            e = ptk_wavefront_launch_iteration(&a, false, grid, cs, nullptr, march_kernel);
+            e = kernels->iteration(&a, false, grid, cs, nullptr, march_kernel);
         const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
         if (e == cudaSuccess) e = e2;
     }
@@ -254,8 +272,7 @@ cudaError_t WfEngine::run(int n, bool trace) {
     if (stage_timing && !persistent) {
         for (int i = 0; i < n; i++) {
             if (stage_ev_used == kStageEvRounds) EN_TRY(flush_stage_events());
-            EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, &stage_ev[stage_ev_used * 6],
-                                                  march_kernel));
+            EN_TRY(kernels->iteration(&args, trace, grid, stream, &stage_ev[stage_ev_used * 6], march_kernel));
             kernel_launches += kWfKernelsPerIteration;
             stage_ev_used++;
         }
@@ -266,7 +283,7 @@ cudaError_t WfEngine::run(int n, bool trace) {
         int variant = 0;
         for (uint32_t j = lo; j < njobs; j++) variant = pt_variant_union(variant, jobs[j % max_jobs].variant);
         for (int i = 0; i < n && persist_issued < total; i++) {
-            EN_TRY(ptk_persist_launch(&args, variant, sms, persist_budget, stream));
+            EN_TRY(kernels->persist(&args, variant, sms, persist_budget, stream));
             kernel_launches += 2;  // setup + persistent kernel
             persist_issued = (total - persist_issued > persist_budget) ? persist_issued + persist_budget : total;
         }
@@ -280,7 +297,7 @@ cudaError_t WfEngine::run(int n, bool trace) {
         }
     }
     for (int i = 0; i < n; i++) {
-        EN_TRY(ptk_wavefront_launch_iteration(&args, trace, grid, stream, nullptr, march_kernel));
+        EN_TRY(kernels->iteration(&args, trace, grid, stream, nullptr, march_kernel));
         kernel_launches += kWfKernelsPerIteration;
     }
     return cudaSuccess;
@@ -312,7 +329,7 @@ cudaError_t WfEngine::resolve(uint32_t j, cudaStream_t on) {
     if (j >= njobs || j < lo) return cudaErrorInvalidValue;
     const WfJob& J = job(j);
     kernel_launches += 1;
-    return ptk_wavefront_launch_resolve(&args, j % max_jobs, &J.pc, J.accum, J.colors, on ? on : stream);
+    return kernels->resolve(&args, j % max_jobs, &J.pc, J.accum, J.colors, on ? on : stream);
 }
 
 cudaError_t WfEngine::drain(bool trace, uint64_t max_iterations) {
@@ -331,6 +348,9 @@ cudaError_t WfEngine::drain(bool trace, uint64_t max_iterations) {
         iter += (uint64_t)chunk;
         EN_TRY(read_counters(&c));
         if (c.next_sample == c.total && c.live == 0) return cudaSuccess;
+        // A failed index check skipped an access and may have lost a path:
+        // stop here; the caller reports it (check_failed).
+        if (c.check_site != PT_CHECK_NONE) return cudaSuccess;
         if (iter > max_iterations) return cudaErrorTimeout;
         if (chunk < 64) chunk *= 2;
     }

@@ -56,6 +56,19 @@ inline bool pt_ext_valid(const pt_scene_ext* x, std::string* why) {
     return true;
 }
 
+// Names of the PT_CHECK_* sites for error messages.
+inline const char* pt_check_site_name(uint32_t site) {
+    switch (site) {
+        case PT_CHECK_QUEUE_APPEND: return "queue append past the pool size";
+        case PT_CHECK_QUEUE_SLOT: return "queue entry outside the pool";
+        case PT_CHECK_FREE_INDEX: return "free-list read outside the list";
+        case PT_CHECK_JOB: return "pass index outside the job ring";
+        case PT_CHECK_SAMPLE: return "sample index outside its pass";
+        case PT_CHECK_QUEUE_COUNT: return "queue length above the pool size";
+        default: return "unknown site";
+    }
+}
+
 struct WfEngine {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -97,6 +110,10 @@ struct WfEngine {
     const void* march_kernel = nullptr;
     // Kernels this engine has launched (graph replays counted per kernel).
     uint64_t kernel_launches = 0;
+    // The wavefront kernels launched: the default build, or the checked one
+    // (set_checks; its failed index checks are read back by check_failed).
+    const WfKernelSet* kernels = ptk_wavefront_kernels(false);
+    bool checks = false;
 
     // Bytes of device memory for `pool` slots and `max_jobs` ring entries.
     static size_t bytes_for(uint32_t pool, uint32_t max_jobs);
@@ -117,6 +134,13 @@ struct WfEngine {
     void set_tuning(int refill_min, int drain_lanes, int blocks_per_sm, int march_inner);
     // Sets march_kernel (null: the built-in kernel).
     void set_march_kernel(const void* kernel);
+    // The checked kernel build on or off (the march kernel set by
+    // set_march_kernel must be of the same build).
+    void set_checks(bool on);
+    // After read_counters or drain: the site (PT_CHECK_*) and index of the
+    // first failed index check since the last reset, 0 when none failed or
+    // the checks are off.
+    uint32_t check_failed(uint32_t* index) const;
     // Staged kernels (false) or the persistent path kernel (true).
     void set_persistent(bool on);
     // Persistent mode: every sample added so far is covered by a launch.

@@ -214,7 +214,7 @@ class PtServerOpts(ctypes.Structure):
         ("iterations_per_poll", ctypes.c_int32),
         ("passes_in_flight", ctypes.c_int32),
         ("keep_images", ctypes.c_int32),
-        ("pad", ctypes.c_int32),
+        ("fp64_paths", ctypes.c_int32),
     ]
 
 
@@ -287,6 +287,7 @@ CUDA_API = [
     ("pt_last_error", ctypes.c_char_p, [_vp]),
     ("pt_set_trace", _i, [_vp, _vp, _vp, _vp, _i]),
     ("pt_set_drain_limit", _i, [_vp, ctypes.c_uint64]),
+    ("pt_set_device_checks", _i, [_vp, _i]),
     ("pt_set_fp_contract", _i, [_vp, _i]),
     ("pt_sdf_source_fingerprint", ctypes.c_uint64, [ctypes.c_char_p]),
     ("pt_mathf_eval", _i, [_vp, _i, _vp, _vp, _vp, _i]),
@@ -309,6 +310,7 @@ CUDA_API = [
     ("pt_batch_stream", _vp, [_vp]),
     ("pt_batch_set_march_budget", _i, [_vp, _i]),
     ("pt_batch_set_route", _i, [_vp, _i]),
+    ("pt_batch_set_device_checks", _i, [_vp, _i]),
     ("pt_batch_set_persist_refill", _i, [_vp, _i]),
     ("pt_batch_add_scene", _i, [_vp, _vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
     ("pt_batch_set_scene_ext", _i, [_vp, _i, _vp]),
@@ -316,6 +318,7 @@ CUDA_API = [
     ("pt_batch_add_target", _i, [_vp, _i, _i, _i, ctypes.POINTER(_i)]),
     ("pt_batch_target_device_ptr", _vp, [_vp, _i]),
     ("pt_batch_add_pass", _i, [_vp, _i, _i, ctypes.POINTER(PtPush), ctypes.POINTER(_i)]),
+    ("pt_batch_render_fp64", _i, [_vp, _i, _i, ctypes.POINTER(PtPush)]),
     ("pt_batch_step", _i, [_vp, _i, ctypes.POINTER(_i), _i, ctypes.POINTER(_i)]),
     ("pt_batch_pending", _i, [_vp]),
     ("pt_batch_run", _i, [_vp, ctypes.c_uint64]),

@@ -281,6 +281,10 @@ class Context:
         """Caps the wavefront drain's iterations (0: the library's bound)."""
         self._check(self._lib.pt_set_drain_limit(self._h, max_iterations))
 
+    def set_device_checks(self, on: bool):
+        """The wavefront engine's kernels with index checks (pt_set_device_checks)."""
+        self._check(self._lib.pt_set_device_checks(self._h, int(on)))
+
     def set_trace(self, events_ptr: int, nevents_ptr: int, colors_ptr: int, depth_cap: int):
         self._check(self._lib.pt_set_trace(self._h, events_ptr or None, nevents_ptr or None, colors_ptr or None,
                                            depth_cap))
@@ -332,6 +336,10 @@ class Batch:
     def set_route(self, route: int):
         self._check(self._lib.pt_batch_set_route(self._h, route))
 
+    def set_device_checks(self, on: bool):
+        """Both engines' kernels with index checks (pt_batch_set_device_checks)."""
+        self._check(self._lib.pt_batch_set_device_checks(self._h, int(on)))
+
     def add_scene(self, ubo: np.ndarray, plugins: list) -> int:
         ubo = np.ascontiguousarray(ubo, np.float32)
         assert ubo.size == native.UBO_FLOATS
@@ -364,6 +372,11 @@ class Batch:
         out = ctypes.c_int()
         self._check(self._lib.pt_batch_add_pass(self._h, scene, target, ctypes.byref(push), ctypes.byref(out)))
         return out.value
+
+    def render_fp64(self, scene: int, target: int, push: PtPush):
+        """pt_batch_render_fp64: one dispatch's samples traced in double
+        precision into an FP64 target."""
+        self._check(self._lib.pt_batch_render_fp64(self._h, scene, target, ctypes.byref(push)))
 
     def step(self, iterations: int, capacity: int = 4096) -> list[int]:
         ids = (ctypes.c_int * max(1, capacity))()
@@ -426,10 +439,11 @@ class Server:
 
     def __init__(self, device: int = 0, mode: int = native.PT_SERVE_BATCHED, spp_per_pass: int = 8,
                  hbm_budget: int = 64 << 30, pool_slots: int = 1 << 19, max_passes: int = 4096,
-                 iterations_per_poll: int = 4, passes_in_flight: int = 1, keep_images: bool = False):
+                 iterations_per_poll: int = 4, passes_in_flight: int = 1, keep_images: bool = False,
+                 fp64_paths: bool = False):
         self._lib = native.host()
         opts = native.PtServerOpts(mode, spp_per_pass, hbm_budget, pool_slots, max_passes, iterations_per_poll,
-                                   passes_in_flight, int(keep_images), 0)
+                                   passes_in_flight, int(keep_images), int(fp64_paths))
         h = ctypes.c_void_p()
         rc = self._lib.pt_server_create(ctypes.byref(h), device, ctypes.byref(opts))
         if rc != native.PT_OK:
