@@ -118,6 +118,9 @@ def parse_args():
     ap.add_argument("--workload", default="mandelbulb12",
                     choices=["mandelbulb12", "mandelbulb", "mandelbulb12_full", "batch64", "serve", "progressive"])
     ap.add_argument("--pass-spp", type=int, default=16, help="progressive: samples per pixel per pass")
+    ap.add_argument("--form", default="reference", choices=["reference", "full"],
+                    help="progressive: the scene in the reference's method, or in its full form (fBm terrain "
+                         "compiled at run time, a dispersive glass sphere, sky; menger_terrain_full.json)")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: Poisson arrivals per second")
     ap.add_argument("--duration", type=float, default=30.0, help="serve: seconds of arrivals")
     ap.add_argument("--target-rmse", type=float, default=0.02, help="serve: relative RMSE target per job")
@@ -126,6 +129,11 @@ def parse_args():
     ap.add_argument("--pool-scenes", type=int, default=16, help="serve: scenes in the request pool")
     ap.add_argument("--iters-per-poll", type=int, default=4, help="serve: engine iterations per server poll")
     ap.add_argument("--passes-in-flight", type=int, default=1, help="serve: passes in flight per job")
+    ap.add_argument("--serve-spheres", default="full", choices=["full", "reference"],
+                    help="serve: sphere jobs with real conductor mirrors and Cauchy dielectrics (PT_GEN_SPHERES_FULL, "
+                         "the configuration's materials) or mapped to the reference's Lambertian spectra")
+    ap.add_argument("--ref-paths", default="fp32", choices=["fp32", "fp64"],
+                    help="serve: references of FP32 paths summed in double, or traced in double (slow)")
     ap.add_argument("--sdf-scenes", default="varied", choices=["varied", "shipped"],
                     help="serve: SDF scenes with drawn powers/levels (GLSL compiled at run time) or the shipped snippets")
     ap.add_argument("--burst", type=int, default=0,
@@ -212,13 +220,18 @@ def fp32_peak_tflops(peaks):
 
 
 # DRAM bytes per launch of each stage kernel (dram__bytes_read.sum +
-# dram__bytes_write.sum), averaged over the launches of one dispatch of the
-# workload, from one ncu capture each (the launch-list summaries in
-# profiles/), keyed by workload and path-pool size; the other knobs were the
-# library defaults.  Other settings report null.
+# dram__bytes_write.sum) in the steady state of the workload's scene, keyed
+# by workload and path-pool size; the other knobs were the library defaults.
+# Each comes from one small-case ncu capture of one or two launches per
+# stage with the pool full (2^19 slots: profiles/wf_march_mandelbulb12_512x512_16spp.md;
+# 2^20 slots: profiles/stage_traffic_mandelbulb12_1024x1024_16spp_pool2e20.md):
+# per launch a stage moves the state of the rays in its queues, which a full
+# pool of the same size bounds the same way at the full image size (the last
+# iterations of a dispatch, with the pool draining, move less).  Other
+# settings report null.
 STAGE_TRAFFIC_BYTES = {
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 19): {"march": 78.83e6, "shade": 218.27e6, "gen": 100.56e6},
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): {"march": 333.27e6, "shade": 768.34e6, "gen": 217.00e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 19): {"march": 85.21e6, "shade": 243.73e6, "gen": 119.84e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): {"march": 450.46e6, "shade": 1085.83e6, "gen": 236.63e6},
 }
 # The library's default wavefront knobs.
 DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
@@ -272,7 +285,7 @@ def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, tkey=None
                     "hold no FP32 figure); achieved: hand-counted FP32 operations of the march stage's events "
                     "(pathtracer_gb300/workmodel.py, counts per sample from tests/golden/work_*.json) over the "
                     "summed device time of its launches in one step timed with per-stage CUDA events; traffic: "
-                    "DRAM bytes per launch from one ncu capture of this workload (profiles/)"}
+                    "DRAM bytes per launch from one small-case ncu capture of this scene with the pool full (profiles/)"}
     return roof, stages, ops
 
 
@@ -628,19 +641,21 @@ def serve_measure(opts, local, rank):
     n_sph = opts.pool_scenes - n_sdf
     pool = []
     sdf_kind = native.PT_GEN_SDF_VARIED if opts.sdf_scenes == "varied" else native.PT_GEN_SDF
+    sph_kind = native.PT_GEN_SPHERES_FULL if opts.serve_spheres == "full" else native.PT_GEN_SPHERES
     for k in range(opts.pool_scenes):
-        kind, seed = (native.PT_GEN_SPHERES, 1000 + k) if k < n_sph else (sdf_kind, 2000 + k)
+        kind, seed = (sph_kind, 1000 + k) if k < n_sph else (sdf_kind, 2000 + k)
         sc, spec = Scene.generate(kind, seed + 100000 * rank)
         push = sc.push_constants(spec.width, spec.height, 1, 1, 1, spec.pathLength)
         pool.append((kind, sc, spec, push))
     srv = Server(local, mode=native.PT_SERVE_BATCHED, spp_per_pass=8, hbm_budget=64 << 30,
                  pool_slots=opts.pool or (1 << 19), iterations_per_poll=opts.iters_per_poll,
-                 passes_in_flight=opts.passes_in_flight)
+                 passes_in_flight=opts.passes_in_flight, fp64_paths=opts.ref_paths == "fp64")
     t0 = time.perf_counter()
     for key, (kind, sc, spec, push) in enumerate(pool):
         # SDFs as text: generated snippets are compiled at run time (the
         # batch's march kernel, before its first step: here)
         srv.add_scene_sources(key, sc.pack_ubo(cie), sc.sdf_sources())
+        srv.set_scene_ext(key, sc.pack_ext())  # mirrors and dielectrics of the full-form sphere jobs
         srv.render_reference(key, push, opts.ref_spp, 32)
     ref_secs = time.perf_counter() - t0
 
@@ -660,7 +675,7 @@ def serve_measure(opts, local, rank):
         """Jobs and samples per scene kind; on the serial plain path also the
         seconds spent on each kind (admission to completion)."""
         out = {}
-        for name, kv in (("spheres", native.PT_GEN_SPHERES), ("sdf", sdf_kind)):
+        for name, kv in (("spheres", sph_kind), ("sdf", sdf_kind)):
             sel = [r for r, k in zip(res, kinds) if k == kv]
             out[name] = {"jobs": len(sel), "samples": sum(r.samples for r in sel)}
             if serial:
@@ -710,12 +725,16 @@ def serve_measure(opts, local, rank):
 
 
 def serve_config(opts):
-    return {"workload": SERVE_WORKLOAD + ("_varied_sdf" if opts.sdf_scenes == "varied" else "")
+    return {"workload": SERVE_WORKLOAD + ("_full_spheres" if opts.serve_spheres == "full" else "")
+            + ("_varied_sdf" if opts.sdf_scenes == "varied" else "")
             + ("_burst" if opts.burst else ""), "sdf_scenes": opts.sdf_scenes,
             "rate_jobs_per_s": None if opts.burst else opts.rate,
             "duration_s": None if opts.burst else opts.duration, "burst_jobs": opts.burst or None,
             "target_rmse": opts.target_rmse, "max_spp": opts.max_spp, "spp_per_pass": 8,
-            "reference_spp": opts.ref_spp, "reference": "FP32 paths summed in FP64",
+            "reference_spp": opts.ref_spp,
+            "reference": "FP64 paths" if opts.ref_paths == "fp64" else "FP32 paths summed in FP64",
+            "sphere_jobs": ("full form: Lambertian spectra, conductor mirrors, Cauchy dielectrics"
+                            if opts.serve_spheres == "full" else "materials mapped to Lambertian spectra"),
             "pool_scenes": opts.pool_scenes, "hbm_budget_gib": 64,
             "iterations_per_poll": opts.iters_per_poll, "passes_in_flight": opts.passes_in_flight}
 
@@ -751,6 +770,7 @@ def run_serve(args, rank, world):
 
 
 PROGRESSIVE_WORKLOAD = "menger_terrain_1920x1080_16spp_passes_depth12"
+PROGRESSIVE_SCENES = {"reference": "menger_terrain.json", "full": "menger_terrain_full.json"}
 
 
 def run_progressive(args, rank, world):
@@ -764,14 +784,17 @@ def run_progressive(args, rank, world):
     local = torch.cuda.current_device()
     W, H, depth, spf = 1920, 1080, 12, args.pass_spp
     npass = max(1, args.spp // spf)
-    scene = Scene.load(os.path.join(ROOT, "pathtracer_gb300", "scenes", "menger_terrain.json"))
+    scene = Scene.load(os.path.join(ROOT, "pathtracer_gb300", "scenes", PROGRESSIVE_SCENES[args.form]))
     cie = cie_analytic()
-    ubo, plugins = scene.pack_ubo(cie), scene.sdf_plugins()
+    ubo = scene.pack_ubo(cie)
     base = replicas.frame_base(rank, 1, 1, args.spp)  # distinct samples per replica
 
     b = Batch(local, pool_slots=args.pool or (1 << 19), max_passes=4096)
     b.set_route(native.PT_BATCH_ROUTE_STAGED)
-    sid = b.add_scene(ubo, plugins)
+    # the scene's SDFs as text: shipped snippets select plug-ins, the full
+    # form's fBm terrain is compiled at run time
+    sid = b.add_scene_sources(ubo, scene.sdf_sources())
+    b.set_scene_ext(sid, scene.pack_ext())
     ref = b.add_target(W, H, native.PT_TARGET_FP64)
     t0 = time.perf_counter()
     for k in range(max(1, args.ref_spp // 64)):
@@ -829,7 +852,8 @@ def run_progressive(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": npass, "warmup": 0,
         "ms_per_step": 1000.0 * wf_secs / npass, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": PROGRESSIVE_WORKLOAD, "resolution": [W, H], "spp": spf * npass, "pass_spp": spf,
+        "config": {"workload": PROGRESSIVE_WORKLOAD + ("_full" if args.form == "full" else ""), "resolution": [W, H],
+                   "spp": spf * npass, "pass_spp": spf,
                    "max_depth": depth, "reference_spp": args.ref_spp, "parallelism": f"replicas x{world}"},
         "progressive": {"wavefront": {"value": samples / wf_secs, "seconds": wf_secs},
                         "plain_megakernel": {"value": samples / pl_secs, "seconds": pl_secs},
@@ -1035,7 +1059,8 @@ def main():
         # served vs one after another through the plain megakernel.
         sopts = argparse.Namespace(pool_scenes=8, burst=args.serve_jobs, rate=args.rate, duration=args.duration,
                                    ref_spp=1024, max_spp=512, target_rmse=0.02, sdf_scenes="varied",
-                                   iters_per_poll=4, passes_in_flight=1, pool=0)
+                                   iters_per_poll=4, passes_in_flight=1, pool=0, serve_spheres=args.serve_spheres,
+                                   ref_paths=args.ref_paths)
         t0 = time.perf_counter()
         serve = serve_measure(sopts, local, rank)
         line["serve"] = {"config": serve_config(sopts), **serve, "wall_s": time.perf_counter() - t0,

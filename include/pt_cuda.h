@@ -224,8 +224,10 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push);
  * caller before the first call; mean = sum / count).  It draws the same
  * random stream as pt_dispatch for the same push constants, so the two
  * images differ only by the FP32 arithmetic's error and the few paths whose
- * branches it changes.  Scenes with run-time compiled SDF text: PT_ERR_UNSUPPORTED.
- * Asynchronous on the context's stream (pt_wait); pt_set_trace applies. */
+ * branches it changes.  SDF text compiled at run time is compiled once more
+ * for it, with every GLSL float a double (the text's literals keep their
+ * float values).  Asynchronous on the context's stream (pt_wait);
+ * pt_set_trace applies. */
 int pt_render_fp64(pt_ctx* ctx, const pt_push* push, double* d_sums);
 
 /* Engines behind pt_dispatch; both compute the reference's per-sample
@@ -484,8 +486,9 @@ int pt_batch_add_pass(pt_batch* batch, int scene_id, int target_id, const pt_pus
  * pt_render_fp64's kernel and added to an FP64 target, instead of FP32
  * paths summed in double as a pass does.  Asynchronous on the batch's
  * stream, ordered before every later RMSE reduction of the batch; it is no
- * pass (no pass id, nothing for pt_batch_step to return).  Scenes with
- * run-time compiled SDF text: PT_ERR_UNSUPPORTED. */
+ * pass (no pass id, nothing for pt_batch_step to return).  The batch's SDF
+ * text compiled at run time is compiled once more for it, in double (the
+ * first call after new snippets arrive takes seconds). */
 int pt_batch_render_fp64(pt_batch* batch, int scene_id, int target_id, const pt_push* push);
 /* pt_set_device_checks for both of the batch's engines; a failed check
  * makes pt_batch_step (and pt_batch_run) return PT_ERR_KERNEL.  PT_ERR_BUSY

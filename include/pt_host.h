@@ -173,8 +173,8 @@ typedef struct pt_server_opts {
     int32_t iterations_per_poll; /* engine iterations per pt_server_poll (default 4) */
     int32_t passes_in_flight;    /* per job (default 1) */
     int32_t keep_images;         /* keep finished images until pt_server_release */
-    int32_t fp64_paths;          /* references traced in double precision (pt_batch_render_fp64) where the
-                                    scene allows, else FP32 paths summed in double; default 0 (the latter) */
+    int32_t fp64_paths;          /* references traced in double precision (pt_batch_render_fp64) instead of
+                                    FP32 paths summed in double (the default, 0) */
 } pt_server_opts;
 
 typedef struct pt_server_job {
@@ -223,8 +223,7 @@ int pt_server_set_scene_ext(pt_server* server, int key, const pt_scene_ext* ext)
 /* Renders scene `key`'s FP64 reference for a view (push: resolution, camera,
  * path length) with spp samples per pixel from sample indices no request
  * uses; blocks until done.  With opts.fp64_paths the paths themselves are
- * traced in double precision (scenes with run-time compiled SDF text keep
- * FP32 paths). */
+ * traced in double precision (pt_batch_render_fp64). */
 int pt_server_render_reference(pt_server* server, int key, const pt_push* push, int spp, int spp_per_pass);
 int pt_server_submit(pt_server* server, const pt_server_job* job, uint64_t* job_id);
 /* Admits, feeds and advances the work once; returns jobs finished since the

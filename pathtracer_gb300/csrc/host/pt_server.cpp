@@ -426,9 +426,7 @@ int pt_server_render_reference(pt_server* s, int key, const pt_push* push, int s
     e.ref_h = H;
     s->resident_bytes += (uint64_t)W * (uint64_t)H * 32ull;
     // Sample indices from 2^30 on: independent of every request's samples.
-    // With fp64_paths, scenes whose SDF text is compiled at run time (the
-    // first pass is refused with PT_ERR_UNSUPPORTED) keep FP32 paths.
-    bool fp64_paths = s->opts.fp64_paths != 0;
+    const bool fp64_paths = s->opts.fp64_paths != 0;
     for (int k = 0; k < spp / spp_per_pass; k++) {
         pt_push p = *push;
         p.samplesPerFrame = spp_per_pass;
@@ -436,9 +434,8 @@ int pt_server_render_reference(pt_server* s, int key, const pt_push* push, int s
         p.currentSamples = spp_per_pass;
         if (fp64_paths) {
             rc = pt_batch_render_fp64(s->batch, e.batch_scene, e.ref_target, &p);
-            if (rc == PT_OK) continue;
-            if (rc != PT_ERR_UNSUPPORTED || k > 0) return from_batch(s, rc, "pt_server_render_reference");
-            fp64_paths = false;
+            if (rc != PT_OK) return from_batch(s, rc, "pt_server_render_reference");
+            continue;
         }
         int pid = -1;
         rc = pt_batch_add_pass(s->batch, e.batch_scene, e.ref_target, &p, &pid);

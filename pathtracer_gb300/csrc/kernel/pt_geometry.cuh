@@ -500,8 +500,9 @@ template <typename V> PT_DI SOf<V> sdf(V p) { return p.y - (height(p.x) + height
 
 // A scene's SDF slot `slot` with plug-in `kind`.  PT_SDF_CUSTOM slots hold
 // GLSL compiled at run time: the module built for them (pt_jit.cu) defines
-// pt_user_sdf / pt_user_material before including these headers; the
-// precompiled kernels never see that kind.
+// pt_user_sdf / pt_user_material (FP32 kernels) or pt_user_sdf_d /
+// pt_user_material_d (the FP64 renderer) before including these headers;
+// the precompiled kernels never see that kind.
 template <typename V, typename R = SOf<V>> PT_DI R plugin_sdf(int kind, int slot, V p) {
     switch (kind) {
         case PT_SDF_MANDELBULB: return sdf_mandelbulb::sdf(p);
@@ -510,8 +511,11 @@ template <typename V, typename R = SOf<V>> PT_DI R plugin_sdf(int kind, int slot
         case PT_SDF_TERRAIN: return sdf_terrain::sdf(p);
 #if defined(PT_JIT_USER_SDF)
         case PT_SDF_CUSTOM:
-            if constexpr (sizeof(R) == 4) return pt_user_sdf(slot, p);
-            return R(PT_MAXDIST);
+            if constexpr (sizeof(R) == 4) {
+                return pt_user_sdf(slot, p);
+            } else {
+                return pt_user_sdf_d(slot, p);  // the FP64 renderer's module
+            }
 #endif
         default: return R(PT_MAXDIST);
     }
@@ -523,8 +527,11 @@ template <typename V, typename R = SOf<V>> PT_DI R plugin_material(const pt_sdf_
         case PT_SDF_MANDELBULB: return sdf_mandelbulb::sdfmaterial(p, pl.material);
 #if defined(PT_JIT_USER_SDF)
         case PT_SDF_CUSTOM:
-            if constexpr (sizeof(R) == 4) return pt_user_material(slot, p);
-            return R(0);
+            if constexpr (sizeof(R) == 4) {
+                return pt_user_material(slot, p);
+            } else {
+                return pt_user_material_d(slot, p);
+            }
 #endif
         default: return R(pl.material[0]);
     }

@@ -337,6 +337,7 @@ PTG_FN vec4 fma(vec4 a, vec4 b, vec4 c) {
 }
 
 template <typename V> PTG_FN V clamp(V a, V lo, V hi) { return min(max(a, lo), hi); }
+PTG_FN float clamp(float a, float lo, float hi) { return min(max(a, lo), hi); }
 PTG_FN vec2 clamp(vec2 a, float lo, float hi) { return min(max(a, lo), hi); }
 PTG_FN vec3 clamp(vec3 a, float lo, float hi) { return min(max(a, lo), hi); }
 PTG_FN float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }

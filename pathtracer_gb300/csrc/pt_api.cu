@@ -62,7 +62,7 @@ struct pt_ctx {
     // kJitCache each, so switching between scenes does not recompile), and
     // the one the current snippets use.
     std::vector<JitModule> jit[kJitKinds];
-    int jit_cur[kJitKinds] = {-1, -1};
+    int jit_cur[kJitKinds] = {-1, -1, -1};
     std::string err;
 };
 
@@ -346,9 +346,12 @@ int pt_render_fp64(pt_ctx* ctx, const pt_push* push, double* d_sums) {
     if (!ctx->has_scene) return fail(ctx, PT_ERR_NO_SCENE, "pt_render_fp64: no scene uploaded");
     if (push->resolution[0] <= 0 || push->resolution[1] <= 0 || push->samplesPerFrame <= 0)
         return fail(ctx, PT_ERR_INVALID, "pt_render_fp64: bad resolution or samplesPerFrame");
-    if (!ctx->custom.empty())
-        return fail(ctx, PT_ERR_UNSUPPORTED, "pt_render_fp64: SDF text compiled at run time has no double form");
     PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->custom.empty()) {
+        // scene GLSL: the FP64 megakernel compiled with the snippets in double
+        const int rc = ensure_jit(ctx, kJitFp64);
+        if (rc != PT_OK) return rc;
+    }
     KParams& P = *ctx->params;
     P.pc = *push;
     P.accum = nullptr;
@@ -356,7 +359,9 @@ int pt_render_fp64(pt_ctx* ctx, const pt_push* push, double* d_sums) {
     P.cie = ctx->d_cie;
     P.trace = ctx->trace;
     const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
-    const cudaError_t e = ptk_launch_fp64(&P, trace, ctx->stream);
+    const cudaError_t e =
+        ctx->custom.empty() ? ptk_launch_fp64(&P, trace, ctx->stream)
+                            : pt_jit_launch(ctx->jit[kJitFp64][(size_t)ctx->jit_cur[kJitFp64]], &P, trace, ctx->stream);
     P.sums = nullptr;
     PT_CUDA_TRY(ctx, e);
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));

@@ -120,6 +120,7 @@ struct pt_batch {
     int custom_next = 0;
     JitModule jit;
     bool jit_dirty = false;
+    JitModule jit64;  // the FP64 renderer's megakernel for the same snippets (pt_batch_render_fp64), when needed
     // A scene with a mandelbulb was added: the staged engine's built-in march
     // kernel then probes normals across the warp.
     bool bulb = false;
@@ -394,6 +395,7 @@ int pt_batch_destroy(pt_batch* b) {
     if (b->h_finished) cudaFreeHost(b->h_finished);
     free_rmse(b);
     pt_jit_unload(b->jit);
+    pt_jit_unload(b->jit64);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return PT_OK;
@@ -671,6 +673,25 @@ int prepare_jit(pt_batch* b) {
     return PT_OK;
 }
 
+// The FP64 renderer's megakernel for every snippet the batch holds, compiled
+// again when scenes brought new ones since the last compile.
+int prepare_jit64(pt_batch* b) {
+    const std::string program = pt_jit_program(b->custom, kJitFp64);
+    if (b->jit64.lib && b->jit64.key == program) return PT_OK;
+    std::vector<char> cubin;
+    std::string lowered[kJitMaxKernels], log;
+    JitModule m;
+    int rc = pt_jit_compile(b->device, program, kJitFp64, cubin, lowered, log);
+    if (rc != PT_OK) return bfail(b, rc, "compiling the batch's SDF snippets in double: " + log);
+    rc = pt_jit_load(cubin, kJitFp64, lowered, m, log);
+    if (rc != PT_OK) return bfail(b, rc, log);
+    m.key = program;
+    PT_B_TRY(b, cudaStreamSynchronize(b->stream));  // the old module's launches
+    pt_jit_unload(b->jit64);
+    b->jit64 = m;
+    return PT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -803,9 +824,11 @@ int pt_batch_render_fp64(pt_batch* b, int scene_id, int target_id, const pt_push
         return bfail(b, PT_ERR_INVALID, "pt_batch_render_fp64: resolution differs from the target's");
     if (push->samplesPerFrame <= 0) return bfail(b, PT_ERR_INVALID, "pt_batch_render_fp64: samplesPerFrame <= 0");
     const BatchScene& sc = b->scenes[(size_t)scene_id];
-    if (sc.custom)
-        return bfail(b, PT_ERR_UNSUPPORTED, "pt_batch_render_fp64: SDF text compiled at run time has no double form");
     PT_B_TRY(b, cudaSetDevice(b->device));
+    if (sc.custom) {
+        const int jr = prepare_jit64(b);
+        if (jr != PT_OK) return jr;
+    }
     // The kernel takes the scene by value (its launch's constant bank): read
     // the resident copy back, rotation matrices and extensions included.
     KParams* P = new (std::nothrow) KParams;
@@ -817,7 +840,7 @@ int pt_batch_render_fp64(pt_batch* b, int scene_id, int target_id, const pt_push
         P->pc = *push;
         P->cie = sc.d_cie;
         P->sums = t.d_sum;
-        e = ptk_launch_fp64(P, false, b->stream);
+        e = sc.custom ? pt_jit_launch(b->jit64, P, false, b->stream) : ptk_launch_fp64(P, false, b->stream);
         b->kernel_launches += 1;
     }
     delete P;

@@ -40,14 +40,38 @@ namespace {
 const char* const kNames[kJitKinds][kJitMaxKernels] = {
     {"ptjit::megakernel<false, 15>", "ptjit::megakernel<true, 15>"},
     {"ptjit::wf_march", nullptr},
+    {"ptjit::megakernel<false, 15, double>", "ptjit::megakernel<true, 15, double>"},
 };
 
-int kernel_count(JitKind kind) { return kind == kJitMegakernel ? 2 : 1; }
+int kernel_count(JitKind kind) { return kind == kJitMarch ? 1 : 2; }
 
 }  // namespace
 
 std::string pt_jit_program(const std::vector<JitSlot>& slots, JitKind kind) {
     std::string s = kPrelude;
+    if (kind == kJitFp64) {
+        // The snippets in double: every `float` of the shim and of the
+        // translated text is a double (pt_mathf.h is included first so its
+        // float functions stay float); the user functions return doubles.
+        s += "#include \"../../../include/pt_mathf.h\"\n#define PTG_DOUBLE 1\n#define float double\n";
+        s += "#include \"pt_glsl_shim.h\"\n";
+        for (const JitSlot& j : slots) s += j.code + "\n";
+        s += "#undef float\n";
+        s += "template <typename P> static __device__ __forceinline__ double pt_user_sdf_d(int slot, const P& p) {\n"
+             "  switch (slot) {\n";
+        for (const JitSlot& j : slots)
+            s += "    case " + std::to_string(j.slot) + ": return ptg::" + j.prefix + "::" + j.prefix +
+                 "sdf(ptg::vec3(p.x, p.y, p.z));\n";
+        s += "    default: return 1e5;\n  }\n}\n";
+        s += "template <typename P> static __device__ __forceinline__ double pt_user_material_d(int slot, const P& p) {\n"
+             "  switch (slot) {\n";
+        for (const JitSlot& j : slots)
+            s += "    case " + std::to_string(j.slot) + ": return ptg::" + j.prefix + "::" + j.prefix +
+                 "sdfmaterial(ptg::vec3(p.x, p.y, p.z));\n";
+        s += "    default: return 0.0;\n  }\n}\n";
+        s += "#include \"pt_megakernel_body.cuh\"\n";
+        return s;
+    }
     s += "#include \"pt_glsl_shim.h\"\n";
     for (const JitSlot& j : slots) s += j.code + "\n";
     s += "static __device__ __forceinline__ float pt_user_sdf(int slot, float3 p) {\n  switch (slot) {\n";

@@ -17,9 +17,11 @@ struct JitSlot {
 };
 
 // What a module holds: the megakernel (kernel[0] without, kernel[1] with
-// path traces) or the wavefront engine's march kernel (kernel[0]).  Each is
-// its own NVRTC program, compiled when first needed.
-enum JitKind { kJitMegakernel = 0, kJitMarch = 1, kJitKinds = 2 };
+// path traces), the wavefront engine's march kernel (kernel[0]), or the
+// FP64 reference renderer's megakernel (kernel[0], kernel[1] as for the
+// megakernel; the snippets compiled with every GLSL float a double).  Each
+// is its own NVRTC program, compiled when first needed.
+enum JitKind { kJitMegakernel = 0, kJitMarch = 1, kJitFp64 = 2, kJitKinds = 3 };
 constexpr int kJitMaxKernels = 2;
 
 struct JitModule {
@@ -41,5 +43,5 @@ int pt_jit_compile_for(int sm, const std::string& program, JitKind kind, std::ve
 int pt_jit_load(const std::vector<char>& cubin, JitKind kind, const std::string lowered[kJitMaxKernels], JitModule& m,
                 std::string& err);
 void pt_jit_unload(JitModule& m);
-// The megakernel of a kJitMegakernel module over the dispatch in params.
+// The megakernel of a kJitMegakernel or kJitFp64 module over the dispatch in params.
 cudaError_t pt_jit_launch(const JitModule& m, const KParams* params, bool trace, cudaStream_t stream);

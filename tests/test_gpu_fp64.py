@@ -9,10 +9,15 @@ drawing the same random stream as the FP32 kernels.  Checked here:
   paths' noise, so the FP64 image measures the FP32 arithmetic's error;
 - the accumulated sums: exposed colour sums and sample counts over two
   calls, their mean equal to the FP32 accumulator's up to that error;
-- what it refuses: scenes whose SDF text is compiled at run time.
+- scenes whose SDF text is compiled at run time (the 12-iteration
+  mandelbulb, the fBm terrain), whose snippets are compiled once more with
+  every GLSL float a double;
+- the FP32 method's bias at high sample counts on the Cornell box and the
+  12-iteration mandelbulb in their full forms: the mean of many samples
+  against the FP64 mean of the same samples.
 Scenes: the full-form Cornell box (Cauchy dielectric, flat spectra, analytic
-CMF), the shipped-snippet mandelbulb over a plane, and feature_mix (every
-analytic primitive and plug-in).
+CMF), the shipped-snippet mandelbulb over a plane, feature_mix (every
+analytic primitive and plug-in), and the run-time compiled scenes.
 """
 import os
 
@@ -51,8 +56,16 @@ def _host(tr, n, depth):
         col.cpu().numpy().reshape(n, 3)
 
 
+# Fraction of paths with the FP32 kernels' branch sequence, at least: the
+# escape-time fractal of 12 iterations parts more paths (its march converges
+# a step earlier or later near the surface) than the analytic scenes do.
+FRAC_MIN = {"mandelbulb12_plane": 0.85, "menger_terrain_full": 0.85}
+
+
 @pytest.mark.parametrize("name,W,H,spf,depth", [("cornell_box", 64, 64, 8, 8), ("cornell_box_full", 64, 64, 8, 8),
-                                                ("mandelbulb_plane", 64, 48, 8, 6), ("feature_mix", 64, 48, 8, 6)])
+                                                ("mandelbulb_plane", 64, 48, 8, 6), ("feature_mix", 64, 48, 8, 6),
+                                                ("mandelbulb12_plane", 64, 48, 8, 6),
+                                                ("menger_terrain_full", 48, 40, 4, 12)])
 def test_fp64_paths_follow_the_fp32_paths(rt, name, W, H, spf, depth):
     import torch
 
@@ -104,7 +117,7 @@ def test_fp64_paths_follow_the_fp32_paths(rt, name, W, H, spf, depth):
     # FP32 rounding sends some paths another way at a comparison near its
     # threshold (a grazing hit, an SDF march converging one step apart, a light
     # sample at a shadow edge); from there the two paths are independent.
-    assert frac >= 0.9
+    assert frac >= FRAC_MIN.get(name, 0.9)
     # identical paths: FP32 accuracy, except the cone pdf's cancellation near
     # small lights (a few per cent at the 99th percentile behind the
     # mandelbulb scene's small sun: the error the FP64 reference exposes)
@@ -116,7 +129,7 @@ def test_fp64_paths_follow_the_fp32_paths(rt, name, W, H, spf, depth):
     assert np.all(bias < 0.02), bias
 
 
-def test_fp64_sums_accumulate_and_jit_text_is_refused(rt):
+def test_fp64_sums_accumulate(rt):
     import torch
 
     from pathtracer_gb300 import PathTracerError, native
@@ -133,12 +146,40 @@ def test_fp64_sums_accumulate_and_jit_text_is_refused(rt):
         ctx.wait()
         s = sums.cpu().numpy().reshape(H, W, 4)
         assert np.all(s[..., 3] == 2 * spf) and np.all(np.isfinite(s)) and s[..., :3].sum() > 0
-    jit = rt["Scene"].load(os.path.join(SCENES, "mandelbulb12_plane.json"))
-    with rt["Context"](0) as ctx:
-        ctx.bind(jit, rt["cie"])
         with pytest.raises(PathTracerError) as e:
-            ctx.render_fp64(jit.push_constants(W, H, spf, spf, spf, 6), sums.data_ptr())
-        assert e.value.code == native.PT_ERR_UNSUPPORTED
+            ctx.render_fp64(scene.push_constants(W + 1, H, spf, spf, spf, 8), 0)
+        assert e.value.code == native.PT_ERR_INVALID
+
+
+@pytest.mark.parametrize("name,W,H,passes,spf,depth", [("cornell_box_full", 256, 256, 16, 16, 8),
+                                                       ("mandelbulb12_plane_full", 256, 256, 8, 16, 6)])
+def test_fp32_bias_at_high_spp(rt, name, W, H, passes, spf, depth):
+    """The FP32 method's image after passes x spf samples per pixel against
+    the FP64 renderer's mean of the same samples: the frame's total (the
+    bias of the FP32 arithmetic, the parted paths' noise averaged over the
+    frame) and the per-pixel relative RMSE (mostly the parted paths)."""
+    import torch
+
+    scene = rt["Scene"].load(os.path.join(SCENES, name + ".json"))
+    with rt["Context"](0) as ctx:
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        sums = torch.zeros(W * H * 4, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for k in range(1, passes + 1):
+            push = scene.push_constants(W, H, k * spf, k * spf, spf, depth)
+            ctx.dispatch(push)
+            ctx.render_fp64(push, sums.data_ptr())
+        ctx.wait()
+        acc = ctx.read_accum()[..., :3].astype(np.float64)
+        s64 = sums.cpu().numpy().reshape(H, W, 4)
+    assert np.all(s64[..., 3] == passes * spf)
+    ref = s64[..., :3] / s64[..., 3:4]
+    total = np.abs(acc.sum(axis=(0, 1)) - ref.sum(axis=(0, 1))) / np.abs(ref.sum(axis=(0, 1)))
+    rmse = float(np.sqrt(((acc - ref) ** 2).sum() / (ref ** 2).sum()))
+    print(f"{name} {W}x{H} {passes * spf} spp: frame total rel {total.tolist()}, per-pixel rel RMSE {rmse:.3e}")
+    assert np.all(total < 5e-3), total
+    assert rmse < 0.05
 
 
 def _mean_f32(sums):
@@ -189,10 +230,10 @@ def test_batch_fp64_pass_equals_the_context_renderer(rt):
 
 
 def test_server_references_with_fp64_paths(rt):
-    """pt_server_opts.fp64_paths: references traced in double precision; the
-    same job reaches an RMSE against them close to its RMSE against the
-    FP32-path reference (the two references differ by the FP32 error, far
-    below the job's noise).  A scene compiled at run time keeps FP32 paths."""
+    """pt_server_opts.fp64_paths: references traced in double precision (for
+    the scene compiled at run time too); each job reaches an RMSE against
+    them close to its RMSE against the FP32-path reference (the two
+    references differ by the FP32 error, far below the job's noise)."""
     from pathtracer_gb300 import Server, native
 
     cie = rt["cie"]
@@ -213,5 +254,5 @@ def test_server_references_with_fp64_paths(rt):
             rmse[fp64] = [done[i].rmse for i in ids]
             assert all(done[i].status == native.PT_OK for i in ids)
     print("relative RMSE, FP32-path vs FP64-path references:", rmse)
-    assert 0 < rmse[True][0] and abs(rmse[True][0] - rmse[False][0]) < 0.05 * rmse[False][0]
-    assert rmse[True][1] == rmse[False][1]  # the compiled scene's reference is the same FP32-path one
+    for a, b in zip(rmse[True], rmse[False]):
+        assert 0 < a and abs(a - b) < 0.05 * b
