@@ -123,8 +123,9 @@ float user_bulb8_sdf(float x, float y, float z) {
         const float r4 = r2 * r2;
         dr = 8.0f * (r4 * r2 * r) * dr + 1.0f;
         const float l = sqrtf(zx * zx + zz * zz);
-        const float il = 1.0f / l;
-        const float ir = 1.0f / r;
+        const float q = 1.0f / (l * r); /* one division for 1/l and 1/r */
+        const float il = r * q;
+        const float ir = l * q;
         const cheb8_t a = cheb8(zz * il);
         const cheb8_t b = cheb8(zy * ir);
         const float st8 = a.u7 * (zx * il);

@@ -40,7 +40,7 @@ OPS = {
     # the run-time compiled power-8 mandelbulb of scenes/mandelbulb12_plane.json
     # (the only GLSL text in a workload with a work model)
     "sdf_custom": (33, "march"),       # offset, initial length, 0.5*log(r)*r/dr
-    "bulb8_iters": (66, "march"),      # r^8 and r^7 by products, 2 reciprocals, 2 lengths, 2 Chebyshev pairs
+    "bulb8_iters": (68, "march"),      # r^8 and r^7 by products, 1/l and 1/r from one division, 2 lengths, 2 Chebyshev pairs
     "sdf_material": (23, "march"),     # sdfmaterial + normal normalisation
     # shade: emission, BRDF, sampling and next-event estimation
     "emit": (100, "shade"),            # Planck at 4 wavelengths
