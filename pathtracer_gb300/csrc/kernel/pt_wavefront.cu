@@ -80,20 +80,19 @@ PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t&
     job = __float_as_uint(e.z);
 }
 
-PT_DI void store_state(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t flags, uint32_t sample,
-                       uint32_t job) {
+// A new sample's state.  Its first step is a primary ray (march, then
+// shade_primary), which reads neither the shadow-ray fields (s2, s3) nor
+// the BRDF (s4) and writes them before any shadow ray reads them, so they
+// are not stored here.
+PT_DI void store_new_sample(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t sample, uint32_t job) {
     v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
     v.s1[slot] = make_float4(ps.dir.x, ps.dir.y, ps.dir.z, ps.brdfPdf);
-    v.s2[slot] = make_float4(ps.shDir.x, ps.shDir.y, ps.shDir.z, ps.cosL);
-    v.s3[slot] = make_float4(ps.nrm.x, ps.nrm.y, ps.nrm.z, ps.lightPdf);
-    v.s4[slot] = ps.brdf;
     v.s5[slot] = ps.rr;
     v.s6[slot] = ps.radiance;
     v.s7[slot] = ps.l;
-    v.s8[slot] = make_uint4(ps.seed, flags | bounce_word(ps), sample, (uint32_t)ps.shObj);
+    v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, (uint32_t)ps.shObj);
     v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
 }
-
 
 // The ring entry of the pass that holds global sample s: the last pass in
 // [lo, hi) with first <= s (passes are appended in increasing order of first).
@@ -200,14 +199,11 @@ __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
             const CamInfo cam = J.cam;
             PathState ps;
             start_sample(ps, *J.scene, pc, cam, xx, yy, uvx, uvy, (int)k);
-            ps.nrm = f3(0.0f, 0.0f, 0.0f);
-            ps.shDir = f3(0.0f, 0.0f, 1.0f);
-            ps.brdf = f4s(0.0f);
-            ps.brdfPdf = ps.lightPdf = ps.cosL = 0.0f;
+            ps.brdfPdf = 0.0f;
             ps.shLightID = -1.0f;
             ps.shObj = 0;
             ps.ev = 0;
-            store_state(v, slot, ps, 0u, local, job);
+            store_new_sample(v, slot, ps, local, job);
             march = route_ray(A, v, *J.scene, slot, ps.org, ps.dir);
         }
         push_routed(A, C, nxt, slot, valid, march, false);
