@@ -366,17 +366,25 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
             const StepResult r = shade_primary<TRACE>(ps, *J.scene, h, objectID, J.pc.pathLength);
             finish_shade<TRACE>(A, J, ps, r, sample, freed);
             if (!freed) {
-                // everything but the wavelengths (s7), which a bounce never changes
+                // everything but the wavelengths (s7), which a bounce never
+                // changes; the shadow-ray fields (s2, s3) and the BRDF (s4)
+                // only for a light sample's shadow ray (a next bounce's
+                // primary ray neither reads them nor reaches a reader of them)
                 v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
                 v.s1[slot] = make_float4(ps.dir.x, ps.dir.y, ps.dir.z, ps.brdfPdf);
-                v.s2[slot] = make_float4(ps.shDir.x, ps.shDir.y, ps.shDir.z, ps.cosL);
-                v.s3[slot] = make_float4(ps.nrm.x, ps.nrm.y, ps.nrm.z, ps.lightPdf);
-                v.s4[slot] = ps.brdf;
+                if (r == STEP_SHADOW) {
+                    v.s2[slot] = make_float4(ps.shDir.x, ps.shDir.y, ps.shDir.z, ps.cosL);
+                    v.s3[slot] = make_float4(ps.nrm.x, ps.nrm.y, ps.nrm.z, ps.lightPdf);
+                    v.s4[slot] = ps.brdf;
+                }
                 v.s5[slot] = ps.rr;
                 v.s6[slot] = ps.radiance;
                 v.s8[slot] = make_uint4(ps.seed, ((r == STEP_SHADOW) ? kShadowFlag : 0u) | bounce_word(ps), sample,
                                         (uint32_t)ps.shObj);
-                v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
+                // the light picked (read by the shadow-ray result) and the
+                // traced event word; the pass index (z) never changes
+                if (TRACE || r == STEP_SHADOW)
+                    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
                 again = true;
                 // the light sample's shadow ray, or the next bounce
                 shadow_next = (r == STEP_SHADOW);
