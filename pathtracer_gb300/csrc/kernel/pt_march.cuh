@@ -98,7 +98,16 @@ PT_DI PoolView view(const WfArgs& A) {
     return PoolView{p.s0, p.s1, p.s2, p.s3, p.s4, p.s5, p.s6, p.s7, p.s8, p.s9, p.h0, p.h1};
 }
 
-PT_DI uint32_t slot_job(const PoolView& v, uint32_t slot) { return __float_as_uint(v.s9[slot].z); }
+// s8.w packs the path's pass (its job-ring entry, 20 bits) with the
+// object index of its sampled light (12 bits, signed): a ray's pass is read
+// with its RNG word and flags in one load.
+constexpr uint32_t kJobShift = 12;
+static_assert(PT_MAX_SCENE_OBJECTS < 2048, "object indices must fit the 12-bit signed field of s8.w");
+static_assert(kMaxJobRing <= (1u << (32 - kJobShift)), "job-ring entries must fit the 20-bit field of s8.w");
+PT_DI uint32_t job_word(uint32_t job, int shObj) { return (job << kJobShift) | ((uint32_t)shObj & 0xFFFu); }
+PT_DI uint32_t word_job(uint32_t w) { return w >> kJobShift; }
+PT_DI int word_shobj(uint32_t w) { return (int)(w << 20) >> 20; }
+PT_DI uint32_t slot_job(const PoolView& v, uint32_t slot) { return word_job(v.s8[slot].w); }
 
 // SphereTracing (SC:779-860) with one SDF evaluation per loop iteration per
 // lane.  A converged ray takes its six normal probes on its own lane
@@ -268,9 +277,10 @@ PT_DI void march_rays(const WfArgs& A) {
                 if (idx < n && pt_check(A, qin[idx], A.pool_size, PT_CHECK_QUEUE_SLOT) &&
                     pt_check(A, slot_job(v, qin[idx]), A.job_cap, PT_CHECK_JOB)) {
                     slot = qin[idx];
-                    Sp = A.jobs[slot_job(v, slot)].scene;
+                    const uint4 w8 = v.s8[slot];
+                    Sp = A.jobs[word_job(w8.w)].scene;
                     const float4 o = v.s0[slot];
-                    const uint32_t flags = v.s8[slot].y;
+                    const uint32_t flags = w8.y;
                     shadow_ray = (flags & kShadowFlag) != 0;
                     const float4 d = shadow_ray ? v.s2[slot] : v.s1[slot];
                     org = f3(o.x, o.y, o.z);

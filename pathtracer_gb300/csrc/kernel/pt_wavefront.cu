@@ -73,11 +73,11 @@ PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t&
     ps.bounce = (int)(m.y & kBounceMask);
     ps.medium = (int)((m.y >> kMediumShift) & 3u);
     sample = m.z;
-    ps.shObj = (int)m.w;
+    ps.shObj = word_shobj(m.w);
+    job = word_job(m.w);
     const float4 e = v.s9[slot];
     ps.shLightID = e.x;
     ps.ev = __float_as_uint(e.y);
-    job = __float_as_uint(e.z);
 }
 
 // A new sample's state.  Its first step is a primary ray (march, then
@@ -90,8 +90,8 @@ PT_DI void store_new_sample(const PoolView& v, uint32_t slot, const PathState& p
     v.s5[slot] = ps.rr;
     v.s6[slot] = ps.radiance;
     v.s7[slot] = ps.l;
-    v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, (uint32_t)ps.shObj);
-    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
+    v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, job_word(job, ps.shObj));
+    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
 }
 
 // The ring entry of the pass that holds global sample s: the last pass in
@@ -232,6 +232,7 @@ PT_DI void count_finished(WfJob* __restrict__ jobs, uint32_t job, bool pred) {
 
 // A primary hit reads neither the shadow-ray fields (s2, s3) nor the BRDF
 // (s4): it writes them.
+template <bool TRACE>
 PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uint32_t& flags, uint32_t& sample,
                             uint32_t& job) {
     const float4 a = v.s0[slot], b = v.s1[slot];
@@ -253,11 +254,12 @@ PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uin
     ps.bounce = (int)(m.y & kBounceMask);
     ps.medium = (int)((m.y >> kMediumShift) & 3u);
     sample = m.z;
-    ps.shObj = (int)m.w;
-    const float4 e = v.s9[slot];
-    ps.shLightID = e.x;
-    ps.ev = __float_as_uint(e.y);
-    job = __float_as_uint(e.z);
+    ps.shObj = word_shobj(m.w);
+    job = word_job(m.w);
+    // s9 holds the light pick (set here before a shadow ray reads it) and
+    // the event word, which only a traced dispatch keeps
+    ps.shLightID = -1.0f;
+    ps.ev = TRACE ? __float_as_uint(v.s9[slot].y) : 0u;
 }
 
 // After a shadow-ray result only the throughput, the radiance, the RNG and
@@ -266,8 +268,8 @@ PT_DI void store_after_shadow(const PoolView& v, uint32_t slot, const PathState&
                               bool trace) {
     v.s5[slot] = ps.rr;
     v.s6[slot] = ps.radiance;
-    v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, (uint32_t)ps.shObj);
-    if (trace) v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
+    v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, job_word(job, ps.shObj));
+    if (trace) v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
 }
 
 // The end of a shaded step: trace records, the sample's colour when the
@@ -354,7 +356,7 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
         if (valid) {
             PathState ps;
             uint32_t flags, sample;
-            load_for_primary(v, slot, ps, flags, sample, job);
+            load_for_primary<TRACE>(v, slot, ps, flags, sample, job);
             const WfJob& J = A.jobs[job];
             const float4 h0 = v.h0[slot], h1 = v.h1[slot];
             Hit h;
@@ -380,11 +382,11 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
                 v.s5[slot] = ps.rr;
                 v.s6[slot] = ps.radiance;
                 v.s8[slot] = make_uint4(ps.seed, ((r == STEP_SHADOW) ? kShadowFlag : 0u) | bounce_word(ps), sample,
-                                        (uint32_t)ps.shObj);
+                                        job_word(job, ps.shObj));
                 // the light picked (read by the shadow-ray result) and the
-                // traced event word; the pass index (z) never changes
+                // traced event word
                 if (TRACE || r == STEP_SHADOW)
-                    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), __uint_as_float(job), 0.0f);
+                    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
                 again = true;
                 // the light sample's shadow ray, or the next bounce
                 shadow_next = (r == STEP_SHADOW);

@@ -12,8 +12,8 @@
 // Path state, structure of arrays, one entry per pool slot:
 //   s0 org.xyz, mis       s1 dir.xyz, brdfPdf    s2 shDir.xyz, cosL
 //   s3 nrm.xyz, lightPdf  s4 brdf                s5 throughput
-//   s6 radiance           s7 wavelengths         s8 seed, flags|bounce, sample (in its pass), shObj
-//   s9 shLightID, trace event word, job          h0 hitdist, materialID, lightID, objectID
+//   s6 radiance           s7 wavelengths         s8 seed, flags|bounce, sample (in its pass), job << 12 | shObj
+//   s9 shLightID, trace event word               h0 hitdist, materialID, lightID, objectID
 //   h1 hit normal
 // and the sphere-tracing state of a ray whose march continues in the next
 // iteration: m0 t, insT, omega, prevRadius; m1 tMinMax.xy, k, set1 bits;
@@ -25,6 +25,10 @@ struct WfPool {
     float4 *m0, *m1;
     uint32_t* m2;
 };
+
+// Entries of a job ring at most (a ring index is stored in 20 bits of the
+// path state).
+constexpr uint32_t kMaxJobRing = 1u << 20;
 
 // One render pass of one job: samplesPerFrame samples of every pixel.
 // The table is a ring of job_cap entries: pass number j (counting every pass

@@ -87,6 +87,7 @@ static cudaError_t common_setup(WfEngine& e, int device, cudaStream_t stream, ui
 }
 
 cudaError_t WfEngine::create(int dev, cudaStream_t s, uint32_t pool_slots, uint32_t max_job_count, int march_budget) {
+    if (max_job_count == 0 || max_job_count > kMaxJobRing) return cudaErrorInvalidValue;
     destroy();
     buffer_bytes = bytes_for(pool_slots, max_job_count);
     EN_TRY(cudaMalloc(&buffer, buffer_bytes));
@@ -103,7 +104,8 @@ cudaError_t WfEngine::create(int dev, cudaStream_t s, uint32_t pool_slots, uint3
 cudaError_t WfEngine::attach(int dev, cudaStream_t s, uint32_t pool_slots, uint32_t max_job_count, int march_budget,
                              void* device_buffer, size_t bytes, WfCounters* host_counters_storage,
                              WfJob* host_jobs) {
-    if (bytes < bytes_for(pool_slots, max_job_count) || !device_buffer || !host_counters_storage || !host_jobs)
+    if (bytes < bytes_for(pool_slots, max_job_count) || !device_buffer || !host_counters_storage || !host_jobs ||
+        max_job_count == 0 || max_job_count > kMaxJobRing)
         return cudaErrorInvalidValue;
     jobs = host_jobs;
     owns_jobs = false;
