@@ -81,17 +81,16 @@ PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t&
 }
 
 // A new sample's state.  Its first step is a primary ray (march, then
-// shade_primary), which reads neither the shadow-ray fields (s2, s3) nor
-// the BRDF (s4) and writes them before any shadow ray reads them, so they
-// are not stored here.
+// shade_primary), which reads neither the shadow-ray fields (s2, s3), the
+// BRDF (s4) nor the light pick (s9.x) and writes them before any shadow ray
+// reads them; at bounce 0 the throughput, the radiance and the event word
+// are start_sample's constants (1, 0, 0), which load_for_primary sets
+// instead of reading s5, s6 and s9.  So only s0, s1, s7 and s8 are stored.
 PT_DI void store_new_sample(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t sample, uint32_t job) {
     v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
     v.s1[slot] = make_float4(ps.dir.x, ps.dir.y, ps.dir.z, ps.brdfPdf);
-    v.s5[slot] = ps.rr;
-    v.s6[slot] = ps.radiance;
     v.s7[slot] = ps.l;
     v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, job_word(job, ps.shObj));
-    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
 }
 
 // The ring entry of the pass that holds global sample s: the last pass in
@@ -245,8 +244,6 @@ PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uin
     ps.nrm = f3(0.0f, 0.0f, 0.0f);
     ps.lightPdf = 0.0f;
     ps.brdf = f4s(0.0f);
-    ps.rr = v.s5[slot];
-    ps.radiance = v.s6[slot];
     ps.l = v.s7[slot];
     const uint4 m = v.s8[slot];
     ps.seed = m.x;
@@ -256,10 +253,20 @@ PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uin
     sample = m.z;
     ps.shObj = word_shobj(m.w);
     job = word_job(m.w);
-    // s9 holds the light pick (set here before a shadow ray reads it) and
-    // the event word, which only a traced dispatch keeps
+    // A first hit (bounce 0) has start_sample's throughput 1, radiance 0 and
+    // no events yet (store_new_sample stores none of them).  s9 holds the
+    // light pick (set here before a shadow ray reads it) and the event word,
+    // which only a traced dispatch keeps.
+    if (ps.bounce == 0) {
+        ps.rr = f4s(1.0f);
+        ps.radiance = f4s(0.0f);
+        ps.ev = 0u;
+    } else {
+        ps.rr = v.s5[slot];
+        ps.radiance = v.s6[slot];
+        ps.ev = TRACE ? __float_as_uint(v.s9[slot].y) : 0u;
+    }
     ps.shLightID = -1.0f;
-    ps.ev = TRACE ? __float_as_uint(v.s9[slot].y) : 0u;
 }
 
 // After a shadow-ray result only the throughput, the radiance, the RNG and
