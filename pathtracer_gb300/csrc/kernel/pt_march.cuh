@@ -87,15 +87,31 @@ PT_DI void q_push(const WfArgs& A, uint32_t* __restrict__ queue, uint32_t* count
     if (pred && pt_check(A, at, A.pool_size, PT_CHECK_QUEUE_APPEND)) queue[at] = value;
 }
 
+// One 16-byte field of the pool's pairs (WfPool): element slot of a field
+// is the first or second half of the slot's 32-byte pair.
+template <typename T> struct PairField {
+    T* p;
+    PT_DI T& operator[](uint32_t slot) const { return p[2u * slot]; }
+};
+template <typename T> PT_DI PairField<T> first_of(float4* pair) { return PairField<T>{reinterpret_cast<T*>(pair)}; }
+template <typename T> PT_DI PairField<T> second_of(float4* pair) {
+    return PairField<T>{reinterpret_cast<T*>(pair) + 1};
+}
+
 struct PoolView {
-    float4 *s0, *s1, *s2, *s3, *s4, *s5, *s6, *s7;  // see WfPool
-    uint4* s8;
-    float4 *s9, *h0, *h1;
+    PairField<float4> s0, s1, s2, s3, s4, s5, s6, s7;  // see WfPool
+    PairField<uint4> s8;
+    PairField<float4> s9, h0, h1, m0, m1;
+    uint32_t* m2;
 };
 
 PT_DI PoolView view(const WfArgs& A) {
     const WfPool& p = A.pool;
-    return PoolView{p.s0, p.s1, p.s2, p.s3, p.s4, p.s5, p.s6, p.s7, p.s8, p.s9, p.h0, p.h1};
+    return PoolView{first_of<float4>(p.s01), second_of<float4>(p.s01), first_of<float4>(p.s23),
+                    second_of<float4>(p.s23), first_of<float4>(p.s49), first_of<float4>(p.s56),
+                    second_of<float4>(p.s56), first_of<float4>(p.s78), second_of<uint4>(p.s78),
+                    second_of<float4>(p.s49), first_of<float4>(p.h01), second_of<float4>(p.h01),
+                    first_of<float4>(p.m01), second_of<float4>(p.m01), p.m2};
 }
 
 // s8.w packs the path's pass (its job-ring entry, 20 bits) with the
@@ -215,7 +231,7 @@ PT_DI void march_rays(const WfArgs& A) {
     const uint32_t n = C.n_march[cur];
     const uint32_t* __restrict__ qin = A.q_march[cur];
     const PoolView v = view(A);
-    const WfPool& M = A.pool;
+    const PoolView& M = v;
     const int lane = threadIdx.x & 31;
     const int budget = A.march_budget;
     const int refill_min = A.refill_min;

@@ -143,9 +143,9 @@ PT_DI bool route_ray(const WfArgs& A, const PoolView& v, const KScene& S, uint32
         uint32_t set1 = 0;
         march = search_sdf(S, org, invdir, tmm, set1);
         if (march) {
-            A.pool.m0[slot] = make_float4(fmaxf(tmm.x, 1e-3f), 0.0f, kOmegaMax, 0.0f);
-            A.pool.m1[slot] = make_float4(tmm.x, tmm.y, 0.0f, __uint_as_float(set1));
-            A.pool.m2[slot] = 0u;
+            v.m0[slot] = make_float4(fmaxf(tmm.x, 1e-3f), 0.0f, kOmegaMax, 0.0f);
+            v.m1[slot] = make_float4(tmm.x, tmm.y, 0.0f, __uint_as_float(set1));
+            v.m2[slot] = 0u;
         }
     }
     v.h0[slot] = make_float4(h.hitdist, h.materialID, h.lightID, __int_as_float(objectID));

@@ -9,7 +9,7 @@
 
 #include "pt_scene.cuh"
 
-// Path state, structure of arrays, one entry per pool slot:
+// Path state, one entry per pool slot, in 16-byte fields:
 //   s0 org.xyz, mis       s1 dir.xyz, brdfPdf    s2 shDir.xyz, cosL
 //   s3 nrm.xyz, lightPdf  s4 brdf                s5 throughput
 //   s6 radiance           s7 wavelengths         s8 seed, flags|bounce, sample (in its pass), job << 12 | shObj
@@ -18,11 +18,13 @@
 // and the sphere-tracing state of a ray whose march continues in the next
 // iteration: m0 t, insT, omega, prevRadius; m1 tMinMax.xy, k, set1 bits;
 // m2 saved flag | points << 10 | loop iterations.
+// Fields the stages read or write together are stored in pairs, one slot's
+// pair in one 32-byte sector: (s0, s1), (s2, s3), (s4, s9), (s5, s6),
+// (s7, s8), (h0, h1), (m0, m1).  Slots come from the queues in no useful
+// order, so a lone 16-byte field would use half of each sector it moves
+// (and a lone store makes the L2 read the other half from DRAM).
 struct WfPool {
-    float4 *s0, *s1, *s2, *s3, *s4, *s5, *s6, *s7;
-    uint4* s8;
-    float4 *s9, *h0, *h1;
-    float4 *m0, *m1;
+    float4 *s01, *s23, *s49, *s56, *s78, *h01, *m01;  // 2 x 16 B per slot each
     uint32_t* m2;
 };
 

@@ -22,20 +22,13 @@ T* take(uintptr_t& p, size_t count) {
 size_t layout(uintptr_t base, uint32_t pool, uint32_t max_jobs, WfArgs* a) {
     uintptr_t p = base;
     WfPool& P = a->pool;
-    P.s0 = take<float4>(p, pool);
-    P.s1 = take<float4>(p, pool);
-    P.s2 = take<float4>(p, pool);
-    P.s3 = take<float4>(p, pool);
-    P.s4 = take<float4>(p, pool);
-    P.s5 = take<float4>(p, pool);
-    P.s6 = take<float4>(p, pool);
-    P.s7 = take<float4>(p, pool);
-    P.s8 = take<uint4>(p, pool);
-    P.s9 = take<float4>(p, pool);
-    P.h0 = take<float4>(p, pool);
-    P.h1 = take<float4>(p, pool);
-    P.m0 = take<float4>(p, pool);
-    P.m1 = take<float4>(p, pool);
+    P.s01 = take<float4>(p, 2 * (size_t)pool);
+    P.s23 = take<float4>(p, 2 * (size_t)pool);
+    P.s49 = take<float4>(p, 2 * (size_t)pool);
+    P.s56 = take<float4>(p, 2 * (size_t)pool);
+    P.s78 = take<float4>(p, 2 * (size_t)pool);
+    P.h01 = take<float4>(p, 2 * (size_t)pool);
+    P.m01 = take<float4>(p, 2 * (size_t)pool);
     P.m2 = take<uint32_t>(p, pool);
     a->q_march[0] = take<uint32_t>(p, pool);
     a->q_march[1] = take<uint32_t>(p, pool);
