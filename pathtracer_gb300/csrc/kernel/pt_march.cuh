@@ -102,8 +102,15 @@ struct PoolView {
     PairField<float4> s0, s1, s2, s3, s4, s5, s6, s7;  // see WfPool
     PairField<uint4> s8;
     PairField<float4> s9, h0, h1, m0, m1;
-    uint32_t* m2;
 };
+
+// The word in m1.z of a suspended march: bit 31 set, the SDF sign k
+// (-1, 0, 1) + 1 in bits 26-27, points in bits 10-25 and the loop
+// iterations in bits 0-9.  A ray fresh from intersection has 0 there.
+PT_DI uint32_t march_word(float k, int points, int iter) {
+    const uint32_t kc = (k > 0.0f) ? 2u : ((k < 0.0f) ? 0u : 1u);
+    return 0x80000000u | (kc << 26) | ((uint32_t)min(points, 0xffff) << 10) | (uint32_t)iter;
+}
 
 PT_DI PoolView view(const WfArgs& A) {
     const WfPool& p = A.pool;
@@ -111,7 +118,7 @@ PT_DI PoolView view(const WfArgs& A) {
                     second_of<float4>(p.s23), first_of<float4>(p.s49), first_of<float4>(p.s56),
                     second_of<float4>(p.s56), first_of<float4>(p.s78), second_of<uint4>(p.s78),
                     second_of<float4>(p.s49), first_of<float4>(p.h01), second_of<float4>(p.h01),
-                    first_of<float4>(p.m01), second_of<float4>(p.m01), p.m2};
+                    first_of<float4>(p.m01), second_of<float4>(p.m01)};
 }
 
 // s8.w packs the path's pass (its job-ring entry, 20 bits) with the
@@ -306,14 +313,14 @@ PT_DI void march_rays(const WfArgs& A) {
                     hit_sel = -2;
                     // A ray from isect (flag bit clear: start with the sign
                     // probe) or one suspended by an earlier launch.
-                    const uint32_t saved = M.m2[slot];
                     const float4 a0 = M.m0[slot], a1 = M.m1[slot];
+                    const uint32_t saved = __float_as_uint(a1.z);
                     t = a0.x;
                     insT = a0.y;
                     omega = a0.z;
                     prevR = a0.w;
                     tmm = make_float2(a1.x, a1.y);
-                    k = a1.z;
+                    k = (float)(int)((saved >> 26) & 3u) - 1.0f;
                     set1 = __float_as_uint(a1.w);
                     iter = (int)(saved & 1023u);
                     points = (int)((saved >> 10) & 0xffffu);
@@ -416,8 +423,8 @@ PT_DI void march_rays(const WfArgs& A) {
                 } else if (!finished && (++steps >= budget || (drain && steps >= kDrainMinSteps))) {
                     // out of budget for this launch: save the state, continue next iteration
                     M.m0[slot] = make_float4(t, insT, omega, prevR);
-                    M.m1[slot] = make_float4(tmm.x, tmm.y, k, __uint_as_float(set1));
-                    M.m2[slot] = 0x80000000u | ((uint32_t)min(points, 0xffff) << 10) | (uint32_t)iter;
+                    M.m1[slot] = make_float4(tmm.x, tmm.y, __uint_as_float(march_word(k, points, iter)),
+                                             __uint_as_float(set1));
                     suspend = true;
                 }
             } else if (!WARP_NORMALS && phase >= MP_NORMAL0 && phase <= MP_NORMAL5) {

@@ -144,8 +144,7 @@ PT_DI bool route_ray(const WfArgs& A, const PoolView& v, const KScene& S, uint32
         march = search_sdf(S, org, invdir, tmm, set1);
         if (march) {
             v.m0[slot] = make_float4(fmaxf(tmm.x, 1e-3f), 0.0f, kOmegaMax, 0.0f);
-            v.m1[slot] = make_float4(tmm.x, tmm.y, 0.0f, __uint_as_float(set1));
-            v.m2[slot] = 0u;
+            v.m1[slot] = make_float4(tmm.x, tmm.y, __uint_as_float(0u), __uint_as_float(set1));  // not suspended
         }
     }
     v.h0[slot] = make_float4(h.hitdist, h.materialID, h.lightID, __int_as_float(objectID));
@@ -270,11 +269,14 @@ PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uin
 }
 
 // After a shadow-ray result only the throughput, the radiance, the RNG and
-// bounce word and (traced) the event word change.
+// bounce word and (traced) the event word change.  The wavelengths (s7)
+// never change but are stored with s8 so the pair's sector is written
+// whole (a partial sector write makes the L2 read the rest from DRAM).
 PT_DI void store_after_shadow(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t sample, uint32_t job,
                               bool trace) {
     v.s5[slot] = ps.rr;
     v.s6[slot] = ps.radiance;
+    v.s7[slot] = ps.l;
     v.s8[slot] = make_uint4(ps.seed, bounce_word(ps), sample, job_word(job, ps.shObj));
     if (trace) v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
 }
@@ -375,8 +377,7 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
             const StepResult r = shade_primary<TRACE>(ps, *J.scene, h, objectID, J.pc.pathLength);
             finish_shade<TRACE>(A, J, ps, r, sample, freed);
             if (!freed) {
-                // everything but the wavelengths (s7), which a bounce never
-                // changes; the shadow-ray fields (s2, s3) and the BRDF (s4)
+                // the path state; the shadow-ray fields (s2, s3) and the BRDF (s4)
                 // only for a light sample's shadow ray (a next bounce's
                 // primary ray neither reads them nor reaches a reader of them)
                 v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
@@ -388,6 +389,7 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
                 }
                 v.s5[slot] = ps.rr;
                 v.s6[slot] = ps.radiance;
+                v.s7[slot] = ps.l;  // unchanged: written with s8 so their sector is written whole
                 v.s8[slot] = make_uint4(ps.seed, ((r == STEP_SHADOW) ? kShadowFlag : 0u) | bounce_word(ps), sample,
                                         job_word(job, ps.shObj));
                 // the light picked (read by the shadow-ray result) and the

@@ -16,8 +16,8 @@
 //   s9 shLightID, trace event word               h0 hitdist, materialID, lightID, objectID
 //   h1 hit normal
 // and the sphere-tracing state of a ray whose march continues in the next
-// iteration: m0 t, insT, omega, prevRadius; m1 tMinMax.xy, k, set1 bits;
-// m2 saved flag | points << 10 | loop iterations.
+// iteration: m0 t, insT, omega, prevRadius; m1 tMinMax.xy, saved flag |
+// (k + 1) << 26 | points << 10 | loop iterations, set1 bits.
 // Fields the stages read or write together are stored in pairs, one slot's
 // pair in one 32-byte sector: (s0, s1), (s2, s3), (s4, s9), (s5, s6),
 // (s7, s8), (h0, h1), (m0, m1).  Slots come from the queues in no useful
@@ -25,7 +25,6 @@
 // (and a lone store makes the L2 read the other half from DRAM).
 struct WfPool {
     float4 *s01, *s23, *s49, *s56, *s78, *h01, *m01;  // 2 x 16 B per slot each
-    uint32_t* m2;
 };
 
 // Entries of a job ring at most (a ring index is stored in 20 bits of the
@@ -103,7 +102,7 @@ struct WfArgs {
 // Host side (not seen by the run-time compiled program, pt_jit.cu).
 #if !defined(__CUDACC_RTC__)
 // Bytes of the engine's device buffers for a pool of `pool` slots.
-inline size_t ptk_wavefront_pool_bytes(uint32_t pool) { return (size_t)pool * (14 * 16 + 8 * 4) + 32 * 256; }
+inline size_t ptk_wavefront_pool_bytes(uint32_t pool) { return (size_t)pool * (14 * 16 + 7 * 4) + 32 * 256; }
 
 cudaError_t ptk_wavefront_launch_init(const WfArgs* a, cudaStream_t stream);
 // Writes pass number `index` (camera derived on the device) and publishes

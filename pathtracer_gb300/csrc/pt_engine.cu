@@ -29,7 +29,6 @@ size_t layout(uintptr_t base, uint32_t pool, uint32_t max_jobs, WfArgs* a) {
     P.s78 = take<float4>(p, 2 * (size_t)pool);
     P.h01 = take<float4>(p, 2 * (size_t)pool);
     P.m01 = take<float4>(p, 2 * (size_t)pool);
-    P.m2 = take<uint32_t>(p, pool);
     a->q_march[0] = take<uint32_t>(p, pool);
     a->q_march[1] = take<uint32_t>(p, pool);
     a->q_shade[0] = take<uint32_t>(p, pool);

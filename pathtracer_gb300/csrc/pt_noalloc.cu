@@ -42,7 +42,7 @@ constexpr uint32_t kPool = PT_NOALLOC_POOL_SLOTS;
 constexpr uint32_t kMaxSamples = PT_NOALLOC_MAX_SAMPLES;
 // The engine's arrays for kPool slots and one pass (WfEngine::bytes_for).
 constexpr size_t kEngineBytes =
-    14 * r256((size_t)kPool * 16) + 8 * r256((size_t)kPool * 4) + r256(sizeof(WfCounters)) + r256(sizeof(WfJob));
+    7 * r256((size_t)kPool * 32) + 7 * r256((size_t)kPool * 4) + r256(sizeof(WfCounters)) + r256(sizeof(WfJob));
 constexpr size_t kSceneOff = 0;
 constexpr size_t kCieOff = kSceneOff + r256(sizeof(KScene));
 constexpr size_t kEngineOff = kCieOff + r256(sizeof(float) * PT_CIE_TABLE_SIZE);
