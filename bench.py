@@ -114,7 +114,7 @@ def parse_args():
     ap.add_argument("--fp-contract", type=int, default=0,
                     help="FMA contraction in run-time compiled kernels (1: faster, not bit-exact; 0: the shader's rounding)")
     ap.add_argument("--autotune", type=int, default=1,
-                    help="rounds of pt_autotune_wavefront on a 1024x1024x8spp dispatch before timing (0: off)")
+                    help="rounds of pt_autotune_wavefront on a 1024x1024x16spp dispatch before timing (0: off)")
     ap.add_argument("--workload", default="mandelbulb12",
                     choices=["mandelbulb12", "mandelbulb", "mandelbulb12_full", "batch64", "serve", "progressive"])
     ap.add_argument("--pass-spp", type=int, default=16, help="progressive: samples per pixel per pass")
@@ -222,19 +222,20 @@ def fp32_peak_tflops(peaks):
 # DRAM bytes per launch of each stage kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum) in the steady state of the workload's scene, keyed
 # by workload and path-pool size; the other knobs were the library defaults.
-# Each comes from one small-case ncu capture of one or two launches per
-# stage with the pool full (2^19 slots: profiles/wf_march_mandelbulb12_512x512_16spp.md;
-# 2^20 slots: profiles/stage_traffic_mandelbulb12_1024x1024_16spp_pool2e20.md):
+# Each comes from one small-case ncu capture of two launches per stage with
+# the pool full (profiles/wf_stages_mandelbulb12_1024x1024_16spp_pool2e22.md):
 # per launch a stage moves the state of the rays in its queues, which a full
 # pool of the same size bounds the same way at the full image size (the last
-# iterations of a dispatch, with the pool draining, move less).  Other
-# settings report null.
+# iterations of a dispatch, with the pool draining, move less).  At 2^22
+# slots gen had nothing to start in the captured launches: no figure.
+# Other settings report null.
 STAGE_TRAFFIC_BYTES = {
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 19): {"march": 85.21e6, "shade": 243.73e6, "gen": 119.84e6},
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): {"march": 450.46e6, "shade": 1085.83e6, "gen": 236.63e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): {"march": 298.29e6, "shade": 408.59e6, "gen": 36.42e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 21): {"march": 810.17e6, "shade": 1052.52e6, "gen": 78.50e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 22): {"march": 1183.62e6, "shade": 1670.13e6},
 }
 # The library's default wavefront knobs.
-DEFAULT_TUNING = {"pool_slots": 1 << 19, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
+DEFAULT_TUNING = {"pool_slots": 1 << 22, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
                   "march_inner": 6}
 
 
@@ -652,7 +653,7 @@ def serve_measure(opts, local, rank):
         push = sc.push_constants(spec.width, spec.height, 1, 1, 1, spec.pathLength)
         pool.append((kind, sc, spec, push))
     srv = Server(local, mode=native.PT_SERVE_BATCHED, spp_per_pass=8, hbm_budget=64 << 30,
-                 pool_slots=opts.pool or (1 << 19), iterations_per_poll=opts.iters_per_poll,
+                 pool_slots=opts.pool or (1 << 21), iterations_per_poll=opts.iters_per_poll,
                  passes_in_flight=opts.passes_in_flight, fp64_paths=opts.ref_paths == "fp64")
     t0 = time.perf_counter()
     for key, (kind, sc, spec, push) in enumerate(pool):
@@ -793,7 +794,7 @@ def run_progressive(args, rank, world):
     ubo = scene.pack_ubo(cie)
     base = replicas.frame_base(rank, 1, 1, args.spp)  # distinct samples per replica
 
-    b = Batch(local, pool_slots=args.pool or (1 << 19), max_passes=4096)
+    b = Batch(local, pool_slots=args.pool or (1 << 22), max_passes=4096)
     b.set_route(native.PT_BATCH_ROUTE_STAGED)
     # the scene's SDFs as text: shipped snippets select plug-ins, the full
     # form's fBm terrain is compiled at run time
@@ -942,7 +943,7 @@ def main():
     tuned, tune_secs = None, 0.0
     if args.autotune and args.engine == "wavefront":
         t0 = time.perf_counter()
-        tuned, _ = ctx.autotune(scene.push_constants(W, H, 8, 8, 8, args.depth), rounds=args.autotune)
+        tuned, _ = ctx.autotune(scene.push_constants(W, H, 16, 16, 16, args.depth), rounds=args.autotune)
         tune_secs = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2

@@ -243,8 +243,10 @@ int pt_render_fp64(pt_ctx* ctx, const pt_push* push, double* d_sums);
 #define PT_ENGINE_WAVEFRONT 1
 int pt_set_engine(pt_ctx* ctx, int engine);
 int pt_get_engine(pt_ctx* ctx);
-/* Path slots of the wavefront pool (default 2^19, whose state fits in L2; 252 B each, plus 16 B per
- * sample of the dispatch for the sample colours). */
+/* Path slots of the wavefront pool (default 2^22: a deeper pool keeps more
+ * rays to refill march lanes from; 252 B each, plus 16 B per sample of the
+ * dispatch for the sample colours; a dispatch uses at most its own sample
+ * count of slots). */
 int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots);
 /* Sphere-tracing iterations a ray may take per march launch before it is
  * suspended to the next wavefront iteration (default 64, 1..512). */

@@ -168,7 +168,7 @@ typedef struct pt_server_opts {
     int32_t mode;                /* PT_SERVE_* */
     int32_t spp_per_pass;        /* default 8 */
     uint64_t hbm_budget;         /* bytes for admitted jobs (default 64 GiB) */
-    uint32_t pool_slots;         /* staged-engine path slots (default 2^19) */
+    uint32_t pool_slots;         /* staged-engine path slots (default 2^21) */
     uint32_t max_passes;         /* passes in flight per engine (default 4096) */
     int32_t iterations_per_poll; /* engine iterations per pt_server_poll (default 4) */
     int32_t passes_in_flight;    /* per job (default 1) */

@@ -309,7 +309,7 @@ int pt_server_create(pt_server** out, int device, const pt_server_opts* opts) {
     pt_server_opts& o = s->opts;
     if (o.spp_per_pass <= 0) o.spp_per_pass = 8;
     if (o.hbm_budget == 0) o.hbm_budget = 64ull << 30;
-    if (o.pool_slots == 0) o.pool_slots = 1u << 19;
+    if (o.pool_slots == 0) o.pool_slots = 1u << 21;
     if (o.max_passes == 0) o.max_passes = 4096;
     if (o.iterations_per_poll <= 0) o.iterations_per_poll = 4;
     if (o.passes_in_flight <= 0) o.passes_in_flight = 1;

@@ -38,7 +38,7 @@ struct pt_ctx {
     int nplug = 0;
     KTrace trace{nullptr, nullptr, nullptr, 0};
     int engine = PT_ENGINE_WAVEFRONT;
-    uint32_t pool_cap = 1u << 19;  // wavefront path slots (the state of 2^19 paths fits in L2)
+    uint32_t pool_cap = 1u << 22;  // wavefront path slots: more rays to refill march lanes from (measured best)
     int march_budget = 64;
     bool stage_timing = false;
     int refill_min = 2;    // measured best on GB300 (mandelbulb 1024x1024)
@@ -469,7 +469,7 @@ int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavef
         *secs = b;
         return rc;
     };
-    static const uint32_t kPools[] = {1u << 18, 3u << 17, 1u << 19, 3u << 18, 1u << 20};
+    static const uint32_t kPools[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22};
     static const int kBudgets[] = {32, 64, 128};
     static const int kRefill[] = {1, 2, 4, 8};
     static const int kDrain[] = {0, 8, 16, 24};
@@ -481,7 +481,10 @@ int pt_autotune_wavefront(pt_ctx* ctx, const pt_push* push, int rounds, pt_wavef
     int rc = time_one(cur, &cur_t);
     for (int r = 0; r < rounds && rc == PT_OK; r++) {
         for (int knob = 0; knob < 6 && rc == PT_OK; knob++) {
-            const int nvals = knob == 0 ? 5 : knob == 1 ? 3 : knob == 2 ? 4 : knob == 3 ? 4 : knob == 4 ? 3 : 4;
+            constexpr int kCount[6] = {(int)(sizeof kPools / sizeof kPools[0]), (int)(sizeof kBudgets / sizeof kBudgets[0]),
+                                       (int)(sizeof kRefill / sizeof kRefill[0]), (int)(sizeof kDrain / sizeof kDrain[0]),
+                                       (int)(sizeof kBlocks / sizeof kBlocks[0]), (int)(sizeof kInner / sizeof kInner[0])};
+            const int nvals = kCount[knob];
             for (int i = 0; i < nvals && rc == PT_OK; i++) {
                 pt_wavefront_tuning c = cur;
                 switch (knob) {

@@ -438,7 +438,7 @@ class Server:
     """pt_server: progressive render serving with error targets (libpt_host)."""
 
     def __init__(self, device: int = 0, mode: int = native.PT_SERVE_BATCHED, spp_per_pass: int = 8,
-                 hbm_budget: int = 64 << 30, pool_slots: int = 1 << 19, max_passes: int = 4096,
+                 hbm_budget: int = 64 << 30, pool_slots: int = 1 << 21, max_passes: int = 4096,
                  iterations_per_poll: int = 4, passes_in_flight: int = 1, keep_images: bool = False,
                  fp64_paths: bool = False):
         self._lib = native.host()

@@ -2,9 +2,9 @@
 serve them.
 
 The small-image parity tests (test_gpu_parity.py) cannot show what only
-appears at full size: a path pool recycled hundreds of times, marches
+appears at full size: a path pool recycled many times, marches
 suspended and resumed over many iterations, queue indices wrapping around
-the 2^19-slot pool, grids of thousands of blocks.  Here each workload runs
+the path pool, grids of thousands of blocks.  Here each workload runs
 at its stated size through the same entry point and settings as bench.py,
 and the oracle (oracle/pt_oracle.c) renders a stratified set of rows of the
 same frame (all of it where that is cheap) for comparison:
@@ -145,7 +145,7 @@ def test_cornell_box_256_16spp_depth8_whole_frame(rt, engine):
 @pytest.mark.parametrize("engine", ENGINES)
 def test_mandelbulb12_1024_64spp_depth6_rows(rt, engine):
     """The bench's workload and dispatch (one dispatch of 64 spp; the
-    wavefront engine with its default 2^19-slot pool and knobs)."""
+    wavefront engine with its default pool and knobs)."""
     from oracle import compare
 
     W, H, spf, depth = 1024, 1024, 64, 6

@@ -53,7 +53,7 @@ def test_dispatch_drain_limit(env):
         ctx.set_engine(native.PT_ENGINE_WAVEFRONT)
         ctx.bind(scene, cie)
         ctx.resize_accum(W, H)
-        ctx.set_drain_limit(2)  # 1 M samples through a 2^19-slot pool need far more iterations
+        ctx.set_drain_limit(2)  # 1 M samples of depth-6 paths need far more iterations
         with pytest.raises(renderer.PathTracerError) as e:
             ctx.dispatch(push)
         assert e.value.code == native.PT_ERR_KERNEL
