@@ -430,8 +430,12 @@ __global__ void wf_persist_setup(const __grid_constant__ WfArgs A, uint64_t budg
     C.iterations += 1;
 }
 
-template <int FEAT>
-__global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_constant__ WfArgs A) {
+// The persistent path loop.  ONE: every sample of the launch belongs to one
+// pass, whose scene S1 is the launch's parameter (the constant bank, as
+// for the megakernel); otherwise each lane reads its pass's scene through
+// the pass's pointer.
+template <int FEAT, bool ONE>
+PT_DI void persist_paths(const WfArgs& A, const KScene* S1) {
     WfCounters& C = *A.counters;
     const uint64_t end = C.pk_end;
     const uint32_t job_lo = C.job_lo, job_hi = C.job_hi;
@@ -485,7 +489,7 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
                 const float uvx = (2.0f * (float)xx - (float)W) / (float)H;
                 const float uvy = (2.0f * (float)yy - (float)H) / (float)H;
                 const CamInfo cam = J.cam;
-                start_sample(ps, *J.scene, pc, cam, xx, yy, uvx, uvy, (int)k);
+                start_sample(ps, ONE ? *S1 : *J.scene, pc, cam, xx, yy, uvx, uvy, (int)k);
                 shadow = false;
                 active = true;
             }
@@ -497,7 +501,7 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
         bool finished = false;
         if (active) {
             const WfJob& J = A.jobs[job];
-            const KScene& S = *J.scene;
+            const KScene& S = ONE ? *S1 : *J.scene;
             const int depth = J.pc.pathLength;
             Hit h;
             h.hitdist = PT_MAXDIST;
@@ -519,6 +523,17 @@ __global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_const
         }
         count_finished(A.jobs, job, finished);
     }
+}
+
+template <int FEAT>
+__global__ void __launch_bounds__(kPersistThreads) wf_persist(const __grid_constant__ WfArgs A) {
+    persist_paths<FEAT, false>(A, nullptr);
+}
+
+template <int FEAT>
+__global__ void __launch_bounds__(kPersistThreads)
+    wf_persist_one(const __grid_constant__ WfArgs A, const __grid_constant__ KScene S1) {
+    persist_paths<FEAT, true>(A, &S1);
 }
 
 __global__ void wf_book(const __grid_constant__ WfArgs A) {
@@ -645,50 +660,51 @@ cudaError_t PTK_WF(ptk_wavefront_launch_iteration)(const WfArgs* a, bool trace, 
     return cudaGetLastError();
 }
 
-int PTK_WF(ptk_persist_blocks_per_sm)(int variant);
+namespace {
+
+// Blocks of a persistent kernel that fit on one SM at once, cached.
+template <int FEAT, bool ONE>
+int persist_blocks() {
+    static int cache = 0;
+    if (cache) return cache;
+    int n = 0;
+    const void* k = ONE ? reinterpret_cast<const void*>(wf_persist_one<FEAT>)
+                        : reinterpret_cast<const void*>(wf_persist<FEAT>);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kPersistThreads, 0) != cudaSuccess || n < 1) n = 1;
+    cache = n;
+    return n;
+}
+
+template <int FEAT>
+void launch_persist(const WfArgs* a, int sms, const KScene* one_scene, cudaStream_t stream) {
+    if (one_scene) {
+        wf_persist_one<FEAT><<<sms * persist_blocks<FEAT, true>(), kPersistThreads, 0, stream>>>(*a, *one_scene);
+    } else {
+        wf_persist<FEAT><<<sms * persist_blocks<FEAT, false>(), kPersistThreads, 0, stream>>>(*a);
+    }
+}
+
+}  // namespace
 
 cudaError_t PTK_WF(ptk_persist_launch)(const WfArgs* a, int variant, int sms, uint64_t budget,
-                                       cudaStream_t stream) {
+                                       const KScene* one_scene, cudaStream_t stream) {
     wf_persist_setup<<<1, 1, 0, stream>>>(*a, budget);
     switch (variant) {
-        case 0: wf_persist<0><<<sms * PTK_WF(ptk_persist_blocks_per_sm)(0), kPersistThreads, 0, stream>>>(*a); break;
-        case PT_FEAT_BOX:
-            wf_persist<PT_FEAT_BOX>
-                <<<sms * PTK_WF(ptk_persist_blocks_per_sm)(PT_FEAT_BOX), kPersistThreads, 0, stream>>>(*a);
-            break;
-        case PT_FEAT_ANALYTIC:
-            wf_persist<PT_FEAT_ANALYTIC>
-                <<<sms * PTK_WF(ptk_persist_blocks_per_sm)(PT_FEAT_ANALYTIC), kPersistThreads, 0, stream>>>(*a);
-            break;
-        default:
-            wf_persist<PT_FEAT_ALL>
-                <<<sms * PTK_WF(ptk_persist_blocks_per_sm)(PT_FEAT_ALL), kPersistThreads, 0, stream>>>(*a);
-            break;
+        case 0: launch_persist<0>(a, sms, one_scene, stream); break;
+        case PT_FEAT_BOX: launch_persist<PT_FEAT_BOX>(a, sms, one_scene, stream); break;
+        case PT_FEAT_ANALYTIC: launch_persist<PT_FEAT_ANALYTIC>(a, sms, one_scene, stream); break;
+        default: launch_persist<PT_FEAT_ALL>(a, sms, one_scene, stream); break;
     }
     return cudaGetLastError();
 }
 
 int PTK_WF(ptk_persist_blocks_per_sm)(int variant) {
-    static int cache[16] = {0};
-    const int v = variant & 15;
-    if (cache[v]) return cache[v];
-    int n = 0;
-    cudaError_t e;
-    switch (v) {
-        case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<0>, kPersistThreads, 0); break;
-        case PT_FEAT_BOX:
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<PT_FEAT_BOX>, kPersistThreads, 0);
-            break;
-        case PT_FEAT_ANALYTIC:
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<PT_FEAT_ANALYTIC>, kPersistThreads, 0);
-            break;
-        default:
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wf_persist<PT_FEAT_ALL>, kPersistThreads, 0);
-            break;
+    switch (variant & 15) {
+        case 0: return persist_blocks<0, false>();
+        case PT_FEAT_BOX: return persist_blocks<PT_FEAT_BOX, false>();
+        case PT_FEAT_ANALYTIC: return persist_blocks<PT_FEAT_ANALYTIC, false>();
+        default: return persist_blocks<PT_FEAT_ALL, false>();
     }
-    if (e != cudaSuccess || n < 1) n = 1;
-    cache[v] = n;
-    return n;
 }
 
 cudaError_t PTK_WF(ptk_wavefront_launch_resolve)(const WfArgs* a, uint32_t job, const pt_push* pc, float4* accum,

@@ -44,6 +44,7 @@ struct WfJob {
     uint32_t count;       // W*H*spf
     uint32_t finished;    // samples finished (atomic)
     int32_t variant;      // primitive classes of the scene (PT_FEAT_*), for the persistent kernel
+    const KScene* host_scene;  // host copy of *scene (persistent single-pass launches; null: none)
     CamInfo cam;          // camera derived on the device (wf_job_setup)
     pt_push pc;
 };
@@ -128,8 +129,11 @@ enum { PT_STAGE_ISECT = 0, PT_STAGE_MARCH, PT_STAGE_SHADE, PT_STAGE_GEN, PT_STAG
 // Persistent mode: one launch of the persistent path kernel over the next
 // `budget` samples of the job ring, compiled for primitive classes `variant`
 // (PT_FEAT_*: 0, BOX, ANALYTIC or ALL), with every block resident at once
-// on `sms` multiprocessors.
-cudaError_t ptk_persist_launch(const WfArgs* a, int variant, int sms, uint64_t budget, cudaStream_t stream);
+// on `sms` multiprocessors.  one_scene (host copy, or null): every sample of
+// the launch belongs to one pass of this scene, which then travels as the
+// launch's parameter and is read from the constant bank.
+cudaError_t ptk_persist_launch(const WfArgs* a, int variant, int sms, uint64_t budget, const KScene* one_scene,
+                               cudaStream_t stream);
 // Blocks of the persistent kernel variant that fit on one SM at once.
 int ptk_persist_blocks_per_sm(int variant);
 constexpr int kPersistThreads = 128;
@@ -144,7 +148,7 @@ struct WfKernelSet {
     cudaError_t (*job_add)(const WfArgs*, const WfJob*, uint32_t, uint32_t, cudaStream_t);
     cudaError_t (*iteration)(const WfArgs*, bool, int, cudaStream_t, cudaEvent_t*, const void*);
     const void* (*march_warp_normals)();
-    cudaError_t (*persist)(const WfArgs*, int, int, uint64_t, cudaStream_t);
+    cudaError_t (*persist)(const WfArgs*, int, int, uint64_t, const KScene*, cudaStream_t);
     int (*persist_blocks_per_sm)(int);
     cudaError_t (*resolve)(const WfArgs*, uint32_t, const pt_push*, float4*, const float4*, cudaStream_t);
 };

@@ -25,6 +25,7 @@
 #include <cmath>
 #include <deque>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -39,6 +40,8 @@ namespace {
 
 struct BatchScene {
     KScene* d_scene = nullptr;
+    std::shared_ptr<KScene> h_scene;  // host copy (rotation matrices and extensions included), for the
+                                      // persistent kernel's single-pass launches
     float* d_cie = nullptr;
     bool live = false;
     bool has_sdf = false;
@@ -489,7 +492,10 @@ int add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int 
         b->kernel_launches += 1;
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);  // the copies read S and ubo
-    delete S;
+    // keep S as the host copy, with the rotation matrices the device derived
+    if (e == cudaSuccess && S->meta.total_objects > 0)
+        e = cudaMemcpy(&S->rot[0][0], &bs.d_scene->rot[0][0], sizeof(S->rot), cudaMemcpyDeviceToHost);
+    bs.h_scene.reset(S);
     if (e != cudaSuccess) {
         if (bs.d_scene) cudaFree(bs.d_scene);
         if (bs.d_cie) cudaFree(bs.d_cie);
@@ -621,6 +627,7 @@ int pt_batch_add_pass(pt_batch* b, int scene_id, int target_id, const pt_push* p
     j.colors = p.d_colors;
     j.pc = *push;
     j.variant = sc.variant;
+    j.host_scene = e == kPersistent ? sc.h_scene.get() : nullptr;
     const cudaError_t r = E.add_pass(j, &p.eidx);
     if (r != cudaSuccess) {
         cudaFreeAsync(p.d_colors, b->stream);
@@ -988,6 +995,7 @@ int pt_batch_set_scene_ext(pt_batch* b, int scene_id, const pt_scene_ext* ext) {
         if (b->engine_live[e]) PT_B_TRY(b, cudaStreamSynchronize(b->engine[e].stream));
     PT_B_TRY(b, cudaMemcpyAsync(&s.d_scene->ext, &x, sizeof x, cudaMemcpyHostToDevice, b->stream));
     PT_B_TRY(b, cudaStreamSynchronize(b->stream));  // the copy reads the stack
+    if (s.h_scene) s.h_scene->ext = x;
     return PT_OK;
 }
 
@@ -1002,6 +1010,7 @@ int pt_batch_release_scene(pt_batch* b, int scene_id) {
     cudaFree(s.d_cie);
     s.d_scene = nullptr;
     s.d_cie = nullptr;
+    s.h_scene.reset();
     s.live = false;
     return PT_OK;
 }

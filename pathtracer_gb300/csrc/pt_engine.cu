@@ -277,9 +277,27 @@ cudaError_t WfEngine::run(int n, bool trace) {
         int variant = 0;
         for (uint32_t j = lo; j < njobs; j++) variant = pt_variant_union(variant, jobs[j % max_jobs].variant);
         for (int i = 0; i < n && persist_issued < total; i++) {
-            EN_TRY(kernels->persist(&args, variant, sms, persist_budget, stream));
+            // A launch that stays within one pass (the rest of a large pass,
+            // or the next budget of it) takes that pass's scene as its
+            // parameter, read from the constant bank like the megakernel's;
+            // a launch spanning passes reads each lane's scene by pointer.
+            uint64_t budget = total - persist_issued < persist_budget ? total - persist_issued : persist_budget;
+            const KScene* one = nullptr;
+            int v = variant;
+            for (uint32_t j = lo; j < njobs; j++) {
+                const WfJob& J = jobs[j % max_jobs];
+                if (persist_issued < J.first || persist_issued >= J.first + J.count) continue;
+                const uint64_t left = J.first + J.count - persist_issued;
+                if (J.host_scene && (left >= budget || left >= kPersistOnePassMin)) {
+                    budget = left < budget ? left : budget;
+                    one = J.host_scene;
+                    v = J.variant;
+                }
+                break;
+            }
+            EN_TRY(kernels->persist(&args, v, sms, budget, one, stream));
             kernel_launches += 2;  // setup + persistent kernel
-            persist_issued = (total - persist_issued > persist_budget) ? persist_issued + persist_budget : total;
+            persist_issued += budget;
         }
         return cudaSuccess;
     }
@@ -329,9 +347,10 @@ cudaError_t WfEngine::resolve(uint32_t j, cudaStream_t on) {
 cudaError_t WfEngine::drain(bool trace, uint64_t max_iterations) {
     if (persistent) {
         // Every launch finishes the samples it covers.
-        const uint64_t launches = (total - persist_issued + persist_budget - 1) / persist_budget;
-        if (launches > max_iterations) return cudaErrorTimeout;
-        EN_TRY(run((int)launches, false));
+        for (uint64_t launches = 0; persist_issued < total; launches++) {
+            if (launches >= max_iterations) return cudaErrorTimeout;
+            EN_TRY(run(1, false));
+        }
         return read_counters(host_counters);
     }
     uint64_t iter = 0;

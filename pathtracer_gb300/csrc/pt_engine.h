@@ -98,6 +98,9 @@ struct WfEngine {
     bool persistent = false;
     int sms = 0;
     uint64_t persist_budget = 1ull << 23;
+    // A pass's remainder at least this large gets a launch of its own (with
+    // its scene in the constant bank) instead of sharing one with the next.
+    static constexpr uint64_t kPersistOnePassMin = 1ull << 20;
     uint64_t persist_issued = 0;  // samples covered by launches so far
     // Stage timing (off by default): every iteration is launched without the
     // graph, bracketed by events; stage_ms accumulates device milliseconds.
