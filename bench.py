@@ -106,6 +106,8 @@ def parse_args():
     ap.add_argument("--engine", default="wavefront", choices=["wavefront", "megakernel"])
     ap.add_argument("--compare-engines", type=int, default=1, help="also time the other engine (1 step)")
     ap.add_argument("--pool", type=int, default=0, help="wavefront path slots (0: library default)")
+    ap.add_argument("--wf-engines", type=int, default=0,
+                    help="wavefront engines a large dispatch is split between (1..4; 0: library default)")
     ap.add_argument("--budget", type=int, default=0, help="wavefront march steps per launch (0: default)")
     ap.add_argument("--refill", type=int, default=0, help="wavefront march refill threshold (0: default)")
     ap.add_argument("--drain", type=int, default=-1, help="wavefront march drain lanes (-1: default)")
@@ -289,7 +291,8 @@ def stage_roofline(ctx, run_step, samples, workload, peaks, peak_kind, tkey=None
             "note": f"peak: nominal FP32 FMA rate (SMs x 128 x 2) at the measured max SM clock ({peak_kind} peaks "
                     "hold no FP32 figure); achieved: hand-counted FP32 operations of the march stage's events "
                     "(pathtracer_gb300/workmodel.py, counts per sample from tests/golden/work_*.json) over the "
-                    "summed device time of its launches in one step timed with per-stage CUDA events; traffic: "
+                    "summed device time of its launches in one step timed with per-stage CUDA events (one engine, "
+                    "its kernels one at a time); traffic: "
                     "DRAM bytes per launch from one small-case ncu capture of this scene with the pool full (profiles/)"}
     return roof, stages, ops
 
@@ -928,6 +931,8 @@ def main():
     ctx.set_engine(engine_id)
     if args.pool:
         ctx.set_wavefront_pool(args.pool)
+    if args.wf_engines:
+        ctx.set_wavefront_engines(args.wf_engines)
     if args.fp_contract:
         ctx.set_fp_contract(True)
     if args.budget:
@@ -953,6 +958,8 @@ def main():
 
     base = replicas.frame_base(rank, args.warmup + args.steps, ndisp, spf)
 
+    launches = [0]  # the library's count of the kernels each dispatch launched
+
     def one_step(step_idx):
         frame = base + step_idx * ndisp * spf
         cur = 0
@@ -960,6 +967,7 @@ def main():
             frame += spf
             cur += spf
             ctx.dispatch(scene.push_constants(W, H, frame, cur, spf, args.depth))
+            launches[0] += ctx.last_kernel_launches()
 
     for i in range(args.warmup):
         one_step(i)
@@ -971,6 +979,7 @@ def main():
     torch.cuda.synchronize()
 
     times = []
+    launches[0] = 0
     with ClockSampler(local) as clk:
         t_wall0 = time.perf_counter()
         for i in range(args.steps):
@@ -985,6 +994,7 @@ def main():
         ctx.wait()
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall0
+    timed_launches = launches[0]
     ms = [a.elapsed_time(b) for a, b in times]
     ms_step = sum(ms) / len(ms)
     iters = ctx.last_iterations()
@@ -1047,15 +1057,17 @@ def main():
                    "samples_per_dispatch": spf, "dispatches_per_step": ndisp,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
                    "wavefront_tuning": ctx.tuning() if args.engine == "wavefront" else None,
+                   "wavefront_engines": ctx.wavefront_engines() if args.engine == "wavefront" else None,
                    "autotuned": bool(tuned), "autotune_s": tune_secs,
                    "fp_contract": bool(args.fp_contract)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "engine": args.engine,
         "engines": {args.engine: {"value": value / world, "ms_per_step": ms_step}, **other},
         "wavefront_iterations_per_dispatch": iters if args.engine == "wavefront" else None,
-        # per wavefront dispatch: init, job_add, 4 kernels per iteration (graph
-        # replays counted per kernel), resolve
-        "gpu_launches": args.steps * ndisp * ((4 * iters + 3) if args.engine == "wavefront" else 1),
+        # the library's count per dispatch (pt_last_kernel_launches): per
+        # wavefront engine init, job_add and 4 kernels per iteration (graph
+        # replays counted per kernel), then the resolve
+        "gpu_launches": timed_launches,
         "wall_s_timed_region": t_wall,
         "roofline": roofline,
         "stages": stages,

@@ -248,11 +248,27 @@ int pt_get_engine(pt_ctx* ctx);
  * dispatch for the sample colours; a dispatch uses at most its own sample
  * count of slots). */
 int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots);
+/* Wavefront engines a large dispatch is split between (1..4; default 2).
+ * A dispatch of at least two pools' worth of samples per engine is rendered
+ * by up to that many engines with a pool each, on streams of their own (the
+ * context's stream and streams the context owns, forked from and joined
+ * back to it), each taking an equal share of the dispatch's samples in
+ * sample order: one engine's kernels fill the SMs that the others' kernel
+ * tails and host round trips leave idle.  The same bits as one engine
+ * (every sample's colour lands in the dispatch's colour buffer and is
+ * summed per pixel in sample order).  Each engine holds a pool; one engine
+ * runs when a trace or stage timing is on. */
+int pt_set_wavefront_engines(pt_ctx* ctx, int engines);
+int pt_get_wavefront_engines(pt_ctx* ctx);
 /* Sphere-tracing iterations a ray may take per march launch before it is
  * suspended to the next wavefront iteration (default 64, 1..512). */
 int pt_set_march_budget(pt_ctx* ctx, int steps);
-/* Wavefront iterations the last dispatch needed (diagnostics). */
+/* Wavefront iterations the last dispatch needed (diagnostics; split between
+ * two engines: the larger engine's count). */
 uint32_t pt_last_iterations(pt_ctx* ctx);
+/* Kernels the last pt_dispatch launched (diagnostics; a wavefront dispatch
+ * counts each iteration's stage kernels, pass setup and the resolve). */
+uint64_t pt_last_kernel_launches(pt_ctx* ctx);
 
 /* Replaces vkWaitForFences (src/pathtracer.cpp:3846): waits at most
  * timeout_ns and returns PT_ERR_TIMEOUT instead of blocking forever. */
@@ -373,7 +389,7 @@ int pt_dispatch_noalloc(const pt_ubo* ubo, const pt_sdf_plugin* plugins, int npl
  * defaults suit the SDF scenes measured on GB300; pt_autotune_wavefront
  * picks them for a given scene and dispatch shape. */
 typedef struct pt_wavefront_tuning {
-    uint32_t pool_slots;   /* path slots (1024..2^28; default 2^19) */
+    uint32_t pool_slots;   /* path slots (1024..2^28; default 2^22) */
     int32_t march_budget;  /* SDF steps per ray per march launch (1..512; default 64) */
     int32_t refill_min;    /* idle lanes a march warp gathers before refilling them together (1..32) */
     int32_t drain_lanes;   /* a march warp left with fewer rays after its queue drained suspends them (0..32) */

@@ -185,7 +185,7 @@ __global__ void PT_GEN_BOUNDS wf_gen(const __grid_constant__ WfArgs A) {
             const uint64_t s = first + i;
             const uint32_t job = find_job(A.jobs, A.job_cap, job_lo, job_hi, s);
             const WfJob& J = A.jobs[job];
-            const uint32_t local = (uint32_t)(s - J.first);
+            const uint32_t local = J.local_base + (uint32_t)(s - J.first);
             const pt_push& pc = J.pc;
             const int W = pc.resolution[0], H = pc.resolution[1];
             const uint32_t npix = (uint32_t)W * (uint32_t)H;
@@ -287,7 +287,8 @@ template <bool TRACE>
 PT_DI void finish_shade(const WfArgs& A, const WfJob& J, const PathState& ps, StepResult r, uint32_t sample,
                         bool& freed) {
     const pt_push& pc = J.pc;
-    const bool in_pass = pt_check(A, sample, J.count, PT_CHECK_SAMPLE);  // trace and colour indices
+    // trace and colour indices
+    const bool in_pass = pt_check(A, sample - J.local_base, J.count, PT_CHECK_SAMPLE);
     if (TRACE && r != STEP_SHADOW && A.trace.events && in_pass) {
         const size_t p = trace_index(pc, sample);
         const int b = ps.bounce - 1;
@@ -480,7 +481,7 @@ PT_DI void persist_paths(const WfArgs& A, const KScene* S1) {
                 const uint64_t s = cbase + rank;
                 job = (s < cjob_end) ? cjob : find_job(A.jobs, A.job_cap, job_lo, job_hi, s);
                 const WfJob& J = A.jobs[job];
-                local = (uint32_t)(s - J.first);
+                local = J.local_base + (uint32_t)(s - J.first);
                 const pt_push& pc = J.pc;
                 const int W = pc.resolution[0], H = pc.resolution[1];
                 const uint32_t npix = (uint32_t)W * (uint32_t)H;
@@ -515,7 +516,7 @@ PT_DI void persist_paths(const WfArgs& A, const KScene* S1) {
             shadow = (r == STEP_SHADOW);
             if (r == STEP_TERMINATED) {
                 const float3 col = sample_color(ps, S, J.cie);
-                if (pt_check(A, local, J.count, PT_CHECK_SAMPLE))
+                if (pt_check(A, local - J.local_base, J.count, PT_CHECK_SAMPLE))
                     J.colors[local] = make_float4(col.x, col.y, col.z, 0.0f);
                 finished = true;
                 active = false;

@@ -44,6 +44,7 @@ struct WfJob {
     uint32_t count;       // W*H*spf
     uint32_t finished;    // samples finished (atomic)
     int32_t variant;      // primitive classes of the scene (PT_FEAT_*), for the persistent kernel
+    uint32_t local_base;  // pass index of this entry's first sample (a pass split between engines; else 0)
     const KScene* host_scene;  // host copy of *scene (persistent single-pass launches; null: none)
     CamInfo cam;          // camera derived on the device (wf_job_setup)
     pt_push pc;

@@ -47,11 +47,21 @@ struct pt_ctx {
     int blocks_per_sm = 4;
     KScene* d_scene = nullptr;     // device copy for the wavefront kernels
     WfEngine* wf = nullptr;        // wavefront driver (created on first use, grows with the dispatch)
+    // More engines, on streams of their own, take equal shares of a large
+    // dispatch's samples (pt_set_wavefront_engines); `fork` orders them after
+    // the context's stream, `join` the resolve after them.
+    static constexpr int kMaxEngines = 4;
+    int wf_engines = 2;
+    WfEngine* wf_more[kMaxEngines - 1] = {};
+    cudaStream_t stream_more[kMaxEngines - 1] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kMaxEngines - 1] = {};
     float4* d_colors = nullptr;    // per-sample colours of the current dispatch
     uint8_t* d_rgb = nullptr;      // pt_read_rgb8 staging (W*H*3 bytes)
     size_t rgb_bytes = 0;
     size_t colors_bytes = 0;
     uint32_t last_iterations = 0;
+    uint64_t last_launches = 0;    // kernels the last pt_dispatch launched
     uint64_t drain_limit = 0;      // iteration cap of the wavefront drain (0: the bound computed per dispatch)
     bool fp_contract = false;      // run-time compiled kernels with FMA contraction (pt_set_fp_contract)
     bool device_checks = false;    // the wavefront engine's checked kernel build (pt_set_device_checks)
@@ -147,10 +157,22 @@ int pt_destroy(pt_ctx* ctx) {
     if (ctx->d_cie) cudaFree(ctx->d_cie);
     if (ctx->d_rot) cudaFree(ctx->d_rot);
     if (ctx->d_scene) cudaFree(ctx->d_scene);
+    for (cudaStream_t s : ctx->stream_more)
+        if (s) cudaStreamSynchronize(s);
     if (ctx->wf) {
         ctx->wf->destroy();
         delete ctx->wf;
     }
+    for (WfEngine* e : ctx->wf_more)
+        if (e) {
+            e->destroy();
+            delete e;
+        }
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    for (cudaEvent_t ev : ctx->join)
+        if (ev) cudaEventDestroy(ev);
+    for (cudaStream_t s : ctx->stream_more)
+        if (s) cudaStreamDestroy(s);
     if (ctx->d_colors) cudaFree(ctx->d_colors);
     if (ctx->d_rgb) cudaFree(ctx->d_rgb);
     for (auto& cache : ctx->jit)
@@ -332,9 +354,11 @@ int pt_dispatch(pt_ctx* ctx, const pt_push* push) {
         const bool staged = ctx->engine == PT_ENGINE_WAVEFRONT && push->pathLength > 0;
         const int rc = ensure_jit(ctx, staged ? kJitMarch : kJitMegakernel);
         if (rc != PT_OK) return rc;
+        ctx->last_launches = 1;
         if (!staged) return dispatch_jit(ctx, trace);
     }
     if (ctx->engine == PT_ENGINE_WAVEFRONT && push->pathLength > 0) return dispatch_wavefront(ctx, push);
+    ctx->last_launches = 1;
     PT_CUDA_TRY(ctx, ptk_launch_megakernel(&P, trace, ctx->stream));
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
@@ -387,6 +411,18 @@ int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots) {
 
 uint32_t pt_last_iterations(pt_ctx* ctx) { return ctx ? ctx->last_iterations : 0; }
 
+uint64_t pt_last_kernel_launches(pt_ctx* ctx) { return ctx ? ctx->last_launches : 0; }
+
+int pt_set_wavefront_engines(pt_ctx* ctx, int engines) {
+    if (!ctx) return PT_ERR_INVALID;
+    if (engines < 1 || engines > pt_ctx::kMaxEngines)
+        return fail(ctx, PT_ERR_INVALID, "pt_set_wavefront_engines: 1..4 engines");
+    ctx->wf_engines = engines;
+    return PT_OK;
+}
+
+int pt_get_wavefront_engines(pt_ctx* ctx) { return ctx ? ctx->wf_engines : -1; }
+
 int pt_set_march_budget(pt_ctx* ctx, int steps) {
     if (!ctx) return PT_ERR_INVALID;
     if (steps < 1 || steps > 512) return fail(ctx, PT_ERR_INVALID, "pt_set_march_budget: 1..512 steps");
@@ -397,7 +433,7 @@ int pt_set_march_budget(pt_ctx* ctx, int steps) {
 int pt_set_stage_timing(pt_ctx* ctx, int on) {
     if (!ctx) return PT_ERR_INVALID;
     ctx->stage_timing = on != 0;
-    if (ctx->wf) PT_CUDA_TRY(ctx, ctx->wf->set_stage_timing(ctx->stage_timing));
+    if (ctx->wf) PT_CUDA_TRY(ctx, ctx->wf->set_stage_timing(ctx->stage_timing));  // a second engine runs untimed
     return PT_OK;
 }
 
@@ -614,30 +650,59 @@ const char* pt_last_error(pt_ctx* ctx) {
 }  // extern "C"
 
 // The wavefront dispatch: one pass of one job on the context's engine,
-// drained, then resolved into the accumulator.
+// drained, then resolved into the accumulator.  A dispatch of at least two
+// pools' worth of samples per engine is split into equal shares (in sample
+// order) between up to wf_engines engines on streams of their own.
 static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     const uint64_t total64 = (uint64_t)push->resolution[0] * (uint64_t)push->resolution[1] *
                              (uint64_t)push->samplesPerFrame;
     if (total64 >= (1ull << 32)) return fail(ctx, PT_ERR_INVALID, "pt_dispatch: more than 2^32 samples in one dispatch");
     const uint32_t total = (uint32_t)total64;
-    uint32_t pool = total < ctx->pool_cap ? total : ctx->pool_cap;
-    if (pool < 1024u) pool = 1024u;
-    if (!ctx->wf || ctx->wf->pool < pool || ctx->wf->pool > ctx->pool_cap) {
-        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        if (!ctx->wf) ctx->wf = new (std::nothrow) WfEngine();
-        if (!ctx->wf) return fail(ctx, PT_ERR_OOM, "pt_dispatch: out of host memory");
-        PT_CUDA_TRY(ctx, ctx->wf->create(ctx->device, ctx->stream, pool, 4096, ctx->march_budget));
+    const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
+    int n = 1;
+    if (!trace && !ctx->stage_timing) {
+        const uint64_t fit = total64 / (2ull * ctx->pool_cap);
+        n = fit < (uint64_t)ctx->wf_engines ? (int)fit : ctx->wf_engines;
+        if (n < 1) n = 1;
     }
+    constexpr int kMax = pt_ctx::kMaxEngines;
+    uint32_t base[kMax + 1];
+    for (int e = 0; e <= n; e++) base[e] = (uint32_t)(total64 * (uint64_t)e / (uint64_t)n);
+    WfEngine** slot[kMax] = {&ctx->wf, &ctx->wf_more[0], &ctx->wf_more[1], &ctx->wf_more[2]};
+    cudaStream_t streams[kMax] = {ctx->stream, nullptr, nullptr, nullptr};
+    for (int e = 1; e < n; e++) {
+        if (!ctx->stream_more[e - 1]) {
+            PT_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->stream_more[e - 1], cudaStreamNonBlocking));
+            PT_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->join[e - 1], cudaEventDisableTiming));
+        }
+        streams[e] = ctx->stream_more[e - 1];
+    }
+    if (n > 1 && !ctx->fork) PT_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+    uint64_t launches0 = 0;  // engines count their launches, creation's init included
+    for (int e = 0; e < kMax; e++)
+        if (*slot[e]) launches0 += (*slot[e])->kernel_launches;
     // Run-time compiled SDF snippets: their march kernel (the other stages
     // evaluate no SDF); a mandelbulb: the built-in kernel with the warp-wide
     // normal pass.
     bool bulb = false;
     for (int i = 0; i < ctx->nplug; i++) bulb = bulb || ctx->plug[i].kind == PT_SDF_MANDELBULB;
-    ctx->wf->set_checks(ctx->device_checks);
-    ctx->wf->set_march_kernel(!ctx->custom.empty()
-                                  ? reinterpret_cast<const void*>(
-                                        ctx->jit[kJitMarch][(size_t)ctx->jit_cur[kJitMarch]].kernel[0])
-                                  : (bulb ? ctx->wf->kernels->march_warp_normals() : nullptr));
+    for (int e = 0; e < n; e++) {
+        const uint32_t share = base[e + 1] - base[e];
+        uint32_t pool = share < ctx->pool_cap ? share : ctx->pool_cap;
+        if (pool < 1024u) pool = 1024u;
+        WfEngine*& W = *slot[e];
+        if (!W || W->pool < pool || W->pool > ctx->pool_cap) {
+            PT_CUDA_TRY(ctx, cudaStreamSynchronize(streams[e]));
+            if (!W) W = new (std::nothrow) WfEngine();
+            if (!W) return fail(ctx, PT_ERR_OOM, "pt_dispatch: out of host memory");
+            PT_CUDA_TRY(ctx, W->create(ctx->device, streams[e], pool, 4096, ctx->march_budget));
+        }
+        W->set_checks(ctx->device_checks);
+        W->set_march_kernel(!ctx->custom.empty()
+                                ? reinterpret_cast<const void*>(
+                                      ctx->jit[kJitMarch][(size_t)ctx->jit_cur[kJitMarch]].kernel[0])
+                                : (bulb ? W->kernels->march_warp_normals() : nullptr));
+    }
     const size_t cbytes = (size_t)total * sizeof(float4);
     if (cbytes > ctx->colors_bytes) {
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -647,14 +712,9 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
         PT_CUDA_TRY(ctx, cudaMalloc(&ctx->d_colors, cbytes));
         ctx->colors_bytes = cbytes;
     }
-    WfEngine& E = *ctx->wf;
-    E.set_stream(ctx->stream);
-    E.set_march_budget(ctx->march_budget);
-    E.set_tuning(ctx->refill_min, ctx->drain_lanes, ctx->blocks_per_sm, ctx->march_inner);
-    if (E.stage_timing != ctx->stage_timing) PT_CUDA_TRY(ctx, E.set_stage_timing(ctx->stage_timing));
-    E.args.trace = ctx->trace;
-    const bool trace = ctx->trace.events || ctx->trace.nevents || ctx->trace.colors;
-    PT_CUDA_TRY(ctx, E.reset());
+    // the other engines' streams start after everything queued on the context's
+    if (n > 1) PT_CUDA_TRY(ctx, cudaEventRecord(ctx->fork, ctx->stream));
+    for (int e = 1; e < n; e++) PT_CUDA_TRY(ctx, cudaStreamWaitEvent(streams[e], ctx->fork, 0));
     WfJob j;
     std::memset(&j, 0, sizeof j);
     j.scene = ctx->d_scene;
@@ -663,23 +723,50 @@ static int dispatch_wavefront(pt_ctx* ctx, const pt_push* push) {
     j.colors = ctx->d_colors;
     j.pc = *push;
     j.variant = PT_FEAT_ALL;
-    uint32_t idx = 0;
-    PT_CUDA_TRY(ctx, E.add_pass(j, &idx));
+    uint32_t idx0 = 0;
+    WfEngine* engines[kMax];
+    for (int e = 0; e < n; e++) {
+        WfEngine& E = **slot[e];
+        engines[e] = &E;
+        E.set_stream(streams[e]);
+        E.set_march_budget(ctx->march_budget);
+        E.set_tuning(ctx->refill_min, ctx->drain_lanes, ctx->blocks_per_sm, ctx->march_inner);
+        if (e == 0 && E.stage_timing != ctx->stage_timing) PT_CUDA_TRY(ctx, E.set_stage_timing(ctx->stage_timing));
+        E.args.trace = e == 0 ? ctx->trace : KTrace{nullptr, nullptr, nullptr, 0};
+        PT_CUDA_TRY(ctx, E.reset());
+        uint32_t idx = 0;
+        PT_CUDA_TRY(ctx, E.add_pass_part(j, base[e], base[e + 1] - base[e], &idx));
+        if (e == 0) idx0 = idx;
+    }
     // Every iteration moves every live path by one ray; a ray's march spans at
     // most ceil(512 / budget) + 1 iterations.
+    WfEngine& E = *ctx->wf;
     const uint64_t march_iters = 512ull / (uint64_t)ctx->march_budget + 2;
-    uint64_t max_iter = ((uint64_t)total / E.pool + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
+    const uint64_t share_max = (total64 + (uint64_t)n - 1) / (uint64_t)n;  // the largest share
+    uint64_t max_iter = (share_max / E.pool + 2) * (2ull * (uint64_t)push->pathLength + 3) * march_iters + 16;
     if (ctx->drain_limit > 0 && ctx->drain_limit < max_iter) max_iter = ctx->drain_limit;
-    const cudaError_t e = E.drain(trace, max_iter);
-    if (e == cudaErrorTimeout) return fail(ctx, PT_ERR_KERNEL, "pt_dispatch: wavefront did not drain");
-    PT_CUDA_TRY(ctx, e);
-    uint32_t bad_index = 0;
-    if (const uint32_t site = E.check_failed(&bad_index))
-        return fail(ctx, PT_ERR_KERNEL, std::string("pt_dispatch: device index check failed: ") +
-                                            pt_check_site_name(site) + " (index " + std::to_string(bad_index) + ")");
-    ctx->last_iterations = E.host_counters->iterations;
+    const cudaError_t de = n > 1 ? wf_drain_many(engines, n, max_iter) : E.drain(trace, max_iter);
+    for (int e = 1; e < n; e++) {  // the resolve (and anything after it) waits for every engine
+        PT_CUDA_TRY(ctx, cudaEventRecord(ctx->join[e - 1], streams[e]));
+        PT_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->join[e - 1], 0));
+    }
+    if (de == cudaErrorTimeout) return fail(ctx, PT_ERR_KERNEL, "pt_dispatch: wavefront did not drain");
+    PT_CUDA_TRY(ctx, de);
+    ctx->last_iterations = 0;
+    for (int e = 0; e < n; e++) {
+        uint32_t bad_index = 0;
+        if (const uint32_t site = engines[e]->check_failed(&bad_index))
+            return fail(ctx, PT_ERR_KERNEL, std::string("pt_dispatch: device index check failed: ") +
+                                                pt_check_site_name(site) + " (index " + std::to_string(bad_index) + ")");
+        if (engines[e]->host_counters->iterations > ctx->last_iterations)
+            ctx->last_iterations = engines[e]->host_counters->iterations;
+    }
     E.args.trace = KTrace{nullptr, nullptr, nullptr, 0};
-    PT_CUDA_TRY(ctx, E.resolve(idx));
+    PT_CUDA_TRY(ctx, E.resolve(idx0));  // the whole pass: every share's colours
+    uint64_t launches1 = 0;
+    for (int e = 0; e < kMax; e++)
+        if (*slot[e]) launches1 += (*slot[e])->kernel_launches;
+    ctx->last_launches = launches1 - launches0;
     PT_CUDA_TRY(ctx, cudaEventRecord(ctx->done, ctx->stream));
     return PT_OK;
 }
@@ -710,7 +797,13 @@ static int ensure_jit(pt_ctx* ctx, JitKind kind) {
     m.key = program;
     if (cache.size() == kJitCache) {  // evict the oldest
         PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        if (kind == kJitMarch && ctx->wf) ctx->wf->set_march_kernel(nullptr);  // no graph may keep its kernel
+        for (cudaStream_t s : ctx->stream_more)
+            if (s) PT_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        if (kind == kJitMarch) {  // no graph may keep its kernel
+            if (ctx->wf) ctx->wf->set_march_kernel(nullptr);
+            for (WfEngine* e : ctx->wf_more)
+                if (e) e->set_march_kernel(nullptr);
+        }
         pt_jit_unload(cache.front());
         cache.erase(cache.begin());
     }

@@ -181,11 +181,20 @@ cudaError_t WfEngine::reset() {
 }
 
 cudaError_t WfEngine::add_pass(const WfJob& job, uint32_t* index) {
+    return add_pass_part(job, 0, (uint32_t)((uint64_t)job.pc.resolution[0] * (uint64_t)job.pc.resolution[1] *
+                                            (uint64_t)job.pc.samplesPerFrame),
+                         index);
+}
+
+cudaError_t WfEngine::add_pass_part(const WfJob& job, uint32_t local_base, uint32_t count, uint32_t* index) {
     if (njobs - lo >= max_jobs) return cudaErrorInvalidValue;
+    const uint64_t whole = (uint64_t)job.pc.resolution[0] * (uint64_t)job.pc.resolution[1] *
+                           (uint64_t)job.pc.samplesPerFrame;
+    if ((uint64_t)local_base + count > whole) return cudaErrorInvalidValue;
     WfJob j = job;
     j.first = total;
-    j.count = (uint32_t)((uint64_t)j.pc.resolution[0] * (uint64_t)j.pc.resolution[1] *
-                         (uint64_t)j.pc.samplesPerFrame);
+    j.count = count;
+    j.local_base = local_base;
     j.finished = 0;
     std::memset(&j.cam, 0, sizeof j.cam);
     const uint32_t idx = njobs;
@@ -342,6 +351,43 @@ cudaError_t WfEngine::resolve(uint32_t j, cudaStream_t on) {
     const WfJob& J = job(j);
     kernel_launches += 1;
     return kernels->resolve(&args, j % max_jobs, &J.pc, J.accum, J.colors, on ? on : stream);
+}
+
+cudaError_t wf_drain_many(WfEngine* const* e, int n, uint64_t max_iterations) {
+    constexpr int kMax = 8;
+    if (n < 1 || n > kMax) return cudaErrorInvalidValue;
+    for (int i = 0; i < n; i++) {
+        if (e[i]->persistent) return cudaErrorInvalidValue;
+        for (int k = 0; k < i; k++)
+            if (e[k]->stream == e[i]->stream) return cudaErrorInvalidValue;
+    }
+    int chunk[kMax];
+    uint64_t iter[kMax];
+    bool done[kMax];
+    for (int i = 0; i < n; i++) {
+        chunk[i] = 8;
+        iter[i] = 8;
+        done[i] = false;
+        EN_TRY(e[i]->run(chunk[i], false));
+    }
+    for (int left = n; left > 0;) {
+        for (int i = 0; i < n; i++) {
+            if (done[i]) continue;
+            WfCounters c;
+            EN_TRY(e[i]->read_counters(&c));  // waits for this engine's stream only
+            // finished, or stopped by a failed index check (the caller reports it)
+            if ((c.next_sample == c.total && c.live == 0) || c.check_site != PT_CHECK_NONE) {
+                done[i] = true;
+                left--;
+                continue;
+            }
+            if (iter[i] > max_iterations) return cudaErrorTimeout;
+            if (chunk[i] < 64) chunk[i] *= 2;
+            EN_TRY(e[i]->run(chunk[i], false));
+            iter[i] += (uint64_t)chunk[i];
+        }
+    }
+    return cudaSuccess;
 }
 
 cudaError_t WfEngine::drain(bool trace, uint64_t max_iterations) {

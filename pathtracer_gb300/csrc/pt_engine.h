@@ -69,6 +69,14 @@ inline const char* pt_check_site_name(uint32_t site) {
     }
 }
 
+struct WfEngine;
+// Drains n (1..8) staged engines on different streams, each relaunched as
+// soon as its last chunk of iterations has been read back, so that one
+// engine's kernels fill the SMs that the others' kernel tails and host
+// round trips leave idle.  Same results and iteration bound (per engine) as
+// drain() without a trace.
+cudaError_t wf_drain_many(WfEngine* const* engines, int n, uint64_t max_iterations);
+
 struct WfEngine {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -154,6 +162,11 @@ struct WfEngine {
     // (job.variant: the scene's primitive classes, PT_FEAT_ALL when unknown).
     // Fails with cudaErrorInvalidValue while the ring is full.
     cudaError_t add_pass(const WfJob& job, uint32_t* index);
+    // Appends samples [local_base, local_base + count) of a pass (in the
+    // pass's sample order, [k][pixel]); the rest of the pass is rendered
+    // elsewhere (another engine) and the pass is resolved once both parts
+    // have finished.  The colour buffer is the whole pass's.
+    cudaError_t add_pass_part(const WfJob& job, uint32_t local_base, uint32_t count, uint32_t* index);
     // Passes [lo, new_lo) were resolved: their ring entries may be reused.
     void retire(uint32_t new_lo);
     // Launches `n` iterations.

@@ -296,6 +296,9 @@ CUDA_API = [
     ("pt_get_engine", _i, [_vp]),
     ("pt_set_wavefront_pool", _i, [_vp, ctypes.c_uint32]),
     ("pt_last_iterations", ctypes.c_uint32, [_vp]),
+    ("pt_last_kernel_launches", ctypes.c_uint64, [_vp]),
+    ("pt_set_wavefront_engines", _i, [_vp, _i]),
+    ("pt_get_wavefront_engines", _i, [_vp]),
     ("pt_set_march_budget", _i, [_vp, _i]),
     ("pt_set_stage_timing", _i, [_vp, _i]),
     ("pt_get_stage_times", _i, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]),

@@ -236,6 +236,13 @@ class Context:
     def set_wavefront_pool(self, slots: int):
         self._check(self._lib.pt_set_wavefront_pool(self._h, slots))
 
+    def set_wavefront_engines(self, engines: int):
+        """pt_set_wavefront_engines: engines (1..4, on streams of their own) a large dispatch is split between."""
+        self._check(self._lib.pt_set_wavefront_engines(self._h, engines))
+
+    def wavefront_engines(self) -> int:
+        return self._lib.pt_get_wavefront_engines(self._h)
+
     def set_march_budget(self, steps: int):
         self._check(self._lib.pt_set_march_budget(self._h, steps))
 
@@ -272,6 +279,10 @@ class Context:
 
     def last_iterations(self) -> int:
         return self._lib.pt_last_iterations(self._h)
+
+    def last_kernel_launches(self) -> int:
+        """Kernels the last dispatch launched."""
+        return self._lib.pt_last_kernel_launches(self._h)
 
     def set_fp_contract(self, on: bool):
         """pt_set_fp_contract: FMA contraction in run-time compiled kernels (off: bit-exact)."""
