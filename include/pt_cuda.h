@@ -372,8 +372,8 @@ int pt_quartic_surface_eval(pt_ctx* ctx, int which, const float* d_rays6, float*
  * shipped SDF plug-ins only (PT_SDF_CUSTOM: PT_ERR_UNSUPPORTED).
  * The first call on each device looks up the array's device address; with
  * lazy module loading (the CUDA default) that first call also commits the
- * array's 32 MiB, so make it once as a warm-up (before any stream capture):
- * later calls allocate nothing.  All calls share the array, so calls that
+ * array's 32 MiB, so make it once as a warm-up: later calls allocate
+ * nothing.  All calls share the array, so calls that
  * overlap on the GPU race; the counters are reset at the start of every
  * call.  A per-device host lock is held for the whole call and the call
  * returns only when the dispatch is complete on `stream` (NULL: the default

@@ -17,10 +17,10 @@
 // (with that device current) and caches it (devices 0..63).  With lazy module
 // loading (the CUDA default) that lookup is also what loads this file's
 // module, so the first call on a device commits the array's 32 MiB; later
-// calls allocate nothing.  Make the first call (a warm-up) before any stream
-// capture.  Every call shares the array and overwrites what it needs (the
-// counters are reset, the colours and path slots are rewritten), so calls
-// that overlap on the GPU race.  A per-device host lock is held for the whole
+// calls allocate nothing, so make the first call a warm-up.  Every call
+// shares the array and overwrites what it needs (the counters are reset,
+// the colours and path slots are rewritten), so calls that overlap on the
+// GPU race.  A per-device host lock is held for the whole
 // call and each call returns only once its work on the stream is complete,
 // so calls from several host threads run one after another.
 #include <cuda_runtime.h>
