@@ -799,6 +799,8 @@ def run_progressive(args, rank, world):
 
     b = Batch(local, pool_slots=args.pool or (1 << 22), max_passes=4096)
     b.set_route(native.PT_BATCH_ROUTE_STAGED)
+    if args.wf_engines:
+        b.set_wavefront_engines(min(args.wf_engines, 2))
     # the scene's SDFs as text: shipped snippets select plug-ins, the full
     # form's fBm terrain is compiled at run time
     sid = b.add_scene_sources(ubo, scene.sdf_sources())

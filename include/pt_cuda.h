@@ -467,8 +467,8 @@ typedef struct pt_batch_info {
     uint64_t kernel_launches; /* kernels the batch has launched (graph replays counted per kernel) */
 } pt_batch_info;
 
-/* pool_slots >= 1024 paths in flight in the staged engine; max_passes passes
- * of each engine in flight at once. */
+/* pool_slots >= 1024 paths in flight in each staged engine; max_passes
+ * passes of each engine in flight at once. */
 int pt_batch_create(pt_batch** out, int device, uint32_t pool_slots, uint32_t max_passes);
 int pt_batch_destroy(pt_batch* batch);
 const char* pt_batch_last_error(pt_batch* batch);
@@ -478,6 +478,12 @@ int pt_batch_set_march_budget(pt_batch* batch, int steps);
  * samples together (1..32, default 16: starting samples one lane at a time
  * runs the camera and lens code with few lanes active). */
 int pt_batch_set_persist_refill(pt_batch* batch, int lanes);
+/* Staged engines (1 or 2; default 2) for passes added from now on: with 2, a
+ * staged pass of at least 4 * pool_slots samples is split in two halves (in
+ * sample order) between two staged engines with a pool each, on two streams,
+ * as pt_set_wavefront_engines does for a context; the same bits as one
+ * engine.  The second engine's pool is allocated by the first such pass. */
+int pt_batch_set_wavefront_engines(pt_batch* batch, int engines);
 /* Engine choice for passes added from now on (PT_BATCH_ROUTE_*). */
 int pt_batch_set_route(pt_batch* batch, int route);
 int pt_batch_add_scene(pt_batch* batch, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int nplugins,

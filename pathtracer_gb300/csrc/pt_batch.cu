@@ -72,6 +72,12 @@ struct BatchPass {
     int scene = -1, target = -1;
     int engine = 0;     // kStaged or kPersistent
     uint32_t eidx = 0;  // pass number within its engine's ring
+    // A large staged pass is split in two: samples [0, count0) on kStaged,
+    // [count0, count) on kStaged2 (engine2 = kStaged2, ring entry eidx2).
+    int engine2 = -1;
+    uint32_t eidx2 = 0;
+    uint32_t count0 = 0;
+    bool part_finished[2] = {false, false};
     float4* d_colors = nullptr;
     uint32_t count = 0;
     uint32_t spf = 0;
@@ -79,19 +85,22 @@ struct BatchPass {
     bool done = false;      // resolved
 };
 
-constexpr int kStaged = 0, kPersistent = 1;
+constexpr int kStaged = 0, kPersistent = 1, kStaged2 = 2;
+constexpr int kEngines = 3;
 
 }  // namespace
 
 struct pt_batch {
     int device = 0;
     cudaStream_t stream = nullptr;       // resolution, uploads, allocation
-    cudaStream_t estream[2] = {nullptr, nullptr};
+    cudaStream_t estream[kEngines] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev = nullptr;            // orders engine work after the batch stream
     cudaMemPool_t mempool = nullptr;     // colour buffers and targets; keeps freed memory mapped
-    WfEngine engine[2];
-    bool engine_live[2] = {false, false};
-    std::deque<uint32_t> eorder[2];      // batch pass ids of each engine's ring, from its lo
+    WfEngine engine[kEngines];           // kStaged, kPersistent, kStaged2
+    bool engine_live[kEngines] = {false, false, false};
+    std::deque<uint32_t> eorder[kEngines];  // batch pass ids of each engine's ring, from its lo
+    // Staged engines a large staged pass is split between (pt_batch_set_wavefront_engines).
+    int staged_engines = 2;
     uint32_t pool_slots = 0, max_passes = 0;
     int route = PT_BATCH_ROUTE_AUTO;
     int march_budget = 64;
@@ -167,7 +176,7 @@ const void* staged_march_kernel(const pt_batch* b) {
     return b->bulb ? ptk_wavefront_kernels(b->device_checks)->march_warp_normals() : nullptr;
 }
 
-// Creates engine e on first use: the staged engine with the batch's pool,
+// Creates engine e on first use: a staged engine with the batch's pool,
 // the persistent engine with the smallest pool (it keeps paths in registers).
 cudaError_t ensure_engine(pt_batch* b, int e) {
     if (b->engine_live[e]) return cudaSuccess;
@@ -175,7 +184,7 @@ cudaError_t ensure_engine(pt_batch* b, int e) {
         const cudaError_t r = cudaStreamCreateWithFlags(&b->estream[e], cudaStreamNonBlocking);
         if (r != cudaSuccess) return r;
     }
-    const uint32_t pool = e == kStaged ? b->pool_slots : 1024u;
+    const uint32_t pool = e == kPersistent ? 1024u : b->pool_slots;
     const cudaError_t r = b->engine[e].create(b->device, b->estream[e], pool, b->max_passes, b->march_budget);
     if (r != cudaSuccess) {
         b->engine[e].destroy();
@@ -184,9 +193,15 @@ cudaError_t ensure_engine(pt_batch* b, int e) {
     b->engine[e].set_persistent(e == kPersistent);
     b->engine[e].args.persist_refill = b->persist_refill;
     b->engine[e].set_checks(b->device_checks);
-    if (e == kStaged) b->engine[e].set_march_kernel(staged_march_kernel(b));
+    if (e != kPersistent) b->engine[e].set_march_kernel(staged_march_kernel(b));
     b->engine_live[e] = true;
     return cudaSuccess;
+}
+
+// Sets the march kernel of every live staged engine.
+void set_staged_march_kernel(pt_batch* b, const void* kernel) {
+    for (int e : {kStaged, kStaged2})
+        if (b->engine_live[e]) b->engine[e].set_march_kernel(kernel);
 }
 
 // FP64 target: adds the pass's exposed sample colours (Rendering's exposure
@@ -375,7 +390,7 @@ int pt_batch_create(pt_batch** out, int device, uint32_t pool_slots, uint32_t ma
 int pt_batch_destroy(pt_batch* b) {
     if (!b) return PT_ERR_INVALID;
     cudaSetDevice(b->device);
-    for (int e = 0; e < 2; e++)
+    for (int e = 0; e < kEngines; e++)
         if (b->estream[e]) cudaStreamSynchronize(b->estream[e]);
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (auto& s : b->scenes) {
@@ -389,7 +404,7 @@ int pt_batch_destroy(pt_batch* b) {
     for (auto& p : b->passes)
         if (p.d_colors) cudaFreeAsync(p.d_colors, b->stream);
     if (b->stream) cudaStreamSynchronize(b->stream);
-    for (int e = 0; e < 2; e++) {
+    for (int e = 0; e < kEngines; e++) {
         b->engine[e].destroy();
         if (b->estream[e]) cudaStreamDestroy(b->estream[e]);
     }
@@ -412,7 +427,7 @@ int pt_batch_set_march_budget(pt_batch* b, int steps) {
     if (!b) return PT_ERR_INVALID;
     if (steps < 1 || steps > 512) return bfail(b, PT_ERR_INVALID, "pt_batch_set_march_budget: 1..512 steps");
     b->march_budget = steps;
-    for (int e = 0; e < 2; e++) b->engine[e].set_march_budget(steps);
+    for (int e = 0; e < kEngines; e++) b->engine[e].set_march_budget(steps);
     return PT_OK;
 }
 
@@ -420,7 +435,14 @@ int pt_batch_set_persist_refill(pt_batch* b, int lanes) {
     if (!b) return PT_ERR_INVALID;
     if (lanes < 1 || lanes > 32) return bfail(b, PT_ERR_INVALID, "pt_batch_set_persist_refill: 1..32 lanes");
     b->persist_refill = lanes;
-    for (int e = 0; e < 2; e++) b->engine[e].args.persist_refill = lanes;
+    for (int e = 0; e < kEngines; e++) b->engine[e].args.persist_refill = lanes;
+    return PT_OK;
+}
+
+int pt_batch_set_wavefront_engines(pt_batch* b, int engines) {
+    if (!b) return PT_ERR_INVALID;
+    if (engines != 1 && engines != 2) return bfail(b, PT_ERR_INVALID, "pt_batch_set_wavefront_engines: 1 or 2 engines");
+    b->staged_engines = engines;
     return PT_OK;
 }
 
@@ -611,11 +633,22 @@ int pt_batch_add_pass(pt_batch* b, int scene_id, int target_id, const pt_push* p
     WfEngine& E = b->engine[e];
     if (E.njobs - E.lo >= E.max_jobs)
         return bfail(b, PT_ERR_BUSY, "pt_batch_add_pass: every pass slot is in flight; step the batch first");
+    // A staged pass of at least two pools' worth of samples per engine is
+    // split in two halves (in sample order) between two staged engines on
+    // two streams: one engine's kernels fill the SMs the other's leave idle.
+    const bool split = e == kStaged && b->staged_engines == 2 && count >= 4ull * b->pool_slots;
+    if (split) {
+        PT_B_TRY(b, ensure_engine(b, kStaged2));
+        const WfEngine& E2 = b->engine[kStaged2];
+        if (E2.njobs - E2.lo >= E2.max_jobs)
+            return bfail(b, PT_ERR_BUSY, "pt_batch_add_pass: every pass slot is in flight; step the batch first");
+    }
     BatchPass p;
     p.scene = scene_id;
     p.target = target_id;
     p.engine = e;
     p.count = (uint32_t)count;
+    p.count0 = split ? (uint32_t)(count / 2) : (uint32_t)count;
     p.spf = (uint32_t)push->samplesPerFrame;
     // Allocated on the batch stream; engine streams wait for it in pt_batch_step.
     PT_B_TRY(b, cudaMallocFromPoolAsync(&p.d_colors, count * sizeof(float4), b->mempool, b->stream));
@@ -628,15 +661,23 @@ int pt_batch_add_pass(pt_batch* b, int scene_id, int target_id, const pt_push* p
     j.pc = *push;
     j.variant = sc.variant;
     j.host_scene = e == kPersistent ? sc.h_scene.get() : nullptr;
-    const cudaError_t r = E.add_pass(j, &p.eidx);
+    const cudaError_t r = E.add_pass_part(j, 0, p.count0, &p.eidx);
     if (r != cudaSuccess) {
         cudaFreeAsync(p.d_colors, b->stream);
         return bcuda(b, r, "pt_batch_add_pass");
+    }
+    if (split) {
+        p.engine2 = kStaged2;
+        // The first half is in the ring already: should this launch fail (a
+        // lost context), the colour buffer is kept rather than freed under it.
+        const cudaError_t r2 = b->engine[kStaged2].add_pass_part(j, p.count0, p.count - p.count0, &p.eidx2);
+        if (r2 != cudaSuccess) return bcuda(b, r2, "pt_batch_add_pass");
     }
     const uint32_t id = b->next_pass++;
     if (b->passes.empty()) b->pass_base = id;
     b->passes.push_back(p);
     b->eorder[e].push_back(id);
+    if (split) b->eorder[kStaged2].push_back(id);
     t.passes_in_flight++;
     b->scenes[(size_t)scene_id].passes_in_flight++;
     b->samples_added += count;
@@ -666,14 +707,15 @@ int prepare_jit(pt_batch* b) {
     rc = pt_jit_load(cubin, kJitMarch, lowered, m, log);
     if (rc != PT_OK) return bfail(b, rc, log);
     m.key = program;
-    if (b->estream[kStaged]) {
-        const cudaError_t e = cudaStreamSynchronize(b->estream[kStaged]);  // the old module's launches
+    for (int se : {kStaged, kStaged2}) {
+        if (!b->estream[se]) continue;
+        const cudaError_t e = cudaStreamSynchronize(b->estream[se]);  // the old module's launches
         if (e != cudaSuccess) {
             pt_jit_unload(m);
             return bcuda(b, e, "pt_batch_step");
         }
     }
-    if (b->engine_live[kStaged]) b->engine[kStaged].set_march_kernel(reinterpret_cast<const void*>(m.kernel[0]));
+    set_staged_march_kernel(b, reinterpret_cast<const void*>(m.kernel[0]));
     pt_jit_unload(b->jit);
     b->jit = m;
     b->jit_dirty = false;
@@ -711,24 +753,29 @@ int pt_batch_step(pt_batch* b, int iterations, int* completed, int capacity, int
     PT_B_TRY(b, cudaSetDevice(b->device));
     const int jr = prepare_jit(b);
     if (jr != PT_OK) return jr;
-    if (b->engine_live[kStaged] && b->engine[kStaged].march_kernel != staged_march_kernel(b)) {
-        // a mandelbulb scene arrived: no launch of the old kernel may be in flight
-        PT_B_TRY(b, cudaStreamSynchronize(b->estream[kStaged]));
-        b->engine[kStaged].set_march_kernel(staged_march_kernel(b));
+    for (int se : {kStaged, kStaged2})
+        if (b->engine_live[se] && b->engine[se].march_kernel != staged_march_kernel(b)) {
+            // a mandelbulb scene arrived: no launch of the old kernel may be in flight
+            PT_B_TRY(b, cudaStreamSynchronize(b->estream[se]));
+            b->engine[se].set_march_kernel(staged_march_kernel(b));
+        }
+    bool busy[kEngines];
+    bool any = false;
+    for (int e = 0; e < kEngines; e++) {
+        busy[e] = b->engine_live[e] && b->engine[e].njobs > b->engine[e].lo;
+        any = any || busy[e];
     }
-    bool busy[2];
-    for (int e = 0; e < 2; e++) busy[e] = b->engine_live[e] && b->engine[e].njobs > b->engine[e].lo;
-    if (iterations > 0 && (busy[0] || busy[1])) {
+    if (iterations > 0 && any) {
         // Colour buffers and job entries were set up on the batch stream.
         PT_B_TRY(b, cudaEventRecord(b->ev, b->stream));
-        for (int e = 0; e < 2; e++) {
+        for (int e = 0; e < kEngines; e++) {
             if (!busy[e]) continue;
             PT_B_TRY(b, cudaStreamWaitEvent(b->estream[e], b->ev, 0));
             PT_B_TRY(b, b->engine[e].run(iterations, false));
         }
         b->iterations += (uint64_t)iterations;
     }
-    for (int e = 0; e < 2; e++) {
+    for (int e = 0; e < kEngines; e++) {
         if (!busy[e]) continue;
         WfEngine& E = b->engine[e];
         if (E.checks) {
@@ -742,7 +789,9 @@ int pt_batch_step(pt_batch* b, int iterations, int* completed, int capacity, int
         PT_B_TRY(b, E.read_finished(E.lo, E.njobs, b->h_finished));
         for (uint32_t j = E.lo; j < E.njobs; j++) {
             BatchPass& p = *pass_at(b, b->eorder[e][j - E.lo]);
-            if (b->h_finished[j - E.lo] >= p.count) p.finished = true;
+            const int part = e == p.engine ? 0 : 1;
+            if (b->h_finished[j - E.lo] >= (part == 0 ? p.count0 : p.count - p.count0)) p.part_finished[part] = true;
+            p.finished = p.part_finished[0] && (p.engine2 < 0 || p.part_finished[1]);
         }
     }
     std::fill(b->blocked.begin(), b->blocked.end(), 0);
@@ -779,7 +828,7 @@ int pt_batch_step(pt_batch* b, int iterations, int* completed, int capacity, int
     }
     // Retire each engine's resolved prefix (its ring entries are reused) and
     // drop the batch's resolved prefix.
-    for (int e = 0; e < 2; e++) {
+    for (int e = 0; e < kEngines; e++) {
         if (!b->engine_live[e]) continue;
         uint32_t lo = b->engine[e].lo;
         while (!b->eorder[e].empty() && pass_at(b, b->eorder[e].front())->done) {
@@ -809,13 +858,13 @@ int pt_batch_set_device_checks(pt_batch* b, int on) {
     if (pt_batch_pending(b) > 0) return bfail(b, PT_ERR_BUSY, "pt_batch_set_device_checks: passes are in flight");
     PT_B_TRY(b, cudaSetDevice(b->device));
     b->device_checks = on != 0;
-    for (int e = 0; e < 2; e++) {
+    for (int e = 0; e < kEngines; e++) {
         if (!b->engine_live[e]) continue;
         PT_B_TRY(b, cudaStreamSynchronize(b->engine[e].stream));
         b->engine[e].set_checks(b->device_checks);
     }
     if (!b->custom.empty()) b->jit_dirty = true;  // the march kernel of the other build
-    if (b->engine_live[kStaged] && !b->jit_dirty) b->engine[kStaged].set_march_kernel(staged_march_kernel(b));
+    if (!b->jit_dirty) set_staged_march_kernel(b, staged_march_kernel(b));
     return PT_OK;
 }
 
@@ -886,7 +935,7 @@ int pt_batch_stats(pt_batch* b, pt_batch_info* out) {
     out->passes_staged = b->engine_live[kStaged] ? b->engine[kStaged].njobs : 0;
     out->passes_persistent = b->engine_live[kPersistent] ? b->engine[kPersistent].njobs : 0;
     out->kernel_launches = b->kernel_launches;
-    for (int e = 0; e < 2; e++)
+    for (int e = 0; e < kEngines; e++)
         if (b->engine_live[e]) out->kernel_launches += b->engine[e].kernel_launches;
     return PT_OK;
 }
@@ -991,7 +1040,7 @@ int pt_batch_set_scene_ext(pt_batch* b, int scene_id, const pt_scene_ext* ext) {
         std::memset(&x, 0, sizeof x);
     }
     PT_B_TRY(b, cudaSetDevice(b->device));
-    for (int e = 0; e < 2; e++)
+    for (int e = 0; e < kEngines; e++)
         if (b->engine_live[e]) PT_B_TRY(b, cudaStreamSynchronize(b->engine[e].stream));
     PT_B_TRY(b, cudaMemcpyAsync(&s.d_scene->ext, &x, sizeof x, cudaMemcpyHostToDevice, b->stream));
     PT_B_TRY(b, cudaStreamSynchronize(b->stream));  // the copy reads the stack

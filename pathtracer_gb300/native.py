@@ -315,6 +315,7 @@ CUDA_API = [
     ("pt_batch_set_route", _i, [_vp, _i]),
     ("pt_batch_set_device_checks", _i, [_vp, _i]),
     ("pt_batch_set_persist_refill", _i, [_vp, _i]),
+    ("pt_batch_set_wavefront_engines", _i, [_vp, _i]),
     ("pt_batch_add_scene", _i, [_vp, _vp, ctypes.POINTER(PtSdfPlugin), _i, ctypes.POINTER(_i)]),
     ("pt_batch_set_scene_ext", _i, [_vp, _i, _vp]),
     ("pt_batch_add_scene_sources", _i, [_vp, _vp, ctypes.POINTER(ctypes.c_char_p), _i, ctypes.POINTER(_i)]),

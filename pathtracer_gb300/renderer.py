@@ -344,6 +344,10 @@ class Batch:
     def set_persist_refill(self, lanes: int):
         self._check(self._lib.pt_batch_set_persist_refill(self._h, lanes))
 
+    def set_wavefront_engines(self, engines: int):
+        """pt_batch_set_wavefront_engines: 1, or 2 staged engines that split large passes."""
+        self._check(self._lib.pt_batch_set_wavefront_engines(self._h, engines))
+
     def set_route(self, route: int):
         self._check(self._lib.pt_batch_set_route(self._h, route))
 

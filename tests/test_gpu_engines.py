@@ -8,7 +8,11 @@ So the accumulator must be the one-engine accumulator bit for bit, and the
 megakernel's.  The tests use a 1024-slot pool so that small dispatches are
 split (and recycle every slot many times), odd sample totals (uneven
 shares), progressive passes, the run-time compiled march kernel and the
-checked kernel build; one test runs the bench's full-size dispatch.
+checked kernel build; one test runs the bench's full-size dispatch.  A
+batch splits its large staged passes the same way
+(pt_batch_set_wavefront_engines): float and FP64 targets must be the
+one-engine targets bit for bit, with passes of several jobs in flight
+together or one job's passes after another.
 """
 import os
 
@@ -107,3 +111,70 @@ def test_split_engines_full_size(rt, engines):
     got, l = _render(rt, scene, 1024, 1024, 64, 6, 1, engines=engines, pool=0, passes=1)
     assert np.array_equal(got.view(np.uint32), one.view(np.uint32))
     assert l[0] > 4 * 100
+
+
+def _batch(rt, jobs, engines, kind=0, checks=False, interleave=True):
+    """jobs: (scene, W, H, spf, depth, passes) on the staged route of a batch
+    with 1024-slot pools; passes of all jobs in flight together."""
+    from pathtracer_gb300 import Batch
+
+    native = rt["native"]
+    with Batch(0, pool_slots=1024, max_passes=64) as b:
+        b.set_route(native.PT_BATCH_ROUTE_STAGED)
+        b.set_wavefront_engines(engines)
+        b.set_device_checks(checks)
+        ids = []
+        for scene, W, H, spf, depth, passes in jobs:
+            sid = b.add_scene_sources(scene.pack_ubo(rt["cie"]), scene.sdf_sources())
+            ids.append((sid, b.add_target(W, H, kind)))
+        npass = max(j[5] for j in jobs)
+        for k in range(1, npass + 1):
+            for (sid, tid), (scene, W, H, spf, depth, passes) in zip(ids, jobs):
+                if k <= passes:
+                    b.add_pass(sid, tid, scene.push_constants(W, H, k * spf, k * spf, spf, depth))
+            if not interleave:
+                b.run()
+        b.run()
+        st = b.stats()
+        assert st["samples_done"] == st["samples_added"]
+        return [b.read_target(tid) for _, tid in ids]
+
+
+def _batch_jobs(rt):
+    S = rt["Scene"]
+    # the first two jobs' passes are split (>= 4096 samples), the third's not
+    return [(S.load(os.path.join(SCENES, "mandelbulb12_plane.json")), 48, 40, 8, 6, 2),
+            (S.load(os.path.join(SCENES, "menger_terrain.json")), 51, 41, 3, 12, 3),
+            (S.load(os.path.join(SCENES, "cornell_box.json")), 30, 20, 4, 8, 2)]
+
+
+@pytest.mark.parametrize("interleave", [True, False])
+def test_batch_split_passes_equal_one_engine(rt, interleave):
+    jobs = _batch_jobs(rt)
+    one = _batch(rt, jobs, 1, interleave=interleave)
+    two = _batch(rt, jobs, 2, interleave=interleave)
+    for a, b in zip(one, two):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    # and each equals its passes dispatched alone on one engine
+    for got, (scene, W, H, spf, depth, passes) in zip(two, jobs):
+        want, _ = _render(rt, scene, W, H, spf, depth, 1, engines=1, passes=passes)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_batch_split_passes_fp64_target_and_checks(rt):
+    jobs = _batch_jobs(rt)[:2]
+    native = rt["native"]
+    one = _batch(rt, jobs, 1, kind=native.PT_TARGET_FP64)
+    two = _batch(rt, jobs, 2, kind=native.PT_TARGET_FP64, checks=True)
+    for a, b in zip(one, two):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_batch_engines_knob(rt):
+    from pathtracer_gb300 import Batch
+
+    with Batch(0, pool_slots=1024, max_passes=4) as b:
+        for bad in (0, 3):
+            with pytest.raises(rt["Error"]):
+                b.set_wavefront_engines(bad)
+        b.set_wavefront_engines(1)
