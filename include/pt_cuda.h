@@ -208,7 +208,8 @@ typedef struct pt_scene_ext {
 int pt_upload_scene_ext(pt_ctx* ctx, const pt_ubo* ubo, const pt_scene_ext* ext);
 
 /* Replaces CreateTexelBuffer (src/pathtracer.cpp:2250-2256): a zeroed
- * W*H float4 accumulator. */
+ * W*H float4 accumulator (at the current size: the same buffer, zeroed in
+ * stream order; another size: a new buffer, after the stream drains). */
 int pt_resize_accum(pt_ctx* ctx, int width, int height);
 
 /* Replaces RecordComputeCommandBuffer + vkQueueSubmit

@@ -296,13 +296,18 @@ int pt_resize_accum(pt_ctx* ctx, int width, int height) {
     if (width <= 0 || height <= 0 || (long long)width * (long long)height > (1ll << 31))
         return fail(ctx, PT_ERR_INVALID, "pt_resize_accum: bad size");
     PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)width * (size_t)height * sizeof(float4);
+    if (ctx->d_accum && width == ctx->width && height == ctx->height) {
+        // the same size: zeroed in place, in stream order (no free, no allocation)
+        PT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_accum, 0, bytes, ctx->stream));
+        return PT_OK;
+    }
     PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->d_accum) {
         cudaFree(ctx->d_accum);
         ctx->d_accum = nullptr;
         ctx->width = ctx->height = 0;
     }
-    const size_t bytes = (size_t)width * (size_t)height * sizeof(float4);
     PT_CUDA_TRY(ctx, cudaMalloc(&ctx->d_accum, bytes));
     PT_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_accum, 0, bytes, ctx->stream));
     ctx->width = width;

@@ -178,3 +178,27 @@ def test_batch_engines_knob(rt):
             with pytest.raises(rt["Error"]):
                 b.set_wavefront_engines(bad)
         b.set_wavefront_engines(1)
+
+
+def test_resize_to_the_same_size_zeroes_in_place(rt):
+    """pt_resize_accum at the current size keeps the buffer and zeroes it in
+    stream order, after the dispatch queued before it; a render after it
+    equals a fresh context's render."""
+    scene = rt["Scene"].load(os.path.join(SCENES, "cornell_box.json"))
+    W, H, spf, depth = 64, 48, 8, 8
+    want, _ = _render(rt, scene, W, H, spf, depth, 1, passes=1)
+    with rt["Context"](0) as ctx:
+        ctx.set_wavefront_pool(1024)
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        ptr = ctx.accum_device_ptr()
+        ctx.dispatch(scene.push_constants(W, H, 7 * spf, 3 * spf, spf, depth))
+        ctx.resize_accum(W, H)
+        assert ctx.accum_device_ptr() == ptr
+        assert not ctx.read_accum().any()
+        ctx.dispatch(scene.push_constants(W, H, spf, spf, spf, depth))
+        ctx.wait()
+        got = ctx.read_accum()
+        ctx.resize_accum(W + 1, H)
+        assert not ctx.read_accum().any()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
