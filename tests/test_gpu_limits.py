@@ -43,7 +43,10 @@ def _plain(renderer, cie, scene, W, H, spf, depth, engine):
         return ctx.read_accum()
 
 
-def test_dispatch_drain_limit(env):
+@pytest.mark.parametrize("engines", [1, 2])
+def test_dispatch_drain_limit(env, engines):
+    """With two engines the dispatch is split (2^17-slot pools, 8 pools of
+    samples): the limit stops both, and the next dispatch resets both."""
     native, renderer, cie = env
     scene = renderer.Scene.load(os.path.join(SCENES, "mandelbulb_plane.json"))
     W, H, spf, depth = 256, 256, 16, 6
@@ -51,6 +54,9 @@ def test_dispatch_drain_limit(env):
     want = _plain(renderer, cie, scene, W, H, spf, depth, native.PT_ENGINE_WAVEFRONT)
     with renderer.Context(0) as ctx:
         ctx.set_engine(native.PT_ENGINE_WAVEFRONT)
+        ctx.set_wavefront_engines(engines)
+        if engines > 1:
+            ctx.set_wavefront_pool(1 << 17)
         ctx.bind(scene, cie)
         ctx.resize_accum(W, H)
         ctx.set_drain_limit(2)  # 1 M samples of depth-6 paths need far more iterations
