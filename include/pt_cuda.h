@@ -257,8 +257,9 @@ int pt_set_wavefront_pool(pt_ctx* ctx, uint32_t slots);
  * sample order: one engine's kernels fill the SMs that the others' kernel
  * tails and host round trips leave idle.  The same bits as one engine
  * (every sample's colour lands in the dispatch's colour buffer and is
- * summed per pixel in sample order).  Each engine holds a pool; one engine
- * runs when a trace or stage timing is on. */
+ * summed per pixel in sample order).  Each engine holds a pool (lowering
+ * the count frees the pools past it); one engine runs when a trace or stage
+ * timing is on. */
 int pt_set_wavefront_engines(pt_ctx* ctx, int engines);
 int pt_get_wavefront_engines(pt_ctx* ctx);
 /* Sphere-tracing iterations a ray may take per march launch before it is

@@ -423,6 +423,15 @@ int pt_set_wavefront_engines(pt_ctx* ctx, int engines) {
     if (engines < 1 || engines > pt_ctx::kMaxEngines)
         return fail(ctx, PT_ERR_INVALID, "pt_set_wavefront_engines: 1..4 engines");
     ctx->wf_engines = engines;
+    // engines past the new count give their pools back
+    PT_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    for (int e = engines - 1; e < pt_ctx::kMaxEngines - 1; e++) {
+        if (!ctx->wf_more[e]) continue;
+        PT_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream_more[e]));
+        ctx->wf_more[e]->destroy();
+        delete ctx->wf_more[e];
+        ctx->wf_more[e] = nullptr;
+    }
     return PT_OK;
 }
 

@@ -93,13 +93,26 @@ def test_small_dispatch_runs_on_one_engine(rt):
 
 
 def test_engines_knob(rt):
+    """Defaults, range, and lowering the count between dispatches (the
+    engines past it are freed; the next dispatches render the same bits)."""
+    scene = rt["Scene"].load(os.path.join(SCENES, "mandelbulb_plane.json"))
+    W, H, spf, depth = 64, 48, 8, 6
+    want, _ = _render(rt, scene, W, H, spf, depth, 1, engines=1, passes=3)
     with rt["Context"](0) as ctx:
         assert ctx.wavefront_engines() == 2
         for bad in (0, 5, -1):
             with pytest.raises(rt["Error"]):
                 ctx.set_wavefront_engines(bad)
-        ctx.set_wavefront_engines(1)
-        assert ctx.wavefront_engines() == 1
+        ctx.set_wavefront_pool(1024)
+        ctx.bind(scene, rt["cie"])
+        ctx.resize_accum(W, H)
+        for k, n in ((1, 4), (2, 1), (3, 3)):
+            ctx.set_wavefront_engines(n)
+            assert ctx.wavefront_engines() == n
+            ctx.dispatch(scene.push_constants(W, H, k * spf, k * spf, spf, depth))
+        ctx.wait()
+        got = ctx.read_accum()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
 @pytest.mark.parametrize("engines", [2, 3, 4])
