@@ -330,7 +330,7 @@ def cpu_baseline(args, W, H, spf_total, nthreads):
     reference's own shader built for the CPU where it was built ("reference":
     OpenMP over the rows' pixels), else the oracle (the CPU restatement,
     "port": one row per call, rows spread over `nthreads` host threads).
-    The scene is read, packed and given its CIE table by the checker-side
+    The scene is read, packed and given its CIE table by the oracle's own
     restatement of the reference host (oracle/pack.py): no library of the
     product is loaded on this path."""
     import ctypes

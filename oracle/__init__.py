@@ -1,1 +1,1 @@
-"""CPU restatement of the reference shader: test infrastructure (the checker)."""
+"""CPU restatement of the reference shader: test infrastructure (the oracle)."""

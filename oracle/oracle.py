@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU restatement of src/shader.comp (oracle/pt_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: the tests, the smoke check and the CPU-baseline
-leg of bench.py use it as the checker.  The product never imports it.
+leg of bench.py use it as the oracle.  The product never imports it.
 """
 from __future__ import annotations
 

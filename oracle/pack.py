@@ -1,5 +1,5 @@
 """The reference host's scene loading, uniform-buffer packing and push
-constants, restated in Python for the checker side.
+constants, restated in Python for the oracle's side.
 
 TEST INFRASTRUCTURE ONLY: the tests and the CPU legs of bench.py use it so
 that the oracle (and the reference's own shader built for the CPU) can be fed

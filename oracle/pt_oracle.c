@@ -1,7 +1,7 @@
 /*
  * pt_oracle.c — scalar CPU restatement of src/shader.comp (phyastro/PathTracer).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for libpt_cuda.  Each function below
+ * TEST INFRASTRUCTURE ONLY: the oracle for libpt_cuda.  Each function below
  * cites the shader lines it restates (SC = src/shader.comp) and evaluates the
  * GLSL expressions in the same order, in float, without contraction
  * (compiled with -ffp-contract=off); `fma` is called exactly where the shader

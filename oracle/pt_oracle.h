@@ -4,7 +4,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this
  * library; only the tests, the smoke check and the CPU-baseline leg of the
- * benchmark load it, as the checker.
+ * benchmark load it, as the oracle the GPU results are compared with.
  *
  * Parity status: the reference has no tests, golden vectors or images, and
  * it cannot run on these machines (Vulkan + Windows), so this restatement is

@@ -149,7 +149,7 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, str]:
 
 
 def build_oracle(force: bool = False) -> str:
-    """Compiles the CPU restatement used by the tests (oracle/, the checker)."""
+    """Compiles the oracle (oracle/: the CPU restatement the tests check against)."""
     out = os.path.join(ROOT, "oracle", "_build", "libpt_oracle.so")
     src = os.path.join(ROOT, "oracle", "pt_oracle.c")
     hdrs = [os.path.join(ROOT, "oracle", "pt_oracle.h"), os.path.join(ROOT, "include", "pt_cuda.h"),

@@ -45,7 +45,7 @@ def test_batch_cpu_baseline(built):
 @pytest.mark.parametrize("workload", ["mandelbulb12", "mandelbulb"])
 def test_reference_arm_loads_no_product_library(built, workload):
     """The reference arm packs the scene and builds its CIE table with the
-    checker-side restatement (oracle/pack.py): only libraries under oracle/
+    oracle's restatement (oracle/pack.py): only libraries under oracle/
     are mapped into the process, none of the product's."""
     code = (
         "import sys; sys.argv = ['bench.py', '--impl', 'reference', '--workload', %r, '--res', '32', '--spp', '2',"

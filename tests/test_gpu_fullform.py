@@ -4,7 +4,7 @@ smooth Lambertian spectra, conductor mirror, Cauchy and Sellmeier
 dielectrics).
 
 The GPU side binds the product's scene (libpt_host packs the extensions);
-the oracle side packs the same JSON with the checker's own restatement
+the oracle side packs the same JSON with the oracle's own restatement
 (oracle/pack.py), so the packer is not checked against itself.  Every engine
 runs the scenes of the workloads in their full form:
 - cornell_box_full (flat 0.75 sphere, Cauchy A 1.5, B 0.0042 um^2 sphere,
@@ -44,7 +44,7 @@ def rt(built):
 
 
 def _oracle_side(name):
-    """ubo, ext and plug-ins of a scene file from the checker's restatement."""
+    """ubo, ext and plug-ins of a scene file from the oracle's restatement."""
     from oracle import oracle, pack
 
     sc = pack.load_scene(os.path.join(SCENES, name + ".json"))

@@ -1,4 +1,4 @@
-"""The checker-side restatement of the reference host's scene loading,
+"""The oracle's restatement of the reference host's scene loading,
 uniform-buffer packing and push constants (oracle/pack.py) against the
 product's host library (libpt_host: pt_scene_parse, pt_scene_pack_ubo,
 pt_scene_push_constants, pt_cie_analytic_table, pt_parse_sdf_source).
