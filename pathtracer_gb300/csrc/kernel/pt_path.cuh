@@ -307,10 +307,14 @@ PT_DI StepResult roulette(PathStateT<R>& ps, int depth) {
     ps.bounce++;
     return (ps.bounce >= depth) ? STEP_TERMINATED : STEP_CONTINUE;
 }
+// The bounce's throughput update (SC:1373-1374, before the roulette).
+template <typename R> PT_DI V4<R> bounce_throughput(const PathStateT<R>& ps) {
+    const R costheta = dot3(ps.dir, ps.nrm);
+    return ps.rr * ((ps.brdf * costheta) / ps.brdfPdf);
+}
 template <bool TRACE, typename R>
 PT_DI StepResult finish_bounce(PathStateT<R>& ps, int depth) {
-    const R costheta = dot3(ps.dir, ps.nrm);
-    ps.rr = ps.rr * ((ps.brdf * costheta) / ps.brdfPdf);
+    ps.rr = bounce_throughput(ps);
     return roulette<TRACE>(ps, depth);
 }
 
@@ -507,6 +511,13 @@ PT_DI StepResult shade_primary(PathStateT<R>& ps, const KScene& S, const HitT<R>
     return finish_bounce<TRACE>(ps, depth);
 }
 
+// The NEE term of a light sample whose shadow ray reached the light.
+template <typename R> PT_DI V4<R> shadow_contribution(const PathStateT<R>& ps, const KScene& S) {
+    const V2<R> lt = light_mix(S, ps.shLightID);
+    const V4<R> rrl = ps.rr * ((ps.brdf * ps.cosL) / ps.lightPdf);
+    return (emit(ps.l, lt.x, lt.y) * rrl) * (PT_LIT(R, 1.0) - ps.mis);
+}
+
 // LightSourceVisibilityCheck result (SC:1121-1223) and the NEE term, then the
 // rest of the bounce.
 template <bool TRACE, typename R>
@@ -514,15 +525,34 @@ PT_DI StepResult shade_shadow(PathStateT<R>& ps, const KScene& S, int objectID, 
     const int obj = (objectID == -2) ? -1 : objectID;
     V4<R> contrib = v4s<R>(PT_LIT(R, 0.0));
     if (obj == ps.shObj) {
-        const V2<R> lt = light_mix(S, ps.shLightID);
-        const V4<R> rrl = ps.rr * ((ps.brdf * ps.cosL) / ps.lightPdf);
-        contrib = (emit(ps.l, lt.x, lt.y) * rrl) * (PT_LIT(R, 1.0) - ps.mis);
+        contrib = shadow_contribution(ps, S);
         if (TRACE) ps.ev |= 3u << PT_EV_SHADOW_SHIFT;
     } else {
         if (TRACE) ps.ev |= 2u << PT_EV_SHADOW_SHIFT;
     }
     ps.radiance = ps.radiance + contrib;
     return finish_bounce<TRACE>(ps, depth);
+}
+
+// shade_shadow with its two products made when the shadow ray was: the NEE
+// term (shadow_contribution) and the bounce's next throughput
+// (bounce_throughput), from the same values by the same operations, so the
+// result is shade_shadow's bit for bit.  The staged engine stores those two
+// instead of the light sample's geometry and the BRDF they come from.
+template <bool TRACE, typename R>
+PT_DI StepResult shade_shadow_made(PathStateT<R>& ps, int objectID, const V4<R>& contrib, const V4<R>& rr_next,
+                                   int depth) {
+    const int obj = (objectID == -2) ? -1 : objectID;
+    V4<R> c = v4s<R>(PT_LIT(R, 0.0));
+    if (obj == ps.shObj) {
+        c = contrib;
+        if (TRACE) ps.ev |= 3u << PT_EV_SHADOW_SHIFT;
+    } else {
+        if (TRACE) ps.ev |= 2u << PT_EV_SHADOW_SHIFT;
+    }
+    ps.radiance = ps.radiance + c;
+    ps.rr = rr_next;
+    return roulette<TRACE>(ps, depth);
 }
 
 // SC:1477-1489: the sample's XYZ with NaN rejection.

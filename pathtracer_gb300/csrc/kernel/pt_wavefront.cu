@@ -52,18 +52,25 @@ PT_DI uint32_t bounce_word(const PathState& ps) {
     return ((uint32_t)ps.medium << kMediumShift) | ((uint32_t)ps.bounce & kBounceMask);
 }
 
-PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t& flags, uint32_t& sample,
-                      uint32_t& job) {
-    const float4 a = v.s0[slot], b = v.s1[slot], c = v.s2[slot], d = v.s3[slot];
+// A shadow-ray result's state: the bounce's next ray (s0, s1), the NEE
+// term and the next throughput made with the shadow ray (s3, s5: see
+// shade_shadow_made), the radiance, wavelengths and RNG/pass words and,
+// traced, the event word.  The light sample's geometry and the BRDF those
+// two came from are not stored, so they are neither read here.
+template <bool TRACE>
+PT_DI void load_for_shadow(const PoolView& v, uint32_t slot, PathState& ps, float4& contrib, uint32_t& flags,
+                           uint32_t& sample, uint32_t& job) {
+    const float4 a = v.s0[slot], b = v.s1[slot];
     ps.org = f3(a.x, a.y, a.z);
     ps.mis = a.w;
     ps.dir = f3(b.x, b.y, b.z);
     ps.brdfPdf = b.w;
-    ps.shDir = f3(c.x, c.y, c.z);
-    ps.cosL = c.w;
-    ps.nrm = f3(d.x, d.y, d.z);
-    ps.lightPdf = d.w;
-    ps.brdf = v.s4[slot];
+    ps.shDir = f3(0.0f, 0.0f, 0.0f);
+    ps.cosL = 0.0f;
+    ps.nrm = f3(0.0f, 0.0f, 0.0f);
+    ps.lightPdf = 0.0f;
+    ps.brdf = f4s(0.0f);
+    contrib = v.s3[slot];
     ps.rr = v.s5[slot];
     ps.radiance = v.s6[slot];
     ps.l = v.s7[slot];
@@ -75,15 +82,20 @@ PT_DI void load_state(const PoolView& v, uint32_t slot, PathState& ps, uint32_t&
     sample = m.z;
     ps.shObj = word_shobj(m.w);
     job = word_job(m.w);
-    const float4 e = v.s9[slot];
-    ps.shLightID = e.x;
-    ps.ev = __float_as_uint(e.y);
+    if (TRACE) {
+        const float4 e = v.s9[slot];
+        ps.shLightID = e.x;
+        ps.ev = __float_as_uint(e.y);
+    } else {
+        ps.shLightID = -1.0f;
+        ps.ev = 0u;
+    }
 }
 
 // A new sample's state.  Its first step is a primary ray (march, then
 // shade_primary), which reads neither the shadow-ray fields (s2, s3), the
-// BRDF (s4) nor the light pick (s9.x) and writes them before any shadow ray
-// reads them; at bounce 0 the throughput, the radiance and the event word
+// BRDF (s4) nor the light pick (s9.x) and writes what a shadow ray reads
+// before it reads it; at bounce 0 the throughput, the radiance and the event word
 // are start_sample's constants (1, 0, 0), which load_for_primary sets
 // instead of reading s5, s6 and s9.  So only s0, s1, s7 and s8 are stored.
 PT_DI void store_new_sample(const PoolView& v, uint32_t slot, const PathState& ps, uint32_t sample, uint32_t job) {
@@ -254,8 +266,7 @@ PT_DI void load_for_primary(const PoolView& v, uint32_t slot, PathState& ps, uin
     job = word_job(m.w);
     // A first hit (bounce 0) has start_sample's throughput 1, radiance 0 and
     // no events yet (store_new_sample stores none of them).  s9 holds the
-    // light pick (set here before a shadow ray reads it) and the event word,
-    // which only a traced dispatch keeps.
+    // light pick and the event word, which only a traced dispatch keeps.
     if (ps.bounce == 0) {
         ps.rr = f4s(1.0f);
         ps.radiance = f4s(0.0f);
@@ -335,11 +346,13 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
         }
         if (valid) {
             PathState ps;
+            float4 contrib;
             uint32_t flags, sample;
-            load_state(v, slot, ps, flags, sample, job);
+            load_for_shadow<TRACE>(v, slot, ps, contrib, flags, sample, job);
             const WfJob& J = A.jobs[job];
             const int objectID = __float_as_int(v.h0[slot].w);
-            const StepResult r = shade_shadow<TRACE>(ps, *J.scene, objectID, J.pc.pathLength);
+            const float4 rr_next = ps.rr;
+            const StepResult r = shade_shadow_made<TRACE>(ps, objectID, contrib, rr_next, J.pc.pathLength);
             finish_shade<TRACE>(A, J, ps, r, sample, freed);
             if (!freed) {
                 store_after_shadow(v, slot, ps, sample, job, TRACE);
@@ -378,25 +391,27 @@ __global__ void PT_SHADE_BOUNDS wf_shade(const __grid_constant__ WfArgs A) {
             const StepResult r = shade_primary<TRACE>(ps, *J.scene, h, objectID, J.pc.pathLength);
             finish_shade<TRACE>(A, J, ps, r, sample, freed);
             if (!freed) {
-                // the path state; the shadow-ray fields (s2, s3) and the BRDF (s4)
-                // only for a light sample's shadow ray (a next bounce's
-                // primary ray neither reads them nor reaches a reader of them)
+                // the path state.  For a light sample's shadow ray: its
+                // direction (s2, read by the march) and, made now with the
+                // shadow step's own operations (shade_shadow_made), the NEE
+                // term (s3) and the bounce's next throughput (s5), so the
+                // shadow step reads neither the light sample's geometry nor
+                // the BRDF (s4 is kept only when traced, beside s9).  A next
+                // bounce's primary ray reads none of s2-s4.
                 v.s0[slot] = make_float4(ps.org.x, ps.org.y, ps.org.z, ps.mis);
                 v.s1[slot] = make_float4(ps.dir.x, ps.dir.y, ps.dir.z, ps.brdfPdf);
                 if (r == STEP_SHADOW) {
                     v.s2[slot] = make_float4(ps.shDir.x, ps.shDir.y, ps.shDir.z, ps.cosL);
-                    v.s3[slot] = make_float4(ps.nrm.x, ps.nrm.y, ps.nrm.z, ps.lightPdf);
-                    v.s4[slot] = ps.brdf;
+                    v.s3[slot] = shadow_contribution(ps, *J.scene);
+                    if (TRACE) v.s4[slot] = ps.brdf;
                 }
-                v.s5[slot] = ps.rr;
+                v.s5[slot] = (r == STEP_SHADOW) ? bounce_throughput(ps) : ps.rr;
                 v.s6[slot] = ps.radiance;
                 v.s7[slot] = ps.l;  // unchanged: written with s8 so their sector is written whole
                 v.s8[slot] = make_uint4(ps.seed, ((r == STEP_SHADOW) ? kShadowFlag : 0u) | bounce_word(ps), sample,
                                         job_word(job, ps.shObj));
-                // the light picked (read by the shadow-ray result) and the
-                // traced event word
-                if (TRACE || r == STEP_SHADOW)
-                    v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
+                // traced: the light picked and the event word
+                if (TRACE) v.s9[slot] = make_float4(ps.shLightID, __uint_as_float(ps.ev), 0.0f, 0.0f);
                 again = true;
                 // the light sample's shadow ray, or the next bounce
                 shadow_next = (r == STEP_SHADOW);
