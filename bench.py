@@ -223,18 +223,19 @@ def fp32_peak_tflops(peaks):
 
 # DRAM bytes per launch of each stage kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum) in the steady state of the workload's scene, keyed
-# by workload and path-pool size; the other knobs were the library defaults.
-# Each comes from one small-case ncu capture of two launches per stage with
-# the pool full (profiles/wf_stages_mandelbulb12_1024x1024_16spp_pool2e22.md):
+# by workload and path-pool size; the other knobs were the library defaults
+# (one engine).  Each comes from one small-case ncu capture of two launches
+# per stage with the pool full
+# (profiles/wf_stages_mandelbulb12_1024x1024_16spp_pool2e22.md):
 # per launch a stage moves the state of the rays in its queues, which a full
 # pool of the same size bounds the same way at the full image size (the last
 # iterations of a dispatch, with the pool draining, move less).  At 2^22
 # slots gen had nothing to start in the captured launches: no figure.
 # Other settings report null.
 STAGE_TRAFFIC_BYTES = {
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): {"march": 298.29e6, "shade": 408.59e6, "gen": 36.42e6},
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 21): {"march": 810.17e6, "shade": 1052.52e6, "gen": 78.50e6},
-    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 22): {"march": 1183.62e6, "shade": 1670.13e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 20): {"march": 297.99e6, "shade": 351.92e6, "gen": 36.48e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 21): {"march": 809.99e6, "shade": 949.24e6, "gen": 78.17e6},
+    ("mandelbulb12_plane_1024x1024_64spp_depth6", 1 << 22): {"march": 1183.41e6, "shade": 1504.67e6},
 }
 # The library's default wavefront knobs.
 DEFAULT_TUNING = {"pool_slots": 1 << 22, "march_budget": 64, "refill_min": 2, "drain_lanes": 24, "blocks_per_sm": 4,
