@@ -150,9 +150,10 @@ uint64_t pt_sdf_source_fingerprint(const char* source);
  * PT_ERR_UNSUPPORTED with a reason in err for what the shim does not cover. */
 int pt_glsl_translate(const char* glsl, const char* prefix, char* out, size_t cap, size_t* needed, char* err,
                       size_t err_cap);
-/* Compiles (without loading) the run-time megakernel for n snippets for
- * compute capability sm (e.g. 103): a check that needs no GPU.  The log
- * receives the compiler's messages. */
+/* Compiles (without loading) the run-time kernels a context builds for n
+ * snippets (megakernel, march kernel, FP64 renderer) for compute capability
+ * sm (e.g. 103): a check that needs no GPU.  The log receives the
+ * compiler's messages. */
 int pt_jit_check(const char* const* sources, int n, int sm, char* log, size_t log_cap);
 
 /* Replaces the UBO upload (src/pathtracer.cpp:3805-3807). */

@@ -503,12 +503,29 @@ template <typename V> PT_DI SOf<V> sdf(V p) { return p.y - (height(p.x) + height
 // pt_user_sdf / pt_user_material (FP32 kernels) or pt_user_sdf_d /
 // pt_user_material_d (the FP64 renderer) before including these headers;
 // the precompiled kernels never see that kind.
+//
+// PT_SDF_KINDS (bit k: kind k) lists the kinds a kernel evaluates: a run-time
+// compiled kernel is given those of the scenes it renders, so the code of
+// the other built-in SDFs is not in it; precompiled kernels take every kind.
+#ifndef PT_SDF_KINDS
+#define PT_SDF_KINDS 0xFFFFFFFFu
+#endif
+static_assert(PT_SDF_BLOB == 1 && PT_SDF_MANDELBULB == 2 && PT_SDF_MENGER == 3 && PT_SDF_TERRAIN == 4,
+              "the bit positions tested in plugin_sdf and plugin_material");
 template <typename V, typename R = SOf<V>> PT_DI R plugin_sdf(int kind, int slot, V p) {
     switch (kind) {
+#if (PT_SDF_KINDS >> 2) & 1u
         case PT_SDF_MANDELBULB: return sdf_mandelbulb::sdf(p);
+#endif
+#if (PT_SDF_KINDS >> 3) & 1u
         case PT_SDF_MENGER: return sdf_menger::sdf(p);
+#endif
+#if (PT_SDF_KINDS >> 1) & 1u
         case PT_SDF_BLOB: return sdf_blob::sdf(p);
+#endif
+#if (PT_SDF_KINDS >> 4) & 1u
         case PT_SDF_TERRAIN: return sdf_terrain::sdf(p);
+#endif
 #if defined(PT_JIT_USER_SDF)
         case PT_SDF_CUSTOM:
             if constexpr (sizeof(R) == 4) {
@@ -523,8 +540,12 @@ template <typename V, typename R = SOf<V>> PT_DI R plugin_sdf(int kind, int slot
 template <typename V, typename R = SOf<V>> PT_DI R plugin_material(const pt_sdf_plugin& pl, int slot, V p) {
     if (pl.material_mode == PT_SDFMAT_CONSTANT) return R(pl.material[0]);
     switch (pl.kind) {
+#if (PT_SDF_KINDS >> 1) & 1u
         case PT_SDF_BLOB: return sdf_blob::sdfmaterial(p, pl.material);
+#endif
+#if (PT_SDF_KINDS >> 2) & 1u
         case PT_SDF_MANDELBULB: return sdf_mandelbulb::sdfmaterial(p, pl.material);
+#endif
 #if defined(PT_JIT_USER_SDF)
         case PT_SDF_CUSTOM:
             if constexpr (sizeof(R) == 4) {
@@ -544,6 +565,12 @@ template <typename R> PT_DI V3<R> sdf_pos(const KScene& S, int i) {
 // in scene order, sdf = min(sdf, SDFi(p - pos_i)) for every bit i of set1.
 template <typename V, typename R = SOf<V>> PT_DI R scene_sdf(const KScene& S, V p, uint32_t set1) {
     R sdf = R(PT_MAXDIST);
+#if defined(PT_ONE_SDF)
+    // A run-time compiled kernel for scenes whose one SDF is scene GLSL in
+    // slot 0: the loop below with its one trip written out (same operations).
+    if (set1 & 1u) sdf = m_fmin(sdf, plugin_sdf(PT_SDF_CUSTOM, S.meta.custom_base, p - sdf_pos<R>(S, 0)));
+    return sdf;
+#endif
     uint32_t bits = set1 & ((S.meta.nplug >= 32) ? 0xFFFFFFFFu : ((1u << S.meta.nplug) - 1u));
     while (bits) {
         const int i = __ffs(bits) - 1;
@@ -559,6 +586,14 @@ template <typename V, typename R = SOf<V>> PT_DI R scene_sdf(const KScene& S, V 
 template <typename V, typename R = SOf<V>> PT_DI R scene_sdf_sel(const KScene& S, V p, uint32_t set1, int& sel) {
     R sdf = R(PT_MAXDIST);
     sel = -1;
+#if defined(PT_ONE_SDF)
+    if (set1 & 1u) {  // as in scene_sdf
+        const R di = plugin_sdf(PT_SDF_CUSTOM, S.meta.custom_base, p - sdf_pos<R>(S, 0));
+        if (!(sdf < di)) sel = 0;
+        sdf = m_fmin(sdf, di);
+    }
+    return sdf;
+#endif
     uint32_t bits = set1 & ((S.meta.nplug >= 32) ? 0xFFFFFFFFu : ((1u << S.meta.nplug) - 1u));
     while (bits) {
         const int i = __ffs(bits) - 1;

@@ -132,6 +132,8 @@ struct pt_batch {
     int custom_next = 0;
     JitModule jit;
     bool jit_dirty = false;
+    uint32_t sdf_kinds = 0;  // plug-in kinds of every scene added (bit k: kind k)
+    uint32_t jit_kinds = 0;  // the kinds `jit` was compiled for (PT_SDF_KINDS)
     JitModule jit64;  // the FP64 renderer's megakernel for the same snippets (pt_batch_render_fp64), when needed
     // A scene with a mandelbulb was added: the staged engine's built-in march
     // kernel then probes normals across the warp.
@@ -475,11 +477,13 @@ int add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int 
     if (n[5] > PT_MAX_LIVE_SDFS || nplugins > PT_MAX_LIVE_SDFS)
         return bfail(b, PT_ERR_UNSUPPORTED, "pt_batch_add_scene: at most 32 SDFs can be evaluated (32-bit set mask)");
     bool custom = false, bulb = false;
+    uint32_t kinds = 0;
     for (int i = 0; i < nplugins; i++) {
         if (plugins[i].kind < PT_SDF_NONE || plugins[i].kind > PT_SDF_CUSTOM)
             return bfail(b, PT_ERR_INVALID, "pt_batch_add_scene: unknown plug-in kind");
         custom = custom || plugins[i].kind == PT_SDF_CUSTOM;
         bulb = bulb || plugins[i].kind == PT_SDF_MANDELBULB;
+        kinds |= 1u << plugins[i].kind;
     }
     PT_B_TRY(b, cudaSetDevice(b->device));
     KScene* S = new (std::nothrow) KScene;
@@ -528,6 +532,10 @@ int add_scene(pt_batch* b, const pt_ubo* ubo, const pt_sdf_plugin* plugins, int 
     bs.custom = custom;
     bs.variant = pt_feature_variant(n);
     b->bulb = b->bulb || bulb;
+    // the compiled march kernel holds the code of the kinds seen so far: a
+    // scene with another kind needs it compiled again
+    b->sdf_kinds |= kinds;
+    if (b->jit.lib && (kinds & ~b->jit_kinds)) b->jit_dirty = true;
     *scene_id = (int)b->scenes.size();
     b->scenes.push_back(bs);
     return PT_OK;
@@ -697,8 +705,10 @@ namespace {
 // brought new ones since the last compile, and hands it to the staged engine.
 int prepare_jit(pt_batch* b) {
     if (!b->jit_dirty) return PT_OK;
-    const std::string program =
-        (b->device_checks ? "#define PT_DEBUG_CHECKS 1\n" : "") + pt_jit_program(b->custom, kJitMarch);
+    const uint32_t kinds = b->sdf_kinds;
+    const std::string program = std::string(b->device_checks ? "#define PT_DEBUG_CHECKS 1\n" : "") +
+                                "#define PT_SDF_KINDS " + std::to_string(kinds) + "u\n" +
+                                pt_jit_program(b->custom, kJitMarch);
     std::vector<char> cubin;
     std::string lowered[kJitMaxKernels], log;
     JitModule m;
@@ -718,6 +728,7 @@ int prepare_jit(pt_batch* b) {
     set_staged_march_kernel(b, reinterpret_cast<const void*>(m.kernel[0]));
     pt_jit_unload(b->jit);
     b->jit = m;
+    b->jit_kinds = kinds;
     b->jit_dirty = false;
     return PT_OK;
 }

@@ -601,8 +601,9 @@ def glsl_translate(glsl: str, prefix: str = "u0_") -> str:
 
 
 def jit_check(sources: list[str], sm: int = 103) -> str:
-    """Compiles the run-time megakernel for these snippets without a GPU;
-    returns the compiler log, raises with it on failure."""
+    """Compiles the run-time kernels a context builds for these snippets
+    (pt_jit_check) without a GPU; returns the compiler log, raises with it
+    on failure."""
     arr = (ctypes.c_char_p * max(1, len(sources)))(*[s.encode() for s in sources])
     log = ctypes.create_string_buffer(1 << 16)
     rc = native.cuda().pt_jit_check(arr, len(sources), sm, log, len(log))
