@@ -505,8 +505,8 @@ template <typename V> PT_DI SOf<V> sdf(V p) { return p.y - (height(p.x) + height
 // the precompiled kernels never see that kind.
 //
 // PT_SDF_KINDS (bit k: kind k) lists the kinds a kernel evaluates: a run-time
-// compiled kernel is given those of the scenes it renders, so the code of
-// the other built-in SDFs is not in it; precompiled kernels take every kind.
+// compiled march kernel is given those of the scenes it renders, so the code
+// of the other built-in SDFs is not in it; other kernels take every kind.
 #ifndef PT_SDF_KINDS
 #define PT_SDF_KINDS 0xFFFFFFFFu
 #endif

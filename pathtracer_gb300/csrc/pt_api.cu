@@ -795,15 +795,17 @@ static int ensure_jit(pt_ctx* ctx, JitKind kind) {
     // the cache key carries the contraction choice with the program text;
     // a checked march kernel is the same source with PT_DEBUG_CHECKS
     // the megakernel and march kernel of a scene whose one SDF is scene
-    // GLSL evaluate it without the loop over the SDF set (PT_ONE_SDF)
+    // GLSL evaluate it without the loop over the SDF set (PT_ONE_SDF;
+    // measured faster in both)
     const bool one_sdf = (kind == kJitMegakernel || kind == kJitMarch) && ctx->nplug == 1 &&
                          ctx->custom.size() == 1 && ctx->custom[0].slot == 0;
     const std::string checks = kind == kJitMarch && ctx->device_checks ? "#define PT_DEBUG_CHECKS 1\n" : "";
-    // and hold the code of the scene's plug-in kinds only
+    // the march kernel holds the code of the scene's plug-in kinds only (the
+    // megakernel keeps every kind: without the others it measured slower)
     uint32_t kinds = 0;
     for (int i = 0; i < ctx->nplug; i++) kinds |= 1u << ctx->plug[i].kind;
     const std::string kind_mask =
-        kind == kJitFp64 ? std::string() : "#define PT_SDF_KINDS " + std::to_string(kinds) + "u\n";
+        kind != kJitMarch ? std::string() : "#define PT_SDF_KINDS " + std::to_string(kinds) + "u\n";
     const std::string program = checks + (one_sdf ? "#define PT_ONE_SDF 1\n" : "") + kind_mask +
                                 pt_jit_program(ctx->custom, kind) + (ctx->fp_contract ? "// fmad\n" : "");
     for (size_t i = 0; i < cache.size(); i++)

@@ -159,12 +159,14 @@ extern "C" int pt_jit_check(const char* const* sources, int n, int sm, char* log
     for (int k = 0; k < kJitKinds && rc == PT_OK; k++) {
         std::vector<char> cubin;
         std::string lowered[kJitMaxKernels];
-        // what a context compiles for a scene of these snippets: its
-        // megakernel and march kernel hold no built-in plug-in and, for one
-        // snippet, evaluate it without the loop over the SDF set
+        // what a context compiles for a scene of these snippets: its march
+        // kernel holds no built-in plug-in, and for one snippet the
+        // megakernel and march kernel evaluate it without the loop over the
+        // SDF set
         const bool fp32 = k == kJitMegakernel || k == kJitMarch;
-        const std::string head = std::string(fp32 && n == 1 ? "#define PT_ONE_SDF 1\n" : "") +
-                                 (fp32 ? "#define PT_SDF_KINDS " + std::to_string(1u << PT_SDF_CUSTOM) + "u\n" : "");
+        const std::string head =
+            std::string(fp32 && n == 1 ? "#define PT_ONE_SDF 1\n" : "") +
+            (k == kJitMarch ? "#define PT_SDF_KINDS " + std::to_string(1u << PT_SDF_CUSTOM) + "u\n" : "");
         rc = pt_jit_compile_for(sm, head + pt_jit_program(slots, (JitKind)k), (JitKind)k, cubin, lowered, msg);
         all += msg;
     }
